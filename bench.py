@@ -1,0 +1,386 @@
+"""Benchmark: batched persistent raycast of the 1024^3 uint16 bricked volume.
+
+Workload (one step): a 64-view orbit at 1920x1080 of a 1024^3 uint16 volume
+with 12-bit values (64 seeded blobs on a low-frequency background + Gaussian
+noise), bricked as 256^3 bricks with 2 ghost voxels (125 bricks at LOD 0,
+4 LOD levels), 4096-entry 1D TF, 1.5 samples per voxel, finest level, one
+persistent launch over all 64 views.  Inputs are seeded synthetic data; no
+dataset ships with the reference for this size.
+
+Printed line (one JSON object, rank 0):
+  value     frames/s of the batched persistent kernel, device time (CUDA
+            events on the launching stream), volume resident in HBM.  The
+            brick pool (2.3 GB) is larger than L2, so no flush is needed.
+  e2e       frames/s through the public API with host buffers: paint_batch
+            (view descriptors host->device) + read back of all 64 RGBA8
+            framebuffers into host memory, wall clock.
+  roofline  dominant kernel (the persistent raycast): algorithmic bytes per
+            launch = stored bytes of the distinct non-skipped bricks each view
+            samples, summed over views, / kernel time, against the measured
+            HBM copy bandwidth.
+  cpu_baseline  the FP64 CPU oracle (a port: the reference's raycaster is
+            GLSL in an absent submodule) on a bounded pixel sample of view 0.
+
+--impl reference times that CPU implementation alone (all host threads) on
+the same workload and metric.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s & Gsamples/s, batched vs per-view, <=2/255 vs FP64 oracle; p99 ms"
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(wl, vol, view, proj, seconds, threads, rng_seed):
+    """Oracle render of seeded pixel batches of one view until `seconds` of
+    CPU work; returns (pixels/s, samples/s, pixels, the oracle rgba, pixel ids)."""
+    import numpy as np
+    from oracle import orc
+    rng = np.random.default_rng(rng_seed)
+    npix_total = wl.width * wl.height
+    done, ns, t0 = 0, 0, time.perf_counter()
+    pix_all, ref_all = [], []
+    batch = 2048
+    while True:
+        pix = rng.integers(0, npix_total, batch)
+        ref, n = orc.render(vol, view, proj, wl.width, wl.height, wl.tf, spv=wl.spv,
+                            value_range=wl.value_range, pixels=pix, threads=threads)
+        done += batch
+        ns += n
+        pix_all.append(pix)
+        ref_all.append(ref)
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+        batch = min(batch * 2, 65536)
+    return done / el, ns / el, done, np.concatenate(ref_all), np.concatenate(pix_all), el
+
+
+def run_reference(args):
+    """The reference's CPU implementation of the path (the FP64 oracle port:
+    Tuvok's raycaster is unbuildable here), all host threads, per step a
+    bounded pixel sample of view 0 of the same workload."""
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    import numpy as np
+    from imagevis3d_gb300 import synth_volume, workloads
+    from oracle import orc
+    wl = workloads.config2(nviews=64)
+    vol = synth_volume(wl.synth) if not args.cpu_volume else orc.synth_blobs(wl.synth)
+    threads = orc.max_threads()
+    view, proj = wl.views[0]
+    for _ in range(args.warmup):
+        cpu_sample(wl, vol, view, proj, 0.5, threads, 1)
+    rates, srates, total_t = [], [], 0.0
+    for s in range(args.steps):
+        pr, sr, n, _, _, el = cpu_sample(wl, vol, view, proj, args.ref_seconds, threads, 100 + s)
+        rates.append(pr / (wl.width * wl.height))
+        srates.append(sr)
+        total_t += el
+    fps = statistics.mean(rates)
+    out = {
+        "metric": METRIC, "value": fps, "unit": "frames/s", "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
+        "config": {"workload": wl.name, "views": 64, "width": wl.width, "height": wl.height,
+                   "samples_per_voxel": wl.spv},
+        "gsamples_per_s": statistics.mean(srates) / 1e9,
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": "seeded pixel subsets of view 0, %.0f s of CPU work per step, "
+                                   "frames/s = pixels/s / (1920*1080)" % args.ref_seconds},
+        "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the persistent kernel from the committed ncu
+    summary, scaled to this workload (see the summary for the capture)."""
+    p = os.path.join(ROOT, "profiles", "raycast_persistent_1024cube_u16.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch_full:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--views", type=int, default=64)
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--cpu-volume", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-texture", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from imagevis3d_gb300 import GBVR_SAMPLER_SW, GBVR_SAMPLER_TEX, Renderer, synth_volume, workloads
+    from imagevis3d_gb300.replicas import shard
+
+    wl = workloads.config2(size=args.size, nviews=args.views)
+    # replicas: each rank renders its own share of the orbit (no exchange)
+    mine = shard(len(wl.views), rank, world)
+    views = [wl.views[i] for i in mine]
+    r = Renderer()
+    r.loadSynthetic(wl.synth, **wl.brick, build_texture=not args.no_texture)
+    r.resize((wl.width, wl.height))
+    r.set1DTrans(wl.tf)
+    r.setValueRange(*wl.value_range)
+    r.setSampleRateModifier(wl.spv)
+    info = r.datasetInfo()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def maxover(x):
+        if dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident batched throughput (value) ----
+    for _ in range(args.warmup):
+        r.paintBatch(views)
+    vis = [v for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    clocks = ClockSampler(vis[local] if local < len(vis) else local)
+    barrier()
+    clocks.start()
+    kernel_ms, step_ms, samples, brick_bytes = [], [], 0, 0
+    for _ in range(args.steps):
+        r.paintBatch(views)
+        st = r.stats()
+        kernel_ms.append(st["kernel_ms"])
+        step_ms.append(st["gpu_ms"])
+        samples += st["samples"]
+        brick_bytes += st["brick_bytes"]
+    barrier()
+    clk = clocks.stop()
+    dev_s = maxover(sum(step_ms) / 1000.0)
+    frames_total = len(wl.views) * args.steps  # all ranks
+    value = frames_total / dev_s
+    ksec = sum(kernel_ms) / 1000.0
+    achieved = (brick_bytes / args.steps) / (ksec / args.steps) / 1e9
+    st_last = r.stats()
+
+    # ---- per-view plain kernel (64 launches) ----
+    plain_ms = []
+    for _ in range(2):
+        r.paintViews(views)
+    for _ in range(args.steps):
+        r.paintViews(views)
+        plain_ms.append(r.stats()["gpu_ms"])
+    plain_fps = len(views) * args.steps / (sum(plain_ms) / 1000.0)
+
+    # ---- texture-hardware trilinear, same batch ----
+    tex_fps = None
+    if not args.no_texture:
+        r.setSampler(GBVR_SAMPLER_TEX)
+        for _ in range(2):
+            r.paintBatch(views)
+        tms = []
+        for _ in range(args.steps):
+            r.paintBatch(views)
+            tms.append(r.stats()["gpu_ms"])
+        tex_fps = len(views) * args.steps / (sum(tms) / 1000.0)
+        r.setSampler(GBVR_SAMPLER_SW)
+
+    # ---- end to end through the public API with host buffers ----
+    fb = [None] * len(views)
+    r.paintBatch(views)
+    for i in range(len(views)):
+        r.readFramebuffer(i)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.paintBatch(views)
+        for i in range(len(views)):
+            fb[i] = r.readFramebuffer(i)
+    barrier()
+    e2e_s = maxover(time.perf_counter() - t0)
+    e2e = frames_total / e2e_s
+    h2d = r.stats()["h2d_bytes"]
+    d2h = len(views) * wl.width * wl.height * 4
+
+    # per-view drop-in end to end: paint + readback one view at a time
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        for v, p in views:
+            r.setView(v, p)
+            r.paint()
+            r.readFramebuffer(0)
+    e2e_plain = len(views) * max(1, args.steps // 2) / (time.perf_counter() - t0)
+
+    out = None
+    if rank == 0:
+        pk = peaks()
+        peak = pk["hbm_gbs"] if pk else 6800.0
+        cpu = None
+        err = None
+        if not args.no_cpu:
+            from oracle import orc
+            vol = synth_volume(wl.synth)
+            threads = orc.max_threads()
+            v0, p0 = wl.views[0]
+            pr, sr, n, ref, pix, el = cpu_sample(wl, vol, v0, p0, args.cpu_seconds, threads, 7)
+            cpu = {"value": pr / (wl.width * wl.height), "unit": "frames/s", "cores": threads,
+                   "kind": "port", "gsamples_per_s": sr / 1e9,
+                   "sample": "%d seeded pixels of view 0 (%.1f s, FP64 oracle, %d threads); "
+                             "frames/s = pixels/s / (%d*%d)" % (n, el, threads, wl.width, wl.height)}
+            # image error of the GPU frame on the same pixels
+            r2 = Renderer(float_fb=True)
+            r2.loadSynthetic(wl.synth, **wl.brick)
+            r2.resize((wl.width, wl.height))
+            r2.set1DTrans(wl.tf)
+            r2.setValueRange(*wl.value_range)
+            r2.setSampleRateModifier(wl.spv)
+            r2.setView(v0, p0)
+            r2.paint()
+            img = r2.readFramebuffer(0, as_float=True).reshape(-1, 4)[pix]
+            r2.cleanup()
+            d = np.abs(img - ref)
+            err = {"max": float(d.max()), "rms": float(np.sqrt((d * d).mean())),
+                   "pixels": int(pix.size), "tol_max": 2 / 255, "tol_rms": 0.5 / 255}
+        gs = samples / (sum(kernel_ms) / 1000.0) / 1e9
+        out = {
+            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded Philox blob volume)",
+            "config": {"workload": wl.name, "volume": "%d^3 uint16 (12-bit)" % args.size,
+                       "bricks": "256^3 incl. 2 ghosts, %d bricks at LOD 0, %d LODs" %
+                                 (int(np.prod(info["lod_bricks"][0])), info["lod_count"]),
+                       "views": len(wl.views), "width": wl.width, "height": wl.height,
+                       "samples_per_voxel": wl.spv, "lod": 0, "tf_entries": 4096,
+                       "sampler": "fp32 software trilinear",
+                       "l2": "inputs larger than L2 (brick pool %.2f GB)" % (info["device_bytes"] / 1e9),
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "gsamples_per_s": gs,
+            "per_view_plain_fps": plain_fps,
+            "batched_vs_per_view": value / plain_fps,
+            "texture_trilinear_fps": tex_fps,
+            "e2e_per_view_fps": e2e_plain,
+            "image_error_vs_fp64": err,
+            "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic_from_profile(),
+                         "kernel": "k_render_persistent<uint16,1D,SW>",
+                         "bytes_per_launch": brick_bytes / args.steps,
+                         "kernel_ms": 1000.0 * ksec / args.steps,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if pk else "fallback"},
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps,
+            "clocks": clk,
+            "stats_last_step": {k: st_last[k] for k in ("samples", "bricks_touched", "bricks_skipped",
+                                                         "brick_bytes")},
+        }
+        print(json.dumps(out))
+    r.cleanup()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,1366 @@
+// Host runtime behind the C ABI of include/gbvr.h: dataset build and
+// residency (brick pool + page table), render state, paint (plain per view or
+// one persistent batch replayed as a CUDA graph), readback and statistics.
+//
+// The renderer object mirrors the state Tuvok's AbstrRenderer keeps behind
+// the Lua calls of LuaScripts/BatchRenderer.lua:22-41 and the setters of
+// ImageVis3D/UI/RenderWindow.h:77-314.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/gbvr.h"
+#include "gbvr_internal.h"
+#include "uvf.h"
+
+namespace gbvr {
+bool write_image(const std::string& path, const unsigned char* rgba, int w, int h, bool alpha);
+}
+
+using namespace gbvr;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& m) {
+  g_err = m;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? GBVR_ENOMEM : GBVR_ECUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(x)                                  \
+  do {                                               \
+    cudaError_t e_ = (x);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #x); \
+  } while (0)
+
+#define TRY(x)                 \
+  do {                         \
+    int rc_ = (x);             \
+    if (rc_ != GBVR_OK) return rc_; \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t bytes) {
+    if (bytes <= n && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e == cudaSuccess) n = bytes;
+    else p = nullptr;
+    return e;
+  }
+  template <typename T>
+  T* as() const { return (T*)p; }
+};
+
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  ~PinnedBuf() { if (p) cudaFreeHost(p); }
+  cudaError_t alloc(size_t bytes) {
+    if (bytes <= n && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMallocHost(&p, bytes ? bytes : 16);
+    if (e == cudaSuccess) n = bytes;
+    return e;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// 4x4 helpers (row-major, column vectors), double precision on the host.
+// ---------------------------------------------------------------------------
+void mat_mul(const double* a, const double* b, double* o) {
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      double s = 0;
+      for (int k = 0; k < 4; ++k) s += a[4 * r + k] * b[4 * k + c];
+      o[4 * r + c] = s;
+    }
+}
+
+bool mat_inv(const double* m, double* inv) {
+  double a[4][8];
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 8; ++c) a[r][c] = c < 4 ? m[4 * r + c] : (c - 4 == r ? 1.0 : 0.0);
+  for (int c = 0; c < 4; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < 4; ++r)
+      if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+    if (std::fabs(a[piv][c]) < 1e-300) return false;
+    if (piv != c)
+      for (int k = 0; k < 8; ++k) std::swap(a[c][k], a[piv][k]);
+    double d = a[c][c];
+    for (int k = 0; k < 8; ++k) a[c][k] /= d;
+    for (int r = 0; r < 4; ++r) {
+      if (r == c) continue;
+      double f = a[r][c];
+      if (f == 0) continue;
+      for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+    }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) inv[4 * r + c] = a[r][c + 4];
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 on the host (same stream as the device generator).
+// ---------------------------------------------------------------------------
+void philox_host(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+    uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+    c[0] = n0; c[1] = (uint32_t)p1; c[2] = n2; c[3] = (uint32_t)p0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// Per-axis blob / background tables of a synthetic volume (host math, double,
+// rounded to float): the device kernel then combines them in a fixed float32
+// order.
+struct BlobTablesHost {
+  std::vector<float> amp, ex, ey, ez, bgx, bgy, bgz;
+};
+
+void make_blob_tables(const gbvr_synth_params& p, BlobTablesHost& t) {
+  const uint32_t k0 = p.seed, k1 = 0x70617261u;
+  const int nb = p.nblobs;
+  const long long dims[3] = {p.dims[0], p.dims[1], p.dims[2]};
+  t.amp.resize(nb);
+  std::vector<float>* tabs[3] = {&t.ex, &t.ey, &t.ez};
+  for (int a = 0; a < 3; ++a) tabs[a]->resize((size_t)nb * dims[a]);
+  for (int k = 0; k < nb; ++k) {
+    uint32_t c0[4] = {(uint32_t)k, 0u, 0x626c6f62u, 0u}, c1[4] = {(uint32_t)k, 1u, 0x626c6f62u, 0u};
+    philox_host(c0, k0, k1);
+    philox_host(c1, k0, k1);
+    double cen[3];
+    for (int a = 0; a < 3; ++a) cen[a] = (double)(c0[a] >> 8) / 16777216.0 * (double)dims[a];
+    double sig = p.sigma_lo + (double)(c1[0] >> 8) / 16777216.0 * ((double)p.sigma_hi - p.sigma_lo);
+    double am = p.amp_lo + (double)(c1[1] >> 8) / 16777216.0 * ((double)p.amp_hi - p.amp_lo);
+    t.amp[k] = (float)am;
+    for (int a = 0; a < 3; ++a)
+      for (long long i = 0; i < dims[a]; ++i) {
+        double dd = (double)i - cen[a];
+        (*tabs[a])[(size_t)k * dims[a] + i] = (float)std::exp(-(dd * dd) / (2.0 * sig * sig));
+      }
+  }
+  if (p.bg_freq > 0) {
+    uint32_t c[4] = {0xffffffffu, 2u, 0x626c6f62u, 0u};
+    philox_host(c, k0, k1);
+    std::vector<float>* bt[3] = {&t.bgx, &t.bgy, &t.bgz};
+    for (int a = 0; a < 3; ++a) {
+      double ph = (double)(c[a] >> 8) / 16777216.0;
+      bt[a]->resize(dims[a]);
+      for (long long i = 0; i < dims[a]; ++i)
+        (*bt[a])[i] = (float)std::cos(2.0 * M_PI * ((double)p.bg_freq * ((double)i + 0.5) / (double)dims[a] + ph));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dataset: the brick pool and its page table (one LOD pyramid).
+// ---------------------------------------------------------------------------
+struct Level {
+  long long dims[3];
+  int nb[3];
+  int interior;
+  int brick_base;
+  int nbricks;
+};
+
+struct Dataset {
+  bool loaded = false;
+  int dtype = DT_U8;
+  long long dims[3] = {0, 0, 0};
+  double aspect[3] = {1, 1, 1};
+  int brick = 256, ghost = 2;
+  std::vector<Level> levels;
+  std::vector<BrickInfo> bricks;
+  DevBuf pool, d_bricks;
+  uint64_t stored_bytes = 0;
+  double gmin = 0, gmax = 0;
+  int bit_width = 8;
+  std::vector<uint64_t> hist1d;
+  long long merge = 1;
+  std::vector<uint64_t> hist2d;
+  float max_grad = 0.f;
+  std::vector<cudaArray_t> arrays;
+  std::vector<cudaTextureObject_t> texs;
+  std::string raster_id = "GB300 volume raster";
+
+  void release() {
+    for (auto t : texs) cudaDestroyTextureObject(t);
+    for (auto a : arrays) cudaFreeArray(a);
+    texs.clear();
+    arrays.clear();
+    pool.release();
+    d_bricks.release();
+    levels.clear();
+    bricks.clear();
+    hist1d.clear();
+    hist2d.clear();
+    loaded = false;
+  }
+  ~Dataset() { release(); }
+};
+
+// LOD and brick-grid rules: see the oracle (same statements) and the design doc.
+int lod_dims(const long long dims[3], int brick, int ghost, int max_lods, std::vector<std::array<long long, 3>>& out) {
+  long long I = brick - 2 * ghost;
+  long long n[3] = {dims[0], dims[1], dims[2]};
+  out.clear();
+  for (;;) {
+    out.push_back({n[0], n[1], n[2]});
+    long long mx = std::max(n[0], std::max(n[1], n[2]));
+    if (mx <= I || out.size() == 16) break;
+    if (max_lods > 0 && (int)out.size() >= max_lods) break;
+    for (int a = 0; a < 3; ++a) n[a] = (n[a] + 1) / 2;
+  }
+  return (int)out.size();
+}
+
+size_t elem_align(int dtype) { return 256 / dtype_size(dtype); }
+
+void plan_level(const long long dims[3], int brick, int ghost, int level, Level& L, std::vector<BrickInfo>& bricks,
+                unsigned long long& cursor, int dtype) {
+  long long I = brick - 2 * ghost;
+  long long mx = std::max(dims[0], std::max(dims[1], dims[2]));
+  bool single = mx <= I;
+  for (int a = 0; a < 3; ++a) {
+    L.dims[a] = dims[a];
+    L.nb[a] = single ? 1 : (int)((dims[a] + I - 1) / I);
+  }
+  L.interior = single ? (int)std::max<long long>(mx, 1) : (int)I;
+  L.brick_base = (int)bricks.size();
+  L.nbricks = L.nb[0] * L.nb[1] * L.nb[2];
+  for (int bz = 0; bz < L.nb[2]; ++bz)
+    for (int by = 0; by < L.nb[1]; ++by)
+      for (int bx = 0; bx < L.nb[0]; ++bx) {
+        BrickInfo b;
+        memset(&b, 0, sizeof(b));
+        int bc[3] = {bx, by, bz};
+        int o[3], s[3], lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+          if (single) {
+            o[a] = 0;
+            s[a] = (int)dims[a];
+            lo[a] = -1;
+            hi[a] = (int)dims[a];
+          } else {
+            long long ilo = (long long)bc[a] * I, ihi = std::min<long long>(ilo + I, dims[a]);
+            long long slo = std::max<long long>(ilo - ghost, 0), shi = std::min<long long>(ihi + ghost, dims[a]);
+            o[a] = (int)slo;
+            s[a] = (int)(shi - slo);
+            lo[a] = bc[a] == 0 ? -1 : (int)ilo;
+            hi[a] = (int)ihi;
+          }
+        }
+        b.ox = o[0]; b.oy = o[1]; b.oz = o[2];
+        b.sx = s[0]; b.sy = s[1]; b.sz = s[2];
+        b.lox = lo[0]; b.loy = lo[1]; b.loz = lo[2];
+        b.hix = hi[0]; b.hiy = hi[1]; b.hiz = hi[2];
+        b.level = level;
+        b.offset = cursor;
+        unsigned long long n = (unsigned long long)s[0] * s[1] * s[2];
+        const unsigned long long al = elem_align(dtype);
+        cursor += (n + al - 1) / al * al;
+        bricks.push_back(b);
+      }
+}
+
+int build_textures(Dataset& ds, cudaStream_t s) {
+  cudaChannelFormatDesc cd;
+  if (ds.dtype == DT_U8) cd = cudaCreateChannelDesc<unsigned char>();
+  else if (ds.dtype == DT_U16) cd = cudaCreateChannelDesc<unsigned short>();
+  else cd = cudaCreateChannelDesc<float>();
+  const size_t es = dtype_size(ds.dtype);
+  for (BrickInfo& b : ds.bricks) {
+    cudaArray_t arr;
+    CUDA_TRY(cudaMalloc3DArray(&arr, &cd, make_cudaExtent(b.sx, b.sy, b.sz)));
+    ds.arrays.push_back(arr);
+    cudaMemcpy3DParms cp = {};
+    cp.srcPtr = make_cudaPitchedPtr((char*)ds.pool.p + b.offset * es, (size_t)b.sx * es, b.sx, b.sy);
+    cp.dstArray = arr;
+    cp.extent = make_cudaExtent(b.sx, b.sy, b.sz);
+    cp.kind = cudaMemcpyDeviceToDevice;
+    CUDA_TRY(cudaMemcpy3DAsync(&cp, s));
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = arr;
+    cudaTextureDesc td = {};
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = ds.dtype == DT_F32 ? cudaReadModeElementType : cudaReadModeNormalizedFloat;
+    td.normalizedCoords = 0;
+    cudaTextureObject_t t;
+    CUDA_TRY(cudaCreateTextureObject(&t, &rd, &td, nullptr));
+    ds.texs.push_back(t);
+    b.tex = (unsigned long long)t;
+  }
+  CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyHostToDevice, s));
+  return GBVR_OK;
+}
+
+// GPU UVF build: LOD pyramid, bricks with ghosts, per-brick min/max, 1D and
+// 2D histograms.  d_level0 (device, flat, x fastest) is consumed.
+int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims[3], const gbvr_brick_params* bp,
+                  cudaStream_t s) {
+  ds.release();
+  ds.dtype = dtype;
+  for (int a = 0; a < 3; ++a) ds.dims[a] = dims[a];
+  ds.brick = bp && bp->brick_size > 0 ? bp->brick_size : 256;
+  ds.ghost = bp && bp->overlap >= 0 ? bp->overlap : 2;
+  if (bp && bp->brick_size == 0 && bp->overlap == 0) ds.ghost = 2;
+  if (ds.ghost < 2) return fail(GBVR_EINVAL, "overlap must be >= 2 (gradients need two ghost voxels)");
+  if (ds.brick - 2 * ds.ghost < 8) return fail(GBVR_EINVAL, "brick_size too small for the overlap");
+  if (ds.brick > 2048) return fail(GBVR_EOVERSIZED, "brick_size exceeds the 2048 voxel limit");
+  for (int a = 0; a < 3; ++a) ds.aspect[a] = (bp && bp->aspect[a] > 0) ? bp->aspect[a] : 1.0;
+  std::vector<std::array<long long, 3>> ld;
+  lod_dims(dims, ds.brick, ds.ghost, bp ? bp->max_lods : 0, ld);
+  const size_t es = dtype_size(dtype);
+  // level volumes
+  std::vector<std::unique_ptr<DevBuf>> lv;
+  lv.emplace_back(new DevBuf());
+  std::swap(lv[0]->p, d_level0.p);
+  std::swap(lv[0]->n, d_level0.n);
+  for (size_t l = 1; l < ld.size(); ++l) {
+    lv.emplace_back(new DevBuf());
+    CUDA_TRY(lv[l]->alloc((size_t)ld[l][0] * ld[l][1] * ld[l][2] * es));
+    long long pd[3] = {ld[l - 1][0], ld[l - 1][1], ld[l - 1][2]};
+    CUDA_TRY(launch_downsample(lv[l - 1]->p, dtype, pd, lv[l]->p, s));
+  }
+  // page table
+  unsigned long long cursor = 0;
+  for (size_t l = 0; l < ld.size(); ++l) {
+    Level L;
+    long long d[3] = {ld[l][0], ld[l][1], ld[l][2]};
+    plan_level(d, ds.brick, ds.ghost, (int)l, L, ds.bricks, cursor, dtype);
+    ds.levels.push_back(L);
+  }
+  ds.stored_bytes = 0;
+  for (auto& b : ds.bricks) ds.stored_bytes += (uint64_t)b.sx * b.sy * b.sz * es;
+  CUDA_TRY(ds.pool.alloc(cursor * es));
+  CUDA_TRY(ds.d_bricks.alloc(sizeof(BrickInfo) * ds.bricks.size()));
+  CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyHostToDevice, s));
+  for (size_t l = 0; l < ld.size(); ++l) {
+    const Level& L = ds.levels[l];
+    long long d[3] = {ld[l][0], ld[l][1], ld[l][2]};
+    CUDA_TRY(launch_gather_bricks(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks, ds.pool.p, s));
+  }
+  CUDA_TRY(launch_brick_minmax(ds.pool.p, dtype, ds.d_bricks.as<BrickInfo>(), (int)ds.bricks.size(), s));
+  CUDA_TRY(cudaMemcpyAsync(ds.bricks.data(), ds.d_bricks.p, sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  ds.gmin = INFINITY;
+  ds.gmax = -INFINITY;
+  for (int i = 0; i < ds.levels[0].nbricks; ++i) {
+    ds.gmin = std::min(ds.gmin, (double)ds.bricks[i].vmin);
+    ds.gmax = std::max(ds.gmax, (double)ds.bricks[i].vmax);
+  }
+  // histograms of LOD 0 (integer data)
+  const long long n0 = dims[0] * dims[1] * dims[2];
+  if (dtype != DT_F32) {
+    int nbins = (int)ds.gmax + 1;
+    DevBuf dh;
+    CUDA_TRY(dh.alloc(sizeof(uint64_t) * nbins));
+    CUDA_TRY(cudaMemsetAsync(dh.p, 0, sizeof(uint64_t) * nbins, s));
+    CUDA_TRY(launch_hist1d(lv[0]->p, dtype, n0, dh.as<unsigned long long>(), nbins, s));
+    std::vector<uint64_t> full(nbins);
+    CUDA_TRY(cudaMemcpyAsync(full.data(), dh.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    long long size = nbins;
+    while (size > 1 && full[size - 1] == 0) --size;
+    ds.merge = (size + 4095) / 4096;
+    if (ds.merge < 1) ds.merge = 1;
+    long long outsize = (size + ds.merge - 1) / ds.merge;
+    ds.hist1d.assign(outsize, 0);
+    for (long long i = 0; i < size; ++i) ds.hist1d[i / ds.merge] += full[i];
+    // 2D
+    DevBuf d2, dsc;
+    const size_t n2 = (size_t)outsize * 256;
+    CUDA_TRY(d2.alloc(sizeof(uint64_t) * n2));
+    CUDA_TRY(dsc.alloc(sizeof(Hist2DScratch)));
+    CUDA_TRY(cudaMemsetAsync(d2.p, 0, sizeof(uint64_t) * n2, s));
+    CUDA_TRY(launch_hist2d(lv[0]->p, dtype, dims, ds.gmax, outsize, ds.merge, d2.as<unsigned long long>(),
+                           dsc.as<Hist2DScratch>(), s));
+    ds.hist2d.resize(n2);
+    Hist2DScratch hs;
+    CUDA_TRY(cudaMemcpyAsync(ds.hist2d.data(), d2.p, sizeof(uint64_t) * n2, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(&hs, dsc.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    double g;
+    memcpy(&g, &hs.gmax_bits, 8);
+    ds.max_grad = (float)g;
+    ds.bit_width = dtype == DT_U8 ? 8 : 16;
+  } else {
+    ds.bit_width = 32;
+  }
+  if (bp && bp->build_texture) TRY(build_textures(ds, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  ds.loaded = true;
+  return GBVR_OK;
+}
+
+}  // namespace
+
+namespace gbvr {
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace gbvr
+
+// ---------------------------------------------------------------------------
+// Renderer
+// ---------------------------------------------------------------------------
+struct gbvr_renderer {
+  Dataset ds;
+  uint32_t flags = 0;
+  int width = 640, height = 480;  // BatchRenderer.lua:31-33 default context size
+  int mode = GBVR_RM_1DTRANS, interp = GBVR_LINEAR, sampler = GBVR_SAMPLER_SW;
+  std::vector<float> tf1d;
+  std::vector<float> tf2d;
+  int tf2d_w = 0, tf2d_h = 0;
+  float tf2d_grad_max = 0.f;
+  bool range_set = false;
+  double vlo = 0, vhi = 1;
+  float iso = 0.f;
+  bool iso_set = false;
+  float iso_rgb[3] = {1, 1, 1};
+  int lighting = 1;
+  // MainWindow::UpdateColorWidget defaults (ImageVis3D.cpp:898-901): colour
+  // times the alpha intensity
+  float amb[3] = {0.1f, 0.1f, 0.1f}, diff[3] = {1, 1, 1}, spec[3] = {1, 1, 1};
+  float light_dir[3] = {0, 0, -1};
+  float shininess = 8.f;
+  float spv = 1.f;
+  int lod_min = 0, lod_max = 1 << 20;
+  bool view_set = false;
+  float view[16], proj[16];
+  float bg_top[3] = {0, 0, 0}, bg_bot[3] = {0, 0, 0};
+  float ert = 0.99f;
+  // device state
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+  DevBuf d_tf, d_skip, d_fb8, d_fb32, d_frames, d_prefix, d_counter, d_samples, d_touched;
+  PinnedBuf h_frames, h_prefix;
+  bool tf_dirty = true, skip_dirty = true;
+  int skip_level = -1;
+  int fb_views = 0, fb_w = 0, fb_h = 0;
+  int last_views = 0, last_level = 0;
+  float last_ms = 0.f, last_kernel_ms = 0.f;
+  uint64_t last_h2d = 0;
+  int grid = 0;
+  // graph cache for the batch launch
+  struct GraphKey {
+    int n, w, h, level, dtype, mode, sampler;
+    void* fb8;
+    void* fb32;
+    bool operator<(const GraphKey& o) const {
+      return std::tie(n, w, h, level, dtype, mode, sampler, fb8, fb32) <
+             std::tie(o.n, o.w, o.h, o.level, o.dtype, o.mode, o.sampler, o.fb8, o.fb32);
+    }
+  };
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+
+  void drop_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+  }
+  ~gbvr_renderer() {
+    drop_graphs();
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (evk0) cudaEventDestroy(evk0);
+    if (evk1) cudaEventDestroy(evk1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+int check_r(gbvr_renderer* r) {
+  if (!r) return fail(GBVR_EINVAL, "null renderer");
+  return GBVR_OK;
+}
+int check_loaded(gbvr_renderer* r) {
+  TRY(check_r(r));
+  if (!r->ds.loaded) return fail(GBVR_ESTATE, "no dataset loaded");
+  return GBVR_OK;
+}
+
+int render_level(gbvr_renderer* r) {
+  int n = (int)r->ds.levels.size();
+  int l = std::min(std::max(r->lod_min, 0), n - 1);
+  return l;
+}
+
+void default_range(gbvr_renderer* r, double& lo, double& hi) {
+  if (r->range_set) { lo = r->vlo; hi = r->vhi; return; }
+  const Dataset& ds = r->ds;
+  if (ds.dtype == DT_F32) {
+    lo = ds.gmin;
+    hi = ds.gmax > ds.gmin ? ds.gmax : ds.gmin + 1;
+  } else {
+    lo = 0;
+    hi = (double)((long long)ds.hist1d.size() * ds.merge - 1);
+    if (hi <= 0) hi = 1;
+  }
+}
+
+// Default TF: a linear ramp, as a freshly opened dataset gets in the reference.
+void ensure_tf(gbvr_renderer* r) {
+  if (r->tf1d.empty()) {
+    int n = r->ds.hist1d.empty() ? 256 : (int)std::min<size_t>(r->ds.hist1d.size(), 4096);
+    r->tf1d.resize(4 * n);
+    for (int i = 0; i < n; ++i) {
+      float v = n > 1 ? (float)i / (n - 1) : 1.f;
+      r->tf1d[4 * i] = r->tf1d[4 * i + 1] = r->tf1d[4 * i + 2] = v;
+      r->tf1d[4 * i + 3] = v;
+    }
+    r->tf_dirty = true;
+  }
+}
+
+int upload_tf(gbvr_renderer* r, int level) {
+  ensure_tf(r);
+  const bool two = r->mode == GBVR_RM_2DTRANS;
+  if (two && r->tf2d.empty()) return fail(GBVR_ESTATE, "2D transfer function not set");
+  const std::vector<float>& tf = two ? r->tf2d : r->tf1d;
+  if (r->tf_dirty) {
+    CUDA_TRY(r->d_tf.alloc(sizeof(float) * tf.size()));
+    CUDA_TRY(cudaMemcpyAsync(r->d_tf.p, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice, r->stream));
+    r->tf_dirty = false;
+    r->skip_dirty = true;
+  }
+  if (r->skip_dirty || r->skip_level != level) {
+    const Level& L = r->ds.levels[level];
+    CUDA_TRY(r->d_skip.alloc(r->ds.bricks.size()));
+    double lo, hi;
+    default_range(r, lo, hi);
+    int w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4), h = two ? r->tf2d_h : 1;
+    float idx_scale = (float)((w - 1) / (hi - lo));
+    CUDA_TRY(launch_classify(r->ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks, r->d_tf.as<float4>(), w, h,
+                             r->mode, (float)lo, idx_scale, r->iso, r->d_skip.as<unsigned char>() + L.brick_base,
+                             r->stream));
+    r->skip_dirty = false;
+    r->skip_level = level;
+  }
+  return GBVR_OK;
+}
+
+void default_camera(gbvr_renderer* r, float view[16], float proj[16]);
+
+FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int level, int vidx) {
+  FrameDesc f;
+  memset(&f, 0, sizeof(f));
+  const Dataset& ds = r->ds;
+  const Level& L = ds.levels[level];
+  f.pool = ds.pool.p;
+  f.bricks = ds.d_bricks.as<BrickInfo>() + L.brick_base;
+  f.skip = r->d_skip.as<unsigned char>() + L.brick_base;
+  f.dtype = ds.dtype;
+  f.sampler = r->sampler;
+  double ext[3], mx = 0;
+  for (int a = 0; a < 3; ++a) {
+    ext[a] = (double)ds.dims[a] * ds.aspect[a];
+    mx = std::max(mx, ext[a]);
+  }
+  long long maxd = 0;
+  for (int a = 0; a < 3; ++a) {
+    ext[a] /= mx;
+    f.dims[a] = (int)L.dims[a];
+    f.nb[a] = L.nb[a];
+    f.vox_scale[a] = (float)((double)L.dims[a] / ext[a]);
+    f.half_extent[a] = (float)(0.5 * ext[a]);
+    maxd = std::max(maxd, L.dims[a]);
+  }
+  f.interior = L.interior;
+  const bool two = r->mode == GBVR_RM_2DTRANS;
+  f.tf = r->d_tf.as<float4>();
+  f.tf_w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4);
+  f.tf_h = two ? r->tf2d_h : 1;
+  f.mode = r->mode;
+  f.interp = r->interp;
+  double lo, hi;
+  default_range(r, lo, hi);
+  f.value_lo = (float)lo;
+  f.idx_scale = (float)((f.tf_w - 1) / (hi - lo));
+  float gm = r->tf2d_grad_max > 0 ? r->tf2d_grad_max : ds.max_grad;
+  if (!(gm > 0)) gm = 1.f;
+  f.grad_scale = (float)((f.tf_h - 1) / ((double)gm * (hi - lo)));
+  f.dt = (float)(1.0 / ((double)r->spv * (double)maxd));
+  f.opacity_exp = (float)(1.0 / (double)r->spv);
+  f.ert = r->ert;
+  f.iso = r->iso;
+  for (int k = 0; k < 3; ++k) {
+    f.iso_rgb[k] = r->iso_rgb[k];
+    f.amb[k] = r->amb[k];
+    f.diff[k] = r->diff[k];
+    f.spec[k] = r->spec[k];
+    f.bg[k] = r->bg_bot[k];
+  }
+  f.lighting = r->lighting;
+  f.shininess = r->shininess;
+  double V[16], P[16], M[16], Mi[16], Vi[16];
+  for (int i = 0; i < 16; ++i) { V[i] = view[i]; P[i] = proj[i]; }
+  mat_mul(P, V, M);
+  mat_inv(M, Mi);
+  mat_inv(V, Vi);
+  for (int i = 0; i < 16; ++i) f.inv_vp[i] = (float)Mi[i];
+  double ld[3];
+  for (int rr = 0; rr < 3; ++rr)
+    ld[rr] = Vi[4 * rr] * r->light_dir[0] + Vi[4 * rr + 1] * r->light_dir[1] + Vi[4 * rr + 2] * r->light_dir[2];
+  double ll = std::sqrt(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
+  for (int k = 0; k < 3; ++k) f.light_to[k] = ll > 0 ? (float)(-ld[k] / ll) : 0.f;
+  f.width = r->width;
+  f.height = r->height;
+  f.tiles_x = (r->width + TILE_W - 1) / TILE_W;
+  f.tiles_y = (r->height + TILE_H - 1) / TILE_H;
+  const size_t npix = (size_t)r->width * r->height;
+  f.out_rgba8 = r->d_fb8.as<uchar4>() + (size_t)vidx * npix;
+  f.out_f32 = r->d_fb32.p ? r->d_fb32.as<float4>() + (size_t)vidx * npix : nullptr;
+  f.samples = r->d_samples.as<unsigned long long>() + vidx;
+  f.touched = r->d_touched.as<unsigned char>() + (size_t)vidx * L.nbricks;
+  return f;
+}
+
+// Cached graphs bake in device and pinned pointers: drop them whenever a
+// buffer they reference moves.
+struct PtrSnapshot {
+  void* p[10];
+  explicit PtrSnapshot(const gbvr_renderer* r)
+      : p{r->d_fb8.p, r->d_fb32.p, r->d_frames.p, r->d_prefix.p, r->d_counter.p,
+          r->d_samples.p, r->d_touched.p, r->h_frames.p, r->h_prefix.p, r->d_skip.p} {}
+  bool operator!=(const PtrSnapshot& o) const { return memcmp(p, o.p, sizeof(p)) != 0; }
+};
+
+int prepare(gbvr_renderer* r, int nviews, int& level) {
+  TRY(check_loaded(r));
+  if (nviews <= 0) return fail(GBVR_EINVAL, "view count must be positive");
+  level = render_level(r);
+  const size_t npix = (size_t)r->width * r->height;
+  if (r->fb_views < nviews || r->fb_w != r->width || r->fb_h != r->height) {
+    CUDA_TRY(r->d_fb8.alloc(npix * 4 * nviews));
+    if (r->flags & 1u) CUDA_TRY(r->d_fb32.alloc(npix * 16 * nviews));
+    r->fb_views = nviews;
+    r->fb_w = r->width;
+    r->fb_h = r->height;
+    r->drop_graphs();
+  }
+  CUDA_TRY(r->d_samples.alloc(sizeof(unsigned long long) * nviews));
+  CUDA_TRY(r->d_touched.alloc((size_t)nviews * r->ds.levels[level].nbricks));
+  TRY(upload_tf(r, level));
+  return GBVR_OK;
+}
+
+int finish(gbvr_renderer* r, int nviews, int level) {
+  CUDA_TRY(cudaEventSynchronize(r->ev1));
+  CUDA_TRY(cudaEventElapsedTime(&r->last_ms, r->ev0, r->ev1));
+  CUDA_TRY(cudaEventElapsedTime(&r->last_kernel_ms, r->evk0, r->evk1));
+  r->last_views = nviews;
+  r->last_level = level;
+  return GBVR_OK;
+}
+
+int paint_plain(gbvr_renderer* r, const gbvr_view* views, int n) {
+  int level;
+  TRY(prepare(r, n, level));
+  CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream));
+  CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
+  CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
+  CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
+  for (int v = 0; v < n; ++v) {
+    float dv[16], dp[16];
+    const float *vw = views ? views[v].view : nullptr, *pj = views ? views[v].proj : nullptr;
+    if (!views) {
+      if (r->view_set) { vw = r->view; pj = r->proj; }
+      else { default_camera(r, dv, dp); vw = dv; pj = dp; }
+    }
+    FrameDesc f = make_frame(r, vw, pj, level, v);
+    CUDA_TRY(launch_render_plain(f, r->stream));
+  }
+  CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
+  CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
+  r->last_h2d = 0;  // descriptors travel as kernel parameters
+  return finish(r, n, level);
+}
+
+int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
+  int level;
+  const PtrSnapshot before(r);
+  TRY(prepare(r, n, level));
+  CUDA_TRY(r->h_frames.alloc(sizeof(FrameDesc) * n));
+  CUDA_TRY(r->h_prefix.alloc(sizeof(int) * (n + 1)));
+  CUDA_TRY(r->d_frames.alloc(sizeof(FrameDesc) * n));
+  CUDA_TRY(r->d_prefix.alloc(sizeof(int) * (n + 1)));
+  CUDA_TRY(r->d_counter.alloc(sizeof(int)));
+  // the previous replay may still read the pinned staging buffers
+  CUDA_TRY(cudaStreamSynchronize(r->stream));
+  FrameDesc* hf = (FrameDesc*)r->h_frames.p;
+  int* hp = (int*)r->h_prefix.p;
+  int total = 0;
+  for (int v = 0; v < n; ++v) {
+    hf[v] = make_frame(r, views[v].view, views[v].proj, level, v);
+    hp[v] = total;
+    total += hf[v].tiles_x * hf[v].tiles_y;
+  }
+  hp[n] = total;
+  if (PtrSnapshot(r) != before) r->drop_graphs();
+  if (!r->grid) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    r->grid = persistent_grid_size(dev);
+  }
+  gbvr_renderer::GraphKey key{n, r->width, r->height, level, r->ds.dtype, r->mode, r->sampler, r->d_fb8.p, r->d_fb32.p};
+  auto it = r->graphs.find(key);
+  if (it == r->graphs.end()) {
+    cudaGraph_t g;
+    CUDA_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
+    cudaMemcpyAsync(r->d_frames.p, r->h_frames.p, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, r->stream);
+    cudaMemcpyAsync(r->d_prefix.p, r->h_prefix.p, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, r->stream);
+    cudaMemsetAsync(r->d_counter.p, 0, sizeof(int), r->stream);
+    cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream);
+    cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream);
+    cudaEventRecord(r->evk0, r->stream);
+    cudaError_t le = launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), n,
+                                                    r->d_prefix.as<int>(), total, r->d_counter.as<int>(), r->grid,
+                                                    r->stream);
+    cudaEventRecord(r->evk1, r->stream);
+    cudaError_t ce = cudaStreamEndCapture(r->stream, &g);
+    if (le != cudaSuccess) return cuda_fail(le, "persistent launch capture");
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+    cudaGraphExec_t ge;
+    cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
+    it = r->graphs.emplace(key, ge).first;
+  }
+  CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
+  CUDA_TRY(cudaGraphLaunch(it->second, r->stream));
+  CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
+  r->last_h2d = sizeof(FrameDesc) * n + sizeof(int) * (n + 1);
+  return finish(r, n, level);
+}
+
+void look_at(const double eye[3], const double c[3], const double up[3], double* m) {
+  double f[3] = {c[0] - eye[0], c[1] - eye[1], c[2] - eye[2]};
+  double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+  for (double& x : f) x /= fl;
+  double s[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
+  double sl = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+  for (double& x : s) x /= sl;
+  double u[3] = {s[1] * f[2] - s[2] * f[1], s[2] * f[0] - s[0] * f[2], s[0] * f[1] - s[1] * f[0]};
+  double rows[3][3] = {{s[0], s[1], s[2]}, {u[0], u[1], u[2]}, {-f[0], -f[1], -f[2]}};
+  for (int r = 0; r < 3; ++r) {
+    for (int k = 0; k < 3; ++k) m[4 * r + k] = rows[r][k];
+    m[4 * r + 3] = -(rows[r][0] * eye[0] + rows[r][1] * eye[1] + rows[r][2] * eye[2]);
+  }
+  m[12] = m[13] = m[14] = 0;
+  m[15] = 1;
+}
+
+void perspective(double fovy_deg, double aspect, double zn, double zf, double* m) {
+  double t = 1.0 / std::tan(fovy_deg * M_PI / 360.0);
+  for (int i = 0; i < 16; ++i) m[i] = 0;
+  m[0] = t / aspect;
+  m[5] = t;
+  m[10] = (zf + zn) / (zn - zf);
+  m[11] = 2 * zf * zn / (zn - zf);
+  m[14] = -1;
+}
+
+void orbit(double az_deg, double el_deg, double radius, double fov, int w, int h, float* view, float* proj) {
+  double az = az_deg * M_PI / 180.0, el = el_deg * M_PI / 180.0;
+  double eye[3] = {radius * std::cos(el) * std::sin(az), radius * std::sin(el), radius * std::cos(el) * std::cos(az)};
+  double c[3] = {0, 0, 0}, up[3] = {0, 1, 0};
+  double V[16], P[16];
+  look_at(eye, c, up, V);
+  perspective(fov, (double)w / h, std::max(0.01, radius - 2.0), radius + 2.0, P);
+  for (int i = 0; i < 16; ++i) { view[i] = (float)V[i]; proj[i] = (float)P[i]; }
+}
+
+void default_camera(gbvr_renderer* r, float view[16], float proj[16]) {
+  // 45 degree field of view, orbit radius 2.5 x the (unit-normalised) box diagonal
+  orbit(0.0, 0.0, 2.5 * std::sqrt(3.0), 45.0, r->width, r->height, view, proj);
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int gbvr_last_error(char* buf, size_t size) {
+  if (!buf || size == 0) return GBVR_EINVAL;
+  size_t n = std::min(size - 1, g_err.size());
+  memcpy(buf, g_err.data(), n);
+  buf[n] = 0;
+  return GBVR_OK;
+}
+
+int gbvr_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes) {
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (sm_count) CUDA_TRY(cudaDeviceGetAttribute(sm_count, cudaDevAttrMultiProcessorCount, dev));
+  size_t f = 0, t = 0;
+  CUDA_TRY(cudaMemGetInfo(&f, &t));
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return GBVR_OK;
+}
+
+int gbvr_create(int renderer_type, uint32_t flags, gbvr_renderer** out) {
+  if (!out) return fail(GBVR_EINVAL, "null output handle");
+  *out = nullptr;
+  if (renderer_type != GBVR_CUDA_RAYCASTER)
+    return fail(GBVR_EINVAL, "this library implements only GBVR_CUDA_RAYCASTER (type 9)");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(GBVR_ECUDA, "no CUDA device available");
+  std::unique_ptr<gbvr_renderer> r(new gbvr_renderer());
+  r->flags = flags;
+  CUDA_TRY(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreate(&r->ev0));
+  CUDA_TRY(cudaEventCreate(&r->ev1));
+  CUDA_TRY(cudaEventCreate(&r->evk0));
+  CUDA_TRY(cudaEventCreate(&r->evk1));
+  *out = r.release();
+  return GBVR_OK;
+}
+
+int gbvr_destroy(gbvr_renderer* r) {
+  if (!r) return GBVR_OK;
+  if (r->stream) cudaStreamSynchronize(r->stream);
+  delete r;
+  return GBVR_OK;
+}
+
+int gbvr_load_volume(gbvr_renderer* r, const void* host, const int64_t dims[3], int dtype, const gbvr_brick_params* bp) {
+  TRY(check_r(r));
+  if (!host || !dims || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return fail(GBVR_EINVAL, "bad volume");
+  if (dtype < 0 || dtype > 2) return fail(GBVR_EINVAL, "bad dtype");
+  long long d[3] = {dims[0], dims[1], dims[2]};
+  const size_t bytes = (size_t)d[0] * d[1] * d[2] * dtype_size(dtype);
+  DevBuf lv;
+  CUDA_TRY(lv.alloc(bytes));
+  CUDA_TRY(cudaMemcpyAsync(lv.p, host, bytes, cudaMemcpyHostToDevice, r->stream));
+  r->drop_graphs();
+  r->skip_dirty = true;
+  r->tf_dirty = true;
+  TRY(build_dataset(r->ds, lv, dtype, d, bp, r->stream));
+  return GBVR_OK;
+}
+
+int gbvr_load_synthetic(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr_brick_params* bp) {
+  TRY(check_r(r));
+  if (!p || p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 || p->nblobs < 0)
+    return fail(GBVR_EINVAL, "bad synthetic parameters");
+  BlobTablesHost t;
+  make_blob_tables(*p, t);
+  DevBuf amp, ex, ey, ez, bx, by, bz, lv;
+  auto up = [&](DevBuf& d, const std::vector<float>& v) -> cudaError_t {
+    cudaError_t e = d.alloc(sizeof(float) * std::max<size_t>(v.size(), 1));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(d.p, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice, r->stream);
+  };
+  CUDA_TRY(up(amp, t.amp));
+  CUDA_TRY(up(ex, t.ex));
+  CUDA_TRY(up(ey, t.ey));
+  CUDA_TRY(up(ez, t.ez));
+  CUDA_TRY(up(bx, t.bgx));
+  CUDA_TRY(up(by, t.bgy));
+  CUDA_TRY(up(bz, t.bgz));
+  long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
+  CUDA_TRY(lv.alloc((size_t)d[0] * d[1] * d[2] * dtype_size(p->dtype)));
+  BlobTablesDev td;
+  td.nblobs = p->nblobs;
+  td.amp = amp.as<float>();
+  td.ex = ex.as<float>();
+  td.ey = ey.as<float>();
+  td.ez = ez.as<float>();
+  bool bg = p->bg_freq > 0;
+  td.bgx = bg ? bx.as<float>() : nullptr;
+  td.bgy = bg ? by.as<float>() : nullptr;
+  td.bgz = bg ? bz.as<float>() : nullptr;
+  td.bg_level = p->bg_level;
+  td.bg_amp = p->bg_amp;
+  td.scale = p->scale;
+  td.noise_amp = p->noise_amp;
+  td.noise_kind = p->noise_kind;
+  td.vmax = p->vmax;
+  td.seed = p->seed;
+  CUDA_TRY(launch_synth_blobs(td, d, p->dtype, lv.p, r->stream));
+  r->drop_graphs();
+  r->skip_dirty = true;
+  r->tf_dirty = true;
+  TRY(build_dataset(r->ds, lv, p->dtype, d, bp, r->stream));
+  return GBVR_OK;
+}
+
+int gbvr_synth_volume(const gbvr_synth_params* p, void* host_out, size_t bytes) {
+  if (!p || !host_out) return fail(GBVR_EINVAL, "null argument");
+  const size_t need = (size_t)p->dims[0] * p->dims[1] * p->dims[2] * dtype_size(p->dtype);
+  if (bytes < need) return fail(GBVR_EINVAL, "output buffer too small");
+  gbvr_renderer tmp;
+  CUDA_TRY(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking));
+  BlobTablesHost t;
+  make_blob_tables(*p, t);
+  DevBuf amp, ex, ey, ez, bx, by, bz, lv;
+  auto up = [&](DevBuf& d, const std::vector<float>& v) -> cudaError_t {
+    cudaError_t e = d.alloc(sizeof(float) * std::max<size_t>(v.size(), 1));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(d.p, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice, tmp.stream);
+  };
+  CUDA_TRY(up(amp, t.amp));
+  CUDA_TRY(up(ex, t.ex));
+  CUDA_TRY(up(ey, t.ey));
+  CUDA_TRY(up(ez, t.ez));
+  CUDA_TRY(up(bx, t.bgx));
+  CUDA_TRY(up(by, t.bgy));
+  CUDA_TRY(up(bz, t.bgz));
+  CUDA_TRY(lv.alloc(need));
+  BlobTablesDev td{p->nblobs, amp.as<float>(), ex.as<float>(), ey.as<float>(), ez.as<float>(),
+                   p->bg_freq > 0 ? bx.as<float>() : nullptr, p->bg_freq > 0 ? by.as<float>() : nullptr,
+                   p->bg_freq > 0 ? bz.as<float>() : nullptr, p->bg_level, p->bg_amp, p->scale, p->noise_amp,
+                   p->noise_kind, p->vmax, p->seed};
+  long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
+  CUDA_TRY(launch_synth_blobs(td, d, p->dtype, lv.p, tmp.stream));
+  CUDA_TRY(cudaMemcpyAsync(host_out, lv.p, need, cudaMemcpyDeviceToHost, tmp.stream));
+  CUDA_TRY(cudaStreamSynchronize(tmp.stream));
+  return GBVR_OK;
+}
+
+int gbvr_load_uvf(gbvr_renderer* r, const char* path, int verify, const gbvr_brick_params* bp) {
+  TRY(check_r(r));
+  if (!path) return fail(GBVR_EINVAL, "null path");
+  UvfFile uf;
+  std::string msg;
+  int rc = uvf_read(path, verify != 0, uf, msg);
+  if (rc) return fail(rc, msg);
+  const UvfRaster& ra = uf.raster;
+  int dtype;
+  if (ra.is_float) dtype = DT_F32;
+  else if (ra.bit_size == 8 && !ra.is_signed) dtype = DT_U8;
+  else if (ra.bit_size == 16 && !ra.is_signed) dtype = DT_U16;
+  else return fail(GBVR_EFORMAT, "unsupported raster element type");
+  uint64_t lods = 1;
+  for (uint64_t c : ra.lod_counts) lods = std::max(lods, c);
+  if (lods != 1) return fail(GBVR_EFORMAT, "multi-LOD raster blocks are rebuilt from LOD 0: store LOD 0 only");
+  const size_t bytes = (size_t)ra.dims[0] * ra.dims[1] * ra.dims[2] * dtype_size(dtype);
+  std::vector<unsigned char> host(bytes);
+  rc = uvf_read_voxels(path, uf, host.data(), bytes, msg);
+  if (rc) return fail(rc, msg);
+  gbvr_brick_params p = {};
+  if (bp) p = *bp;
+  if (p.brick_size <= 0) p.brick_size = (int)ra.brick_size[0];
+  if (p.overlap <= 0) p.overlap = std::max(2, (int)(ra.overlap[0] / 2));
+  for (int a = 0; a < 3; ++a)
+    if (p.aspect[a] <= 0) p.aspect[a] = ra.transform[5 * a] > 0 ? ra.transform[5 * a] : 1.0;
+  int64_t dims[3] = {(int64_t)ra.dims[0], (int64_t)ra.dims[1], (int64_t)ra.dims[2]};
+  TRY(gbvr_load_volume(r, host.data(), dims, dtype, &p));
+  r->ds.raster_id = ra.id;
+  return GBVR_OK;
+}
+
+int gbvr_get_dataset_info(gbvr_renderer* r, gbvr_dataset_info* info) {
+  TRY(check_loaded(r));
+  if (!info) return fail(GBVR_EINVAL, "null info");
+  memset(info, 0, sizeof(*info));
+  const Dataset& ds = r->ds;
+  for (int a = 0; a < 3; ++a) info->dims[a] = ds.dims[a];
+  info->dtype = ds.dtype;
+  info->bit_width = ds.bit_width;
+  info->range[0] = ds.gmin;
+  info->range[1] = ds.gmax;
+  info->lod_count = (int)ds.levels.size();
+  info->brick_size = ds.brick;
+  info->overlap = ds.ghost;
+  for (size_t l = 0; l < ds.levels.size() && l < 16; ++l)
+    for (int a = 0; a < 3; ++a) {
+      info->lod_dims[l][a] = ds.levels[l].dims[a];
+      info->lod_bricks[l][a] = ds.levels[l].nb[a];
+    }
+  info->total_bricks = (int64_t)ds.bricks.size();
+  info->device_bytes = ds.stored_bytes;
+  info->hist1d_size = (int)ds.hist1d.size();
+  info->hist2d_max_grad = ds.max_grad;
+  return GBVR_OK;
+}
+
+int gbvr_get_hist1d(gbvr_renderer* r, uint64_t* out, size_t n) {
+  TRY(check_loaded(r));
+  if (!out || n < r->ds.hist1d.size()) return fail(GBVR_EINVAL, "histogram buffer too small");
+  memcpy(out, r->ds.hist1d.data(), sizeof(uint64_t) * r->ds.hist1d.size());
+  return GBVR_OK;
+}
+
+int gbvr_get_hist2d(gbvr_renderer* r, uint64_t* out, size_t nx, size_t ny, float* max_grad) {
+  TRY(check_loaded(r));
+  if (!out || nx * ny < r->ds.hist2d.size() || ny != 256) return fail(GBVR_EINVAL, "histogram buffer too small");
+  memcpy(out, r->ds.hist2d.data(), sizeof(uint64_t) * r->ds.hist2d.size());
+  if (max_grad) *max_grad = r->ds.max_grad;
+  return GBVR_OK;
+}
+
+int gbvr_get_brick_minmax(gbvr_renderer* r, int lod, double* out, size_t nbricks) {
+  TRY(check_loaded(r));
+  if (lod < 0 || lod >= (int)r->ds.levels.size()) return fail(GBVR_EINVAL, "bad lod");
+  const Level& L = r->ds.levels[lod];
+  if (!out || nbricks < (size_t)L.nbricks) return fail(GBVR_EINVAL, "buffer too small");
+  for (int i = 0; i < L.nbricks; ++i) {
+    out[2 * i] = r->ds.bricks[L.brick_base + i].vmin;
+    out[2 * i + 1] = r->ds.bricks[L.brick_base + i].vmax;
+  }
+  return GBVR_OK;
+}
+
+int gbvr_get_brick(gbvr_renderer* r, int lod, const int32_t brick[3], void* out, size_t bytes, int64_t origin[3],
+                   int64_t stored_dims[3]) {
+  TRY(check_loaded(r));
+  if (lod < 0 || lod >= (int)r->ds.levels.size() || !brick) return fail(GBVR_EINVAL, "bad lod");
+  const Level& L = r->ds.levels[lod];
+  for (int a = 0; a < 3; ++a)
+    if (brick[a] < 0 || brick[a] >= L.nb[a]) return fail(GBVR_EINVAL, "brick index out of range");
+  const BrickInfo& b = r->ds.bricks[L.brick_base + (brick[2] * L.nb[1] + brick[1]) * L.nb[0] + brick[0]];
+  const size_t es = dtype_size(r->ds.dtype);
+  const size_t need = (size_t)b.sx * b.sy * b.sz * es;
+  if (origin) { origin[0] = b.ox; origin[1] = b.oy; origin[2] = b.oz; }
+  if (stored_dims) { stored_dims[0] = b.sx; stored_dims[1] = b.sy; stored_dims[2] = b.sz; }
+  if (!out) return GBVR_OK;
+  if (bytes < need) return fail(GBVR_EINVAL, "brick buffer too small");
+  CUDA_TRY(cudaMemcpy(out, (const char*)r->ds.pool.p + b.offset * es, need, cudaMemcpyDeviceToHost));
+  return GBVR_OK;
+}
+
+int gbvr_resize(gbvr_renderer* r, int width, int height) {
+  TRY(check_r(r));
+  if (width <= 0 || height <= 0 || width > 16384 || height > 16384) return fail(GBVR_EINVAL, "bad framebuffer size");
+  r->width = width;
+  r->height = height;
+  return GBVR_OK;
+}
+
+int gbvr_set_render_mode(gbvr_renderer* r, int mode) {
+  TRY(check_r(r));
+  if (mode < 0 || mode > 2) return fail(GBVR_EINVAL, "bad render mode");
+  if (mode != r->mode) { r->tf_dirty = true; r->skip_dirty = true; }
+  r->mode = mode;
+  return GBVR_OK;
+}
+
+int gbvr_set_tf1d(gbvr_renderer* r, const float* rgba, int n) {
+  TRY(check_r(r));
+  if (!rgba || n < 2 || n > 65536) return fail(GBVR_EINVAL, "1D transfer function needs 2..65536 entries");
+  r->tf1d.assign(rgba, rgba + 4 * (size_t)n);
+  r->tf_dirty = true;
+  r->skip_dirty = true;
+  return GBVR_OK;
+}
+
+int gbvr_set_tf2d(gbvr_renderer* r, const float* rgba, int w, int h, float max_grad) {
+  TRY(check_r(r));
+  if (!rgba || w < 2 || h < 2 || w > 4096 || h > 4096) return fail(GBVR_EINVAL, "bad 2D transfer function size");
+  r->tf2d.assign(rgba, rgba + 4 * (size_t)w * h);
+  r->tf2d_w = w;
+  r->tf2d_h = h;
+  r->tf2d_grad_max = max_grad;
+  r->tf_dirty = true;
+  r->skip_dirty = true;
+  return GBVR_OK;
+}
+
+int gbvr_set_value_range(gbvr_renderer* r, double lo, double hi) {
+  TRY(check_r(r));
+  if (!(hi > lo)) return fail(GBVR_EINVAL, "value range must have hi > lo");
+  r->range_set = true;
+  r->vlo = lo;
+  r->vhi = hi;
+  r->skip_dirty = true;
+  return GBVR_OK;
+}
+
+int gbvr_set_iso(gbvr_renderer* r, float value, const float rgb[3]) {
+  TRY(check_r(r));
+  r->iso = value;
+  r->iso_set = true;
+  if (rgb) for (int k = 0; k < 3; ++k) r->iso_rgb[k] = rgb[k];
+  r->skip_dirty = true;
+  return GBVR_OK;
+}
+
+int gbvr_set_lighting(gbvr_renderer* r, int enabled, const float amb[4], const float diff[4], const float spec[4],
+                      const float dir[3]) {
+  TRY(check_r(r));
+  r->lighting = enabled != 0;
+  for (int k = 0; k < 3; ++k) {
+    if (amb) r->amb[k] = amb[k] * amb[3];
+    if (diff) r->diff[k] = diff[k] * diff[3];
+    if (spec) r->spec[k] = spec[k] * spec[3];
+    if (dir) r->light_dir[k] = dir[k];
+  }
+  return GBVR_OK;
+}
+
+int gbvr_set_sample_rate(gbvr_renderer* r, float spv) {
+  TRY(check_r(r));
+  if (!(spv >= 0.05f && spv <= 64.f)) return fail(GBVR_EINVAL, "samples per voxel must be in [0.05, 64]");
+  r->spv = spv;
+  return GBVR_OK;
+}
+
+int gbvr_set_interpolant(gbvr_renderer* r, int interp) {
+  TRY(check_r(r));
+  if (interp != GBVR_NEAREST && interp != GBVR_LINEAR) return fail(GBVR_EINVAL, "bad interpolant");
+  r->interp = interp;
+  return GBVR_OK;
+}
+
+int gbvr_set_sampler(gbvr_renderer* r, int sampler) {
+  TRY(check_r(r));
+  if (sampler != GBVR_SAMPLER_SW && sampler != GBVR_SAMPLER_TEX) return fail(GBVR_EINVAL, "bad sampler");
+  if (sampler == GBVR_SAMPLER_TEX && r->ds.loaded && r->ds.texs.empty())
+    return fail(GBVR_ESTATE, "dataset was loaded without build_texture");
+  r->sampler = sampler;
+  return GBVR_OK;
+}
+
+int gbvr_set_lod_limits(gbvr_renderer* r, int min_lod, int max_lod) {
+  TRY(check_r(r));
+  if (min_lod < 0 || max_lod < min_lod) return fail(GBVR_EINVAL, "bad LOD limits");
+  r->lod_min = min_lod;
+  r->lod_max = max_lod;
+  return GBVR_OK;
+}
+
+int gbvr_set_view(gbvr_renderer* r, const float view[16], const float proj[16]) {
+  TRY(check_r(r));
+  if (!view || !proj) return fail(GBVR_EINVAL, "null matrix");
+  memcpy(r->view, view, sizeof(r->view));
+  memcpy(r->proj, proj, sizeof(r->proj));
+  r->view_set = true;
+  return GBVR_OK;
+}
+
+int gbvr_set_background(gbvr_renderer* r, const float top[3], const float bottom[3]) {
+  TRY(check_r(r));
+  for (int k = 0; k < 3; ++k) {
+    if (top) r->bg_top[k] = top[k];
+    if (bottom) r->bg_bot[k] = bottom[k];
+  }
+  return GBVR_OK;
+}
+
+int gbvr_set_early_termination(gbvr_renderer* r, float alpha) {
+  TRY(check_r(r));
+  if (!(alpha > 0.f && alpha <= 1.0f)) return fail(GBVR_EINVAL, "termination alpha must be in (0, 1]");
+  r->ert = alpha;
+  return GBVR_OK;
+}
+
+int gbvr_paint(gbvr_renderer* r) {
+  TRY(check_loaded(r));
+  return paint_plain(r, nullptr, 1);
+}
+
+int gbvr_paint_views(gbvr_renderer* r, const gbvr_view* views, int n) {
+  TRY(check_loaded(r));
+  if (!views) return fail(GBVR_EINVAL, "null views");
+  return paint_plain(r, views, n);
+}
+
+int gbvr_paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
+  TRY(check_loaded(r));
+  if (!views) return fail(GBVR_EINVAL, "null views");
+  return paint_batch(r, views, n);
+}
+
+int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t bytes) {
+  TRY(check_r(r));
+  const size_t need = (size_t)r->fb_w * r->fb_h * 4;
+  if (view < 0 || view >= r->last_views) return fail(GBVR_EINVAL, "view index out of range");
+  if (!rgba8 || bytes < need) return fail(GBVR_EINVAL, "framebuffer buffer too small");
+  CUDA_TRY(cudaMemcpyAsync(rgba8, (const char*)r->d_fb8.p + need * view, need, cudaMemcpyDeviceToHost, r->stream));
+  CUDA_TRY(cudaStreamSynchronize(r->stream));
+  return GBVR_OK;
+}
+
+int gbvr_read_framebuffer_f32(gbvr_renderer* r, int view, float* rgba, size_t bytes) {
+  TRY(check_r(r));
+  if (!r->d_fb32.p) return fail(GBVR_ESTATE, "renderer was created without the float framebuffer flag (1)");
+  const size_t need = (size_t)r->fb_w * r->fb_h * 16;
+  if (view < 0 || view >= r->last_views) return fail(GBVR_EINVAL, "view index out of range");
+  if (!rgba || bytes < need) return fail(GBVR_EINVAL, "framebuffer buffer too small");
+  CUDA_TRY(cudaMemcpyAsync(rgba, (const char*)r->d_fb32.p + need * view, need, cudaMemcpyDeviceToHost, r->stream));
+  CUDA_TRY(cudaStreamSynchronize(r->stream));
+  return GBVR_OK;
+}
+
+int gbvr_capture_single_frame(gbvr_renderer* r, const char* path, int preserve_transparency) {
+  TRY(check_r(r));
+  if (!path) return fail(GBVR_EINVAL, "null path");
+  if (r->last_views < 1) return fail(GBVR_ESTATE, "nothing painted yet");
+  std::vector<uint8_t> px((size_t)r->fb_w * r->fb_h * 4);
+  TRY(gbvr_read_framebuffer(r, 0, px.data(), px.size()));
+  if (!write_image(path, px.data(), r->fb_w, r->fb_h, preserve_transparency != 0))
+    return fail(GBVR_EIO, std::string("cannot write ") + path);
+  return GBVR_OK;
+}
+
+int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out) {
+  TRY(check_r(r));
+  if (!out) return fail(GBVR_EINVAL, "null stats");
+  memset(out, 0, sizeof(*out));
+  out->frames = (uint64_t)r->last_views;
+  out->lod = r->last_level;
+  out->subframes = 1;
+  out->gpu_ms = r->last_ms;
+  out->kernel_ms = r->last_kernel_ms;
+  out->h2d_bytes = r->last_h2d;
+  if (r->last_views < 1 || !r->ds.loaded) return GBVR_OK;
+  const int n = r->last_views;
+  const Level& L = r->ds.levels[r->last_level];
+  std::vector<unsigned long long> s(n);
+  std::vector<unsigned char> t((size_t)n * L.nbricks), skip(L.nbricks);
+  CUDA_TRY(cudaMemcpyAsync(s.data(), r->d_samples.p, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, r->stream));
+  CUDA_TRY(cudaMemcpyAsync(t.data(), r->d_touched.p, t.size(), cudaMemcpyDeviceToHost, r->stream));
+  CUDA_TRY(cudaMemcpyAsync(skip.data(), r->d_skip.as<unsigned char>() + L.brick_base, L.nbricks, cudaMemcpyDeviceToHost, r->stream));
+  CUDA_TRY(cudaStreamSynchronize(r->stream));
+  const size_t es = dtype_size(r->ds.dtype);
+  for (int v = 0; v < n; ++v) {
+    out->samples += s[v];
+    for (int b = 0; b < L.nbricks; ++b)
+      if (t[(size_t)v * L.nbricks + b]) {
+        const BrickInfo& bi = r->ds.bricks[L.brick_base + b];
+        out->bricks_touched++;
+        out->brick_bytes += (uint64_t)bi.sx * bi.sy * bi.sz * es;
+      }
+  }
+  for (int b = 0; b < L.nbricks; ++b) out->bricks_skipped += skip[b];
+  return GBVR_OK;
+}
+
+int gbvr_write_uvf(gbvr_renderer* r, const char* path) {
+  TRY(check_loaded(r));
+  if (!path) return fail(GBVR_EINVAL, "null path");
+  const Dataset& ds = r->ds;
+  // LOD 0 re-assembled from its bricks' interiors
+  const size_t es = dtype_size(ds.dtype);
+  const size_t bytes = (size_t)ds.dims[0] * ds.dims[1] * ds.dims[2] * es;
+  std::vector<unsigned char> vol(bytes);
+  const Level& L = ds.levels[0];
+  std::vector<unsigned char> tmp;
+  for (int i = 0; i < L.nbricks; ++i) {
+    const BrickInfo& b = ds.bricks[L.brick_base + i];
+    tmp.resize((size_t)b.sx * b.sy * b.sz * es);
+    CUDA_TRY(cudaMemcpy(tmp.data(), (const char*)ds.pool.p + b.offset * es, tmp.size(), cudaMemcpyDeviceToHost));
+    int lo[3] = {std::max(b.lox, 0), std::max(b.loy, 0), std::max(b.loz, 0)};
+    int hi[3] = {b.hix, b.hiy, b.hiz};
+    for (int z = lo[2]; z < hi[2]; ++z)
+      for (int y = lo[1]; y < hi[1]; ++y)
+        memcpy(&vol[(((size_t)z * ds.dims[1] + y) * ds.dims[0] + lo[0]) * es],
+               &tmp[(((size_t)(z - b.oz) * b.sy + (y - b.oy)) * b.sx + (lo[0] - b.ox)) * es], (size_t)(hi[0] - lo[0]) * es);
+  }
+  UvfWriteSpec s;
+  s.raster.id = ds.raster_id;
+  for (int a = 0; a < 3; ++a) {
+    s.raster.dims[a] = (uint64_t)ds.dims[a];
+    s.raster.brick_size[a] = (uint64_t)ds.brick;
+    s.raster.overlap[a] = (uint64_t)(2 * ds.ghost);
+  }
+  for (int i = 0; i < 16; ++i) s.raster.transform[i] = (i % 5 == 0) ? 1.0 : 0.0;
+  for (int a = 0; a < 3; ++a) s.raster.transform[5 * a] = ds.aspect[a];
+  s.raster.lod_counts = {1};
+  s.raster.bit_size = ds.dtype == DT_U8 ? 8 : ds.dtype == DT_U16 ? 16 : 32;
+  s.raster.mantissa = ds.dtype == DT_F32 ? 23 : s.raster.bit_size;
+  s.raster.is_signed = ds.dtype == DT_F32;
+  s.voxels = vol.data();
+  s.voxel_bytes = bytes;
+  s.hist1d = ds.hist1d;
+  s.hist2d = ds.hist2d;
+  s.hist2d_nx = ds.hist1d.size();
+  s.hist2d_ny = ds.hist2d.empty() ? 0 : 256;
+  s.hist2d_max_grad = ds.max_grad;
+  // MaxMinDataBlock(1): one entry per stored brick of LOD 0, gradients not
+  // computed (DataSource.h:467-469; c60.uvf stores -DBL_MAX / +DBL_MAX)
+  for (int i = 0; i < L.nbricks; ++i) {
+    const BrickInfo& b = ds.bricks[L.brick_base + i];
+    s.minmax.push_back({(double)b.vmin, (double)b.vmax, -1.7976931348623157e308, 1.7976931348623157e308});
+  }
+  std::string msg;
+  int rc = uvf_write(path, s, msg);
+  if (rc) return fail(rc, msg);
+  return GBVR_OK;
+}
+
+int gbvr_build_uvf(const void* host, const int64_t dims[3], int dtype, const gbvr_brick_params* bp, const char* out_path) {
+  gbvr_renderer* r = nullptr;
+  TRY(gbvr_create(GBVR_CUDA_RAYCASTER, 0, &r));
+  std::unique_ptr<gbvr_renderer> hold(r);
+  TRY(gbvr_load_volume(r, host, dims, dtype, bp));
+  return gbvr_write_uvf(r, out_path);
+}
+
+int gbvr_dev_hist1d(const void* dev_vol, int dtype, int64_t n, uint64_t* dev_hist, int nbins, void* stream) {
+  if (!dev_vol || !dev_hist || n < 0 || nbins <= 0) return fail(GBVR_EINVAL, "bad argument");
+  CUDA_TRY(launch_hist1d(dev_vol, dtype, n, (unsigned long long*)dev_hist, nbins, (cudaStream_t)stream));
+  return GBVR_OK;
+}
+
+int gbvr_dev_hist2d(const void* dev_vol, int dtype, const int64_t dims[3], double max_scalar, int64_t nx,
+                    int64_t merge, uint64_t* dev_hist, float* max_grad, void* stream) {
+  if (!dev_vol || !dev_hist || !dims || nx <= 0 || merge <= 0) return fail(GBVR_EINVAL, "bad argument");
+  DevBuf sc;
+  CUDA_TRY(sc.alloc(sizeof(Hist2DScratch)));
+  long long d[3] = {dims[0], dims[1], dims[2]};
+  CUDA_TRY(launch_hist2d(dev_vol, dtype, d, max_scalar, nx, merge, (unsigned long long*)dev_hist, sc.as<Hist2DScratch>(),
+                         (cudaStream_t)stream));
+  Hist2DScratch hs;
+  CUDA_TRY(cudaMemcpyAsync(&hs, sc.p, sizeof(hs), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  double g;
+  memcpy(&g, &hs.gmax_bits, 8);
+  if (max_grad) *max_grad = (float)g;
+  return GBVR_OK;
+}
+
+int gbvr_dev_downsample(const void* dev_in, int dtype, const int64_t dims[3], void* dev_out, void* stream) {
+  if (!dev_in || !dev_out || !dims) return fail(GBVR_EINVAL, "bad argument");
+  long long d[3] = {dims[0], dims[1], dims[2]};
+  CUDA_TRY(launch_downsample(dev_in, dtype, d, dev_out, (cudaStream_t)stream));
+  return GBVR_OK;
+}
+
+int gbvr_orbit_camera(float azimuth_deg, float elevation_deg, float radius, float fov_deg, int width, int height,
+                      float view[16], float proj[16]) {
+  if (!view || !proj || width <= 0 || height <= 0 || !(radius > 0)) return fail(GBVR_EINVAL, "bad camera");
+  orbit(azimuth_deg, elevation_deg, radius, fov_deg, width, height, view, proj);
+  return GBVR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+// Internal structures shared by the host runtime and the CUDA kernels.
+//
+// Data layout in HBM (one dataset):
+//   pool      one device allocation holding every brick of every LOD level,
+//             each brick a dense x-fastest block of its stored voxels
+//             (interior + up to `ghost` voxels copied from each neighbour),
+//             starting on a 256-byte boundary.
+//   bricks    BrickInfo[total bricks], level-major, then z, y, x brick order.
+//   skip      one byte per brick, recomputed by the classify kernel whenever
+//             the transfer function, render mode or isovalue changes.
+//   frames    FrameDesc[n] for the views rendered by one launch.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbvr {
+
+enum DType { DT_U8 = 0, DT_U16 = 1, DT_F32 = 2 };
+enum Mode { MODE_1D = 0, MODE_2D = 1, MODE_ISO = 2 };
+enum Sampler { SAMPLER_SW = 0, SAMPLER_TEX = 1 };
+
+inline size_t dtype_size(int dt) { return dt == DT_U8 ? 1 : dt == DT_U16 ? 2 : 4; }
+
+// One stored brick.  All coordinates are voxel indices of its LOD level.
+struct __align__(16) BrickInfo {
+  unsigned long long offset;  // element offset of voxel (0,0,0) in the pool
+  unsigned long long tex;     // cudaTextureObject_t when the texture sampler is built
+  int ox, oy, oz;             // level coordinate of stored voxel (0,0,0)
+  int sx, sy, sz;             // stored dims
+  int lox, loy, loz;          // interior [lo, hi): a sample whose floor(pos) lies
+  int hix, hiy, hiz;          //   here is taken from this brick (lo = -1 on the low face)
+  float vmin, vmax;           // over the stored voxels, ghosts included
+  int level;
+  int pad;
+};
+
+struct LevelInfo {
+  int dims[3];
+  int nb[3];
+  int interior;
+  int brick_base;  // index of the level's first brick
+};
+
+// Everything one view needs; read by every warp working on one of its tiles.
+struct __align__(16) FrameDesc {
+  // dataset
+  const void* pool;
+  const BrickInfo* bricks;   // the rendered level's bricks
+  const unsigned char* skip; // skip flags of the rendered level's bricks
+  int dtype;
+  int sampler;
+  int dims[3];               // rendered level
+  int nb[3];
+  int interior;
+  float vox_scale[3];        // world -> voxel-centre coordinates: (p + extent/2) * scale - 0.5
+  float half_extent[3];
+  // classification
+  const float4* tf;          // 1D: [tf_w]; 2D: [tf_h][tf_w]
+  int tf_w, tf_h;
+  int mode;
+  int interp;
+  float value_lo;
+  float idx_scale;           // (tf_w - 1) / (value_hi - value_lo)
+  float grad_scale;          // 2D: (tf_h - 1) / (grad_max * (value_hi - value_lo))
+  float dt;                  // step, world units
+  float opacity_exp;         // dt / dt0 = 1 / samples_per_voxel
+  float ert;
+  float iso;
+  float iso_rgb[3];
+  int lighting;
+  float amb[3], diff[3], spec[3];
+  float shininess;
+  float light_to[3];         // unit vector towards the light, world space
+  float bg[3];
+  // camera
+  float inv_vp[16];          // row-major inverse of proj*view
+  int width, height;
+  int tiles_x, tiles_y;
+  // outputs
+  uchar4* out_rgba8;         // may be null
+  float4* out_f32;           // may be null
+  unsigned long long* samples;  // per-frame sample counter
+  unsigned char* touched;    // per-frame flag per brick of the rendered level
+};
+
+// Ray tile handled by one warp: 8 x 4 pixels.
+constexpr int TILE_W = 8;
+constexpr int TILE_H = 4;
+
+// ---- launch wrappers (kernels_render.cu) ----
+cudaError_t launch_classify(const BrickInfo* bricks, int nbricks, const float4* tf, int tf_w,
+                            int tf_h, int mode, float value_lo, float idx_scale, float iso,
+                            unsigned char* skip, cudaStream_t s);
+cudaError_t launch_render_plain(const FrameDesc& f, cudaStream_t s);
+cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, const FrameDesc* frames,
+                                           int nframes, const int* tile_prefix, int total_tiles,
+                                           int* counter, int grid, cudaStream_t s);
+int persistent_grid_size(int device);
+
+// ---- launch wrappers (kernels_build.cu) ----
+struct BlobTablesDev {
+  int nblobs;
+  const float* amp;
+  const float* ex;
+  const float* ey;
+  const float* ez;
+  const float* bgx;
+  const float* bgy;
+  const float* bgz;
+  float bg_level, bg_amp, scale, noise_amp;
+  int noise_kind;
+  float vmax;
+  uint32_t seed;
+};
+cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], int dtype, void* out,
+                               cudaStream_t s);
+cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3], void* out,
+                              cudaStream_t s);
+cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3],
+                                 const BrickInfo* bricks_dev, int nbricks, void* pool,
+                                 cudaStream_t s);
+cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_dev, int nbricks,
+                                cudaStream_t s);
+cudaError_t launch_hist1d(const void* vol, int dtype, long long n, unsigned long long* hist,
+                          int nbins, cudaStream_t s);
+// 2D histogram passes; scratch holds the pass-1 reduction state.
+struct Hist2DScratch {
+  unsigned long long smax;      // max integer squared central-difference sum
+  unsigned long long gmax_bits; // max f64 |grad| among voxels attaining smax
+};
+cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], double max_scalar,
+                          long long nx, long long merge, unsigned long long* hist,
+                          Hist2DScratch* scratch, cudaStream_t s);
+
+}  // namespace gbvr

@@ -1,0 +1,418 @@
+// UVF build kernels: seeded volume synthesis, 2x2x2 LOD averaging, brick
+// gather with ghost voxels, per-brick min/max, 1D and 2D histograms.
+//
+// These replace the CPU loops behind the reference's UVF build sequence
+// (UVFReader/DataSource.h:475-616: FlatDataToBrickedLOD with
+// CombineAverage<T,1> and SimpleMaxMin<T,1>, Histogram1DDataBlock::Compute /
+// Compress(4096), Histogram2DDataBlock::Compute).  Every kernel here is
+// integer-exact (or a fixed float32 operation order with round-to-nearest
+// intrinsics), so results are bit-identical to the CPU restatement.
+#include "gbvr_internal.h"
+
+namespace gbvr {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11), the counter-based generator used for
+// all seeded draws; identical on host and device.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+    uint32_t lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+    uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+__device__ __forceinline__ float blob_noise(const BlobTablesDev& t, unsigned long long idx) {
+  if (t.noise_kind == 1) {
+    uint32_t c[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), 0x6e6f6973u, 0u};
+    philox(c, t.seed, 0x766f6c21u);
+    float u = __fmul_rn((float)(c[0] >> 8), 1.0f / 16777216.0f);
+    float n = __fmul_rn(u, __fmul_rn(2.0f, t.noise_amp));
+    return __fsub_rn(n, t.noise_amp);
+  }
+  if (t.noise_kind == 2) {
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      uint32_t c[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), 0x6e6f6973u, (uint32_t)k};
+      philox(c, t.seed, 0x766f6c21u);
+      s += (c[0] >> 16) + (c[1] >> 16) + (c[2] >> 16) + (c[3] >> 16);
+    }
+    float z = __fmul_rn((float)s, 1.0f / 65536.0f);
+    z = __fsub_rn(z, 6.0f);
+    return __fmul_rn(z, t.noise_amp);
+  }
+  return 0.0f;
+}
+
+// One CTA per (y, z) row; blob weights of the row staged in shared memory.
+template <typename T>
+__global__ void k_synth_blobs(BlobTablesDev t, long long X, long long Y, long long Z, T* __restrict__ out) {
+  extern __shared__ float w_row[];
+  const long long y = blockIdx.x, z = blockIdx.y;
+  for (int k = threadIdx.x; k < t.nblobs; k += blockDim.x) {
+    float w = __fmul_rn(t.amp[k], t.ez[(long long)k * Z + z]);
+    w_row[k] = __fmul_rn(w, t.ey[(long long)k * Y + y]);
+  }
+  float bgyz = 0.f;
+  if (t.bgx) bgyz = t.bgy[y];
+  __syncthreads();
+  for (long long x = threadIdx.x; x < X; x += blockDim.x) {
+    float acc = 0.0f;
+    if (t.bgx) {
+      float b = __fmul_rn(t.bgx[x], bgyz);
+      b = __fmul_rn(b, t.bgz[z]);
+      b = __fmul_rn(b, t.bg_amp);
+      acc = __fadd_rn(t.bg_level, b);
+    }
+    for (int k = 0; k < t.nblobs; ++k) acc = __fadd_rn(acc, __fmul_rn(w_row[k], __ldg(t.ex + (long long)k * X + x)));
+    float v = __fmul_rn(acc, t.scale);
+    long long idx = (z * Y + y) * X + x;
+    v = __fadd_rn(v, blob_noise(t, (unsigned long long)idx));
+    if (sizeof(T) == 4) {
+      out[idx] = (T)v;
+    } else {
+      float r = rintf(v);
+      r = fminf(fmaxf(r, 0.0f), t.vmax);
+      out[idx] = (T)r;
+    }
+  }
+}
+
+cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], int dtype, void* out, cudaStream_t s) {
+  dim3 grid((unsigned)dims[1], (unsigned)dims[2]);
+  int threads = dims[0] >= 256 ? 256 : 128;
+  size_t smem = sizeof(float) * (t.nblobs > 0 ? t.nblobs : 1);
+  if (dtype == DT_U8) k_synth_blobs<uint8_t><<<grid, threads, smem, s>>>(t, dims[0], dims[1], dims[2], (uint8_t*)out);
+  else if (dtype == DT_U16) k_synth_blobs<uint16_t><<<grid, threads, smem, s>>>(t, dims[0], dims[1], dims[2], (uint16_t*)out);
+  else k_synth_blobs<float><<<grid, threads, smem, s>>>(t, dims[0], dims[1], dims[2], (float*)out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// 2x2x2 LOD averaging (DataSource.h:551,563 CombineAverage<T,1>): the mean of
+// the children that exist, floor for integers, float(sum/count) with a double
+// sum for float32.  One thread per output voxel; x fastest for coalescing.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_downsample(const T* __restrict__ in, long long X, long long Y, long long Z, T* __restrict__ out,
+                             long long OX, long long OY, long long OZ) {
+  long long n = OX * OY * OZ;
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < n; o += (long long)gridDim.x * blockDim.x) {
+    long long x = o % OX, t = o / OX, y = t % OY, z = t / OY;
+    long long x0 = 2 * x, y0 = 2 * y, z0 = 2 * z;
+    int nx = (x0 + 1 < X) ? 2 : 1, ny = (y0 + 1 < Y) ? 2 : 1, nz = (z0 + 1 < Z) ? 2 : 1;
+    if (sizeof(T) == 4) {
+      double sum = 0.0;
+      for (int dz = 0; dz < nz; ++dz)
+        for (int dy = 0; dy < ny; ++dy)
+          for (int dx = 0; dx < nx; ++dx) sum += (double)__ldg(in + ((z0 + dz) * Y + (y0 + dy)) * X + x0 + dx);
+      out[o] = (T)(float)(sum / (double)(nx * ny * nz));
+    } else {
+      unsigned sum = 0;
+      for (int dz = 0; dz < nz; ++dz)
+        for (int dy = 0; dy < ny; ++dy)
+          for (int dx = 0; dx < nx; ++dx) sum += (unsigned)__ldg(in + ((z0 + dz) * Y + (y0 + dy)) * X + x0 + dx);
+      out[o] = (T)(sum / (unsigned)(nx * ny * nz));
+    }
+  }
+}
+
+static int grid_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b > 152LL * 64) b = 152LL * 64;
+  return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3], void* out, cudaStream_t s) {
+  long long OX = (dims[0] + 1) / 2, OY = (dims[1] + 1) / 2, OZ = (dims[2] + 1) / 2;
+  int threads = 256;
+  int blocks = grid_for(OX * OY * OZ, threads);
+  if (dtype == DT_U8)
+    k_downsample<uint8_t><<<blocks, threads, 0, s>>>((const uint8_t*)in, dims[0], dims[1], dims[2], (uint8_t*)out, OX, OY, OZ);
+  else if (dtype == DT_U16)
+    k_downsample<uint16_t><<<blocks, threads, 0, s>>>((const uint16_t*)in, dims[0], dims[1], dims[2], (uint16_t*)out, OX, OY, OZ);
+  else
+    k_downsample<float><<<blocks, threads, 0, s>>>((const float*)in, dims[0], dims[1], dims[2], (float*)out, OX, OY, OZ);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Brick gather: copy each brick's stored box (interior + ghosts) out of the
+// flat level into its pool slot.  One CTA per (brick, z-slice) row block;
+// x fastest so both sides are coalesced.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_gather(const T* __restrict__ level, long long X, long long Y, const BrickInfo* __restrict__ bricks,
+                         T* __restrict__ pool) {
+  const BrickInfo b = bricks[blockIdx.y];
+  const long long plane = (long long)b.sx * b.sy;
+  for (int zs = blockIdx.x; zs < b.sz; zs += gridDim.x) {
+    T* dst = pool + b.offset + (long long)zs * plane;
+    const T* src = level + ((long long)(b.oz + zs) * Y + b.oy) * X + b.ox;
+    for (long long i = threadIdx.x; i < plane; i += blockDim.x) {
+      long long r = i / b.sx, x = i - r * b.sx;
+      dst[i] = __ldg(src + r * X + x);
+    }
+  }
+}
+
+cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3], const BrickInfo* bricks_dev,
+                                 int nbricks, void* pool, cudaStream_t s) {
+  if (nbricks <= 0) return cudaSuccess;
+  dim3 grid((unsigned)(dims[2] < 256 ? dims[2] : 256), (unsigned)nbricks);
+  int threads = 512;
+  if (dtype == DT_U8)
+    k_gather<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], bricks_dev, (uint8_t*)pool);
+  else if (dtype == DT_U16)
+    k_gather<uint16_t><<<grid, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], bricks_dev, (uint16_t*)pool);
+  else
+    k_gather<float><<<grid, threads, 0, s>>>((const float*)level, dims[0], dims[1], bricks_dev, (float*)pool);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Per-brick min/max over the stored voxels (ghosts included: the renderer's
+// empty-space test needs the range of every voxel a sample can touch).
+// One CTA per brick.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_brick_minmax(const T* __restrict__ pool, BrickInfo* __restrict__ bricks) {
+  BrickInfo& b = bricks[blockIdx.x];
+  const T* p = pool + b.offset;
+  const long long n = (long long)b.sx * b.sy * b.sz;
+  float mn = INFINITY, mx = -INFINITY;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    float v = (float)__ldg(p + i);
+    mn = fminf(mn, v);
+    mx = fmaxf(mx, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  __shared__ float smn[32], smx[32];
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { smn[w] = mn; smx[w] = mx; }
+  __syncthreads();
+  if (w == 0) {
+    int nw = blockDim.x >> 5;
+    mn = l < nw ? smn[l] : INFINITY;
+    mx = l < nw ? smx[l] : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (l == 0) { b.vmin = mn; b.vmax = mx; }
+  }
+}
+
+cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_dev, int nbricks, cudaStream_t s) {
+  if (nbricks <= 0) return cudaSuccess;
+  if (dtype == DT_U8) k_brick_minmax<uint8_t><<<nbricks, 1024, 0, s>>>((const uint8_t*)pool, bricks_dev);
+  else if (dtype == DT_U16) k_brick_minmax<uint16_t><<<nbricks, 1024, 0, s>>>((const uint16_t*)pool, bricks_dev);
+  else k_brick_minmax<float><<<nbricks, 1024, 0, s>>>((const float*)pool, bricks_dev);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// 1D histogram (Histogram1DDataBlock::Compute, DataSource.h:603): one bin per
+// value.  Privatised in shared memory (u32 per CTA, flushed with u64 global
+// atomics) when the value range fits; global atomics otherwise.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_hist1d_smem(const T* __restrict__ v, long long n, unsigned long long* __restrict__ hist, int nbins) {
+  extern __shared__ unsigned sh[];
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned b = (unsigned)__ldg(v + i);
+    if (b < (unsigned)nbins) atomicAdd(sh + b, 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+    if (sh[i]) atomicAdd(hist + i, (unsigned long long)sh[i]);
+}
+
+template <typename T>
+__global__ void k_hist1d_global(const T* __restrict__ v, long long n, unsigned long long* __restrict__ hist, int nbins) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned b = (unsigned)__ldg(v + i);
+    if (b < (unsigned)nbins) atomicAdd(hist + b, 1ULL);
+  }
+}
+
+cudaError_t launch_hist1d(const void* vol, int dtype, long long n, unsigned long long* hist, int nbins, cudaStream_t s) {
+  if (dtype == DT_F32) return cudaErrorInvalidValue;
+  int threads = 512;
+  int blocks = grid_for(n, threads);
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  if (nbins <= 16384) {
+    size_t smem = sizeof(unsigned) * nbins;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(dtype == DT_U8 ? (const void*)k_hist1d_smem<uint8_t> : (const void*)k_hist1d_smem<uint16_t>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    if (dtype == DT_U8) k_hist1d_smem<uint8_t><<<blocks, threads, smem, s>>>((const uint8_t*)vol, n, hist, nbins);
+    else k_hist1d_smem<uint16_t><<<blocks, threads, smem, s>>>((const uint16_t*)vol, n, hist, nbins);
+  } else {
+    k_hist1d_global<uint16_t><<<blocks, threads, 0, s>>>((const uint16_t*)vol, n, hist, nbins);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// 2D histogram (Histogram2DDataBlock::Compute, DataSource.h:609-616), rule
+// recovered bit-exactly from DemoData/c60.uvf and stated as an f64 formula:
+//   f = voxel / maxScalar; g_a = central difference / 2 inside, one-sided
+//   first difference on borders; |g| = sqrt((gx^2 + gy^2) + gz^2);
+//   y-bin = floor(|g| / max|g| * 255).
+// Evaluating that in f64 for every voxel is slow on this part, so the kernel
+// works in exact integers: with D_a = v[i+1] - v[i-1] inside and
+// 2 (v[1] - v[0]) on borders, |g| = sqrt(S) / (2 maxScalar) with
+// S = Dx^2 + Dy^2 + Dz^2, and the exact bin is the largest k with
+// k^2 Smax <= 65025 S.  The f64 formula can only land on a different integer
+// when 65025 S - k^2 Smax is within f64 rounding of zero; since that
+// difference is an integer and |r - k| >= 1 / (511 Smax) whenever it is
+// non-zero, which exceeds the f64 error bound (~2e-13 at r <= 255) for every
+// 8- or 16-bit volume, only exact ties (65025 S == k^2 Smax) are evaluated
+// with the f64 formula itself, using __d*_rn intrinsics in the same order.
+// Pass 1 finds Smax and the f64 max |g| over the voxels attaining it;
+// pass 2 bins.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void int_diffs(const T* __restrict__ v, long long X, long long Y, long long Z, long long x,
+                                          long long y, long long z, long long i, int D[3]) {
+  const long long sx = 1, sy = X, sz = X * Y;
+  const long long c[3] = {x, y, z}, n[3] = {X, Y, Z}, st[3] = {sx, sy, sz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (n[a] == 1) D[a] = 0;
+    else if (c[a] == 0) D[a] = 2 * ((int)__ldg(v + i + st[a]) - (int)__ldg(v + i));
+    else if (c[a] == n[a] - 1) D[a] = 2 * ((int)__ldg(v + i) - (int)__ldg(v + i - st[a]));
+    else D[a] = (int)__ldg(v + i + st[a]) - (int)__ldg(v + i - st[a]);
+  }
+}
+
+// The f64 formula for one voxel, operation for operation.
+template <typename T>
+__device__ double grad_f64(const T* __restrict__ v, long long X, long long Y, long long Z, long long x, long long y,
+                           long long z, long long i, double c) {
+  const long long c3[3] = {x, y, z}, n[3] = {X, Y, Z}, st[3] = {1, X, X * Y};
+  double g[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (n[a] == 1) { g[a] = 0.0; continue; }
+    if (c3[a] == 0) g[a] = __dsub_rn(__ddiv_rn((double)__ldg(v + i + st[a]), c), __ddiv_rn((double)__ldg(v + i), c));
+    else if (c3[a] == n[a] - 1) g[a] = __dsub_rn(__ddiv_rn((double)__ldg(v + i), c), __ddiv_rn((double)__ldg(v + i - st[a]), c));
+    else g[a] = __ddiv_rn(__dsub_rn(__ddiv_rn((double)__ldg(v + i + st[a]), c), __ddiv_rn((double)__ldg(v + i - st[a]), c)), 2.0);
+  }
+  double s = __dmul_rn(g[0], g[0]);
+  s = __dadd_rn(s, __dmul_rn(g[1], g[1]));
+  s = __dadd_rn(s, __dmul_rn(g[2], g[2]));
+  return __dsqrt_rn(s);
+}
+
+template <typename T>
+__global__ void k_hist2d_pass1(const T* __restrict__ v, long long X, long long Y, long long Z, Hist2DScratch* sc) {
+  const long long n = X * Y * Z;
+  unsigned long long smax = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    long long x = i % X, t = i / X, y = t % Y, z = t / Y;
+    int D[3];
+    int_diffs(v, X, Y, Z, x, y, z, i, D);
+    unsigned long long S = (unsigned long long)((long long)D[0] * D[0] + (long long)D[1] * D[1] + (long long)D[2] * D[2]);
+    smax = S > smax ? S : smax;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long t = __shfl_xor_sync(0xffffffffu, smax, o);
+    smax = t > smax ? t : smax;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(&sc->smax, smax);
+}
+
+// f64 max |g| over the voxels with S == Smax (positive doubles order like
+// their bit patterns).
+template <typename T>
+__global__ void k_hist2d_pass1b(const T* __restrict__ v, long long X, long long Y, long long Z, double c,
+                                Hist2DScratch* sc) {
+  const long long n = X * Y * Z;
+  const unsigned long long smax = sc->smax;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    long long x = i % X, t = i / X, y = t % Y, z = t / Y;
+    int D[3];
+    int_diffs(v, X, Y, Z, x, y, z, i, D);
+    unsigned long long S = (unsigned long long)((long long)D[0] * D[0] + (long long)D[1] * D[1] + (long long)D[2] * D[2]);
+    if (S == smax && smax > 0) {
+      double g = grad_f64(v, X, Y, Z, x, y, z, i, c);
+      atomicMax(&sc->gmax_bits, (unsigned long long)__double_as_longlong(g));
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y, long long Z, double c, long long nx,
+                               long long merge, unsigned long long* __restrict__ hist, const Hist2DScratch* sc) {
+  const long long n = X * Y * Z;
+  const unsigned long long smax = sc->smax;
+  const double gmax = __longlong_as_double((long long)sc->gmax_bits);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    long long x = i % X, t = i / X, y = t % Y, z = t / Y;
+    int D[3];
+    int_diffs(v, X, Y, Z, x, y, z, i, D);
+    unsigned long long S = (unsigned long long)((long long)D[0] * D[0] + (long long)D[1] * D[1] + (long long)D[2] * D[2]);
+    int k = 0;
+    if (smax > 0 && S > 0) {
+      const unsigned long long lhs = 65025ULL * S;
+      k = (int)(255.0 * sqrt((double)S / (double)smax));
+      if (k > 255) k = 255;
+      while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
+      while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;
+      if ((unsigned long long)k * k * smax == lhs) {
+        // exact tie: the f64 formula decides between k and k - 1
+        double g = grad_f64(v, X, Y, Z, x, y, z, i, c);
+        double r = __dmul_rn(__ddiv_rn(g, gmax), 255.0);
+        k = (int)floor(r);
+        if (k > 255) k = 255;
+      }
+    }
+    long long bx = (long long)__ldg(v + i) / merge;
+    if (bx >= nx) bx = nx - 1;
+    // warp-aggregated increment: empty space puts most voxels in one bin
+    const unsigned long long bin = (unsigned long long)(bx * 256 + k);
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, bin);
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(hist + bin, (unsigned long long)__popc(peers));
+  }
+}
+
+cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], double max_scalar, long long nx,
+                          long long merge, unsigned long long* hist, Hist2DScratch* scratch, cudaStream_t s) {
+  if (dtype == DT_F32) return cudaErrorInvalidValue;
+  const long long X = dims[0], Y = dims[1], Z = dims[2];
+  const double c = max_scalar > 0 ? max_scalar : 1.0;
+  int threads = 256;
+  int blocks = grid_for(X * Y * Z, threads);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(Hist2DScratch), s);
+  if (e != cudaSuccess) return e;
+  if (dtype == DT_U8) {
+    const uint8_t* v = (const uint8_t*)vol;
+    k_hist2d_pass1<<<blocks, threads, 0, s>>>(v, X, Y, Z, scratch);
+    k_hist2d_pass1b<<<blocks, threads, 0, s>>>(v, X, Y, Z, c, scratch);
+    k_hist2d_pass2<<<blocks, threads, 0, s>>>(v, X, Y, Z, c, nx, merge, hist, scratch);
+  } else {
+    const uint16_t* v = (const uint16_t*)vol;
+    k_hist2d_pass1<<<blocks, threads, 0, s>>>(v, X, Y, Z, scratch);
+    k_hist2d_pass1b<<<blocks, threads, 0, s>>>(v, X, Y, Z, c, scratch);
+    k_hist2d_pass2<<<blocks, threads, 0, s>>>(v, X, Y, Z, c, nx, merge, hist, scratch);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace gbvr

@@ -1,0 +1,120 @@
+// Host-only UVF entry points of the C ABI (the UVFReader inspection tool and
+// a raster writer); they touch no GPU.
+#include <cstring>
+#include <string>
+
+#include "../../include/gbvr.h"
+#include "uvf.h"
+
+namespace gbvr {
+int set_error(int code, const std::string& msg);
+}
+
+using namespace gbvr;
+
+extern "C" {
+
+int gbvr_uvf_inspect(const char* path, int verify, gbvr_uvf_summary* out) {
+  if (!path || !out) return set_error(GBVR_EINVAL, "null argument");
+  UvfFile f;
+  std::string msg;
+  int rc = uvf_read(path, verify != 0, f, msg);
+  if (rc) return set_error(rc, msg);
+  memset(out, 0, sizeof(*out));
+  out->version = f.version;
+  out->checksum_semantic = f.checksum_semantic;
+  memcpy(out->checksum, f.checksum.data(), f.checksum.size() < 16 ? f.checksum.size() : 16);
+  out->checksum_verified = verify && f.checksum_ok;
+  out->nblocks = (int)f.blocks.size();
+  for (size_t i = 0; i < f.blocks.size() && i < 32; ++i) out->block_semantics[i] = f.blocks[i].semantic;
+  const UvfRaster& r = f.raster;
+  for (int a = 0; a < 3; ++a) {
+    out->dims[a] = (int64_t)r.dims[a];
+    out->brick_size[a] = (int64_t)r.brick_size[a];
+    out->overlap[a] = (int64_t)r.overlap[a];
+  }
+  out->dtype = r.is_float ? GBVR_F32 : (r.bit_size == 8 ? GBVR_U8 : GBVR_U16);
+  out->lod_count = r.lod_counts.empty() ? 1 : (int)r.lod_counts[0];
+  out->data_offset = r.data_pos;
+  out->hist1d_size = (int64_t)f.hist1d.size();
+  out->hist2d_nx = (int64_t)f.hist2d_nx;
+  out->hist2d_ny = (int64_t)f.hist2d_ny;
+  out->hist2d_max_grad = f.hist2d_max_grad;
+  out->minmax_count = (int64_t)f.minmax.size();
+  if (!f.minmax.empty()) {
+    out->minmax_first[0] = f.minmax[0].min_scalar;
+    out->minmax_first[1] = f.minmax[0].max_scalar;
+    out->minmax_first[2] = f.minmax[0].min_grad;
+    out->minmax_first[3] = f.minmax[0].max_grad;
+  }
+  return GBVR_OK;
+}
+
+int gbvr_uvf_read_volume(const char* path, void* out, size_t bytes) {
+  if (!path || !out) return set_error(GBVR_EINVAL, "null argument");
+  UvfFile f;
+  std::string msg;
+  int rc = uvf_read(path, false, f, msg);
+  if (rc) return set_error(rc, msg);
+  const UvfRaster& r = f.raster;
+  const size_t need = (size_t)r.dims[0] * r.dims[1] * r.dims[2] * (r.bit_size / 8);
+  if (bytes < need) return set_error(GBVR_EINVAL, "buffer too small for the raster data");
+  rc = uvf_read_voxels(path, f, out, need, msg);
+  if (rc) return set_error(rc, msg);
+  return GBVR_OK;
+}
+
+int gbvr_uvf_read_hist1d(const char* path, uint64_t* out, size_t n) {
+  UvfFile f;
+  std::string msg;
+  int rc = uvf_read(path ? path : "", false, f, msg);
+  if (rc) return set_error(rc, msg);
+  if (!out || n < f.hist1d.size()) return set_error(GBVR_EINVAL, "buffer too small");
+  memcpy(out, f.hist1d.data(), 8 * f.hist1d.size());
+  return GBVR_OK;
+}
+
+int gbvr_uvf_read_hist2d(const char* path, uint64_t* out, size_t n, float* max_grad) {
+  UvfFile f;
+  std::string msg;
+  int rc = uvf_read(path ? path : "", false, f, msg);
+  if (rc) return set_error(rc, msg);
+  if (!out || n < f.hist2d.size()) return set_error(GBVR_EINVAL, "buffer too small");
+  memcpy(out, f.hist2d.data(), 8 * f.hist2d.size());
+  if (max_grad) *max_grad = f.hist2d_max_grad;
+  return GBVR_OK;
+}
+
+int gbvr_uvf_write_raster(const char* path, const char* raster_id, const void* voxels, const int64_t dims[3], int dtype,
+                          int32_t brick_size, int32_t overlap, const uint64_t* hist1d, size_t n1, const uint64_t* hist2d,
+                          size_t nx, size_t ny, float max_grad, const double* minmax, size_t nminmax) {
+  if (!path || !voxels || !dims || dtype < 0 || dtype > 2) return set_error(GBVR_EINVAL, "bad argument");
+  UvfWriteSpec s;
+  s.raster.id = raster_id ? raster_id : "";
+  const size_t es = dtype == GBVR_U8 ? 1 : dtype == GBVR_U16 ? 2 : 4;
+  for (int a = 0; a < 3; ++a) {
+    s.raster.dims[a] = (uint64_t)dims[a];
+    s.raster.brick_size[a] = (uint64_t)brick_size;
+    s.raster.overlap[a] = (uint64_t)(2 * overlap);
+  }
+  s.raster.bit_size = 8 * es;
+  s.raster.mantissa = dtype == GBVR_F32 ? 23 : 8 * es;
+  s.raster.is_signed = dtype == GBVR_F32;
+  s.voxels = voxels;
+  s.voxel_bytes = (uint64_t)dims[0] * dims[1] * dims[2] * es;
+  if (hist1d && n1) s.hist1d.assign(hist1d, hist1d + n1);
+  if (hist2d && nx * ny) {
+    s.hist2d.assign(hist2d, hist2d + nx * ny);
+    s.hist2d_nx = nx;
+    s.hist2d_ny = ny;
+    s.hist2d_max_grad = max_grad;
+  }
+  for (size_t i = 0; minmax && i < nminmax; ++i)
+    s.minmax.push_back({minmax[4 * i], minmax[4 * i + 1], minmax[4 * i + 2], minmax[4 * i + 3]});
+  std::string msg;
+  int rc = uvf_write(path, s, msg);
+  if (rc) return set_error(rc, msg);
+  return GBVR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,259 @@
+"""Host-side mirror of the reference renderer interface, over the C ABI.
+
+Method names follow the Lua methods the reference's scripts call on a
+renderer instance (LuaScripts/BatchRenderer.lua:22-41, the RenderWindow
+setters of ImageVis3D/UI/RenderWindow.cpp): ``loadDataset``, ``resize``,
+``setRenderMode``, ``paint``, ``captureSingleFrame``, ``cleanup`` and so on.
+Errors raise ``GbvrError`` carrying the library's status and message.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+_DT = {np.dtype(np.uint8): L.GBVR_U8, np.dtype(np.uint16): L.GBVR_U16,
+       np.dtype(np.float32): L.GBVR_F32}
+_NP = {L.GBVR_U8: np.uint8, L.GBVR_U16: np.uint16, L.GBVR_F32: np.float32}
+
+
+def _fp(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(L.FP)
+
+
+def brick_params(brick_size=256, overlap=2, max_lods=0, build_texture=False, aspect=(1, 1, 1)):
+    bp = L.BrickParams()
+    bp.brick_size = brick_size
+    bp.overlap = overlap
+    bp.max_lods = max_lods
+    bp.build_texture = 1 if build_texture else 0
+    for i in range(3):
+        bp.aspect[i] = aspect[i]
+    return bp
+
+
+def synth_params(dims, dtype, seed, nblobs, sigma, amp, scale, noise_kind=0, noise_amp=0.0,
+                 vmax=255.0, bg_freq=0.0, bg_level=0.0, bg_amp=0.0):
+    p = L.SynthParams()
+    for i in range(3):
+        p.dims[i] = int(dims[i])
+    p.dtype = _DT[np.dtype(dtype)]
+    p.seed = seed
+    p.nblobs = nblobs
+    p.sigma_lo, p.sigma_hi = sigma
+    p.amp_lo, p.amp_hi = amp
+    p.scale = scale
+    p.noise_kind = noise_kind
+    p.noise_amp = noise_amp
+    p.vmax = vmax
+    p.bg_freq = bg_freq
+    p.bg_level = bg_level
+    p.bg_amp = bg_amp
+    return p
+
+
+def orbit_camera(azimuth_deg, elevation_deg, radius, fov_deg, width, height):
+    """View and projection (row-major float32 4x4) of an orbit camera."""
+    v = np.zeros(16, np.float32)
+    pr = np.zeros(16, np.float32)
+    L.call("gbvr_orbit_camera", azimuth_deg, elevation_deg, radius, fov_deg, width, height,
+           v.ctypes.data_as(L.FP), pr.ctypes.data_as(L.FP))
+    return v.reshape(4, 4), pr.reshape(4, 4)
+
+
+def synth_volume(params):
+    """Generate a seeded volume on the GPU and return it as a (z, y, x) array."""
+    dims = [params.dims[i] for i in range(3)]
+    out = np.empty((dims[2], dims[1], dims[0]), _NP[params.dtype])
+    L.call("gbvr_synth_volume", C.byref(params), out.ctypes.data_as(C.c_void_p), out.nbytes)
+    return out
+
+
+class Renderer:
+    """A GBVR_CUDA_RAYCASTER renderer instance (``tuvok.renderer.new``)."""
+
+    def __init__(self, float_fb=False, renderer_type=L.GBVR_CUDA_RAYCASTER):
+        h = C.c_void_p()
+        L.call("gbvr_create", renderer_type, L.GBVR_FLAG_FLOAT_FB if float_fb else 0, C.byref(h))
+        self._h = h
+        self.width, self.height = 640, 480
+        self._nviews = 1
+
+    # -- lifetime -----------------------------------------------------------
+    def cleanup(self):
+        if self._h:
+            L.lib().gbvr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.cleanup()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.cleanup()
+
+    # -- datasets -----------------------------------------------------------
+    def loadDataset(self, path, verify=True, **bp):
+        L.call("gbvr_load_uvf", self._h, path.encode(), 1 if verify else 0,
+               C.byref(brick_params(**bp)) if bp else None)
+
+    def loadVolume(self, vol, **bp):
+        vol = np.ascontiguousarray(vol)
+        dims = (C.c_int64 * 3)(vol.shape[2], vol.shape[1], vol.shape[0])
+        L.call("gbvr_load_volume", self._h, vol.ctypes.data_as(C.c_void_p), dims, _DT[vol.dtype],
+               C.byref(brick_params(**bp)))
+
+    def loadSynthetic(self, params, **bp):
+        L.call("gbvr_load_synthetic", self._h, C.byref(params), C.byref(brick_params(**bp)))
+
+    def datasetInfo(self):
+        info = L.DatasetInfo()
+        L.call("gbvr_get_dataset_info", self._h, C.byref(info))
+        n = info.lod_count
+        return dict(dims=tuple(info.dims), dtype=info.dtype, bit_width=info.bit_width,
+                    range=tuple(info.range), lod_count=n, brick_size=info.brick_size,
+                    overlap=info.overlap,
+                    lod_dims=[tuple(info.lod_dims[i]) for i in range(n)],
+                    lod_bricks=[tuple(info.lod_bricks[i]) for i in range(n)],
+                    total_bricks=info.total_bricks, device_bytes=info.device_bytes,
+                    hist1d_size=info.hist1d_size, hist2d_max_grad=info.hist2d_max_grad)
+
+    def getHistogram(self):
+        n = self.datasetInfo()["hist1d_size"]
+        out = np.zeros(n, np.uint64)
+        L.call("gbvr_get_hist1d", self._h, out.ctypes.data_as(L.U64P), n)
+        return out
+
+    def get2DHistogram(self):
+        nx = self.datasetInfo()["hist1d_size"]
+        out = np.zeros((nx, 256), np.uint64)
+        mg = C.c_float()
+        L.call("gbvr_get_hist2d", self._h, out.ctypes.data_as(L.U64P), nx, 256, C.byref(mg))
+        return out, mg.value
+
+    def brickMinMax(self, lod):
+        nb = int(np.prod(self.datasetInfo()["lod_bricks"][lod]))
+        out = np.zeros((nb, 2), np.float64)
+        L.call("gbvr_get_brick_minmax", self._h, lod, out.ctypes.data_as(C.POINTER(C.c_double)), nb)
+        return out
+
+    def getBrick(self, lod, brick):
+        b = (C.c_int32 * 3)(*brick)
+        o = (C.c_int64 * 3)()
+        s = (C.c_int64 * 3)()
+        L.call("gbvr_get_brick", self._h, lod, b, None, 0, o, s)
+        out = np.empty((s[2], s[1], s[0]), _NP[self.datasetInfo()["dtype"]])
+        L.call("gbvr_get_brick", self._h, lod, b, out.ctypes.data_as(C.c_void_p), out.nbytes, o, s)
+        return out, tuple(o)
+
+    def writeUVF(self, path):
+        L.call("gbvr_write_uvf", self._h, path.encode())
+
+    # -- state --------------------------------------------------------------
+    def resize(self, size):
+        self.width, self.height = int(size[0]), int(size[1])
+        L.call("gbvr_resize", self._h, self.width, self.height)
+
+    def setRenderMode(self, mode):
+        L.call("gbvr_set_render_mode", self._h, mode)
+
+    def set1DTrans(self, tf):
+        tf, p = _fp(tf)
+        L.call("gbvr_set_tf1d", self._h, p, tf.shape[0])
+
+    def set2DTrans(self, tf, max_grad=0.0):
+        tf, p = _fp(tf)
+        L.call("gbvr_set_tf2d", self._h, p, tf.shape[1], tf.shape[0], max_grad)
+
+    def setValueRange(self, lo, hi):
+        L.call("gbvr_set_value_range", self._h, lo, hi)
+
+    def setIsoValue(self, value, rgb=None):
+        c = None
+        if rgb is not None:
+            arr, c = _fp(rgb)
+        L.call("gbvr_set_iso", self._h, value, c)
+
+    def setLightColors(self, ambient, diffuse, specular, direction, enabled=True):
+        a, pa = _fp(ambient)
+        d, pd = _fp(diffuse)
+        s, ps = _fp(specular)
+        v, pv = _fp(direction)
+        L.call("gbvr_set_lighting", self._h, 1 if enabled else 0, pa, pd, ps, pv)
+
+    def setLightingEnabled(self, enabled):
+        L.call("gbvr_set_lighting", self._h, 1 if enabled else 0, None, None, None, None)
+
+    def setSampleRateModifier(self, spv):
+        L.call("gbvr_set_sample_rate", self._h, spv)
+
+    def setInterpolant(self, interp):
+        L.call("gbvr_set_interpolant", self._h, interp)
+
+    def setSampler(self, sampler):
+        L.call("gbvr_set_sampler", self._h, sampler)
+
+    def setLODLimits(self, lo, hi):
+        L.call("gbvr_set_lod_limits", self._h, lo, hi)
+
+    def setView(self, view, proj):
+        v, pv = _fp(view)
+        p, pp = _fp(proj)
+        L.call("gbvr_set_view", self._h, pv, pp)
+
+    def setBGColors(self, top, bottom):
+        t, pt = _fp(top)
+        b, pb = _fp(bottom)
+        L.call("gbvr_set_background", self._h, pt, pb)
+
+    def setEarlyTermination(self, alpha):
+        L.call("gbvr_set_early_termination", self._h, alpha)
+
+    # -- paint / readback ---------------------------------------------------
+    def paint(self):
+        L.call("gbvr_paint", self._h)
+        self._nviews = 1
+
+    @staticmethod
+    def _views(views):
+        arr = (L.View * len(views))()
+        for i, (v, p) in enumerate(views):
+            v = np.ascontiguousarray(v, np.float32).ravel()
+            p = np.ascontiguousarray(p, np.float32).ravel()
+            for k in range(16):
+                arr[i].view[k] = float(v[k])
+                arr[i].proj[k] = float(p[k])
+        return arr
+
+    def paintBatch(self, views):
+        arr = self._views(views)
+        L.call("gbvr_paint_batch", self._h, arr, len(views))
+        self._nviews = len(views)
+
+    def paintViews(self, views):
+        arr = self._views(views)
+        L.call("gbvr_paint_views", self._h, arr, len(views))
+        self._nviews = len(views)
+
+    def readFramebuffer(self, view=0, as_float=False):
+        if as_float:
+            out = np.empty((self.height, self.width, 4), np.float32)
+            L.call("gbvr_read_framebuffer_f32", self._h, view, out.ctypes.data_as(C.c_void_p), out.nbytes)
+        else:
+            out = np.empty((self.height, self.width, 4), np.uint8)
+            L.call("gbvr_read_framebuffer", self._h, view, out.ctypes.data_as(C.c_void_p), out.nbytes)
+        return out
+
+    def captureSingleFrame(self, path, preserve_transparency=True):
+        L.call("gbvr_capture_single_frame", self._h, path.encode(), 1 if preserve_transparency else 0)
+
+    def stats(self):
+        s = L.Stats()
+        L.call("gbvr_get_stats", self._h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in L.Stats._fields_}

@@ -1,0 +1,106 @@
+"""Seeded synthetic workloads: volumes, transfer functions and cameras.
+
+Each workload restates one benchmark configuration of the raycaster with
+seeded synthetic data (no dataset files ship with the reference beyond
+DemoData/c60.uvf).  Volumes come from the Philox blob generator of the
+library (``gbvr_synth_params``); transfer functions and cameras are built here
+on the host from ``numpy.random.default_rng(seed)``, so the GPU path and the
+CPU oracle receive identical inputs.
+"""
+import math
+
+import numpy as np
+
+from .renderer import orbit_camera, synth_params
+
+SEED = 20261203
+DIAG = math.sqrt(3.0)  # diagonal of the unit-normalised cube
+
+
+def tf1d_seeded(n, seed, zero_below, value_max, points=4):
+    """Piecewise-linear RGBA table of n entries through `points` seeded
+    control points; alpha is 0 for data values below `zero_below`.
+    Entry i corresponds to data value i * value_max / (n - 1)."""
+    rng = np.random.default_rng(seed)
+    xs = np.sort(rng.uniform(zero_below, value_max, points))
+    cols = rng.uniform(0.0, 1.0, (points, 3))
+    alphas = rng.uniform(0.15, 1.0, points)
+    v = np.arange(n) * (value_max / (n - 1))
+    tf = np.zeros((n, 4), np.float32)
+    for c in range(3):
+        tf[:, c] = np.interp(v, xs, cols[:, c])
+    a = np.interp(v, np.concatenate([[zero_below], xs]), np.concatenate([[0.0], alphas]))
+    a[v < zero_below] = 0.0
+    tf[:, 3] = a
+    return tf
+
+
+def tf2d_seeded(w, h, seed, widgets=3):
+    """w x h RGBA table over (value, gradient magnitude) with seeded Gaussian
+    ellipse widgets; row = gradient bin, column = value bin."""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(w) + 0.5) / w
+    y = (np.arange(h) + 0.5) / h
+    X, Y = np.meshgrid(x, y)
+    tf = np.zeros((h, w, 4), np.float64)
+    for _ in range(widgets):
+        cx, cy = rng.uniform(0.25, 0.85), rng.uniform(0.1, 0.6)
+        sx, sy = rng.uniform(0.03, 0.12), rng.uniform(0.08, 0.3)
+        col = rng.uniform(0.2, 1.0, 3)
+        amax = rng.uniform(0.3, 0.9)
+        g = np.exp(-0.5 * (((X - cx) / sx) ** 2 + ((Y - cy) / sy) ** 2)) * amax
+        for c in range(3):
+            tf[..., c] = np.maximum(tf[..., c], col[c] * (g > 1e-3))
+        tf[..., 3] = np.maximum(tf[..., 3], np.where(g > 1e-3, g, 0.0))
+    return tf.astype(np.float32)
+
+
+def orbit_views(n, width, height, elevation=20.0, radius=2.5 * DIAG, fov=45.0, start=0.0):
+    """n cameras evenly spaced in azimuth, as the 360-degree capture takes
+    them (ImageVis3D/UI/ImageVis3D_Capturing.cpp:170)."""
+    return [orbit_camera(start + 360.0 * i / n, elevation, radius, fov, width, height) for i in range(n)]
+
+
+class Workload:
+    def __init__(self, name, synth, brick, tf, spv, width, height, views, lod=0,
+                 value_range=None, mode=0):
+        self.name = name
+        self.synth = synth
+        self.brick = brick
+        self.tf = tf
+        self.spv = spv
+        self.width = width
+        self.height = height
+        self.views = views
+        self.lod = lod
+        self.value_range = value_range
+        self.mode = mode
+
+
+def config1(seed=SEED + 1):
+    """128^3 uint8, 8 blobs (sigma 6..20, amplitude 0.3..1.0) + uniform noise
+    +-4, one 128^3 brick, 256-entry TF (alpha 0 below 40), 512^2 at 45 deg,
+    orbit radius 2.5 x diagonal, one seeded azimuth, 1 sample / voxel."""
+    sp = synth_params((128, 128, 128), np.uint8, seed, 8, (6.0, 20.0), (0.3, 1.0), 255.0,
+                      noise_kind=1, noise_amp=4.0, vmax=255.0)
+    tf = tf1d_seeded(256, seed, 40.0, 255.0)
+    az = float(np.random.default_rng(seed).uniform(0, 360))
+    views = [orbit_camera(az, 20.0, 2.5 * DIAG, 45.0, 512, 512)]
+    return Workload("c1_128cube_u8_1brick_512sq", sp, dict(brick_size=256, overlap=2), tf, 1.0,
+                    512, 512, views, value_range=(0.0, 255.0))
+
+
+def config2(size=1024, width=1920, height=1080, nviews=64, brick=256, seed=SEED + 2):
+    """size^3 uint16 with 12-bit values: 64 blobs on a low-frequency
+    background + Gaussian noise sigma 20; 256^3 bricks incl. 2 ghost voxels,
+    LOD pyramid by 2x2x2 averaging; 4096-entry TF; 1920x1080 orbit of 64
+    views; 1.5 samples / voxel; finest level rendered."""
+    s = size / 1024.0
+    sp = synth_params((size, size, size), np.uint16, seed, 64, (24.0 * s, 90.0 * s), (0.3, 1.0),
+                      2600.0, noise_kind=2, noise_amp=20.0, vmax=4095.0, bg_freq=1.0,
+                      bg_level=0.15, bg_amp=0.1)
+    tf = tf1d_seeded(4096, seed, 700.0, 4095.0)
+    views = orbit_views(nviews, width, height)
+    return Workload("c2_%dcube_u16_%dbrick_%dx%d_x%d" % (size, brick, width, height, nviews), sp,
+                    dict(brick_size=brick, overlap=2), tf, 1.5, width, height, views,
+                    value_range=(0.0, 4095.0))

@@ -1,0 +1,283 @@
+/*
+ * gbvr.h - C ABI of the GB300-native bricked volume raycaster and UVF builder.
+ *
+ * This is the drop-in boundary for ImageVis3D's raycast path.  The reference
+ * reaches its renderer through Tuvok's AbstrRenderer, created by
+ * `tuvok.renderer.new` and driven by Lua method calls (the sequence in
+ * LuaScripts/BatchRenderer.lua:22-41); each entry point below names the call
+ * it replaces.  Conventions:
+ *   - every function returns GBVR_OK (0) or a negative GBVR_E* status; the
+ *     message of the last failure on the calling thread is returned by
+ *     gbvr_last_error().  No C++ exception crosses this boundary.
+ *   - handles are opaque; host buffers are owned by the caller; device memory
+ *     is owned by the library.
+ *   - one renderer per host thread; calls on one renderer are not reentrant
+ *     (as paint is not, ImageVis3D/UI/RenderWindow.cpp:2455-2458).
+ *   - matrices are row-major float[16] acting on column vectors (p' = M p),
+ *     OpenGL clip conventions (near plane at z_ndc = -1).
+ *   - volumes are x-fastest; dims[0] = x.  dtype: GBVR_U8, GBVR_U16, GBVR_F32.
+ */
+#ifndef GBVR_H
+#define GBVR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBVR_OK 0
+#define GBVR_EINVAL (-1)      /* invalid argument */
+#define GBVR_ECUDA (-2)       /* CUDA runtime error */
+#define GBVR_ENOMEM (-3)      /* device or pinned allocation failed */
+#define GBVR_EIO (-4)         /* file could not be read or written */
+#define GBVR_EFORMAT (-5)     /* malformed or unsupported UVF content */
+#define GBVR_ECHECKSUM (-6)   /* UVF checksum mismatch */
+#define GBVR_ESTATE (-7)      /* call out of order (e.g. paint before load) */
+#define GBVR_EOVERSIZED (-8)  /* brick larger than the device limit */
+
+#define GBVR_U8 0
+#define GBVR_U16 1
+#define GBVR_F32 2
+
+/* Renderer types.  Tuvok's MasterController::EVolumeRendererType ordinals are
+ * persisted as integers (ImageVis3D/UI/ImageVis3D_Settings.cpp:480; names at
+ * ImageVis3D/UI/RenderWindowGL.cpp:176-188 and SettingsDlg.cpp:486-515), so
+ * the new type is appended after them and none is renumbered. */
+#define GBVR_OPENGL_SBVR 0
+#define GBVR_OPENGL_RAYCASTER 1
+#define GBVR_DIRECTX_SBVR 2
+#define GBVR_DIRECTX_RAYCASTER 3
+#define GBVR_OPENGL_2DSBVR 4
+#define GBVR_DIRECTX_2DSBVR 5
+#define GBVR_OPENGL_GRIDLEAPER 6
+#define GBVR_DIRECTX_GRIDLEAPER 7
+#define GBVR_OPENGL_CHOOSE 8
+#define GBVR_CUDA_RAYCASTER 9 /* this library; the only type it creates */
+
+/* Render modes (AbstrRenderer::ERenderMode, RenderWindow.cpp:2051-2059). */
+#define GBVR_RM_1DTRANS 0
+#define GBVR_RM_2DTRANS 1
+#define GBVR_RM_ISOSURFACE 2
+
+/* Interpolants (RenderWindow.cpp:437-446, ImageVis3D.cpp:881-888). */
+#define GBVR_NEAREST 0
+#define GBVR_LINEAR 1
+
+/* Trilinear sampler: FP32 software interpolation or texture hardware. */
+#define GBVR_SAMPLER_SW 0
+#define GBVR_SAMPLER_TEX 1
+
+/* gbvr_create flags */
+#define GBVR_FLAG_FLOAT_FB 1u /* also keep float RGBA framebuffers (for error measurement) */
+
+typedef struct gbvr_renderer gbvr_renderer;
+
+typedef struct gbvr_brick_params {
+  int32_t brick_size;   /* largest stored brick edge incl. ghosts (uvfconvert
+                           -bricksize, CmdLineConverter/main.cpp:172-174) */
+  int32_t overlap;      /* ghost voxels per face (DEFAULT_BRICKOVERLAP = 2,
+                           CmdLineConverter/main.cpp:145) */
+  int32_t max_lods;     /* 0 = halve until one brick holds the level */
+  int32_t build_texture;/* also build 3D textures for GBVR_SAMPLER_TEX */
+  double aspect[3];     /* voxel spacing; 0 = (1,1,1) */
+} gbvr_brick_params;
+
+typedef struct gbvr_dataset_info {
+  int64_t dims[3];
+  int32_t dtype;
+  int32_t bit_width;      /* getBitWidth (ImageVis3D_WindowHandling.cpp:862-946) */
+  double range[2];        /* getRange: global min / max of LOD 0 */
+  int32_t lod_count;      /* getLODLevelCount */
+  int32_t brick_size, overlap;
+  int64_t lod_dims[16][3];/* getDomainSize(lod) */
+  int32_t lod_bricks[16][3];
+  int64_t total_bricks;
+  uint64_t device_bytes;  /* bytes of the brick pool (sum of stored bricks) */
+  int32_t hist1d_size;    /* bins of the 1D histogram (<= 4096) */
+  float hist2d_max_grad;  /* max gradient magnitude of the 2D histogram */
+} gbvr_dataset_info;
+
+/* One view of a batch: camera, output size and (optionally) its own TF. */
+typedef struct gbvr_view {
+  float view[16];
+  float proj[16];
+} gbvr_view;
+
+typedef struct gbvr_stats {
+  uint64_t frames;             /* views rendered by the last paint call */
+  uint64_t samples;            /* volume samples evaluated (all views) */
+  uint64_t bricks_touched;     /* sum over views of distinct non-skipped bricks sampled */
+  uint64_t bricks_skipped;     /* bricks of the rendered level classified empty */
+  uint64_t brick_bytes;        /* sum over views of stored bytes of touched bricks */
+  uint64_t brick_misses;       /* bricks not resident when requested */
+  uint64_t bytes_paged;        /* host->device brick bytes of the last paint */
+  uint64_t h2d_bytes;          /* host->device bytes copied by the last paint (view descriptors) */
+  int32_t lod;                 /* level rendered (getMinLODIndex) */
+  int32_t subframes;           /* getCurrentSubFrameCount: always 1 */
+  double gpu_ms;               /* device time of the last paint (CUDA events) */
+  double kernel_ms;            /* device time of its raycast kernel launch(es) alone */
+} gbvr_stats;
+
+/* ---- errors / device ---- */
+int gbvr_last_error(char* buf, size_t size);
+int gbvr_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes);
+
+/* ---- renderer lifetime ----
+ * gbvr_create replaces tuvok.renderer.new(type, pow2, 8bit, noBorder, biasTF)
+ *   (LuaScripts/BatchRenderer.lua:22, ImageVis3D/UI/RenderWindowGL.cpp:97-100);
+ *   only GBVR_CUDA_RAYCASTER is accepted.  flags are reserved (0).
+ * gbvr_destroy replaces renderer.cleanup() + deleteClass (BatchRenderer.lua:40-41,
+ *   RenderWindow.cpp:1591-1603). */
+int gbvr_create(int renderer_type, uint32_t flags, gbvr_renderer** out);
+int gbvr_destroy(gbvr_renderer* r);
+
+/* ---- datasets ----
+ * gbvr_load_uvf replaces renderer.loadDataset(path) (BatchRenderer.lua:25,
+ *   RenderWindowGL.cpp:111): reads a UVF v2/v3 file (raster data block,
+ *   histograms, min/max), verifies its MD5 unless verify == 0
+ *   (ImageVis3D_FileHandling.cpp:567-585), and bricks it on the device.
+ * gbvr_load_volume takes a flat host volume and runs the GPU UVF build
+ *   (bricks + LOD pyramid + min/max + histograms) into the device pool,
+ *   replacing tuvok.io.convertDataset (ImageVis3D_FileHandling.cpp:609-611)
+ *   followed by loadDataset.
+ * gbvr_load_synthetic generates a seeded volume directly on the device (see
+ *   gbvr_synth_params) and builds it the same way. */
+int gbvr_load_uvf(gbvr_renderer* r, const char* path, int verify, const gbvr_brick_params* bp);
+int gbvr_load_volume(gbvr_renderer* r, const void* host, const int64_t dims[3], int dtype,
+                     const gbvr_brick_params* bp);
+int gbvr_get_dataset_info(gbvr_renderer* r, gbvr_dataset_info* info);
+/* getHistogram / get2DHistogram (ImageVis3D_WindowHandling.cpp:880-946) */
+int gbvr_get_hist1d(gbvr_renderer* r, uint64_t* out, size_t n);
+int gbvr_get_hist2d(gbvr_renderer* r, uint64_t* out, size_t nx, size_t ny, float* max_grad);
+/* per-brick min/max of one level in brick order (MaxMinDataBlock) */
+int gbvr_get_brick_minmax(gbvr_renderer* r, int lod, double* out_minmax, size_t nbricks);
+/* copy one stored brick (interior + ghosts) back to the host */
+int gbvr_get_brick(gbvr_renderer* r, int lod, const int32_t brick[3], void* out, size_t bytes,
+                   int64_t origin[3], int64_t stored_dims[3]);
+/* write the loaded dataset as a UVF v2 file (raster + 1D/2D histogram + min/max
+ * + key/value blocks, MD5 checksum), the sequence of UVFReader/DataSource.h:453-667 */
+int gbvr_write_uvf(gbvr_renderer* r, const char* path);
+
+/* ---- render state (setters of RenderWindow.h:77-314) ---- */
+int gbvr_resize(gbvr_renderer* r, int width, int height);                 /* resize(UINTVECTOR2) */
+int gbvr_set_render_mode(gbvr_renderer* r, int mode);                     /* setRenderMode */
+int gbvr_set_tf1d(gbvr_renderer* r, const float* rgba, int n);            /* changed1DTrans */
+int gbvr_set_tf2d(gbvr_renderer* r, const float* rgba, int w, int h, float max_grad); /* changed2DTrans */
+int gbvr_set_value_range(gbvr_renderer* r, double lo, double hi);         /* TF domain (biasScaleTF) */
+int gbvr_set_iso(gbvr_renderer* r, float value, const float rgb[3]);      /* setIsoValue, setIsosurfaceColor */
+int gbvr_set_lighting(gbvr_renderer* r, int enabled, const float amb[4], const float diff[4],
+                      const float spec[4], const float dir[3]);          /* setLightingEnabled, setLightColors */
+int gbvr_set_sample_rate(gbvr_renderer* r, float samples_per_voxel);      /* setSampleRateModifier */
+int gbvr_set_interpolant(gbvr_renderer* r, int interp);                   /* setInterpolant */
+int gbvr_set_sampler(gbvr_renderer* r, int sampler);                      /* SW or texture trilinear */
+int gbvr_set_lod_limits(gbvr_renderer* r, int min_lod, int max_lod);      /* setLODLimits */
+int gbvr_set_view(gbvr_renderer* r, const float view[16], const float proj[16]); /* setRotation4x4/... */
+int gbvr_set_background(gbvr_renderer* r, const float top[3], const float bottom[3]); /* setBGColors */
+int gbvr_set_early_termination(gbvr_renderer* r, float alpha);           /* 0.99 by default */
+
+/* ---- paint ----
+ * gbvr_paint replaces renderer.paint() (BatchRenderer.lua:35,
+ *   RenderWindow.cpp:2464): one plain launch for the current view.
+ * gbvr_paint_batch renders n views of the loaded dataset in one persistent
+ *   launch over a shared ray-tile queue (CUDA-graph replayed when the batch
+ *   shape repeats); framebuffer i holds view i.  This is the batched form of
+ *   the 360-degree capture loop (ImageVis3D_Capturing.cpp:159-202).
+ * gbvr_paint_views renders the same n views with n plain launches, the
+ *   per-view form timed beside the batch. */
+int gbvr_paint(gbvr_renderer* r);
+int gbvr_paint_batch(gbvr_renderer* r, const gbvr_view* views, int n);
+int gbvr_paint_views(gbvr_renderer* r, const gbvr_view* views, int n);
+
+/* ---- readback (captureSingleFrame, RenderWindow.cpp:1642-1671; RGBA8 model
+ * StandaloneTuvok/CmdRenderer.cpp:34-56).  Row 0 is the top image row. ---- */
+int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t bytes);
+int gbvr_read_framebuffer_f32(gbvr_renderer* r, int view, float* rgba, size_t bytes);
+int gbvr_capture_single_frame(gbvr_renderer* r, const char* path, int preserve_transparency);
+int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out);
+
+/* ---- seeded synthetic volumes ----
+ * Sum of isotropic Gaussian blobs (+ optional low-frequency background and
+ * uniform or Irwin-Hall Gaussian noise), drawn with Philox4x32-10 from seed;
+ * the volume kinds of the UVFReader generator (UVFReader/DataSource.h:335-396)
+ * re-specified so CPU and GPU agree bit for bit. */
+typedef struct gbvr_synth_params {
+  int64_t dims[3];
+  int32_t dtype;
+  uint32_t seed;
+  int32_t nblobs;
+  float sigma_lo, sigma_hi;    /* voxels */
+  float amp_lo, amp_hi;
+  float bg_freq;               /* 0 = no background */
+  float bg_level, bg_amp;
+  float scale;                 /* value = scale * (background + blobs) + noise */
+  int32_t noise_kind;          /* 0 none, 1 uniform +-noise_amp, 2 Gaussian sigma noise_amp */
+  float noise_amp;
+  float vmax;                  /* integer types clamp to [0, vmax] */
+} gbvr_synth_params;
+
+int gbvr_synth_volume(const gbvr_synth_params* p, void* host_out, size_t bytes);
+int gbvr_load_synthetic(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr_brick_params* bp);
+
+/* ---- GPU UVF build without a renderer (uvfconvert, CmdLineConverter/main.cpp:406-408):
+ * host volume in, UVF v2 file out. ---- */
+int gbvr_build_uvf(const void* host, const int64_t dims[3], int dtype, const gbvr_brick_params* bp,
+                   const char* out_path);
+
+/* ---- device-resident build kernels, for callers that keep volumes in HBM.
+ * Pointers are device pointers; sizes are elements. ---- */
+int gbvr_dev_hist1d(const void* dev_vol, int dtype, int64_t n, uint64_t* dev_hist, int nbins,
+                    void* stream);
+int gbvr_dev_hist2d(const void* dev_vol, int dtype, const int64_t dims[3], double max_scalar,
+                    int64_t nx, int64_t merge, uint64_t* dev_hist, float* max_grad, void* stream);
+int gbvr_dev_downsample(const void* dev_in, int dtype, const int64_t dims[3], void* dev_out,
+                        void* stream);
+
+/* Orbit camera around the volume centre: the rotation the 360-degree capture
+ * applies per frame (ImageVis3D_Capturing.cpp:170 fAngle = i/N * 360,
+ * RenderWindow.cpp:207-214 RotationY).  Eye at radius (world units, the
+ * largest volume axis spans 1), azimuth about +y, elevation above the xz
+ * plane, looking at the origin with +y up; perspective fov_deg vertical. */
+int gbvr_orbit_camera(float azimuth_deg, float elevation_deg, float radius, float fov_deg, int width,
+                      int height, float view[16], float proj[16]);
+
+/* ---- host-only UVF inspection (the UVFReader tool, UVFReader/main.cpp:23-205,
+ * UVFReader/BlockInfo.h:27-401).  No GPU is used. ---- */
+typedef struct gbvr_uvf_summary {
+  uint64_t version;
+  uint64_t checksum_semantic;  /* 0 none, 1 crc32, 2 MD5 */
+  uint8_t checksum[16];
+  int32_t checksum_verified;   /* 1 when verify was requested and matched */
+  int32_t nblocks;
+  uint64_t block_semantics[32];
+  int64_t dims[3];
+  int32_t dtype;
+  int32_t lod_count;
+  int64_t brick_size[3];
+  int64_t overlap[3];          /* as stored: 2 x ghost voxels */
+  uint64_t data_offset;        /* file offset of the voxels */
+  int64_t hist1d_size;
+  int64_t hist2d_nx, hist2d_ny;
+  float hist2d_max_grad;
+  int64_t minmax_count;
+  double minmax_first[4];      /* min, max, min gradient, max gradient of brick 0 */
+} gbvr_uvf_summary;
+
+int gbvr_uvf_inspect(const char* path, int verify, gbvr_uvf_summary* out);
+int gbvr_uvf_read_volume(const char* path, void* out, size_t bytes);
+int gbvr_uvf_read_hist1d(const char* path, uint64_t* out, size_t n);
+int gbvr_uvf_read_hist2d(const char* path, uint64_t* out, size_t n, float* max_grad);
+/* Write a single-brick, single-LOD UVF v2 file from host arrays: raster block
+ * `raster_id`, then the given 1D / 2D histograms and min/max entries (each
+ * may be empty), MD5 over bytes 49..end.  This is the layout of c60.uvf. */
+int gbvr_uvf_write_raster(const char* path, const char* raster_id, const void* voxels,
+                          const int64_t dims[3], int dtype, int32_t brick_size, int32_t overlap,
+                          const uint64_t* hist1d, size_t n1, const uint64_t* hist2d, size_t nx,
+                          size_t ny, float max_grad, const double* minmax, size_t nminmax);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBVR_H */

@@ -1,0 +1,655 @@
+// CPU oracle for the bricked volume raycaster and the UVF build.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA path is
+// compared against; nothing in the product links or calls it.  Only tests/,
+// __graft_entry__.smoke() and bench.py's cpu_baseline leg load it.
+//
+// The reference implementation of this path (Tuvok's GLSL raycaster, its
+// ExtendedOctree bricker and its histogram blocks) lives in an un-vendored git
+// submodule (https://github.com/SCIInstitute/Tuvok.git, branch master, no
+// pinned commit) that is absent from the reference tree, so it cannot be
+// compiled.  What this file restates, and where each rule comes from:
+//
+//  * UVF build call sequence:     UVFReader/DataSource.h:398-683
+//      - LOD count rule            DataSource.h:521-529 (halve until it fits)
+//      - overlap stored as 2*g     DataSource.h:537-539, CmdLineConverter/main.cpp:145
+//      - averaging combiner        DataSource.h:547-572 (CombineAverage<T,1>)
+//      - per-brick min/max         DataSource.h:467-469,552 (SimpleMaxMin<T,1>)
+//      - 1D histogram + Compress   DataSource.h:601-608
+//      - 2D histogram              DataSource.h:609-616
+//  * Renderer parameters:          LuaScripts/BatchRenderer.lua:18-41,
+//                                  ImageVis3D/UI/RenderWindow.cpp:437-451,2051-2140
+//
+// Parity is pinned against DemoData/c60.uvf (the reference's own output):
+// the 1D histogram, the 2D histogram (bit-exact, including its float32
+// max-gradient) and the min/max block.  Rendered images cannot be pinned
+// against the reference (no GL stack); the raycaster below is the project's
+// documented sampling rule evaluated in FP64.
+//
+// Build: g++ -O2 -fopenmp -ffp-contract=off -shared -fPIC (see oracle/build.py).
+// -ffp-contract=off matters: the integer-exact generators and the f64
+// histogram rule must not be contracted into FMAs on any host.
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include <limits>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef int64_t i64;
+typedef uint64_t u64;
+
+enum { DT_U8 = 0, DT_U16 = 1, DT_F32 = 2 };
+
+static inline double load_voxel(const void* p, int dt, i64 i) {
+  switch (dt) {
+    case DT_U8: return (double)((const uint8_t*)p)[i];
+    case DT_U16: return (double)((const uint16_t*)p)[i];
+    default: return (double)((const float*)p)[i];
+  }
+}
+static inline size_t dt_size(int dt) { return dt == DT_U8 ? 1 : dt == DT_U16 ? 2 : 4; }
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy
+// as 1, 2, 3", SC'11).  Counter-based, so any voxel's draw is independent.
+// ---------------------------------------------------------------------------
+static inline void mulhilo(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo) {
+  u64 p = (u64)a * (u64)b;
+  *hi = (uint32_t)(p >> 32);
+  *lo = (uint32_t)p;
+}
+void orc_philox(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+  uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  uint32_t k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo(0xD2511F53u, c0, &hi0, &lo0);
+    mulhilo(0xCD9E8D57u, c2, &hi1, &lo1);
+    uint32_t n0 = hi1 ^ c1 ^ k0, n1 = lo1, n2 = hi0 ^ c3 ^ k1, n3 = lo0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// ---------------------------------------------------------------------------
+// LOD pyramid and brick grid (rules stated in the header of this file).
+// ---------------------------------------------------------------------------
+// Level l+1 has ceil(n/2) voxels per axis.  Levels are added until the
+// largest axis fits in one brick interior (brick - 2*ghost), as the
+// reference's raster path halves the largest dimension until it fits a brick
+// (DataSource.h:521-529).  max_lods > 0 caps the count.
+int orc_lod_dims(const i64 dims[3], int brick, int ghost, int max_lods, i64* out /*[L][3]*/) {
+  i64 interior = brick - 2 * ghost;
+  i64 n[3] = {dims[0], dims[1], dims[2]};
+  int count = 0;
+  for (;;) {
+    out[3 * count + 0] = n[0];
+    out[3 * count + 1] = n[1];
+    out[3 * count + 2] = n[2];
+    ++count;
+    i64 mx = std::max(n[0], std::max(n[1], n[2]));
+    if (mx <= interior || count == 16) break;
+    if (max_lods > 0 && count >= max_lods) break;
+    for (int a = 0; a < 3; ++a) n[a] = (n[a] + 1) / 2;
+  }
+  return count;
+}
+
+// A level is a single brick without ghosts when its largest axis fits the
+// brick interior (c60.uvf: 128^3 in a 256-brick with overlap 4 stores exactly
+// 128^3 voxels).  Otherwise it is a grid of interior-sized bricks, each stored
+// with `ghost` voxels of its neighbours on every face that has a neighbour.
+void orc_brick_grid(const i64 dims[3], int brick, int ghost, i64 nb[3], i64* interior) {
+  i64 I = brick - 2 * ghost;
+  i64 mx = std::max(dims[0], std::max(dims[1], dims[2]));
+  if (mx <= I) {
+    nb[0] = nb[1] = nb[2] = 1;
+    *interior = mx;
+    return;
+  }
+  for (int a = 0; a < 3; ++a) nb[a] = (dims[a] + I - 1) / I;
+  *interior = I;
+}
+
+void orc_brick_extent(const i64 dims[3], int brick, int ghost, const i64 b[3],
+                      i64 origin[3], i64 sdims[3]) {
+  i64 nb[3], I;
+  orc_brick_grid(dims, brick, ghost, nb, &I);
+  for (int a = 0; a < 3; ++a) {
+    if (nb[0] * nb[1] * nb[2] == 1) {
+      origin[a] = 0;
+      sdims[a] = dims[a];
+      continue;
+    }
+    i64 lo = std::max<i64>(b[a] * I - ghost, 0);
+    i64 hi = std::min<i64>((b[a] + 1) * I + ghost, dims[a]);
+    origin[a] = lo;
+    sdims[a] = hi - lo;
+  }
+}
+
+void orc_extract_brick(const void* vol, int dt, const i64 dims[3], int brick, int ghost,
+                       const i64 b[3], void* out) {
+  i64 o[3], s[3];
+  orc_brick_extent(dims, brick, ghost, b, o, s);
+  size_t es = dt_size(dt);
+  for (i64 z = 0; z < s[2]; ++z)
+    for (i64 y = 0; y < s[1]; ++y) {
+      const char* src = (const char*)vol + (((o[2] + z) * dims[1] + (o[1] + y)) * dims[0] + o[0]) * es;
+      char* dst = (char*)out + ((z * s[1] + y) * s[0]) * es;
+      memcpy(dst, src, s[0] * es);
+    }
+}
+
+// 2x2x2 average: each output voxel averages the children that exist (1..8 at
+// odd edges).  Integer types take floor(sum / count), i.e. the truncating
+// conversion T(double(sum)/count) of an averaging combiner over non-negative
+// values; float32 takes float(sum / count) with the sum in double.
+void orc_downsample(const void* in, int dt, const i64 dims[3], void* out) {
+  i64 od[3] = {(dims[0] + 1) / 2, (dims[1] + 1) / 2, (dims[2] + 1) / 2};
+#pragma omp parallel for schedule(static)
+  for (i64 z = 0; z < od[2]; ++z)
+    for (i64 y = 0; y < od[1]; ++y)
+      for (i64 x = 0; x < od[0]; ++x) {
+        double sum = 0;
+        u64 isum = 0;
+        int cnt = 0;
+        for (int dz = 0; dz < 2; ++dz)
+          for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+              i64 sx = 2 * x + dx, sy = 2 * y + dy, sz = 2 * z + dz;
+              if (sx >= dims[0] || sy >= dims[1] || sz >= dims[2]) continue;
+              i64 i = (sz * dims[1] + sy) * dims[0] + sx;
+              if (dt == DT_F32) sum += ((const float*)in)[i];
+              else isum += (u64)load_voxel(in, dt, i);
+              ++cnt;
+            }
+        i64 o = (z * od[1] + y) * od[0] + x;
+        if (dt == DT_U8) ((uint8_t*)out)[o] = (uint8_t)(isum / cnt);
+        else if (dt == DT_U16) ((uint16_t*)out)[o] = (uint16_t)(isum / cnt);
+        else ((float*)out)[o] = (float)(sum / cnt);
+      }
+}
+
+void orc_minmax(const void* data, int dt, i64 n, double* mn, double* mx) {
+  double a = std::numeric_limits<double>::infinity(), b = -a;
+  for (i64 i = 0; i < n; ++i) {
+    double v = load_voxel(data, dt, i);
+    a = std::min(a, v);
+    b = std::max(b, v);
+  }
+  *mn = a;
+  *mx = b;
+}
+
+// 1D histogram of an integer volume: one bin per value, trailing empty bins
+// trimmed (size = max + 1), then merged to at most `max_bins` bins by summing
+// runs of f = ceil(size / max_bins) consecutive values.
+i64 orc_hist1d(const void* vol, int dt, i64 n, int max_bins, u64* out /* >= 65536 */,
+               i64* merge_factor) {
+  std::vector<u64> h(dt == DT_U8 ? 256 : 65536, 0);
+  for (i64 i = 0; i < n; ++i) h[(size_t)load_voxel(vol, dt, i)]++;
+  i64 size = (i64)h.size();
+  while (size > 1 && h[size - 1] == 0) --size;
+  i64 f = (size + max_bins - 1) / max_bins;
+  if (f < 1) f = 1;
+  i64 outsize = (size + f - 1) / f;
+  for (i64 j = 0; j < outsize; ++j) {
+    u64 s = 0;
+    for (i64 k = j * f; k < std::min(size, (j + 1) * f); ++k) s += h[k];
+    out[j] = s;
+  }
+  *merge_factor = f;
+  return outsize;
+}
+
+// 2D histogram, value x gradient magnitude (rule recovered bit-exactly from
+// DemoData/c60.uvf; call site DataSource.h:609-616):
+//   f(i)  = voxel(i) / maxScalar                     (f64)
+//   g_a   = (f(i+1) - f(i-1)) / 2 inside, one-sided first differences on the
+//           borders, 0 on an axis of length 1
+//   |g|   = sqrt((gx*gx + gy*gy) + gz*gz), x the fastest axis
+//   max   = max |g|;  y-bin = floor(|g| / max * 255) (0 when max == 0)
+//   x-bin = value / merge_factor (the 1D histogram's merge)
+// out is nx * 256 u64, x slowest.  Returns max |g| in f64.
+double orc_hist2d(const void* vol, int dt, const i64 dims[3], double max_scalar, i64 nx,
+                  i64 merge_factor, u64* out) {
+  const i64 X = dims[0], Y = dims[1], Z = dims[2];
+  const double c = max_scalar > 0 ? max_scalar : 1.0;
+  auto f = [&](i64 x, i64 y, i64 z) { return load_voxel(vol, dt, (z * Y + y) * X + x) / c; };
+  auto grad = [&](i64 x, i64 y, i64 z) {
+    double gx, gy, gz;
+    if (X == 1) gx = 0;
+    else if (x == 0) gx = f(1, y, z) - f(0, y, z);
+    else if (x == X - 1) gx = f(X - 1, y, z) - f(X - 2, y, z);
+    else gx = (f(x + 1, y, z) - f(x - 1, y, z)) / 2.0;
+    if (Y == 1) gy = 0;
+    else if (y == 0) gy = f(x, 1, z) - f(x, 0, z);
+    else if (y == Y - 1) gy = f(x, Y - 1, z) - f(x, Y - 2, z);
+    else gy = (f(x, y + 1, z) - f(x, y - 1, z)) / 2.0;
+    if (Z == 1) gz = 0;
+    else if (z == 0) gz = f(x, y, 1) - f(x, y, 0);
+    else if (z == Z - 1) gz = f(x, y, Z - 1) - f(x, y, Z - 2);
+    else gz = (f(x, y, z + 1) - f(x, y, z - 1)) / 2.0;
+    double s = gx * gx;
+    s = s + gy * gy;
+    s = s + gz * gz;
+    return std::sqrt(s);
+  };
+  double mg = 0;
+#pragma omp parallel for reduction(max : mg) schedule(static)
+  for (i64 z = 0; z < Z; ++z)
+    for (i64 y = 0; y < Y; ++y)
+      for (i64 x = 0; x < X; ++x) mg = std::max(mg, grad(x, y, z));
+  memset(out, 0, sizeof(u64) * nx * 256);
+  for (i64 z = 0; z < Z; ++z)
+    for (i64 y = 0; y < Y; ++y)
+      for (i64 x = 0; x < X; ++x) {
+        double g = grad(x, y, z);
+        i64 by = 0;
+        if (mg > 0) {
+          double r = g / mg;
+          r = r * 255.0;
+          by = (i64)std::floor(r);
+          if (by > 255) by = 255;
+        }
+        i64 bx = (i64)load_voxel(vol, dt, (z * Y + y) * X + x) / merge_factor;
+        if (bx >= nx) bx = nx - 1;
+        out[bx * 256 + by]++;
+      }
+  return mg;
+}
+
+// ---------------------------------------------------------------------------
+// Seeded synthetic volumes.  Every voxel is a fixed sequence of float32
+// multiplies and adds over per-axis tables, so a CUDA kernel that performs the
+// same sequence with round-to-nearest intrinsics reproduces it bit for bit.
+// ---------------------------------------------------------------------------
+struct orc_blob_tables {
+  int nblobs;
+  const float* amp;     // [nblobs]
+  const float* ex;      // [nblobs][nx]
+  const float* ey;      // [nblobs][ny]
+  const float* ez;      // [nblobs][nz]
+  const float* bgx;     // [nx] or null
+  const float* bgy;     // [ny]
+  const float* bgz;     // [nz]
+  float bg_level;       // background = bg_level + bg_amp * bgx*bgy*bgz
+  float bg_amp;
+  float scale;          // value = scale * (background + sum of blobs) + noise
+  float noise_amp;      // uniform: +-noise_amp; gaussian: sigma
+  int noise_kind;       // 0 none, 1 uniform, 2 Irwin-Hall(12) gaussian
+  float vmax;           // clamp to [0, vmax]
+  uint32_t seed;
+};
+
+static inline float blob_noise(const orc_blob_tables* t, u64 idx) {
+  uint32_t ctr[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), 0x6e6f6973u, 0};
+  uint32_t key[2] = {t->seed, 0x766f6c21u};
+  uint32_t r[4];
+  if (t->noise_kind == 1) {
+    orc_philox(ctr, key, r);
+    float u = (float)(r[0] >> 8) * (1.0f / 16777216.0f);
+    float n = u * (2.0f * t->noise_amp);
+    return n - t->noise_amp;
+  }
+  if (t->noise_kind == 2) {
+    uint32_t s = 0;
+    for (int k = 0; k < 3; ++k) {
+      ctr[3] = (uint32_t)k;
+      orc_philox(ctr, key, r);
+      for (int j = 0; j < 4; ++j) s += (r[j] >> 16);
+    }
+    float z = (float)s * (1.0f / 65536.0f);
+    z = z - 6.0f;
+    return z * t->noise_amp;
+  }
+  return 0.0f;
+}
+
+// Per-axis tables of the blob generator, restated from the recipe:
+//  blob k: Philox(ctr {k, 0, 'blob', 0}, key {seed, 'para'}) -> centre
+//          u_i * n_i (u_i = top 24 bits / 2^24); Philox(ctr {k, 1, ...})
+//          -> sigma = lo + u0 (hi - lo), amplitude = lo + u1 (hi - lo)
+//  e_k(i)  = float(exp(-(i - c)^2 / (2 sigma^2)))           (double math)
+//  background b(i) = float(cos(2 pi (f (i + 0.5) / n + phase))), phases from
+//          Philox(ctr {0xffffffff, 2, 'blob', 0})
+// Caller provides storage: amp[nb], ex[nb*nx], ey[nb*ny], ez[nb*nz],
+// bg*[n] (when bg_freq > 0).
+void orc_blob_tables_make(const i64 dims[3], uint32_t seed, int nb, double sig_lo, double sig_hi,
+                          double amp_lo, double amp_hi, double bg_freq, float* amp, float* ex,
+                          float* ey, float* ez, float* bgx, float* bgy, float* bgz) {
+  const uint32_t key[2] = {seed, 0x70617261u};
+  float* tabs[3] = {ex, ey, ez};
+  for (int k = 0; k < nb; ++k) {
+    uint32_t c0[4] = {(uint32_t)k, 0u, 0x626c6f62u, 0u}, r0[4];
+    uint32_t c1[4] = {(uint32_t)k, 1u, 0x626c6f62u, 0u}, r1[4];
+    orc_philox(c0, key, r0);
+    orc_philox(c1, key, r1);
+    double cen[3];
+    for (int a = 0; a < 3; ++a) cen[a] = (double)(r0[a] >> 8) / 16777216.0 * (double)dims[a];
+    double sig = sig_lo + (double)(r1[0] >> 8) / 16777216.0 * (sig_hi - sig_lo);
+    double am = amp_lo + (double)(r1[1] >> 8) / 16777216.0 * (amp_hi - amp_lo);
+    amp[k] = (float)am;
+    for (int a = 0; a < 3; ++a)
+      for (i64 i = 0; i < dims[a]; ++i) {
+        double dd = (double)i - cen[a];
+        tabs[a][(i64)k * dims[a] + i] = (float)std::exp(-(dd * dd) / (2.0 * sig * sig));
+      }
+  }
+  if (bg_freq > 0) {
+    uint32_t c[4] = {0xffffffffu, 2u, 0x626c6f62u, 0u}, r[4];
+    orc_philox(c, key, r);
+    float* bt[3] = {bgx, bgy, bgz};
+    for (int a = 0; a < 3; ++a) {
+      double ph = (double)(r[a] >> 8) / 16777216.0;
+      for (i64 i = 0; i < dims[a]; ++i)
+        bt[a][i] = (float)std::cos(2.0 * M_PI * (bg_freq * ((double)i + 0.5) / (double)dims[a] + ph));
+    }
+  }
+}
+
+void orc_synth_blobs(const orc_blob_tables* t, const i64 dims[3], int dt, void* out) {
+  const i64 X = dims[0], Y = dims[1], Z = dims[2];
+#pragma omp parallel for schedule(static)
+  for (i64 z = 0; z < Z; ++z)
+    for (i64 y = 0; y < Y; ++y)
+      for (i64 x = 0; x < X; ++x) {
+        float acc = 0.0f;
+        if (t->bgx) {
+          float b = t->bgx[x] * t->bgy[y];
+          b = b * t->bgz[z];
+          b = b * t->bg_amp;
+          acc = t->bg_level + b;
+        }
+        for (int k = 0; k < t->nblobs; ++k) {
+          float w = t->amp[k] * t->ez[(i64)k * Z + z];
+          w = w * t->ey[(i64)k * Y + y];
+          w = w * t->ex[(i64)k * X + x];
+          acc = acc + w;
+        }
+        float v = acc * t->scale;
+        i64 idx = (z * Y + y) * X + x;
+        v = v + blob_noise(t, (u64)idx);
+        if (dt == DT_F32) {
+          ((float*)out)[idx] = v;
+          continue;
+        }
+        float r = std::nearbyint(v);
+        if (r < 0.0f) r = 0.0f;
+        if (r > t->vmax) r = t->vmax;
+        if (dt == DT_U8) ((uint8_t*)out)[idx] = (uint8_t)r;
+        else ((uint16_t*)out)[idx] = (uint16_t)r;
+      }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 raycaster: the project's sampling rule, evaluated directly on the flat
+// volume of the rendered LOD (no bricks: the bricked GPU walk must reproduce
+// sampling of the whole level, since ghost voxels are exact copies).
+// ---------------------------------------------------------------------------
+struct orc_render_params {
+  const void* vol;      // flat level, x fastest
+  int dtype;
+  i64 dims[3];          // dims of the rendered level
+  double extent[3];     // world box = [-extent/2, +extent/2] (largest axis 1)
+  const float* tf;      // 1D: [n][4]; 2D: [h][w][4] (row = gradient bin)
+  int tf_w, tf_h;       // 1D: tf_w entries, tf_h = 1
+  int mode;             // 0 1D TF, 1 2D TF + Phong, 2 isosurface
+  int interp;           // 0 nearest, 1 trilinear
+  double value_lo, value_hi;   // data value mapped to TF coordinate 0 / 1
+  double grad_max;      // 2D TF: |grad| (normalised value per voxel) at the last row
+  double samples_per_voxel;
+  double ert;           // early ray termination threshold (0.99)
+  double iso;           // data value
+  double iso_rgb[3];
+  int lighting;
+  double amb[3], diff[3], spec[3];
+  double shininess;
+  double light_dir_eye[3];  // direction the light travels, eye space
+  double bg[3];
+  double inv_viewproj[16];  // row-major inverse of proj*view (column vectors)
+  double inv_view[16];      // row-major inverse of view
+  int width, height;
+};
+
+struct Vol {
+  const orc_render_params* p;
+  double sample_nearest(double x, double y, double z) const {
+    i64 ix = (i64)std::floor(x + 0.5), iy = (i64)std::floor(y + 0.5), iz = (i64)std::floor(z + 0.5);
+    ix = std::min(std::max<i64>(ix, 0), p->dims[0] - 1);
+    iy = std::min(std::max<i64>(iy, 0), p->dims[1] - 1);
+    iz = std::min(std::max<i64>(iz, 0), p->dims[2] - 1);
+    return load_voxel(p->vol, p->dtype, (iz * p->dims[1] + iy) * p->dims[0] + ix);
+  }
+  double sample(double x, double y, double z) const {
+    if (!p->interp) return sample_nearest(x, y, z);
+    double fx0 = std::floor(x), fy0 = std::floor(y), fz0 = std::floor(z);
+    double fx = x - fx0, fy = y - fy0, fz = z - fz0;
+    i64 x0 = (i64)fx0, y0 = (i64)fy0, z0 = (i64)fz0;
+    i64 X = p->dims[0], Y = p->dims[1], Z = p->dims[2];
+    auto cl = [](i64 v, i64 n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); };
+    i64 xa = cl(x0, X), xb = cl(x0 + 1, X), ya = cl(y0, Y), yb = cl(y0 + 1, Y);
+    i64 za = cl(z0, Z), zb = cl(z0 + 1, Z);
+    auto v = [&](i64 xi, i64 yi, i64 zi) { return load_voxel(p->vol, p->dtype, (zi * Y + yi) * X + xi); };
+    auto lerp = [](double a, double b, double t) { return a + t * (b - a); };
+    double c00 = lerp(v(xa, ya, za), v(xb, ya, za), fx);
+    double c10 = lerp(v(xa, yb, za), v(xb, yb, za), fx);
+    double c01 = lerp(v(xa, ya, zb), v(xb, ya, zb), fx);
+    double c11 = lerp(v(xa, yb, zb), v(xb, yb, zb), fx);
+    double c0 = lerp(c00, c10, fy), c1 = lerp(c01, c11, fy);
+    return lerp(c0, c1, fz);
+  }
+  // central differences of the interpolated field, h = 1 voxel, in data
+  // value units per voxel
+  void gradient(double x, double y, double z, double g[3]) const {
+    g[0] = (sample(x + 1, y, z) - sample(x - 1, y, z)) * 0.5;
+    g[1] = (sample(x, y + 1, z) - sample(x, y - 1, z)) * 0.5;
+    g[2] = (sample(x, y, z + 1) - sample(x, y, z - 1)) * 0.5;
+  }
+};
+
+static void mat_vec4(const double* m, const double v[4], double o[4]) {
+  for (int r = 0; r < 4; ++r) o[r] = m[4 * r] * v[0] + m[4 * r + 1] * v[1] + m[4 * r + 2] * v[2] + m[4 * r + 3] * v[3];
+}
+
+static void tf1d_lookup(const orc_render_params* p, double idx, double c[4]) {
+  int n = p->tf_w;
+  if (idx < 0) idx = 0;
+  if (idx > n - 1) idx = n - 1;
+  int i0 = (int)std::floor(idx);
+  int i1 = std::min(i0 + 1, n - 1);
+  double f = idx - i0;
+  for (int k = 0; k < 4; ++k) {
+    double a = p->tf[4 * i0 + k], b = p->tf[4 * i1 + k];
+    c[k] = a + f * (b - a);
+  }
+}
+
+static void tf2d_lookup(const orc_render_params* p, double ix, double iy, double c[4]) {
+  int w = p->tf_w, h = p->tf_h;
+  ix = std::min(std::max(ix, 0.0), (double)(w - 1));
+  iy = std::min(std::max(iy, 0.0), (double)(h - 1));
+  int x0 = (int)std::floor(ix), y0 = (int)std::floor(iy);
+  int x1 = std::min(x0 + 1, w - 1), y1 = std::min(y0 + 1, h - 1);
+  double fx = ix - x0, fy = iy - y0;
+  for (int k = 0; k < 4; ++k) {
+    double a = p->tf[4 * (y0 * w + x0) + k], b = p->tf[4 * (y0 * w + x1) + k];
+    double cc = p->tf[4 * (y1 * w + x0) + k], d = p->tf[4 * (y1 * w + x1) + k];
+    double t0 = a + fx * (b - a), t1 = cc + fx * (d - cc);
+    c[k] = t0 + fy * (t1 - t0);
+  }
+}
+
+// Phong with a directional light; the normal is the negated normalised
+// gradient, flipped to face the viewer (two-sided).
+static void shade(const orc_render_params* p, const double g[3], const double vdir[3],
+                  const double L[3], const double col[3], double out[3]) {
+  double gl = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+  if (gl <= 0) {
+    for (int k = 0; k < 3; ++k) out[k] = col[k] * p->amb[k];
+    return;
+  }
+  double n[3] = {-g[0] / gl, -g[1] / gl, -g[2] / gl};
+  double V[3] = {-vdir[0], -vdir[1], -vdir[2]};
+  double nv = n[0] * V[0] + n[1] * V[1] + n[2] * V[2];
+  if (nv < 0) for (int k = 0; k < 3; ++k) n[k] = -n[k];
+  double nl = std::max(0.0, n[0] * L[0] + n[1] * L[1] + n[2] * L[2]);
+  double H[3] = {L[0] + V[0], L[1] + V[1], L[2] + V[2]};
+  double hl = std::sqrt(H[0] * H[0] + H[1] * H[1] + H[2] * H[2]);
+  double nh = 0;
+  if (hl > 0) nh = std::max(0.0, (n[0] * H[0] + n[1] * H[1] + n[2] * H[2]) / hl);
+  double sp = std::pow(nh, p->shininess);
+  for (int k = 0; k < 3; ++k) out[k] = col[k] * (p->amb[k] + p->diff[k] * nl) + p->spec[k] * sp;
+}
+
+static void render_pixel(const orc_render_params* p, int px, int py, double* out,
+                         i64* nsamples) {
+  Vol V{p};
+  double ndc_x = (px + 0.5) / p->width * 2.0 - 1.0;
+  double ndc_y = 1.0 - (py + 0.5) / p->height * 2.0;
+  double a[4] = {ndc_x, ndc_y, -1.0, 1.0}, b[4] = {ndc_x, ndc_y, 1.0, 1.0}, na[4], fb[4];
+  mat_vec4(p->inv_viewproj, a, na);
+  mat_vec4(p->inv_viewproj, b, fb);
+  double o[3], d[3];
+  for (int k = 0; k < 3; ++k) {
+    o[k] = na[k] / na[3];
+    d[k] = fb[k] / fb[3] - o[k];
+  }
+  double dl = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  for (int k = 0; k < 3; ++k) d[k] /= dl;
+  double t0 = 0.0, t1 = std::numeric_limits<double>::infinity();
+  for (int k = 0; k < 3; ++k) {
+    double lo = -0.5 * p->extent[k], hi = 0.5 * p->extent[k];
+    if (d[k] == 0.0) {
+      if (o[k] < lo || o[k] > hi) { t1 = -1; break; }
+      continue;
+    }
+    double ta = (lo - o[k]) / d[k], tb = (hi - o[k]) / d[k];
+    t0 = std::max(t0, std::min(ta, tb));
+    t1 = std::min(t1, std::max(ta, tb));
+  }
+  double C[3] = {0, 0, 0}, A = 0;
+  // light: travels along light_dir_eye, transformed to world by the inverse view
+  double L[3] = {0, 0, 0};
+  {
+    double ld[3];
+    for (int r = 0; r < 3; ++r)
+      ld[r] = p->inv_view[4 * r] * p->light_dir_eye[0] + p->inv_view[4 * r + 1] * p->light_dir_eye[1] +
+              p->inv_view[4 * r + 2] * p->light_dir_eye[2];
+    double ll = std::sqrt(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
+    if (ll > 0) for (int k = 0; k < 3; ++k) L[k] = -ld[k] / ll;
+  }
+  i64 ns = 0;
+  if (t1 > t0) {
+    i64 maxd = std::max(p->dims[0], std::max(p->dims[1], p->dims[2]));
+    double dt = 1.0 / (p->samples_per_voxel * (double)maxd);
+    double K = std::ceil((t1 - t0) / dt - 0.5);
+    i64 nk = K > 0 ? (i64)K : 0;
+    double e = 1.0 / p->samples_per_voxel;
+    double scale_v[3], off_v[3];
+    for (int k = 0; k < 3; ++k) {
+      scale_v[k] = (double)p->dims[k] / p->extent[k];
+      off_v[k] = 0.5 * p->extent[k];
+    }
+    auto to_vox = [&](double t, double x[3]) {
+      for (int k = 0; k < 3; ++k) x[k] = (o[k] + t * d[k] + off_v[k]) * scale_v[k] - 0.5;
+    };
+    double vscale = 1.0 / (p->value_hi - p->value_lo);
+    double prev_t = t0;
+    for (i64 k = 0; k < nk; ++k) {
+      double t = t0 + (k + 0.5) * dt;
+      double x[3];
+      to_vox(t, x);
+      double v = V.sample(x[0], x[1], x[2]);
+      ++ns;
+      if (p->mode == 2) {
+        if (v >= p->iso) {
+          double tl = (k == 0) ? t0 : prev_t, th = t;
+          for (int it = 0; it < 4; ++it) {
+            double tm = 0.5 * (tl + th), xm[3];
+            to_vox(tm, xm);
+            if (V.sample(xm[0], xm[1], xm[2]) >= p->iso) th = tm;
+            else tl = tm;
+          }
+          double th_hit = 0.5 * (tl + th), xh[3], g[3], col[3];
+          to_vox(th_hit, xh);
+          V.gradient(xh[0], xh[1], xh[2], g);
+          for (int c = 0; c < 3; ++c) g[c] *= scale_v[c];  // world-space direction
+          if (p->lighting) shade(p, g, d, L, p->iso_rgb, col);
+          else for (int c = 0; c < 3; ++c) col[c] = p->iso_rgb[c];
+          for (int c = 0; c < 3; ++c) C[c] = col[c];
+          A = 1.0;
+          break;
+        }
+        prev_t = t;
+        continue;
+      }
+      double c[4];
+      double vn = (v - p->value_lo) * vscale;
+      if (p->mode == 0) {
+        tf1d_lookup(p, vn * (p->tf_w - 1), c);
+      } else {
+        double g[3];
+        V.gradient(x[0], x[1], x[2], g);
+        double gm = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]) * vscale;
+        tf2d_lookup(p, vn * (p->tf_w - 1), gm / p->grad_max * (p->tf_h - 1), c);
+        if (p->lighting && c[3] > 0) {
+          double lit[3], gw[3];
+          for (int q = 0; q < 3; ++q) gw[q] = g[q] * scale_v[q];
+          shade(p, gw, d, L, c, lit);
+          c[0] = lit[0]; c[1] = lit[1]; c[2] = lit[2];
+        }
+      }
+      double al = c[3];
+      if (e != 1.0) al = 1.0 - std::pow(1.0 - al, e);
+      double w = (1.0 - A) * al;
+      C[0] += w * c[0];
+      C[1] += w * c[1];
+      C[2] += w * c[2];
+      A += w;
+      if (A >= p->ert) break;
+    }
+  }
+  for (int k = 0; k < 3; ++k) out[k] = C[k] + (1.0 - A) * p->bg[k];
+  out[3] = A;
+  if (nsamples) *nsamples = ns;
+}
+
+// Render `npix` pixels (indices into the width*height image, row 0 = top) or
+// the whole image when pixels == null.  out: [npix][4] doubles.  Returns the
+// number of samples taken.
+i64 orc_render(const orc_render_params* p, const int64_t* pixels, i64 npix, double* out, int threads) {
+  i64 total = pixels ? npix : (i64)p->width * p->height;
+  i64 ns_total = 0;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : ns_total)
+  for (i64 i = 0; i < total; ++i) {
+    i64 pix = pixels ? pixels[i] : i;
+    i64 ns = 0;
+    render_pixel(p, (int)(pix % p->width), (int)(pix / p->width), out + 4 * i, &ns);
+    ns_total += ns;
+  }
+  return ns_total;
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

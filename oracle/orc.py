@@ -1,0 +1,196 @@
+"""ctypes binding of the CPU oracle (oracle/liborc.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's cpu_baseline leg, never by the product.  See oracle.cpp for the
+rules it restates and the reference files they come from.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+I64 = C.c_int64
+D = C.c_double
+U64P = C.POINTER(C.c_uint64)
+_DT = {np.dtype(np.uint8): 0, np.dtype(np.uint16): 1, np.dtype(np.float32): 2}
+
+
+class RenderParams(C.Structure):
+    _fields_ = [
+        ("vol", C.c_void_p), ("dtype", C.c_int), ("dims", I64 * 3), ("extent", D * 3),
+        ("tf", C.POINTER(C.c_float)), ("tf_w", C.c_int), ("tf_h", C.c_int), ("mode", C.c_int),
+        ("interp", C.c_int), ("value_lo", D), ("value_hi", D), ("grad_max", D),
+        ("samples_per_voxel", D), ("ert", D), ("iso", D), ("iso_rgb", D * 3), ("lighting", C.c_int),
+        ("amb", D * 3), ("diff", D * 3), ("spec", D * 3), ("shininess", D),
+        ("light_dir_eye", D * 3), ("bg", D * 3), ("inv_viewproj", D * 16), ("inv_view", D * 16),
+        ("width", C.c_int), ("height", C.c_int),
+    ]
+
+
+class BlobTables(C.Structure):
+    _fields_ = [
+        ("nblobs", C.c_int), ("amp", C.c_void_p), ("ex", C.c_void_p), ("ey", C.c_void_p),
+        ("ez", C.c_void_p), ("bgx", C.c_void_p), ("bgy", C.c_void_p), ("bgz", C.c_void_p),
+        ("bg_level", C.c_float), ("bg_amp", C.c_float), ("scale", C.c_float),
+        ("noise_amp", C.c_float), ("noise_kind", C.c_int), ("vmax", C.c_float),
+        ("seed", C.c_uint32),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = C.CDLL(path)
+        _lib.orc_render.restype = I64
+        _lib.orc_hist1d.restype = I64
+        _lib.orc_hist2d.restype = D
+        _lib.orc_lod_dims.restype = C.c_int
+        _lib.orc_max_threads.restype = C.c_int
+    return _lib
+
+
+def _dims(vol):
+    return (I64 * 3)(vol.shape[2], vol.shape[1], vol.shape[0])
+
+
+def lod_dims(dims, brick, ghost, max_lods=0):
+    out = (I64 * 96)()
+    n = lib().orc_lod_dims((I64 * 3)(*dims), brick, ghost, max_lods, out)
+    return [tuple(out[3 * i:3 * i + 3]) for i in range(n)]
+
+
+def brick_grid(dims, brick, ghost):
+    nb = (I64 * 3)()
+    interior = I64()
+    lib().orc_brick_grid((I64 * 3)(*dims), brick, ghost, nb, C.byref(interior))
+    return tuple(nb), interior.value
+
+
+def extract_brick(vol, brick, ghost, b):
+    dims = (vol.shape[2], vol.shape[1], vol.shape[0])
+    o = (I64 * 3)()
+    s = (I64 * 3)()
+    lib().orc_brick_extent((I64 * 3)(*dims), brick, ghost, (I64 * 3)(*b), o, s)
+    out = np.empty((s[2], s[1], s[0]), vol.dtype)
+    vol = np.ascontiguousarray(vol)
+    lib().orc_extract_brick(vol.ctypes.data_as(C.c_void_p), _DT[vol.dtype], _dims(vol), brick, ghost,
+                            (I64 * 3)(*b), out.ctypes.data_as(C.c_void_p))
+    return out, tuple(o)
+
+
+def downsample(vol):
+    vol = np.ascontiguousarray(vol)
+    out = np.empty(((vol.shape[0] + 1) // 2, (vol.shape[1] + 1) // 2, (vol.shape[2] + 1) // 2), vol.dtype)
+    lib().orc_downsample(vol.ctypes.data_as(C.c_void_p), _DT[vol.dtype], _dims(vol),
+                         out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def hist1d(vol, max_bins=4096):
+    vol = np.ascontiguousarray(vol)
+    out = np.zeros(65536, np.uint64)
+    f = I64()
+    n = lib().orc_hist1d(vol.ctypes.data_as(C.c_void_p), _DT[vol.dtype], I64(vol.size), max_bins,
+                         out.ctypes.data_as(U64P), C.byref(f))
+    return out[:n].copy(), f.value
+
+
+def hist2d(vol, max_scalar, nx, merge=1):
+    vol = np.ascontiguousarray(vol)
+    out = np.zeros(nx * 256, np.uint64)
+    mg = lib().orc_hist2d(vol.ctypes.data_as(C.c_void_p), _DT[vol.dtype], _dims(vol), D(max_scalar),
+                          I64(nx), I64(merge), out.ctypes.data_as(U64P))
+    return out.reshape(nx, 256), mg
+
+
+def synth_blobs(params):
+    """CPU restatement of the seeded blob generator (gbvr_synth_params)."""
+    dims = [params.dims[i] for i in range(3)]
+    nb = params.nblobs
+    amp = np.zeros(max(nb, 1), np.float32)
+    ex = np.zeros(max(nb * dims[0], 1), np.float32)
+    ey = np.zeros(max(nb * dims[1], 1), np.float32)
+    ez = np.zeros(max(nb * dims[2], 1), np.float32)
+    bgx = np.zeros(dims[0], np.float32)
+    bgy = np.zeros(dims[1], np.float32)
+    bgz = np.zeros(dims[2], np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    lib().orc_blob_tables_make((I64 * 3)(*dims), C.c_uint32(params.seed), nb, D(params.sigma_lo),
+                               D(params.sigma_hi), D(params.amp_lo), D(params.amp_hi),
+                               D(params.bg_freq), fp(amp), fp(ex), fp(ey), fp(ez), fp(bgx), fp(bgy),
+                               fp(bgz))
+    t = BlobTables()
+    t.nblobs = nb
+    t.amp, t.ex, t.ey, t.ez = (a.ctypes.data for a in (amp, ex, ey, ez))
+    bg = params.bg_freq > 0
+    t.bgx = bgx.ctypes.data if bg else None
+    t.bgy = bgy.ctypes.data if bg else None
+    t.bgz = bgz.ctypes.data if bg else None
+    t.bg_level, t.bg_amp, t.scale = params.bg_level, params.bg_amp, params.scale
+    t.noise_amp, t.noise_kind, t.vmax, t.seed = params.noise_amp, params.noise_kind, params.vmax, params.seed
+    dt = {0: np.uint8, 1: np.uint16, 2: np.float32}[params.dtype]
+    out = np.empty((dims[2], dims[1], dims[0]), dt)
+    keep = (amp, ex, ey, ez, bgx, bgy, bgz)  # noqa: F841  (alive during the call)
+    lib().orc_synth_blobs(C.byref(t), (I64 * 3)(*dims), params.dtype, out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0), mode=0,
+           interp=1, ert=0.99, extent=None, grad_max=1.0, iso=0.0, iso_rgb=(1, 1, 1), lighting=1,
+           amb=(0.1, 0.1, 0.1), diff=(1, 1, 1), spec=(1, 1, 1), shininess=8.0,
+           light_dir=(0, 0, -1), bg=(0, 0, 0), pixels=None, threads=0):
+    """FP64 render of `vol` (the flat level, (z, y, x)).  Returns
+    (rgba float64 [n, 4] or [h, w, 4], samples)."""
+    vol = np.ascontiguousarray(vol)
+    tf = np.ascontiguousarray(tf, np.float32)
+    p = RenderParams()
+    p.vol = vol.ctypes.data
+    p.dtype = _DT[vol.dtype]
+    for i, d in enumerate((vol.shape[2], vol.shape[1], vol.shape[0])):
+        p.dims[i] = d
+    if extent is None:
+        m = max(vol.shape)
+        extent = (vol.shape[2] / m, vol.shape[1] / m, vol.shape[0] / m)
+    for i in range(3):
+        p.extent[i] = extent[i]
+    p.tf = tf.ctypes.data_as(C.POINTER(C.c_float))
+    if tf.ndim == 2:
+        p.tf_w, p.tf_h = tf.shape[0], 1
+    else:
+        p.tf_w, p.tf_h = tf.shape[1], tf.shape[0]
+    p.mode, p.interp = mode, interp
+    p.value_lo, p.value_hi = value_range
+    p.grad_max = grad_max
+    p.samples_per_voxel, p.ert, p.iso = spv, ert, iso
+    p.lighting = lighting
+    for i in range(3):
+        p.iso_rgb[i], p.amb[i], p.diff[i], p.spec[i] = iso_rgb[i], amb[i], diff[i], spec[i]
+        p.light_dir_eye[i], p.bg[i] = light_dir[i], bg[i]
+    p.shininess = shininess
+    V = np.asarray(view, np.float64).reshape(4, 4)
+    Pm = np.asarray(proj, np.float64).reshape(4, 4)
+    Mi = np.linalg.inv(Pm @ V)
+    Vi = np.linalg.inv(V)
+    for i in range(16):
+        p.inv_viewproj[i] = Mi.ravel()[i]
+        p.inv_view[i] = Vi.ravel()[i]
+    p.width, p.height = width, height
+    if pixels is None:
+        out = np.zeros((height * width, 4), np.float64)
+        ns = lib().orc_render(C.byref(p), None, I64(0), out.ctypes.data_as(C.POINTER(D)), threads)
+        return out.reshape(height, width, 4), ns
+    pix = np.ascontiguousarray(pixels, np.int64)
+    out = np.zeros((pix.size, 4), np.float64)
+    ns = lib().orc_render(C.byref(p), pix.ctypes.data_as(C.POINTER(I64)), I64(pix.size),
+                          out.ctypes.data_as(C.POINTER(D)), threads)
+    return out, ns
+
+
+def max_threads():
+    return lib().orc_max_threads()

@@ -739,18 +739,15 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   gbvr_renderer::GraphKey key{n, r->width, r->height, level, r->ds.dtype, r->mode, r->sampler, r->d_fb8.p, r->d_fb32.p};
   auto it = r->graphs.find(key);
   if (it == r->graphs.end()) {
+    // The graph holds the persistent launch; descriptor uploads and counter
+    // resets are plain stream operations before it, so the kernel-only
+    // events can bracket the graph launch.
     cudaGraph_t g;
+    (void)cudaGetLastError();
     CUDA_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
-    cudaMemcpyAsync(r->d_frames.p, r->h_frames.p, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, r->stream);
-    cudaMemcpyAsync(r->d_prefix.p, r->h_prefix.p, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, r->stream);
-    cudaMemsetAsync(r->d_counter.p, 0, sizeof(int), r->stream);
-    cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream);
-    cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream);
-    cudaEventRecord(r->evk0, r->stream);
     cudaError_t le = launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), n,
                                                     r->d_prefix.as<int>(), total, r->d_counter.as<int>(), r->grid,
                                                     r->stream);
-    cudaEventRecord(r->evk1, r->stream);
     cudaError_t ce = cudaStreamEndCapture(r->stream, &g);
     if (le != cudaSuccess) return cuda_fail(le, "persistent launch capture");
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
@@ -761,7 +758,14 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     it = r->graphs.emplace(key, ge).first;
   }
   CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
+  CUDA_TRY(cudaMemcpyAsync(r->d_frames.p, r->h_frames.p, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, r->stream));
+  CUDA_TRY(cudaMemcpyAsync(r->d_prefix.p, r->h_prefix.p, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, r->stream));
+  CUDA_TRY(cudaMemsetAsync(r->d_counter.p, 0, sizeof(int), r->stream));
+  CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream));
+  CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
+  CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
   CUDA_TRY(cudaGraphLaunch(it->second, r->stream));
+  CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
   r->last_h2d = sizeof(FrameDesc) * n + sizeof(int) * (n + 1);
   return finish(r, n, level);

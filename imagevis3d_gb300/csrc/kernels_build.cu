@@ -85,6 +85,7 @@ __global__ void k_synth_blobs(BlobTablesDev t, long long X, long long Y, long lo
 }
 
 cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], int dtype, void* out, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   dim3 grid((unsigned)dims[1], (unsigned)dims[2]);
   int threads = dims[0] >= 256 ? 256 : 128;
   size_t smem = sizeof(float) * (t.nblobs > 0 ? t.nblobs : 1);
@@ -130,6 +131,7 @@ static int grid_for(long long n, int threads) {
 }
 
 cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3], void* out, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   long long OX = (dims[0] + 1) / 2, OY = (dims[1] + 1) / 2, OZ = (dims[2] + 1) / 2;
   int threads = 256;
   int blocks = grid_for(OX * OY * OZ, threads);
@@ -164,6 +166,7 @@ __global__ void k_gather(const T* __restrict__ level, long long X, long long Y, 
 
 cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3], const BrickInfo* bricks_dev,
                                  int nbricks, void* pool, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (nbricks <= 0) return cudaSuccess;
   dim3 grid((unsigned)(dims[2] < 256 ? dims[2] : 256), (unsigned)nbricks);
   int threads = 512;
@@ -213,6 +216,7 @@ __global__ void k_brick_minmax(const T* __restrict__ pool, BrickInfo* __restrict
 }
 
 cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_dev, int nbricks, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (nbricks <= 0) return cudaSuccess;
   if (dtype == DT_U8) k_brick_minmax<uint8_t><<<nbricks, 1024, 0, s>>>((const uint8_t*)pool, bricks_dev);
   else if (dtype == DT_U16) k_brick_minmax<uint16_t><<<nbricks, 1024, 0, s>>>((const uint16_t*)pool, bricks_dev);
@@ -248,6 +252,7 @@ __global__ void k_hist1d_global(const T* __restrict__ v, long long n, unsigned l
 }
 
 cudaError_t launch_hist1d(const void* vol, int dtype, long long n, unsigned long long* hist, int nbins, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (dtype == DT_F32) return cudaErrorInvalidValue;
   int threads = 512;
   int blocks = grid_for(n, threads);
@@ -394,6 +399,7 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
 
 cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], double max_scalar, long long nx,
                           long long merge, unsigned long long* hist, Hist2DScratch* scratch, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (dtype == DT_F32) return cudaErrorInvalidValue;
   const long long X = dims[0], Y = dims[1], Z = dims[2];
   const double c = max_scalar > 0 ? max_scalar : 1.0;

@@ -460,6 +460,7 @@ __global__ void k_classify(const BrickInfo* __restrict__ bricks, int nbricks, co
 
 cudaError_t launch_classify(const BrickInfo* bricks, int nbricks, const float4* tf, int tf_w, int tf_h, int mode,
                             float value_lo, float idx_scale, float iso, unsigned char* skip, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (nbricks <= 0) return cudaSuccess;
   int threads = 128;
   int blocks = (nbricks * 32 + threads - 1) / threads;
@@ -469,6 +470,7 @@ cudaError_t launch_classify(const BrickInfo* bricks, int nbricks, const float4* 
 
 template <typename T, int MODE, int SAMPLER>
 static cudaError_t plain_t(const FrameDesc& f, cudaStream_t s) {
+  (void)cudaGetLastError();
   int tiles = f.tiles_x * f.tiles_y;
   int warps_per_block = RENDER_THREADS / 32;
   int blocks = (tiles + warps_per_block - 1) / warps_per_block;
@@ -480,6 +482,7 @@ static cudaError_t plain_t(const FrameDesc& f, cudaStream_t s) {
 template <typename T, int MODE, int SAMPLER>
 static cudaError_t persistent_t(const FrameDesc* frames, int nframes, const int* prefix, int total, int* counter,
                                 int grid, cudaStream_t s) {
+  (void)cudaGetLastError();
   k_render_persistent<T, MODE, SAMPLER><<<grid, RENDER_THREADS, 0, s>>>(frames, nframes, prefix, total, counter);
   return cudaGetLastError();
 }
@@ -510,6 +513,7 @@ static cudaError_t persistent_t(const FrameDesc* frames, int nframes, const int*
   } while (0)
 
 cudaError_t launch_render_plain(const FrameDesc& f, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   GBVR_DISPATCH(plain_t, f.dtype, f.mode, f.sampler, f, s);
 }
 
@@ -517,6 +521,7 @@ cudaError_t launch_render_plain(const FrameDesc& f, cudaStream_t s) {
 // host groups a mixed batch by these and issues one launch per group).
 cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, const FrameDesc* frames, int nframes,
                                            const int* prefix, int total, int* counter, int grid, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   GBVR_DISPATCH(persistent_t, dtype, mode, sampler, frames, nframes, prefix, total, counter, grid, s);
 }
 

@@ -93,13 +93,14 @@ def config1(seed=SEED + 1):
 def config2(size=1024, width=1920, height=1080, nviews=64, brick=256, seed=SEED + 2):
     """size^3 uint16 with 12-bit values: 64 blobs on a low-frequency
     background + Gaussian noise sigma 20; 256^3 bricks incl. 2 ghost voxels,
-    LOD pyramid by 2x2x2 averaging; 4096-entry TF; 1920x1080 orbit of 64
+    LOD pyramid by 2x2x2 averaging; 4096-entry TF, transparent below 900 so
+    background-only bricks are skipped; 1920x1080 orbit of 64
     views; 1.5 samples / voxel; finest level rendered."""
     s = size / 1024.0
     sp = synth_params((size, size, size), np.uint16, seed, 64, (24.0 * s, 90.0 * s), (0.3, 1.0),
                       2600.0, noise_kind=2, noise_amp=20.0, vmax=4095.0, bg_freq=1.0,
                       bg_level=0.15, bg_amp=0.1)
-    tf = tf1d_seeded(4096, seed, 700.0, 4095.0)
+    tf = tf1d_seeded(4096, seed, 900.0, 4095.0)
     views = orbit_views(nviews, width, height)
     return Workload("c2_%dcube_u16_%dbrick_%dx%d_x%d" % (size, brick, width, height, nviews), sp,
                     dict(brick_size=brick, overlap=2), tf, 1.5, width, height, views,

@@ -33,8 +33,10 @@ def test_config1_matches_oracle(orc):
     ref, ns = orc.render(vol, view, proj, wl.width, wl.height, wl.tf, spv=wl.spv,
                          value_range=wl.value_range)
     assert_close(img, ref)
-    assert np.array_equal(img8, np.rint(np.clip(img, 0, 1) * 255).astype(np.uint8))
-    assert (ref[..., 3] > 0.05).mean() > 0.05, "workload renders something"
+    # RGBA8 = round-to-nearest-even of the float32 product c * 255 (saturated)
+    want8 = np.rint(np.clip(img, 0, 1).astype(np.float32) * np.float32(255)).astype(np.uint8)
+    assert np.array_equal(img8, want8)
+    assert (ref[..., 3] > 0.05).mean() > 0.02, "workload renders something"
     # samples counted in-kernel agree with the oracle's count to within ERT/boundary effects
     assert abs(st["samples"] - ns) <= 0.01 * ns
 
@@ -55,13 +57,13 @@ def test_c60_with_reference_tf_matches_oracle(orc, c60):
 
 @pytest.fixture(scope="module")
 def multibrick(orc):
-    sp = synth_params((150, 130, 110), np.uint16, 11, 24, (5.0, 22.0), (0.3, 1.0), 2600.0,
+    sp = synth_params((150, 130, 110), np.uint16, 11, 10, (4.0, 12.0), (0.3, 1.0), 2600.0,
                       noise_kind=2, noise_amp=20.0, vmax=4095.0, bg_freq=1.0, bg_level=0.15, bg_amp=0.1)
     vol = orc.synth_blobs(sp)
     levels = [vol]
     for _ in orc.lod_dims((150, 130, 110), 64, 2)[1:]:
         levels.append(orc.downsample(levels[-1]))
-    tf = workloads.tf1d_seeded(4096, 11, 700.0, 4095.0)
+    tf = workloads.tf1d_seeded(4096, 11, 900.0, 4095.0)
     return vol, levels, tf
 
 
@@ -186,9 +188,10 @@ def test_2d_tf_with_lighting_matches_oracle(orc, multibrick):
     assert ref[..., 3].max() > 0.2
 
 
-@pytest.mark.parametrize("iso", [900.0, 1800.0, 2600.0])
-def test_isosurface_matches_oracle(orc, multibrick, iso):
+@pytest.mark.parametrize("q", [99.0, 99.7, 99.95])
+def test_isosurface_matches_oracle(orc, multibrick, q):
     vol, _, _ = multibrick
+    iso = float(np.percentile(vol, q))
     view, proj = orbit_camera(120.0, 10.0, 2.5 * workloads.DIAG, 45.0, 160, 120)
     with Renderer(float_fb=True) as r:
         r.loadVolume(vol, brick_size=64, overlap=2)
@@ -204,7 +207,7 @@ def test_isosurface_matches_oracle(orc, multibrick, iso):
     assert (hit_g != hit_r).mean() < 0.002
     both = hit_g & hit_r
     assert_close(img[both], ref[both])
-    assert hit_r.mean() > 0.01
+    assert hit_r.mean() > 0.002
 
 
 def test_texture_sampler_matches_oracle(orc, multibrick):

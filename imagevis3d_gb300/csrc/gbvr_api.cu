@@ -269,19 +269,13 @@ void plan_level(const long long dims[3], int brick, int ghost, int level, Level&
         int bc[3] = {bx, by, bz};
         int o[3], s[3], lo[3], hi[3];
         for (int a = 0; a < 3; ++a) {
-          if (single) {
-            o[a] = 0;
-            s[a] = (int)dims[a];
-            lo[a] = -1;
-            hi[a] = (int)dims[a];
-          } else {
-            long long ilo = (long long)bc[a] * I, ihi = std::min<long long>(ilo + I, dims[a]);
-            long long slo = std::max<long long>(ilo - ghost, 0), shi = std::min<long long>(ihi + ghost, dims[a]);
-            o[a] = (int)slo;
-            s[a] = (int)(shi - slo);
-            lo[a] = bc[a] == 0 ? -1 : (int)ilo;
-            hi[a] = (int)ihi;
-          }
+          // interior [ilo, ihi); stored box = interior + `ghost` voxels on
+          // every face (replicated edge voxels outside the level)
+          long long ilo = (long long)bc[a] * L.interior, ihi = std::min<long long>(ilo + L.interior, dims[a]);
+          o[a] = (int)(ilo - ghost);
+          s[a] = (int)(ihi - ilo + 2 * ghost);
+          lo[a] = bc[a] == 0 ? -1 : (int)ilo;
+          hi[a] = (int)ihi;
         }
         b.ox = o[0]; b.oy = o[1]; b.oz = o[2];
         b.sx = s[0]; b.sy = s[1]; b.sz = s[2];

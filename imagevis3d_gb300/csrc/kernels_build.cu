@@ -150,16 +150,19 @@ cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3]
 // x fastest so both sides are coalesced.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_gather(const T* __restrict__ level, long long X, long long Y, const BrickInfo* __restrict__ bricks,
-                         T* __restrict__ pool) {
+__global__ void k_gather(const T* __restrict__ level, long long X, long long Y, long long Z,
+                         const BrickInfo* __restrict__ bricks, T* __restrict__ pool) {
   const BrickInfo b = bricks[blockIdx.y];
   const long long plane = (long long)b.sx * b.sy;
   for (int zs = blockIdx.x; zs < b.sz; zs += gridDim.x) {
     T* dst = pool + b.offset + (long long)zs * plane;
-    const T* src = level + ((long long)(b.oz + zs) * Y + b.oy) * X + b.ox;
+    const long long z = min(max((long long)b.oz + zs, 0LL), Z - 1);
     for (long long i = threadIdx.x; i < plane; i += blockDim.x) {
-      long long r = i / b.sx, x = i - r * b.sx;
-      dst[i] = __ldg(src + r * X + x);
+      long long r = i / b.sx, xs = i - r * b.sx;
+      // ghosts outside the level replicate its edge voxels
+      const long long y = min(max((long long)b.oy + r, 0LL), Y - 1);
+      const long long x = min(max((long long)b.ox + xs, 0LL), X - 1);
+      dst[i] = __ldg(level + (z * Y + y) * X + x);
     }
   }
 }
@@ -171,11 +174,11 @@ cudaError_t launch_gather_bricks(const void* level, int dtype, const long long d
   dim3 grid((unsigned)(dims[2] < 256 ? dims[2] : 256), (unsigned)nbricks);
   int threads = 512;
   if (dtype == DT_U8)
-    k_gather<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], bricks_dev, (uint8_t*)pool);
+    k_gather<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], bricks_dev, (uint8_t*)pool);
   else if (dtype == DT_U16)
-    k_gather<uint16_t><<<grid, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], bricks_dev, (uint16_t*)pool);
+    k_gather<uint16_t><<<grid, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], dims[2], bricks_dev, (uint16_t*)pool);
   else
-    k_gather<float><<<grid, threads, 0, s>>>((const float*)level, dims[0], dims[1], bricks_dev, (float*)pool);
+    k_gather<float><<<grid, threads, 0, s>>>((const float*)level, dims[0], dims[1], dims[2], bricks_dev, (float*)pool);
   return cudaGetLastError();
 }
 

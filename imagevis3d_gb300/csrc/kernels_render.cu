@@ -38,10 +38,16 @@ struct VoxelTraits<float> {
   static constexpr float tex_scale = 1.0f;
 };
 
-template <typename T>
-__device__ __forceinline__ float ldv(const T* p) {
-  return (float)__ldg(p);
+// Voxel value as float.  8- and 16-bit values are placed in the mantissa of
+// 2^23 and the bias subtracted: exact, and it keeps the conversion off the
+// narrow integer-to-float pipe.
+__device__ __forceinline__ float ldv(const uint8_t* p) {
+  return __int_as_float(0x4B000000 | (unsigned)__ldg(p)) - 8388608.0f;
 }
+__device__ __forceinline__ float ldv(const uint16_t* p) {
+  return __int_as_float(0x4B000000 | (unsigned)__ldg(p)) - 8388608.0f;
+}
+__device__ __forceinline__ float ldv(const float* p) { return __ldg(p); }
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
 
@@ -65,46 +71,53 @@ __device__ __forceinline__ void load_brick(const FrameDesc& f, int bi, BrickView
   b.loz = w3.x; b.hix = w3.y; b.hiy = w3.z; b.hiz = w3.w;
 }
 
-// Value of the level at voxel-centre position p, using brick b (whose stored
-// region covers the trilinear footprint of every p whose floor lies in its
-// interior, and of p +- 1 voxel, because ghost = 2).  Clamping to the stored
-// box equals clamp-to-edge of the whole level: the box ends only at the
-// level's boundary.
+// A sample position split into its voxel cell (global integer floor) and
+// the trilinear fractions, exactly as the CPU oracle splits it.
+struct Cell {
+  int x, y, z;
+  float fx, fy, fz;
+};
+
+// Cell of a position, clamped to [-1, n-1]: positions computed in FP32 can
+// land a rounding error outside the level; clamping keeps brick lookup and
+// membership consistent (so the walk always advances) and equals the
+// clamp-to-edge rule.  NaN converts to 0.
+__device__ __forceinline__ int clamp_cell(float p, int n) { return clampi((int)floorf(p), -1, n - 1); }
+
+__device__ __forceinline__ Cell make_cell(const FrameDesc& f, float px, float py, float pz) {
+  Cell c;
+  const float x0 = floorf(px), y0 = floorf(py), z0 = floorf(pz);
+  c.fx = px - x0; c.fy = py - y0; c.fz = pz - z0;
+  c.x = clampi((int)x0, -1, f.dims[0] - 1);
+  c.y = clampi((int)y0, -1, f.dims[1] - 1);
+  c.z = clampi((int)z0, -1, f.dims[2] - 1);
+  return c;
+}
+
+// Every stored brick holds its interior plus 2 ghost voxels on every face
+// (replicated edge voxels outside the level).  A cell inside the interior,
+// shifted by up to one voxel per axis (gradient taps), keeps its whole
+// 2x2x2 trilinear footprint inside the stored box, so no clamping is needed:
+// local indices run from lo - o - 1 >= 0 to hi - o + 1 <= stored - 1.
 template <typename T, int SAMPLER>
-__device__ __forceinline__ float sample_brick(const FrameDesc& f, const BrickView& b, float px,
-                                              float py, float pz) {
+__device__ __forceinline__ float sample_cell(const FrameDesc& f, const BrickView& b, int gx, int gy, int gz, float fx,
+                                             float fy, float fz) {
+  const int ix = gx - b.ox, iy = gy - b.oy, iz = gz - b.oz;
   if (SAMPLER == SAMPLER_TEX) {
     cudaTextureObject_t tex = (cudaTextureObject_t)b.tex;
-    if (f.interp) {
-      return tex3D<float>(tex, px - (float)b.ox + 0.5f, py - (float)b.oy + 0.5f,
-                          pz - (float)b.oz + 0.5f) * VoxelTraits<T>::tex_scale;
-    }
-    int ix = clampi((int)floorf(px + 0.5f) - b.ox, 0, b.sx - 1);
-    int iy = clampi((int)floorf(py + 0.5f) - b.oy, 0, b.sy - 1);
-    int iz = clampi((int)floorf(pz + 0.5f) - b.oz, 0, b.sz - 1);
-    return tex3D<float>(tex, ix + 0.5f, iy + 0.5f, iz + 0.5f) * VoxelTraits<T>::tex_scale;
+    if (f.interp)
+      return tex3D<float>(tex, (float)ix + (fx + 0.5f), (float)iy + (fy + 0.5f), (float)iz + (fz + 0.5f)) *
+             VoxelTraits<T>::tex_scale;
+    return tex3D<float>(tex, (float)(ix + (fx >= 0.5f)) + 0.5f, (float)(iy + (fy >= 0.5f)) + 0.5f,
+                        (float)(iz + (fz >= 0.5f)) + 0.5f) * VoxelTraits<T>::tex_scale;
   }
   const T* base = reinterpret_cast<const T*>(f.pool) + (size_t)b.off;
-  if (!f.interp) {
-    int ix = clampi((int)floorf(px + 0.5f) - b.ox, 0, b.sx - 1);
-    int iy = clampi((int)floorf(py + 0.5f) - b.oy, 0, b.sy - 1);
-    int iz = clampi((int)floorf(pz + 0.5f) - b.oz, 0, b.sz - 1);
-    return ldv(base + ((size_t)iz * b.sy + iy) * b.sx + ix);
-  }
-  float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
-  float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
-  int x0 = (int)fx0 - b.ox, y0 = (int)fy0 - b.oy, z0 = (int)fz0 - b.oz;
-  int xa = clampi(x0, 0, b.sx - 1), xb = clampi(x0 + 1, 0, b.sx - 1);
-  int ya = clampi(y0, 0, b.sy - 1), yb = clampi(y0 + 1, 0, b.sy - 1);
-  int za = clampi(z0, 0, b.sz - 1), zb = clampi(z0 + 1, 0, b.sz - 1);
-  const size_t slice = (size_t)b.sx * b.sy;
-  const T* pa = base + za * slice;
-  const T* pb = base + zb * slice;
-  const int ra = ya * b.sx, rb = yb * b.sx;
-  float v000 = ldv(pa + ra + xa), v100 = ldv(pa + ra + xb);
-  float v010 = ldv(pa + rb + xa), v110 = ldv(pa + rb + xb);
-  float v001 = ldv(pb + ra + xa), v101 = ldv(pb + ra + xb);
-  float v011 = ldv(pb + rb + xa), v111 = ldv(pb + rb + xb);
+  const int row = b.sx, slice = b.sx * b.sy;
+  if (!f.interp) return ldv(base + (iz + (fz >= 0.5f)) * slice + (iy + (fy >= 0.5f)) * row + ix + (fx >= 0.5f));
+  const T* p0 = base + iz * slice + iy * row + ix;
+  const T* p1 = p0 + slice;
+  float v000 = ldv(p0), v100 = ldv(p0 + 1), v010 = ldv(p0 + row), v110 = ldv(p0 + row + 1);
+  float v001 = ldv(p1), v101 = ldv(p1 + 1), v011 = ldv(p1 + row), v111 = ldv(p1 + row + 1);
   float c00 = fmaf(fx, v100 - v000, v000);
   float c10 = fmaf(fx, v110 - v010, v010);
   float c01 = fmaf(fx, v101 - v001, v001);
@@ -121,16 +134,6 @@ __device__ __forceinline__ int brick_index(const FrameDesc& f, int gx, int gy, i
   return (bz * f.nb[1] + by) * f.nb[0] + bx;
 }
 
-// Voxel cell of a sample, clamped to [-1, n-1]: positions computed in FP32
-// can land a rounding error outside the level; clamping keeps brick lookup
-// and membership consistent (so the walk always advances), and matches the
-// clamp-to-edge sampling rule.  NaN converts to 0.
-__device__ __forceinline__ void cell(const FrameDesc& f, float px, float py, float pz, int& gx, int& gy, int& gz) {
-  gx = clampi((int)floorf(px), -1, f.dims[0] - 1);
-  gy = clampi((int)floorf(py), -1, f.dims[1] - 1);
-  gz = clampi((int)floorf(pz), -1, f.dims[2] - 1);
-}
-
 __device__ __forceinline__ bool inside(const BrickView& b, int gx, int gy, int gz) {
   return gx >= b.lox && gx < b.hix && gy >= b.loy && gy < b.hiy && gz >= b.loz && gz < b.hiz;
 }
@@ -138,22 +141,22 @@ __device__ __forceinline__ bool inside(const BrickView& b, int gx, int gy, int g
 // Sample at an arbitrary position (isosurface bisection): find its brick first.
 template <typename T, int SAMPLER>
 __device__ float sample_anywhere(const FrameDesc& f, float px, float py, float pz) {
-  int gx, gy, gz;
-  cell(f, px, py, pz, gx, gy, gz);
-  int bi = brick_index(f, gx, gy, gz);
+  Cell c = make_cell(f, px, py, pz);
   BrickView b;
-  load_brick(f, bi, b);
-  return sample_brick<T, SAMPLER>(f, b, px, py, pz);
+  load_brick(f, brick_index(f, c.x, c.y, c.z), b);
+  return sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z, c.fx, c.fy, c.fz);
 }
 
 // Central differences of the interpolated field at h = 1 voxel (data units
-// per voxel).
+// per voxel): the taps are the same fractions one cell over.
 template <typename T, int SAMPLER>
-__device__ __forceinline__ void gradient(const FrameDesc& f, const BrickView& b, float px, float py,
-                                         float pz, float g[3]) {
-  g[0] = (sample_brick<T, SAMPLER>(f, b, px + 1.f, py, pz) - sample_brick<T, SAMPLER>(f, b, px - 1.f, py, pz)) * 0.5f;
-  g[1] = (sample_brick<T, SAMPLER>(f, b, px, py + 1.f, pz) - sample_brick<T, SAMPLER>(f, b, px, py - 1.f, pz)) * 0.5f;
-  g[2] = (sample_brick<T, SAMPLER>(f, b, px, py, pz + 1.f) - sample_brick<T, SAMPLER>(f, b, px, py, pz - 1.f)) * 0.5f;
+__device__ __forceinline__ void gradient(const FrameDesc& f, const BrickView& b, const Cell& c, float g[3]) {
+  g[0] = (sample_cell<T, SAMPLER>(f, b, c.x + 1, c.y, c.z, c.fx, c.fy, c.fz) -
+          sample_cell<T, SAMPLER>(f, b, c.x - 1, c.y, c.z, c.fx, c.fy, c.fz)) * 0.5f;
+  g[1] = (sample_cell<T, SAMPLER>(f, b, c.x, c.y + 1, c.z, c.fx, c.fy, c.fz) -
+          sample_cell<T, SAMPLER>(f, b, c.x, c.y - 1, c.z, c.fx, c.fy, c.fz)) * 0.5f;
+  g[2] = (sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z + 1, c.fx, c.fy, c.fz) -
+          sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z - 1, c.fx, c.fy, c.fz)) * 0.5f;
 }
 
 // Phong, directional light, two-sided: normal = -grad/|grad| turned towards
@@ -252,61 +255,105 @@ __device__ __forceinline__ void setup_ray(const FrameDesc& f, int px, int py, Ra
   r.hit = t1 > t0 && (t1 - t0) < 4.0f;
 }
 
+struct Accum {
+  float C0, C1, C2, A;
+};
+
+// Classify one sample and composite it front to back; returns true when the
+// ray is opaque enough to stop.
+template <int MODE>
+__device__ __forceinline__ bool composite(const FrameDesc& f, float4 c, Accum& acc) {
+  float al = c.w;
+  if (f.opacity_exp != 1.f) al = 1.f - __powf(1.f - al, f.opacity_exp);
+  const float w = (1.f - acc.A) * al;
+  acc.C0 = fmaf(w, c.x, acc.C0);
+  acc.C1 = fmaf(w, c.y, acc.C1);
+  acc.C2 = fmaf(w, c.z, acc.C2);
+  acc.A += w;
+  return acc.A >= f.ert;
+}
+
 template <typename T, int MODE, int SAMPLER>
 __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) {
-  float C0 = 0.f, C1 = 0.f, C2 = 0.f, A = 0.f;
+  Accum acc = {0.f, 0.f, 0.f, 0.f};
   if (r.hit) {
     const float dt = f.dt;
     const float t0 = r.t0;
     const int K = max(0, (int)ceilf((r.t1 - t0) / dt - 0.5f));
     const float V[3] = {-r.dw[0], -r.dw[1], -r.dw[2]};
+    auto pos_of = [&](int kk, float& px, float& py, float& pz) {
+      const float t = fmaf((float)kk + 0.5f, dt, t0);
+      px = fmaf(t, r.dv[0], r.ov[0]);
+      py = fmaf(t, r.dv[1], r.ov[1]);
+      pz = fmaf(t, r.dv[2], r.ov[2]);
+    };
     int k = 0;
     bool done = false;
     while (k < K && !done) {
-      float t = fmaf((float)k + 0.5f, dt, t0);
-      float px = fmaf(t, r.dv[0], r.ov[0]), py = fmaf(t, r.dv[1], r.ov[1]), pz = fmaf(t, r.dv[2], r.ov[2]);
-      int gx, gy, gz;
-      cell(f, px, py, pz, gx, gy, gz);
-      int bi = brick_index(f, gx, gy, gz);
+      float px, py, pz;
+      pos_of(k, px, py, pz);
+      const int bi = brick_index(f, clamp_cell(px, f.dims[0]), clamp_cell(py, f.dims[1]), clamp_cell(pz, f.dims[2]));
       BrickView b;
       load_brick(f, bi, b);
+      // Samples [k, ke) of this ray lie in the brick: estimate the exit from
+      // the interior planes, then settle it with the floor(pos) rule that
+      // assigns samples to bricks.  Positions are monotone in k, so the
+      // members form one run and only its ends need checking.
+      float te = INFINITY;
+      te = fminf(te, r.dv[0] > 0.f ? ((float)b.hix - r.ov[0]) / r.dv[0]
+                                   : (r.dv[0] < 0.f ? ((float)b.lox - r.ov[0]) / r.dv[0] : INFINITY));
+      te = fminf(te, r.dv[1] > 0.f ? ((float)b.hiy - r.ov[1]) / r.dv[1]
+                                   : (r.dv[1] < 0.f ? ((float)b.loy - r.ov[1]) / r.dv[1] : INFINITY));
+      te = fminf(te, r.dv[2] > 0.f ? ((float)b.hiz - r.ov[2]) / r.dv[2]
+                                   : (r.dv[2] < 0.f ? ((float)b.loz - r.ov[2]) / r.dv[2] : INFINITY));
+      const float kef = ceilf((te - t0) / dt - 0.5f);
+      int ke = kef >= (float)K ? K : max(k + 1, (int)kef);
+      auto in_b = [&](int kk) {
+        float qx, qy, qz;
+        pos_of(kk, qx, qy, qz);
+        return inside(b, clamp_cell(qx, f.dims[0]), clamp_cell(qy, f.dims[1]), clamp_cell(qz, f.dims[2]));
+      };
+      while (ke > k + 1 && !in_b(ke - 1)) --ke;
+      while (ke < K && in_b(ke)) ++ke;
       if (__ldg(f.skip + bi)) {
-        // Jump past the brick: estimate the exit from its interior planes,
-        // then settle the boundary samples by the same floor(pos) rule that
-        // assigns samples to bricks, so no sample of a neighbour is skipped.
-        float te = INFINITY;
-        te = fminf(te, r.dv[0] > 0.f ? ((float)b.hix - r.ov[0]) / r.dv[0]
-                                     : (r.dv[0] < 0.f ? ((float)b.lox - r.ov[0]) / r.dv[0] : INFINITY));
-        te = fminf(te, r.dv[1] > 0.f ? ((float)b.hiy - r.ov[1]) / r.dv[1]
-                                     : (r.dv[1] < 0.f ? ((float)b.loy - r.ov[1]) / r.dv[1] : INFINITY));
-        te = fminf(te, r.dv[2] > 0.f ? ((float)b.hiz - r.ov[2]) / r.dv[2]
-                                     : (r.dv[2] < 0.f ? ((float)b.loz - r.ov[2]) / r.dv[2] : INFINITY));
-        float kef = ceilf((te - t0) / dt - 0.5f);
-        int ke = kef >= (float)K ? K : max(k + 1, (int)kef);
-        auto in_b = [&](int kk) {
-          float tt = fmaf((float)kk + 0.5f, dt, t0);
-          int cx, cy, cz;
-          cell(f, fmaf(tt, r.dv[0], r.ov[0]), fmaf(tt, r.dv[1], r.ov[1]), fmaf(tt, r.dv[2], r.ov[2]), cx, cy, cz);
-          return inside(b, cx, cy, cz);
-        };
-        while (ke > k + 1 && !in_b(ke - 1)) --ke;
-        while (ke < K && in_b(ke)) ++ke;
         k = ke;
         continue;
       }
       if (f.touched) f.touched[bi] = 1;
-      for (; k < K; ++k) {
-        t = fmaf((float)k + 0.5f, dt, t0);
-        px = fmaf(t, r.dv[0], r.ov[0]);
-        py = fmaf(t, r.dv[1], r.ov[1]);
-        pz = fmaf(t, r.dv[2], r.ov[2]);
-        cell(f, px, py, pz, gx, gy, gz);
-        if (!inside(b, gx, gy, gz)) break;
-        float v = sample_brick<T, SAMPLER>(f, b, px, py, pz);
+      if (MODE == MODE_1D) {
+        // two samples per iteration: both footprints are fetched before
+        // either is composited
+        for (; k + 1 < ke; k += 2) {
+          float ax, ay, az, bx, by, bz;
+          pos_of(k, ax, ay, az);
+          pos_of(k + 1, bx, by, bz);
+          const Cell ca = make_cell(f, ax, ay, az), cb = make_cell(f, bx, by, bz);
+          const float va = sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz);
+          const float vb = sample_cell<T, SAMPLER>(f, b, cb.x, cb.y, cb.z, cb.fx, cb.fy, cb.fz);
+          ++nsamp;
+          if (composite<MODE>(f, tf1d(f, va), acc)) { done = true; break; }
+          ++nsamp;
+          if (composite<MODE>(f, tf1d(f, vb), acc)) { done = true; break; }
+        }
+        if (!done && k < ke) {
+          float ax, ay, az;
+          pos_of(k, ax, ay, az);
+          const Cell ca = make_cell(f, ax, ay, az);
+          ++nsamp;
+          if (composite<MODE>(f, tf1d(f, sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz)), acc))
+            done = true;
+          ++k;
+        }
+        continue;
+      }
+      for (; k < ke; ++k) {
+        pos_of(k, px, py, pz);
+        const Cell c = make_cell(f, px, py, pz);
+        const float v = sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z, c.fx, c.fy, c.fz);
         ++nsamp;
         if (MODE == MODE_ISO) {
           if (v >= f.iso) {
-            float tl = k == 0 ? t0 : fmaf((float)k - 0.5f, dt, t0), th = t;
+            float tl = k == 0 ? t0 : fmaf((float)k - 0.5f, dt, t0), th = fmaf((float)k + 0.5f, dt, t0);
 #pragma unroll 1
             for (int it = 0; it < 4; ++it) {
               float tm = 0.5f * (tl + th);
@@ -316,53 +363,41 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
               else tl = tm;
             }
             float th2 = 0.5f * (tl + th);
-            float hx = fmaf(th2, r.dv[0], r.ov[0]), hy = fmaf(th2, r.dv[1], r.ov[1]), hz = fmaf(th2, r.dv[2], r.ov[2]);
+            const Cell hc = make_cell(f, fmaf(th2, r.dv[0], r.ov[0]), fmaf(th2, r.dv[1], r.ov[1]),
+                                      fmaf(th2, r.dv[2], r.ov[2]));
             BrickView hb;
-            int hx0, hy0, hz0;
-            cell(f, hx, hy, hz, hx0, hy0, hz0);
-            load_brick(f, brick_index(f, hx0, hy0, hz0), hb);
+            load_brick(f, brick_index(f, hc.x, hc.y, hc.z), hb);
             float g[3], col[3];
-            gradient<T, SAMPLER>(f, hb, hx, hy, hz, g);
+            gradient<T, SAMPLER>(f, hb, hc, g);
             g[0] *= f.vox_scale[0];
             g[1] *= f.vox_scale[1];
             g[2] *= f.vox_scale[2];
             if (f.lighting) shade(f, g, V, f.iso_rgb, col);
             else { col[0] = f.iso_rgb[0]; col[1] = f.iso_rgb[1]; col[2] = f.iso_rgb[2]; }
-            C0 = col[0]; C1 = col[1]; C2 = col[2];
-            A = 1.f;
+            acc.C0 = col[0]; acc.C1 = col[1]; acc.C2 = col[2];
+            acc.A = 1.f;
             done = true;
             break;
           }
           continue;
         }
-        float4 c;
-        if (MODE == MODE_1D) {
-          c = tf1d(f, v);
-        } else {
-          float g[3];
-          gradient<T, SAMPLER>(f, b, px, py, pz, g);
-          float gm = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-          c = tf2d(f, v, gm);
-          if (f.lighting && c.w > 0.f) {
-            float gw[3] = {g[0] * f.vox_scale[0], g[1] * f.vox_scale[1], g[2] * f.vox_scale[2]};
-            float col[3] = {c.x, c.y, c.z}, lit[3];
-            shade(f, gw, V, col, lit);
-            c.x = lit[0]; c.y = lit[1]; c.z = lit[2];
-          }
+        // 2D transfer function over (value, |gradient|), Phong lit
+        float g[3];
+        gradient<T, SAMPLER>(f, b, c, g);
+        const float gm = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        float4 cl = tf2d(f, v, gm);
+        if (f.lighting && cl.w > 0.f) {
+          float gw[3] = {g[0] * f.vox_scale[0], g[1] * f.vox_scale[1], g[2] * f.vox_scale[2]};
+          float col[3] = {cl.x, cl.y, cl.z}, lit[3];
+          shade(f, gw, V, col, lit);
+          cl.x = lit[0]; cl.y = lit[1]; cl.z = lit[2];
         }
-        float al = c.w;
-        if (f.opacity_exp != 1.f) al = 1.f - __powf(1.f - al, f.opacity_exp);
-        float w = (1.f - A) * al;
-        C0 = fmaf(w, c.x, C0);
-        C1 = fmaf(w, c.y, C1);
-        C2 = fmaf(w, c.z, C2);
-        A += w;
-        if (A >= f.ert) { done = true; break; }
+        if (composite<MODE>(f, cl, acc)) { done = true; break; }
       }
     }
   }
-  float rem = 1.f - A;
-  return make_float4(fmaf(rem, f.bg[0], C0), fmaf(rem, f.bg[1], C1), fmaf(rem, f.bg[2], C2), A);
+  const float rem = 1.f - acc.A;
+  return make_float4(fmaf(rem, f.bg[0], acc.C0), fmaf(rem, f.bg[1], acc.C1), fmaf(rem, f.bg[2], acc.C2), acc.A);
 }
 
 template <typename T, int MODE, int SAMPLER>
@@ -393,7 +428,7 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
 constexpr int RENDER_THREADS = 128;
 
 template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS) k_render_plain(const __grid_constant__ FrameDesc f) {
+__global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_plain(const __grid_constant__ FrameDesc f) {
   int warp = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (warp >= f.tiles_x * f.tiles_y) return;
   render_tile<T, MODE, SAMPLER>(f, warp);
@@ -411,7 +446,7 @@ __device__ __forceinline__ int find_frame(const int* __restrict__ prefix, int nf
 }
 
 template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS) k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
+__global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
                                                          const int* __restrict__ tile_prefix, int total,
                                                          int* __restrict__ counter) {
   const int lane = threadIdx.x & 31;

@@ -104,16 +104,19 @@ int orc_lod_dims(const i64 dims[3], int brick, int ghost, int max_lods, i64* out
   return count;
 }
 
-// A level is a single brick without ghosts when its largest axis fits the
-// brick interior (c60.uvf: 128^3 in a 256-brick with overlap 4 stores exactly
-// 128^3 voxels).  Otherwise it is a grid of interior-sized bricks, each stored
-// with `ghost` voxels of its neighbours on every face that has a neighbour.
+// A level is a single brick when its largest axis fits the brick interior
+// (brick - 2*ghost; c60.uvf: 128^3 in a 256-brick with overlap 4 is one
+// brick).  Otherwise it is a grid of interior-sized bricks.  Every stored
+// brick carries `ghost` voxels on every face: copies of the neighbouring
+// brick's voxels inside the level, and replicated edge voxels (clamp to edge)
+// outside it, so a stored brick is (interior + 2 ghost)^3 voxels with its
+// origin at interior_start - ghost.
 void orc_brick_grid(const i64 dims[3], int brick, int ghost, i64 nb[3], i64* interior) {
   i64 I = brick - 2 * ghost;
   i64 mx = std::max(dims[0], std::max(dims[1], dims[2]));
   if (mx <= I) {
     nb[0] = nb[1] = nb[2] = 1;
-    *interior = mx;
+    *interior = std::max<i64>(mx, 1);
     return;
   }
   for (int a = 0; a < 3; ++a) nb[a] = (dims[a] + I - 1) / I;
@@ -125,15 +128,9 @@ void orc_brick_extent(const i64 dims[3], int brick, int ghost, const i64 b[3],
   i64 nb[3], I;
   orc_brick_grid(dims, brick, ghost, nb, &I);
   for (int a = 0; a < 3; ++a) {
-    if (nb[0] * nb[1] * nb[2] == 1) {
-      origin[a] = 0;
-      sdims[a] = dims[a];
-      continue;
-    }
-    i64 lo = std::max<i64>(b[a] * I - ghost, 0);
-    i64 hi = std::min<i64>((b[a] + 1) * I + ghost, dims[a]);
-    origin[a] = lo;
-    sdims[a] = hi - lo;
+    i64 ilo = b[a] * I, ihi = std::min<i64>(ilo + I, dims[a]);
+    origin[a] = ilo - ghost;
+    sdims[a] = ihi - ilo + 2 * ghost;
   }
 }
 
@@ -142,12 +139,13 @@ void orc_extract_brick(const void* vol, int dt, const i64 dims[3], int brick, in
   i64 o[3], s[3];
   orc_brick_extent(dims, brick, ghost, b, o, s);
   size_t es = dt_size(dt);
+  auto cl = [](i64 v, i64 n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); };
   for (i64 z = 0; z < s[2]; ++z)
-    for (i64 y = 0; y < s[1]; ++y) {
-      const char* src = (const char*)vol + (((o[2] + z) * dims[1] + (o[1] + y)) * dims[0] + o[0]) * es;
-      char* dst = (char*)out + ((z * s[1] + y) * s[0]) * es;
-      memcpy(dst, src, s[0] * es);
-    }
+    for (i64 y = 0; y < s[1]; ++y)
+      for (i64 x = 0; x < s[0]; ++x) {
+        i64 src = (cl(o[2] + z, dims[2]) * dims[1] + cl(o[1] + y, dims[1])) * dims[0] + cl(o[0] + x, dims[0]);
+        memcpy((char*)out + ((z * s[1] + y) * s[0] + x) * es, (const char*)vol + src * es, es);
+      }
 }
 
 // 2x2x2 average: each output voxel averages the children that exist (1..8 at

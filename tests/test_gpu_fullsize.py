@@ -42,11 +42,14 @@ def test_bricks_tile_the_volume_with_exact_ghosts(c2):
     wl, vol, r = c2
     mm = r.brickMinMax(0)
     rng = np.random.default_rng(7)
-    for _ in range(6):
-        b = tuple(int(x) for x in rng.integers(0, 5, 3))
+    picks = [(0, 0, 0), (4, 4, 4)] + [tuple(int(x) for x in rng.integers(0, 5, 3)) for _ in range(4)]
+    for b in picks:
         data, o = r.getBrick(0, b)
-        sl = vol[o[2]:o[2] + data.shape[0], o[1]:o[1] + data.shape[1], o[0]:o[0] + data.shape[2]]
-        assert np.array_equal(data, sl)
+        # stored box = interior + 2 ghosts per face, edge voxels replicated
+        zi = np.clip(np.arange(o[2], o[2] + data.shape[0]), 0, 1023)
+        yi = np.clip(np.arange(o[1], o[1] + data.shape[1]), 0, 1023)
+        xi = np.clip(np.arange(o[0], o[0] + data.shape[2]), 0, 1023)
+        assert np.array_equal(data, vol[np.ix_(zi, yi, xi)])
         i = (b[2] * 5 + b[1]) * 5 + b[0]
         assert mm[i, 0] == data.min() and mm[i, 1] == data.max()
 

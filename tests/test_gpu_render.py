@@ -188,10 +188,9 @@ def test_2d_tf_with_lighting_matches_oracle(orc, multibrick):
     assert ref[..., 3].max() > 0.2
 
 
-@pytest.mark.parametrize("q", [99.0, 99.7, 99.95])
-def test_isosurface_matches_oracle(orc, multibrick, q):
+@pytest.mark.parametrize("iso", [1000.0, 1300.0, 1600.0])
+def test_isosurface_matches_oracle(orc, multibrick, iso):
     vol, _, _ = multibrick
-    iso = float(np.percentile(vol, q))
     view, proj = orbit_camera(120.0, 10.0, 2.5 * workloads.DIAG, 45.0, 160, 120)
     with Renderer(float_fb=True) as r:
         r.loadVolume(vol, brick_size=64, overlap=2)
@@ -207,7 +206,7 @@ def test_isosurface_matches_oracle(orc, multibrick, q):
     assert (hit_g != hit_r).mean() < 0.002
     both = hit_g & hit_r
     assert_close(img[both], ref[both])
-    assert hit_r.mean() > 0.002
+    assert hit_r.mean() > 0.003
 
 
 def test_texture_sampler_matches_oracle(orc, multibrick):

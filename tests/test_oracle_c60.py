@@ -54,19 +54,20 @@ def test_brick_grid_and_ghosts(orc):
     vol = rng.integers(0, 4096, (70, 90, 130), dtype=np.uint16)  # z, y, x
     nb, interior = orc.brick_grid((130, 90, 70), 32, 2)
     assert interior == 28 and nb == (5, 4, 3)
+    padded = np.pad(vol, 2, mode="edge")  # clamp-to-edge ghosts outside the level
     for b in [(0, 0, 0), (4, 3, 2), (2, 1, 1)]:
         data, o = orc.extract_brick(vol, 32, 2, b)
-        z0, y0, x0 = o[2], o[1], o[0]
-        assert np.array_equal(data, vol[z0:z0 + data.shape[0], y0:y0 + data.shape[1], x0:x0 + data.shape[2]])
-        # stored box = interior + 2 ghosts where a neighbour exists
         for a, n in zip(range(3), (130, 90, 70)):
             lo = b[a] * 28
             hi = min(lo + 28, n)
-            assert o[a] == max(lo - 2, 0)
-            assert o[a] + data.shape[2 - a] == min(hi + 2, n)
-    # single-brick level: no ghosts
-    data, o = orc.extract_brick(vol[:20, :20, :20].copy(), 32, 2, (0, 0, 0))
-    assert data.shape == (20, 20, 20) and o == (0, 0, 0)
+            assert o[a] == lo - 2 and data.shape[2 - a] == hi - lo + 4
+        z0, y0, x0 = o[2] + 2, o[1] + 2, o[0] + 2
+        assert np.array_equal(data, padded[z0:z0 + data.shape[0], y0:y0 + data.shape[1], x0:x0 + data.shape[2]])
+    # single-brick level: the whole level plus replicated ghosts
+    small = vol[:20, :20, :20].copy()
+    data, o = orc.extract_brick(small, 32, 2, (0, 0, 0))
+    assert data.shape == (24, 24, 24) and o == (-2, -2, -2)
+    assert np.array_equal(data, np.pad(small, 2, mode="edge"))
 
 
 def test_downsample_rule(orc):

@@ -25,7 +25,8 @@ ERRORS = {
 
 class BrickParams(C.Structure):
     _fields_ = [("brick_size", C.c_int32), ("overlap", C.c_int32), ("max_lods", C.c_int32),
-                ("build_texture", C.c_int32), ("aspect", C.c_double * 3)]
+                ("build_texture", C.c_int32), ("layouts", C.c_int32), ("reserved", C.c_int32),
+                ("aspect", C.c_double * 3)]
 
 
 class DatasetInfo(C.Structure):
@@ -47,6 +48,11 @@ class Stats(C.Structure):
                 ("brick_misses", C.c_uint64), ("bytes_paged", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("lod", C.c_int32), ("subframes", C.c_int32), ("gpu_ms", C.c_double),
                 ("kernel_ms", C.c_double)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("tile_w", C.c_int32), ("ctas_per_sm", C.c_int32), ("candidates", C.c_int32),
+                ("best_ms", C.c_float), ("default_ms", C.c_float)]
 
 
 class SynthParams(C.Structure):
@@ -107,6 +113,8 @@ SIGNATURES = {
     "gbvr_set_view": [P, FP, FP],
     "gbvr_set_background": [P, FP, FP],
     "gbvr_set_early_termination": [P, F],
+    "gbvr_set_launch_shape": [P, I, I],
+    "gbvr_autotune": [P, C.POINTER(View), I, C.POINTER(TuneResult)],
     "gbvr_paint": [P],
     "gbvr_paint_batch": [P, C.POINTER(View), I],
     "gbvr_paint_views": [P, C.POINTER(View), I],

@@ -202,6 +202,8 @@ struct Dataset {
   long long dims[3] = {0, 0, 0};
   double aspect[3] = {1, 1, 1};
   int brick = 256, ghost = 2;
+  int layouts = 1;
+  unsigned long long copy_stride = 0;  // elements between layout copies
   std::vector<Level> levels;
   std::vector<BrickInfo> bricks;
   DevBuf pool, d_bricks;
@@ -361,13 +363,17 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   }
   ds.stored_bytes = 0;
   for (auto& b : ds.bricks) ds.stored_bytes += (uint64_t)b.sx * b.sy * b.sz * es;
-  CUDA_TRY(ds.pool.alloc(cursor * es));
+  ds.layouts = (bp && bp->layouts == 3) ? 3 : 1;
+  ds.copy_stride = cursor;
+  CUDA_TRY(ds.pool.alloc(cursor * es * ds.layouts));
   CUDA_TRY(ds.d_bricks.alloc(sizeof(BrickInfo) * ds.bricks.size()));
   CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyHostToDevice, s));
   for (size_t l = 0; l < ld.size(); ++l) {
     const Level& L = ds.levels[l];
     long long d[3] = {ld[l][0], ld[l][1], ld[l][2]};
-    CUDA_TRY(launch_gather_bricks(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks, ds.pool.p, s));
+    for (int perm = 0; perm < ds.layouts; ++perm)
+      CUDA_TRY(launch_gather_bricks(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks,
+                                    (char*)ds.pool.p + (size_t)perm * cursor * es, perm, s));
   }
   CUDA_TRY(launch_brick_minmax(ds.pool.p, dtype, ds.d_bricks.as<BrickInfo>(), (int)ds.bricks.size(), s));
   CUDA_TRY(cudaMemcpyAsync(ds.bricks.data(), ds.d_bricks.p, sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyDeviceToHost, s));
@@ -457,6 +463,7 @@ struct gbvr_renderer {
   float view[16], proj[16];
   float bg_top[3] = {0, 0, 0}, bg_bot[3] = {0, 0, 0};
   float ert = 0.99f;
+  int tile_w = TILE_W, ctas_per_sm = 0;
   // device state
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
@@ -468,15 +475,15 @@ struct gbvr_renderer {
   int last_views = 0, last_level = 0;
   float last_ms = 0.f, last_kernel_ms = 0.f;
   uint64_t last_h2d = 0;
-  int grid = 0;
+  int max_ctas_per_sm = 0, sm_count = 0;
   // graph cache for the batch launch
   struct GraphKey {
-    int n, w, h, level, dtype, mode, sampler;
+    int n, w, h, level, dtype, mode, sampler, grid;
     void* fb8;
     void* fb32;
     bool operator<(const GraphKey& o) const {
-      return std::tie(n, w, h, level, dtype, mode, sampler, fb8, fb32) <
-             std::tie(o.n, o.w, o.h, o.level, o.dtype, o.mode, o.sampler, o.fb8, o.fb32);
+      return std::tie(n, w, h, level, dtype, mode, sampler, grid, fb8, fb32) <
+             std::tie(o.n, o.w, o.h, o.level, o.dtype, o.mode, o.sampler, o.grid, o.fb8, o.fb32);
     }
   };
   std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -633,8 +640,20 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
   for (int k = 0; k < 3; ++k) f.light_to[k] = ll > 0 ? (float)(-ld[k] / ll) : 0.f;
   f.width = r->width;
   f.height = r->height;
-  f.tiles_x = (r->width + TILE_W - 1) / TILE_W;
-  f.tiles_y = (r->height + TILE_H - 1) / TILE_H;
+  f.tile_w = r->tile_w;
+  f.tiles_x = (r->width + r->tile_w - 1) / r->tile_w;
+  f.tiles_y = (r->height + 32 / r->tile_w - 1) / (32 / r->tile_w);
+  // layout copy: the axis whose voxel-space extent along screen x is largest
+  // (row 0 of the view matrix is the camera's right vector in world space)
+  f.perm = 0;
+  if (ds.layouts == 3) {
+    double best = -1;
+    for (int a = 0; a < 3; ++a) {
+      double w = std::fabs((double)view[a] * f.vox_scale[a]);
+      if (w > best) { best = w; f.perm = a; }
+    }
+  }
+  f.copy_off = (unsigned long long)f.perm * ds.copy_stride;
   const size_t npix = (size_t)r->width * r->height;
   f.out_rgba8 = r->d_fb8.as<uchar4>() + (size_t)vidx * npix;
   f.out_f32 = r->d_fb32.p ? r->d_fb32.as<float4>() + (size_t)vidx * npix : nullptr;
@@ -725,12 +744,16 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   }
   hp[n] = total;
   if (PtrSnapshot(r) != before) r->drop_graphs();
-  if (!r->grid) {
+  if (!r->sm_count) {
     int dev = 0;
     cudaGetDevice(&dev);
-    r->grid = persistent_grid_size(dev);
+    cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    r->max_ctas_per_sm = persistent_grid_size(dev) / std::max(r->sm_count, 1);
+    if (r->max_ctas_per_sm < 1) r->max_ctas_per_sm = 1;
   }
-  gbvr_renderer::GraphKey key{n, r->width, r->height, level, r->ds.dtype, r->mode, r->sampler, r->d_fb8.p, r->d_fb32.p};
+  const int per_sm = r->ctas_per_sm > 0 ? std::min(r->ctas_per_sm, r->max_ctas_per_sm) : r->max_ctas_per_sm;
+  const int grid = r->sm_count * per_sm;
+  gbvr_renderer::GraphKey key{n, r->width, r->height, level, r->ds.dtype, r->mode, r->sampler, grid, r->d_fb8.p, r->d_fb32.p};
   auto it = r->graphs.find(key);
   if (it == r->graphs.end()) {
     // The graph holds the persistent launch; descriptor uploads and counter
@@ -740,7 +763,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     (void)cudaGetLastError();
     CUDA_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t le = launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), n,
-                                                    r->d_prefix.as<int>(), total, r->d_counter.as<int>(), r->grid,
+                                                    r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid,
                                                     r->stream);
     cudaError_t ce = cudaStreamEndCapture(r->stream, &g);
     if (le != cudaSuccess) return cuda_fail(le, "persistent launch capture");
@@ -1178,6 +1201,45 @@ int gbvr_set_early_termination(gbvr_renderer* r, float alpha) {
   TRY(check_r(r));
   if (!(alpha > 0.f && alpha <= 1.0f)) return fail(GBVR_EINVAL, "termination alpha must be in (0, 1]");
   r->ert = alpha;
+  return GBVR_OK;
+}
+
+int gbvr_set_launch_shape(gbvr_renderer* r, int tile_w, int ctas_per_sm) {
+  TRY(check_r(r));
+  if (tile_w != 4 && tile_w != 8 && tile_w != 16 && tile_w != 32) return fail(GBVR_EINVAL, "tile_w must be 4, 8, 16 or 32");
+  if (ctas_per_sm < 0 || ctas_per_sm > 64) return fail(GBVR_EINVAL, "bad ctas_per_sm");
+  r->tile_w = tile_w;
+  r->ctas_per_sm = ctas_per_sm;
+  return GBVR_OK;
+}
+
+int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_result* out) {
+  TRY(check_loaded(r));
+  if (!views || n <= 0) return fail(GBVR_EINVAL, "no tuning views");
+  const int tiles[] = {4, 8, 16, 32};
+  const int ctas[] = {0, 4, 6};
+  float best = INFINITY, def = INFINITY;
+  int bt = 8, bc = 0, count = 0;
+  for (int tw : tiles)
+    for (int c : ctas) {
+      r->tile_w = tw;
+      r->ctas_per_sm = c;
+      TRY(paint_batch(r, views, n));  // warm-up (and graph instantiation)
+      TRY(paint_batch(r, views, n));
+      float ms = r->last_kernel_ms;
+      ++count;
+      if (tw == TILE_W && c == 0) def = ms;
+      if (ms < best) { best = ms; bt = tw; bc = c; }
+    }
+  r->tile_w = bt;
+  r->ctas_per_sm = bc;
+  if (out) {
+    out->tile_w = bt;
+    out->ctas_per_sm = bc;
+    out->candidates = count;
+    out->best_ms = best;
+    out->default_ms = def;
+  }
   return GBVR_OK;
 }
 

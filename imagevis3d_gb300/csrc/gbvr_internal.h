@@ -30,6 +30,9 @@ struct __align__(16) BrickInfo {
   int lox, loy, loz;          // interior [lo, hi): a sample whose floor(pos) lies
   int hix, hiy, hiz;          //   here is taken from this brick (lo = -1 on the low face)
   float vmin, vmax;           // over the stored voxels, ghosts included
+  // Layout copies: the pool may hold the same bricks up to three times, with
+  // x, y or z as the fastest axis; a view samples the copy whose fastest
+  // axis is closest to its screen x axis so a warp's rays coalesce.
   int level;
   int pad;
 };
@@ -76,6 +79,9 @@ struct __align__(16) FrameDesc {
   float inv_vp[16];          // row-major inverse of proj*view
   int width, height;
   int tiles_x, tiles_y;
+  int tile_w;                // ray tile of one warp: tile_w x (32 / tile_w) pixels
+  int perm;                  // brick layout copy: 0 x-fastest, 1 y-fastest, 2 z-fastest
+  unsigned long long copy_off;  // element offset of that copy in the pool
   // outputs
   uchar4* out_rgba8;         // may be null
   float4* out_f32;           // may be null
@@ -83,9 +89,8 @@ struct __align__(16) FrameDesc {
   unsigned char* touched;    // per-frame flag per brick of the rendered level
 };
 
-// Ray tile handled by one warp: 8 x 4 pixels.
+// Default ray tile handled by one warp: 8 x 4 pixels.
 constexpr int TILE_W = 8;
-constexpr int TILE_H = 4;
 
 // ---- launch wrappers (kernels_render.cu) ----
 cudaError_t launch_classify(const BrickInfo* bricks, int nbricks, const float4* tf, int tf_w,
@@ -116,9 +121,10 @@ cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], 
                                cudaStream_t s);
 cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3], void* out,
                               cudaStream_t s);
+// perm: 0 stores x fastest, 1 y fastest (then z, x), 2 z fastest (then x, y)
 cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3],
                                  const BrickInfo* bricks_dev, int nbricks, void* pool,
-                                 cudaStream_t s);
+                                 int perm, cudaStream_t s);
 cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_dev, int nbricks,
                                 cudaStream_t s);
 cudaError_t launch_hist1d(const void* vol, int dtype, long long n, unsigned long long* hist,

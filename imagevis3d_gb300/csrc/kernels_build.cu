@@ -151,34 +151,39 @@ cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3]
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void k_gather(const T* __restrict__ level, long long X, long long Y, long long Z,
-                         const BrickInfo* __restrict__ bricks, T* __restrict__ pool) {
+                         const BrickInfo* __restrict__ bricks, T* __restrict__ pool, int perm) {
   const BrickInfo b = bricks[blockIdx.y];
   const long long plane = (long long)b.sx * b.sy;
+  // destination strides of x, y, z in this layout copy
+  long long s0, s1, s2;
+  if (perm == 0) { s0 = 1; s1 = b.sx; s2 = (long long)b.sx * b.sy; }
+  else if (perm == 1) { s1 = 1; s2 = b.sy; s0 = (long long)b.sy * b.sz; }
+  else { s2 = 1; s0 = b.sz; s1 = (long long)b.sz * b.sx; }
   for (int zs = blockIdx.x; zs < b.sz; zs += gridDim.x) {
-    T* dst = pool + b.offset + (long long)zs * plane;
+    T* dst = pool + b.offset + zs * s2;
     const long long z = min(max((long long)b.oz + zs, 0LL), Z - 1);
     for (long long i = threadIdx.x; i < plane; i += blockDim.x) {
       long long r = i / b.sx, xs = i - r * b.sx;
       // ghosts outside the level replicate its edge voxels
       const long long y = min(max((long long)b.oy + r, 0LL), Y - 1);
       const long long x = min(max((long long)b.ox + xs, 0LL), X - 1);
-      dst[i] = __ldg(level + (z * Y + y) * X + x);
+      dst[xs * s0 + r * s1] = __ldg(level + (z * Y + y) * X + x);
     }
   }
 }
 
 cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3], const BrickInfo* bricks_dev,
-                                 int nbricks, void* pool, cudaStream_t s) {
+                                 int nbricks, void* pool, int perm, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (nbricks <= 0) return cudaSuccess;
   dim3 grid((unsigned)(dims[2] < 256 ? dims[2] : 256), (unsigned)nbricks);
   int threads = 512;
   if (dtype == DT_U8)
-    k_gather<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], bricks_dev, (uint8_t*)pool);
+    k_gather<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], bricks_dev, (uint8_t*)pool, perm);
   else if (dtype == DT_U16)
-    k_gather<uint16_t><<<grid, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], dims[2], bricks_dev, (uint16_t*)pool);
+    k_gather<uint16_t><<<grid, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], dims[2], bricks_dev, (uint16_t*)pool, perm);
   else
-    k_gather<float><<<grid, threads, 0, s>>>((const float*)level, dims[0], dims[1], dims[2], bricks_dev, (float*)pool);
+    k_gather<float><<<grid, threads, 0, s>>>((const float*)level, dims[0], dims[1], dims[2], bricks_dev, (float*)pool, perm);
   return cudaGetLastError();
 }
 

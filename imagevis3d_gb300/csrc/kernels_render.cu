@@ -111,13 +111,18 @@ __device__ __forceinline__ float sample_cell(const FrameDesc& f, const BrickView
     return tex3D<float>(tex, (float)(ix + (fx >= 0.5f)) + 0.5f, (float)(iy + (fy >= 0.5f)) + 0.5f,
                         (float)(iz + (fz >= 0.5f)) + 0.5f) * VoxelTraits<T>::tex_scale;
   }
-  const T* base = reinterpret_cast<const T*>(f.pool) + (size_t)b.off;
-  const int row = b.sx, slice = b.sx * b.sy;
-  if (!f.interp) return ldv(base + (iz + (fz >= 0.5f)) * slice + (iy + (fy >= 0.5f)) * row + ix + (fx >= 0.5f));
-  const T* p0 = base + iz * slice + iy * row + ix;
-  const T* p1 = p0 + slice;
-  float v000 = ldv(p0), v100 = ldv(p0 + 1), v010 = ldv(p0 + row), v110 = ldv(p0 + row + 1);
-  float v001 = ldv(p1), v101 = ldv(p1 + 1), v011 = ldv(p1 + row), v111 = ldv(p1 + row + 1);
+  const T* base = reinterpret_cast<const T*>(f.pool) + f.copy_off + (size_t)b.off;
+  // element strides of the x, y, z axes in the selected layout copy
+  int s0, s1, s2;
+  if (f.perm == 0) { s0 = 1; s1 = b.sx; s2 = b.sx * b.sy; }
+  else if (f.perm == 1) { s1 = 1; s2 = b.sy; s0 = b.sy * b.sz; }
+  else { s2 = 1; s0 = b.sz; s1 = b.sz * b.sx; }
+  if (!f.interp)
+    return ldv(base + (iz + (fz >= 0.5f)) * s2 + (iy + (fy >= 0.5f)) * s1 + (ix + (fx >= 0.5f)) * s0);
+  const T* p0 = base + iz * s2 + iy * s1 + ix * s0;
+  const T* p1 = p0 + s2;
+  float v000 = ldv(p0), v100 = ldv(p0 + s0), v010 = ldv(p0 + s1), v110 = ldv(p0 + s1 + s0);
+  float v001 = ldv(p1), v101 = ldv(p1 + s0), v011 = ldv(p1 + s1), v111 = ldv(p1 + s1 + s0);
   float c00 = fmaf(fx, v100 - v000, v000);
   float c10 = fmaf(fx, v110 - v010, v010);
   float c01 = fmaf(fx, v101 - v001, v001);
@@ -404,8 +409,8 @@ template <typename T, int MODE, int SAMPLER>
 __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
   const int lane = threadIdx.x & 31;
   const int tx = tile % f.tiles_x, ty = tile / f.tiles_x;
-  const int px = tx * TILE_W + (lane & (TILE_W - 1));
-  const int py = ty * TILE_H + (lane / TILE_W);
+  const int px = tx * f.tile_w + (lane & (f.tile_w - 1));
+  const int py = ty * (32 / f.tile_w) + (lane / f.tile_w);
   unsigned nsamp = 0;
   if (px < f.width && py < f.height) {
     RaySetup r;

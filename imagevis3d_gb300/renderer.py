@@ -22,12 +22,14 @@ def _fp(a):
     return a, a.ctypes.data_as(L.FP)
 
 
-def brick_params(brick_size=256, overlap=2, max_lods=0, build_texture=False, aspect=(1, 1, 1)):
+def brick_params(brick_size=256, overlap=2, max_lods=0, build_texture=False, layouts=1,
+                 aspect=(1, 1, 1)):
     bp = L.BrickParams()
     bp.brick_size = brick_size
     bp.overlap = overlap
     bp.max_lods = max_lods
     bp.build_texture = 1 if build_texture else 0
+    bp.layouts = layouts
     for i in range(3):
         bp.aspect[i] = aspect[i]
     return bp
@@ -214,6 +216,15 @@ class Renderer:
 
     def setEarlyTermination(self, alpha):
         L.call("gbvr_set_early_termination", self._h, alpha)
+
+    def setLaunchShape(self, tile_w=8, ctas_per_sm=0):
+        L.call("gbvr_set_launch_shape", self._h, tile_w, ctas_per_sm)
+
+    def autotune(self, views):
+        arr = self._views(views)
+        res = L.TuneResult()
+        L.call("gbvr_autotune", self._h, arr, len(views), C.byref(res))
+        return {k: getattr(res, k) for k, _ in L.TuneResult._fields_}
 
     # -- paint / readback ---------------------------------------------------
     def paint(self):

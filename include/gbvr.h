@@ -81,6 +81,10 @@ typedef struct gbvr_brick_params {
                            CmdLineConverter/main.cpp:145) */
   int32_t max_lods;     /* 0 = halve until one brick holds the level */
   int32_t build_texture;/* also build 3D textures for GBVR_SAMPLER_TEX */
+  int32_t layouts;      /* 1: bricks stored x-fastest only; 3: also y- and z-fastest
+                           copies (3x device memory), each view samples the copy
+                           whose fastest axis is closest to its screen x axis */
+  int32_t reserved;
   double aspect[3];     /* voxel spacing; 0 = (1,1,1) */
 } gbvr_brick_params;
 
@@ -176,6 +180,24 @@ int gbvr_set_lod_limits(gbvr_renderer* r, int min_lod, int max_lod);      /* set
 int gbvr_set_view(gbvr_renderer* r, const float view[16], const float proj[16]); /* setRotation4x4/... */
 int gbvr_set_background(gbvr_renderer* r, const float top[3], const float bottom[3]); /* setBGColors */
 int gbvr_set_early_termination(gbvr_renderer* r, float alpha);           /* 0.99 by default */
+/* Launch shape of the raycast kernels: a warp renders tile_w x (32 / tile_w)
+ * pixels (tile_w in 4, 8, 16, 32); ctas_per_sm sizes the persistent grid as
+ * SMs x ctas_per_sm (0 = as many as fit).  No counterpart in the reference
+ * (GL rasterisation chose its own fragment order). */
+int gbvr_set_launch_shape(gbvr_renderer* r, int tile_w, int ctas_per_sm);
+
+typedef struct gbvr_tune_result {
+  int32_t tile_w;
+  int32_t ctas_per_sm;
+  int32_t candidates;
+  float best_ms;        /* kernel time of the chosen shape on the tuning batch */
+  float default_ms;     /* kernel time of the default shape (8, 0) */
+} gbvr_tune_result;
+
+/* Autotuner: times every candidate launch shape on `views` with the batched
+ * kernel (after one warm-up each), keeps the fastest and returns the result.
+ * The frame content does not depend on the shape (rays are independent). */
+int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_result* out);
 
 /* ---- paint ----
  * gbvr_paint replaces renderer.paint() (BatchRenderer.lua:35,

@@ -39,7 +39,9 @@ def test_c60_build_bit_exact(c60):
         mm = r.brickMinMax(0)
         assert tuple(mm[0]) == (c60["minmax"][0], c60["minmax"][1])
         b, o = r.getBrick(0, (0, 0, 0))
-        assert o == (0, 0, 0) and np.array_equal(b, c60["volume"])
+        # one brick: the level plus 2 replicated ghost voxels per face
+        assert o == (-2, -2, -2) and np.array_equal(b[2:-2, 2:-2, 2:-2], c60["volume"])
+        assert np.array_equal(b, np.pad(c60["volume"], 2, mode="edge"))
 
 
 def test_c60_load_uvf_and_write_back_byte_exact(c60, tmp_path):

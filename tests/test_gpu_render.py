@@ -238,3 +238,33 @@ def test_state_errors_are_statuses():
             r.resize((0, 10))
         with pytest.raises(GbvrError):
             r.loadDataset("/nonexistent.uvf")
+
+
+def test_layout_copies_and_launch_shapes_do_not_change_pixels(multibrick):
+    """x/y/z-fastest brick copies and every warp tile shape give the same
+    image bit for bit: only the memory order and the schedule change."""
+    vol, _, tf = multibrick
+    views = workloads.orbit_views(4, 96, 80, elevation=35.0, start=10.0)
+    views.append(orbit_camera(0.0, 89.0, 2.5 * workloads.DIAG, 45.0, 96, 80))  # looking down y
+    imgs = {}
+    for layouts in (1, 3):
+        with Renderer(float_fb=True) as r:
+            r.loadVolume(vol, brick_size=64, overlap=2, layouts=layouts)
+            r.resize((96, 80))
+            r.set1DTrans(tf)
+            r.setValueRange(0.0, 4095.0)
+            r.setSampleRateModifier(1.5)
+            for tw in ((8, 16, 32, 4) if layouts == 3 else (8,)):
+                r.setLaunchShape(tw, 0)
+                r.paintBatch(views)
+                imgs[(layouts, tw)] = [r.readFramebuffer(i, as_float=True) for i in range(len(views))]
+            if layouts == 3:
+                tune = r.autotune(views)
+                assert tune["tile_w"] in (4, 8, 16, 32) and tune["candidates"] == 12
+                assert tune["best_ms"] <= tune["default_ms"]
+                r.paintBatch(views)
+                imgs["tuned"] = [r.readFramebuffer(i, as_float=True) for i in range(len(views))]
+    ref = imgs[(1, 8)]
+    for key, got in imgs.items():
+        for i in range(len(views)):
+            assert np.array_equal(got[i], ref[i]), (key, i)

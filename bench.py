@@ -219,12 +219,14 @@ def main():
     mine = shard(len(wl.views), rank, world)
     views = [wl.views[i] for i in mine]
     r = Renderer()
-    r.loadSynthetic(wl.synth, **wl.brick, build_texture=not args.no_texture)
+    r.loadSynthetic(wl.synth, **wl.brick, build_texture=not args.no_texture, layouts=3)
     r.resize((wl.width, wl.height))
     r.set1DTrans(wl.tf)
     r.setValueRange(*wl.value_range)
     r.setSampleRateModifier(wl.spv)
     info = r.datasetInfo()
+    # launch shape picked by the autotuner on this batch (setup, untimed)
+    tune = r.autotune(views)
 
     def barrier():
         if dist is not None:
@@ -273,8 +275,10 @@ def main():
 
     # ---- texture-hardware trilinear, same batch ----
     tex_fps = None
+    tune_tex = None
     if not args.no_texture:
         r.setSampler(GBVR_SAMPLER_TEX)
+        tune_tex = r.autotune(views)
         for _ in range(2):
             r.paintBatch(views)
         tms = []
@@ -283,6 +287,7 @@ def main():
             tms.append(r.stats()["gpu_ms"])
         tex_fps = len(views) * args.steps / (sum(tms) / 1000.0)
         r.setSampler(GBVR_SAMPLER_SW)
+        r.setLaunchShape(tune["tile_w"], tune["ctas_per_sm"])
 
     # ---- end to end through the public API with host buffers ----
     fb = [None] * len(views)
@@ -353,12 +358,15 @@ def main():
                        "views": len(wl.views), "width": wl.width, "height": wl.height,
                        "samples_per_voxel": wl.spv, "lod": 0, "tf_entries": 4096,
                        "sampler": "fp32 software trilinear",
+                       "brick_layouts": "x/y/z-fastest copies, chosen per view",
+                       "empty_skipping": "bricks + 8^3 macro-cells",
                        "l2": "inputs larger than L2 (brick pool %.2f GB)" % (info["device_bytes"] / 1e9),
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "gsamples_per_s": gs,
             "per_view_plain_fps": plain_fps,
             "batched_vs_per_view": value / plain_fps,
             "texture_trilinear_fps": tex_fps,
+            "autotune": {"sw": tune, "tex": tune_tex},
             "e2e_per_view_fps": e2e_plain,
             "image_error_vs_fp64": err,
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d,

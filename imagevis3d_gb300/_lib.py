@@ -114,6 +114,7 @@ SIGNATURES = {
     "gbvr_set_background": [P, FP, FP],
     "gbvr_set_early_termination": [P, F],
     "gbvr_set_launch_shape": [P, I, I],
+    "gbvr_set_empty_skipping": [P, I],
     "gbvr_autotune": [P, C.POINTER(View), I, C.POINTER(TuneResult)],
     "gbvr_paint": [P],
     "gbvr_paint_batch": [P, C.POINTER(View), I],

@@ -194,7 +194,12 @@ struct Level {
   int interior;
   int brick_base;
   int nbricks;
+  int nc[3];                          // macro-cell grid
+  std::shared_ptr<DevBuf> cells;      // float2 min/max per macro-cell
 };
+
+// macro-cell edge (voxels) for empty-space skipping inside bricks
+constexpr int CELL_SHIFT = 3;
 
 struct Dataset {
   bool loaded = false;
@@ -369,8 +374,12 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   CUDA_TRY(ds.d_bricks.alloc(sizeof(BrickInfo) * ds.bricks.size()));
   CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyHostToDevice, s));
   for (size_t l = 0; l < ld.size(); ++l) {
-    const Level& L = ds.levels[l];
+    Level& L = ds.levels[l];
     long long d[3] = {ld[l][0], ld[l][1], ld[l][2]};
+    for (int a = 0; a < 3; ++a) L.nc[a] = (int)((d[a] + (1 << CELL_SHIFT) - 1) >> CELL_SHIFT);
+    L.cells = std::make_shared<DevBuf>();
+    CUDA_TRY(L.cells->alloc(sizeof(float2) * (size_t)L.nc[0] * L.nc[1] * L.nc[2]));
+    CUDA_TRY(launch_cell_minmax(lv[l]->p, dtype, d, CELL_SHIFT, L.nc, L.cells->as<float2>(), s));
     for (int perm = 0; perm < ds.layouts; ++perm)
       CUDA_TRY(launch_gather_bricks(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks,
                                     (char*)ds.pool.p + (size_t)perm * cursor * es, perm, s));
@@ -464,10 +473,11 @@ struct gbvr_renderer {
   float bg_top[3] = {0, 0, 0}, bg_bot[3] = {0, 0, 0};
   float ert = 0.99f;
   int tile_w = TILE_W, ctas_per_sm = 0;
+  int empty_skip = 2;
   // device state
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
-  DevBuf d_tf, d_skip, d_fb8, d_fb32, d_frames, d_prefix, d_counter, d_samples, d_touched;
+  DevBuf d_tf, d_skip, d_fb8, d_fb32, d_frames, d_prefix, d_counter, d_samples, d_touched, d_tfprefix, d_occ;
   PinnedBuf h_frames, h_prefix;
   bool tf_dirty = true, skip_dirty = true;
   int skip_level = -1;
@@ -561,13 +571,28 @@ int upload_tf(gbvr_renderer* r, int level) {
   if (r->skip_dirty || r->skip_level != level) {
     const Level& L = r->ds.levels[level];
     CUDA_TRY(r->d_skip.alloc(r->ds.bricks.size()));
+    const size_t ncell = (size_t)L.nc[0] * L.nc[1] * L.nc[2];
+    CUDA_TRY(r->d_occ.alloc(ncell));
     double lo, hi;
     default_range(r, lo, hi);
     int w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4), h = two ? r->tf2d_h : 1;
+    // prefix count of TF columns with any non-zero alpha
+    std::vector<int> pre(w + 1, 0);
+    for (int x = 0; x < w; ++x) {
+      int nz = 0;
+      for (int y = 0; y < h && !nz; ++y) nz = tf[4 * ((size_t)y * w + x) + 3] != 0.f;
+      pre[x + 1] = pre[x] + nz;
+    }
+    CUDA_TRY(r->d_tfprefix.alloc(sizeof(int) * pre.size()));
+    CUDA_TRY(cudaMemcpyAsync(r->d_tfprefix.p, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, r->stream));
     float idx_scale = (float)((w - 1) / (hi - lo));
-    CUDA_TRY(launch_classify(r->ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks, r->d_tf.as<float4>(), w, h,
-                             r->mode, (float)lo, idx_scale, r->iso, r->d_skip.as<unsigned char>() + L.brick_base,
-                             r->stream));
+    CUDA_TRY(launch_classify_bricks(r->ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks, r->d_tfprefix.as<int>(), w,
+                                    r->mode, (float)lo, idx_scale, r->iso,
+                                    r->d_skip.as<unsigned char>() + L.brick_base, r->stream));
+    CUDA_TRY(launch_classify_cells(L.cells->as<float2>(), (long long)ncell, r->d_tfprefix.as<int>(), w, r->mode,
+                                   (float)lo, idx_scale, r->iso, r->d_occ.as<unsigned char>(), r->stream));
+    // the host prefix vector must outlive the async copy
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
     r->skip_dirty = false;
     r->skip_level = level;
   }
@@ -641,6 +666,10 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
   f.width = r->width;
   f.height = r->height;
   f.tile_w = r->tile_w;
+  f.empty_skip = r->empty_skip;
+  f.occ = r->d_occ.as<unsigned char>();
+  for (int a = 0; a < 3; ++a) f.nc[a] = L.nc[a];
+  f.cell_shift = CELL_SHIFT;
   f.tiles_x = (r->width + r->tile_w - 1) / r->tile_w;
   f.tiles_y = (r->height + 32 / r->tile_w - 1) / (32 / r->tile_w);
   // layout copy: the axis whose voxel-space extent along screen x is largest
@@ -1210,6 +1239,13 @@ int gbvr_set_launch_shape(gbvr_renderer* r, int tile_w, int ctas_per_sm) {
   if (ctas_per_sm < 0 || ctas_per_sm > 64) return fail(GBVR_EINVAL, "bad ctas_per_sm");
   r->tile_w = tile_w;
   r->ctas_per_sm = ctas_per_sm;
+  return GBVR_OK;
+}
+
+int gbvr_set_empty_skipping(gbvr_renderer* r, int mode) {
+  TRY(check_r(r));
+  if (mode < 0 || mode > 2) return fail(GBVR_EINVAL, "empty skipping mode must be 0, 1 or 2");
+  r->empty_skip = mode;
   return GBVR_OK;
 }
 

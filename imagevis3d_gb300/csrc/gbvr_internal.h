@@ -79,6 +79,11 @@ struct __align__(16) FrameDesc {
   float inv_vp[16];          // row-major inverse of proj*view
   int width, height;
   int tiles_x, tiles_y;
+  // empty-space skipping: 0 none, 1 whole bricks, 2 bricks and macro-cells
+  int empty_skip;
+  const unsigned char* occ; // per macro-cell of the rendered level: 1 = may contribute
+  int nc[3];                 // macro-cell grid of the level
+  int cell_shift;            // macro-cell edge = 1 << cell_shift voxels
   int tile_w;                // ray tile of one warp: tile_w x (32 / tile_w) pixels
   int perm;                  // brick layout copy: 0 x-fastest, 1 y-fastest, 2 z-fastest
   unsigned long long copy_off;  // element offset of that copy in the pool
@@ -93,9 +98,15 @@ struct __align__(16) FrameDesc {
 constexpr int TILE_W = 8;
 
 // ---- launch wrappers (kernels_render.cu) ----
-cudaError_t launch_classify(const BrickInfo* bricks, int nbricks, const float4* tf, int tf_w,
-                            int tf_h, int mode, float value_lo, float idx_scale, float iso,
-                            unsigned char* skip, cudaStream_t s);
+// Classification of value ranges against the transfer function.  tf_prefix
+// holds tf_w + 1 counts: tf_prefix[i] = number of TF columns j < i with a
+// non-zero alpha (in any row of a 2D TF).  Writes 1 = may contribute.
+cudaError_t launch_classify_bricks(const BrickInfo* bricks, int nbricks, const int* tf_prefix, int tf_w,
+                                   int mode, float value_lo, float idx_scale, float iso,
+                                   unsigned char* skip, cudaStream_t s);
+cudaError_t launch_classify_cells(const float2* cells, long long ncells, const int* tf_prefix, int tf_w,
+                                  int mode, float value_lo, float idx_scale, float iso,
+                                  unsigned char* occ, cudaStream_t s);
 cudaError_t launch_render_plain(const FrameDesc& f, cudaStream_t s);
 cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, const FrameDesc* frames,
                                            int nframes, const int* tile_prefix, int total_tiles,
@@ -127,6 +138,10 @@ cudaError_t launch_gather_bricks(const void* level, int dtype, const long long d
                                  int perm, cudaStream_t s);
 cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_dev, int nbricks,
                                 cudaStream_t s);
+// Macro-cell min/max of a flat level: cell c covers sample cells [c M, c M + M)
+// per axis, whose trilinear footprints span voxels [c M, c M + M] (clamped).
+cudaError_t launch_cell_minmax(const void* level, int dtype, const long long dims[3], int cell_shift,
+                               const int nc[3], float2* out, cudaStream_t s);
 cudaError_t launch_hist1d(const void* vol, int dtype, long long n, unsigned long long* hist,
                           int nbins, cudaStream_t s);
 // 2D histogram passes; scratch holds the pass-1 reduction state.

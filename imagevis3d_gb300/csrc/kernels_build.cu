@@ -233,6 +233,48 @@ cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_d
 }
 
 // ---------------------------------------------------------------------------
+// Macro-cell min/max for empty-space skipping inside bricks: one thread per
+// cell, over the (M + 1)^3 voxels its samples' trilinear footprints can
+// touch (the finer grid of the reference's GridLeaper-style acceleration).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_cell_minmax(const T* __restrict__ v, long long X, long long Y, long long Z, int sh, int ncx, int ncy,
+                              int ncz, float2* __restrict__ out) {
+  const long long n = (long long)ncx * ncy * ncz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long cx = i % ncx, t = i / ncx, cy = t % ncy, cz = t / ncy;
+    const long long x0 = cx << sh, y0 = cy << sh, z0 = cz << sh;
+    const long long x1 = min(x0 + (1LL << sh), X - 1), y1 = min(y0 + (1LL << sh), Y - 1), z1 = min(z0 + (1LL << sh), Z - 1);
+    float mn = INFINITY, mx = -INFINITY;
+    for (long long z = z0; z <= z1; ++z)
+      for (long long y = y0; y <= y1; ++y) {
+        const T* row = v + (z * Y + y) * X;
+        for (long long x = x0; x <= x1; ++x) {
+          float a = (float)__ldg(row + x);
+          mn = fminf(mn, a);
+          mx = fmaxf(mx, a);
+        }
+      }
+    out[i] = make_float2(mn, mx);
+  }
+}
+
+cudaError_t launch_cell_minmax(const void* level, int dtype, const long long dims[3], int sh, const int nc[3],
+                               float2* out, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  const long long n = (long long)nc[0] * nc[1] * nc[2];
+  int threads = 128;
+  int blocks = grid_for(n, threads);
+  if (dtype == DT_U8)
+    k_cell_minmax<uint8_t><<<blocks, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], sh, nc[0], nc[1], nc[2], out);
+  else if (dtype == DT_U16)
+    k_cell_minmax<uint16_t><<<blocks, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], dims[2], sh, nc[0], nc[1], nc[2], out);
+  else
+    k_cell_minmax<float><<<blocks, threads, 0, s>>>((const float*)level, dims[0], dims[1], dims[2], sh, nc[0], nc[1], nc[2], out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // 1D histogram (Histogram1DDataBlock::Compute, DataSource.h:603): one bin per
 // value.  Privatised in shared memory (u32 per CTA, flushed with u64 global
 // atomics) when the value range fits; global atomics otherwise.

@@ -292,39 +292,63 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
       py = fmaf(t, r.dv[1], r.ov[1]);
       pz = fmaf(t, r.dv[2], r.ov[2]);
     };
+    // First sample index >= k + 1 whose cell leaves the box [lo, hi) (per
+    // axis, on clamped floor coordinates), or K: estimated from the box's
+    // exit planes, then settled by the same floor(pos) rule that assigns
+    // samples to bricks and cells.  Positions are monotone in k, so members
+    // form one run and only its ends need checking.
+    auto run_end = [&](int k0, int lx, int ly, int lz, int hx, int hy, int hz) -> int {
+      float te = INFINITY;
+      te = fminf(te, r.dv[0] > 0.f ? ((float)hx - r.ov[0]) / r.dv[0]
+                                   : (r.dv[0] < 0.f ? ((float)lx - r.ov[0]) / r.dv[0] : INFINITY));
+      te = fminf(te, r.dv[1] > 0.f ? ((float)hy - r.ov[1]) / r.dv[1]
+                                   : (r.dv[1] < 0.f ? ((float)ly - r.ov[1]) / r.dv[1] : INFINITY));
+      te = fminf(te, r.dv[2] > 0.f ? ((float)hz - r.ov[2]) / r.dv[2]
+                                   : (r.dv[2] < 0.f ? ((float)lz - r.ov[2]) / r.dv[2] : INFINITY));
+      const float kef = ceilf((te - t0) / dt - 0.5f);
+      int ke = kef >= (float)K ? K : max(k0 + 1, (int)kef);
+      auto in_box = [&](int kk) {
+        float qx, qy, qz;
+        pos_of(kk, qx, qy, qz);
+        const int cx = clamp_cell(qx, f.dims[0]), cy = clamp_cell(qy, f.dims[1]), cz = clamp_cell(qz, f.dims[2]);
+        return cx >= lx && cx < hx && cy >= ly && cy < hy && cz >= lz && cz < hz;
+      };
+      while (ke > k0 + 1 && !in_box(ke - 1)) --ke;
+      while (ke < K && in_box(ke)) ++ke;
+      return ke;
+    };
     int k = 0;
     bool done = false;
+    BrickView b;
+    int bi = -1, bke = 0;  // current brick and the end of the ray's run in it
+    const int sh = f.cell_shift;
     while (k < K && !done) {
       float px, py, pz;
       pos_of(k, px, py, pz);
-      const int bi = brick_index(f, clamp_cell(px, f.dims[0]), clamp_cell(py, f.dims[1]), clamp_cell(pz, f.dims[2]));
-      BrickView b;
-      load_brick(f, bi, b);
-      // Samples [k, ke) of this ray lie in the brick: estimate the exit from
-      // the interior planes, then settle it with the floor(pos) rule that
-      // assigns samples to bricks.  Positions are monotone in k, so the
-      // members form one run and only its ends need checking.
-      float te = INFINITY;
-      te = fminf(te, r.dv[0] > 0.f ? ((float)b.hix - r.ov[0]) / r.dv[0]
-                                   : (r.dv[0] < 0.f ? ((float)b.lox - r.ov[0]) / r.dv[0] : INFINITY));
-      te = fminf(te, r.dv[1] > 0.f ? ((float)b.hiy - r.ov[1]) / r.dv[1]
-                                   : (r.dv[1] < 0.f ? ((float)b.loy - r.ov[1]) / r.dv[1] : INFINITY));
-      te = fminf(te, r.dv[2] > 0.f ? ((float)b.hiz - r.ov[2]) / r.dv[2]
-                                   : (r.dv[2] < 0.f ? ((float)b.loz - r.ov[2]) / r.dv[2] : INFINITY));
-      const float kef = ceilf((te - t0) / dt - 0.5f);
-      int ke = kef >= (float)K ? K : max(k + 1, (int)kef);
-      auto in_b = [&](int kk) {
-        float qx, qy, qz;
-        pos_of(kk, qx, qy, qz);
-        return inside(b, clamp_cell(qx, f.dims[0]), clamp_cell(qy, f.dims[1]), clamp_cell(qz, f.dims[2]));
-      };
-      while (ke > k + 1 && !in_b(ke - 1)) --ke;
-      while (ke < K && in_b(ke)) ++ke;
-      if (__ldg(f.skip + bi)) {
-        k = ke;
-        continue;
+      const int gx = clamp_cell(px, f.dims[0]), gy = clamp_cell(py, f.dims[1]), gz = clamp_cell(pz, f.dims[2]);
+      if (bi < 0 || k >= bke) {
+        bi = brick_index(f, gx, gy, gz);
+        load_brick(f, bi, b);
+        bke = run_end(k, b.lox, b.loy, b.loz, b.hix, b.hiy, b.hiz);
+        if (f.empty_skip >= 1 && __ldg(f.skip + bi)) {
+          k = bke;
+          bi = -1;
+          continue;
+        }
+        if (f.touched) f.touched[bi] = 1;
       }
-      if (f.touched) f.touched[bi] = 1;
+      int ke = bke;
+      if (f.empty_skip >= 2) {
+        const int cx = max(gx, 0) >> sh, cy = max(gy, 0) >> sh, cz = max(gz, 0) >> sh;
+        const int cke = run_end(k, cx == 0 ? -1 : cx << sh, cy == 0 ? -1 : cy << sh, cz == 0 ? -1 : cz << sh,
+                                min((cx + 1) << sh, f.dims[0]), min((cy + 1) << sh, f.dims[1]),
+                                min((cz + 1) << sh, f.dims[2]));
+        ke = min(ke, cke);
+        if (!__ldg(f.occ + ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx)) {
+          k = ke;
+          continue;
+        }
+      }
       if (MODE == MODE_1D) {
         // two samples per iteration: both footprints are fetched before
         // either is composited
@@ -466,45 +490,55 @@ __global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const F
 }
 
 // ---------------------------------------------------------------------------
-// Brick classification: a brick is skipped when no sample inside it can add
-// anything.  Values sampled in a brick lie in [vmin, vmax] of its stored
-// voxels (trilinear weights are convex), so the TF entries a sample can touch
-// are bounded; if every such alpha is 0 the brick contributes exactly nothing.
-// Isosurface: skipped when vmax < iso (no sample can reach the isovalue).
-// One warp per brick.
+// Empty-space classification.  Values sampled where a brick or macro-cell
+// applies lie in [vmin, vmax] of the voxels its samples can touch (trilinear
+// weights are convex), so the TF entries such a sample can read are bounded;
+// if every one has alpha 0 the region contributes exactly nothing and the
+// walk skips it.  Isosurface: skipped when vmax < iso (no sample can reach
+// the isovalue).  One prefix count over the TF columns makes each test O(1).
 // ---------------------------------------------------------------------------
-__global__ void k_classify(const BrickInfo* __restrict__ bricks, int nbricks, const float4* __restrict__ tf,
-                           int tf_w, int tf_h, int mode, float value_lo, float idx_scale, float iso,
-                           unsigned char* __restrict__ skip) {
-  int warp = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-  int lane = threadIdx.x & 31;
-  if (warp >= nbricks) return;
-  const BrickInfo& b = bricks[warp];
-  if (mode == MODE_ISO) {
-    if (lane == 0) skip[warp] = (b.vmax < iso) ? 1 : 0;
-    return;
-  }
-  float ilo = fminf(fmaxf((b.vmin - value_lo) * idx_scale, 0.f), (float)(tf_w - 1));
-  float ihi = fminf(fmaxf((b.vmax - value_lo) * idx_scale, 0.f), (float)(tf_w - 1));
+__device__ __forceinline__ unsigned char classify_range(float mn, float mx, const int* __restrict__ prefix, int tf_w,
+                                                        int mode, float value_lo, float idx_scale, float iso) {
+  if (mode == MODE_ISO) return mx >= iso ? 1 : 0;
+  float ilo = fminf(fmaxf((mn - value_lo) * idx_scale, 0.f), (float)(tf_w - 1));
+  float ihi = fminf(fmaxf((mx - value_lo) * idx_scale, 0.f), (float)(tf_w - 1));
   int lo = max((int)floorf(ilo) - 1, 0);
   int hi = min((int)floorf(ihi) + 2, tf_w - 1);
-  int rows = mode == MODE_2D ? tf_h : 1;
-  int nonzero = 0;
-  for (int r = 0; r < rows && !nonzero; ++r) {
-    for (int i = lo + lane; i <= hi; i += 32)
-      if (tf[r * tf_w + i].w != 0.f) nonzero = 1;
-    nonzero = __any_sync(0xffffffffu, nonzero);
-  }
-  if (lane == 0) skip[warp] = nonzero ? 0 : 1;
+  return (__ldg(prefix + hi + 1) - __ldg(prefix + lo)) > 0 ? 1 : 0;
 }
 
-cudaError_t launch_classify(const BrickInfo* bricks, int nbricks, const float4* tf, int tf_w, int tf_h, int mode,
-                            float value_lo, float idx_scale, float iso, unsigned char* skip, cudaStream_t s) {
+__global__ void k_classify_bricks(const BrickInfo* __restrict__ bricks, int nbricks, const int* __restrict__ prefix,
+                                  int tf_w, int mode, float value_lo, float idx_scale, float iso,
+                                  unsigned char* __restrict__ skip) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nbricks) return;
+  skip[i] = classify_range(bricks[i].vmin, bricks[i].vmax, prefix, tf_w, mode, value_lo, idx_scale, iso) ? 0 : 1;
+}
+
+__global__ void k_classify_cells(const float2* __restrict__ cells, long long n, const int* __restrict__ prefix, int tf_w,
+                                 int mode, float value_lo, float idx_scale, float iso, unsigned char* __restrict__ occ) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float2 c = __ldg(cells + i);
+    occ[i] = classify_range(c.x, c.y, prefix, tf_w, mode, value_lo, idx_scale, iso);
+  }
+}
+
+cudaError_t launch_classify_bricks(const BrickInfo* bricks, int nbricks, const int* prefix, int tf_w, int mode,
+                                   float value_lo, float idx_scale, float iso, unsigned char* skip, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (nbricks <= 0) return cudaSuccess;
-  int threads = 128;
-  int blocks = (nbricks * 32 + threads - 1) / threads;
-  k_classify<<<blocks, threads, 0, s>>>(bricks, nbricks, tf, tf_w, tf_h, mode, value_lo, idx_scale, iso, skip);
+  k_classify_bricks<<<(nbricks + 127) / 128, 128, 0, s>>>(bricks, nbricks, prefix, tf_w, mode, value_lo, idx_scale,
+                                                         iso, skip);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_classify_cells(const float2* cells, long long n, const int* prefix, int tf_w, int mode,
+                                  float value_lo, float idx_scale, float iso, unsigned char* occ, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (n <= 0) return cudaSuccess;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  k_classify_cells<<<(unsigned)blocks, 256, 0, s>>>(cells, n, prefix, tf_w, mode, value_lo, idx_scale, iso, occ);
   return cudaGetLastError();
 }
 

@@ -220,6 +220,9 @@ class Renderer:
     def setLaunchShape(self, tile_w=8, ctas_per_sm=0):
         L.call("gbvr_set_launch_shape", self._h, tile_w, ctas_per_sm)
 
+    def setEmptySkipping(self, mode):
+        L.call("gbvr_set_empty_skipping", self._h, mode)
+
     def autotune(self, views):
         arr = self._views(views)
         res = L.TuneResult()

@@ -186,6 +186,13 @@ int gbvr_set_early_termination(gbvr_renderer* r, float alpha);           /* 0.99
  * (GL rasterisation chose its own fragment order). */
 int gbvr_set_launch_shape(gbvr_renderer* r, int tile_w, int ctas_per_sm);
 
+/* Empty-space skipping: 0 none (every sample is evaluated), 1 whole bricks
+ * classified empty by their min/max against the TF, 2 (default) also
+ * 8^3-voxel macro-cells inside bricks, the finer acceleration grid of the
+ * reference's GridLeaper renderer type (RenderWindowGL.cpp:176-188).  All
+ * three give identical pixels: a skipped region contributes exactly zero. */
+int gbvr_set_empty_skipping(gbvr_renderer* r, int mode);
+
 typedef struct gbvr_tune_result {
   int32_t tile_w;
   int32_t ctas_per_sm;

@@ -268,3 +268,34 @@ def test_layout_copies_and_launch_shapes_do_not_change_pixels(multibrick):
     for key, got in imgs.items():
         for i in range(len(views)):
             assert np.array_equal(got[i], ref[i]), (key, i)
+
+
+@pytest.mark.parametrize("mode", [GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE])
+def test_empty_space_skipping_is_exact(multibrick, mode):
+    """No skipping, brick skipping and macro-cell skipping give the same bits."""
+    vol, _, tf = multibrick
+    views = workloads.orbit_views(3, 128, 96, elevation=25.0, start=15.0)
+    out = []
+    for skip in (0, 1, 2):
+        with Renderer(float_fb=True) as r:
+            r.loadVolume(vol, brick_size=64, overlap=2)
+            r.resize((128, 96))
+            r.setRenderMode(mode)
+            if mode == GBVR_RM_2DTRANS:
+                r.set2DTrans(workloads.tf2d_seeded(256, 64, 9), 0.05)
+            elif mode == GBVR_RM_ISOSURFACE:
+                r.setIsoValue(1300.0, (1.0, 0.8, 0.5))
+            else:
+                r.set1DTrans(tf)
+            r.setValueRange(0.0, 4095.0)
+            r.setSampleRateModifier(1.5)
+            r.setEmptySkipping(skip)
+            r.paintBatch(views)
+            out.append(([r.readFramebuffer(i, as_float=True) for i in range(3)], r.stats()))
+    for i in range(3):
+        assert np.array_equal(out[0][0][i], out[1][0][i])
+        assert np.array_equal(out[0][0][i], out[2][0][i])
+    if mode != GBVR_RM_ISOSURFACE:
+        # skipping removes samples, never adds
+        assert out[2][1]["samples"] <= out[1][1]["samples"] <= out[0][1]["samples"]
+        assert out[2][1]["samples"] < out[0][1]["samples"]

@@ -47,7 +47,7 @@ class Stats(C.Structure):
                 ("bricks_skipped", C.c_uint64), ("brick_bytes", C.c_uint64),
                 ("brick_misses", C.c_uint64), ("bytes_paged", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("lod", C.c_int32), ("subframes", C.c_int32), ("gpu_ms", C.c_double),
-                ("kernel_ms", C.c_double)]
+                ("kernel_ms", C.c_double), ("cells_touched", C.c_uint64), ("cell_bytes", C.c_uint64)]
 
 
 class TuneResult(C.Structure):
@@ -123,6 +123,7 @@ SIGNATURES = {
     "gbvr_read_framebuffer_f32": [P, I, P, SZ],
     "gbvr_capture_single_frame": [P, CP, I],
     "gbvr_get_stats": [P, C.POINTER(Stats)],
+    "gbvr_set_stats_level": [P, I],
     "gbvr_synth_volume": [C.POINTER(SynthParams), P, SZ],
     "gbvr_load_synthetic": [P, C.POINTER(SynthParams), C.POINTER(BrickParams)],
     "gbvr_build_uvf": [P, I64P, I, C.POINTER(BrickParams), CP],

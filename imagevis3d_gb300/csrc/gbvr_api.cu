@@ -474,10 +474,13 @@ struct gbvr_renderer {
   float ert = 0.99f;
   int tile_w = TILE_W, ctas_per_sm = 0;
   int empty_skip = 2;
+  int stats_level = 1;  // 0 samples, 1 + touched bricks, 2 + touched macro-cells
   // device state
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
   DevBuf d_tf, d_skip, d_fb8, d_fb32, d_frames, d_prefix, d_counter, d_samples, d_touched, d_tfprefix, d_occ;
+  DevBuf d_cellbits, d_cellcount;
+  long long cell_words = 0;
   PinnedBuf h_frames, h_prefix;
   bool tf_dirty = true, skip_dirty = true;
   int skip_level = -1;
@@ -687,7 +690,9 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
   f.out_rgba8 = r->d_fb8.as<uchar4>() + (size_t)vidx * npix;
   f.out_f32 = r->d_fb32.p ? r->d_fb32.as<float4>() + (size_t)vidx * npix : nullptr;
   f.samples = r->d_samples.as<unsigned long long>() + vidx;
-  f.touched = r->d_touched.as<unsigned char>() + (size_t)vidx * L.nbricks;
+  f.touched = r->stats_level >= 1 ? r->d_touched.as<unsigned char>() + (size_t)vidx * L.nbricks : nullptr;
+  f.cell_touched = (r->stats_level >= 2 && r->empty_skip >= 2)
+                       ? r->d_cellbits.as<unsigned>() + (size_t)vidx * r->cell_words : nullptr;
   return f;
 }
 
@@ -716,6 +721,14 @@ int prepare(gbvr_renderer* r, int nviews, int& level) {
   }
   CUDA_TRY(r->d_samples.alloc(sizeof(unsigned long long) * nviews));
   CUDA_TRY(r->d_touched.alloc((size_t)nviews * r->ds.levels[level].nbricks));
+  {
+    const Level& L = r->ds.levels[level];
+    r->cell_words = ((long long)L.nc[0] * L.nc[1] * L.nc[2] + 31) / 32;
+    if (r->stats_level >= 2) {
+      CUDA_TRY(r->d_cellbits.alloc(sizeof(unsigned) * r->cell_words * nviews));
+      CUDA_TRY(r->d_cellcount.alloc(sizeof(unsigned long long) * nviews));
+    }
+  }
   TRY(upload_tf(r, level));
   return GBVR_OK;
 }
@@ -734,6 +747,7 @@ int paint_plain(gbvr_renderer* r, const gbvr_view* views, int n) {
   TRY(prepare(r, n, level));
   CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream));
   CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
+  if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words * n, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
   for (int v = 0; v < n; ++v) {
@@ -809,6 +823,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   CUDA_TRY(cudaMemsetAsync(r->d_counter.p, 0, sizeof(int), r->stream));
   CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream));
   CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
+  if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words * n, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
   CUDA_TRY(cudaGraphLaunch(it->second, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
@@ -1358,6 +1373,26 @@ int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out) {
       }
   }
   for (int b = 0; b < L.nbricks; ++b) out->bricks_skipped += skip[b];
+  if (r->stats_level >= 2 && r->empty_skip >= 2 && r->d_cellbits.p) {
+    std::vector<unsigned long long> cc(n);
+    CUDA_TRY(cudaMemsetAsync(r->d_cellcount.p, 0, sizeof(unsigned long long) * n, r->stream));
+    CUDA_TRY(launch_count_bits(r->d_cellbits.as<unsigned>(), r->cell_words, n, r->d_cellcount.as<unsigned long long>(),
+                               r->stream));
+    CUDA_TRY(cudaMemcpyAsync(cc.data(), r->d_cellcount.p, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    const uint64_t cell_vox = (uint64_t)1 << (3 * CELL_SHIFT);
+    for (int v = 0; v < n; ++v) {
+      out->cells_touched += cc[v];
+      out->cell_bytes += cc[v] * cell_vox * es;
+    }
+  }
+  return GBVR_OK;
+}
+
+int gbvr_set_stats_level(gbvr_renderer* r, int level) {
+  TRY(check_r(r));
+  if (level < 0 || level > 2) return fail(GBVR_EINVAL, "stats level must be 0, 1 or 2");
+  r->stats_level = level;
   return GBVR_OK;
 }
 

@@ -92,6 +92,7 @@ struct __align__(16) FrameDesc {
   float4* out_f32;           // may be null
   unsigned long long* samples;  // per-frame sample counter
   unsigned char* touched;    // per-frame flag per brick of the rendered level
+  unsigned* cell_touched;    // per-frame bitmap of sampled non-empty macro-cells (or null)
 };
 
 // Default ray tile handled by one warp: 8 x 4 pixels.
@@ -108,6 +109,9 @@ cudaError_t launch_classify_cells(const float2* cells, long long ncells, const i
                                   int mode, float value_lo, float idx_scale, float iso,
                                   unsigned char* occ, cudaStream_t s);
 cudaError_t launch_render_plain(const FrameDesc& f, cudaStream_t s);
+// popcount of n_frames bitmaps of `words` words each into counts[n_frames]
+cudaError_t launch_count_bits(const unsigned* bits, long long words, int n_frames, unsigned long long* counts,
+                              cudaStream_t s);
 cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, const FrameDesc* frames,
                                            int nframes, const int* tile_prefix, int total_tiles,
                                            int* counter, int grid, cudaStream_t s);

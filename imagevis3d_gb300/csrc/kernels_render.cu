@@ -19,6 +19,8 @@
 //   k_render_persistent   grid = SMs x resident CTAs; warps pull (view, tile)
 //                         items from one atomic counter spanning every view
 //                         of the batch, so views and uneven rays share the GPU.
+#include <algorithm>
+
 #include "gbvr_internal.h"
 
 namespace gbvr {
@@ -344,9 +346,16 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
                                 min((cx + 1) << sh, f.dims[0]), min((cy + 1) << sh, f.dims[1]),
                                 min((cz + 1) << sh, f.dims[2]));
         ke = min(ke, cke);
-        if (!__ldg(f.occ + ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx)) {
+        const size_t ci = ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx;
+        if (!__ldg(f.occ + ci)) {
           k = ke;
           continue;
+        }
+        if (f.cell_touched) {
+          // algorithmic-bytes accounting: one bit per sampled cell
+          unsigned* w = f.cell_touched + (ci >> 5);
+          const unsigned bit = 1u << (ci & 31);
+          if (!(*(volatile unsigned*)w & bit)) atomicOr(w, bit);
         }
       }
       if (MODE == MODE_1D) {
@@ -521,6 +530,23 @@ __global__ void k_classify_cells(const float2* __restrict__ cells, long long n, 
     float2 c = __ldg(cells + i);
     occ[i] = classify_range(c.x, c.y, prefix, tf_w, mode, value_lo, idx_scale, iso);
   }
+}
+
+__global__ void k_count_bits(const unsigned* __restrict__ bits, long long words, unsigned long long* __restrict__ counts) {
+  const unsigned* b = bits + (size_t)blockIdx.y * words;
+  unsigned long long c = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < words; i += (long long)gridDim.x * blockDim.x)
+    c += __popc(__ldg(b + i));
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(counts + blockIdx.y, c);
+}
+
+cudaError_t launch_count_bits(const unsigned* bits, long long words, int n, unsigned long long* counts, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (n <= 0 || words <= 0) return cudaSuccess;
+  dim3 grid((unsigned)std::min<long long>((words + 255) / 256, 64), (unsigned)n);
+  k_count_bits<<<grid, 256, 0, s>>>(bits, words, counts);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_classify_bricks(const BrickInfo* bricks, int nbricks, const int* prefix, int tf_w, int mode,

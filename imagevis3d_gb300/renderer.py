@@ -267,6 +267,9 @@ class Renderer:
     def captureSingleFrame(self, path, preserve_transparency=True):
         L.call("gbvr_capture_single_frame", self._h, path.encode(), 1 if preserve_transparency else 0)
 
+    def setStatsLevel(self, level):
+        L.call("gbvr_set_stats_level", self._h, level)
+
     def stats(self):
         s = L.Stats()
         L.call("gbvr_get_stats", self._h, C.byref(s))

@@ -122,6 +122,8 @@ typedef struct gbvr_stats {
   int32_t subframes;           /* getCurrentSubFrameCount: always 1 */
   double gpu_ms;               /* device time of the last paint (CUDA events) */
   double kernel_ms;            /* device time of its raycast kernel launch(es) alone */
+  uint64_t cells_touched;      /* stats level 2: sum over views of distinct non-empty macro-cells sampled */
+  uint64_t cell_bytes;         /* ... times the cell's voxel bytes (8^3 voxels) */
 } gbvr_stats;
 
 /* ---- errors / device ---- */
@@ -225,6 +227,10 @@ int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t byt
 int gbvr_read_framebuffer_f32(gbvr_renderer* r, int view, float* rgba, size_t bytes);
 int gbvr_capture_single_frame(gbvr_renderer* r, const char* path, int preserve_transparency);
 int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out);
+/* What paint records for gbvr_get_stats: 0 sample counts only, 1 (default)
+ * also the bricks each view touched, 2 also the macro-cells each view
+ * sampled (a bitmap per view; costs an atomic per new cell). */
+int gbvr_set_stats_level(gbvr_renderer* r, int level);
 
 /* ---- seeded synthetic volumes ----
  * Sum of isotropic Gaussian blobs (+ optional low-frequency background and

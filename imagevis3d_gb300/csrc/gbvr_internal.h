@@ -143,7 +143,9 @@ cudaError_t launch_gather_bricks(const void* level, int dtype, const long long d
 cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_dev, int nbricks,
                                 cudaStream_t s);
 // Macro-cell min/max of a flat level: cell c covers sample cells [c M, c M + M)
-// per axis, whose trilinear footprints span voxels [c M, c M + M] (clamped).
+// per axis, whose trilinear footprints span voxels [c M, c M + M]; the range
+// is taken over [c M - 1, c M + M + 1] (clamped) so that a sample rounded
+// across a cell face is still covered.
 cudaError_t launch_cell_minmax(const void* level, int dtype, const long long dims[3], int cell_shift,
                                const int nc[3], float2* out, cudaStream_t s);
 cudaError_t launch_hist1d(const void* vol, int dtype, long long n, unsigned long long* hist,

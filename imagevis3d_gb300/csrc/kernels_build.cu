@@ -234,8 +234,9 @@ cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_d
 
 // ---------------------------------------------------------------------------
 // Macro-cell min/max for empty-space skipping inside bricks: one thread per
-// cell, over the (M + 1)^3 voxels its samples' trilinear footprints can
-// touch (the finer grid of the reference's GridLeaper-style acceleration).
+// cell, over the (M + 3)^3 voxels [c M - 1, c M + M + 1] around the
+// footprints of its samples (the finer grid of the reference's
+// GridLeaper-style acceleration).
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void k_cell_minmax(const T* __restrict__ v, long long X, long long Y, long long Z, int sh, int ncx, int ncy,
@@ -243,8 +244,12 @@ __global__ void k_cell_minmax(const T* __restrict__ v, long long X, long long Y,
   const long long n = (long long)ncx * ncy * ncz;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const long long cx = i % ncx, t = i / ncx, cy = t % ncy, cz = t / ncy;
-    const long long x0 = cx << sh, y0 = cy << sh, z0 = cz << sh;
-    const long long x1 = min(x0 + (1LL << sh), X - 1), y1 = min(y0 + (1LL << sh), Y - 1), z1 = min(z0 + (1LL << sh), Z - 1);
+    // one voxel of margin beyond the footprint [c M, c M + M] on each side:
+    // the walk skips empty cells by their estimated exit, and a sample that
+    // rounding puts in a neighbouring cell is at most that far outside
+    const long long x0 = max((cx << sh) - 1, 0LL), y0 = max((cy << sh) - 1, 0LL), z0 = max((cz << sh) - 1, 0LL);
+    const long long x1 = min((cx << sh) + (1LL << sh) + 1, X - 1), y1 = min((cy << sh) + (1LL << sh) + 1, Y - 1),
+                    z1 = min((cz << sh) + (1LL << sh) + 1, Z - 1);
     float mn = INFINITY, mx = -INFINITY;
     for (long long z = z0; z <= z1; ++z)
       for (long long y = y0; y <= y1; ++y) {

@@ -219,6 +219,7 @@ __device__ __forceinline__ float4 tf2d(const FrameDesc& f, float v, float gmag) 
 
 struct RaySetup {
   float ov[3], dv[3];  // voxel-centre origin and direction (per world unit of t)
+  float inv[3];        // 1 / dv
   float dw[3];         // unit world direction
   float t0, t1;
   bool hit;
@@ -254,6 +255,7 @@ __device__ __forceinline__ void setup_ray(const FrameDesc& f, int px, int py, Ra
     r.dw[i] = d[i];
     r.ov[i] = (o[i] + f.half_extent[i]) * f.vox_scale[i] - 0.5f;
     r.dv[i] = d[i] * f.vox_scale[i];
+    r.inv[i] = 1.f / r.dv[i];
   }
   r.t0 = t0;
   r.t1 = t1;
@@ -288,6 +290,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
     const float t0 = r.t0;
     const int K = max(0, (int)ceilf((r.t1 - t0) / dt - 0.5f));
     const float V[3] = {-r.dw[0], -r.dw[1], -r.dw[2]};
+    const float inv_dt = 1.f / dt;
     auto pos_of = [&](int kk, float& px, float& py, float& pz) {
       const float t = fmaf((float)kk + 0.5f, dt, t0);
       px = fmaf(t, r.dv[0], r.ov[0]);
@@ -341,12 +344,22 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
       }
       int ke = bke;
       if (f.empty_skip >= 2) {
+        // Macro-cell run, estimated from the cell's exit planes only: a
+        // sample that rounding places in a neighbouring cell lies within a
+        // voxel of this one, and the cell's min/max covers one voxel beyond
+        // its samples' footprints, so skipping an empty run never drops a
+        // contributing sample; sampling a run that spills over is harmless.
         const int cx = max(gx, 0) >> sh, cy = max(gy, 0) >> sh, cz = max(gz, 0) >> sh;
-        const int cke = run_end(k, cx == 0 ? -1 : cx << sh, cy == 0 ? -1 : cy << sh, cz == 0 ? -1 : cz << sh,
-                                min((cx + 1) << sh, f.dims[0]), min((cy + 1) << sh, f.dims[1]),
-                                min((cz + 1) << sh, f.dims[2]));
-        ke = min(ke, cke);
+        const float hx = (float)min((cx + 1) << sh, f.dims[0]), lx = (float)(cx << sh);
+        const float hy = (float)min((cy + 1) << sh, f.dims[1]), ly = (float)(cy << sh);
+        const float hz = (float)min((cz + 1) << sh, f.dims[2]), lz = (float)(cz << sh);
+        float te = fminf(fminf(r.dv[0] > 0.f ? (hx - r.ov[0]) * r.inv[0] : (r.dv[0] < 0.f ? (lx - r.ov[0]) * r.inv[0] : INFINITY),
+                               r.dv[1] > 0.f ? (hy - r.ov[1]) * r.inv[1] : (r.dv[1] < 0.f ? (ly - r.ov[1]) * r.inv[1] : INFINITY)),
+                         r.dv[2] > 0.f ? (hz - r.ov[2]) * r.inv[2] : (r.dv[2] < 0.f ? (lz - r.ov[2]) * r.inv[2] : INFINITY));
+        const float kef = ceilf((te - t0) * inv_dt - 0.5f);
+        const int cke = kef >= (float)ke ? ke : max(k + 1, (int)kef);
         const size_t ci = ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx;
+        ke = cke;
         if (!__ldg(f.occ + ci)) {
           k = ke;
           continue;
@@ -466,7 +479,7 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
 constexpr int RENDER_THREADS = 128;
 
 template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_plain(const __grid_constant__ FrameDesc f) {
+__global__ void __launch_bounds__(RENDER_THREADS, 7) k_render_plain(const __grid_constant__ FrameDesc f) {
   int warp = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (warp >= f.tiles_x * f.tiles_y) return;
   render_tile<T, MODE, SAMPLER>(f, warp);
@@ -484,7 +497,7 @@ __device__ __forceinline__ int find_frame(const int* __restrict__ prefix, int nf
 }
 
 template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
+__global__ void __launch_bounds__(RENDER_THREADS, 7) k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
                                                          const int* __restrict__ tile_prefix, int total,
                                                          int* __restrict__ counter) {
   const int lane = threadIdx.x & 31;

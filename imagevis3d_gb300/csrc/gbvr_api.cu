@@ -198,8 +198,10 @@ struct Level {
   std::shared_ptr<DevBuf> cells;      // float2 min/max per macro-cell
 };
 
-// macro-cell edge (voxels) for empty-space skipping inside bricks
+// macro-cell edge (voxels) for empty-space skipping inside bricks, and the
+// cap of the empty-cell distance field
 constexpr int CELL_SHIFT = 3;
+constexpr int CELL_DIST_CAP = 16;
 
 struct Dataset {
   bool loaded = false;
@@ -479,7 +481,7 @@ struct gbvr_renderer {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
   DevBuf d_tf, d_skip, d_fb8, d_fb32, d_frames, d_prefix, d_counter, d_samples, d_touched, d_tfprefix, d_occ;
-  DevBuf d_cellbits, d_cellcount;
+  DevBuf d_cellbits, d_cellcount, d_occtmp;
   long long cell_words = 0;
   PinnedBuf h_frames, h_prefix;
   bool tf_dirty = true, skip_dirty = true;
@@ -594,6 +596,9 @@ int upload_tf(gbvr_renderer* r, int level) {
                                     r->d_skip.as<unsigned char>() + L.brick_base, r->stream));
     CUDA_TRY(launch_classify_cells(L.cells->as<float2>(), (long long)ncell, r->d_tfprefix.as<int>(), w, r->mode,
                                    (float)lo, idx_scale, r->iso, r->d_occ.as<unsigned char>(), r->stream));
+    CUDA_TRY(r->d_occtmp.alloc(ncell));
+    CUDA_TRY(launch_cell_distance(r->d_occ.as<unsigned char>(), r->d_occtmp.as<unsigned char>(), L.nc, CELL_DIST_CAP,
+                                  r->stream));
     // the host prefix vector must outlive the async copy
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     r->skip_dirty = false;

@@ -81,7 +81,7 @@ struct __align__(16) FrameDesc {
   int tiles_x, tiles_y;
   // empty-space skipping: 0 none, 1 whole bricks, 2 bricks and macro-cells
   int empty_skip;
-  const unsigned char* occ; // per macro-cell of the rendered level: 1 = may contribute
+  const unsigned char* occ; // per macro-cell: capped distance (cells) to one that may contribute
   int nc[3];                 // macro-cell grid of the level
   int cell_shift;            // macro-cell edge = 1 << cell_shift voxels
   int tile_w;                // ray tile of one warp: tile_w x (32 / tile_w) pixels
@@ -105,6 +105,9 @@ constexpr int TILE_W = 8;
 cudaError_t launch_classify_bricks(const BrickInfo* bricks, int nbricks, const int* tf_prefix, int tf_w,
                                    int mode, float value_lo, float idx_scale, float iso,
                                    unsigned char* skip, cudaStream_t s);
+// Turn occ (1 = may contribute) into the capped Chebyshev distance to the
+// nearest such cell, in place (tmp: scratch of the same size).
+cudaError_t launch_cell_distance(unsigned char* occ, unsigned char* tmp, const int nc[3], int cap, cudaStream_t s);
 cudaError_t launch_classify_cells(const float2* cells, long long ncells, const int* tf_prefix, int tf_w,
                                   int mode, float value_lo, float idx_scale, float iso,
                                   unsigned char* occ, cudaStream_t s);

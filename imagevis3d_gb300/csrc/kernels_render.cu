@@ -53,11 +53,16 @@ __device__ __forceinline__ float ldv(const float* p) { return __ldg(p); }
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
 
+// A brick as the sampler sees it: voxel (gx, gy, gz) of the level (a cell
+// inside the brick's stored box) is element base + gx s0 + gy s1 + gz s2 of
+// the pool in the frame's layout copy; the texture coordinate of its centre
+// is g + t.
 struct BrickView {
-  unsigned long long off;  // element offset of the brick in the pool
+  long long base;
+  int s0, s1, s2;
   unsigned long long tex;
-  int ox, oy, oz, sx, sy, sz;
-  int lox, loy, loz, hix, hiy, hiz;
+  float tx, ty, tz;
+  int lox, loy, loz, hix, hiy, hiz;  // interior (membership of sample cells)
 };
 
 __device__ __forceinline__ void load_brick(const FrameDesc& f, int bi, BrickView& b) {
@@ -66,10 +71,15 @@ __device__ __forceinline__ void load_brick(const FrameDesc& f, int bi, BrickView
   const int4 w1 = __ldg(reinterpret_cast<const int4*>(B) + 1);  // ox oy oz sx
   const int4 w2 = __ldg(reinterpret_cast<const int4*>(B) + 2);  // sy sz lox loy
   const int4 w3 = __ldg(reinterpret_cast<const int4*>(B) + 3);  // loz hix hiy hiz
-  b.off = ((unsigned long long)(unsigned)w0.y << 32) | (unsigned)w0.x;
+  const long long off = (long long)(((unsigned long long)(unsigned)w0.y << 32) | (unsigned)w0.x);
   b.tex = ((unsigned long long)(unsigned)w0.w << 32) | (unsigned)w0.z;
-  b.ox = w1.x; b.oy = w1.y; b.oz = w1.z; b.sx = w1.w;
-  b.sy = w2.x; b.sz = w2.y; b.lox = w2.z; b.loy = w2.w;
+  const int ox = w1.x, oy = w1.y, oz = w1.z, sx = w1.w, sy = w2.x, sz = w2.y;
+  if (f.perm == 0) { b.s0 = 1; b.s1 = sx; b.s2 = sx * sy; }
+  else if (f.perm == 1) { b.s1 = 1; b.s2 = sy; b.s0 = sy * sz; }
+  else { b.s2 = 1; b.s0 = sz; b.s1 = sz * sx; }
+  b.base = (long long)f.copy_off + off - ((long long)ox * b.s0 + (long long)oy * b.s1 + (long long)oz * b.s2);
+  b.tx = 0.5f - (float)ox; b.ty = 0.5f - (float)oy; b.tz = 0.5f - (float)oz;
+  b.lox = w2.z; b.loy = w2.w;
   b.loz = w3.x; b.hix = w3.y; b.hiy = w3.z; b.hiz = w3.w;
 }
 
@@ -104,25 +114,21 @@ __device__ __forceinline__ Cell make_cell(const FrameDesc& f, float px, float py
 template <typename T, int SAMPLER>
 __device__ __forceinline__ float sample_cell(const FrameDesc& f, const BrickView& b, int gx, int gy, int gz, float fx,
                                              float fy, float fz) {
-  const int ix = gx - b.ox, iy = gy - b.oy, iz = gz - b.oz;
   if (SAMPLER == SAMPLER_TEX) {
     cudaTextureObject_t tex = (cudaTextureObject_t)b.tex;
     if (f.interp)
-      return tex3D<float>(tex, (float)ix + (fx + 0.5f), (float)iy + (fy + 0.5f), (float)iz + (fz + 0.5f)) *
+      return tex3D<float>(tex, ((float)gx + b.tx) + fx, ((float)gy + b.ty) + fy, ((float)gz + b.tz) + fz) *
              VoxelTraits<T>::tex_scale;
-    return tex3D<float>(tex, (float)(ix + (fx >= 0.5f)) + 0.5f, (float)(iy + (fy >= 0.5f)) + 0.5f,
-                        (float)(iz + (fz >= 0.5f)) + 0.5f) * VoxelTraits<T>::tex_scale;
+    return tex3D<float>(tex, (float)(gx + (fx >= 0.5f)) + b.tx, (float)(gy + (fy >= 0.5f)) + b.ty,
+                        (float)(gz + (fz >= 0.5f)) + b.tz) * VoxelTraits<T>::tex_scale;
   }
-  const T* base = reinterpret_cast<const T*>(f.pool) + f.copy_off + (size_t)b.off;
-  // element strides of the x, y, z axes in the selected layout copy
-  int s0, s1, s2;
-  if (f.perm == 0) { s0 = 1; s1 = b.sx; s2 = b.sx * b.sy; }
-  else if (f.perm == 1) { s1 = 1; s2 = b.sy; s0 = b.sy * b.sz; }
-  else { s2 = 1; s0 = b.sz; s1 = b.sz * b.sx; }
+  const T* pool = reinterpret_cast<const T*>(f.pool);
   if (!f.interp)
-    return ldv(base + (iz + (fz >= 0.5f)) * s2 + (iy + (fy >= 0.5f)) * s1 + (ix + (fx >= 0.5f)) * s0);
-  const T* p0 = base + iz * s2 + iy * s1 + ix * s0;
-  const T* p1 = p0 + s2;
+    return ldv(pool + (b.base + (long long)(gz + (fz >= 0.5f)) * b.s2 + (long long)(gy + (fy >= 0.5f)) * b.s1 +
+                       (long long)(gx + (fx >= 0.5f)) * b.s0));
+  const T* p0 = pool + (b.base + (long long)gz * b.s2 + (long long)gy * b.s1 + (long long)gx * b.s0);
+  const T* p1 = p0 + b.s2;
+  const int s0 = b.s0, s1 = b.s1;
   float v000 = ldv(p0), v100 = ldv(p0 + s0), v010 = ldv(p0 + s1), v110 = ldv(p0 + s1 + s0);
   float v001 = ldv(p1), v101 = ldv(p1 + s0), v011 = ldv(p1 + s1), v111 = ldv(p1 + s1 + s0);
   float c00 = fmaf(fx, v100 - v000, v000);
@@ -344,26 +350,32 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
       }
       int ke = bke;
       if (f.empty_skip >= 2) {
-        // Macro-cell run, estimated from the cell's exit planes only: a
-        // sample that rounding places in a neighbouring cell lies within a
-        // voxel of this one, and the cell's min/max covers one voxel beyond
-        // its samples' footprints, so skipping an empty run never drops a
-        // contributing sample; sampling a run that spills over is harmless.
+        // Macro-cells: occ holds, per cell, the Chebyshev distance (in
+        // cells, capped) to the nearest cell that may contribute; 0 = this
+        // cell may contribute.  From an empty cell at distance d the ray may
+        // leave the whole cube of 2d-1 cells around it without sampling.
+        // Runs are estimated from exit planes only: a sample that rounding
+        // places across a face lies within a voxel of it, and every cell's
+        // min/max covers one voxel beyond its samples' footprints, so no
+        // contributing sample is ever skipped; sampling past a face is
+        // harmless.
         const int cx = max(gx, 0) >> sh, cy = max(gy, 0) >> sh, cz = max(gz, 0) >> sh;
-        const float hx = (float)min((cx + 1) << sh, f.dims[0]), lx = (float)(cx << sh);
-        const float hy = (float)min((cy + 1) << sh, f.dims[1]), ly = (float)(cy << sh);
-        const float hz = (float)min((cz + 1) << sh, f.dims[2]), lz = (float)(cz << sh);
+        const size_t ci = ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx;
+        const int d = __ldg(f.occ + ci);
+        const int lo_c = d > 0 ? d - 1 : 0;  // cube = cells [c - lo_c, c + lo_c]
+        const float lx = (float)(max(cx - lo_c, 0) << sh), hx = (float)min((cx + lo_c + 1) << sh, f.dims[0]);
+        const float ly = (float)(max(cy - lo_c, 0) << sh), hy = (float)min((cy + lo_c + 1) << sh, f.dims[1]);
+        const float lz = (float)(max(cz - lo_c, 0) << sh), hz = (float)min((cz + lo_c + 1) << sh, f.dims[2]);
         float te = fminf(fminf(r.dv[0] > 0.f ? (hx - r.ov[0]) * r.inv[0] : (r.dv[0] < 0.f ? (lx - r.ov[0]) * r.inv[0] : INFINITY),
                                r.dv[1] > 0.f ? (hy - r.ov[1]) * r.inv[1] : (r.dv[1] < 0.f ? (ly - r.ov[1]) * r.inv[1] : INFINITY)),
                          r.dv[2] > 0.f ? (hz - r.ov[2]) * r.inv[2] : (r.dv[2] < 0.f ? (lz - r.ov[2]) * r.inv[2] : INFINITY));
         const float kef = ceilf((te - t0) * inv_dt - 0.5f);
-        const int cke = kef >= (float)ke ? ke : max(k + 1, (int)kef);
-        const size_t ci = ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx;
-        ke = cke;
-        if (!__ldg(f.occ + ci)) {
-          k = ke;
+        if (d > 0) {
+          k = kef >= (float)K ? K : max(k + 1, (int)kef);
+          if (k >= bke) bi = -1;
           continue;
         }
+        ke = kef >= (float)ke ? ke : max(k + 1, (int)kef);
         if (f.cell_touched) {
           // algorithmic-bytes accounting: one bit per sampled cell
           unsigned* w = f.cell_touched + (ci >> 5);
@@ -559,6 +571,67 @@ cudaError_t launch_count_bits(const unsigned* bits, long long words, int n, unsi
   if (n <= 0 || words <= 0) return cudaSuccess;
   dim3 grid((unsigned)std::min<long long>((words + 255) / 256, 64), (unsigned)n);
   k_count_bits<<<grid, 256, 0, s>>>(bits, words, counts);
+  return cudaGetLastError();
+}
+
+__global__ void k_occ_to_dist(const unsigned char* __restrict__ occ, unsigned char* __restrict__ d, long long n, int cap) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    d[i] = occ[i] ? 0 : (unsigned char)cap;
+}
+
+// Chebyshev distance transform of the macro-cell occupancy, one relaxation
+// pass per launch: d'(c) = 0 if c may contribute, else min(cap, 1 + min over
+// the 26 neighbours of d(n)); `cap` passes give the exact capped distance.
+__global__ void k_cell_distance(const unsigned char* __restrict__ in, unsigned char* __restrict__ out, int nx, int ny,
+                                int nz, int cap) {
+  const long long n = (long long)nx * ny * nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nx);
+    const long long t = i / nx;
+    const int y = (int)(t % ny), z = (int)(t / ny);
+    int d = __ldg(in + i);
+    if (d == 0) { out[i] = 0; continue; }
+    int m = cap;
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int zz = z + dz;
+      if (zz < 0 || zz >= nz) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int yy = y + dy;
+        if (yy < 0 || yy >= ny) continue;
+        const unsigned char* row = in + ((long long)zz * ny + yy) * nx;
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int xx = x + dx;
+          if (xx < 0 || xx >= nx) continue;
+          m = min(m, (int)__ldg(row + xx));
+        }
+      }
+    }
+    out[i] = (unsigned char)min(cap, m + 1);
+  }
+}
+
+cudaError_t launch_cell_distance(unsigned char* occ, unsigned char* tmp, const int nc[3], int cap, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  const long long n = (long long)nc[0] * nc[1] * nc[2];
+  if (n <= 0) return cudaSuccess;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  // occ enters as 1 = may contribute, 0 = empty; convert to distances
+  // (0 = may contribute, cap = empty) in tmp, then relax back and forth
+  k_occ_to_dist<<<(unsigned)blocks, 256, 0, s>>>(occ, tmp, n, cap);
+  unsigned char* a = tmp;
+  unsigned char* b = occ;
+  for (int p = 0; p < cap; ++p) {
+    k_cell_distance<<<(unsigned)blocks, 256, 0, s>>>(a, b, nc[0], nc[1], nc[2], cap);
+    unsigned char* t = a;
+    a = b;
+    b = t;
+  }
+  // result must end in occ
+  if (a != occ) {
+    cudaError_t e = cudaMemcpyAsync(occ, a, (size_t)n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
   return cudaGetLastError();
 }
 

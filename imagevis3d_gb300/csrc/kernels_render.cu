@@ -384,28 +384,15 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
         }
       }
       if (MODE == MODE_1D) {
-        // two samples per iteration: both footprints are fetched before
-        // either is composited
-        for (; k + 1 < ke; k += 2) {
-          float ax, ay, az, bx, by, bz;
-          pos_of(k, ax, ay, az);
-          pos_of(k + 1, bx, by, bz);
-          const Cell ca = make_cell(f, ax, ay, az), cb = make_cell(f, bx, by, bz);
-          const float va = sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz);
-          const float vb = sample_cell<T, SAMPLER>(f, b, cb.x, cb.y, cb.z, cb.fx, cb.fy, cb.fz);
-          ++nsamp;
-          if (composite<MODE>(f, tf1d(f, va), acc)) { done = true; break; }
-          ++nsamp;
-          if (composite<MODE>(f, tf1d(f, vb), acc)) { done = true; break; }
-        }
-        if (!done && k < ke) {
+        for (; k < ke; ++k) {
           float ax, ay, az;
           pos_of(k, ax, ay, az);
           const Cell ca = make_cell(f, ax, ay, az);
           ++nsamp;
-          if (composite<MODE>(f, tf1d(f, sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz)), acc))
+          if (composite<MODE>(f, tf1d(f, sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz)), acc)) {
             done = true;
-          ++k;
+            break;
+          }
         }
         continue;
       }
@@ -491,7 +478,7 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
 constexpr int RENDER_THREADS = 128;
 
 template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS, 7) k_render_plain(const __grid_constant__ FrameDesc f) {
+__global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_plain(const __grid_constant__ FrameDesc f) {
   int warp = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (warp >= f.tiles_x * f.tiles_y) return;
   render_tile<T, MODE, SAMPLER>(f, warp);
@@ -509,7 +496,7 @@ __device__ __forceinline__ int find_frame(const int* __restrict__ prefix, int nf
 }
 
 template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS, 7) k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
+__global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
                                                          const int* __restrict__ tile_prefix, int total,
                                                          int* __restrict__ counter) {
   const int lane = threadIdx.x & 31;

@@ -257,7 +257,7 @@ def main():
         brick_bytes += st["brick_bytes"]
     barrier()
     clk = clocks.stop()
-    # algorithmic bytes: distinct non-empty 8^3 macro-cells each view samples
+    # algorithmic bytes: distinct non-empty 4^3 macro-cells each view samples
     # (one untimed pass with the per-cell bitmap enabled)
     r.setStatsLevel(2)
     r.paintBatch(views)
@@ -367,7 +367,7 @@ def main():
                        "samples_per_voxel": wl.spv, "lod": 0, "tf_entries": 4096,
                        "sampler": "fp32 software trilinear",
                        "brick_layouts": "x/y/z-fastest copies, chosen per view",
-                       "empty_skipping": "bricks + 8^3 macro-cells",
+                       "empty_skipping": "bricks + 4^3 macro-cells with a distance field",
                        "l2": "inputs larger than L2 (brick pool %.2f GB)" % (info["device_bytes"] / 1e9),
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "gsamples_per_s": gs,
@@ -383,7 +383,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic_from_profile(),
                          "kernel": "k_render_persistent<uint16,1D,SW>",
                          "bytes_per_launch": cell_bytes_per_launch,
-                         "bytes_rule": "sum over views of distinct non-empty 8^3 macro-cells sampled x 8^3 x 2 B",
+                         "bytes_rule": "sum over views of distinct non-empty 8^3 macro-cells sampled x 4^3 x 2 B",
                          "brick_bytes_per_launch": brick_bytes / args.steps,
                          "kernel_ms": 1000.0 * ksec / args.steps,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if pk else "fallback"},

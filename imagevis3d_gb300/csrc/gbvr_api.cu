@@ -200,7 +200,7 @@ struct Level {
 
 // macro-cell edge (voxels) for empty-space skipping inside bricks, and the
 // cap of the empty-cell distance field
-constexpr int CELL_SHIFT = 3;
+constexpr int CELL_SHIFT = 2;
 constexpr int CELL_DIST_CAP = 16;
 
 struct Dataset {

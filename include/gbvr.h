@@ -123,7 +123,7 @@ typedef struct gbvr_stats {
   double gpu_ms;               /* device time of the last paint (CUDA events) */
   double kernel_ms;            /* device time of its raycast kernel launch(es) alone */
   uint64_t cells_touched;      /* stats level 2: sum over views of distinct non-empty macro-cells sampled */
-  uint64_t cell_bytes;         /* ... times the cell's voxel bytes (8^3 voxels) */
+  uint64_t cell_bytes;         /* ... times the cell's voxel bytes (4^3 voxels) */
 } gbvr_stats;
 
 /* ---- errors / device ---- */
@@ -190,7 +190,8 @@ int gbvr_set_launch_shape(gbvr_renderer* r, int tile_w, int ctas_per_sm);
 
 /* Empty-space skipping: 0 none (every sample is evaluated), 1 whole bricks
  * classified empty by their min/max against the TF, 2 (default) also
- * 8^3-voxel macro-cells inside bricks, the finer acceleration grid of the
+ * 4^3-voxel macro-cells inside bricks (jumping whole empty cubes by a
+ * distance field over them), the finer acceleration grid of the
  * reference's GridLeaper renderer type (RenderWindowGL.cpp:176-188).  All
  * three give identical pixels: a skipped region contributes exactly zero. */
 int gbvr_set_empty_skipping(gbvr_renderer* r, int mode);

@@ -383,7 +383,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic_from_profile(),
                          "kernel": "k_render_persistent<uint16,1D,SW>",
                          "bytes_per_launch": cell_bytes_per_launch,
-                         "bytes_rule": "sum over views of distinct non-empty 8^3 macro-cells sampled x 4^3 x 2 B",
+                         "bytes_rule": "sum over views of distinct non-empty 4^3 macro-cells sampled x 4^3 x 2 B",
                          "brick_bytes_per_launch": brick_bytes / args.steps,
                          "kernel_ms": 1000.0 * ksec / args.steps,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if pk else "fallback"},

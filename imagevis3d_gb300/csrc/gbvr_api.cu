@@ -292,7 +292,8 @@ void plan_level(const long long dims[3], int brick, int ghost, int level, Level&
         b.hix = hi[0]; b.hiy = hi[1]; b.hiz = hi[2];
         b.level = level;
         b.offset = cursor;
-        unsigned long long n = (unsigned long long)s[0] * s[1] * s[2];
+        // room for the 4x4x4-blocked copy too (stored dims rounded up to 4)
+        unsigned long long n = (unsigned long long)((s[0] + 3) & ~3) * ((s[1] + 3) & ~3) * ((s[2] + 3) & ~3);
         const unsigned long long al = elem_align(dtype);
         cursor += (n + al - 1) / al * al;
         bricks.push_back(b);
@@ -370,9 +371,11 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   }
   ds.stored_bytes = 0;
   for (auto& b : ds.bricks) ds.stored_bytes += (uint64_t)b.sx * b.sy * b.sz * es;
-  ds.layouts = (bp && bp->layouts == 3) ? 3 : 1;
+  // layout copies: 1 = x-fastest only; 3 = + y- and z-fastest; 4 = + 4^3-blocked
+  ds.layouts = (bp && (bp->layouts == 3 || bp->layouts == 4)) ? bp->layouts : 1;
   ds.copy_stride = cursor;
-  CUDA_TRY(ds.pool.alloc(cursor * es * ds.layouts));
+  const int ncopies = ds.layouts == 4 ? 2 : ds.layouts;
+  CUDA_TRY(ds.pool.alloc(cursor * es * ncopies));
   CUDA_TRY(ds.d_bricks.alloc(sizeof(BrickInfo) * ds.bricks.size()));
   CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyHostToDevice, s));
   for (size_t l = 0; l < ld.size(); ++l) {
@@ -382,9 +385,11 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
     L.cells = std::make_shared<DevBuf>();
     CUDA_TRY(L.cells->alloc(sizeof(float2) * (size_t)L.nc[0] * L.nc[1] * L.nc[2]));
     CUDA_TRY(launch_cell_minmax(lv[l]->p, dtype, d, CELL_SHIFT, L.nc, L.cells->as<float2>(), s));
-    for (int perm = 0; perm < ds.layouts; ++perm)
+    for (int c = 0; c < (ds.layouts == 4 ? 2 : ds.layouts); ++c) {
+      const int perm = (ds.layouts == 4 && c == 1) ? 3 : c;
       CUDA_TRY(launch_gather_bricks(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks,
-                                    (char*)ds.pool.p + (size_t)perm * cursor * es, perm, s));
+                                    (char*)ds.pool.p + (size_t)c * cursor * es, perm, s));
+    }
   }
   CUDA_TRY(launch_brick_minmax(ds.pool.p, dtype, ds.d_bricks.as<BrickInfo>(), (int)ds.bricks.size(), s));
   CUDA_TRY(cudaMemcpyAsync(ds.bricks.data(), ds.d_bricks.p, sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyDeviceToHost, s));
@@ -683,14 +688,16 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
   // layout copy: the axis whose voxel-space extent along screen x is largest
   // (row 0 of the view matrix is the camera's right vector in world space)
   f.perm = 0;
-  if (ds.layouts == 3) {
+  if (ds.layouts == 4) {
+    f.perm = 3;  // blocked copy, independent of the view direction
+  } else if (ds.layouts == 3) {
     double best = -1;
     for (int a = 0; a < 3; ++a) {
       double w = std::fabs((double)view[a] * f.vox_scale[a]);
       if (w > best) { best = w; f.perm = a; }
     }
   }
-  f.copy_off = (unsigned long long)f.perm * ds.copy_stride;
+  f.copy_off = (unsigned long long)(f.perm == 3 ? 1 : f.perm) * ds.copy_stride;
   const size_t npix = (size_t)r->width * r->height;
   f.out_rgba8 = r->d_fb8.as<uchar4>() + (size_t)vidx * npix;
   f.out_f32 = r->d_fb32.p ? r->d_fb32.as<float4>() + (size_t)vidx * npix : nullptr;

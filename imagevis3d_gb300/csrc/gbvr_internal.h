@@ -85,7 +85,7 @@ struct __align__(16) FrameDesc {
   int nc[3];                 // macro-cell grid of the level
   int cell_shift;            // macro-cell edge = 1 << cell_shift voxels
   int tile_w;                // ray tile of one warp: tile_w x (32 / tile_w) pixels
-  int perm;                  // brick layout copy: 0 x-fastest, 1 y-fastest, 2 z-fastest
+  int perm;                  // brick layout copy: 0 x-fastest, 1 y-fastest, 2 z-fastest, 3 4^3 blocks
   unsigned long long copy_off;  // element offset of that copy in the pool
   // outputs
   uchar4* out_rgba8;         // may be null
@@ -139,7 +139,8 @@ cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], 
                                cudaStream_t s);
 cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3], void* out,
                               cudaStream_t s);
-// perm: 0 stores x fastest, 1 y fastest (then z, x), 2 z fastest (then x, y)
+// perm: 0 stores x fastest, 1 y fastest (then z, x), 2 z fastest (then x, y),
+// 3 in 4x4x4 blocks of 64 contiguous voxels (x fastest within and between blocks)
 cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3],
                                  const BrickInfo* bricks_dev, int nbricks, void* pool,
                                  int perm, cudaStream_t s);

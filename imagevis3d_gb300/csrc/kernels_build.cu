@@ -154,20 +154,26 @@ __global__ void k_gather(const T* __restrict__ level, long long X, long long Y, 
                          const BrickInfo* __restrict__ bricks, T* __restrict__ pool, int perm) {
   const BrickInfo b = bricks[blockIdx.y];
   const long long plane = (long long)b.sx * b.sy;
-  // destination strides of x, y, z in this layout copy
-  long long s0, s1, s2;
+  // destination strides of x, y, z in this layout copy (perm 3: 4^3 blocks,
+  // each 64 voxels contiguous with x fastest, blocks in x, y, z order)
+  long long s0 = 0, s1 = 0, s2 = 0;
   if (perm == 0) { s0 = 1; s1 = b.sx; s2 = (long long)b.sx * b.sy; }
   else if (perm == 1) { s1 = 1; s2 = b.sy; s0 = (long long)b.sy * b.sz; }
-  else { s2 = 1; s0 = b.sz; s1 = (long long)b.sz * b.sx; }
+  else if (perm == 2) { s2 = 1; s0 = b.sz; s1 = (long long)b.sz * b.sx; }
+  const long long nbx = (b.sx + 3) >> 2, nby = (b.sy + 3) >> 2;
   for (int zs = blockIdx.x; zs < b.sz; zs += gridDim.x) {
-    T* dst = pool + b.offset + zs * s2;
     const long long z = min(max((long long)b.oz + zs, 0LL), Z - 1);
     for (long long i = threadIdx.x; i < plane; i += blockDim.x) {
       long long r = i / b.sx, xs = i - r * b.sx;
       // ghosts outside the level replicate its edge voxels
       const long long y = min(max((long long)b.oy + r, 0LL), Y - 1);
       const long long x = min(max((long long)b.ox + xs, 0LL), X - 1);
-      dst[xs * s0 + r * s1] = __ldg(level + (z * Y + y) * X + x);
+      long long di;
+      if (perm == 3)
+        di = ((((long long)(zs >> 2) * nby + (r >> 2)) * nbx + (xs >> 2)) << 6) + ((zs & 3) << 4) + ((r & 3) << 2) + (xs & 3);
+      else
+        di = xs * s0 + r * s1 + zs * s2;
+      pool[b.offset + di] = __ldg(level + (z * Y + y) * X + x);
     }
   }
 }

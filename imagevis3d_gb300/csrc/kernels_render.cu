@@ -58,8 +58,9 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v,
 // the pool in the frame's layout copy; the texture coordinate of its centre
 // is g + t.
 struct BrickView {
-  long long base;
-  int s0, s1, s2;
+  long long base;    // perm 3: element offset of the brick's first block
+  int s0, s1, s2;    // perm 3: 64 * blocks per row, 64 * blocks per slab (s1, s2)
+  int ox, oy, oz;    // perm 3: stored origin
   unsigned long long tex;
   float tx, ty, tz;
   int lox, loy, loz, hix, hiy, hiz;  // interior (membership of sample cells)
@@ -74,10 +75,18 @@ __device__ __forceinline__ void load_brick(const FrameDesc& f, int bi, BrickView
   const long long off = (long long)(((unsigned long long)(unsigned)w0.y << 32) | (unsigned)w0.x);
   b.tex = ((unsigned long long)(unsigned)w0.w << 32) | (unsigned)w0.z;
   const int ox = w1.x, oy = w1.y, oz = w1.z, sx = w1.w, sy = w2.x, sz = w2.y;
-  if (f.perm == 0) { b.s0 = 1; b.s1 = sx; b.s2 = sx * sy; }
-  else if (f.perm == 1) { b.s1 = 1; b.s2 = sy; b.s0 = sy * sz; }
-  else { b.s2 = 1; b.s0 = sz; b.s1 = sz * sx; }
-  b.base = (long long)f.copy_off + off - ((long long)ox * b.s0 + (long long)oy * b.s1 + (long long)oz * b.s2);
+  b.ox = ox; b.oy = oy; b.oz = oz;
+  if (f.perm == 3) {
+    b.s0 = 64;
+    b.s1 = ((sx + 3) >> 2) << 6;
+    b.s2 = b.s1 * ((sy + 3) >> 2);
+    b.base = (long long)f.copy_off + off;
+  } else {
+    if (f.perm == 0) { b.s0 = 1; b.s1 = sx; b.s2 = sx * sy; }
+    else if (f.perm == 1) { b.s1 = 1; b.s2 = sy; b.s0 = sy * sz; }
+    else { b.s2 = 1; b.s0 = sz; b.s1 = sz * sx; }
+    b.base = (long long)f.copy_off + off - ((long long)ox * b.s0 + (long long)oy * b.s1 + (long long)oz * b.s2);
+  }
   b.tx = 0.5f - (float)ox; b.ty = 0.5f - (float)oy; b.tz = 0.5f - (float)oz;
   b.lox = w2.z; b.loy = w2.w;
   b.loz = w3.x; b.hix = w3.y; b.hiy = w3.z; b.hiz = w3.w;
@@ -123,6 +132,31 @@ __device__ __forceinline__ float sample_cell(const FrameDesc& f, const BrickView
                         (float)(gz + (fz >= 0.5f)) + b.tz) * VoxelTraits<T>::tex_scale;
   }
   const T* pool = reinterpret_cast<const T*>(f.pool);
+  if (f.perm == 3) {
+    // 4^3 blocks: voxel (lx, ly, lz) of the stored box sits in block
+    // (l >> 2) at position (lz & 3) 16 + (ly & 3) 4 + (lx & 3)
+    int lx = gx - b.ox, ly = gy - b.oy, lz = gz - b.oz;
+    if (!f.interp) {
+      lx += fx >= 0.5f; ly += fy >= 0.5f; lz += fz >= 0.5f;
+      return ldv(pool + (b.base + (long long)(lz >> 2) * b.s2 + (ly >> 2) * b.s1 + ((lx >> 2) << 6) +
+                         (((lz & 3) << 4) | ((ly & 3) << 2) | (lx & 3))));
+    }
+    const T* p0 = pool + (b.base + (long long)(lz >> 2) * b.s2 + (ly >> 2) * b.s1 + ((lx >> 2) << 6) +
+                          (((lz & 3) << 4) | ((ly & 3) << 2) | (lx & 3)));
+    const int dx = (lx & 3) == 3 ? 61 : 1;
+    const int dy = (ly & 3) == 3 ? b.s1 - 12 : 4;
+    const int dz = (lz & 3) == 3 ? b.s2 - 48 : 16;
+    const T* p1 = p0 + dz;
+    float v000 = ldv(p0), v100 = ldv(p0 + dx), v010 = ldv(p0 + dy), v110 = ldv(p0 + dy + dx);
+    float v001 = ldv(p1), v101 = ldv(p1 + dx), v011 = ldv(p1 + dy), v111 = ldv(p1 + dy + dx);
+    float c00 = fmaf(fx, v100 - v000, v000);
+    float c10 = fmaf(fx, v110 - v010, v010);
+    float c01 = fmaf(fx, v101 - v001, v001);
+    float c11 = fmaf(fx, v111 - v011, v011);
+    float c0 = fmaf(fy, c10 - c00, c00);
+    float c1 = fmaf(fy, c11 - c01, c01);
+    return fmaf(fz, c1 - c0, c0);
+  }
   if (!f.interp)
     return ldv(pool + (b.base + (long long)(gz + (fz >= 0.5f)) * b.s2 + (long long)(gy + (fy >= 0.5f)) * b.s1 +
                        (long long)(gx + (fx >= 0.5f)) * b.s0));

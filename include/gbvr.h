@@ -83,7 +83,9 @@ typedef struct gbvr_brick_params {
   int32_t build_texture;/* also build 3D textures for GBVR_SAMPLER_TEX */
   int32_t layouts;      /* 1: bricks stored x-fastest only; 3: also y- and z-fastest
                            copies (3x device memory), each view samples the copy
-                           whose fastest axis is closest to its screen x axis */
+                           whose fastest axis is closest to its screen x axis;
+                           4: also a copy in 4x4x4 voxel blocks (2x memory),
+                           sampled by every view */
   int32_t reserved;
   double aspect[3];     /* voxel spacing; 0 = (1,1,1) */
 } gbvr_brick_params;

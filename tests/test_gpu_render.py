@@ -248,14 +248,14 @@ def test_layout_copies_and_launch_shapes_do_not_change_pixels(multibrick):
     views = workloads.orbit_views(4, 96, 80, elevation=35.0, start=10.0)
     views.append(orbit_camera(0.0, 89.0, 2.5 * workloads.DIAG, 45.0, 96, 80))  # looking down y
     imgs = {}
-    for layouts in (1, 3):
+    for layouts in (1, 3, 4):
         with Renderer(float_fb=True) as r:
             r.loadVolume(vol, brick_size=64, overlap=2, layouts=layouts)
             r.resize((96, 80))
             r.set1DTrans(tf)
             r.setValueRange(0.0, 4095.0)
             r.setSampleRateModifier(1.5)
-            for tw in ((8, 16, 32, 4) if layouts == 3 else (8,)):
+            for tw in ((8, 16, 32, 4) if layouts == 3 else (8, 4)):
                 r.setLaunchShape(tw, 0)
                 r.paintBatch(views)
                 imgs[(layouts, tw)] = [r.readFramebuffer(i, as_float=True) for i in range(len(views))]

@@ -219,7 +219,7 @@ def main():
     mine = shard(len(wl.views), rank, world)
     views = [wl.views[i] for i in mine]
     r = Renderer()
-    r.loadSynthetic(wl.synth, **wl.brick, build_texture=not args.no_texture, layouts=3)
+    r.loadSynthetic(wl.synth, **wl.brick, build_texture=not args.no_texture, layouts=4)
     r.resize((wl.width, wl.height))
     r.set1DTrans(wl.tf)
     r.setValueRange(*wl.value_range)
@@ -366,7 +366,7 @@ def main():
                        "views": len(wl.views), "width": wl.width, "height": wl.height,
                        "samples_per_voxel": wl.spv, "lod": 0, "tf_entries": 4096,
                        "sampler": "fp32 software trilinear",
-                       "brick_layouts": "x/y/z-fastest copies, chosen per view",
+                       "brick_layouts": "4x4x4-blocked copy (plus the x-fastest copy)",
                        "empty_skipping": "bricks + 4^3 macro-cells with a distance field",
                        "l2": "inputs larger than L2 (brick pool %.2f GB)" % (info["device_bytes"] / 1e9),
                        "parallelism": "replicas" if world > 1 else "1 GPU"},

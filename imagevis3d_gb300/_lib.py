@@ -130,6 +130,7 @@ SIGNATURES = {
     "gbvr_dev_hist1d": [P, I, C.c_int64, P, I, P],
     "gbvr_dev_hist2d": [P, I, I64P, D, C.c_int64, C.c_int64, P, FP, P],
     "gbvr_dev_downsample": [P, I, I64P, P, P],
+    "gbvr_dev_synth_volume_noalloc": [C.POINTER(SynthParams), P, SZ, P],
     "gbvr_orbit_camera": [F, F, F, F, I, I, FP, FP],
     "gbvr_uvf_inspect": [CP, I, C.POINTER(UvfSummary)],
     "gbvr_uvf_read_volume": [CP, P, SZ],

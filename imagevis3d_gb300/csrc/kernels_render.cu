@@ -417,7 +417,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
           if (!(*(volatile unsigned*)w & bit)) atomicOr(w, bit);
         }
       }
-      if (MODE == MODE_1D) {
+      if constexpr (MODE == MODE_1D) {
         for (; k < ke; ++k) {
           float ax, ay, az;
           pos_of(k, ax, ay, az);
@@ -428,8 +428,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
             break;
           }
         }
-        continue;
-      }
+      } else {
       for (; k < ke; ++k) {
         pos_of(k, px, py, pz);
         const Cell c = make_cell(f, px, py, pz);
@@ -477,6 +476,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
           cl.x = lit[0]; cl.y = lit[1]; cl.z = lit[2];
         }
         if (composite<MODE>(f, cl, acc)) { done = true; break; }
+      }
       }
     }
   }

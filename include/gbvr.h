@@ -272,6 +272,25 @@ int gbvr_dev_hist2d(const void* dev_vol, int dtype, const int64_t dims[3], doubl
 int gbvr_dev_downsample(const void* dev_in, int dtype, const int64_t dims[3], void* dev_out,
                         void* stream);
 
+/* ---- seeded synthesis into caller-owned device memory, allocating nothing.
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they call: a host application that owns the GPU memory budget
+ * and hands out only pre-allocated buffers, or code issuing work beside other
+ * streams, where cudaFree (and often cudaMalloc) would synchronise the whole
+ * device.  Same volume as gbvr_synth_volume, written to dev_out (a device
+ * pointer of at least X*Y*Z*element bytes) on `stream` (a cudaStream_t, or
+ * null for the default stream); the call returns once the work is queued.
+ * The generator's tables go through a fixed device array of
+ * GBVR_NOALLOC_SYNTH_MAX_FLOATS floats (1 MiB, held on every GPU that loads
+ * the library until the process exits): parameters needing more than
+ * nblobs * (1 + X + Y + Z) + X + Y + Z <= that many floats are rejected with
+ * GBVR_EINVAL.  The first call on a device sets the array up there (it loads
+ * the library's device code and resolves the array's address), so make one
+ * call on each device before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (different streams, no ordering) race. */
+#define GBVR_NOALLOC_SYNTH_MAX_FLOATS 262144
+int gbvr_dev_synth_volume_noalloc(const gbvr_synth_params* p, void* dev_out, size_t bytes, void* stream);
+
 /* Orbit camera around the volume centre: the rotation the 360-degree capture
  * applies per frame (ImageVis3D_Capturing.cpp:170 fAngle = i/N * 360,
  * RenderWindow.cpp:207-214 RotationY).  Eye at radius (world units, the

@@ -122,6 +122,8 @@ SIGNATURES = {
     "gbvr_read_framebuffer": [P, I, P, SZ],
     "gbvr_read_framebuffer_f32": [P, I, P, SZ],
     "gbvr_capture_single_frame": [P, CP, I],
+    "gbvr_capture_view": [P, I, CP, I],
+    "gbvr_load_tf1d_file": [CP, I, FP, I, C.POINTER(I)],
     "gbvr_get_stats": [P, C.POINTER(Stats)],
     "gbvr_set_stats_level": [P, I],
     "gbvr_synth_volume": [C.POINTER(SynthParams), P, SZ],

@@ -1355,6 +1355,17 @@ int gbvr_capture_single_frame(gbvr_renderer* r, const char* path, int preserve_t
   return GBVR_OK;
 }
 
+int gbvr_capture_view(gbvr_renderer* r, int view, const char* path, int preserve_transparency) {
+  TRY(check_r(r));
+  if (!path) return fail(GBVR_EINVAL, "null path");
+  if (view < 0 || view >= r->last_views) return fail(GBVR_EINVAL, "view index out of range");
+  std::vector<uint8_t> px((size_t)r->fb_w * r->fb_h * 4);
+  TRY(gbvr_read_framebuffer(r, view, px.data(), px.size()));
+  if (!write_image(path, px.data(), r->fb_w, r->fb_h, preserve_transparency != 0))
+    return fail(GBVR_EIO, std::string("cannot write ") + path);
+  return GBVR_OK;
+}
+
 int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out) {
   TRY(check_r(r));
   if (!out) return fail(GBVR_EINVAL, "null stats");

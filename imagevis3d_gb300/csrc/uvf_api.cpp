@@ -1,7 +1,9 @@
 // Host-only UVF entry points of the C ABI (the UVFReader inspection tool and
 // a raster writer); they touch no GPU.
+#include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/gbvr.h"
 #include "uvf.h"
@@ -114,6 +116,34 @@ int gbvr_uvf_write_raster(const char* path, const char* raster_id, const void* v
   std::string msg;
   int rc = uvf_write(path, s, msg);
   if (rc) return set_error(rc, msg);
+  return GBVR_OK;
+}
+
+int gbvr_load_tf1d_file(const char* path, int target_size, float* rgba_out, int capacity, int* n_out) {
+  if (!path || !rgba_out || capacity <= 0) return set_error(GBVR_EINVAL, "bad argument");
+  FILE* f = fopen(path, "r");
+  if (!f) return set_error(GBVR_EIO, std::string("cannot open ") + path);
+  long n = 0;
+  std::vector<float> t;
+  bool ok = fscanf(f, "%ld", &n) == 1 && n > 0 && n <= (1 << 20);
+  if (ok) {
+    t.resize(4 * (size_t)n);
+    for (long i = 0; ok && i < 4 * n; ++i) ok = fscanf(f, "%f", &t[i]) == 1;
+  }
+  fclose(f);
+  if (!ok) return set_error(GBVR_EFORMAT, std::string("not a 1D transfer function file: ") + path);
+  const long m = target_size > 0 ? target_size : n;
+  if (m > capacity) return set_error(GBVR_EINVAL, "capacity below the table size");
+  for (long j = 0; j < m; ++j) {
+    // linear resampling: entry j sits at position j (n - 1) / (m - 1)
+    double pos = m > 1 ? (double)j * (double)(n - 1) / (double)(m - 1) : 0.0;
+    long i0 = (long)pos;
+    if (i0 > n - 1) i0 = n - 1;
+    long i1 = i0 + 1 < n ? i0 + 1 : n - 1;
+    double w = pos - (double)i0;
+    for (int c = 0; c < 4; ++c) rgba_out[4 * j + c] = (float)((1.0 - w) * t[4 * i0 + c] + w * t[4 * i1 + c]);
+  }
+  if (n_out) *n_out = (int)m;
   return GBVR_OK;
 }
 

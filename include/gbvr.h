@@ -229,6 +229,9 @@ int gbvr_paint_views(gbvr_renderer* r, const gbvr_view* views, int n);
 int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t bytes);
 int gbvr_read_framebuffer_f32(gbvr_renderer* r, int view, float* rgba, size_t bytes);
 int gbvr_capture_single_frame(gbvr_renderer* r, const char* path, int preserve_transparency);
+/* capture view i of the last paint (the capture-sequence frames of
+ * ImageVis3D_Capturing.cpp:188 / RenderWindow.cpp:1718-1725) */
+int gbvr_capture_view(gbvr_renderer* r, int view, const char* path, int preserve_transparency);
 int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out);
 /* What paint records for gbvr_get_stats: 0 sample counts only, 1 (default)
  * also the bricks each view touched, 2 also the macro-cells each view
@@ -298,6 +301,14 @@ int gbvr_dev_synth_volume_noalloc(const gbvr_synth_params* p, void* dev_out, siz
  * plane, looking at the origin with +y up; perspective fov_deg vertical. */
 int gbvr_orbit_camera(float azimuth_deg, float elevation_deg, float radius, float fov_deg, int width,
                       int height, float view[16], float proj[16]);
+
+/* ---- transfer-function files (host only) ----
+ * .1dt: first token N, then N lines "r g b a" (DemoData/c60.1dt), the format
+ * TransferFunction1D::Load reads (Q1DTransferFunction.cpp:573-588).  With
+ * target_size > 0 the table is resampled linearly to that many entries (as
+ * loadFromFileWithSize does for the dataset's histogram size); 0 keeps N.
+ * Writes at most `capacity` entries and the count to *n_out. */
+int gbvr_load_tf1d_file(const char* path, int target_size, float* rgba_out, int capacity, int* n_out);
 
 /* ---- host-only UVF inspection (the UVFReader tool, UVFReader/main.cpp:23-205,
  * UVFReader/BlockInfo.h:27-401).  No GPU is used. ---- */

@@ -7,5 +7,6 @@ library is missing the binding raises instead of falling back.
 from ._lib import (GbvrError, GBVR_U8, GBVR_U16, GBVR_F32, GBVR_CUDA_RAYCASTER,  # noqa: F401
                    GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE, GBVR_NEAREST,
                    GBVR_LINEAR, GBVR_SAMPLER_SW, GBVR_SAMPLER_TEX, lib)
-from .renderer import Renderer, brick_params, orbit_camera, synth_params, synth_volume  # noqa: F401
+from .renderer import (Renderer, brick_params, fbm_params, fbm_volume, orbit_camera, synth_params,  # noqa: F401
+                       synth_volume)
 from . import workloads  # noqa: F401

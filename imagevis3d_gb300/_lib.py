@@ -63,6 +63,12 @@ class SynthParams(C.Structure):
                 ("noise_kind", C.c_int32), ("noise_amp", C.c_float), ("vmax", C.c_float)]
 
 
+class FbmParams(C.Structure):
+    _fields_ = [("dims", C.c_int64 * 3), ("dtype", C.c_int32), ("seed", C.c_uint32),
+                ("octaves", C.c_int32), ("base_period", C.c_int32), ("threshold", C.c_float),
+                ("vmax", C.c_float)]
+
+
 class UvfSummary(C.Structure):
     _fields_ = [("version", C.c_uint64), ("checksum_semantic", C.c_uint64),
                 ("checksum", C.c_uint8 * 16), ("checksum_verified", C.c_int32),
@@ -128,6 +134,8 @@ SIGNATURES = {
     "gbvr_set_stats_level": [P, I],
     "gbvr_synth_volume": [C.POINTER(SynthParams), P, SZ],
     "gbvr_load_synthetic": [P, C.POINTER(SynthParams), C.POINTER(BrickParams)],
+    "gbvr_synth_fbm_volume": [C.POINTER(FbmParams), P, SZ],
+    "gbvr_load_synthetic_fbm": [P, C.POINTER(FbmParams), C.POINTER(BrickParams)],
     "gbvr_build_uvf": [P, I64P, I, C.POINTER(BrickParams), CP],
     "gbvr_dev_hist1d": [P, I, C.c_int64, P, I, P],
     "gbvr_dev_hist2d": [P, I, I64P, D, C.c_int64, C.c_int64, P, FP, P],

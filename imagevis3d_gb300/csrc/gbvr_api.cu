@@ -1033,6 +1033,44 @@ int gbvr_synth_volume(const gbvr_synth_params* p, void* host_out, size_t bytes) 
   return GBVR_OK;
 }
 
+static int check_fbm(const gbvr_fbm_params* p) {
+  if (!p || p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 ||
+      p->octaves < 1 || p->octaves > 12 || p->base_period < 1 || (long long)p->base_period << (p->octaves - 1) > 65535 ||
+      !(p->threshold < 1.0f))
+    return fail(GBVR_EINVAL, "bad fractal-volume parameters");
+  return GBVR_OK;
+}
+
+int gbvr_synth_fbm_volume(const gbvr_fbm_params* p, void* host_out, size_t bytes) {
+  TRY(check_fbm(p));
+  if (!host_out) return fail(GBVR_EINVAL, "null output");
+  const size_t need = (size_t)p->dims[0] * p->dims[1] * p->dims[2] * dtype_size(p->dtype);
+  if (bytes < need) return fail(GBVR_EINVAL, "output buffer too small");
+  gbvr_renderer tmp;
+  CUDA_TRY(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking));
+  DevBuf lv;
+  CUDA_TRY(lv.alloc(need));
+  long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
+  CUDA_TRY(launch_synth_fbm(d, p->dtype, p->seed, p->octaves, p->base_period, p->threshold, p->vmax, lv.p, tmp.stream));
+  CUDA_TRY(cudaMemcpyAsync(host_out, lv.p, need, cudaMemcpyDeviceToHost, tmp.stream));
+  CUDA_TRY(cudaStreamSynchronize(tmp.stream));
+  return GBVR_OK;
+}
+
+int gbvr_load_synthetic_fbm(gbvr_renderer* r, const gbvr_fbm_params* p, const gbvr_brick_params* bp) {
+  TRY(check_r(r));
+  TRY(check_fbm(p));
+  long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
+  DevBuf lv;
+  CUDA_TRY(lv.alloc((size_t)d[0] * d[1] * d[2] * dtype_size(p->dtype)));
+  CUDA_TRY(launch_synth_fbm(d, p->dtype, p->seed, p->octaves, p->base_period, p->threshold, p->vmax, lv.p, r->stream));
+  r->drop_graphs();
+  r->skip_dirty = true;
+  r->tf_dirty = true;
+  TRY(build_dataset(r->ds, lv, p->dtype, d, bp, r->stream));
+  return GBVR_OK;
+}
+
 int gbvr_load_uvf(gbvr_renderer* r, const char* path, int verify, const gbvr_brick_params* bp) {
   TRY(check_r(r));
   if (!path) return fail(GBVR_EINVAL, "null path");

@@ -137,6 +137,8 @@ struct BlobTablesDev {
 };
 cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], int dtype, void* out,
                                cudaStream_t s);
+cudaError_t launch_synth_fbm(const long long dims[3], int dtype, uint32_t seed, int octaves, int base_period,
+                             float thr, float vmax, void* out, cudaStream_t s);
 cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3], void* out,
                               cudaStream_t s);
 // perm: 0 stores x fastest, 1 y fastest (then z, x), 2 z fastest (then x, y),

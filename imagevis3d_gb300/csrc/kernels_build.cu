@@ -130,6 +130,91 @@ static int grid_for(long long n, int threads) {
   return (int)(b < 1 ? 1 : b);
 }
 
+// ---------------------------------------------------------------------------
+// Seeded fractal (fBm) volume: octaves of periodic value noise with
+// lowbias32-hashed lattice values (C. Wellons, 2018), smoothstep trilinear
+// weights, weight 2^-o per octave; normalised, thresholded, scaled.  Each
+// step is one round-to-nearest float32 operation in the order of the CPU
+// restatement, so both produce the same bits.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+__device__ __forceinline__ float fbm_lat(uint32_t i, uint32_t j, uint32_t k, uint32_t P, uint32_t salt) {
+  return __fmul_rn((float)(lowbias32(((k * P + j) * P + i) ^ salt) >> 8), 1.0f / 16777216.0f);
+}
+
+__device__ __forceinline__ float fbm_lerp(float a, float b, float t) {
+  return __fadd_rn(a, __fmul_rn(__fsub_rn(b, a), t));
+}
+
+template <typename T>
+__global__ void k_synth_fbm(long long X, long long Y, long long Z, uint32_t seed, int octaves, int base_period,
+                            float thr, float vmax, T* __restrict__ out) {
+  const long long n = X * Y * Z;
+  const long long dims[3] = {X, Y, Z};
+  const float inv = __fdiv_rn(1.0f, __fsub_rn(1.0f, thr));
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long x = idx % X, t0 = idx / X, y = t0 % Y, z = t0 / Y;
+    const long long c[3] = {x, y, z};
+    float acc = 0.0f, norm = 0.0f, amp = 1.0f;
+    for (int o = 0; o < octaves; ++o) {
+      const uint32_t P = (uint32_t)base_period << o;
+      const uint32_t salt = seed + 0x9E3779B9u * (uint32_t)(o + 1);
+      uint32_t i0[3], i1[3];
+      float s[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float scale = __fdiv_rn((float)P, (float)dims[a]);
+        const float u = __fmul_rn(__fadd_rn((float)c[a], 0.5f), scale);
+        const float f = floorf(u);
+        const float t = __fsub_rn(u, f);
+        s[a] = __fmul_rn(__fmul_rn(t, t), __fsub_rn(3.0f, __fadd_rn(t, t)));
+        const uint32_t ii = (uint32_t)(long long)f % P;
+        i0[a] = ii;
+        i1[a] = (ii + 1) % P;
+      }
+      const float c00 = fbm_lerp(fbm_lat(i0[0], i0[1], i0[2], P, salt), fbm_lat(i1[0], i0[1], i0[2], P, salt), s[0]);
+      const float c10 = fbm_lerp(fbm_lat(i0[0], i1[1], i0[2], P, salt), fbm_lat(i1[0], i1[1], i0[2], P, salt), s[0]);
+      const float c01 = fbm_lerp(fbm_lat(i0[0], i0[1], i1[2], P, salt), fbm_lat(i1[0], i0[1], i1[2], P, salt), s[0]);
+      const float c11 = fbm_lerp(fbm_lat(i0[0], i1[1], i1[2], P, salt), fbm_lat(i1[0], i1[1], i1[2], P, salt), s[0]);
+      const float v = fbm_lerp(fbm_lerp(c00, c10, s[1]), fbm_lerp(c01, c11, s[1]), s[2]);
+      acc = __fadd_rn(acc, __fmul_rn(amp, v));
+      norm = __fadd_rn(norm, amp);
+      amp = __fmul_rn(amp, 0.5f);
+    }
+    float v = __fdiv_rn(acc, norm);
+    v = __fmul_rn(__fsub_rn(v, thr), inv);
+    v = fminf(fmaxf(v, 0.0f), 1.0f);
+    v = __fmul_rn(v, vmax);
+    if (sizeof(T) == 4) out[idx] = (T)v;
+    else out[idx] = (T)rintf(v);
+  }
+}
+
+cudaError_t launch_synth_fbm(const long long dims[3], int dtype, uint32_t seed, int octaves, int base_period,
+                             float thr, float vmax, void* out, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  const long long n = dims[0] * dims[1] * dims[2];
+  int threads = 256;
+  int blocks = grid_for(n, threads);
+  if (dtype == DT_U8)
+    k_synth_fbm<uint8_t><<<blocks, threads, 0, s>>>(dims[0], dims[1], dims[2], seed, octaves, base_period, thr, vmax, (uint8_t*)out);
+  else if (dtype == DT_U16)
+    k_synth_fbm<uint16_t><<<blocks, threads, 0, s>>>(dims[0], dims[1], dims[2], seed, octaves, base_period, thr, vmax, (uint16_t*)out);
+  else
+    k_synth_fbm<float><<<blocks, threads, 0, s>>>(dims[0], dims[1], dims[2], seed, octaves, base_period, thr, vmax, (float*)out);
+  return cudaGetLastError();
+}
+
+
 cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3], void* out, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   long long OX = (dims[0] + 1) / 2, OY = (dims[1] + 1) / 2, OZ = (dims[2] + 1) / 2;

@@ -55,6 +55,27 @@ def synth_params(dims, dtype, seed, nblobs, sigma, amp, scale, noise_kind=0, noi
     return p
 
 
+def fbm_params(dims, dtype, seed, octaves=6, base_period=2, threshold=0.58, vmax=255.0):
+    p = L.FbmParams()
+    for i in range(3):
+        p.dims[i] = int(dims[i])
+    p.dtype = _DT[np.dtype(dtype)]
+    p.seed = seed
+    p.octaves = octaves
+    p.base_period = base_period
+    p.threshold = threshold
+    p.vmax = vmax
+    return p
+
+
+def fbm_volume(params):
+    """Generate a seeded fractal volume on the GPU; returns a (z, y, x) array."""
+    dims = [params.dims[i] for i in range(3)]
+    out = np.empty((dims[2], dims[1], dims[0]), _NP[params.dtype])
+    L.call("gbvr_synth_fbm_volume", C.byref(params), out.ctypes.data_as(C.c_void_p), out.nbytes)
+    return out
+
+
 def orbit_camera(azimuth_deg, elevation_deg, radius, fov_deg, width, height):
     """View and projection (row-major float32 4x4) of an orbit camera."""
     v = np.zeros(16, np.float32)
@@ -112,7 +133,10 @@ class Renderer:
                C.byref(brick_params(**bp)))
 
     def loadSynthetic(self, params, **bp):
-        L.call("gbvr_load_synthetic", self._h, C.byref(params), C.byref(brick_params(**bp)))
+        if isinstance(params, L.FbmParams):
+            L.call("gbvr_load_synthetic_fbm", self._h, C.byref(params), C.byref(brick_params(**bp)))
+        else:
+            L.call("gbvr_load_synthetic", self._h, C.byref(params), C.byref(brick_params(**bp)))
 
     def datasetInfo(self):
         info = L.DatasetInfo()

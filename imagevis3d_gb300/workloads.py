@@ -11,7 +11,7 @@ import math
 
 import numpy as np
 
-from .renderer import orbit_camera, synth_params
+from .renderer import fbm_params, orbit_camera, synth_params
 
 SEED = 20261203
 DIAG = math.sqrt(3.0)  # diagonal of the unit-normalised cube
@@ -35,9 +35,10 @@ def tf1d_seeded(n, seed, zero_below, value_max, points=4):
     return tf
 
 
-def tf2d_seeded(w, h, seed, widgets=3):
+def tf2d_seeded(w, h, seed, widgets=3, zero_cols=0):
     """w x h RGBA table over (value, gradient magnitude) with seeded Gaussian
-    ellipse widgets; row = gradient bin, column = value bin."""
+    ellipse widgets; row = gradient bin, column = value bin.  The first
+    `zero_cols` value columns are transparent (empty space stays empty)."""
     rng = np.random.default_rng(seed)
     x = (np.arange(w) + 0.5) / w
     y = (np.arange(h) + 0.5) / h
@@ -52,6 +53,7 @@ def tf2d_seeded(w, h, seed, widgets=3):
         for c in range(3):
             tf[..., c] = np.maximum(tf[..., c], col[c] * (g > 1e-3))
         tf[..., 3] = np.maximum(tf[..., 3], np.where(g > 1e-3, g, 0.0))
+    tf[:, :zero_cols, 3] = 0.0
     return tf.astype(np.float32)
 
 
@@ -105,3 +107,20 @@ def config2(size=1024, width=1920, height=1080, nviews=64, brick=256, seed=SEED 
     return Workload("c2_%dcube_u16_%dbrick_%dx%d_x%d" % (size, brick, width, height, nviews), sp,
                     dict(brick_size=brick, overlap=2), tf, 1.5, width, height, views,
                     value_range=(0.0, 4095.0))
+
+
+def config3(size=2048, width=2560, height=1440, nviews=16, brick=256, seed=SEED + 3):
+    """size^3 uint8 seeded fractal: 6-octave periodic value-noise fBm,
+    thresholded to sparse structures (~70% of 256^3 bricks empty at 2048^3);
+    2D TF 256 x 256 over (value, |gradient|) with 3 seeded Gaussian-ellipse
+    widgets and Phong (1 light); isosurface mode at 3 seeded isovalues;
+    2560 x 1440 orbit views, 1 sample / voxel."""
+    fp = fbm_params((size, size, size), np.uint8, seed, octaves=6, base_period=2, threshold=0.58, vmax=255.0)
+    tf = tf2d_seeded(256, 256, seed, widgets=3, zero_cols=8)
+    views = orbit_views(nviews, width, height)
+    isos = [float(v) for v in np.sort(np.random.default_rng(seed).uniform(40.0, 160.0, 3))]
+    wl = Workload("c3_%dcube_u8_fbm_%dx%d_x%d" % (size, width, height, nviews), fp,
+                  dict(brick_size=brick, overlap=2), tf, 1.0, width, height, views,
+                  value_range=(0.0, 255.0), mode=1)
+    wl.isovalues = isos
+    return wl

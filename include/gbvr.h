@@ -261,6 +261,24 @@ typedef struct gbvr_synth_params {
 int gbvr_synth_volume(const gbvr_synth_params* p, void* host_out, size_t bytes);
 int gbvr_load_synthetic(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr_brick_params* bp);
 
+/* Seeded fractal volume: `octaves` octaves of periodic value noise (lattice
+ * of base_period << o cells per axis at octave o, hashed lattice values,
+ * smoothstep trilinear, weight 2^-o), normalised to [0, 1], then
+ * v = clamp((f - threshold) / (1 - threshold), 0, 1) * vmax: sparse
+ * structures in empty space. */
+typedef struct gbvr_fbm_params {
+  int64_t dims[3];
+  int32_t dtype;
+  uint32_t seed;
+  int32_t octaves;
+  int32_t base_period;
+  float threshold;
+  float vmax;
+} gbvr_fbm_params;
+
+int gbvr_synth_fbm_volume(const gbvr_fbm_params* p, void* host_out, size_t bytes);
+int gbvr_load_synthetic_fbm(gbvr_renderer* r, const gbvr_fbm_params* p, const gbvr_brick_params* bp);
+
 /* ---- GPU UVF build without a renderer (uvfconvert, CmdLineConverter/main.cpp:406-408):
  * host volume in, UVF v2 file out. ---- */
 int gbvr_build_uvf(const void* host, const int64_t dims[3], int dtype, const gbvr_brick_params* bp,

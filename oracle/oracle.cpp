@@ -391,6 +391,90 @@ void orc_synth_blobs(const orc_blob_tables* t, const i64 dims[3], int dt, void* 
 }
 
 // ---------------------------------------------------------------------------
+// Seeded fractal (fBm) volume: `octaves` octaves of periodic value noise.
+// Octave o has a lattice of P = base_period << o cells across every axis,
+// lattice values from the integer hash "lowbias32" (C. Wellons, 2018) of the
+// wrapped lattice index, smoothstep-weighted trilinear interpolation, and
+// weight 2^-o; the sum is normalised, thresholded and scaled:
+//   v = clamp((fbm - thr) / (1 - thr), 0, 1) * vmax, rounded to nearest.
+// Every step is a single float32 operation in a fixed order.
+// ---------------------------------------------------------------------------
+static inline uint32_t lowbias32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+static inline float fbm_lattice(uint32_t i, uint32_t j, uint32_t k, uint32_t P, uint32_t salt) {
+  uint32_t h = lowbias32(((k * P + j) * P + i) ^ salt);
+  return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
+static inline float fbm_lerp(float a, float b, float t) {
+  float d = b - a;
+  d = d * t;
+  return a + d;
+}
+
+float orc_fbm_value(const i64 dims[3], uint32_t seed, int octaves, int base_period, i64 x, i64 y, i64 z) {
+  float acc = 0.0f, norm = 0.0f, amp = 1.0f;
+  const i64 c[3] = {x, y, z};
+  for (int o = 0; o < octaves; ++o) {
+    const uint32_t P = (uint32_t)base_period << o;
+    const uint32_t salt = seed + 0x9E3779B9u * (uint32_t)(o + 1);
+    uint32_t i0[3], i1[3];
+    float s[3];
+    for (int a = 0; a < 3; ++a) {
+      float scale = (float)P / (float)dims[a];
+      float u = (float)c[a] + 0.5f;
+      u = u * scale;
+      float f = std::floor(u);
+      float t = u - f;
+      float tt = t * t;
+      float w = 3.0f - (t + t);
+      s[a] = tt * w;
+      uint32_t ii = (uint32_t)(i64)f % P;
+      i0[a] = ii;
+      i1[a] = (ii + 1) % P;
+    }
+    float c00 = fbm_lerp(fbm_lattice(i0[0], i0[1], i0[2], P, salt), fbm_lattice(i1[0], i0[1], i0[2], P, salt), s[0]);
+    float c10 = fbm_lerp(fbm_lattice(i0[0], i1[1], i0[2], P, salt), fbm_lattice(i1[0], i1[1], i0[2], P, salt), s[0]);
+    float c01 = fbm_lerp(fbm_lattice(i0[0], i0[1], i1[2], P, salt), fbm_lattice(i1[0], i0[1], i1[2], P, salt), s[0]);
+    float c11 = fbm_lerp(fbm_lattice(i0[0], i1[1], i1[2], P, salt), fbm_lattice(i1[0], i1[1], i1[2], P, salt), s[0]);
+    float c0 = fbm_lerp(c00, c10, s[1]);
+    float c1 = fbm_lerp(c01, c11, s[1]);
+    float n = fbm_lerp(c0, c1, s[2]);
+    acc = acc + amp * n;
+    norm = norm + amp;
+    amp = amp * 0.5f;
+  }
+  return acc / norm;
+}
+
+void orc_synth_fbm(const i64 dims[3], int dt, uint32_t seed, int octaves, int base_period, float thr, float vmax,
+                   void* out) {
+  const i64 X = dims[0], Y = dims[1], Z = dims[2];
+  const float inv = 1.0f / (1.0f - thr);
+#pragma omp parallel for schedule(static)
+  for (i64 z = 0; z < Z; ++z)
+    for (i64 y = 0; y < Y; ++y)
+      for (i64 x = 0; x < X; ++x) {
+        float f = orc_fbm_value(dims, seed, octaves, base_period, x, y, z);
+        float v = f - thr;
+        v = v * inv;
+        v = std::min(std::max(v, 0.0f), 1.0f);
+        v = v * vmax;
+        i64 idx = (z * Y + y) * X + x;
+        if (dt == DT_F32) ((float*)out)[idx] = v;
+        else if (dt == DT_U8) ((uint8_t*)out)[idx] = (uint8_t)std::nearbyint(v);
+        else ((uint16_t*)out)[idx] = (uint16_t)std::nearbyint(v);
+      }
+}
+
+// ---------------------------------------------------------------------------
 // FP64 raycaster: the project's sampling rule, evaluated directly on the flat
 // volume of the rendered LOD (no bricks: the bricked GPU walk must reproduce
 // sampling of the whole level, since ghost voxels are exact copies).

@@ -194,3 +194,14 @@ def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0)
 
 def max_threads():
     return lib().orc_max_threads()
+
+
+def synth_fbm(params):
+    """CPU restatement of the seeded fractal generator (gbvr_fbm_params)."""
+    dims = [params.dims[i] for i in range(3)]
+    dt = {0: np.uint8, 1: np.uint16, 2: np.float32}[params.dtype]
+    out = np.empty((dims[2], dims[1], dims[0]), dt)
+    lib().orc_synth_fbm((I64 * 3)(*dims), params.dtype, C.c_uint32(params.seed), params.octaves,
+                        params.base_period, C.c_float(params.threshold), C.c_float(params.vmax),
+                        out.ctypes.data_as(C.c_void_p))
+    return out

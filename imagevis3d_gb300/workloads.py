@@ -35,7 +35,7 @@ def tf1d_seeded(n, seed, zero_below, value_max, points=4):
     return tf
 
 
-def tf2d_seeded(w, h, seed, widgets=3, zero_cols=0):
+def tf2d_seeded(w, h, seed, widgets=3, zero_cols=0, x_range=(0.25, 0.85)):
     """w x h RGBA table over (value, gradient magnitude) with seeded Gaussian
     ellipse widgets; row = gradient bin, column = value bin.  The first
     `zero_cols` value columns are transparent (empty space stays empty)."""
@@ -45,7 +45,7 @@ def tf2d_seeded(w, h, seed, widgets=3, zero_cols=0):
     X, Y = np.meshgrid(x, y)
     tf = np.zeros((h, w, 4), np.float64)
     for _ in range(widgets):
-        cx, cy = rng.uniform(0.25, 0.85), rng.uniform(0.1, 0.6)
+        cx, cy = rng.uniform(*x_range), rng.uniform(0.1, 0.6)
         sx, sy = rng.uniform(0.03, 0.12), rng.uniform(0.08, 0.3)
         col = rng.uniform(0.2, 1.0, 3)
         amax = rng.uniform(0.3, 0.9)
@@ -116,9 +116,9 @@ def config3(size=2048, width=2560, height=1440, nviews=16, brick=256, seed=SEED 
     widgets and Phong (1 light); isosurface mode at 3 seeded isovalues;
     2560 x 1440 orbit views, 1 sample / voxel."""
     fp = fbm_params((size, size, size), np.uint8, seed, octaves=6, base_period=2, threshold=0.58, vmax=255.0)
-    tf = tf2d_seeded(256, 256, seed, widgets=3, zero_cols=8)
+    tf = tf2d_seeded(256, 256, seed, widgets=3, zero_cols=8, x_range=(0.05, 0.45))
     views = orbit_views(nviews, width, height)
-    isos = [float(v) for v in np.sort(np.random.default_rng(seed).uniform(40.0, 160.0, 3))]
+    isos = [float(v) for v in np.sort(np.random.default_rng(seed).uniform(12.0, 48.0, 3))]
     wl = Workload("c3_%dcube_u8_fbm_%dx%d_x%d" % (size, width, height, nviews), fp,
                   dict(brick_size=brick, overlap=2), tf, 1.0, width, height, views,
                   value_range=(0.0, 255.0), mode=1)

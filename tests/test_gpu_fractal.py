@@ -22,6 +22,8 @@ def test_fbm_generator_bit_exact(orc, dims, dtype):
 @pytest.fixture(scope="module")
 def fractal(orc):
     wl = workloads.config3(size=160, width=160, height=120, nviews=4)
+    # closer cameras than the benchmark's so the sparse structures fill the small frames
+    wl.views = workloads.orbit_views(4, 160, 120, radius=1.5 * workloads.DIAG, start=20.0)
     vol = orc.synth_fbm(wl.synth)
     assert np.array_equal(fbm_volume(wl.synth), vol)
     return wl, vol

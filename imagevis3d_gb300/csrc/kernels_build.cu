@@ -380,10 +380,19 @@ __global__ void k_hist1d_smem(const T* __restrict__ v, long long n, unsigned lon
   extern __shared__ unsigned sh[];
   for (int i = threadIdx.x; i < nbins; i += blockDim.x) sh[i] = 0;
   __syncthreads();
+  unsigned run_bin = 0xffffffffu, run = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     unsigned b = (unsigned)__ldg(v + i);
-    if (b < (unsigned)nbins) atomicAdd(sh + b, 1u);
+    if (b >= (unsigned)nbins) continue;
+    if (b == run_bin) {
+      ++run;  // runs of one value (empty space) cost no shared-memory atomic
+    } else {
+      if (run) atomicAdd(sh + run_bin, run);
+      run_bin = b;
+      run = 1;
+    }
   }
+  if (run) atomicAdd(sh + run_bin, run);
   __syncthreads();
   for (int i = threadIdx.x; i < nbins; i += blockDim.x)
     if (sh[i]) atomicAdd(hist + i, (unsigned long long)sh[i]);
@@ -513,6 +522,7 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
   const long long n = X * Y * Z;
   const unsigned long long smax = sc->smax;
   const double gmax = __longlong_as_double((long long)sc->gmax_bits);
+  unsigned long long run_bin = ~0ULL, run = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     long long x = i % X, t = i / X, y = t % Y, z = t / Y;
     int D[3];
@@ -535,12 +545,19 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
     }
     long long bx = (long long)__ldg(v + i) / merge;
     if (bx >= nx) bx = nx - 1;
-    // warp-aggregated increment: empty space puts most voxels in one bin
+    // run-length accumulation per thread: empty space puts almost every
+    // voxel in one bin, and one atomic per voxel (or per warp) on a single
+    // address serialises
     const unsigned long long bin = (unsigned long long)(bx * 256 + k);
-    const unsigned active = __activemask();
-    const unsigned peers = __match_any_sync(active, bin);
-    if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(hist + bin, (unsigned long long)__popc(peers));
+    if (bin == run_bin) {
+      ++run;
+    } else {
+      if (run) atomicAdd(hist + run_bin, run);
+      run_bin = bin;
+      run = 1;
+    }
   }
+  if (run) atomicAdd(hist + run_bin, run);
 }
 
 cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], double max_scalar, long long nx,

@@ -9,4 +9,5 @@ from ._lib import (GbvrError, GBVR_U8, GBVR_U16, GBVR_F32, GBVR_CUDA_RAYCASTER, 
                    GBVR_LINEAR, GBVR_SAMPLER_SW, GBVR_SAMPLER_TEX, lib)
 from .renderer import (Renderer, brick_params, fbm_params, fbm_volume, orbit_camera, synth_params,  # noqa: F401
                        synth_volume)
+from .server import Server  # noqa: F401
 from . import workloads  # noqa: F401

@@ -19,7 +19,7 @@ GBVR_FLAG_FLOAT_FB = 1
 
 ERRORS = {
     -1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EIO", -5: "EFORMAT",
-    -6: "ECHECKSUM", -7: "ESTATE", -8: "EOVERSIZED",
+    -6: "ECHECKSUM", -7: "ESTATE", -8: "EOVERSIZED", -9: "ETIMEOUT",
 }
 
 
@@ -53,6 +53,27 @@ class Stats(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("tile_w", C.c_int32), ("ctas_per_sm", C.c_int32), ("candidates", C.c_int32),
                 ("best_ms", C.c_float), ("default_ms", C.c_float)]
+
+
+class ServerParams(C.Structure):
+    _fields_ = [("max_batch", C.c_int32), ("tile_w", C.c_int32), ("fb_budget_bytes", C.c_uint64)]
+
+
+class Request(C.Structure):
+    _fields_ = [("dataset", C.c_int32), ("tf", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+                ("view", C.c_float * 16), ("proj", C.c_float * 16), ("samples_per_voxel", C.c_float),
+                ("reserved", C.c_int32), ("out_rgba8", C.c_void_p)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batch_size", C.c_int32), ("batch", C.c_uint64),
+                ("latency_ms", C.c_double), ("queue_ms", C.c_double), ("gpu_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("batches", C.c_uint64),
+                ("mean_batch", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("max_ms", C.c_double), ("frames_per_s", C.c_double)]
 
 
 class SynthParams(C.Structure):
@@ -142,6 +163,15 @@ SIGNATURES = {
     "gbvr_dev_downsample": [P, I, I64P, P, P],
     "gbvr_dev_synth_volume_noalloc": [C.POINTER(SynthParams), P, SZ, P],
     "gbvr_orbit_camera": [F, F, F, F, I, I, FP, FP],
+    "gbvr_server_create": [C.POINTER(ServerParams), C.POINTER(P)],
+    "gbvr_server_destroy": [P],
+    "gbvr_server_add_volume": [P, P, I64P, I, C.POINTER(BrickParams), C.POINTER(I)],
+    "gbvr_server_add_synthetic": [P, C.POINTER(SynthParams), C.POINTER(BrickParams), C.POINTER(I)],
+    "gbvr_server_add_tf": [P, I, I, FP, I, I, F, F, FP, D, D, C.POINTER(I)],
+    "gbvr_server_submit": [P, C.POINTER(Request), C.POINTER(C.c_uint64)],
+    "gbvr_server_wait": [P, C.c_uint64, D, C.POINTER(RequestResult)],
+    "gbvr_server_get_stats": [P, C.POINTER(ServerStats)],
+    "gbvr_server_reset_stats": [P],
     "gbvr_uvf_inspect": [CP, I, C.POINTER(UvfSummary)],
     "gbvr_uvf_read_volume": [CP, P, SZ],
     "gbvr_uvf_read_hist1d": [CP, U64P, SZ],

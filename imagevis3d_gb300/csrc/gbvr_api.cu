@@ -444,6 +444,174 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   return GBVR_OK;
 }
 
+
+// Classify one level of a dataset against a transfer function: per brick a
+// skip byte (d_skip, indexed by global brick number) and per macro-cell the
+// capped distance to a cell that may contribute (d_occ).  tf: RGBA rows of w
+// entries, h rows.  Blocks until done (the host prefix table is temporary).
+int classify_level(const Dataset& ds, int level, const std::vector<float>& tf, int w, int h, int mode, double lo,
+                   double hi, float iso, DevBuf& d_tfprefix, DevBuf& d_skip, DevBuf& d_occ, DevBuf& d_occtmp,
+                   cudaStream_t s) {
+  const Level& L = ds.levels[level];
+  CUDA_TRY(d_skip.alloc(ds.bricks.size()));
+  const size_t ncell = (size_t)L.nc[0] * L.nc[1] * L.nc[2];
+  CUDA_TRY(d_occ.alloc(ncell));
+  // prefix count of TF columns with any non-zero alpha
+  std::vector<int> pre(w + 1, 0);
+  for (int x = 0; x < w; ++x) {
+    int nz = 0;
+    for (int y = 0; y < h && !nz; ++y) nz = tf[4 * ((size_t)y * w + x) + 3] != 0.f;
+    pre[x + 1] = pre[x] + nz;
+  }
+  CUDA_TRY(d_tfprefix.alloc(sizeof(int) * pre.size()));
+  CUDA_TRY(cudaMemcpyAsync(d_tfprefix.p, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, s));
+  const float idx_scale = (float)((w - 1) / (hi - lo));
+  CUDA_TRY(launch_classify_bricks(ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks, d_tfprefix.as<int>(), w, mode,
+                                  (float)lo, idx_scale, iso, d_skip.as<unsigned char>() + L.brick_base, s));
+  CUDA_TRY(launch_classify_cells(L.cells->as<float2>(), (long long)ncell, d_tfprefix.as<int>(), w, mode, (float)lo,
+                                 idx_scale, iso, d_occ.as<unsigned char>(), s));
+  CUDA_TRY(d_occtmp.alloc(ncell));
+  CUDA_TRY(launch_cell_distance(d_occ.as<unsigned char>(), d_occtmp.as<unsigned char>(), L.nc, CELL_DIST_CAP, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return GBVR_OK;
+}
+
+
+// Generate a seeded blob volume into a new device buffer (tables built on
+// the host, combined on the device in a fixed float32 order).
+int synth_to_device(const gbvr_synth_params* p, DevBuf& lv, cudaStream_t s) {
+  if (!p || p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 || p->nblobs < 0)
+    return fail(GBVR_EINVAL, "bad synthetic parameters");
+  BlobTablesHost t;
+  make_blob_tables(*p, t);
+  DevBuf amp, ex, ey, ez, bx, by, bz;
+  auto up = [&](DevBuf& d, const std::vector<float>& v) -> cudaError_t {
+    cudaError_t e = d.alloc(sizeof(float) * std::max<size_t>(v.size(), 1));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(d.p, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice, s);
+  };
+  CUDA_TRY(up(amp, t.amp));
+  CUDA_TRY(up(ex, t.ex));
+  CUDA_TRY(up(ey, t.ey));
+  CUDA_TRY(up(ez, t.ez));
+  CUDA_TRY(up(bx, t.bgx));
+  CUDA_TRY(up(by, t.bgy));
+  CUDA_TRY(up(bz, t.bgz));
+  long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
+  CUDA_TRY(lv.alloc((size_t)d[0] * d[1] * d[2] * dtype_size(p->dtype)));
+  const bool bg = p->bg_freq > 0;
+  BlobTablesDev td{p->nblobs, amp.as<float>(), ex.as<float>(), ey.as<float>(), ez.as<float>(),
+                   bg ? bx.as<float>() : nullptr, bg ? by.as<float>() : nullptr, bg ? bz.as<float>() : nullptr,
+                   p->bg_level, p->bg_amp, p->scale, p->noise_amp, p->noise_kind, p->vmax, p->seed};
+  CUDA_TRY(launch_synth_blobs(td, d, p->dtype, lv.p, s));
+  // the tables are freed on return: wait for the kernel that reads them
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return GBVR_OK;
+}
+
+// Everything a frame needs besides its outputs.
+struct FrameParams {
+  const float* view;
+  const float* proj;
+  int width, height;
+  float spv;
+  int level;
+  int mode, interp, sampler;
+  float ert;
+  float iso;
+  float iso_rgb[3];
+  int lighting;
+  float amb[3], diff[3], spec[3], shininess, light_dir[3], bg[3];
+  int tile_w, empty_skip;
+  const float4* tf;
+  int tf_w, tf_h;
+  double lo, hi;
+  float grad_max;
+  const unsigned char* skip;  // per brick of the dataset (all levels)
+  const unsigned char* occ;   // per macro-cell of `level`
+};
+
+void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
+  memset(&f, 0, sizeof(f));
+  const Level& L = ds.levels[p.level];
+  f.pool = ds.pool.p;
+  f.bricks = ds.d_bricks.as<BrickInfo>() + L.brick_base;
+  f.skip = p.skip + L.brick_base;
+  f.dtype = ds.dtype;
+  f.sampler = p.sampler;
+  double ext[3], mx = 0;
+  for (int a = 0; a < 3; ++a) {
+    ext[a] = (double)ds.dims[a] * ds.aspect[a];
+    mx = std::max(mx, ext[a]);
+  }
+  long long maxd = 0;
+  for (int a = 0; a < 3; ++a) {
+    ext[a] /= mx;
+    f.dims[a] = (int)L.dims[a];
+    f.nb[a] = L.nb[a];
+    f.vox_scale[a] = (float)((double)L.dims[a] / ext[a]);
+    f.half_extent[a] = (float)(0.5 * ext[a]);
+    maxd = std::max(maxd, L.dims[a]);
+  }
+  f.interior = L.interior;
+  f.tf = p.tf;
+  f.tf_w = p.tf_w;
+  f.tf_h = p.tf_h;
+  f.mode = p.mode;
+  f.interp = p.interp;
+  f.value_lo = (float)p.lo;
+  f.idx_scale = (float)((f.tf_w - 1) / (p.hi - p.lo));
+  float gm = p.grad_max > 0 ? p.grad_max : ds.max_grad;
+  if (!(gm > 0)) gm = 1.f;
+  f.grad_scale = (float)((f.tf_h - 1) / ((double)gm * (p.hi - p.lo)));
+  f.dt = (float)(1.0 / ((double)p.spv * (double)maxd));
+  f.opacity_exp = (float)(1.0 / (double)p.spv);
+  f.ert = p.ert;
+  f.iso = p.iso;
+  for (int k = 0; k < 3; ++k) {
+    f.iso_rgb[k] = p.iso_rgb[k];
+    f.amb[k] = p.amb[k];
+    f.diff[k] = p.diff[k];
+    f.spec[k] = p.spec[k];
+    f.bg[k] = p.bg[k];
+  }
+  f.lighting = p.lighting;
+  f.shininess = p.shininess;
+  double V[16], P[16], M[16], Mi[16], Vi[16];
+  for (int i = 0; i < 16; ++i) { V[i] = p.view[i]; P[i] = p.proj[i]; }
+  mat_mul(P, V, M);
+  mat_inv(M, Mi);
+  mat_inv(V, Vi);
+  for (int i = 0; i < 16; ++i) f.inv_vp[i] = (float)Mi[i];
+  double ld[3];
+  for (int rr = 0; rr < 3; ++rr)
+    ld[rr] = Vi[4 * rr] * p.light_dir[0] + Vi[4 * rr + 1] * p.light_dir[1] + Vi[4 * rr + 2] * p.light_dir[2];
+  double ll = std::sqrt(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
+  for (int k = 0; k < 3; ++k) f.light_to[k] = ll > 0 ? (float)(-ld[k] / ll) : 0.f;
+  f.width = p.width;
+  f.height = p.height;
+  f.tile_w = p.tile_w;
+  f.empty_skip = p.empty_skip;
+  f.occ = p.occ;
+  for (int a = 0; a < 3; ++a) f.nc[a] = L.nc[a];
+  f.cell_shift = CELL_SHIFT;
+  f.tiles_x = (p.width + p.tile_w - 1) / p.tile_w;
+  f.tiles_y = (p.height + 32 / p.tile_w - 1) / (32 / p.tile_w);
+  // layout copy: the axis whose voxel-space extent along screen x is largest
+  // (row 0 of the view matrix is the camera's right vector in world space)
+  f.perm = 0;
+  if (ds.layouts == 4) {
+    f.perm = 3;  // blocked copy, independent of the view direction
+  } else if (ds.layouts == 3) {
+    double best = -1;
+    for (int a = 0; a < 3; ++a) {
+      double w = std::fabs((double)p.view[a] * f.vox_scale[a]);
+      if (w > best) { best = w; f.perm = a; }
+    }
+  }
+  f.copy_off = (unsigned long long)(f.perm == 3 ? 1 : f.perm) * ds.copy_stride;
+}
+
 }  // namespace
 
 namespace gbvr {
@@ -579,33 +747,11 @@ int upload_tf(gbvr_renderer* r, int level) {
     r->skip_dirty = true;
   }
   if (r->skip_dirty || r->skip_level != level) {
-    const Level& L = r->ds.levels[level];
-    CUDA_TRY(r->d_skip.alloc(r->ds.bricks.size()));
-    const size_t ncell = (size_t)L.nc[0] * L.nc[1] * L.nc[2];
-    CUDA_TRY(r->d_occ.alloc(ncell));
     double lo, hi;
     default_range(r, lo, hi);
     int w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4), h = two ? r->tf2d_h : 1;
-    // prefix count of TF columns with any non-zero alpha
-    std::vector<int> pre(w + 1, 0);
-    for (int x = 0; x < w; ++x) {
-      int nz = 0;
-      for (int y = 0; y < h && !nz; ++y) nz = tf[4 * ((size_t)y * w + x) + 3] != 0.f;
-      pre[x + 1] = pre[x] + nz;
-    }
-    CUDA_TRY(r->d_tfprefix.alloc(sizeof(int) * pre.size()));
-    CUDA_TRY(cudaMemcpyAsync(r->d_tfprefix.p, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, r->stream));
-    float idx_scale = (float)((w - 1) / (hi - lo));
-    CUDA_TRY(launch_classify_bricks(r->ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks, r->d_tfprefix.as<int>(), w,
-                                    r->mode, (float)lo, idx_scale, r->iso,
-                                    r->d_skip.as<unsigned char>() + L.brick_base, r->stream));
-    CUDA_TRY(launch_classify_cells(L.cells->as<float2>(), (long long)ncell, r->d_tfprefix.as<int>(), w, r->mode,
-                                   (float)lo, idx_scale, r->iso, r->d_occ.as<unsigned char>(), r->stream));
-    CUDA_TRY(r->d_occtmp.alloc(ncell));
-    CUDA_TRY(launch_cell_distance(r->d_occ.as<unsigned char>(), r->d_occtmp.as<unsigned char>(), L.nc, CELL_DIST_CAP,
-                                  r->stream));
-    // the host prefix vector must outlive the async copy
-    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    TRY(classify_level(r->ds, level, tf, w, h, r->mode, lo, hi, r->iso, r->d_tfprefix, r->d_skip, r->d_occ,
+                       r->d_occtmp, r->stream));
     r->skip_dirty = false;
     r->skip_level = level;
   }
@@ -615,89 +761,42 @@ int upload_tf(gbvr_renderer* r, int level) {
 void default_camera(gbvr_renderer* r, float view[16], float proj[16]);
 
 FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int level, int vidx) {
-  FrameDesc f;
-  memset(&f, 0, sizeof(f));
-  const Dataset& ds = r->ds;
-  const Level& L = ds.levels[level];
-  f.pool = ds.pool.p;
-  f.bricks = ds.d_bricks.as<BrickInfo>() + L.brick_base;
-  f.skip = r->d_skip.as<unsigned char>() + L.brick_base;
-  f.dtype = ds.dtype;
-  f.sampler = r->sampler;
-  double ext[3], mx = 0;
-  for (int a = 0; a < 3; ++a) {
-    ext[a] = (double)ds.dims[a] * ds.aspect[a];
-    mx = std::max(mx, ext[a]);
-  }
-  long long maxd = 0;
-  for (int a = 0; a < 3; ++a) {
-    ext[a] /= mx;
-    f.dims[a] = (int)L.dims[a];
-    f.nb[a] = L.nb[a];
-    f.vox_scale[a] = (float)((double)L.dims[a] / ext[a]);
-    f.half_extent[a] = (float)(0.5 * ext[a]);
-    maxd = std::max(maxd, L.dims[a]);
-  }
-  f.interior = L.interior;
-  const bool two = r->mode == GBVR_RM_2DTRANS;
-  f.tf = r->d_tf.as<float4>();
-  f.tf_w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4);
-  f.tf_h = two ? r->tf2d_h : 1;
-  f.mode = r->mode;
-  f.interp = r->interp;
-  double lo, hi;
-  default_range(r, lo, hi);
-  f.value_lo = (float)lo;
-  f.idx_scale = (float)((f.tf_w - 1) / (hi - lo));
-  float gm = r->tf2d_grad_max > 0 ? r->tf2d_grad_max : ds.max_grad;
-  if (!(gm > 0)) gm = 1.f;
-  f.grad_scale = (float)((f.tf_h - 1) / ((double)gm * (hi - lo)));
-  f.dt = (float)(1.0 / ((double)r->spv * (double)maxd));
-  f.opacity_exp = (float)(1.0 / (double)r->spv);
-  f.ert = r->ert;
-  f.iso = r->iso;
+  FrameParams p;
+  memset(&p, 0, sizeof(p));
+  p.view = view;
+  p.proj = proj;
+  p.width = r->width;
+  p.height = r->height;
+  p.spv = r->spv;
+  p.level = level;
+  p.mode = r->mode;
+  p.interp = r->interp;
+  p.sampler = r->sampler;
+  p.ert = r->ert;
+  p.iso = r->iso;
+  p.lighting = r->lighting;
+  p.shininess = r->shininess;
   for (int k = 0; k < 3; ++k) {
-    f.iso_rgb[k] = r->iso_rgb[k];
-    f.amb[k] = r->amb[k];
-    f.diff[k] = r->diff[k];
-    f.spec[k] = r->spec[k];
-    f.bg[k] = r->bg_bot[k];
+    p.iso_rgb[k] = r->iso_rgb[k];
+    p.amb[k] = r->amb[k];
+    p.diff[k] = r->diff[k];
+    p.spec[k] = r->spec[k];
+    p.light_dir[k] = r->light_dir[k];
+    p.bg[k] = r->bg_bot[k];
   }
-  f.lighting = r->lighting;
-  f.shininess = r->shininess;
-  double V[16], P[16], M[16], Mi[16], Vi[16];
-  for (int i = 0; i < 16; ++i) { V[i] = view[i]; P[i] = proj[i]; }
-  mat_mul(P, V, M);
-  mat_inv(M, Mi);
-  mat_inv(V, Vi);
-  for (int i = 0; i < 16; ++i) f.inv_vp[i] = (float)Mi[i];
-  double ld[3];
-  for (int rr = 0; rr < 3; ++rr)
-    ld[rr] = Vi[4 * rr] * r->light_dir[0] + Vi[4 * rr + 1] * r->light_dir[1] + Vi[4 * rr + 2] * r->light_dir[2];
-  double ll = std::sqrt(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
-  for (int k = 0; k < 3; ++k) f.light_to[k] = ll > 0 ? (float)(-ld[k] / ll) : 0.f;
-  f.width = r->width;
-  f.height = r->height;
-  f.tile_w = r->tile_w;
-  f.empty_skip = r->empty_skip;
-  f.occ = r->d_occ.as<unsigned char>();
-  for (int a = 0; a < 3; ++a) f.nc[a] = L.nc[a];
-  f.cell_shift = CELL_SHIFT;
-  f.tiles_x = (r->width + r->tile_w - 1) / r->tile_w;
-  f.tiles_y = (r->height + 32 / r->tile_w - 1) / (32 / r->tile_w);
-  // layout copy: the axis whose voxel-space extent along screen x is largest
-  // (row 0 of the view matrix is the camera's right vector in world space)
-  f.perm = 0;
-  if (ds.layouts == 4) {
-    f.perm = 3;  // blocked copy, independent of the view direction
-  } else if (ds.layouts == 3) {
-    double best = -1;
-    for (int a = 0; a < 3; ++a) {
-      double w = std::fabs((double)view[a] * f.vox_scale[a]);
-      if (w > best) { best = w; f.perm = a; }
-    }
-  }
-  f.copy_off = (unsigned long long)(f.perm == 3 ? 1 : f.perm) * ds.copy_stride;
+  p.tile_w = r->tile_w;
+  p.empty_skip = r->empty_skip;
+  const bool two = r->mode == GBVR_RM_2DTRANS;
+  p.tf = r->d_tf.as<float4>();
+  p.tf_w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4);
+  p.tf_h = two ? r->tf2d_h : 1;
+  default_range(r, p.lo, p.hi);
+  p.grad_max = r->tf2d_grad_max;
+  p.skip = r->d_skip.as<unsigned char>();
+  p.occ = r->d_occ.as<unsigned char>();
+  FrameDesc f;
+  fill_frame(f, r->ds, p);
+  const Level& L = r->ds.levels[level];
   const size_t npix = (size_t)r->width * r->height;
   f.out_rgba8 = r->d_fb8.as<uchar4>() + (size_t)vidx * npix;
   f.out_f32 = r->d_fb32.p ? r->d_fb32.as<float4>() + (size_t)vidx * npix : nullptr;
@@ -956,46 +1055,12 @@ int gbvr_load_volume(gbvr_renderer* r, const void* host, const int64_t dims[3], 
 
 int gbvr_load_synthetic(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr_brick_params* bp) {
   TRY(check_r(r));
-  if (!p || p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 || p->nblobs < 0)
-    return fail(GBVR_EINVAL, "bad synthetic parameters");
-  BlobTablesHost t;
-  make_blob_tables(*p, t);
-  DevBuf amp, ex, ey, ez, bx, by, bz, lv;
-  auto up = [&](DevBuf& d, const std::vector<float>& v) -> cudaError_t {
-    cudaError_t e = d.alloc(sizeof(float) * std::max<size_t>(v.size(), 1));
-    if (e != cudaSuccess || v.empty()) return e;
-    return cudaMemcpyAsync(d.p, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice, r->stream);
-  };
-  CUDA_TRY(up(amp, t.amp));
-  CUDA_TRY(up(ex, t.ex));
-  CUDA_TRY(up(ey, t.ey));
-  CUDA_TRY(up(ez, t.ez));
-  CUDA_TRY(up(bx, t.bgx));
-  CUDA_TRY(up(by, t.bgy));
-  CUDA_TRY(up(bz, t.bgz));
-  long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
-  CUDA_TRY(lv.alloc((size_t)d[0] * d[1] * d[2] * dtype_size(p->dtype)));
-  BlobTablesDev td;
-  td.nblobs = p->nblobs;
-  td.amp = amp.as<float>();
-  td.ex = ex.as<float>();
-  td.ey = ey.as<float>();
-  td.ez = ez.as<float>();
-  bool bg = p->bg_freq > 0;
-  td.bgx = bg ? bx.as<float>() : nullptr;
-  td.bgy = bg ? by.as<float>() : nullptr;
-  td.bgz = bg ? bz.as<float>() : nullptr;
-  td.bg_level = p->bg_level;
-  td.bg_amp = p->bg_amp;
-  td.scale = p->scale;
-  td.noise_amp = p->noise_amp;
-  td.noise_kind = p->noise_kind;
-  td.vmax = p->vmax;
-  td.seed = p->seed;
-  CUDA_TRY(launch_synth_blobs(td, d, p->dtype, lv.p, r->stream));
+  DevBuf lv;
+  TRY(synth_to_device(p, lv, r->stream));
   r->drop_graphs();
   r->skip_dirty = true;
   r->tf_dirty = true;
+  long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
   TRY(build_dataset(r->ds, lv, p->dtype, d, bp, r->stream));
   return GBVR_OK;
 }
@@ -1552,6 +1617,509 @@ int gbvr_orbit_camera(float azimuth_deg, float elevation_deg, float radius, floa
                       float view[16], float proj[16]) {
   if (!view || !proj || width <= 0 || height <= 0 || !(radius > 0)) return fail(GBVR_EINVAL, "bad camera");
   orbit(azimuth_deg, elevation_deg, radius, fov_deg, width, height, view, proj);
+  return GBVR_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Serving loop: many resident datasets and transfer functions, requests from
+// any thread, continuous batching into persistent launches.
+//
+// A worker thread owns the GPU side.  Two batch slots alternate: while one
+// batch renders, the next is assembled from the requests that arrived and
+// queued behind it on the same stream, so the GPU is not idle between
+// batches.  A batch takes pending requests in arrival order until it holds
+// max_batch requests or its framebuffer area (half of fb_budget_bytes) is
+// full; requests that do not fit wait for the next batch (admission by
+// memory).  Within a batch, requests are grouped by voxel type and render
+// mode (one persistent launch each, all queued back to back).  Every ray is
+// computed independently of the batch it lands in, so a request's image is
+// the same alone and in any mix.
+// ===========================================================================
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
+
+namespace {
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct ServerTf {
+  int dataset = 0;
+  int mode = GBVR_RM_1DTRANS, w = 0, h = 1, level = 0;
+  std::vector<float> host;
+  DevBuf d_tf, d_prefix, d_skip, d_occ, d_occtmp;
+  double lo = 0, hi = 1;
+  float grad_max = 0.f, iso = 0.f, iso_rgb[3] = {1, 1, 1};
+};
+
+struct ServerRequest {
+  gbvr_request req;
+  uint64_t ticket = 0;
+  double t_submit = 0, t_launch = 0, t_done = 0;
+  int status = 1;  // 1 pending, 0 done, < 0 error
+  int batch_size = 0;
+  uint64_t batch = 0;
+  double gpu_ms = 0;
+};
+
+struct BatchSlot {
+  DevBuf d_frames, d_prefix, d_counter, d_samples, d_fb;
+  PinnedBuf h_frames, h_prefix, h_fb;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<ServerRequest*> reqs;
+  std::vector<size_t> fb_off;
+  size_t fb_used = 0;
+  bool busy = false;
+  uint64_t seq = 0;
+};
+
+}  // namespace
+
+struct gbvr_server {
+  gbvr_server_params params;
+  int device = 0;
+  int sm_count = 0, max_ctas = 1;
+  cudaStream_t stream = nullptr;
+  std::vector<std::unique_ptr<Dataset>> datasets;
+  std::vector<std::unique_ptr<ServerTf>> tfs;
+  BatchSlot slots[2];
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<ServerRequest*> pending;
+  std::unordered_map<uint64_t, std::unique_ptr<ServerRequest>> reqs;
+  uint64_t next_ticket = 1, next_batch = 1;
+  bool stop = false;
+  std::string worker_error;
+  std::thread worker;
+  // statistics since the last reset
+  std::vector<double> latencies;
+  uint64_t submitted = 0, completed = 0, batches = 0, batched_requests = 0;
+  double t_first = -1, t_last = 0;
+
+  ~gbvr_server() {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      stop = true;
+    }
+    cv_work.notify_all();
+    if (worker.joinable()) worker.join();
+    for (auto& s : slots) {
+      if (s.ev0) cudaEventDestroy(s.ev0);
+      if (s.ev1) cudaEventDestroy(s.ev1);
+    }
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+// Assemble and launch one batch into `slot` (worker thread, mutex released).
+int launch_batch(gbvr_server* s, BatchSlot& slot) {
+  const int n = (int)slot.reqs.size();
+  // group by voxel type and mode: one persistent launch per group
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  auto key = [&](int i) {
+    const ServerRequest* q = slot.reqs[i];
+    return s->datasets[q->req.dataset]->dtype * 3 + s->tfs[q->req.tf]->mode;
+  };
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key(x) < key(y); });
+  std::vector<ServerRequest*> sorted(n);
+  std::vector<size_t> offs(n);
+  for (int i = 0; i < n; ++i) {
+    sorted[i] = slot.reqs[order[i]];
+    offs[i] = slot.fb_off[order[i]];
+  }
+  slot.reqs.swap(sorted);
+  slot.fb_off.swap(offs);
+  CUDA_TRY(slot.d_frames.alloc(sizeof(FrameDesc) * s->params.max_batch));
+  CUDA_TRY(slot.d_prefix.alloc(sizeof(int) * (s->params.max_batch + 8) * 2));
+  CUDA_TRY(slot.d_counter.alloc(sizeof(int) * 16));
+  CUDA_TRY(slot.d_samples.alloc(sizeof(unsigned long long) * s->params.max_batch));
+  CUDA_TRY(slot.h_frames.alloc(sizeof(FrameDesc) * s->params.max_batch));
+  CUDA_TRY(slot.h_prefix.alloc(sizeof(int) * (s->params.max_batch + 8) * 2));
+  FrameDesc* hf = (FrameDesc*)slot.h_frames.p;
+  int* hp = (int*)slot.h_prefix.p;
+  struct Group { int first, count, prefix_at, total, dtype, mode; };
+  std::vector<Group> groups;
+  int pcur = 0;
+  for (int i = 0; i < n; ++i) {
+    const ServerRequest* q = slot.reqs[i];
+    const Dataset& ds = *s->datasets[q->req.dataset];
+    const ServerTf& t = *s->tfs[q->req.tf];
+    FrameParams p;
+    memset(&p, 0, sizeof(p));
+    p.view = q->req.view;
+    p.proj = q->req.proj;
+    p.width = q->req.width;
+    p.height = q->req.height;
+    p.spv = q->req.samples_per_voxel > 0 ? q->req.samples_per_voxel : 1.f;
+    p.level = t.level;
+    p.mode = t.mode;
+    p.interp = GBVR_LINEAR;
+    p.sampler = GBVR_SAMPLER_SW;
+    p.ert = 0.99f;
+    p.iso = t.iso;
+    p.lighting = 1;
+    p.shininess = 8.f;
+    for (int k = 0; k < 3; ++k) {
+      p.iso_rgb[k] = t.iso_rgb[k];
+      p.amb[k] = 0.1f;
+      p.diff[k] = 1.f;
+      p.spec[k] = 1.f;
+      p.light_dir[k] = k == 2 ? -1.f : 0.f;
+      p.bg[k] = 0.f;
+    }
+    p.tile_w = s->params.tile_w;
+    p.empty_skip = 2;
+    p.tf = t.d_tf.as<float4>();
+    p.tf_w = t.w;
+    p.tf_h = t.h;
+    p.lo = t.lo;
+    p.hi = t.hi;
+    p.grad_max = t.grad_max;
+    p.skip = t.d_skip.as<unsigned char>();
+    p.occ = t.d_occ.as<unsigned char>();
+    fill_frame(hf[i], ds, p);
+    hf[i].out_rgba8 = (uchar4*)((char*)slot.d_fb.p + slot.fb_off[i]);
+    hf[i].samples = slot.d_samples.as<unsigned long long>() + i;
+    const int dt = ds.dtype, md = t.mode;
+    if (groups.empty() || groups.back().dtype != dt || groups.back().mode != md) {
+      if (!groups.empty()) {
+        Group& g = groups.back();
+        hp[g.prefix_at + g.count] = g.total;
+        pcur = g.prefix_at + g.count + 1;
+      }
+      groups.push_back({i, 0, pcur, 0, dt, md});
+    }
+    Group& g = groups.back();
+    hp[g.prefix_at + g.count] = g.total;
+    g.total += hf[i].tiles_x * hf[i].tiles_y;
+    ++g.count;
+  }
+  if (!groups.empty()) {
+    Group& g = groups.back();
+    hp[g.prefix_at + g.count] = g.total;
+    pcur = g.prefix_at + g.count + 1;
+  }
+  cudaStream_t st = s->stream;
+  CUDA_TRY(cudaEventRecord(slot.ev0, st));
+  CUDA_TRY(cudaMemcpyAsync(slot.d_frames.p, hf, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(slot.d_prefix.p, hp, sizeof(int) * pcur, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(slot.d_counter.p, 0, sizeof(int) * 16, st));
+  CUDA_TRY(cudaMemsetAsync(slot.d_samples.p, 0, sizeof(unsigned long long) * n, st));
+  const int grid = s->sm_count * s->max_ctas;
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const Group& g = groups[gi];
+    CUDA_TRY(launch_render_persistent_typed(g.dtype, g.mode, GBVR_SAMPLER_SW, slot.d_frames.as<FrameDesc>() + g.first,
+                                            g.count, slot.d_prefix.as<int>() + g.prefix_at, g.total,
+                                            slot.d_counter.as<int>() + gi, grid, st));
+  }
+  CUDA_TRY(cudaMemcpyAsync(slot.h_fb.p, slot.d_fb.p, slot.fb_used, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaEventRecord(slot.ev1, st));
+  return GBVR_OK;
+}
+
+void server_worker(gbvr_server* s) {
+  cudaSetDevice(s->device);
+  const size_t slot_budget = s->params.fb_budget_bytes / 2;
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    const bool in_flight = s->slots[0].busy || s->slots[1].busy;
+    if (in_flight) {
+      // poll the batch in flight, waking early when new requests arrive so
+      // a free slot can be filled and queued behind it
+      s->cv_work.wait_for(lk, std::chrono::microseconds(100));
+    } else {
+      s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty(); });
+    }
+    if (s->stop && s->pending.empty() && !s->slots[0].busy && !s->slots[1].busy) break;
+    // fill every free slot with pending requests
+    for (auto& slot : s->slots) {
+      if (slot.busy || s->pending.empty()) continue;
+      slot.reqs.clear();
+      slot.fb_off.clear();
+      size_t used = 0;
+      while (!s->pending.empty() && (int)slot.reqs.size() < s->params.max_batch) {
+        ServerRequest* q = s->pending.front();
+        const size_t bytes = (size_t)q->req.width * q->req.height * 4;
+        const size_t aligned = (bytes + 255) & ~(size_t)255;
+        if (aligned > slot_budget) {  // can never be admitted
+          s->pending.pop_front();
+          q->status = GBVR_EINVAL;
+          q->t_done = now_ms();
+          s->cv_done.notify_all();
+          continue;
+        }
+        if (used + aligned > slot_budget) break;  // waits for the next batch
+        s->pending.pop_front();
+        slot.reqs.push_back(q);
+        slot.fb_off.push_back(used);
+        used += aligned;
+      }
+      if (slot.reqs.empty()) continue;
+      slot.fb_used = used;
+      slot.busy = true;
+      slot.seq = s->next_batch++;
+      const double t = now_ms();
+      for (ServerRequest* q : slot.reqs) {
+        q->t_launch = t;
+        q->batch = slot.seq;
+        q->batch_size = (int)slot.reqs.size();
+      }
+      lk.unlock();
+      int rc = launch_batch(s, slot);
+      lk.lock();
+      if (rc != GBVR_OK) {
+        s->worker_error = g_err;
+        for (ServerRequest* q : slot.reqs) {
+          q->status = rc;
+          q->t_done = now_ms();
+        }
+        slot.busy = false;
+        s->cv_done.notify_all();
+      }
+    }
+    // retire the oldest batch in flight once its copies have landed
+    BatchSlot* oldest = nullptr;
+    for (auto& slot : s->slots)
+      if (slot.busy && (!oldest || slot.seq < oldest->seq)) oldest = &slot;
+    if (!oldest) continue;
+    cudaError_t e = cudaEventQuery(oldest->ev1);
+    if (e == cudaErrorNotReady) continue;
+    lk.unlock();
+    float ms = 0.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, oldest->ev0, oldest->ev1);
+    if (e == cudaSuccess)
+      for (size_t i = 0; i < oldest->reqs.size(); ++i) {
+        const ServerRequest* q = oldest->reqs[i];
+        memcpy(q->req.out_rgba8, (const char*)oldest->h_fb.p + oldest->fb_off[i],
+               (size_t)q->req.width * q->req.height * 4);
+      }
+    lk.lock();
+    const double t = now_ms();
+    for (ServerRequest* q : oldest->reqs) {
+      q->status = e == cudaSuccess ? GBVR_OK : GBVR_ECUDA;
+      q->t_done = t;
+      q->gpu_ms = ms;
+      if (e == cudaSuccess) {
+        s->latencies.push_back(t - q->t_submit);
+        ++s->completed;
+        s->t_last = t;
+      }
+    }
+    if (e != cudaSuccess) s->worker_error = cudaGetErrorString(e);
+    ++s->batches;
+    s->batched_requests += oldest->reqs.size();
+    oldest->busy = false;
+    oldest->reqs.clear();
+    s->cv_done.notify_all();
+  }
+}
+
+int check_s(gbvr_server* s) {
+  if (!s) return fail(GBVR_EINVAL, "null server");
+  return GBVR_OK;
+}
+
+int server_add_dataset(gbvr_server* s, DevBuf& lv, int dtype, const long long d[3], const gbvr_brick_params* bp,
+                       int* id) {
+  std::unique_ptr<Dataset> ds(new Dataset());
+  gbvr_brick_params b = {};
+  if (bp) b = *bp;
+  if (b.layouts == 0) b.layouts = 4;
+  TRY(build_dataset(*ds, lv, dtype, d, &b, s->stream));
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->datasets.push_back(std::move(ds));
+  if (id) *id = (int)s->datasets.size() - 1;
+  return GBVR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbvr_server_create(const gbvr_server_params* params, gbvr_server** out) {
+  if (!out) return fail(GBVR_EINVAL, "null output handle");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(GBVR_ECUDA, "no CUDA device available");
+  std::unique_ptr<gbvr_server> s(new gbvr_server());
+  gbvr_server_params p = {};
+  if (params) p = *params;
+  if (p.max_batch <= 0) p.max_batch = 64;
+  if (p.max_batch > 4096) return fail(GBVR_EINVAL, "max_batch above 4096");
+  if (p.tile_w == 0) p.tile_w = TILE_W;
+  if (p.tile_w != 4 && p.tile_w != 8 && p.tile_w != 16 && p.tile_w != 32) return fail(GBVR_EINVAL, "bad tile_w");
+  if (p.fb_budget_bytes == 0) p.fb_budget_bytes = (uint64_t)2 << 30;
+  s->params = p;
+  CUDA_TRY(cudaGetDevice(&s->device));
+  CUDA_TRY(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device));
+  s->max_ctas = std::max(1, persistent_grid_size(s->device) / std::max(s->sm_count, 1));
+  CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  for (auto& slot : s->slots) {
+    CUDA_TRY(cudaEventCreate(&slot.ev0));
+    CUDA_TRY(cudaEventCreate(&slot.ev1));
+    CUDA_TRY(slot.d_fb.alloc(p.fb_budget_bytes / 2));
+    CUDA_TRY(slot.h_fb.alloc(p.fb_budget_bytes / 2));
+  }
+  gbvr_server* raw = s.get();
+  s->worker = std::thread(server_worker, raw);
+  *out = s.release();
+  return GBVR_OK;
+}
+
+int gbvr_server_destroy(gbvr_server* s) {
+  delete s;
+  return GBVR_OK;
+}
+
+int gbvr_server_add_volume(gbvr_server* s, const void* host, const int64_t dims[3], int dtype,
+                           const gbvr_brick_params* bp, int* id) {
+  TRY(check_s(s));
+  if (!host || !dims || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0 || dtype < 0 || dtype > 2)
+    return fail(GBVR_EINVAL, "bad volume");
+  long long d[3] = {dims[0], dims[1], dims[2]};
+  const size_t bytes = (size_t)d[0] * d[1] * d[2] * dtype_size(dtype);
+  DevBuf lv;
+  CUDA_TRY(lv.alloc(bytes));
+  CUDA_TRY(cudaMemcpyAsync(lv.p, host, bytes, cudaMemcpyHostToDevice, s->stream));
+  return server_add_dataset(s, lv, dtype, d, bp, id);
+}
+
+int gbvr_server_add_synthetic(gbvr_server* s, const gbvr_synth_params* p, const gbvr_brick_params* bp, int* id) {
+  TRY(check_s(s));
+  DevBuf lv;
+  TRY(synth_to_device(p, lv, s->stream));
+  long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
+  return server_add_dataset(s, lv, p->dtype, d, bp, id);
+}
+
+int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba, int w, int h, float grad_max,
+                       float iso, const float iso_rgb[3], double lo, double hi, int* tf_id) {
+  TRY(check_s(s));
+  if (dataset < 0 || dataset >= (int)s->datasets.size()) return fail(GBVR_EINVAL, "bad dataset id");
+  if (mode < 0 || mode > 2) return fail(GBVR_EINVAL, "bad render mode");
+  if (mode == GBVR_RM_1DTRANS) h = 1;
+  if (mode == GBVR_RM_ISOSURFACE) {
+    static const float dummy[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (!rgba) { rgba = dummy; w = 2; h = 1; }
+  }
+  if (!rgba || w < 2 || h < 1 || w > 65536 || h > 4096) return fail(GBVR_EINVAL, "bad transfer function size");
+  const Dataset& ds = *s->datasets[dataset];
+  std::unique_ptr<ServerTf> t(new ServerTf());
+  t->dataset = dataset;
+  t->mode = mode;
+  t->w = w;
+  t->h = h;
+  t->host.assign(rgba, rgba + 4 * (size_t)w * h);
+  t->grad_max = grad_max;
+  t->iso = iso;
+  if (iso_rgb) for (int k = 0; k < 3; ++k) t->iso_rgb[k] = iso_rgb[k];
+  if (hi > lo) {
+    t->lo = lo;
+    t->hi = hi;
+  } else if (ds.dtype == DT_F32) {
+    t->lo = ds.gmin;
+    t->hi = ds.gmax > ds.gmin ? ds.gmax : ds.gmin + 1;
+  } else {
+    t->lo = 0;
+    t->hi = std::max(1.0, (double)((long long)ds.hist1d.size() * ds.merge - 1));
+  }
+  CUDA_TRY(t->d_tf.alloc(sizeof(float) * t->host.size()));
+  CUDA_TRY(cudaMemcpyAsync(t->d_tf.p, t->host.data(), sizeof(float) * t->host.size(), cudaMemcpyHostToDevice, s->stream));
+  TRY(classify_level(ds, t->level, t->host, w, h, mode, t->lo, t->hi, t->iso, t->d_prefix, t->d_skip, t->d_occ,
+                     t->d_occtmp, s->stream));
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->tfs.push_back(std::move(t));
+  if (tf_id) *tf_id = (int)s->tfs.size() - 1;
+  return GBVR_OK;
+}
+
+int gbvr_server_submit(gbvr_server* s, const gbvr_request* req, uint64_t* ticket) {
+  TRY(check_s(s));
+  if (!req || !req->out_rgba8 || req->width <= 0 || req->height <= 0 || req->width > 16384 || req->height > 16384)
+    return fail(GBVR_EINVAL, "bad request");
+  std::unique_ptr<ServerRequest> q(new ServerRequest());
+  q->req = *req;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (req->dataset < 0 || req->dataset >= (int)s->datasets.size() || req->tf < 0 || req->tf >= (int)s->tfs.size() ||
+        s->tfs[req->tf]->dataset != req->dataset)
+      return fail(GBVR_EINVAL, "request names an unknown dataset or a transfer function of another dataset");
+    q->ticket = s->next_ticket++;
+    q->t_submit = now_ms();
+    if (s->t_first < 0) s->t_first = q->t_submit;
+    ++s->submitted;
+    if (ticket) *ticket = q->ticket;
+    s->pending.push_back(q.get());
+    s->reqs.emplace(q->ticket, std::move(q));
+  }
+  s->cv_work.notify_one();
+  return GBVR_OK;
+}
+
+int gbvr_server_wait(gbvr_server* s, uint64_t ticket, double timeout_s, gbvr_request_result* out) {
+  TRY(check_s(s));
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return fail(GBVR_EINVAL, "unknown ticket");
+  ServerRequest* q = it->second.get();
+  auto done = [&] { return q->status != 1; };
+  if (timeout_s > 0) {
+    if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done))
+      return fail(GBVR_ETIMEOUT, "request not finished within the timeout");
+  } else {
+    s->cv_done.wait(lk, done);
+  }
+  if (out) {
+    out->status = q->status;
+    out->batch_size = q->batch_size;
+    out->batch = q->batch;
+    out->latency_ms = q->t_done - q->t_submit;
+    out->queue_ms = q->t_launch > 0 ? q->t_launch - q->t_submit : 0;
+    out->gpu_ms = q->gpu_ms;
+  }
+  const int st = q->status;
+  s->reqs.erase(it);
+  if (st != GBVR_OK) return fail(st, s->worker_error.empty() ? "request failed" : s->worker_error);
+  return GBVR_OK;
+}
+
+int gbvr_server_get_stats(gbvr_server* s, gbvr_server_stats* out) {
+  TRY(check_s(s));
+  if (!out) return fail(GBVR_EINVAL, "null stats");
+  std::lock_guard<std::mutex> lk(s->mu);
+  memset(out, 0, sizeof(*out));
+  out->submitted = s->submitted;
+  out->completed = s->completed;
+  out->batches = s->batches;
+  out->mean_batch = s->batches ? (double)s->batched_requests / s->batches : 0;
+  std::vector<double> l = s->latencies;
+  std::sort(l.begin(), l.end());
+  if (!l.empty()) {
+    auto pct = [&](double q) { return l[std::min(l.size() - 1, (size_t)std::floor(q * (l.size() - 1) + 0.5))]; };
+    out->p50_ms = pct(0.50);
+    out->p99_ms = pct(0.99);
+    out->max_ms = l.back();
+  }
+  if (s->completed && s->t_last > s->t_first) out->frames_per_s = s->completed / ((s->t_last - s->t_first) / 1000.0);
+  return GBVR_OK;
+}
+
+int gbvr_server_reset_stats(gbvr_server* s) {
+  TRY(check_s(s));
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->latencies.clear();
+  s->submitted = s->completed = s->batches = s->batched_requests = 0;
+  s->t_first = -1;
+  s->t_last = 0;
   return GBVR_OK;
 }
 

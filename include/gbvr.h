@@ -36,6 +36,7 @@ extern "C" {
 #define GBVR_ECHECKSUM (-6)   /* UVF checksum mismatch */
 #define GBVR_ESTATE (-7)      /* call out of order (e.g. paint before load) */
 #define GBVR_EOVERSIZED (-8)  /* brick larger than the device limit */
+#define GBVR_ETIMEOUT (-9)    /* a wait ran out of time */
 
 #define GBVR_U8 0
 #define GBVR_U16 1
@@ -311,6 +312,70 @@ int gbvr_dev_downsample(const void* dev_in, int dtype, const int64_t dims[3], vo
  * calls that overlap on the GPU (different streams, no ordering) race. */
 #define GBVR_NOALLOC_SYNTH_MAX_FLOATS 262144
 int gbvr_dev_synth_volume_noalloc(const gbvr_synth_params* p, void* dev_out, size_t bytes, void* stream);
+
+/* ---- serving (continuous batching) ----
+ * A server keeps many datasets and transfer-function presets resident and
+ * renders requests submitted from any thread.  A worker thread batches the
+ * pending requests into persistent launches: a batch takes requests in
+ * arrival order until it holds max_batch of them or its framebuffer area
+ * (half of fb_budget_bytes; two batches are in flight) is full; the rest
+ * wait for the next batch, which is assembled while the current one
+ * renders.  A request's image does not depend on the batch it lands in.
+ * No counterpart in the reference (its GUI renders one window per paint,
+ * ImageVis3D/UI/RenderWindow.cpp:2453-2502). */
+typedef struct gbvr_server gbvr_server;
+
+typedef struct gbvr_server_params {
+  int32_t max_batch;          /* requests per batch (0 = 64) */
+  int32_t tile_w;             /* warp tile width (0 = 8) */
+  uint64_t fb_budget_bytes;   /* device + pinned framebuffer memory (0 = 2 GiB) */
+} gbvr_server_params;
+
+typedef struct gbvr_request {
+  int32_t dataset;            /* id from gbvr_server_add_* */
+  int32_t tf;                 /* id from gbvr_server_add_tf (of that dataset) */
+  int32_t width, height;
+  float view[16], proj[16];
+  float samples_per_voxel;    /* 0 = 1 */
+  int32_t reserved;
+  uint8_t* out_rgba8;         /* caller's host buffer, width*height*4 bytes, valid until waited for */
+} gbvr_request;
+
+typedef struct gbvr_request_result {
+  int32_t status;
+  int32_t batch_size;         /* requests in the batch that rendered it */
+  uint64_t batch;
+  double latency_ms;          /* submit to completion (host clock) */
+  double queue_ms;            /* submit to launch */
+  double gpu_ms;              /* device time of its batch */
+} gbvr_request_result;
+
+typedef struct gbvr_server_stats {
+  uint64_t submitted, completed, batches;
+  double mean_batch;
+  double p50_ms, p99_ms, max_ms;  /* request latency percentiles */
+  double frames_per_s;            /* completed requests / (last completion - first submit) */
+} gbvr_server_stats;
+
+int gbvr_server_create(const gbvr_server_params* params, gbvr_server** out);
+int gbvr_server_destroy(gbvr_server* s);
+int gbvr_server_add_volume(gbvr_server* s, const void* host, const int64_t dims[3], int dtype,
+                           const gbvr_brick_params* bp, int* dataset_id);
+int gbvr_server_add_synthetic(gbvr_server* s, const gbvr_synth_params* p, const gbvr_brick_params* bp,
+                              int* dataset_id);
+/* A transfer-function preset of one dataset, classified once for empty-space
+ * skipping: mode GBVR_RM_1DTRANS (w entries, h ignored), GBVR_RM_2DTRANS
+ * (w x h, grad_max as gbvr_set_tf2d) or GBVR_RM_ISOSURFACE (rgba may be null;
+ * iso, iso_rgb).  [lo, hi] is the value range mapped onto the TF (hi <= lo:
+ * the dataset's default). */
+int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba, int w, int h, float grad_max,
+                       float iso, const float iso_rgb[3], double lo, double hi, int* tf_id);
+int gbvr_server_submit(gbvr_server* s, const gbvr_request* req, uint64_t* ticket);
+/* Blocks until the request is done (timeout_s <= 0: no limit); its pixels are
+ * then in req.out_rgba8.  A ticket can be waited for once. */
+int gbvr_server_wait(gbvr_server* s, uint64_t ticket, double timeout_s, gbvr_request_result* out);
+int gbvr_server_get_stats(gbvr_server* s, gbvr_server_stats* out);
+int gbvr_server_reset_stats(gbvr_server* s);
 
 /* Orbit camera around the volume centre: the rotation the 360-degree capture
  * applies per frame (ImageVis3D_Capturing.cpp:170 fAngle = i/N * 360,

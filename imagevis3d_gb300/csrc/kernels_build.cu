@@ -103,23 +103,27 @@ cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], 
 template <typename T>
 __global__ void k_downsample(const T* __restrict__ in, long long X, long long Y, long long Z, T* __restrict__ out,
                              long long OX, long long OY, long long OZ) {
-  long long n = OX * OY * OZ;
-  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < n; o += (long long)gridDim.x * blockDim.x) {
-    long long x = o % OX, t = o / OX, y = t % OY, z = t / OY;
-    long long x0 = 2 * x, y0 = 2 * y, z0 = 2 * z;
-    int nx = (x0 + 1 < X) ? 2 : 1, ny = (y0 + 1 < Y) ? 2 : 1, nz = (z0 + 1 < Z) ? 2 : 1;
-    if (sizeof(T) == 4) {
-      double sum = 0.0;
-      for (int dz = 0; dz < nz; ++dz)
-        for (int dy = 0; dy < ny; ++dy)
-          for (int dx = 0; dx < nx; ++dx) sum += (double)__ldg(in + ((z0 + dz) * Y + (y0 + dy)) * X + x0 + dx);
-      out[o] = (T)(float)(sum / (double)(nx * ny * nz));
-    } else {
-      unsigned sum = 0;
-      for (int dz = 0; dz < nz; ++dz)
-        for (int dy = 0; dy < ny; ++dy)
-          for (int dx = 0; dx < nx; ++dx) sum += (unsigned)__ldg(in + ((z0 + dz) * Y + (y0 + dy)) * X + x0 + dx);
-      out[o] = (T)(sum / (unsigned)(nx * ny * nz));
+  for (long long row = blockIdx.x; row < OY * OZ; row += gridDim.x) {
+    const long long z = row / OY, y = row - z * OY;
+    const long long y0 = 2 * y, z0 = 2 * z;
+    const int ny = (y0 + 1 < Y) ? 2 : 1, nz = (z0 + 1 < Z) ? 2 : 1;
+    for (long long x = threadIdx.x; x < OX; x += blockDim.x) {
+      const long long x0 = 2 * x;
+      const int nx = (x0 + 1 < X) ? 2 : 1;
+      const long long o = row * OX + x;
+      if (sizeof(T) == 4) {
+        double sum = 0.0;
+        for (int dz = 0; dz < nz; ++dz)
+          for (int dy = 0; dy < ny; ++dy)
+            for (int dx = 0; dx < nx; ++dx) sum += (double)__ldg(in + ((z0 + dz) * Y + (y0 + dy)) * X + x0 + dx);
+        out[o] = (T)(float)(sum / (double)(nx * ny * nz));
+      } else {
+        unsigned sum = 0;
+        for (int dz = 0; dz < nz; ++dz)
+          for (int dy = 0; dy < ny; ++dy)
+            for (int dx = 0; dx < nx; ++dx) sum += (unsigned)__ldg(in + ((z0 + dz) * Y + (y0 + dy)) * X + x0 + dx);
+        out[o] = (T)(sum / (unsigned)(nx * ny * nz));
+      }
     }
   }
 }
@@ -157,12 +161,12 @@ __device__ __forceinline__ float fbm_lerp(float a, float b, float t) {
 template <typename T>
 __global__ void k_synth_fbm(long long X, long long Y, long long Z, uint32_t seed, int octaves, int base_period,
                             float thr, float vmax, T* __restrict__ out) {
-  const long long n = X * Y * Z;
   const long long dims[3] = {X, Y, Z};
   const float inv = __fdiv_rn(1.0f, __fsub_rn(1.0f, thr));
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long x = idx % X, t0 = idx / X, y = t0 % Y, z = t0 / Y;
+  for (long long row = blockIdx.x; row < Y * Z; row += gridDim.x)
+  for (long long x = threadIdx.x; x < X; x += blockDim.x) {
+    const long long z = row / Y, y = row - z * Y;
+    const long long idx = row * X + x;
     const long long c[3] = {x, y, z};
     float acc = 0.0f, norm = 0.0f, amp = 1.0f;
     for (int o = 0; o < octaves; ++o) {
@@ -202,9 +206,9 @@ __global__ void k_synth_fbm(long long X, long long Y, long long Z, uint32_t seed
 cudaError_t launch_synth_fbm(const long long dims[3], int dtype, uint32_t seed, int octaves, int base_period,
                              float thr, float vmax, void* out, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
-  const long long n = dims[0] * dims[1] * dims[2];
-  int threads = 256;
-  int blocks = grid_for(n, threads);
+  const long long rows = dims[1] * dims[2];
+  int threads = dims[0] >= 256 ? 256 : 128;
+  int blocks = (int)(rows < 152LL * 256 ? rows : 152LL * 256);
   if (dtype == DT_U8)
     k_synth_fbm<uint8_t><<<blocks, threads, 0, s>>>(dims[0], dims[1], dims[2], seed, octaves, base_period, thr, vmax, (uint8_t*)out);
   else if (dtype == DT_U16)
@@ -218,8 +222,8 @@ cudaError_t launch_synth_fbm(const long long dims[3], int dtype, uint32_t seed, 
 cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3], void* out, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   long long OX = (dims[0] + 1) / 2, OY = (dims[1] + 1) / 2, OZ = (dims[2] + 1) / 2;
-  int threads = 256;
-  int blocks = grid_for(OX * OY * OZ, threads);
+  int threads = OX >= 256 ? 256 : 128;
+  int blocks = (int)(OY * OZ < 152LL * 64 ? OY * OZ : 152LL * 64);
   if (dtype == DT_U8)
     k_downsample<uint8_t><<<blocks, threads, 0, s>>>((const uint8_t*)in, dims[0], dims[1], dims[2], (uint8_t*)out, OX, OY, OZ);
   else if (dtype == DT_U16)
@@ -246,10 +250,11 @@ __global__ void k_gather(const T* __restrict__ level, long long X, long long Y, 
   else if (perm == 1) { s1 = 1; s2 = b.sy; s0 = (long long)b.sy * b.sz; }
   else if (perm == 2) { s2 = 1; s0 = b.sz; s1 = (long long)b.sz * b.sx; }
   const long long nbx = (b.sx + 3) >> 2, nby = (b.sy + 3) >> 2;
+  (void)plane;
   for (int zs = blockIdx.x; zs < b.sz; zs += gridDim.x) {
     const long long z = min(max((long long)b.oz + zs, 0LL), Z - 1);
-    for (long long i = threadIdx.x; i < plane; i += blockDim.x) {
-      long long r = i / b.sx, xs = i - r * b.sx;
+    for (long long r = 0; r < b.sy; ++r)
+    for (long long xs = threadIdx.x; xs < b.sx; xs += blockDim.x) {
       // ghosts outside the level replicate its edge voxels
       const long long y = min(max((long long)b.oy + r, 0LL), Y - 1);
       const long long x = min(max((long long)b.ox + xs, 0LL), X - 1);
@@ -268,7 +273,7 @@ cudaError_t launch_gather_bricks(const void* level, int dtype, const long long d
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (nbricks <= 0) return cudaSuccess;
   dim3 grid((unsigned)(dims[2] < 256 ? dims[2] : 256), (unsigned)nbricks);
-  int threads = 512;
+  int threads = 256;
   if (dtype == DT_U8)
     k_gather<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], bricks_dev, (uint8_t*)pool, perm);
   else if (dtype == DT_U16)
@@ -479,16 +484,21 @@ __device__ double grad_f64(const T* __restrict__ v, long long X, long long Y, lo
   return __dsqrt_rn(s);
 }
 
+// The three passes walk the volume row by row (one CTA per z-slab of rows,
+// threads along x) so no voxel pays for a 64-bit division of its index.
 template <typename T>
 __global__ void k_hist2d_pass1(const T* __restrict__ v, long long X, long long Y, long long Z, Hist2DScratch* sc) {
-  const long long n = X * Y * Z;
   unsigned long long smax = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    long long x = i % X, t = i / X, y = t % Y, z = t / Y;
-    int D[3];
-    int_diffs(v, X, Y, Z, x, y, z, i, D);
-    unsigned long long S = (unsigned long long)((long long)D[0] * D[0] + (long long)D[1] * D[1] + (long long)D[2] * D[2]);
-    smax = S > smax ? S : smax;
+  for (long long row = blockIdx.x; row < Y * Z; row += gridDim.x) {
+    const long long z = row / Y, y = row - z * Y;
+    for (long long x = threadIdx.x; x < X; x += blockDim.x) {
+      const long long i = row * X + x;
+      int D[3];
+      int_diffs(v, X, Y, Z, x, y, z, i, D);
+      const unsigned long long S =
+          (unsigned long long)((long long)D[0] * D[0] + (long long)D[1] * D[1] + (long long)D[2] * D[2]);
+      smax = S > smax ? S : smax;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long t = __shfl_xor_sync(0xffffffffu, smax, o);
@@ -502,16 +512,20 @@ __global__ void k_hist2d_pass1(const T* __restrict__ v, long long X, long long Y
 template <typename T>
 __global__ void k_hist2d_pass1b(const T* __restrict__ v, long long X, long long Y, long long Z, double c,
                                 Hist2DScratch* sc) {
-  const long long n = X * Y * Z;
   const unsigned long long smax = sc->smax;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    long long x = i % X, t = i / X, y = t % Y, z = t / Y;
-    int D[3];
-    int_diffs(v, X, Y, Z, x, y, z, i, D);
-    unsigned long long S = (unsigned long long)((long long)D[0] * D[0] + (long long)D[1] * D[1] + (long long)D[2] * D[2]);
-    if (S == smax && smax > 0) {
-      double g = grad_f64(v, X, Y, Z, x, y, z, i, c);
-      atomicMax(&sc->gmax_bits, (unsigned long long)__double_as_longlong(g));
+  if (smax == 0) return;
+  for (long long row = blockIdx.x; row < Y * Z; row += gridDim.x) {
+    const long long z = row / Y, y = row - z * Y;
+    for (long long x = threadIdx.x; x < X; x += blockDim.x) {
+      const long long i = row * X + x;
+      int D[3];
+      int_diffs(v, X, Y, Z, x, y, z, i, D);
+      const unsigned long long S =
+          (unsigned long long)((long long)D[0] * D[0] + (long long)D[1] * D[1] + (long long)D[2] * D[2]);
+      if (S == smax) {
+        const double g = grad_f64(v, X, Y, Z, x, y, z, i, c);
+        atomicMax(&sc->gmax_bits, (unsigned long long)__double_as_longlong(g));
+      }
     }
   }
 }
@@ -519,42 +533,44 @@ __global__ void k_hist2d_pass1b(const T* __restrict__ v, long long X, long long 
 template <typename T>
 __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y, long long Z, double c, long long nx,
                                long long merge, unsigned long long* __restrict__ hist, const Hist2DScratch* sc) {
-  const long long n = X * Y * Z;
   const unsigned long long smax = sc->smax;
   const double gmax = __longlong_as_double((long long)sc->gmax_bits);
   unsigned long long run_bin = ~0ULL, run = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    long long x = i % X, t = i / X, y = t % Y, z = t / Y;
-    int D[3];
-    int_diffs(v, X, Y, Z, x, y, z, i, D);
-    unsigned long long S = (unsigned long long)((long long)D[0] * D[0] + (long long)D[1] * D[1] + (long long)D[2] * D[2]);
-    int k = 0;
-    if (smax > 0 && S > 0) {
-      const unsigned long long lhs = 65025ULL * S;
-      k = (int)(255.0 * sqrt((double)S / (double)smax));
-      if (k > 255) k = 255;
-      while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
-      while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;
-      if ((unsigned long long)k * k * smax == lhs) {
-        // exact tie: the f64 formula decides between k and k - 1
-        double g = grad_f64(v, X, Y, Z, x, y, z, i, c);
-        double r = __dmul_rn(__ddiv_rn(g, gmax), 255.0);
-        k = (int)floor(r);
+  for (long long row = blockIdx.x; row < Y * Z; row += gridDim.x) {
+    const long long z = row / Y, y = row - z * Y;
+    for (long long x = threadIdx.x; x < X; x += blockDim.x) {
+      const long long i = row * X + x;
+      int D[3];
+      int_diffs(v, X, Y, Z, x, y, z, i, D);
+      const unsigned long long S =
+          (unsigned long long)((long long)D[0] * D[0] + (long long)D[1] * D[1] + (long long)D[2] * D[2]);
+      int k = 0;
+      if (smax > 0 && S > 0) {
+        const unsigned long long lhs = 65025ULL * S;
+        k = (int)(255.0 * sqrt((double)S / (double)smax));
         if (k > 255) k = 255;
+        while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
+        while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;
+        if ((unsigned long long)k * k * smax == lhs) {
+          // exact tie: the f64 formula decides between k and k - 1
+          const double g = grad_f64(v, X, Y, Z, x, y, z, i, c);
+          const double r = __dmul_rn(__ddiv_rn(g, gmax), 255.0);
+          k = (int)floor(r);
+          if (k > 255) k = 255;
+        }
       }
-    }
-    long long bx = (long long)__ldg(v + i) / merge;
-    if (bx >= nx) bx = nx - 1;
-    // run-length accumulation per thread: empty space puts almost every
-    // voxel in one bin, and one atomic per voxel (or per warp) on a single
-    // address serialises
-    const unsigned long long bin = (unsigned long long)(bx * 256 + k);
-    if (bin == run_bin) {
-      ++run;
-    } else {
-      if (run) atomicAdd(hist + run_bin, run);
-      run_bin = bin;
-      run = 1;
+      long long bx = (long long)__ldg(v + i) / merge;
+      if (bx >= nx) bx = nx - 1;
+      // run-length accumulation per thread: empty space puts almost every
+      // voxel in one bin, and one atomic per voxel on one address serialises
+      const unsigned long long bin = (unsigned long long)(bx * 256 + k);
+      if (bin == run_bin) {
+        ++run;
+      } else {
+        if (run) atomicAdd(hist + run_bin, run);
+        run_bin = bin;
+        run = 1;
+      }
     }
   }
   if (run) atomicAdd(hist + run_bin, run);
@@ -566,8 +582,9 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
   if (dtype == DT_F32) return cudaErrorInvalidValue;
   const long long X = dims[0], Y = dims[1], Z = dims[2];
   const double c = max_scalar > 0 ? max_scalar : 1.0;
-  int threads = 256;
-  int blocks = grid_for(X * Y * Z, threads);
+  const int threads = X >= 256 ? 256 : 128;
+  long long rows = Y * Z;
+  const int blocks = (int)(rows < 152LL * 64 ? rows : 152LL * 64);
   cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(Hist2DScratch), s);
   if (e != cudaSuccess) return e;
   if (dtype == DT_U8) {

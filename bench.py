@@ -275,6 +275,138 @@ def run_c3(args):
     return 0
 
 
+def run_c5(args):
+    """Serving mix (BASELINE config 5): Poisson arrivals of render requests
+    over 12 resident datasets (64^3 .. 1024^3, uint8 / uint16 / float32), image
+    sizes in {256^2, 512^2, 1280x720, 1920x1080}, a random 1D or 2D TF preset
+    and a random camera per request.  Capacity is measured first with a burst;
+    the Poisson stream then runs at 70% of it.  The plain per-request path
+    (one renderer paint + readback per request) is timed on the same requests."""
+    import threading as th
+    import numpy as np
+    from imagevis3d_gb300 import (GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, Renderer, Server, orbit_camera,
+                                  synth_params, workloads)
+    rng = np.random.default_rng(workloads.SEED + 5)
+    sizes_vol = [64, 96, 128, 192, 256, 320, 384, 512, 640, 768, 896, 1024]
+    dtypes = [np.uint8, np.uint16, np.float32]
+    specs = []
+    for i, n in enumerate(sizes_vol):
+        dt = dtypes[i % 3]
+        scale, vmax = {np.uint8: (255.0, 255.0), np.uint16: (2600.0, 4095.0), np.float32: (1.0, 1.0)}[dt]
+        specs.append(synth_params((n, n, n), dt, 500 + i, 24, (0.03 * n, 0.09 * n), (0.3, 1.0), scale,
+                                  noise_kind=2, noise_amp=0.02 * scale, vmax=vmax))
+    img_sizes = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
+    nreq = args.requests
+    srv = Server(max_batch=64, fb_budget_bytes=1 << 30)
+    ds, presets = [], []
+    for i, sp in enumerate(specs):
+        d = srv.add_synthetic(sp, brick_size=256, overlap=2, layouts=1)
+        ds.append(d)
+        vmax = float(sp.vmax) if sp.dtype != 2 else 1.0
+        t1 = workloads.tf1d_seeded(256, 700 + i, 0.3 * vmax, vmax)
+        t2 = workloads.tf2d_seeded(256, 128, 800 + i, zero_cols=60)
+        presets.append([(srv.add_tf(d, GBVR_RM_1DTRANS, t1), GBVR_RM_1DTRANS, t1),
+                        (srv.add_tf(d, GBVR_RM_2DTRANS, t2, grad_max=0.05), GBVR_RM_2DTRANS, t2)])
+    reqs = []
+    for _ in range(nreq):
+        di = int(rng.integers(0, len(ds)))
+        pi = int(rng.integers(0, 2))
+        w, h = img_sizes[int(rng.integers(0, 4))]
+        cam = orbit_camera(float(rng.uniform(0, 360)), float(rng.uniform(-45, 45)),
+                           float(rng.uniform(1.8, 3.0)) * workloads.DIAG, 45.0, w, h)
+        reqs.append((di, pi, w, h, cam))
+
+    def run_stream(arrivals):
+        tickets, done = [], []
+        q = []
+        lock = th.Lock()
+        finished = th.Event()
+
+        def waiter():
+            k = 0
+            while k < len(arrivals):
+                with lock:
+                    if k >= len(q):
+                        t = None
+                    else:
+                        t = q[k]
+                if t is None:
+                    time.sleep(0.0002)
+                    continue
+                srv.wait(t)
+                k += 1
+            finished.set()
+        wt = th.Thread(target=waiter, daemon=True)
+        wt.start()
+        t0 = time.perf_counter()
+        for (di, pi, w, h, cam), ta in zip(reqs, arrivals):
+            delay = ta - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            t = srv.submit(ds[di], presets[di][pi][0], w, h, cam[0], cam[1])
+            with lock:
+                q.append(t)
+        finished.wait()
+        return time.perf_counter() - t0
+
+    # warm-up and capacity (burst)
+    srv.reset_stats()
+    run_stream([0.0] * min(200, nreq))
+    srv.reset_stats()
+    wall = run_stream([0.0] * nreq)
+    burst = srv.stats()
+    capacity = burst["completed"] / wall
+    # Poisson arrivals at 70% of capacity
+    rate = 0.7 * capacity
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq)).tolist()
+    srv.reset_stats()
+    wall = run_stream(arrivals)
+    st = srv.stats()
+    srv.close()
+    # plain per-request path: one renderer per dataset, paint + readback
+    rends = []
+    for i, sp in enumerate(specs):
+        r = Renderer()
+        r.loadSynthetic(sp, brick_size=256, overlap=2)
+        rends.append(r)
+    sample = reqs[:min(len(reqs), args.plain_requests)]
+    lat = []
+    t0 = time.perf_counter()
+    for di, pi, w, h, cam in sample:
+        t1 = time.perf_counter()
+        r = rends[di]
+        _, mode, tf = presets[di][pi]
+        r.resize((w, h))
+        r.setRenderMode(mode)
+        if mode == GBVR_RM_1DTRANS:
+            r.set1DTrans(tf)
+        else:
+            r.set2DTrans(tf, 0.05)
+        r.setView(*cam)
+        r.paint()
+        r.readFramebuffer(0)
+        lat.append((time.perf_counter() - t1) * 1000.0)
+    plain_fps = len(sample) / (time.perf_counter() - t0)
+    for r in rends:
+        r.cleanup()
+    lat.sort()
+    out = {
+        "metric": "serving frames/s & p50/p99 latency (Poisson arrivals, continuous batching)",
+        "value": st["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": nreq, "warmup": 200,
+        "ms_per_step": 1000.0 / max(st["frames_per_s"], 1e-9), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded blob volumes)",
+        "config": {"workload": "c5_serving_12_datasets_%d_requests" % nreq, "datasets": "64^3..1024^3 u8/u16/f32",
+                   "image_sizes": img_sizes, "arrival_rate_per_s": rate, "max_batch": 64},
+        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"], "mean_batch": st["mean_batch"],
+        "burst_capacity_fps": capacity, "burst_p99_ms": burst["p99_ms"],
+        "plain_per_request_fps": plain_fps, "plain_p50_ms": lat[len(lat) // 2],
+        "plain_p99_ms": lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))],
+        "serving_vs_plain": capacity / plain_fps,
+    }
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -288,12 +420,16 @@ def main():
     ap.add_argument("--cpu-volume", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-texture", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"])
+    ap.add_argument("--requests", type=int, default=10000)
+    ap.add_argument("--plain-requests", type=int, default=600)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.workload == "c3" and args.impl == "ours":
         return run_c3(args)
+    if args.workload == "c5" and args.impl == "ours":
+        return run_c5(args)
 
     if args.impl == "reference":
         return run_reference(args)

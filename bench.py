@@ -528,21 +528,22 @@ def main():
         r.setLaunchShape(tune["tile_w"], tune["ctas_per_sm"])
 
     # ---- end to end through the public API with host buffers ----
-    fb = [None] * len(views)
+    # (the caller's destination is page-locked host memory, one copy per step)
+    import torch
+    host_fb = torch.empty((len(views), wl.height, wl.width, 4), dtype=torch.uint8, pin_memory=True)
     r.paintBatch(views)
-    for i in range(len(views)):
-        r.readFramebuffer(i)
+    r.readFramebuffers(0, len(views), host_fb)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         r.paintBatch(views)
-        for i in range(len(views)):
-            fb[i] = r.readFramebuffer(i)
+        r.readFramebuffers(0, len(views), host_fb)
     barrier()
     e2e_s = maxover(time.perf_counter() - t0)
     e2e = frames_total / e2e_s
     h2d = r.stats()["h2d_bytes"]
     d2h = len(views) * wl.width * wl.height * 4
+    del host_fb
 
     # per-view drop-in end to end: paint + readback one view at a time
     t0 = time.perf_counter()

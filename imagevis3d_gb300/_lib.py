@@ -148,6 +148,7 @@ SIGNATURES = {
     "gbvr_paint_views": [P, C.POINTER(View), I],
     "gbvr_read_framebuffer": [P, I, P, SZ],
     "gbvr_read_framebuffer_f32": [P, I, P, SZ],
+    "gbvr_read_framebuffers": [P, I, I, P, SZ],
     "gbvr_capture_single_frame": [P, CP, I],
     "gbvr_capture_view": [P, I, CP, I],
     "gbvr_load_tf1d_file": [CP, I, FP, I, C.POINTER(I)],

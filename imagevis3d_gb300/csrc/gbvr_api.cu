@@ -1436,6 +1436,16 @@ int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t byt
   return GBVR_OK;
 }
 
+int gbvr_read_framebuffers(gbvr_renderer* r, int first, int n, uint8_t* rgba8, size_t bytes) {
+  TRY(check_r(r));
+  const size_t per = (size_t)r->fb_w * r->fb_h * 4;
+  if (first < 0 || n <= 0 || first + n > r->last_views) return fail(GBVR_EINVAL, "view range out of range");
+  if (!rgba8 || bytes < per * n) return fail(GBVR_EINVAL, "framebuffer buffer too small");
+  CUDA_TRY(cudaMemcpyAsync(rgba8, (const char*)r->d_fb8.p + per * first, per * n, cudaMemcpyDeviceToHost, r->stream));
+  CUDA_TRY(cudaStreamSynchronize(r->stream));
+  return GBVR_OK;
+}
+
 int gbvr_read_framebuffer_f32(gbvr_renderer* r, int view, float* rgba, size_t bytes) {
   TRY(check_r(r));
   if (!r->d_fb32.p) return fail(GBVR_ESTATE, "renderer was created without the float framebuffer flag (1)");

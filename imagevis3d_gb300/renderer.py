@@ -288,6 +288,17 @@ class Renderer:
             L.call("gbvr_read_framebuffer", self._h, view, out.ctypes.data_as(C.c_void_p), out.nbytes)
         return out
 
+    def readFramebuffers(self, first=0, n=None, out=None):
+        """Views [first, first + n) in one copy into `out` (any writable
+        buffer of n*h*w*4 bytes, e.g. page-locked memory) or a new array."""
+        n = self._nviews - first if n is None else n
+        if out is None:
+            out = np.empty((n, self.height, self.width, 4), np.uint8)
+        ptr = out.data_ptr() if hasattr(out, "data_ptr") else out.ctypes.data
+        nbytes = out.numel() * out.element_size() if hasattr(out, "numel") else out.nbytes
+        L.call("gbvr_read_framebuffers", self._h, first, n, C.c_void_p(ptr), nbytes)
+        return out
+
     def captureSingleFrame(self, path, preserve_transparency=True):
         L.call("gbvr_capture_single_frame", self._h, path.encode(), 1 if preserve_transparency else 0)
 

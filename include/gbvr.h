@@ -229,6 +229,9 @@ int gbvr_paint_views(gbvr_renderer* r, const gbvr_view* views, int n);
  * StandaloneTuvok/CmdRenderer.cpp:34-56).  Row 0 is the top image row. ---- */
 int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t bytes);
 int gbvr_read_framebuffer_f32(gbvr_renderer* r, int view, float* rgba, size_t bytes);
+/* views [first, first + n) of the last paint in one copy: n x height x width
+ * RGBA8, view-major.  Faster into page-locked host memory. */
+int gbvr_read_framebuffers(gbvr_renderer* r, int first, int n, uint8_t* rgba8, size_t bytes);
 int gbvr_capture_single_frame(gbvr_renderer* r, const char* path, int preserve_transparency);
 /* capture view i of the last paint (the capture-sequence frames of
  * ImageVis3D_Capturing.cpp:188 / RenderWindow.cpp:1718-1725) */

@@ -301,3 +301,20 @@ def test_empty_space_skipping_is_exact(multibrick, mode):
         assert out[2][1]["samples"] <= out[1][1]["samples"] <= out[0][1]["samples"]
     if mode == GBVR_RM_1DTRANS:
         assert out[2][1]["samples"] < out[0][1]["samples"]
+
+
+def test_batch_readback_matches_per_view_readback(multibrick):
+    vol, _, tf = multibrick
+    views = workloads.orbit_views(3, 64, 40)
+    with Renderer() as r:
+        r.loadVolume(vol, brick_size=64, overlap=2)
+        r.resize((64, 40))
+        r.set1DTrans(tf)
+        r.paintBatch(views)
+        allv = r.readFramebuffers()
+        assert allv.shape == (3, 40, 64, 4)
+        for i in range(3):
+            assert np.array_equal(allv[i], r.readFramebuffer(i))
+        assert np.array_equal(r.readFramebuffers(1, 2)[1], allv[2])
+        with pytest.raises(GbvrError):
+            r.readFramebuffers(2, 2)

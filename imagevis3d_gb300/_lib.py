@@ -35,7 +35,8 @@ class DatasetInfo(C.Structure):
                 ("overlap", C.c_int32), ("lod_dims", (C.c_int64 * 3) * 16),
                 ("lod_bricks", (C.c_int32 * 3) * 16), ("total_bricks", C.c_int64),
                 ("device_bytes", C.c_uint64), ("hist1d_size", C.c_int32),
-                ("hist2d_max_grad", C.c_float)]
+                ("hist2d_max_grad", C.c_float), ("host_bytes", C.c_uint64), ("device_slots", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class View(C.Structure):
@@ -47,7 +48,8 @@ class Stats(C.Structure):
                 ("bricks_skipped", C.c_uint64), ("brick_bytes", C.c_uint64),
                 ("brick_misses", C.c_uint64), ("bytes_paged", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("lod", C.c_int32), ("subframes", C.c_int32), ("gpu_ms", C.c_double),
-                ("kernel_ms", C.c_double), ("cells_touched", C.c_uint64), ("cell_bytes", C.c_uint64)]
+                ("kernel_ms", C.c_double), ("cells_touched", C.c_uint64), ("cell_bytes", C.c_uint64),
+                ("page_ms", C.c_double)]
 
 
 class TuneResult(C.Structure):
@@ -156,6 +158,7 @@ SIGNATURES = {
     "gbvr_set_stats_level": [P, I],
     "gbvr_synth_volume": [C.POINTER(SynthParams), P, SZ],
     "gbvr_load_synthetic": [P, C.POINTER(SynthParams), C.POINTER(BrickParams)],
+    "gbvr_load_synthetic_ooc": [P, C.POINTER(SynthParams), C.POINTER(BrickParams), C.c_uint64],
     "gbvr_synth_fbm_volume": [C.POINTER(FbmParams), P, SZ],
     "gbvr_load_synthetic_fbm": [P, C.POINTER(FbmParams), C.POINTER(BrickParams)],
     "gbvr_build_uvf": [P, I64P, I, C.POINTER(BrickParams), CP],
@@ -164,6 +167,7 @@ SIGNATURES = {
     "gbvr_dev_downsample": [P, I, I64P, P, P],
     "gbvr_dev_synth_volume_noalloc": [C.POINTER(SynthParams), P, SZ, P],
     "gbvr_orbit_camera": [F, F, F, F, I, I, FP, FP],
+    "gbvr_look_at_camera": [FP, FP, FP, F, F, F, I, I, FP, FP],
     "gbvr_server_create": [C.POINTER(ServerParams), C.POINTER(P)],
     "gbvr_server_destroy": [P],
     "gbvr_server_add_volume": [P, P, I64P, I, C.POINTER(BrickParams), C.POINTER(I)],

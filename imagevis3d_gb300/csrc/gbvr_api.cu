@@ -195,6 +195,7 @@ struct Level {
   int brick_base;
   int nbricks;
   int nc[3];                          // macro-cell grid
+  int cell_shift = 2;                 // macro-cell edge = 1 << cell_shift voxels
   std::shared_ptr<DevBuf> cells;      // float2 min/max per macro-cell
 };
 
@@ -224,6 +225,19 @@ struct Dataset {
   std::vector<cudaArray_t> arrays;
   std::vector<cudaTextureObject_t> texs;
   std::string raster_id = "GB300 volume raster";
+  // Out of core: every brick lives in page-locked host memory (host_store,
+  // element offsets host_off); the device pool is a cache of nslots
+  // fixed-size slots, and BrickInfo.offset points at a brick's slot while
+  // it is resident.
+  bool ooc = false;
+  PinnedBuf host_store;
+  std::vector<unsigned long long> host_off;
+  size_t slot_elems = 0;
+  int nslots = 0;
+  std::vector<int> slot_of;                  // per brick, -1 = not resident
+  std::vector<int> slot_brick;               // per slot, -1 = free
+  std::vector<unsigned long long> slot_used; // frame of last use, per slot
+  unsigned long long frame = 0;
 
   void release() {
     for (auto t : texs) cudaDestroyTextureObject(t);
@@ -232,6 +246,15 @@ struct Dataset {
     arrays.clear();
     pool.release();
     d_bricks.release();
+    if (host_store.p) cudaFreeHost(host_store.p);
+    host_store.p = nullptr;
+    host_store.n = 0;
+    ooc = false;
+    host_off.clear();
+    slot_of.clear();
+    slot_brick.clear();
+    slot_used.clear();
+    nslots = 0;
     levels.clear();
     bricks.clear();
     hist1d.clear();
@@ -381,6 +404,7 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   for (size_t l = 0; l < ld.size(); ++l) {
     Level& L = ds.levels[l];
     long long d[3] = {ld[l][0], ld[l][1], ld[l][2]};
+    L.cell_shift = CELL_SHIFT;
     for (int a = 0; a < 3; ++a) L.nc[a] = (int)((d[a] + (1 << CELL_SHIFT) - 1) >> CELL_SHIFT);
     L.cells = std::make_shared<DevBuf>();
     CUDA_TRY(L.cells->alloc(sizeof(float2) * (size_t)L.nc[0] * L.nc[1] * L.nc[2]));
@@ -444,6 +468,239 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   return GBVR_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Out-of-core build.  The finest level is generated on the device in z-slabs
+// of S = 2^(levels-1) planes; every level keeps a window of its planes in
+// device memory.  From each window the build emits, as soon as their planes
+// are present: complete brick layers (interior + ghosts, the same bricks as
+// the in-core build) into the page-locked host store, macro-cell layers
+// (min/max) into the level's cell grid, and pairs of planes averaged into the
+// next level's window.  Planes no window still needs are dropped.  Device
+// memory is O(plane area x brick size), independent of the volume depth.
+// ---------------------------------------------------------------------------
+constexpr int OOC_CELL_SHIFT = 3;
+
+int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_params* bp, uint64_t pool_bytes,
+                    cudaStream_t s) {
+  ds.release();
+  const int dtype = p->dtype;
+  const size_t es = dtype_size(dtype);
+  ds.dtype = dtype;
+  long long dims[3] = {p->dims[0], p->dims[1], p->dims[2]};
+  for (int a = 0; a < 3; ++a) ds.dims[a] = dims[a];
+  ds.brick = bp && bp->brick_size > 0 ? bp->brick_size : 256;
+  ds.ghost = bp && bp->overlap > 0 ? bp->overlap : 2;
+  if (ds.ghost < 2) return fail(GBVR_EINVAL, "overlap must be >= 2 (gradients need two ghost voxels)");
+  if (ds.brick - 2 * ds.ghost < 8) return fail(GBVR_EINVAL, "brick_size too small for the overlap");
+  for (int a = 0; a < 3; ++a) ds.aspect[a] = (bp && bp->aspect[a] > 0) ? bp->aspect[a] : 1.0;
+  std::vector<std::array<long long, 3>> ld;
+  const int nlev = lod_dims(dims, ds.brick, ds.ghost, bp ? bp->max_lods : 0, ld);
+  unsigned long long cursor = 0;
+  for (int l = 0; l < nlev; ++l) {
+    Level L;
+    long long d[3] = {ld[l][0], ld[l][1], ld[l][2]};
+    plan_level(d, ds.brick, ds.ghost, l, L, ds.bricks, cursor, dtype);
+    L.cell_shift = OOC_CELL_SHIFT;
+    for (int a = 0; a < 3; ++a) L.nc[a] = (int)((d[a] + (1 << OOC_CELL_SHIFT) - 1) >> OOC_CELL_SHIFT);
+    L.cells = std::make_shared<DevBuf>();
+    CUDA_TRY(L.cells->alloc(sizeof(float2) * (size_t)L.nc[0] * L.nc[1] * L.nc[2]));
+    ds.levels.push_back(L);
+  }
+  const size_t nb = ds.bricks.size();
+  ds.host_off.resize(nb);
+  size_t max_brick = 0;
+  ds.stored_bytes = 0;
+  for (size_t i = 0; i < nb; ++i) {
+    const BrickInfo& b = ds.bricks[i];
+    ds.host_off[i] = b.offset;
+    const size_t n = (size_t)b.sx * b.sy * b.sz;
+    max_brick = std::max(max_brick, n);
+    ds.stored_bytes += n * es;
+  }
+  const size_t al = elem_align(dtype);
+  ds.slot_elems = (max_brick + al - 1) / al * al;
+  const size_t slot_bytes = ds.slot_elems * es;
+  ds.nslots = (int)std::min<uint64_t>(pool_bytes / slot_bytes, (uint64_t)nb);
+  if (ds.nslots < 1) return fail(GBVR_EINVAL, "device pool smaller than one brick");
+  CUDA_TRY(ds.pool.alloc((size_t)ds.nslots * slot_bytes));
+  ds.slot_of.assign(nb, -1);
+  ds.slot_brick.assign(ds.nslots, -1);
+  ds.slot_used.assign(ds.nslots, 0);
+  for (auto& b : ds.bricks) b.offset = 0;
+  {
+    cudaError_t e = cudaMallocHost(&ds.host_store.p, cursor * es);
+    if (e != cudaSuccess) return fail(GBVR_ENOMEM, "page-locked host brick store of " + std::to_string(cursor * es) + " bytes");
+    ds.host_store.n = cursor * es;
+  }
+  // generator tables
+  BlobTablesHost tab;
+  make_blob_tables(*p, tab);
+  DevBuf amp, ex, ey, ez, bx, by, bz;
+  auto up = [&](DevBuf& d, const std::vector<float>& v) -> cudaError_t {
+    cudaError_t e = d.alloc(sizeof(float) * std::max<size_t>(v.size(), 1));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(d.p, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice, s);
+  };
+  CUDA_TRY(up(amp, tab.amp));
+  CUDA_TRY(up(ex, tab.ex));
+  CUDA_TRY(up(ey, tab.ey));
+  CUDA_TRY(up(ez, tab.ez));
+  CUDA_TRY(up(bx, tab.bgx));
+  CUDA_TRY(up(by, tab.bgy));
+  CUDA_TRY(up(bz, tab.bgz));
+  const bool bg = p->bg_freq > 0;
+  BlobTablesDev td{p->nblobs, amp.as<float>(), ex.as<float>(), ey.as<float>(), ez.as<float>(),
+                   bg ? bx.as<float>() : nullptr, bg ? by.as<float>() : nullptr, bg ? bz.as<float>() : nullptr,
+                   p->bg_level, p->bg_amp, p->scale, p->noise_amp, p->noise_kind, p->vmax, p->seed};
+  // per-level windows
+  const long long I = ds.brick - 2 * ds.ghost, g = ds.ghost;
+  const long long S = std::max<long long>(2, 1LL << (nlev - 1));
+  struct Stage {
+    DevBuf a, b;
+    long long z0 = 0, n = 0, cap = 0, X = 0, Y = 0, Z = 0, ds_next = 0;
+    int next_bz = 0, next_cz = 0;
+    size_t plane = 0;
+  };
+  std::vector<Stage> st(nlev);
+  size_t max_layer = 0;
+  for (int l = 0; l < nlev; ++l) {
+    Stage& w = st[l];
+    w.X = ld[l][0];
+    w.Y = ld[l][1];
+    w.Z = ld[l][2];
+    w.plane = (size_t)w.X * w.Y * es;
+    const long long M = 1LL << OOC_CELL_SHIFT;
+    w.cap = std::min<long long>(w.Z, I + 2 * g + M + 3 + std::max<long long>(S >> l, 2) + 4);
+    CUDA_TRY(w.a.alloc(w.plane * w.cap));
+    CUDA_TRY(w.b.alloc(w.plane * w.cap));
+    max_layer = std::max(max_layer, (size_t)ds.levels[l].nb[0] * ds.levels[l].nb[1]);
+  }
+  DevBuf tmp, tmp_info, hist;
+  CUDA_TRY(tmp.alloc(max_layer * slot_bytes));
+  CUDA_TRY(tmp_info.alloc(sizeof(BrickInfo) * max_layer));
+  const int nbins = dtype == DT_U8 ? 256 : 65536;
+  if (dtype != DT_F32) {
+    CUDA_TRY(hist.alloc(sizeof(uint64_t) * nbins));
+    CUDA_TRY(cudaMemsetAsync(hist.p, 0, sizeof(uint64_t) * nbins, s));
+  }
+  std::vector<BrickInfo> layer;
+  auto process = [&](int l) -> int {
+    Stage& w = st[l];
+    Level& L = ds.levels[l];
+    const long long have_end = w.z0 + w.n;
+    long long d3[3] = {w.X, w.Y, w.Z};
+    // complete brick layers -> host store
+    while (w.next_bz < L.nb[2]) {
+      const long long hi = std::min<long long>((long long)w.next_bz * I + I + g, w.Z);
+      if (hi > have_end) break;
+      const int per = L.nb[0] * L.nb[1];
+      const int first = L.brick_base + w.next_bz * per;
+      layer.assign(ds.bricks.begin() + first, ds.bricks.begin() + first + per);
+      for (int j = 0; j < per; ++j) layer[j].offset = (unsigned long long)j * ds.slot_elems;
+      CUDA_TRY(cudaMemcpyAsync(tmp_info.p, layer.data(), sizeof(BrickInfo) * per, cudaMemcpyHostToDevice, s));
+      CUDA_TRY(launch_gather_bricks_window(w.a.p, dtype, d3, w.z0, tmp_info.as<BrickInfo>(), per, tmp.p, 0, s));
+      CUDA_TRY(launch_brick_minmax(tmp.p, dtype, tmp_info.as<BrickInfo>(), per, s));
+      CUDA_TRY(cudaMemcpyAsync(layer.data(), tmp_info.p, sizeof(BrickInfo) * per, cudaMemcpyDeviceToHost, s));
+      for (int j = 0; j < per; ++j) {
+        const BrickInfo& b = ds.bricks[first + j];
+        CUDA_TRY(cudaMemcpyAsync((char*)ds.host_store.p + ds.host_off[first + j] * es,
+                                 (const char*)tmp.p + (size_t)j * slot_bytes, (size_t)b.sx * b.sy * b.sz * es,
+                                 cudaMemcpyDeviceToHost, s));
+      }
+      CUDA_TRY(cudaStreamSynchronize(s));
+      for (int j = 0; j < per; ++j) {
+        ds.bricks[first + j].vmin = layer[j].vmin;
+        ds.bricks[first + j].vmax = layer[j].vmax;
+      }
+      ++w.next_bz;
+    }
+    // complete macro-cell layers -> cell grid
+    const long long M = 1LL << OOC_CELL_SHIFT;
+    int cz1 = w.next_cz;
+    while (cz1 < L.nc[2] && std::min<long long>(cz1 * M + M + 1, w.Z - 1) < have_end) ++cz1;
+    if (cz1 > w.next_cz) {
+      CUDA_TRY(launch_cell_minmax_layers(w.a.p, dtype, d3, w.z0, OOC_CELL_SHIFT, L.nc, w.next_cz, cz1,
+                                         L.cells->as<float2>(), s));
+      w.next_cz = cz1;
+    }
+    // pairs of planes -> next level
+    if (l + 1 < nlev) {
+      Stage& nx = st[l + 1];
+      long long k1 = w.ds_next;
+      while (2 * k1 < w.Z && std::min<long long>(2 * k1 + 2, w.Z) <= have_end) ++k1;
+      if (k1 > w.ds_next) {
+        const long long in0 = 2 * w.ds_next, in1 = std::min<long long>(2 * k1, w.Z);
+        const long long m = k1 - w.ds_next;
+        if (nx.n + m > nx.cap) return fail(GBVR_ECUDA, "out-of-core window overflow");
+        long long dd[3] = {w.X, w.Y, in1 - in0};
+        CUDA_TRY(launch_downsample((const char*)w.a.p + (in0 - w.z0) * w.plane, dtype, dd,
+                                   (char*)nx.a.p + nx.n * nx.plane, s));
+        nx.n += m;
+        w.ds_next = k1;
+      }
+    }
+    // drop planes no consumer needs any more
+    long long keep = w.Z;
+    if (w.next_bz < L.nb[2]) keep = std::min(keep, std::max<long long>((long long)w.next_bz * I - g, 0));
+    if (w.next_cz < L.nc[2]) keep = std::min(keep, std::max<long long>((long long)w.next_cz * M - 1, 0));
+    if (l + 1 < nlev && 2 * w.ds_next < w.Z) keep = std::min(keep, 2 * w.ds_next);
+    keep = std::min(keep, have_end);
+    if (keep > w.z0) {
+      const long long drop = keep - w.z0;
+      if (w.n - drop > 0)
+        CUDA_TRY(cudaMemcpyAsync(w.b.p, (const char*)w.a.p + drop * w.plane, (w.n - drop) * w.plane,
+                                 cudaMemcpyDeviceToDevice, s));
+      std::swap(w.a.p, w.b.p);
+      std::swap(w.a.n, w.b.n);
+      w.n -= drop;
+      w.z0 = keep;
+    }
+    return GBVR_OK;
+  };
+  Stage& w0 = st[0];
+  for (long long z = 0; z < w0.Z; z += S) {
+    const long long nz = std::min(S, w0.Z - z);
+    if (w0.n + nz > w0.cap) return fail(GBVR_ECUDA, "out-of-core window overflow");
+    char* dst = (char*)w0.a.p + w0.n * w0.plane;
+    CUDA_TRY(launch_synth_blobs_planes(td, dims, dtype, z, nz, dst, s));
+    if (dtype != DT_F32)
+      CUDA_TRY(launch_hist1d(dst, dtype, nz * w0.X * w0.Y, hist.as<unsigned long long>(), nbins, s));
+    w0.n += nz;
+    for (int l = 0; l < nlev; ++l) TRY(process(l));
+  }
+  for (int l = 0; l < nlev; ++l)
+    if (st[l].next_bz != ds.levels[l].nb[2] || st[l].next_cz != ds.levels[l].nc[2])
+      return fail(GBVR_ECUDA, "out-of-core build did not complete level " + std::to_string(l));
+  CUDA_TRY(ds.d_bricks.alloc(sizeof(BrickInfo) * nb));
+  CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * nb, cudaMemcpyHostToDevice, s));
+  ds.gmin = INFINITY;
+  ds.gmax = -INFINITY;
+  for (int i = 0; i < ds.levels[0].nbricks; ++i) {
+    ds.gmin = std::min(ds.gmin, (double)ds.bricks[i].vmin);
+    ds.gmax = std::max(ds.gmax, (double)ds.bricks[i].vmax);
+  }
+  if (dtype != DT_F32) {
+    std::vector<uint64_t> full(nbins);
+    CUDA_TRY(cudaMemcpyAsync(full.data(), hist.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    long long size = nbins;
+    while (size > 1 && full[size - 1] == 0) --size;
+    ds.merge = std::max<long long>(1, (size + 4095) / 4096);
+    ds.hist1d.assign((size + ds.merge - 1) / ds.merge, 0);
+    for (long long i = 0; i < size; ++i) ds.hist1d[i / ds.merge] += full[i];
+    ds.bit_width = dtype == DT_U8 ? 8 : 16;
+  } else {
+    ds.bit_width = 32;
+  }
+  ds.max_grad = 0.f;  // the 2D histogram is not built out of core
+  ds.layouts = 1;
+  ds.copy_stride = 0;
+  ds.ooc = true;
+  CUDA_TRY(cudaStreamSynchronize(s));
+  ds.loaded = true;
+  return GBVR_OK;
+}
 
 // Classify one level of a dataset against a transfer function: per brick a
 // skip byte (d_skip, indexed by global brick number) and per macro-cell the
@@ -594,7 +851,7 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
   f.empty_skip = p.empty_skip;
   f.occ = p.occ;
   for (int a = 0; a < 3; ++a) f.nc[a] = L.nc[a];
-  f.cell_shift = CELL_SHIFT;
+  f.cell_shift = L.cell_shift;
   f.tiles_x = (p.width + p.tile_w - 1) / p.tile_w;
   f.tiles_y = (p.height + 32 / p.tile_w - 1) / (32 / p.tile_w);
   // layout copy: the axis whose voxel-space extent along screen x is largest
@@ -654,7 +911,12 @@ struct gbvr_renderer {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
   DevBuf d_tf, d_skip, d_fb8, d_fb32, d_frames, d_prefix, d_counter, d_samples, d_touched, d_tfprefix, d_occ;
-  DevBuf d_cellbits, d_cellcount, d_occtmp;
+  DevBuf d_cellbits, d_cellcount, d_occtmp, d_ooc_skip;
+  // out-of-core paging state and the last paint's statistics
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_copy0 = nullptr, ev_copy1 = nullptr;
+  uint64_t last_misses = 0, last_paged = 0;
+  float last_page_ms = 0.f;
   long long cell_words = 0;
   PinnedBuf h_frames, h_prefix;
   bool tf_dirty = true, skip_dirty = true;
@@ -686,6 +948,9 @@ struct gbvr_renderer {
     if (ev1) cudaEventDestroy(ev1);
     if (evk0) cudaEventDestroy(evk0);
     if (evk1) cudaEventDestroy(evk1);
+    if (ev_copy0) cudaEventDestroy(ev_copy0);
+    if (ev_copy1) cudaEventDestroy(ev_copy1);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -794,6 +1059,11 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
   p.grad_max = r->tf2d_grad_max;
   p.skip = r->d_skip.as<unsigned char>();
   p.occ = r->d_occ.as<unsigned char>();
+  if (r->ds.ooc) {
+    // residency lives in the skip table: brick skipping is always on
+    p.skip = r->d_ooc_skip.as<unsigned char>();
+    p.empty_skip = std::max(p.empty_skip, 1);
+  }
   FrameDesc f;
   fill_frame(f, r->ds, p);
   const Level& L = r->ds.levels[level];
@@ -817,10 +1087,181 @@ struct PtrSnapshot {
   bool operator!=(const PtrSnapshot& o) const { return memcmp(p, o.p, sizeof(p)) != 0; }
 };
 
-int prepare(gbvr_renderer* r, int nviews, int& level) {
+// Out-of-core paging for the views of one paint: pick the finest level (from
+// the LOD limit down) whose bricks that may contribute and intersect a view
+// frustum fit the device slots, upload the missing ones on the copy stream
+// (evicting least-recently-used bricks the frame does not need), and build
+// the frame's skip table: a brick is skipped when it is empty under the TF or
+// not resident.  Bricks needed at the requested level but not resident when
+// the paint began count as misses.
+int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level) {
+  Dataset& ds = r->ds;
+  ensure_tf(r);
+  const bool two = r->mode == GBVR_RM_2DTRANS;
+  if (two && r->tf2d.empty()) return fail(GBVR_ESTATE, "2D transfer function not set");
+  const std::vector<float>& tf = two ? r->tf2d : r->tf1d;
+  const int w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4), h = two ? r->tf2d_h : 1;
+  std::vector<int> pre(w + 1, 0);
+  for (int x = 0; x < w; ++x) {
+    int nz = 0;
+    for (int y = 0; y < h && !nz; ++y) nz = tf[4 * ((size_t)y * w + x) + 3] != 0.f;
+    pre[x + 1] = pre[x] + nz;
+  }
+  double vlo, vhi;
+  default_range(r, vlo, vhi);
+  const float idx_scale = (float)((w - 1) / (vhi - vlo)), lo_f = (float)vlo;
+  auto nonempty = [&](const BrickInfo& b) {
+    if (r->mode == GBVR_RM_ISOSURFACE) return b.vmax >= r->iso;
+    float ilo = std::min(std::max((b.vmin - lo_f) * idx_scale, 0.f), (float)(w - 1));
+    float ihi = std::min(std::max((b.vmax - lo_f) * idx_scale, 0.f), (float)(w - 1));
+    int a0 = std::max((int)std::floor(ilo) - 1, 0), a1 = std::min((int)std::floor(ihi) + 2, w - 1);
+    return pre[a1 + 1] - pre[a0] > 0;
+  };
+  // view-projection matrices of the paint
+  std::vector<std::array<double, 16>> mats(n);
+  for (int v = 0; v < n; ++v) {
+    double V[16], P[16];
+    for (int i = 0; i < 16; ++i) { V[i] = views[v].view[i]; P[i] = views[v].proj[i]; }
+    mat_mul(P, V, mats[v].data());
+  }
+  double ext[3], mx = 0;
+  for (int a = 0; a < 3; ++a) { ext[a] = (double)ds.dims[a] * ds.aspect[a]; mx = std::max(mx, ext[a]); }
+  for (int a = 0; a < 3; ++a) ext[a] /= mx;
+  // conservative: the brick's interior grown by one voxel, all 8 corners
+  // outside one clip plane of every view means no ray of the paint samples it.
+  // Rays start on the near plane and run to the volume's far side, so the
+  // far plane does not cull.
+  auto visible = [&](const Level& L, const BrickInfo& b) {
+    const int lo[3] = {b.lox, b.loy, b.loz}, hi[3] = {b.hix, b.hiy, b.hiz};
+    double c[8][4];
+    for (int k = 0; k < 8; ++k)
+      for (int a = 0; a < 3; ++a) {
+        const double vx = (k >> a) & 1 ? hi[a] + 1.0 : lo[a] - 1.0;
+        c[k][a] = (vx + 0.5) / (double)L.dims[a] * ext[a] - 0.5 * ext[a];
+      }
+    for (int v = 0; v < n; ++v) {
+      const double* M = mats[v].data();
+      bool out = false;
+      for (int plane = 0; plane < 6 && !out; ++plane) {
+        if (plane == 4) continue;  // far
+        const int axis = plane >> 1;
+        const double sgn = (plane & 1) ? -1.0 : 1.0;
+        bool all = true;
+        for (int k = 0; k < 8 && all; ++k) {
+          double cl[4];
+          for (int rr = 0; rr < 4; ++rr)
+            cl[rr] = M[4 * rr] * c[k][0] + M[4 * rr + 1] * c[k][1] + M[4 * rr + 2] * c[k][2] + M[4 * rr + 3];
+          all = sgn * cl[axis] > cl[3];  // outside this side of the clip volume
+        }
+        out = all;
+      }
+      if (!out) return true;
+    }
+    return false;
+  };
+  const int nlev = (int)ds.levels.size();
+  const int target = level;
+  std::vector<int> needed;
+  uint64_t misses = 0;
+  for (int l = target; l < nlev; ++l) {
+    const Level& L = ds.levels[l];
+    needed.clear();
+    for (int i = 0; i < L.nbricks; ++i) {
+      const BrickInfo& b = ds.bricks[L.brick_base + i];
+      if (nonempty(b) && visible(L, b)) needed.push_back(L.brick_base + i);
+    }
+    if (l == target)
+      for (int bidx : needed) misses += ds.slot_of[bidx] < 0;
+    level = l;
+    if ((int)needed.size() <= ds.nslots) break;
+  }
+  if ((int)needed.size() > ds.nslots) needed.resize(ds.nslots);  // coarsest level still too large
+  ++ds.frame;
+  std::vector<char> want(ds.bricks.size(), 0);
+  for (int bidx : needed) {
+    want[bidx] = 1;
+    if (ds.slot_of[bidx] >= 0) ds.slot_used[ds.slot_of[bidx]] = ds.frame;
+  }
+  // victims: free slots first, then least recently used unwanted bricks
+  std::vector<int> victims;
+  for (int sl = 0; sl < ds.nslots; ++sl)
+    if (ds.slot_brick[sl] < 0 || !want[ds.slot_brick[sl]]) victims.push_back(sl);
+  std::sort(victims.begin(), victims.end(), [&](int x, int y) {
+    const bool fx = ds.slot_brick[x] < 0, fy = ds.slot_brick[y] < 0;
+    if (fx != fy) return fx;
+    return ds.slot_used[x] < ds.slot_used[y];
+  });
+  const size_t es = dtype_size(ds.dtype);
+  size_t vi = 0;
+  uint64_t bytes = 0;
+  // slots are overwritten only after every earlier paint has read them
+  CUDA_TRY(cudaEventRecord(r->ev_copy0, r->stream));
+  CUDA_TRY(cudaStreamWaitEvent(r->copy_stream, r->ev_copy0, 0));
+  CUDA_TRY(cudaEventRecord(r->ev_copy0, r->copy_stream));
+  for (int bidx : needed) {
+    if (ds.slot_of[bidx] >= 0) continue;
+    if (vi >= victims.size()) break;
+    const int sl = victims[vi++];
+    if (ds.slot_brick[sl] >= 0) ds.slot_of[ds.slot_brick[sl]] = -1;
+    ds.slot_brick[sl] = bidx;
+    ds.slot_of[bidx] = sl;
+    ds.slot_used[sl] = ds.frame;
+    const BrickInfo& b = ds.bricks[bidx];
+    const size_t nbytes = (size_t)b.sx * b.sy * b.sz * es;
+    CUDA_TRY(cudaMemcpyAsync((char*)ds.pool.p + (size_t)sl * ds.slot_elems * es,
+                             (const char*)ds.host_store.p + ds.host_off[bidx] * es, nbytes, cudaMemcpyHostToDevice,
+                             r->copy_stream));
+    bytes += nbytes;
+  }
+  CUDA_TRY(cudaEventRecord(r->ev_copy1, r->copy_stream));
+  CUDA_TRY(cudaStreamWaitEvent(r->stream, r->ev_copy1, 0));
+  // page table of the rendered level and its skip table
+  const Level& L = ds.levels[level];
+  std::vector<unsigned char> skip(ds.bricks.size(), 1);
+  for (int i = 0; i < L.nbricks; ++i) {
+    BrickInfo& b = ds.bricks[L.brick_base + i];
+    const int sl = ds.slot_of[L.brick_base + i];
+    b.offset = sl >= 0 ? (unsigned long long)sl * ds.slot_elems : 0;
+    skip[L.brick_base + i] = (sl >= 0 && nonempty(b)) ? 0 : 1;
+  }
+  CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.as<BrickInfo>() + L.brick_base, ds.bricks.data() + L.brick_base,
+                           sizeof(BrickInfo) * L.nbricks, cudaMemcpyHostToDevice, r->stream));
+  CUDA_TRY(r->d_ooc_skip.alloc(ds.bricks.size()));
+  CUDA_TRY(cudaMemcpyAsync(r->d_ooc_skip.p, skip.data(), skip.size(), cudaMemcpyHostToDevice, r->stream));
+  CUDA_TRY(cudaEventSynchronize(r->ev_copy1));
+  CUDA_TRY(cudaEventElapsedTime(&r->last_page_ms, r->ev_copy0, r->ev_copy1));
+  // the host tables above must outlive their copies
+  CUDA_TRY(cudaStreamSynchronize(r->stream));
+  r->last_misses = misses;
+  r->last_paged = bytes;
+  return GBVR_OK;
+}
+
+int prepare(gbvr_renderer* r, int nviews, int& level, const gbvr_view* views) {
   TRY(check_loaded(r));
   if (nviews <= 0) return fail(GBVR_EINVAL, "view count must be positive");
   level = render_level(r);
+  if (r->ds.ooc) {
+    if (!r->copy_stream) {
+      CUDA_TRY(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
+      CUDA_TRY(cudaEventCreate(&r->ev_copy0));
+      CUDA_TRY(cudaEventCreate(&r->ev_copy1));
+    }
+    std::vector<gbvr_view> vs;
+    if (!views) {
+      gbvr_view v;
+      if (r->view_set) {
+        memcpy(v.view, r->view, sizeof(v.view));
+        memcpy(v.proj, r->proj, sizeof(v.proj));
+      } else {
+        default_camera(r, v.view, v.proj);
+      }
+      vs.push_back(v);
+      views = vs.data();
+    }
+    TRY(ooc_page(r, views, views == vs.data() ? 1 : nviews, level));
+    r->drop_graphs();  // the page table changes between paints
+  }
   const size_t npix = (size_t)r->width * r->height;
   if (r->fb_views < nviews || r->fb_w != r->width || r->fb_h != r->height) {
     CUDA_TRY(r->d_fb8.alloc(npix * 4 * nviews));
@@ -855,7 +1296,7 @@ int finish(gbvr_renderer* r, int nviews, int level) {
 
 int paint_plain(gbvr_renderer* r, const gbvr_view* views, int n) {
   int level;
-  TRY(prepare(r, n, level));
+  TRY(prepare(r, n, level, views));
   CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream));
   CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
   if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words * n, r->stream));
@@ -880,7 +1321,7 @@ int paint_plain(gbvr_renderer* r, const gbvr_view* views, int n) {
 int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   int level;
   const PtrSnapshot before(r);
-  TRY(prepare(r, n, level));
+  TRY(prepare(r, n, level, views));
   CUDA_TRY(r->h_frames.alloc(sizeof(FrameDesc) * n));
   CUDA_TRY(r->h_prefix.alloc(sizeof(int) * (n + 1)));
   CUDA_TRY(r->d_frames.alloc(sizeof(FrameDesc) * n));
@@ -1136,6 +1577,18 @@ int gbvr_load_synthetic_fbm(gbvr_renderer* r, const gbvr_fbm_params* p, const gb
   return GBVR_OK;
 }
 
+int gbvr_load_synthetic_ooc(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr_brick_params* bp,
+                            uint64_t device_pool_bytes) {
+  TRY(check_r(r));
+  if (!p || p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 || p->nblobs < 0)
+    return fail(GBVR_EINVAL, "bad synthetic parameters");
+  r->drop_graphs();
+  r->skip_dirty = true;
+  r->tf_dirty = true;
+  TRY(build_ooc_synth(r->ds, p, bp, device_pool_bytes, r->stream));
+  return GBVR_OK;
+}
+
 int gbvr_load_uvf(gbvr_renderer* r, const char* path, int verify, const gbvr_brick_params* bp) {
   TRY(check_r(r));
   if (!path) return fail(GBVR_EINVAL, "null path");
@@ -1187,7 +1640,9 @@ int gbvr_get_dataset_info(gbvr_renderer* r, gbvr_dataset_info* info) {
       info->lod_bricks[l][a] = ds.levels[l].nb[a];
     }
   info->total_bricks = (int64_t)ds.bricks.size();
-  info->device_bytes = ds.stored_bytes;
+  info->device_bytes = ds.ooc ? (uint64_t)ds.nslots * ds.slot_elems * dtype_size(ds.dtype) : ds.stored_bytes;
+  info->host_bytes = ds.ooc ? ds.stored_bytes : 0;
+  info->device_slots = ds.ooc ? ds.nslots : 0;
   info->hist1d_size = (int)ds.hist1d.size();
   info->hist2d_max_grad = ds.max_grad;
   return GBVR_OK;
@@ -1234,6 +1689,10 @@ int gbvr_get_brick(gbvr_renderer* r, int lod, const int32_t brick[3], void* out,
   if (stored_dims) { stored_dims[0] = b.sx; stored_dims[1] = b.sy; stored_dims[2] = b.sz; }
   if (!out) return GBVR_OK;
   if (bytes < need) return fail(GBVR_EINVAL, "brick buffer too small");
+  if (r->ds.ooc) {
+    memcpy(out, (const char*)r->ds.host_store.p + r->ds.host_off[&b - r->ds.bricks.data()] * es, need);
+    return GBVR_OK;
+  }
   CUDA_TRY(cudaMemcpy(out, (const char*)r->ds.pool.p + b.offset * es, need, cudaMemcpyDeviceToHost));
   return GBVR_OK;
 }
@@ -1324,7 +1783,7 @@ int gbvr_set_interpolant(gbvr_renderer* r, int interp) {
 int gbvr_set_sampler(gbvr_renderer* r, int sampler) {
   TRY(check_r(r));
   if (sampler != GBVR_SAMPLER_SW && sampler != GBVR_SAMPLER_TEX) return fail(GBVR_EINVAL, "bad sampler");
-  if (sampler == GBVR_SAMPLER_TEX && r->ds.loaded && r->ds.texs.empty())
+  if (sampler == GBVR_SAMPLER_TEX && r->ds.loaded && (r->ds.texs.empty() || r->ds.ooc))
     return fail(GBVR_ESTATE, "dataset was loaded without build_texture");
   r->sampler = sampler;
   return GBVR_OK;
@@ -1488,7 +1947,10 @@ int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out) {
   out->subframes = 1;
   out->gpu_ms = r->last_ms;
   out->kernel_ms = r->last_kernel_ms;
-  out->h2d_bytes = r->last_h2d;
+  out->h2d_bytes = r->last_h2d + r->last_paged;
+  out->brick_misses = r->last_misses;
+  out->bytes_paged = r->last_paged;
+  out->page_ms = r->last_page_ms;
   if (r->last_views < 1 || !r->ds.loaded) return GBVR_OK;
   const int n = r->last_views;
   const Level& L = r->ds.levels[r->last_level];
@@ -1516,7 +1978,7 @@ int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out) {
                                r->stream));
     CUDA_TRY(cudaMemcpyAsync(cc.data(), r->d_cellcount.p, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, r->stream));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
-    const uint64_t cell_vox = (uint64_t)1 << (3 * CELL_SHIFT);
+    const uint64_t cell_vox = (uint64_t)1 << (3 * L.cell_shift);
     for (int v = 0; v < n; ++v) {
       out->cells_touched += cc[v];
       out->cell_bytes += cc[v] * cell_vox * es;
@@ -1535,6 +1997,7 @@ int gbvr_set_stats_level(gbvr_renderer* r, int level) {
 int gbvr_write_uvf(gbvr_renderer* r, const char* path) {
   TRY(check_loaded(r));
   if (!path) return fail(GBVR_EINVAL, "null path");
+  if (r->ds.ooc) return fail(GBVR_EINVAL, "out-of-core datasets are not written back as one raster");
   const Dataset& ds = r->ds;
   // LOD 0 re-assembled from its bricks' interiors
   const size_t es = dtype_size(ds.dtype);
@@ -1620,6 +2083,21 @@ int gbvr_dev_downsample(const void* dev_in, int dtype, const int64_t dims[3], vo
   if (!dev_in || !dev_out || !dims) return fail(GBVR_EINVAL, "bad argument");
   long long d[3] = {dims[0], dims[1], dims[2]};
   CUDA_TRY(launch_downsample(dev_in, dtype, d, dev_out, (cudaStream_t)stream));
+  return GBVR_OK;
+}
+
+int gbvr_look_at_camera(const float eye[3], const float ref[3], const float up[3], float fov_deg, float znear,
+                        float zfar, int width, int height, float view[16], float proj[16]) {
+  if (!eye || !ref || !up || !view || !proj || width <= 0 || height <= 0 || !(znear > 0) || !(zfar > znear))
+    return fail(GBVR_EINVAL, "bad camera");
+  double e[3] = {eye[0], eye[1], eye[2]}, c[3] = {ref[0], ref[1], ref[2]}, u[3] = {up[0], up[1], up[2]};
+  const double f[3] = {c[0] - e[0], c[1] - e[1], c[2] - e[2]};
+  const double x[3] = {f[1] * u[2] - f[2] * u[1], f[2] * u[0] - f[0] * u[2], f[0] * u[1] - f[1] * u[0]};
+  if (!(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] > 0)) return fail(GBVR_EINVAL, "camera direction parallel to up");
+  double V[16], P[16];
+  look_at(e, c, u, V);
+  perspective(fov_deg, (double)width / height, znear, zfar, P);
+  for (int i = 0; i < 16; ++i) { view[i] = (float)V[i]; proj[i] = (float)P[i]; }
   return GBVR_OK;
 }
 

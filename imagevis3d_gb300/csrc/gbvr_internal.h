@@ -137,6 +137,9 @@ struct BlobTablesDev {
 };
 cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], int dtype, void* out,
                                cudaStream_t s);
+// planes [z0, z0 + nz) of the volume into out (nz planes)
+cudaError_t launch_synth_blobs_planes(const BlobTablesDev& t, const long long dims[3], int dtype, long long z0,
+                                      long long nz, void* out, cudaStream_t s);
 cudaError_t launch_synth_fbm(const long long dims[3], int dtype, uint32_t seed, int octaves, int base_period,
                              float thr, float vmax, void* out, cudaStream_t s);
 cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3], void* out,
@@ -146,6 +149,11 @@ cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3]
 cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3],
                                  const BrickInfo* bricks_dev, int nbricks, void* pool,
                                  int perm, cudaStream_t s);
+// bricks from a window of the level holding planes vz0.. (their stored boxes,
+// clamped to the level, must lie in the window)
+cudaError_t launch_gather_bricks_window(const void* level, int dtype, const long long dims[3], long long vz0,
+                                        const BrickInfo* bricks_dev, int nbricks, void* pool, int perm,
+                                        cudaStream_t s);
 cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_dev, int nbricks,
                                 cudaStream_t s);
 // Macro-cell min/max of a flat level: cell c covers sample cells [c M, c M + M)
@@ -154,6 +162,10 @@ cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_d
 // across a cell face is still covered.
 cudaError_t launch_cell_minmax(const void* level, int dtype, const long long dims[3], int cell_shift,
                                const int nc[3], float2* out, cudaStream_t s);
+// cell layers [cz0, cz1) from a window of the level holding planes vz0.. (the
+// layers' footprints must lie in the window)
+cudaError_t launch_cell_minmax_layers(const void* level, int dtype, const long long dims[3], long long vz0,
+                                      int cell_shift, const int nc[3], int cz0, int cz1, float2* out, cudaStream_t s);
 cudaError_t launch_hist1d(const void* vol, int dtype, long long n, unsigned long long* hist,
                           int nbins, cudaStream_t s);
 // 2D histogram passes; scratch holds the pass-1 reduction state.

@@ -52,9 +52,11 @@ __device__ __forceinline__ float blob_noise(const BlobTablesDev& t, unsigned lon
 
 // One CTA per (y, z) row; blob weights of the row staged in shared memory.
 template <typename T>
-__global__ void k_synth_blobs(BlobTablesDev t, long long X, long long Y, long long Z, T* __restrict__ out) {
+__global__ void k_synth_blobs(BlobTablesDev t, long long X, long long Y, long long Z, long long z0,
+                              T* __restrict__ out) {
   extern __shared__ float w_row[];
-  const long long y = blockIdx.x, z = blockIdx.y;
+  // this CTA's row: global z = z0 + blockIdx.y; out holds planes from z0 on
+  const long long y = blockIdx.x, z = z0 + blockIdx.y;
   for (int k = threadIdx.x; k < t.nblobs; k += blockDim.x) {
     float w = __fmul_rn(t.amp[k], t.ez[(long long)k * Z + z]);
     w_row[k] = __fmul_rn(w, t.ey[(long long)k * Y + y]);
@@ -72,27 +74,34 @@ __global__ void k_synth_blobs(BlobTablesDev t, long long X, long long Y, long lo
     }
     for (int k = 0; k < t.nblobs; ++k) acc = __fadd_rn(acc, __fmul_rn(w_row[k], __ldg(t.ex + (long long)k * X + x)));
     float v = __fmul_rn(acc, t.scale);
-    long long idx = (z * Y + y) * X + x;
+    const long long idx = (z * Y + y) * X + x;  // global voxel index (seeds the noise)
+    const long long o = ((z - z0) * Y + y) * X + x;
     v = __fadd_rn(v, blob_noise(t, (unsigned long long)idx));
     if (sizeof(T) == 4) {
-      out[idx] = (T)v;
+      out[o] = (T)v;
     } else {
       float r = rintf(v);
       r = fminf(fmaxf(r, 0.0f), t.vmax);
-      out[idx] = (T)r;
+      out[o] = (T)r;
     }
   }
 }
 
-cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], int dtype, void* out, cudaStream_t s) {
+cudaError_t launch_synth_blobs_planes(const BlobTablesDev& t, const long long dims[3], int dtype, long long z0,
+                                      long long nz, void* out, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
-  dim3 grid((unsigned)dims[1], (unsigned)dims[2]);
+  if (nz <= 0) return cudaSuccess;
+  dim3 grid((unsigned)dims[1], (unsigned)nz);
   int threads = dims[0] >= 256 ? 256 : 128;
   size_t smem = sizeof(float) * (t.nblobs > 0 ? t.nblobs : 1);
-  if (dtype == DT_U8) k_synth_blobs<uint8_t><<<grid, threads, smem, s>>>(t, dims[0], dims[1], dims[2], (uint8_t*)out);
-  else if (dtype == DT_U16) k_synth_blobs<uint16_t><<<grid, threads, smem, s>>>(t, dims[0], dims[1], dims[2], (uint16_t*)out);
-  else k_synth_blobs<float><<<grid, threads, smem, s>>>(t, dims[0], dims[1], dims[2], (float*)out);
+  if (dtype == DT_U8) k_synth_blobs<uint8_t><<<grid, threads, smem, s>>>(t, dims[0], dims[1], dims[2], z0, (uint8_t*)out);
+  else if (dtype == DT_U16) k_synth_blobs<uint16_t><<<grid, threads, smem, s>>>(t, dims[0], dims[1], dims[2], z0, (uint16_t*)out);
+  else k_synth_blobs<float><<<grid, threads, smem, s>>>(t, dims[0], dims[1], dims[2], z0, (float*)out);
   return cudaGetLastError();
+}
+
+cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], int dtype, void* out, cudaStream_t s) {
+  return launch_synth_blobs_planes(t, dims, dtype, 0, dims[2], out, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -239,8 +248,9 @@ cudaError_t launch_downsample(const void* in, int dtype, const long long dims[3]
 // x fastest so both sides are coalesced.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_gather(const T* __restrict__ level, long long X, long long Y, long long Z,
+__global__ void k_gather(const T* __restrict__ level, long long X, long long Y, long long Z, long long vz0,
                          const BrickInfo* __restrict__ bricks, T* __restrict__ pool, int perm) {
+  // level holds planes vz0.. of the level (0: the whole level)
   const BrickInfo b = bricks[blockIdx.y];
   const long long plane = (long long)b.sx * b.sy;
   // destination strides of x, y, z in this layout copy (perm 3: 4^3 blocks,
@@ -263,24 +273,30 @@ __global__ void k_gather(const T* __restrict__ level, long long X, long long Y, 
         di = ((((long long)(zs >> 2) * nby + (r >> 2)) * nbx + (xs >> 2)) << 6) + ((zs & 3) << 4) + ((r & 3) << 2) + (xs & 3);
       else
         di = xs * s0 + r * s1 + zs * s2;
-      pool[b.offset + di] = __ldg(level + (z * Y + y) * X + x);
+      pool[b.offset + di] = __ldg(level + ((z - vz0) * Y + y) * X + x);
     }
   }
 }
 
-cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3], const BrickInfo* bricks_dev,
-                                 int nbricks, void* pool, int perm, cudaStream_t s) {
+cudaError_t launch_gather_bricks_window(const void* level, int dtype, const long long dims[3], long long vz0,
+                                        const BrickInfo* bricks_dev, int nbricks, void* pool, int perm,
+                                        cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (nbricks <= 0) return cudaSuccess;
   dim3 grid((unsigned)(dims[2] < 256 ? dims[2] : 256), (unsigned)nbricks);
   int threads = 256;
   if (dtype == DT_U8)
-    k_gather<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], bricks_dev, (uint8_t*)pool, perm);
+    k_gather<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], vz0, bricks_dev, (uint8_t*)pool, perm);
   else if (dtype == DT_U16)
-    k_gather<uint16_t><<<grid, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], dims[2], bricks_dev, (uint16_t*)pool, perm);
+    k_gather<uint16_t><<<grid, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], dims[2], vz0, bricks_dev, (uint16_t*)pool, perm);
   else
-    k_gather<float><<<grid, threads, 0, s>>>((const float*)level, dims[0], dims[1], dims[2], bricks_dev, (float*)pool, perm);
+    k_gather<float><<<grid, threads, 0, s>>>((const float*)level, dims[0], dims[1], dims[2], vz0, bricks_dev, (float*)pool, perm);
   return cudaGetLastError();
+}
+
+cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3], const BrickInfo* bricks_dev,
+                                 int nbricks, void* pool, int perm, cudaStream_t s) {
+  return launch_gather_bricks_window(level, dtype, dims, 0, bricks_dev, nbricks, pool, perm, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -335,11 +351,12 @@ cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_d
 // GridLeaper-style acceleration).
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_cell_minmax(const T* __restrict__ v, long long X, long long Y, long long Z, int sh, int ncx, int ncy,
-                              int ncz, float2* __restrict__ out) {
-  const long long n = (long long)ncx * ncy * ncz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const long long cx = i % ncx, t = i / ncx, cy = t % ncy, cz = t / ncy;
+__global__ void k_cell_minmax(const T* __restrict__ v, long long X, long long Y, long long Z, long long vz0, int sh,
+                              int ncx, int ncy, int cz0, int cz1, float2* __restrict__ out) {
+  // v holds planes vz0 .. of the level; cells of layers [cz0, cz1) are written
+  const long long n = (long long)ncx * ncy * (cz1 - cz0);
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+    const long long cx = j % ncx, t = j / ncx, cy = t % ncy, cz = cz0 + t / ncy;
     // one voxel of margin beyond the footprint [c M, c M + M] on each side:
     // the walk skips empty cells by their estimated exit, and a sample that
     // rounding puts in a neighbouring cell is at most that far outside
@@ -349,30 +366,36 @@ __global__ void k_cell_minmax(const T* __restrict__ v, long long X, long long Y,
     float mn = INFINITY, mx = -INFINITY;
     for (long long z = z0; z <= z1; ++z)
       for (long long y = y0; y <= y1; ++y) {
-        const T* row = v + (z * Y + y) * X;
+        const T* row = v + ((z - vz0) * Y + y) * X;
         for (long long x = x0; x <= x1; ++x) {
           float a = (float)__ldg(row + x);
           mn = fminf(mn, a);
           mx = fmaxf(mx, a);
         }
       }
-    out[i] = make_float2(mn, mx);
+    out[((long long)cz * ncy + cy) * ncx + cx] = make_float2(mn, mx);
   }
+}
+
+cudaError_t launch_cell_minmax_layers(const void* level, int dtype, const long long dims[3], long long vz0, int sh,
+                                      const int nc[3], int cz0, int cz1, float2* out, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  const long long n = (long long)nc[0] * nc[1] * (cz1 - cz0);
+  if (n <= 0) return cudaSuccess;
+  int threads = 128;
+  int blocks = grid_for(n, threads);
+  if (dtype == DT_U8)
+    k_cell_minmax<uint8_t><<<blocks, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], vz0, sh, nc[0], nc[1], cz0, cz1, out);
+  else if (dtype == DT_U16)
+    k_cell_minmax<uint16_t><<<blocks, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], dims[2], vz0, sh, nc[0], nc[1], cz0, cz1, out);
+  else
+    k_cell_minmax<float><<<blocks, threads, 0, s>>>((const float*)level, dims[0], dims[1], dims[2], vz0, sh, nc[0], nc[1], cz0, cz1, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_cell_minmax(const void* level, int dtype, const long long dims[3], int sh, const int nc[3],
                                float2* out, cudaStream_t s) {
-  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
-  const long long n = (long long)nc[0] * nc[1] * nc[2];
-  int threads = 128;
-  int blocks = grid_for(n, threads);
-  if (dtype == DT_U8)
-    k_cell_minmax<uint8_t><<<blocks, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], sh, nc[0], nc[1], nc[2], out);
-  else if (dtype == DT_U16)
-    k_cell_minmax<uint16_t><<<blocks, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], dims[2], sh, nc[0], nc[1], nc[2], out);
-  else
-    k_cell_minmax<float><<<blocks, threads, 0, s>>>((const float*)level, dims[0], dims[1], dims[2], sh, nc[0], nc[1], nc[2], out);
-  return cudaGetLastError();
+  return launch_cell_minmax_layers(level, dtype, dims, 0, sh, nc, 0, nc[2], out, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -440,8 +440,18 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
 #pragma unroll 1
             for (int it = 0; it < 4; ++it) {
               float tm = 0.5f * (tl + th);
-              float vm = sample_anywhere<T, SAMPLER>(f, fmaf(tm, r.dv[0], r.ov[0]), fmaf(tm, r.dv[1], r.ov[1]),
-                                                     fmaf(tm, r.dv[2], r.ov[2]));
+              const Cell mc = make_cell(f, fmaf(tm, r.dv[0], r.ov[0]), fmaf(tm, r.dv[1], r.ov[1]),
+                                        fmaf(tm, r.dv[2], r.ov[2]));
+              // within one voxel of this brick's interior its ghosts hold the
+              // neighbours' voxels, so the current brick answers (same values;
+              // an out-of-core neighbour need not be resident)
+              float vm;
+              if (mc.x >= b.lox - 1 && mc.x <= b.hix && mc.y >= b.loy - 1 && mc.y <= b.hiy && mc.z >= b.loz - 1 &&
+                  mc.z <= b.hiz)
+                vm = sample_cell<T, SAMPLER>(f, b, mc.x, mc.y, mc.z, mc.fx, mc.fy, mc.fz);
+              else
+                vm = sample_anywhere<T, SAMPLER>(f, fmaf(tm, r.dv[0], r.ov[0]), fmaf(tm, r.dv[1], r.ov[1]),
+                                                 fmaf(tm, r.dv[2], r.ov[2]));
               if (vm >= f.iso) th = tm;
               else tl = tm;
             }

@@ -85,6 +85,16 @@ def orbit_camera(azimuth_deg, elevation_deg, radius, fov_deg, width, height):
     return v.reshape(4, 4), pr.reshape(4, 4)
 
 
+def look_at_camera(eye, ref, up, fov_deg, width, height, znear=0.01, zfar=20.0):
+    """View and projection of a camera at `eye` looking at `ref`."""
+    v = np.zeros(16, np.float32)
+    pr = np.zeros(16, np.float32)
+    e, c, u = (np.ascontiguousarray(x, np.float32) for x in (eye, ref, up))
+    L.call("gbvr_look_at_camera", e.ctypes.data_as(L.FP), c.ctypes.data_as(L.FP), u.ctypes.data_as(L.FP),
+           fov_deg, znear, zfar, width, height, v.ctypes.data_as(L.FP), pr.ctypes.data_as(L.FP))
+    return v.reshape(4, 4), pr.reshape(4, 4)
+
+
 def synth_volume(params):
     """Generate a seeded volume on the GPU and return it as a (z, y, x) array."""
     dims = [params.dims[i] for i in range(3)]
@@ -138,6 +148,9 @@ class Renderer:
         else:
             L.call("gbvr_load_synthetic", self._h, C.byref(params), C.byref(brick_params(**bp)))
 
+    def loadSyntheticOutOfCore(self, params, device_pool_bytes, **bp):
+        L.call("gbvr_load_synthetic_ooc", self._h, C.byref(params), C.byref(brick_params(**bp)), device_pool_bytes)
+
     def datasetInfo(self):
         info = L.DatasetInfo()
         L.call("gbvr_get_dataset_info", self._h, C.byref(info))
@@ -148,7 +161,8 @@ class Renderer:
                     lod_dims=[tuple(info.lod_dims[i]) for i in range(n)],
                     lod_bricks=[tuple(info.lod_bricks[i]) for i in range(n)],
                     total_bricks=info.total_bricks, device_bytes=info.device_bytes,
-                    hist1d_size=info.hist1d_size, hist2d_max_grad=info.hist2d_max_grad)
+                    hist1d_size=info.hist1d_size, hist2d_max_grad=info.hist2d_max_grad,
+                    host_bytes=info.host_bytes, device_slots=info.device_slots)
 
     def getHistogram(self):
         n = self.datasetInfo()["hist1d_size"]

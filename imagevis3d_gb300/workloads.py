@@ -11,7 +11,7 @@ import math
 
 import numpy as np
 
-from .renderer import fbm_params, orbit_camera, synth_params
+from .renderer import fbm_params, look_at_camera, orbit_camera, synth_params
 
 SEED = 20261203
 DIAG = math.sqrt(3.0)  # diagonal of the unit-normalised cube
@@ -123,4 +123,120 @@ def config3(size=2048, width=2560, height=1440, nviews=16, brick=256, seed=SEED 
                   dict(brick_size=brick, overlap=2), tf, 1.0, width, height, views,
                   value_range=(0.0, 255.0), mode=1)
     wl.isovalues = isos
+    return wl
+
+
+# ---------------------------------------------------------------------------
+# Fly-through camera path, restated from the reference's animator
+# (LuaScripts/FlyThroughAnimator.lua:197-330 and 406-463): the first and last
+# key points are duplicated (the non-looping preview); each segment between
+# key points p1 and p2 is a cubic Bezier whose inner control points follow
+# the neighbours' direction at half the segment length (computeTangents); the
+# eye curve is sampled adaptively into an arc-length table (split while the
+# chord and the two half chords differ by more than epsilon = linear length /
+# 100000, each leaf adding its mid and end parameter); frames sit at equal arc
+# length, with eye, ref and up each interpolated on their own Bezier.
+# Parameters here are 0-based key indices (the script's are 1-based).
+# ---------------------------------------------------------------------------
+def _lerp(a, b, t):
+    return a + (b - a) * t
+
+
+def _decasteljau(p0, p1, p2, p3, u):
+    p10, p11, p12 = _lerp(p0, p1, u), _lerp(p1, p2, u), _lerp(p2, p3, u)
+    p20, p21 = _lerp(p10, p11, u), _lerp(p11, p12, u)
+    p30 = _lerp(p20, p21, u)
+    return p10, p20, p30, p21, p12
+
+
+def _tangents(p0, p1, p2, p3):
+    alpha = np.linalg.norm(p2 - p1) / 2.0
+    if alpha == 0.0:
+        return p1, p2
+    n1 = (p2 - p0) / np.linalg.norm(p2 - p0)
+    n2 = (p1 - p3) / np.linalg.norm(p1 - p3)
+    return p1 + n1 * alpha, p2 + n2 * alpha
+
+
+def _sample(p1, q1, q2, p2, ua, ub, eps, samples):
+    # (ua, ub) are the curve parameters at the middle and at the end of this piece
+    seg = _decasteljau(p1, q1, q2, p2, 0.5)
+    p = seg[2]
+    a, b, c = np.linalg.norm(p - p1), np.linalg.norm(p2 - p), np.linalg.norm(p2 - p1)
+    if abs(c - (a + b)) > eps:
+        u = (ub - ua) / 2
+        _sample(p1, seg[0], seg[1], p, ua - u, ua, eps, samples)
+        _sample(p, seg[3], seg[4], p2, ub - u, ub, eps, samples)
+    else:
+        d = samples[-1][0]
+        samples.append((d + a, ua))
+        samples.append((d + a + b, ub))
+
+
+def arc_length_table(keys, split=100000):
+    """keys: the animation's key points (already padded).  Returns the list of
+    (distance, parameter) pairs."""
+    eyes = [k[0] for k in keys]
+    dist = sum(np.linalg.norm(eyes[i - 1] - eyes[i - 2]) for i in range(3, len(keys)))
+    eps = dist / split
+    samples = [(0.0, 1.0)]
+    for i in range(3, len(keys)):
+        q1, q2 = _tangents(eyes[i - 3], eyes[i - 2], eyes[i - 1], eyes[i])
+        _sample(eyes[i - 2], q1, q2, eyes[i - 1], i - 1.5, i - 1.0, eps, samples)
+    return samples
+
+
+def _camera_at(keys, table, s):
+    idx = 1
+    while table[idx][0] < s:
+        idx += 1
+    (d0, u0), (d1, u1) = table[idx - 1], table[idx]
+    u = u0 + (s - d0) / (d1 - d0) * (u1 - u0) if d1 != d0 else u0
+    i = int(np.floor(u))
+    w = u - i
+    if w == 0.0:
+        return keys[i]
+    cam = []
+    for c in range(3):
+        q1, q2 = _tangents(keys[i - 1][c], keys[i][c], keys[i + 1][c], keys[i + 2][c])
+        cam.append(_decasteljau(keys[i][c], q1, q2, keys[i + 1][c], w)[2])
+    return tuple(cam)
+
+
+def flythrough(keys, frames):
+    """keys: list of (eye, ref, up) key points (at least two); returns `frames`
+    (eye, ref, up) triples at equal arc length from the first key to the last."""
+    keys = [tuple(np.asarray(k, np.float64) for k in key) for key in keys]
+    keys = [keys[0]] + keys + [keys[-1]]
+    table = arc_length_table(keys)
+    total = table[-1][0]
+    return [_camera_at(keys, table, min(total * f / max(frames - 1, 1), total)) for f in range(frames)]
+
+
+def flythrough_views(keys, frames, width, height, fov=45.0, znear=0.01, zfar=10.0):
+    return [look_at_camera(e, r, u, fov, width, height, znear, zfar) for e, r, u in flythrough(keys, frames)]
+
+
+def config4(size=(8192, 8192, 4096), width=1920, height=1080, frames=120, brick=256, lods=6, seed=SEED + 4):
+    """Out-of-core volume: 192 seeded blobs over a low-frequency background
+    layer, uint8, 256^3 bricks with 2 ghosts and `lods` levels, a fly-through
+    of `frames` frames at width x height (from outside the volume into it and
+    through), 1D TF with 256 entries (alpha 0 below 60)."""
+    n = max(size)
+    sp = synth_params(size, np.uint8, seed, 192, (0.01 * n, 0.04 * n), (0.3, 1.0), 255.0, noise_kind=1,
+                      noise_amp=4.0, vmax=255.0, bg_freq=1.5, bg_level=0.08, bg_amp=0.1)
+    tf = tf1d_seeded(256, seed, 60.0, 255.0)
+    m = [s / n for s in size]  # normalised half extents are m / 2
+    keys = [((-0.9 * m[0], 0.1, -0.6 * m[2]), (0.0, 0.0, 0.0), (0, 1, 0)),
+            ((-0.45 * m[0], 0.05, -0.35 * m[2]), (0.1, 0.0, 0.1), (0, 1, 0)),
+            ((0.0, -0.05, -0.25 * m[2]), (0.2, -0.05, 0.3), (0, 1, 0)),
+            ((0.35 * m[0], 0.0, 0.0), (0.0, 0.0, 0.35 * m[2]), (0, 1, 0)),
+            ((0.3 * m[0], 0.05, 0.35 * m[2]), (-0.2, 0.0, 0.2), (0, 1, 0)),
+            ((-0.1 * m[0], 0.1, 0.45 * m[2]), (-0.35, 0.0, 0.0), (0, 1, 0)),
+            ((-0.5 * m[0], 0.1, 0.2 * m[2]), (-0.2, 0.0, -0.3), (0, 1, 0))]
+    views = flythrough_views(keys, frames, width, height)
+    wl = Workload("c4_%dx%dx%d_u8_ooc_%dx%d_x%d" % (size[0], size[1], size[2], width, height, frames), sp,
+                  dict(brick_size=brick, overlap=2, max_lods=lods), tf, 1.0, width, height, views,
+                  value_range=(0.0, 255.0))
+    wl.keys = keys
     return wl

@@ -104,6 +104,9 @@ typedef struct gbvr_dataset_info {
   uint64_t device_bytes;  /* bytes of the brick pool (sum of stored bricks) */
   int32_t hist1d_size;    /* bins of the 1D histogram (<= 4096) */
   float hist2d_max_grad;  /* max gradient magnitude of the 2D histogram */
+  uint64_t host_bytes;    /* out of core: bytes of the page-locked host brick store */
+  int32_t device_slots;   /* out of core: bricks the device pool holds at once */
+  int32_t reserved;
 } gbvr_dataset_info;
 
 /* One view of a batch: camera, output size and (optionally) its own TF. */
@@ -127,6 +130,7 @@ typedef struct gbvr_stats {
   double kernel_ms;            /* device time of its raycast kernel launch(es) alone */
   uint64_t cells_touched;      /* stats level 2: sum over views of distinct non-empty macro-cells sampled */
   uint64_t cell_bytes;         /* ... times the cell's voxel bytes (4^3 voxels) */
+  double page_ms;              /* out of core: device time of the last paint's brick uploads */
 } gbvr_stats;
 
 /* ---- errors / device ---- */
@@ -263,6 +267,18 @@ typedef struct gbvr_synth_params {
 } gbvr_synth_params;
 
 int gbvr_synth_volume(const gbvr_synth_params* p, void* host_out, size_t bytes);
+/* Out of core (the reference's GPU-memory-capped brick cache, GPUMemMan with
+ * MaxGPUMem, ImageVis3D_Settings.cpp:509-514): the seeded volume is generated
+ * and bricked on the device in z-slabs straight into a page-locked host
+ * brick store (all LOD levels, same bricks as the in-core build), and the
+ * device keeps at most device_pool_bytes of bricks.  Each paint pages in the
+ * bricks its views need (non-empty under the TF, inside a view frustum) on a
+ * side stream, evicting least-recently-used ones; when they do not fit, the
+ * paint falls back to the finest coarser level that fits.  gbvr_get_stats
+ * reports the level used, brick misses, bytes paged and their device time.
+ * The 2D histogram is not built out of core (max gradient 0). */
+int gbvr_load_synthetic_ooc(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr_brick_params* bp,
+                            uint64_t device_pool_bytes);
 int gbvr_load_synthetic(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr_brick_params* bp);
 
 /* Seeded fractal volume: `octaves` octaves of periodic value noise (lattice
@@ -395,6 +411,13 @@ int gbvr_orbit_camera(float azimuth_deg, float elevation_deg, float radius, floa
  * loadFromFileWithSize does for the dataset's histogram size); 0 keeps N.
  * Writes at most `capacity` entries and the count to *n_out. */
 int gbvr_load_tf1d_file(const char* path, int target_size, float* rgba_out, int capacity, int* n_out);
+
+/* Camera at `eye` looking at `ref` with up vector `up` (world units, the
+ * largest volume axis spans 1), perspective fov_deg vertical, clip planes
+ * znear / zfar: the keyframe camera of the fly-through animator
+ * (LuaScripts/FlyThroughAnimator.lua: eye, ref, vup). */
+int gbvr_look_at_camera(const float eye[3], const float ref[3], const float up[3], float fov_deg, float znear,
+                        float zfar, int width, int height, float view[16], float proj[16]);
 
 /* ---- host-only UVF inspection (the UVFReader tool, UVFReader/main.cpp:23-205,
  * UVFReader/BlockInfo.h:27-401).  No GPU is used. ---- */

@@ -1,0 +1,197 @@
+"""Out-of-core datasets (bricks in page-locked host memory, a device slot pool
+with LRU residency, LOD fallback on overflow).
+
+The streaming build must store the same bricks, brick ranges and histogram as
+the in-core build of the same seeded volume; a paint that resolves level l
+must give the image the in-core renderer gives at level l, bit for bit (the
+skipped bricks are empty under the TF or outside every view frustum, where no
+ray samples); and with the eye inside the volume the image must match the FP64
+oracle within the raycaster's tolerance."""
+import numpy as np
+import pytest
+
+from imagevis3d_gb300 import (GBVR_RM_1DTRANS, GBVR_RM_ISOSURFACE, GBVR_SAMPLER_TEX, GbvrError, Renderer,
+                              orbit_camera, synth_params, workloads)
+from tests.gpu_util import assert_close
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "u16_200x180x170_b64": (synth_params((200, 180, 170), np.uint16, 21, 12, (5.0, 14.0), (0.3, 1.0), 2600.0,
+                                         noise_kind=2, noise_amp=20.0, vmax=4095.0, bg_freq=1.0, bg_level=0.1,
+                                         bg_amp=0.1), dict(brick_size=64, overlap=2)),
+    "u8_131x97x203_b32": (synth_params((131, 97, 203), np.uint8, 5, 9, (3.0, 9.0), (0.3, 1.0), 255.0,
+                                       noise_kind=1, noise_amp=4.0, vmax=255.0), dict(brick_size=32, overlap=2)),
+    "f32_90x75x140_b32_ov3": (synth_params((90, 75, 140), np.float32, 8, 6, (3.0, 8.0), (0.3, 1.0), 1.0,
+                                           noise_kind=2, noise_amp=0.01, vmax=0.0),
+                              dict(brick_size=32, overlap=3)),
+}
+BIG_POOL = 1 << 30
+
+
+def _tf(sp):
+    if sp.dtype == 1:
+        return workloads.tf1d_seeded(4096, 21, 900.0, 4095.0), (0.0, 4095.0)
+    if sp.dtype == 0:
+        return workloads.tf1d_seeded(256, 5, 40.0, 255.0), (0.0, 255.0)
+    return workloads.tf1d_seeded(256, 8, 0.15, 1.0), (0.0, 1.0)
+
+
+def _setup(r, sp, w, h):
+    tf, rng = _tf(sp)
+    r.resize((w, h))
+    r.set1DTrans(tf)
+    r.setValueRange(*rng)
+    r.setSampleRateModifier(1.0)
+
+
+def _paint(r, view, proj):
+    r.setView(view, proj)
+    r.paint()
+    return r.readFramebuffer(0, as_float=True)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_ooc_build_matches_incore(case):
+    sp, bp = CASES[case]
+    with Renderer() as a, Renderer() as b:
+        a.loadSynthetic(sp, **bp)
+        b.loadSyntheticOutOfCore(sp, BIG_POOL, **bp)
+        ia, ib = a.datasetInfo(), b.datasetInfo()
+        for k in ("dims", "lod_count", "lod_dims", "lod_bricks", "total_bricks", "range", "hist1d_size"):
+            assert ia[k] == ib[k], k
+        assert ib["host_bytes"] > 0 and ib["device_slots"] == ib["total_bricks"]
+        if sp.dtype != 2:
+            assert np.array_equal(a.getHistogram(), b.getHistogram())
+        for lod in range(ia["lod_count"]):
+            assert np.array_equal(a.brickMinMax(lod), b.brickMinMax(lod))
+            nb = ia["lod_bricks"][lod]
+            for bz in range(nb[2]):
+                for by in range(nb[1]):
+                    for bx in range(nb[0]):
+                        va, oa = a.getBrick(lod, (bx, by, bz))
+                        vb, ob = b.getBrick(lod, (bx, by, bz))
+                        assert oa == ob and np.array_equal(va, vb), (lod, bx, by, bz)
+
+
+def test_ooc_bricks_match_oracle(orc):
+    sp, bp = CASES["u8_131x97x203_b32"]
+    vol = orc.synth_blobs(sp)
+    with Renderer() as r:
+        r.loadSyntheticOutOfCore(sp, 64 * 32 ** 3, **bp)
+        info = r.datasetInfo()
+        assert info["device_slots"] == 64
+        level = vol
+        for lod in range(info["lod_count"]):
+            if lod:
+                level = orc.downsample(level)
+            nb = info["lod_bricks"][lod]
+            for b in [(0, 0, 0), (nb[0] - 1, nb[1] - 1, nb[2] - 1), (nb[0] // 2, 0, nb[2] // 2)]:
+                want, wo = orc.extract_brick(level, bp["brick_size"], bp["overlap"], b)
+                got, go = r.getBrick(lod, b)
+                assert go == wo and np.array_equal(got, want), (lod, b)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("mode", [GBVR_RM_1DTRANS, GBVR_RM_ISOSURFACE])
+def test_ooc_render_equals_incore(case, mode):
+    sp, bp = CASES[case]
+    views = [orbit_camera(az, el, 2.5 * workloads.DIAG, 45.0, 160, 120) for az, el in ((20, 15), (140, -30), (260, 50))]
+    _, rng = _tf(sp)
+    iso = rng[0] + 0.3 * (rng[1] - rng[0])
+    with Renderer(float_fb=True) as a, Renderer(float_fb=True) as b:
+        a.loadSynthetic(sp, **bp)
+        b.loadSyntheticOutOfCore(sp, BIG_POOL, **bp)
+        for r in (a, b):
+            _setup(r, sp, 160, 120)
+            r.setRenderMode(mode)
+            r.setIsoValue(iso)
+        for view, proj in views:
+            ia = _paint(a, view, proj)
+            ib = _paint(b, view, proj)
+            st = b.stats()
+            assert st["lod"] == 0
+            assert np.array_equal(ia, ib)
+        assert ia[..., 3].max() > 0.3
+        b.paintBatch(views)
+        for i, (view, proj) in enumerate(views):
+            assert np.array_equal(b.readFramebuffer(i, as_float=True), _paint(a, view, proj))
+
+
+def test_ooc_small_pool_falls_back_to_coarser_level():
+    sp, bp = CASES["u16_200x180x170_b64"]
+    slot = 64 ** 3 * 2
+    view, proj = orbit_camera(35.0, 20.0, 2.5 * workloads.DIAG, 45.0, 200, 150)
+    with Renderer(float_fb=True) as a, Renderer(float_fb=True) as b:
+        a.loadSynthetic(sp, **bp)
+        b.loadSyntheticOutOfCore(sp, 6 * slot, **bp)
+        assert b.datasetInfo()["device_slots"] == 6
+        _setup(a, sp, 200, 150)
+        _setup(b, sp, 200, 150)
+        img = _paint(b, view, proj)
+        st = b.stats()
+        assert st["lod"] > 0
+        assert st["brick_misses"] > 0 and st["bytes_paged"] > 0
+        a.setLODLimits(st["lod"], st["lod"])
+        assert np.array_equal(img, _paint(a, view, proj))
+        # the same frame again: everything resident, nothing paged
+        _paint(b, view, proj)
+        assert b.stats()["bytes_paged"] == 0
+
+
+def _inside_path(frames, w, h):
+    keys = [((-0.35, 0.05, -0.3), (0.2, 0.0, 0.1), (0, 1, 0)),
+            ((-0.1, 0.0, -0.2), (0.3, 0.0, 0.2), (0, 1, 0)),
+            ((0.15, -0.05, 0.0), (0.0, 0.0, 0.35), (0, 1, 0)),
+            ((0.1, 0.05, 0.25), (-0.3, 0.0, 0.1), (0, 1, 0))]
+    return workloads.flythrough_views(keys, frames, w, h, fov=60.0)
+
+
+def test_ooc_flythrough_pages_reuses_and_matches_incore():
+    sp, bp = CASES["u16_200x180x170_b64"]
+    slot = 64 ** 3 * 2
+    views = _inside_path(8, 128, 96)
+    with Renderer(float_fb=True) as a, Renderer(float_fb=True) as b:
+        a.loadSynthetic(sp, **bp)
+        b.loadSyntheticOutOfCore(sp, 30 * slot, **bp)
+        _setup(a, sp, 128, 96)
+        _setup(b, sp, 128, 96)
+        paged = []
+        for view, proj in views:
+            img = _paint(b, view, proj)
+            st = b.stats()
+            a.setLODLimits(st["lod"], st["lod"])
+            assert np.array_equal(img, _paint(a, view, proj))
+            paged.append(st["bytes_paged"])
+        assert paged[0] > 0
+        # consecutive frames share most of their bricks
+        assert sum(paged[1:]) < len(paged[1:]) * paged[0]
+
+
+def test_ooc_eye_inside_matches_oracle(orc):
+    sp, bp = CASES["u16_200x180x170_b64"]
+    vol = orc.synth_blobs(sp)
+    tf, rng = _tf(sp)
+    view, proj = _inside_path(3, 128, 96)[1]
+    with Renderer(float_fb=True) as r:
+        r.loadSyntheticOutOfCore(sp, BIG_POOL, **bp)
+        _setup(r, sp, 128, 96)
+        img = _paint(r, view, proj)
+        assert r.stats()["lod"] == 0
+    ref, _ = orc.render(vol, view, proj, 128, 96, tf, spv=1.0, value_range=rng)
+    assert_close(img, ref)
+    assert ref[..., 3].max() > 0.3
+
+
+def test_ooc_rejections(tmp_path):
+    sp, bp = CASES["u8_131x97x203_b32"]
+    with Renderer() as r:
+        with pytest.raises(GbvrError):
+            r.loadSyntheticOutOfCore(sp, 1000, **bp)  # smaller than one brick
+        r.loadSyntheticOutOfCore(sp, BIG_POOL, **bp)
+        with pytest.raises(GbvrError):
+            r.writeUVF(str(tmp_path / "x.uvf"))
+        with pytest.raises(GbvrError):
+            r.setSampler(GBVR_SAMPLER_TEX)
+            r.paint()
+

@@ -558,6 +558,10 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
                                long long merge, unsigned long long* __restrict__ hist, const Hist2DScratch* sc) {
   const unsigned long long smax = sc->smax;
   const double gmax = __longlong_as_double((long long)sc->gmax_bits);
+  const float smax_f = (float)smax;
+  const bool merge1 = merge == 1;
+  // values are below 2^16, so any merge above 2^16 bins like 2^16
+  const unsigned merge32 = (unsigned)(merge < 1 ? 1 : merge > 65536 ? 65536 : merge);
   unsigned long long run_bin = ~0ULL, run = 0;
   for (long long row = blockIdx.x; row < Y * Z; row += gridDim.x) {
     const long long z = row / Y, y = row - z * Y;
@@ -570,7 +574,10 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
       int k = 0;
       if (smax > 0 && S > 0) {
         const unsigned long long lhs = 65025ULL * S;
-        k = (int)(255.0 * sqrt((double)S / (double)smax));
+        // FP32 estimate (within one of the exact bin: S, Smax < 2^36), then
+        // settled by the exact integer tests; FP64 arithmetic is slow on this
+        // part and stays confined to ties
+        k = (int)(255.f * sqrtf(__fdiv_rn((float)S, smax_f)));
         if (k > 255) k = 255;
         while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
         while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;
@@ -582,7 +589,8 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
           if (k > 255) k = 255;
         }
       }
-      long long bx = (long long)__ldg(v + i) / merge;
+      const unsigned val = (unsigned)__ldg(v + i);
+      long long bx = merge1 ? val : val / merge32;
       if (bx >= nx) bx = nx - 1;
       // run-length accumulation per thread: empty space puts almost every
       // voxel in one bin, and one atomic per voxel on one address serialises

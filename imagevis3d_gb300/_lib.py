@@ -72,6 +72,11 @@ class RequestResult(C.Structure):
                 ("latency_ms", C.c_double), ("queue_ms", C.c_double), ("gpu_ms", C.c_double)]
 
 
+class Tf2dSwatch(C.Structure):
+    _fields_ = [("radial", C.c_int32), ("npoints", C.c_int32), ("nstops", C.c_int32), ("reserved", C.c_int32),
+                ("points", C.c_float * 128), ("grad", C.c_float * 4), ("stops", C.c_float * 80)]
+
+
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("batches", C.c_uint64),
                 ("mean_batch", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
@@ -154,6 +159,10 @@ SIGNATURES = {
     "gbvr_capture_single_frame": [P, CP, I],
     "gbvr_capture_view": [P, I, CP, I],
     "gbvr_load_tf1d_file": [CP, I, FP, I, C.POINTER(I)],
+    "gbvr_load_tf2d_file": [CP, C.POINTER(I), C.POINTER(I), FP, I, C.POINTER(I), C.POINTER(Tf2dSwatch), I,
+                            C.POINTER(I)],
+    "gbvr_tf2d_rasterize": [C.POINTER(Tf2dSwatch), I, FP, I, I, I, FP],
+    "gbvr_set_tf2d_file": [P, CP, F],
     "gbvr_get_stats": [P, C.POINTER(Stats)],
     "gbvr_set_stats_level": [P, I],
     "gbvr_synth_volume": [C.POINTER(SynthParams), P, SZ],

@@ -147,4 +147,49 @@ int gbvr_load_tf1d_file(const char* path, int target_size, float* rgba_out, int 
   return GBVR_OK;
 }
 
+int gbvr_load_tf2d_file(const char* path, int* width, int* height, float* tf1d, int tf1d_cap, int* tf1d_n,
+                        gbvr_tf2d_swatch* swatches, int swatch_cap, int* nswatches) {
+  if (!path) return set_error(GBVR_EINVAL, "bad argument");
+  FILE* f = fopen(path, "r");
+  if (!f) return set_error(GBVR_EIO, std::string("cannot open ") + path);
+  auto bad = [&](const char* what) {
+    fclose(f);
+    return set_error(GBVR_EFORMAT, std::string("not a 2D transfer function file (") + what + "): " + path);
+  };
+  int w = 0, h = 0;
+  long n = 0;
+  if (fscanf(f, "%d %d", &w, &h) != 2 || w <= 0 || h <= 0 || w > 16384 || h > 16384) return bad("size");
+  if (fscanf(f, "%ld", &n) != 1 || n < 0 || n > (1 << 20)) return bad("1D size");
+  for (long i = 0; i < 4 * n; ++i) {
+    float v;
+    if (fscanf(f, "%f", &v) != 1) return bad("1D entries");
+    if (tf1d && i < 4L * tf1d_cap) tf1d[i] = v;
+  }
+  int ns = 0;
+  if (fscanf(f, "%d", &ns) != 1 || ns < 0 || ns > (1 << 16)) return bad("swatch count");
+  for (int k = 0; k < ns; ++k) {
+    gbvr_tf2d_swatch sw;
+    memset(&sw, 0, sizeof(sw));
+    if (fscanf(f, "%d %d", &sw.radial, &sw.npoints) != 2 || sw.radial < 0 || sw.radial > 1 || sw.npoints < 3 ||
+        sw.npoints > GBVR_TF2D_MAX_POINTS)
+      return bad("swatch header");
+    for (int j = 0; j < 2 * sw.npoints; ++j)
+      if (fscanf(f, "%f", &sw.points[j]) != 1) return bad("vertex");
+    for (int j = 0; j < 4; ++j)
+      if (fscanf(f, "%f", &sw.grad[j]) != 1) return bad("gradient");
+    if (fscanf(f, "%d", &sw.nstops) != 1 || sw.nstops < 1 || sw.nstops > GBVR_TF2D_MAX_STOPS) return bad("stop count");
+    for (int j = 0; j < 5 * sw.nstops; ++j)
+      if (fscanf(f, "%f", &sw.stops[j]) != 1) return bad("stop");
+    for (int j = 1; j < sw.nstops; ++j)
+      if (!(sw.stops[5 * j] >= sw.stops[5 * (j - 1)])) return bad("stop order");
+    if (swatches && k < swatch_cap) swatches[k] = sw;
+  }
+  fclose(f);
+  if (width) *width = w;
+  if (height) *height = h;
+  if (tf1d_n) *tf1d_n = (int)n;
+  if (nswatches) *nswatches = ns;
+  return GBVR_OK;
+}
+
 }  // extern "C"

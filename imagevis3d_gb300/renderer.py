@@ -95,6 +95,28 @@ def look_at_camera(eye, ref, up, fov_deg, width, height, znear=0.01, zfar=20.0):
     return v.reshape(4, 4), pr.reshape(4, 4)
 
 
+def load_tf2d_file(path):
+    """Parse a .2dt file: (width, height, 1D TF [n, 4], swatches as a ctypes
+    array, swatch count)."""
+    w, h, n1, ns = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    L.call("gbvr_load_tf2d_file", path.encode(), C.byref(w), C.byref(h), None, 0, C.byref(n1), None, 0, C.byref(ns))
+    tf = np.zeros((max(n1.value, 1), 4), np.float32)
+    sw = (L.Tf2dSwatch * max(ns.value, 1))()
+    L.call("gbvr_load_tf2d_file", path.encode(), C.byref(w), C.byref(h), tf.ctypes.data_as(L.FP), n1.value,
+           C.byref(n1), sw, ns.value, C.byref(ns))
+    return w.value, h.value, tf[:n1.value], sw, ns.value
+
+
+def tf2d_rasterize(swatches, nswatches, tf1d, width, height):
+    """GPU rasterisation of swatches over a 1D TF: [height, width, 4] float32,
+    row = gradient bin."""
+    out = np.empty((height, width, 4), np.float32)
+    tf = np.ascontiguousarray(tf1d if tf1d is not None else np.zeros((0, 4)), np.float32)
+    L.call("gbvr_tf2d_rasterize", swatches, nswatches, tf.ctypes.data_as(L.FP), len(tf), width, height,
+           out.ctypes.data_as(L.FP))
+    return out
+
+
 def synth_volume(params):
     """Generate a seeded volume on the GPU and return it as a (z, y, x) array."""
     dims = [params.dims[i] for i in range(3)]
@@ -210,6 +232,10 @@ class Renderer:
     def set2DTrans(self, tf, max_grad=0.0):
         tf, p = _fp(tf)
         L.call("gbvr_set_tf2d", self._h, p, tf.shape[1], tf.shape[0], max_grad)
+
+    def set2DTransFile(self, path, max_grad=0.0):
+        """changed2DTrans from a .2dt file (rasterised on the GPU)."""
+        L.call("gbvr_set_tf2d_file", self._h, path.encode(), max_grad)
 
     def setValueRange(self, lo, hi):
         L.call("gbvr_set_value_range", self._h, lo, hi)

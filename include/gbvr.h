@@ -412,6 +412,51 @@ int gbvr_orbit_camera(float azimuth_deg, float elevation_deg, float radius, floa
  * Writes at most `capacity` entries and the count to *n_out. */
 int gbvr_load_tf1d_file(const char* path, int target_size, float* rgba_out, int capacity, int* n_out);
 
+/* .2dt (DemoData/c60.2dt; TransferFunction2D::Load / Save, reached through
+ * Q2DTransferFunction::LoadFromFile, Q2DTransferFunction.cpp:1234-1261):
+ * "W H", the embedded 1D TF (N, then N lines "r g b a"), the swatch count,
+ * then per swatch: the radial flag, the vertex count, one "x y" line per
+ * vertex, the gradient end points "x0 y0 x1 y1", the stop count and one
+ * "pos r g b a" line per stop.  Coordinates are normalised to the editor
+ * canvas: x = value, y from the top (maximum gradient magnitude) down to 1
+ * (gradient magnitude 0). */
+#define GBVR_TF2D_MAX_POINTS 64
+#define GBVR_TF2D_MAX_STOPS 16
+typedef struct gbvr_tf2d_swatch {
+  int32_t radial;  /* 0: linear gradient from grad[0..1] to grad[2..3]; 1: radial around grad[0..1] */
+  int32_t npoints; /* polygon vertices, 3 .. GBVR_TF2D_MAX_POINTS */
+  int32_t nstops;  /* gradient stops, 1 .. GBVR_TF2D_MAX_STOPS, increasing positions */
+  int32_t reserved;
+  float points[2 * GBVR_TF2D_MAX_POINTS]; /* x0 y0 x1 y1 ... */
+  float grad[4];
+  float stops[5 * GBVR_TF2D_MAX_STOPS]; /* pos r g b a ... */
+} gbvr_tf2d_swatch;
+
+/* Parse a .2dt file (host only).  Writes the canvas size, up to tf1d_cap
+ * entries of the embedded 1D TF (count to *tf1d_n) and up to swatch_cap
+ * swatches (count to *nswatches).  Output pointers may be NULL (with cap 0)
+ * to query the counts. */
+int gbvr_load_tf2d_file(const char* path, int* width, int* height, float* tf1d, int tf1d_cap, int* tf1d_n,
+                        gbvr_tf2d_swatch* swatches, int swatch_cap, int* nswatches);
+
+/* Rasterise swatches into a width x height RGBA float table on the GPU (the
+ * step Tuvok's TransferFunction2D performs before changed2DTrans; the editor
+ * draws it the same way, Q2DTransferFunction.cpp:436-473,1138-1153,
+ * 1182-1217): every entry starts as the 1D TF entry of its column
+ * (floor(x * tf1d_n / width)), then each swatch in order is composited over
+ * it ("source over", non-premultiplied RGBA) where the entry's centre lies
+ * inside the polygon (even-odd rule), with the colour of the gradient at the
+ * centre (position clamped to [0, 1], linear between stops).  Row r of the
+ * table is gradient bin r, i.e. canvas y = 1 - (r + 0.5) / height.  With no
+ * 1D TF (tf1d_n = 0) the table starts transparent black.  out_rgba: host,
+ * width * height * 4 floats. */
+int gbvr_tf2d_rasterize(const gbvr_tf2d_swatch* swatches, int nswatches, const float* tf1d, int tf1d_n, int width,
+                        int height, float* out_rgba);
+
+/* changed2DTrans from a file: parse, rasterise on the GPU at the file's canvas
+ * size and set the result as the renderer's 2D TF (gbvr_set_tf2d). */
+int gbvr_set_tf2d_file(gbvr_renderer* r, const char* path, float max_grad);
+
 /* Camera at `eye` looking at `ref` with up vector `up` (world units, the
  * largest volume axis spans 1), perspective fov_deg vertical, clip planes
  * znear / zfar: the keyframe camera of the fly-through animator

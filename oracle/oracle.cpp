@@ -734,4 +734,94 @@ int orc_max_threads(void) {
 #endif
 }
 
+// ---------------------------------------------------------------------------
+// 2D transfer-function rasterisation from .2dt swatches, restated from the
+// editor's drawing (ImageVis3D/UI/Q2DTransferFunction.cpp:436-473 swatch
+// fill with QLinearGradient / QRadialGradient, 1138-1153 the 1D TF image
+// stretched underneath, 1182-1217 drawing order, 156-160 gradient 0 at the
+// bottom).  Tuvok's own table renderer is not in the tree: parity of this
+// rule with the reference is unpinned; the GPU rasteriser must equal it bit
+// for bit (float arithmetic, the same operation order, no contraction).
+// Swatch layout: radial, npoints, nstops, reserved (int32), points[128],
+// grad[4], stops[80] (float), as gbvr_tf2d_swatch.
+// ---------------------------------------------------------------------------
+struct orc_swatch {
+  int32_t radial, npoints, nstops, reserved;
+  float points[128];
+  float grad[4];
+  float stops[80];
+};
+
+static bool sw_covers(const orc_swatch& s, float cx, float cy, float fw, float fh) {
+  bool in = false;
+  for (int i = 0, j = s.npoints - 1; i < s.npoints; j = i++) {
+    const float xi = s.points[2 * i] * fw, yi = s.points[2 * i + 1] * fh;
+    const float xj = s.points[2 * j] * fw, yj = s.points[2 * j + 1] * fh;
+    if ((yi > cy) != (yj > cy)) {
+      const float xc = xi + ((cy - yi) * (xj - xi)) / (yj - yi);
+      if (cx < xc) in = !in;
+    }
+  }
+  return in;
+}
+
+static float sw_pos(const orc_swatch& s, float cx, float cy, float fw, float fh) {
+  const float g0x = s.grad[0] * fw, g0y = s.grad[1] * fh, g1x = s.grad[2] * fw, g1y = s.grad[3] * fh;
+  const float qx = cx - g0x, qy = cy - g0y, dx = g1x - g0x, dy = g1y - g0y;
+  const float dd = dx * dx + dy * dy;
+  float t;
+  if (s.radial) {
+    const float r = std::sqrt(dd);
+    const float d = std::sqrt(qx * qx + qy * qy);
+    t = r > 0.f ? d / r : 1.f;
+  } else {
+    t = dd > 0.f ? (qx * dx + qy * dy) / dd : 0.f;
+  }
+  return std::min(std::max(t, 0.f), 1.f);
+}
+
+static void sw_colour(const orc_swatch& s, float t, float c[4]) {
+  const int n = s.nstops;
+  const float* st = s.stops;
+  if (!(t > st[0]) || n == 1) {
+    for (int k = 0; k < 4; ++k) c[k] = st[1 + k];
+    return;
+  }
+  if (t >= st[5 * (n - 1)]) {
+    for (int k = 0; k < 4; ++k) c[k] = st[5 * (n - 1) + 1 + k];
+    return;
+  }
+  int i = 0;
+  while (i + 2 < n && st[5 * (i + 1)] <= t) ++i;
+  const float w = (t - st[5 * i]) / (st[5 * (i + 1)] - st[5 * i]);
+  for (int k = 0; k < 4; ++k) {
+    const float a = st[5 * i + 1 + k], b = st[5 * (i + 1) + 1 + k];
+    c[k] = a + w * (b - a);
+  }
+}
+
+void orc_raster_tf2d(const orc_swatch* sw, int ns, const float* tf1d, int n1d, int W, int H, float* out) {
+  const float fw = (float)W, fh = (float)H;
+  for (int r = 0; r < H; ++r)
+    for (int x = 0; x < W; ++x) {
+      float d[4] = {0.f, 0.f, 0.f, 0.f};
+      if (n1d > 0) {
+        const i64 j = (i64)x * n1d / W;
+        for (int k = 0; k < 4; ++k) d[k] = tf1d[4 * j + k];
+      }
+      const float cx = (float)x + 0.5f, cy = (float)(H - 1 - r) + 0.5f;
+      for (int k = 0; k < ns; ++k) {
+        if (!sw_covers(sw[k], cx, cy, fw, fh)) continue;
+        float c[4];
+        sw_colour(sw[k], sw_pos(sw[k], cx, cy, fw, fh), c);
+        const float as = c[3];
+        const float kd = d[3] * (1.f - as);
+        const float a = as + kd;
+        for (int j = 0; j < 3; ++j) d[j] = a > 0.f ? (c[j] * as + d[j] * kd) / a : 0.f;
+        d[3] = a;
+      }
+      for (int k = 0; k < 4; ++k) out[4 * ((i64)r * W + x) + k] = d[k];
+    }
+}
+
 }  // extern "C"

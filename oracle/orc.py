@@ -205,3 +205,37 @@ def synth_fbm(params):
                         params.base_period, C.c_float(params.threshold), C.c_float(params.vmax),
                         out.ctypes.data_as(C.c_void_p))
     return out
+
+
+class Swatch(C.Structure):
+    _fields_ = [("radial", C.c_int32), ("npoints", C.c_int32), ("nstops", C.c_int32), ("reserved", C.c_int32),
+                ("points", C.c_float * 128), ("grad", C.c_float * 4), ("stops", C.c_float * 80)]
+
+
+def make_swatches(swatches):
+    """swatches: list of dicts (radial, points [(x, y)], grad (x0, y0, x1, y1),
+    stops [(pos, r, g, b, a)])."""
+    arr = (Swatch * max(len(swatches), 1))()
+    for k, s in enumerate(swatches):
+        arr[k].radial = int(s["radial"])
+        arr[k].npoints = len(s["points"])
+        arr[k].nstops = len(s["stops"])
+        for j, (x, y) in enumerate(s["points"]):
+            arr[k].points[2 * j], arr[k].points[2 * j + 1] = x, y
+        for j in range(4):
+            arr[k].grad[j] = s["grad"][j]
+        for j, st in enumerate(s["stops"]):
+            for c in range(5):
+                arr[k].stops[5 * j + c] = st[c]
+    return arr
+
+
+def raster_tf2d(swatches, tf1d, width, height):
+    """CPU restatement of the swatch rasteriser: [height, width, 4] float32,
+    row = gradient bin."""
+    arr = make_swatches(swatches)
+    tf = np.ascontiguousarray(tf1d if tf1d is not None else np.zeros((0, 4)), np.float32)
+    out = np.empty((height, width, 4), np.float32)
+    lib().orc_raster_tf2d(arr, len(swatches), tf.ctypes.data_as(C.POINTER(C.c_float)), len(tf), width, height,
+                          out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out

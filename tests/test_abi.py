@@ -36,7 +36,10 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
         pytest.skip("gcc not available")
     structs = {"gbvr_brick_params": L.BrickParams, "gbvr_dataset_info": L.DatasetInfo,
                "gbvr_view": L.View, "gbvr_stats": L.Stats, "gbvr_synth_params": L.SynthParams,
-               "gbvr_uvf_summary": L.UvfSummary}
+               "gbvr_uvf_summary": L.UvfSummary, "gbvr_fbm_params": L.FbmParams,
+               "gbvr_tune_result": L.TuneResult, "gbvr_server_params": L.ServerParams,
+               "gbvr_request": L.Request, "gbvr_request_result": L.RequestResult,
+               "gbvr_server_stats": L.ServerStats, "gbvr_tf2d_swatch": L.Tf2dSwatch}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbvr.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append('printf("%%zu\\n", sizeof(%s));' % cname)

@@ -811,6 +811,7 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
     maxd = std::max(maxd, L.dims[a]);
   }
   f.interior = L.interior;
+  f.inv_interior = 1.f / (float)L.interior;
   f.tf = p.tf;
   f.tf_w = p.tf_w;
   f.tf_h = p.tf_h;

@@ -55,6 +55,7 @@ struct __align__(16) FrameDesc {
   int dims[3];               // rendered level
   int nb[3];
   int interior;
+  float inv_interior;        // 1 / interior (estimate of the brick column, settled exactly)
   float vox_scale[3];        // world -> voxel-centre coordinates: (p + extent/2) * scale - 0.5
   float half_extent[3];
   // classification

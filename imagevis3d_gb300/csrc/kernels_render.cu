@@ -174,10 +174,18 @@ __device__ __forceinline__ float sample_cell(const FrameDesc& f, const BrickView
   return fmaf(fz, c1 - c0, c0);
 }
 
+// floor(g / interior) for 0 <= g < 2^24: a float estimate (off by at most
+// one) settled with exact integer tests, cheaper than an integer division.
+__device__ __forceinline__ int brick_col(const FrameDesc& f, int g, int nb) {
+  if (g < 0) return 0;
+  int q = (int)((float)g * f.inv_interior);
+  if (q * f.interior > g) --q;
+  else if ((q + 1) * f.interior <= g) ++q;
+  return min(q, nb - 1);
+}
+
 __device__ __forceinline__ int brick_index(const FrameDesc& f, int gx, int gy, int gz) {
-  int bx = gx < 0 ? 0 : min(gx / f.interior, f.nb[0] - 1);
-  int by = gy < 0 ? 0 : min(gy / f.interior, f.nb[1] - 1);
-  int bz = gz < 0 ? 0 : min(gz / f.interior, f.nb[2] - 1);
+  const int bx = brick_col(f, gx, f.nb[0]), by = brick_col(f, gy, f.nb[1]), bz = brick_col(f, gz, f.nb[2]);
   return (bz * f.nb[1] + by) * f.nb[0] + bx;
 }
 
@@ -344,13 +352,13 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
     // form one run and only its ends need checking.
     auto run_end = [&](int k0, int lx, int ly, int lz, int hx, int hy, int hz) -> int {
       float te = INFINITY;
-      te = fminf(te, r.dv[0] > 0.f ? ((float)hx - r.ov[0]) / r.dv[0]
-                                   : (r.dv[0] < 0.f ? ((float)lx - r.ov[0]) / r.dv[0] : INFINITY));
-      te = fminf(te, r.dv[1] > 0.f ? ((float)hy - r.ov[1]) / r.dv[1]
-                                   : (r.dv[1] < 0.f ? ((float)ly - r.ov[1]) / r.dv[1] : INFINITY));
-      te = fminf(te, r.dv[2] > 0.f ? ((float)hz - r.ov[2]) / r.dv[2]
-                                   : (r.dv[2] < 0.f ? ((float)lz - r.ov[2]) / r.dv[2] : INFINITY));
-      const float kef = ceilf((te - t0) / dt - 0.5f);
+      te = fminf(te, r.dv[0] > 0.f ? ((float)hx - r.ov[0]) * r.inv[0]
+                                   : (r.dv[0] < 0.f ? ((float)lx - r.ov[0]) * r.inv[0] : INFINITY));
+      te = fminf(te, r.dv[1] > 0.f ? ((float)hy - r.ov[1]) * r.inv[1]
+                                   : (r.dv[1] < 0.f ? ((float)ly - r.ov[1]) * r.inv[1] : INFINITY));
+      te = fminf(te, r.dv[2] > 0.f ? ((float)hz - r.ov[2]) * r.inv[2]
+                                   : (r.dv[2] < 0.f ? ((float)lz - r.ov[2]) * r.inv[2] : INFINITY));
+      const float kef = ceilf((te - t0) * inv_dt - 0.5f);
       int ke = kef >= (float)K ? K : max(k0 + 1, (int)kef);
       auto in_box = [&](int kk) {
         float qx, qy, qz;

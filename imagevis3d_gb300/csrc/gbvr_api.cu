@@ -786,6 +786,8 @@ struct FrameParams {
   float grad_max;
   const unsigned char* skip;  // per brick of the dataset (all levels)
   const unsigned char* occ;   // per macro-cell of `level`
+  int clip_on;
+  float clip[4];
 };
 
 void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
@@ -853,6 +855,11 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
   f.occ = p.occ;
   for (int a = 0; a < 3; ++a) f.nc[a] = L.nc[a];
   f.cell_shift = L.cell_shift;
+  f.cells = L.cells ? L.cells->as<float2>() : nullptr;
+  f.level_max = -INFINITY;
+  for (int i = 0; i < L.nbricks; ++i) f.level_max = std::max(f.level_max, ds.bricks[L.brick_base + i].vmax);
+  f.clip_on = p.clip_on;
+  for (int k = 0; k < 4; ++k) f.clip[k] = p.clip[k];
   f.tiles_x = (p.width + p.tile_w - 1) / p.tile_w;
   f.tiles_y = (p.height + 32 / p.tile_w - 1) / (32 / p.tile_w);
   // layout copy: the axis whose voxel-space extent along screen x is largest
@@ -884,6 +891,8 @@ struct gbvr_renderer {
   uint32_t flags = 0;
   int width = 640, height = 480;  // BatchRenderer.lua:31-33 default context size
   int mode = GBVR_RM_1DTRANS, interp = GBVR_LINEAR, sampler = GBVR_SAMPLER_SW;
+  int clip_on = 0;
+  float clip[4] = {0.f, 0.f, 1.f, 0.f};
   std::vector<float> tf1d;
   std::vector<float> tf2d;
   int tf2d_w = 0, tf2d_h = 0;
@@ -1060,6 +1069,8 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
   p.grad_max = r->tf2d_grad_max;
   p.skip = r->d_skip.as<unsigned char>();
   p.occ = r->d_occ.as<unsigned char>();
+  p.clip_on = r->clip_on;
+  for (int k = 0; k < 4; ++k) p.clip[k] = r->clip[k];
   if (r->ds.ooc) {
     // residency lives in the skip table: brick skipping is always on
     p.skip = r->d_ooc_skip.as<unsigned char>();
@@ -1113,6 +1124,7 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level) {
   const float idx_scale = (float)((w - 1) / (vhi - vlo)), lo_f = (float)vlo;
   auto nonempty = [&](const BrickInfo& b) {
     if (r->mode == GBVR_RM_ISOSURFACE) return b.vmax >= r->iso;
+    if (r->mode == GBVR_RM_MIP) return true;
     float ilo = std::min(std::max((b.vmin - lo_f) * idx_scale, 0.f), (float)(w - 1));
     float ihi = std::min(std::max((b.vmax - lo_f) * idx_scale, 0.f), (float)(w - 1));
     int a0 = std::max((int)std::floor(ilo) - 1, 0), a1 = std::min((int)std::floor(ihi) + 2, w - 1);
@@ -1708,9 +1720,22 @@ int gbvr_resize(gbvr_renderer* r, int width, int height) {
 
 int gbvr_set_render_mode(gbvr_renderer* r, int mode) {
   TRY(check_r(r));
-  if (mode < 0 || mode > 2) return fail(GBVR_EINVAL, "bad render mode");
+  if (mode < 0 || mode > 3) return fail(GBVR_EINVAL, "bad render mode");
   if (mode != r->mode) { r->tf_dirty = true; r->skip_dirty = true; }
   r->mode = mode;
+  return GBVR_OK;
+}
+
+int gbvr_set_clip_plane(gbvr_renderer* r, int enabled, const float plane[4]) {
+  TRY(check_r(r));
+  if (enabled) {
+    if (!plane) return fail(GBVR_EINVAL, "null plane");
+    for (int k = 0; k < 4; ++k)
+      if (!std::isfinite(plane[k])) return fail(GBVR_EINVAL, "plane coefficients must be finite");
+    for (int k = 0; k < 4; ++k) r->clip[k] = plane[k];
+  }
+  r->clip_on = enabled ? 1 : 0;
+  r->drop_graphs();
   return GBVR_OK;
 }
 
@@ -2494,7 +2519,7 @@ int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba,
                        float iso, const float iso_rgb[3], double lo, double hi, int* tf_id) {
   TRY(check_s(s));
   if (dataset < 0 || dataset >= (int)s->datasets.size()) return fail(GBVR_EINVAL, "bad dataset id");
-  if (mode < 0 || mode > 2) return fail(GBVR_EINVAL, "bad render mode");
+  if (mode < 0 || mode > 3) return fail(GBVR_EINVAL, "bad render mode");
   if (mode == GBVR_RM_1DTRANS) h = 1;
   if (mode == GBVR_RM_ISOSURFACE) {
     static const float dummy[8] = {0, 0, 0, 0, 0, 0, 0, 0};

@@ -16,7 +16,7 @@
 namespace gbvr {
 
 enum DType { DT_U8 = 0, DT_U16 = 1, DT_F32 = 2 };
-enum Mode { MODE_1D = 0, MODE_2D = 1, MODE_ISO = 2 };
+enum Mode { MODE_1D = 0, MODE_2D = 1, MODE_ISO = 2, MODE_MIP = 3 };
 enum Sampler { SAMPLER_SW = 0, SAMPLER_TEX = 1 };
 
 inline size_t dtype_size(int dt) { return dt == DT_U8 ? 1 : dt == DT_U16 ? 2 : 4; }
@@ -85,6 +85,10 @@ struct __align__(16) FrameDesc {
   const unsigned char* occ; // per macro-cell: capped distance (cells) to one that may contribute
   int nc[3];                 // macro-cell grid of the level
   int cell_shift;            // macro-cell edge = 1 << cell_shift voxels
+  const float2* cells;       // MIP: per macro-cell min/max of the level (footprint + 1 voxel)
+  float level_max;           // MIP: largest voxel of the level; no sample exceeds it
+  int clip_on;               // clip plane: samples with clip . (x, y, z, 1) > 0 are dropped
+  float clip[4];
   int tile_w;                // ray tile of one warp: tile_w x (32 / tile_w) pixels
   int perm;                  // brick layout copy: 0 x-fastest, 1 y-fastest, 2 z-fastest, 3 4^3 blocks
   unsigned long long copy_off;  // element offset of that copy in the pool

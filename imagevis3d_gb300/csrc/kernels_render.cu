@@ -333,10 +333,11 @@ __device__ __forceinline__ bool composite(const FrameDesc& f, float4 c, Accum& a
 template <typename T, int MODE, int SAMPLER>
 __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) {
   Accum acc = {0.f, 0.f, 0.f, 0.f};
+  float runmax = -INFINITY;  // MIP: largest sample so far
   if (r.hit) {
     const float dt = f.dt;
     const float t0 = r.t0;
-    const int K = max(0, (int)ceilf((r.t1 - t0) / dt - 0.5f));
+    int K = max(0, (int)ceilf((r.t1 - t0) / dt - 0.5f));
     const float V[3] = {-r.dw[0], -r.dw[1], -r.dw[2]};
     const float inv_dt = 1.f / dt;
     auto pos_of = [&](int kk, float& px, float& py, float& pz) {
@@ -371,6 +372,35 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
       return ke;
     };
     int k = 0;
+    if (f.clip_on) {
+      // Clip plane: keep the samples with n . p + d <= 0.  Along the ray
+      // n . p + d = s0 + s1 t is monotone, so the kept samples are a prefix
+      // or a suffix of [0, K): estimated from the crossing, then settled with
+      // the per-sample test itself.  Sample positions do not move.
+      float s0 = f.clip[3], s1 = 0.f;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const float o = (r.ov[i] + 0.5f) / f.vox_scale[i] - f.half_extent[i];
+        s0 = fmaf(f.clip[i], o, s0);
+        s1 = fmaf(f.clip[i], r.dw[i], s1);
+      }
+      auto keep = [&](int kk) { return fmaf(s1, fmaf((float)kk + 0.5f, dt, t0), s0) <= 0.f; };
+      if (s1 > 0.f) {
+        const float kf = floorf((-s0 / s1 - t0) * inv_dt - 0.5f);
+        int e = kf < 0.f ? 0 : (kf >= (float)K ? K : (int)kf + 1);
+        while (e > 0 && !keep(e - 1)) --e;
+        while (e < K && keep(e)) ++e;
+        K = e;
+      } else if (s1 < 0.f) {
+        const float kf = ceilf((-s0 / s1 - t0) * inv_dt - 0.5f);
+        int e = kf <= 0.f ? 0 : (kf >= (float)K ? K : (int)kf);
+        while (e < K && !keep(e)) ++e;
+        while (e > 0 && keep(e - 1)) --e;
+        k = e;
+      } else if (!(s0 <= 0.f)) {
+        K = 0;
+      }
+    }
     bool done = false;
     BrickView b;
     int bi = -1, bke = 0;  // current brick and the end of the ray's run in it
@@ -383,7 +413,10 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
         bi = brick_index(f, gx, gy, gz);
         load_brick(f, bi, b);
         bke = run_end(k, b.lox, b.loy, b.loz, b.hix, b.hiy, b.hiz);
-        if (f.empty_skip >= 1 && __ldg(f.skip + bi)) {
+        bool skip_b = f.empty_skip >= 1 && __ldg(f.skip + bi);
+        // MIP: a brick whose largest voxel cannot raise the maximum is skipped
+        if constexpr (MODE == MODE_MIP) skip_b = skip_b || (f.empty_skip >= 1 && __ldg(&f.bricks[bi].vmax) <= runmax);
+        if (skip_b) {
           k = bke;
           bi = -1;
           continue;
@@ -403,7 +436,9 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
         // harmless.
         const int cx = max(gx, 0) >> sh, cy = max(gy, 0) >> sh, cz = max(gz, 0) >> sh;
         const size_t ci = ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx;
-        const int d = __ldg(f.occ + ci);
+        int d;
+        if constexpr (MODE == MODE_MIP) d = __ldg(&f.cells[ci].y) <= runmax ? 1 : 0;  // one cell at a time
+        else d = __ldg(f.occ + ci);
         const int lo_c = d > 0 ? d - 1 : 0;  // cube = cells [c - lo_c, c + lo_c]
         const float lx = (float)(max(cx - lo_c, 0) << sh), hx = (float)min((cx + lo_c + 1) << sh, f.dims[0]);
         const float ly = (float)(max(cy - lo_c, 0) << sh), hy = (float)min((cy + lo_c + 1) << sh, f.dims[1]);
@@ -425,7 +460,16 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
           if (!(*(volatile unsigned*)w & bit)) atomicOr(w, bit);
         }
       }
-      if constexpr (MODE == MODE_1D) {
+      if constexpr (MODE == MODE_MIP) {
+        for (; k < ke; ++k) {
+          float ax, ay, az;
+          pos_of(k, ax, ay, az);
+          const Cell ca = make_cell(f, ax, ay, az);
+          ++nsamp;
+          runmax = fmaxf(runmax, sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz));
+        }
+        if (runmax >= f.level_max) done = true;
+      } else if constexpr (MODE == MODE_1D) {
         for (; k < ke; ++k) {
           float ax, ay, az;
           pos_of(k, ax, ay, az);
@@ -498,6 +542,16 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
       }
     }
   }
+  if constexpr (MODE == MODE_MIP) {
+    // the maximum through the 1D TF, composited once (no opacity correction)
+    if (runmax > -INFINITY) {
+      const float4 c = tf1d(f, runmax);
+      acc.C0 = c.x * c.w;
+      acc.C1 = c.y * c.w;
+      acc.C2 = c.z * c.w;
+      acc.A = c.w;
+    }
+  }
   const float rem = 1.f - acc.A;
   return make_float4(fmaf(rem, f.bg[0], acc.C0), fmaf(rem, f.bg[1], acc.C1), fmaf(rem, f.bg[2], acc.C2), acc.A);
 }
@@ -568,11 +622,12 @@ __global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const F
 // weights are convex), so the TF entries such a sample can read are bounded;
 // if every one has alpha 0 the region contributes exactly nothing and the
 // walk skips it.  Isosurface: skipped when vmax < iso (no sample can reach
-// the isovalue).  One prefix count over the TF columns makes each test O(1).
+// the isovalue).  MIP skips by the running maximum in the walk instead.  One prefix count over the TF columns makes each test O(1).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned char classify_range(float mn, float mx, const int* __restrict__ prefix, int tf_w,
                                                         int mode, float value_lo, float idx_scale, float iso) {
   if (mode == MODE_ISO) return mx >= iso ? 1 : 0;
+  if (mode == MODE_MIP) return 1;  // the maximum goes through the TF: nothing is empty up front
   float ilo = fminf(fmaxf((mn - value_lo) * idx_scale, 0.f), (float)(tf_w - 1));
   float ihi = fminf(fmaxf((mx - value_lo) * idx_scale, 0.f), (float)(tf_w - 1));
   int lo = max((int)floorf(ilo) - 1, 0);
@@ -713,28 +768,34 @@ static cudaError_t persistent_t(const FrameDesc* frames, int nframes, const int*
 }
 
 #define GBVR_DISPATCH(FN, dtype, mode, sampler, ...)                                          \
-  do {                                                                                          \
-    switch ((dtype) * 6 + (mode) * 2 + (sampler)) {                                             \
-      case 0: return FN<uint8_t, MODE_1D, SAMPLER_SW>(__VA_ARGS__);                             \
-      case 1: return FN<uint8_t, MODE_1D, SAMPLER_TEX>(__VA_ARGS__);                            \
-      case 2: return FN<uint8_t, MODE_2D, SAMPLER_SW>(__VA_ARGS__);                             \
-      case 3: return FN<uint8_t, MODE_2D, SAMPLER_TEX>(__VA_ARGS__);                            \
-      case 4: return FN<uint8_t, MODE_ISO, SAMPLER_SW>(__VA_ARGS__);                            \
-      case 5: return FN<uint8_t, MODE_ISO, SAMPLER_TEX>(__VA_ARGS__);                           \
-      case 6: return FN<uint16_t, MODE_1D, SAMPLER_SW>(__VA_ARGS__);                            \
-      case 7: return FN<uint16_t, MODE_1D, SAMPLER_TEX>(__VA_ARGS__);                           \
-      case 8: return FN<uint16_t, MODE_2D, SAMPLER_SW>(__VA_ARGS__);                            \
-      case 9: return FN<uint16_t, MODE_2D, SAMPLER_TEX>(__VA_ARGS__);                           \
-      case 10: return FN<uint16_t, MODE_ISO, SAMPLER_SW>(__VA_ARGS__);                          \
-      case 11: return FN<uint16_t, MODE_ISO, SAMPLER_TEX>(__VA_ARGS__);                         \
-      case 12: return FN<float, MODE_1D, SAMPLER_SW>(__VA_ARGS__);                              \
-      case 13: return FN<float, MODE_1D, SAMPLER_TEX>(__VA_ARGS__);                             \
-      case 14: return FN<float, MODE_2D, SAMPLER_SW>(__VA_ARGS__);                              \
-      case 15: return FN<float, MODE_2D, SAMPLER_TEX>(__VA_ARGS__);                             \
-      case 16: return FN<float, MODE_ISO, SAMPLER_SW>(__VA_ARGS__);                             \
-      case 17: return FN<float, MODE_ISO, SAMPLER_TEX>(__VA_ARGS__);                            \
-      default: return cudaErrorInvalidValue;                                                    \
-    }                                                                                           \
+  do {                                                                                        \
+    switch ((dtype) * 8 + (mode) * 2 + (sampler)) {                                           \
+      case 0: return FN<uint8_t, MODE_1D, SAMPLER_SW>(__VA_ARGS__);                           \
+      case 1: return FN<uint8_t, MODE_1D, SAMPLER_TEX>(__VA_ARGS__);                          \
+      case 2: return FN<uint8_t, MODE_2D, SAMPLER_SW>(__VA_ARGS__);                           \
+      case 3: return FN<uint8_t, MODE_2D, SAMPLER_TEX>(__VA_ARGS__);                          \
+      case 4: return FN<uint8_t, MODE_ISO, SAMPLER_SW>(__VA_ARGS__);                          \
+      case 5: return FN<uint8_t, MODE_ISO, SAMPLER_TEX>(__VA_ARGS__);                         \
+      case 6: return FN<uint8_t, MODE_MIP, SAMPLER_SW>(__VA_ARGS__);                          \
+      case 7: return FN<uint8_t, MODE_MIP, SAMPLER_TEX>(__VA_ARGS__);                         \
+      case 8: return FN<uint16_t, MODE_1D, SAMPLER_SW>(__VA_ARGS__);                          \
+      case 9: return FN<uint16_t, MODE_1D, SAMPLER_TEX>(__VA_ARGS__);                         \
+      case 10: return FN<uint16_t, MODE_2D, SAMPLER_SW>(__VA_ARGS__);                         \
+      case 11: return FN<uint16_t, MODE_2D, SAMPLER_TEX>(__VA_ARGS__);                        \
+      case 12: return FN<uint16_t, MODE_ISO, SAMPLER_SW>(__VA_ARGS__);                        \
+      case 13: return FN<uint16_t, MODE_ISO, SAMPLER_TEX>(__VA_ARGS__);                       \
+      case 14: return FN<uint16_t, MODE_MIP, SAMPLER_SW>(__VA_ARGS__);                        \
+      case 15: return FN<uint16_t, MODE_MIP, SAMPLER_TEX>(__VA_ARGS__);                       \
+      case 16: return FN<float, MODE_1D, SAMPLER_SW>(__VA_ARGS__);                            \
+      case 17: return FN<float, MODE_1D, SAMPLER_TEX>(__VA_ARGS__);                           \
+      case 18: return FN<float, MODE_2D, SAMPLER_SW>(__VA_ARGS__);                            \
+      case 19: return FN<float, MODE_2D, SAMPLER_TEX>(__VA_ARGS__);                           \
+      case 20: return FN<float, MODE_ISO, SAMPLER_SW>(__VA_ARGS__);                           \
+      case 21: return FN<float, MODE_ISO, SAMPLER_TEX>(__VA_ARGS__);                          \
+      case 22: return FN<float, MODE_MIP, SAMPLER_SW>(__VA_ARGS__);                           \
+      case 23: return FN<float, MODE_MIP, SAMPLER_TEX>(__VA_ARGS__);                          \
+      default: return cudaErrorInvalidValue;                                                  \
+    }                                                                                         \
   } while (0)
 
 cudaError_t launch_render_plain(const FrameDesc& f, cudaStream_t s) {

@@ -61,6 +61,12 @@ extern "C" {
 #define GBVR_RM_1DTRANS 0
 #define GBVR_RM_2DTRANS 1
 #define GBVR_RM_ISOSURFACE 2
+/* Maximum-intensity projection: the largest sample along the ray through the
+ * 1D TF, composited once over the background.  Tuvok has no such render
+ * mode: MIP is a property of its 2D render regions (setUseMIP,
+ * RenderWindow.cpp:286-289; CaptureMIPFrame, :1690-1713); here it takes any
+ * camera, e.g. an orthographic one along a slice axis. */
+#define GBVR_RM_MIP 3
 
 /* Interpolants (RenderWindow.cpp:437-446, ImageVis3D.cpp:881-888). */
 #define GBVR_NEAREST 0
@@ -178,6 +184,10 @@ int gbvr_resize(gbvr_renderer* r, int width, int height);                 /* res
 int gbvr_set_render_mode(gbvr_renderer* r, int mode);                     /* setRenderMode */
 int gbvr_set_tf1d(gbvr_renderer* r, const float* rgba, int n);            /* changed1DTrans */
 int gbvr_set_tf2d(gbvr_renderer* r, const float* rgba, int w, int h, float max_grad); /* changed2DTrans */
+/* setClipPlane / setClipPlaneEnabled (RenderWindow.cpp:1920-1927, RenderWindow.h:131,168): samples at world
+ * points p (the normalised volume box) with plane[0..2] . p + plane[3] > 0 are dropped; enabled = 0 turns the
+ * plane off (plane may then be NULL). */
+int gbvr_set_clip_plane(gbvr_renderer* r, int enabled, const float plane[4]);
 int gbvr_set_value_range(gbvr_renderer* r, double lo, double hi);         /* TF domain (biasScaleTF) */
 int gbvr_set_iso(gbvr_renderer* r, float value, const float rgb[3]);      /* setIsoValue, setIsosurfaceColor */
 int gbvr_set_lighting(gbvr_renderer* r, int enabled, const float amb[4], const float diff[4],

@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libgbvr.so")
 GBVR_OK = 0
 GBVR_U8, GBVR_U16, GBVR_F32 = 0, 1, 2
 GBVR_CUDA_RAYCASTER = 9
-GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE = 0, 1, 2
+GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE, GBVR_RM_MIP = 0, 1, 2, 3
 GBVR_NEAREST, GBVR_LINEAR = 0, 1
 GBVR_SAMPLER_SW, GBVR_SAMPLER_TEX = 0, 1
 GBVR_FLAG_FLOAT_FB = 1
@@ -135,6 +135,8 @@ SIGNATURES = {
     "gbvr_write_uvf": [P, CP],
     "gbvr_resize": [P, I, I],
     "gbvr_set_render_mode": [P, I],
+    "gbvr_set_clip_plane": [P, I, FP],
+    "gbvr_paint_slice": [P, I, C.c_int64, I, I, I],
     "gbvr_set_tf1d": [P, FP, I],
     "gbvr_set_tf2d": [P, FP, I, I, F],
     "gbvr_set_value_range": [P, D, D],

@@ -921,6 +921,7 @@ struct gbvr_renderer {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
   DevBuf d_tf, d_skip, d_fb8, d_fb32, d_frames, d_prefix, d_counter, d_samples, d_touched, d_tfprefix, d_occ;
+  DevBuf d_tf_slice;  // the 1D TF for 2D slice views, whatever the render mode
   DevBuf d_cellbits, d_cellcount, d_occtmp, d_ooc_skip;
   // out-of-core paging state and the last paint's statistics
   cudaStream_t copy_stream = nullptr;
@@ -1331,6 +1332,59 @@ int paint_plain(gbvr_renderer* r, const gbvr_view* views, int n) {
   return finish(r, n, level);
 }
 
+// 2D slice view into framebuffer 0 (see k_render_slice).
+int paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_y, int use_mip) {
+  TRY(check_loaded(r));
+  const Dataset& ds = r->ds;
+  if (axis < 0 || axis > 2) return fail(GBVR_EINVAL, "slice axis must be 0, 1 or 2");
+  if (index < 0 || index >= ds.dims[axis]) return fail(GBVR_EINVAL, "slice index outside the volume");
+  if (ds.ooc) return fail(GBVR_ESTATE, "2D slices of out-of-core datasets are not supported");
+  int level;
+  TRY(prepare(r, 1, level, nullptr));
+  ensure_tf(r);
+  CUDA_TRY(r->d_tf_slice.alloc(sizeof(float) * r->tf1d.size()));
+  CUDA_TRY(cudaMemcpyAsync(r->d_tf_slice.p, r->tf1d.data(), sizeof(float) * r->tf1d.size(), cudaMemcpyHostToDevice,
+                           r->stream));
+  float dv[16], dp[16];
+  default_camera(r, dv, dp);
+  FrameDesc f = make_frame(r, dv, dp, level, 0);
+  double lo, hi;
+  default_range(r, lo, hi);
+  f.tf = r->d_tf_slice.as<float4>();
+  f.tf_w = (int)(r->tf1d.size() / 4);
+  f.idx_scale = (float)((f.tf_w - 1) / (hi - lo));
+  f.interp = r->interp;
+  const Level& L = ds.levels[level];
+  double ext[3], mx = 0;
+  for (int a = 0; a < 3; ++a) { ext[a] = (double)ds.dims[a] * ds.aspect[a]; mx = std::max(mx, ext[a]); }
+  for (int a = 0; a < 3; ++a) ext[a] /= mx;
+  const int ua = axis == 0 ? 1 : 0, va = axis == 2 ? 1 : 2;
+  SliceDesc sd;
+  sd.axis = axis;
+  // the slice's world position (centre of voxel `index` of the finest level) on the rendered level
+  const double w = ((double)index + 0.5) / (double)ds.dims[axis] * ext[axis];
+  sd.coord = (float)(w * (double)L.dims[axis] / ext[axis] - 0.5);
+  const double sc = std::min((double)r->width / ext[ua], (double)r->height / ext[va]);
+  sd.inv_s = (float)(1.0 / sc);
+  sd.half_w = 0.5f * (float)r->width;
+  sd.half_h = 0.5f * (float)r->height;
+  sd.ext_u = (float)ext[ua];
+  sd.ext_v = (float)ext[va];
+  sd.scale_u = (float)((double)L.dims[ua] / ext[ua]);
+  sd.scale_v = (float)((double)L.dims[va] / ext[va]);
+  sd.flip_x = flip_x ? 1 : 0;
+  sd.flip_y = flip_y ? 1 : 0;
+  sd.mip = use_mip ? 1 : 0;
+  CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long), r->stream));
+  CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
+  CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
+  CUDA_TRY(launch_render_slice(f, sd, r->stream));
+  CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
+  CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
+  r->last_h2d = sizeof(float) * r->tf1d.size();
+  return finish(r, 1, level);
+}
+
 int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   int level;
   const PtrSnapshot before(r);
@@ -1724,6 +1778,11 @@ int gbvr_set_render_mode(gbvr_renderer* r, int mode) {
   if (mode != r->mode) { r->tf_dirty = true; r->skip_dirty = true; }
   r->mode = mode;
   return GBVR_OK;
+}
+
+int gbvr_paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_y, int use_mip) {
+  TRY(check_r(r));
+  return paint_slice(r, axis, index, flip_x, flip_y, use_mip);
 }
 
 int gbvr_set_clip_plane(gbvr_renderer* r, int enabled, const float plane[4]) {

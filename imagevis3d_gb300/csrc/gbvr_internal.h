@@ -100,6 +100,18 @@ struct __align__(16) FrameDesc {
   unsigned* cell_touched;    // per-frame bitmap of sampled non-empty macro-cells (or null)
 };
 
+// A 2D slice view: screen pixels map to the plane through the slice (or to
+// rays along its axis for MIP).
+struct SliceDesc {
+  int axis;            // 0 x (sagittal), 1 y (axial), 2 z (coronal)
+  float coord;         // level voxel coordinate of the slice along `axis`
+  float inv_s;         // world units per pixel
+  float half_w, half_h;  // framebuffer half size, pixels
+  float ext_u, ext_v;  // world extents of the in-plane axes (u = lower-numbered, v = higher)
+  float scale_u, scale_v;  // level voxels per world unit along u, v
+  int flip_x, flip_y, mip;
+};
+
 // Default ray tile handled by one warp: 8 x 4 pixels.
 constexpr int TILE_W = 8;
 
@@ -124,6 +136,7 @@ cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, con
                                            int nframes, const int* tile_prefix, int total_tiles,
                                            int* counter, int grid, cudaStream_t s);
 int persistent_grid_size(int device);
+cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStream_t s);
 
 // ---- launch wrappers (kernels_build.cu) ----
 struct BlobTablesDev {

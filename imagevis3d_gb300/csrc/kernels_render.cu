@@ -617,6 +617,90 @@ __global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const F
 }
 
 // ---------------------------------------------------------------------------
+// 2D slice views (renderRegion2D: a slice at a depth along one axis, or the
+// maximum along that axis): one thread per pixel.  The slice fills the
+// framebuffer at its aspect ratio, centred, with the background around it;
+// screen x follows the lower-numbered in-plane axis, screen y the higher one
+// upwards, each optionally mirrored.  The value at the pixel (trilinear on
+// the level, the axis coordinate at the slice's voxel centre) goes through
+// the 1D TF and over the background.  MIP walks the voxel centres along the
+// axis brick by brick, skipping bricks whose largest voxel cannot raise the
+// maximum.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_render_slice(const __grid_constant__ FrameDesc f, const __grid_constant__ SliceDesc s) {
+  const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y;
+  unsigned ns = 0;
+  if (px < f.width) {
+    float uw = ((float)px + 0.5f - s.half_w) * s.inv_s;
+    float vw = (s.half_h - ((float)py + 0.5f)) * s.inv_s;
+    if (s.flip_x) uw = -uw;
+    if (s.flip_y) vw = -vw;
+    float4 out = make_float4(f.bg[0], f.bg[1], f.bg[2], 0.f);
+    if (fabsf(uw) <= 0.5f * s.ext_u && fabsf(vw) <= 0.5f * s.ext_v) {
+      const float pu = (uw + 0.5f * s.ext_u) * s.scale_u - 0.5f;
+      const float pv = (vw + 0.5f * s.ext_v) * s.scale_v - 0.5f;
+      auto pos = [&](float pa, float& x, float& y, float& z) {
+        x = s.axis == 0 ? pa : pu;
+        y = s.axis == 1 ? pa : (s.axis == 0 ? pu : pv);
+        z = s.axis == 2 ? pa : pv;
+      };
+      float v, x, y, z;
+      if (!s.mip) {
+        pos(s.coord, x, y, z);
+        v = sample_anywhere<T, SAMPLER_SW>(f, x, y, z);
+        ns = 1;
+      } else {
+        v = -INFINITY;
+        const int n = f.dims[s.axis];
+        int k = 0;
+        while (k < n) {
+          pos((float)k, x, y, z);
+          const Cell c = make_cell(f, x, y, z);
+          const int bi = brick_index(f, c.x, c.y, c.z);
+          BrickView b;
+          load_brick(f, bi, b);
+          const int hi = s.axis == 0 ? b.hix : (s.axis == 1 ? b.hiy : b.hiz);
+          if (__ldg(&f.bricks[bi].vmax) > v) {
+            for (; k < hi; ++k) {
+              const int cx = s.axis == 0 ? k : c.x, cy = s.axis == 1 ? k : c.y, cz = s.axis == 2 ? k : c.z;
+              v = fmaxf(v, sample_cell<T, SAMPLER_SW>(f, b, cx, cy, cz, s.axis == 0 ? 0.f : c.fx,
+                                                     s.axis == 1 ? 0.f : c.fy, s.axis == 2 ? 0.f : c.fz));
+              ++ns;
+            }
+          } else {
+            k = hi;
+          }
+          if (v >= f.level_max) break;
+        }
+      }
+      const float4 c = tf1d(f, v);
+      out = make_float4(fmaf(c.w, c.x, (1.f - c.w) * f.bg[0]), fmaf(c.w, c.y, (1.f - c.w) * f.bg[1]),
+                        fmaf(c.w, c.z, (1.f - c.w) * f.bg[2]), c.w);
+    }
+    const size_t o = (size_t)py * f.width + px;
+    if (f.out_f32) f.out_f32[o] = out;
+    if (f.out_rgba8)
+      f.out_rgba8[o] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(out.x) * 255.f),
+                                   (unsigned char)__float2uint_rn(__saturatef(out.y) * 255.f),
+                                   (unsigned char)__float2uint_rn(__saturatef(out.z) * 255.f),
+                                   (unsigned char)__float2uint_rn(__saturatef(out.w) * 255.f));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ns += __shfl_xor_sync(0xffffffffu, ns, o);
+  if ((threadIdx.x & 31) == 0 && f.samples && ns) atomicAdd(f.samples, (unsigned long long)ns);
+}
+
+cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  dim3 grid((unsigned)((f.width + 127) / 128), (unsigned)f.height);
+  if (f.dtype == DT_U8) k_render_slice<uint8_t><<<grid, 128, 0, s>>>(f, sd);
+  else if (f.dtype == DT_U16) k_render_slice<uint16_t><<<grid, 128, 0, s>>>(f, sd);
+  else k_render_slice<float><<<grid, 128, 0, s>>>(f, sd);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Empty-space classification.  Values sampled where a brick or macro-cell
 // applies lie in [vmin, vmax] of the voxels its samples can touch (trilinear
 // weights are convex), so the TF entries such a sample can read are bounded;

@@ -237,6 +237,21 @@ class Renderer:
         """changed2DTrans from a .2dt file (rasterised on the GPU)."""
         L.call("gbvr_set_tf2d_file", self._h, path.encode(), max_grad)
 
+    def paintSlice(self, axis, index, flip_x=False, flip_y=False, use_mip=False):
+        """A 2D render region: the slice `index` (finest-level voxels) across
+        `axis` (0 sagittal x, 1 axial y, 2 coronal z), or the maximum along it."""
+        L.call("gbvr_paint_slice", self._h, axis, index, int(flip_x), int(flip_y), int(use_mip))
+        self._nviews = 1
+
+    def setClipPlane(self, plane, enabled=True):
+        """setClipPlane + setClipPlaneEnabled: drop samples with
+        a x + b y + c z + d > 0 (world coordinates of the normalised box)."""
+        if plane is None:
+            L.call("gbvr_set_clip_plane", self._h, 0, None)
+            return
+        pl, pp = _fp(plane)
+        L.call("gbvr_set_clip_plane", self._h, 1 if enabled else 0, pp)
+
     def setValueRange(self, lo, hi):
         L.call("gbvr_set_value_range", self._h, lo, hi)
 

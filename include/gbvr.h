@@ -184,6 +184,15 @@ int gbvr_resize(gbvr_renderer* r, int width, int height);                 /* res
 int gbvr_set_render_mode(gbvr_renderer* r, int mode);                     /* setRenderMode */
 int gbvr_set_tf1d(gbvr_renderer* r, const float* rgba, int n);            /* changed1DTrans */
 int gbvr_set_tf2d(gbvr_renderer* r, const float* rgba, int w, int h, float max_grad); /* changed2DTrans */
+/* 2D render region (tuvok.renderRegion2D.new(mode, sliceIndex, renderer), setSliceDepth, set2DFlipMode,
+ * setUseMIP: RenderWindow.cpp:1548-1571, 235-239, 270-289) into framebuffer 0.  axis = the window mode:
+ * 0 sagittal (x), 1 axial (y), 2 coronal (z), as the reference indexes getDomainSize() by it; index = the
+ * slice in voxels of the finest level, rendered at the LOD limit's level.  The slice fills the framebuffer
+ * at its aspect ratio, centred, background around it; screen x follows the lower-numbered in-plane axis,
+ * screen y the higher one upwards; flip_x / flip_y mirror them.  Each pixel: the trilinear value at the
+ * slice through the 1D TF over the background.  use_mip: the maximum along the axis instead (maximum-
+ * intensity projection of the whole volume).  Not for out-of-core datasets. */
+int gbvr_paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_y, int use_mip);
 /* setClipPlane / setClipPlaneEnabled (RenderWindow.cpp:1920-1927, RenderWindow.h:131,168): samples at world
  * points p (the normalised volume box) with plane[0..2] . p + plane[3] > 0 are dropped; enabled = 0 turns the
  * plane off (plane may then be NULL). */

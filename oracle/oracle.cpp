@@ -486,7 +486,7 @@ struct orc_render_params {
   double extent[3];     // world box = [-extent/2, +extent/2] (largest axis 1)
   const float* tf;      // 1D: [n][4]; 2D: [h][w][4] (row = gradient bin)
   int tf_w, tf_h;       // 1D: tf_w entries, tf_h = 1
-  int mode;             // 0 1D TF, 1 2D TF + Phong, 2 isosurface
+  int mode;             // 0 1D TF, 1 2D TF + Phong, 2 isosurface, 3 maximum-intensity projection
   int interp;           // 0 nearest, 1 trilinear
   double value_lo, value_hi;   // data value mapped to TF coordinate 0 / 1
   double grad_max;      // 2D TF: |grad| (normalised value per voxel) at the last row
@@ -502,6 +502,8 @@ struct orc_render_params {
   double inv_viewproj[16];  // row-major inverse of proj*view (column vectors)
   double inv_view[16];      // row-major inverse of view
   int width, height;
+  int clip_on;              // clip plane: samples with clip . (x, y, z, 1) > 0 (world) are dropped
+  double clip[4];
 };
 
 struct Vol {
@@ -648,12 +650,29 @@ static void render_pixel(const orc_render_params* p, int px, int py, double* out
     };
     double vscale = 1.0 / (p->value_hi - p->value_lo);
     double prev_t = t0;
+    double vmax = -std::numeric_limits<double>::infinity();
+    bool any = false;
     for (i64 k = 0; k < nk; ++k) {
       double t = t0 + (k + 0.5) * dt;
+      if (p->clip_on) {
+        // the GPU settles the kept range with the same test per sample
+        double s = p->clip[3];
+        for (int q = 0; q < 3; ++q) s += p->clip[q] * (o[q] + t * d[q]);
+        if (s > 0) {
+          prev_t = t;
+          continue;
+        }
+      }
       double x[3];
       to_vox(t, x);
       double v = V.sample(x[0], x[1], x[2]);
       ++ns;
+      if (p->mode == 3) {
+        vmax = std::max(vmax, v);
+        any = true;
+        prev_t = t;
+        continue;
+      }
       if (p->mode == 2) {
         if (v >= p->iso) {
           double tl = (k == 0) ? t0 : prev_t, th = t;
@@ -701,10 +720,60 @@ static void render_pixel(const orc_render_params* p, int px, int py, double* out
       A += w;
       if (A >= p->ert) break;
     }
+    if (p->mode == 3 && any) {
+      // maximum-intensity projection: the maximum through the 1D TF, once
+      double c[4];
+      tf1d_lookup(p, (vmax - p->value_lo) * vscale * (p->tf_w - 1), c);
+      for (int q = 0; q < 3; ++q) C[q] = c[q] * c[3];
+      A = c[3];
+    }
   }
   for (int k = 0; k < 3; ++k) out[k] = C[k] + (1.0 - A) * p->bg[k];
   out[3] = A;
   if (nsamples) *nsamples = ns;
+}
+
+// 2D slice view: framebuffer pixel -> point on the slice plane (the plane
+// fills the image at its aspect ratio, centred; screen x = the lower-numbered
+// in-plane axis, screen y = the higher one upwards; flips mirror them); the
+// trilinear value at the slice's axis coordinate `coord` (level voxels), or
+// with mip the maximum over the voxel centres along the axis, through the 1D
+// TF over the background.  out: [height][width][4] doubles.
+void orc_render_slice(const orc_render_params* p, int axis, double coord, int flip_x, int flip_y, int mip,
+                      double* out) {
+  Vol V{p};
+  const int ua = axis == 0 ? 1 : 0, va = axis == 2 ? 1 : 2;
+  const double eu = p->extent[ua], ev = p->extent[va];
+  const double sc = std::min((double)p->width / eu, (double)p->height / ev);
+  const double vscale = 1.0 / (p->value_hi - p->value_lo);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int py = 0; py < p->height; ++py)
+    for (int px = 0; px < p->width; ++px) {
+      double uw = (px + 0.5 - 0.5 * p->width) / sc, vw = (0.5 * p->height - (py + 0.5)) / sc;
+      if (flip_x) uw = -uw;
+      if (flip_y) vw = -vw;
+      double* o = out + 4 * ((i64)py * p->width + px);
+      o[0] = p->bg[0]; o[1] = p->bg[1]; o[2] = p->bg[2]; o[3] = 0.0;
+      if (std::fabs(uw) > 0.5 * eu || std::fabs(vw) > 0.5 * ev) continue;
+      double x[3];
+      x[ua] = (uw + 0.5 * eu) * (double)p->dims[ua] / eu - 0.5;
+      x[va] = (vw + 0.5 * ev) * (double)p->dims[va] / ev - 0.5;
+      double v;
+      if (!mip) {
+        x[axis] = coord;
+        v = V.sample(x[0], x[1], x[2]);
+      } else {
+        v = -std::numeric_limits<double>::infinity();
+        for (i64 k = 0; k < p->dims[axis]; ++k) {
+          x[axis] = (double)k;
+          v = std::max(v, V.sample(x[0], x[1], x[2]));
+        }
+      }
+      double c[4];
+      tf1d_lookup(p, (v - p->value_lo) * vscale * (p->tf_w - 1), c);
+      for (int q = 0; q < 3; ++q) o[q] = c[3] * c[q] + (1.0 - c[3]) * p->bg[q];
+      o[3] = c[3];
+    }
 }
 
 // Render `npix` pixels (indices into the width*height image, row 0 = top) or

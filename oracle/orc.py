@@ -25,7 +25,7 @@ class RenderParams(C.Structure):
         ("samples_per_voxel", D), ("ert", D), ("iso", D), ("iso_rgb", D * 3), ("lighting", C.c_int),
         ("amb", D * 3), ("diff", D * 3), ("spec", D * 3), ("shininess", D),
         ("light_dir_eye", D * 3), ("bg", D * 3), ("inv_viewproj", D * 16), ("inv_view", D * 16),
-        ("width", C.c_int), ("height", C.c_int),
+        ("width", C.c_int), ("height", C.c_int), ("clip_on", C.c_int), ("clip", D * 4),
     ]
 
 
@@ -144,8 +144,10 @@ def synth_blobs(params):
 def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0), mode=0,
            interp=1, ert=0.99, extent=None, grad_max=1.0, iso=0.0, iso_rgb=(1, 1, 1), lighting=1,
            amb=(0.1, 0.1, 0.1), diff=(1, 1, 1), spec=(1, 1, 1), shininess=8.0,
-           light_dir=(0, 0, -1), bg=(0, 0, 0), pixels=None, threads=0):
-    """FP64 render of `vol` (the flat level, (z, y, x)).  Returns
+           light_dir=(0, 0, -1), bg=(0, 0, 0), pixels=None, threads=0, clip=None):
+    """FP64 render of `vol` (the flat level, (z, y, x)).  mode 0 1D TF, 1 2D TF
+    + Phong, 2 isosurface, 3 maximum-intensity projection; clip = plane
+    (a, b, c, d) dropping samples with a x + b y + c z + d > 0.  Returns
     (rgba float64 [n, 4] or [h, w, 4], samples)."""
     vol = np.ascontiguousarray(vol)
     tf = np.ascontiguousarray(tf, np.float32)
@@ -181,6 +183,10 @@ def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0)
         p.inv_viewproj[i] = Mi.ravel()[i]
         p.inv_view[i] = Vi.ravel()[i]
     p.width, p.height = width, height
+    if clip is not None:
+        p.clip_on = 1
+        for i in range(4):
+            p.clip[i] = clip[i]
     if pixels is None:
         out = np.zeros((height * width, 4), np.float64)
         ns = lib().orc_render(C.byref(p), None, I64(0), out.ctypes.data_as(C.POINTER(D)), threads)
@@ -190,6 +196,33 @@ def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0)
     ns = lib().orc_render(C.byref(p), pix.ctypes.data_as(C.POINTER(I64)), I64(pix.size),
                           out.ctypes.data_as(C.POINTER(D)), threads)
     return out, ns
+
+
+def render_slice(vol, axis, coord, width, height, tf, value_range=(0.0, 255.0), flip_x=False, flip_y=False,
+                 mip=False, interp=1, extent=None, bg=(0, 0, 0)):
+    """FP64 2D slice view of the flat level `vol` ((z, y, x)): [h, w, 4]."""
+    vol = np.ascontiguousarray(vol)
+    tf = np.ascontiguousarray(tf, np.float32)
+    p = RenderParams()
+    p.vol = vol.ctypes.data
+    p.dtype = _DT[vol.dtype]
+    for i, d in enumerate((vol.shape[2], vol.shape[1], vol.shape[0])):
+        p.dims[i] = d
+    if extent is None:
+        m = max(vol.shape)
+        extent = (vol.shape[2] / m, vol.shape[1] / m, vol.shape[0] / m)
+    for i in range(3):
+        p.extent[i] = extent[i]
+        p.bg[i] = bg[i]
+    p.tf = tf.ctypes.data_as(C.POINTER(C.c_float))
+    p.tf_w, p.tf_h = tf.shape[0], 1
+    p.interp = interp
+    p.value_lo, p.value_hi = value_range
+    p.width, p.height = width, height
+    out = np.zeros((height, width, 4), np.float64)
+    lib().orc_render_slice(C.byref(p), axis, D(coord), int(flip_x), int(flip_y), int(mip),
+                           out.ctypes.data_as(C.POINTER(D)))
+    return out
 
 
 def max_threads():

@@ -7,6 +7,9 @@
 // Compress(4096), Histogram2DDataBlock::Compute).  Every kernel here is
 // integer-exact (or a fixed float32 operation order with round-to-nearest
 // intrinsics), so results are bit-identical to the CPU restatement.
+#include <algorithm>
+#include <cstdint>
+
 #include "gbvr_internal.h"
 
 namespace gbvr {
@@ -607,8 +610,246 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
   if (run) atomicAdd(hist + run_bin, run);
 }
 
+// ---- vectorised row walk: rows whose length is a multiple of 4 voxels ----
+// Each thread takes 4 consecutive voxels of a row per step: one 4-voxel load
+// from each of the row, the rows at y +- 1 and the planes at z +- 1, and two
+// scalar loads for the x neighbours.  The border rules (one-sided difference
+// x 2 on the volume's faces) are decided once per row as a pair of row
+// pointers and a multiplier.  Same integer differences as int_diffs.
+template <typename T> struct Quad;
+template <> struct Quad<uint8_t> { using V = uchar4; };
+template <> struct Quad<uint16_t> { using V = ushort4; };
+
+template <typename T>
+__device__ __forceinline__ void ld4(const T* p, int q[4]) {
+  const typename Quad<T>::V w = __ldg(reinterpret_cast<const typename Quad<T>::V*>(p));
+  q[0] = w.x; q[1] = w.y; q[2] = w.z; q[3] = w.w;
+}
+
+template <typename T>
+struct RowWalk {
+  const T *c, *ym, *yp, *zm, *zp;
+  int my, mz;
+  __device__ __forceinline__ RowWalk(const T* v, int X, int Y, int Z, long long row, int y, int z) {
+    const long long plane = (long long)X * Y;
+    c = v + row * X;
+    if (Y == 1) { ym = yp = c; my = 0; }
+    else if (y == 0) { ym = c; yp = c + X; my = 2; }
+    else if (y == Y - 1) { ym = c - X; yp = c; my = 2; }
+    else { ym = c - X; yp = c + X; my = 1; }
+    if (Z == 1) { zm = zp = c; mz = 0; }
+    else if (z == 0) { zm = c; zp = c + plane; mz = 2; }
+    else if (z == Z - 1) { zm = c - plane; zp = c; mz = 2; }
+    else { zm = c - plane; zp = c + plane; mz = 1; }
+  }
+  // S = Dx^2 + Dy^2 + Dz^2 and the voxel values for x0 .. x0 + 3
+  __device__ __forceinline__ void quad(int x0, int X, unsigned long long S[4], int val[4]) const {
+    int a[4], b[4], e[4], f[4];
+    ld4(c + x0, val);
+    ld4(ym + x0, a);
+    ld4(yp + x0, b);
+    ld4(zm + x0, e);
+    ld4(zp + x0, f);
+    const int xl = x0 > 0 ? (int)__ldg(c + x0 - 1) : 0;
+    const int xr = x0 + 4 < X ? (int)__ldg(c + x0 + 4) : 0;
+    int dx[4];
+    dx[0] = x0 == 0 ? 2 * (val[1] - val[0]) : val[1] - xl;
+    dx[1] = val[2] - val[0];
+    dx[2] = val[3] - val[1];
+    dx[3] = x0 + 4 == X ? 2 * (val[3] - val[2]) : xr - val[2];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const long long dy = (long long)my * (b[j] - a[j]), dz = (long long)mz * (f[j] - e[j]);
+      S[j] = (unsigned long long)((long long)dx[j] * dx[j] + dy * dy + dz * dz);
+    }
+  }
+};
+
+template <typename T>
+__global__ void k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DScratch* sc) {
+  unsigned long long smax = 0;
+  const long long rows = (long long)Y * Z;
+  for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int z = (int)(row / Y), y = (int)(row - (long long)z * Y);
+    const RowWalk<T> w(v, X, Y, Z, row, y, z);
+    for (int x0 = 4 * threadIdx.x; x0 < X; x0 += 4 * blockDim.x) {
+      unsigned long long S[4];
+      int val[4];
+      w.quad(x0, X, S, val);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) smax = S[j] > smax ? S[j] : smax;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, smax, o);
+    smax = t > smax ? t : smax;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(&sc->smax, smax);
+}
+
+template <typename T>
+__global__ void k_h2v_gmax(const T* __restrict__ v, int X, int Y, int Z, double c, Hist2DScratch* sc) {
+  const unsigned long long smax = sc->smax;
+  if (smax == 0) return;
+  const long long rows = (long long)Y * Z;
+  for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int z = (int)(row / Y), y = (int)(row - (long long)z * Y);
+    const RowWalk<T> w(v, X, Y, Z, row, y, z);
+    for (int x0 = 4 * threadIdx.x; x0 < X; x0 += 4 * blockDim.x) {
+      unsigned long long S[4];
+      int val[4];
+      w.quad(x0, X, S, val);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (S[j] == smax) {
+          const double g = grad_f64(v, X, Y, Z, x0 + j, y, z, row * X + x0 + j, c);
+          atomicMax(&sc->gmax_bits, (unsigned long long)__double_as_longlong(g));
+        }
+    }
+  }
+}
+
+// Pass 2.  SMEM: the block counts into a shared copy of the whole histogram
+// (two 16-bit counters per word; nx * 256 <= 65536 bins = 128 KB) and adds it
+// to the global one every `flush_rows` rows of its own, before any counter
+// can reach 2^16 (flush_rows * X <= 65535).  Runs of equal bins along a
+// thread's voxels are counted in registers first either way.
+template <typename T, bool SMEM>
+__global__ void k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx, int merge,
+                          unsigned long long* __restrict__ hist, const Hist2DScratch* sc, int flush_rows) {
+  extern __shared__ unsigned sh[];
+  const unsigned long long smax = sc->smax;
+  const double gmax = __longlong_as_double((long long)sc->gmax_bits);
+  const float smax_f = (float)smax;
+  const unsigned merge32 = (unsigned)merge;
+  const int words = nx * 128;
+  if (SMEM) {
+    for (int i = threadIdx.x; i < words; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+  }
+  unsigned run_bin = ~0u, run = 0;
+  auto add = [&](unsigned bin, unsigned cnt) {
+    if (SMEM) atomicAdd(sh + (bin >> 1), cnt << ((bin & 1u) << 4));
+    else atomicAdd(hist + bin, (unsigned long long)cnt);
+  };
+  auto flush = [&]() {
+    if (run) add(run_bin, run);
+    run = 0;
+    run_bin = ~0u;
+    __syncthreads();
+    for (int i = threadIdx.x; i < words; i += blockDim.x) {
+      const unsigned wv = sh[i];
+      if (wv) {
+        if (wv & 0xffffu) atomicAdd(hist + 2 * i, (unsigned long long)(wv & 0xffffu));
+        if (wv >> 16) atomicAdd(hist + 2 * i + 1, (unsigned long long)(wv >> 16));
+        sh[i] = 0;
+      }
+    }
+    __syncthreads();
+  };
+  const long long rows = (long long)Y * Z;
+  int since = 0;
+  for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int z = (int)(row / Y), y = (int)(row - (long long)z * Y);
+    const RowWalk<T> w(v, X, Y, Z, row, y, z);
+    for (int x0 = 4 * threadIdx.x; x0 < X; x0 += 4 * blockDim.x) {
+      unsigned long long S[4];
+      int val[4];
+      w.quad(x0, X, S, val);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        int k = 0;
+        if (smax > 0 && S[j] > 0) {
+          const unsigned long long lhs = 65025ULL * S[j];
+          // FP32 estimate (within one of the exact bin), settled exactly
+          k = (int)(255.f * sqrtf(__fdiv_rn((float)S[j], smax_f)));
+          if (k > 255) k = 255;
+          while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
+          while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;
+          if ((unsigned long long)k * k * smax == lhs) {
+            // exact tie: the f64 formula decides
+            const double g = grad_f64(v, X, Y, Z, x0 + j, y, z, row * X + x0 + j, c);
+            k = (int)floor(__dmul_rn(__ddiv_rn(g, gmax), 255.0));
+            if (k > 255) k = 255;
+          }
+        }
+        int bx = merge32 == 1 ? val[j] : (int)((unsigned)val[j] / merge32);
+        if (bx >= nx) bx = nx - 1;
+        const unsigned bin = (unsigned)bx * 256u + (unsigned)k;
+        if (bin == run_bin) {
+          ++run;
+        } else {
+          if (run) add(run_bin, run);
+          run_bin = bin;
+          run = 1;
+        }
+      }
+    }
+    if (SMEM && ++since == flush_rows) {
+      flush();
+      since = 0;
+    }
+  }
+  if (SMEM) {
+    flush();
+  } else if (run) {
+    add(run_bin, run);
+  }
+}
+
 cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], double max_scalar, long long nx,
                           long long merge, unsigned long long* hist, Hist2DScratch* scratch, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (dtype == DT_F32) return cudaErrorInvalidValue;
+  {
+    const long long X = dims[0], Y = dims[1], Z = dims[2];
+    const size_t es = dtype == DT_U8 ? 1 : 2;
+    const bool vec = X >= 4 && X % 4 == 0 && X <= (1LL << 30) && Y <= (1LL << 30) && Z <= (1LL << 30) &&
+                     ((uintptr_t)vol % (4 * es)) == 0 && merge >= 1 && merge <= 65536 && nx >= 1 && nx <= (1LL << 22);
+    if (vec) {
+      int dev = 0, sms = 152;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      const double c = max_scalar > 0 ? max_scalar : 1.0;
+      const long long cpr = X / 4;
+      int threads = (int)std::min<long long>(1024, (cpr + 31) / 32 * 32);
+      if (threads < 128) threads = 128;
+      const long long rows = Y * Z;
+      const int grid = (int)std::min<long long>(rows, (long long)sms * (2048 / threads));
+      cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(Hist2DScratch), s);
+      if (e != cudaSuccess) return e;
+      const bool smem = nx * 256 <= 65536 && X <= 65535;
+      const size_t shbytes = smem ? (size_t)nx * 128 * sizeof(unsigned) : 0;
+      const int flush_rows = smem ? (int)std::max<long long>(1, 65535 / X) : 0;
+      const int per_sm = smem ? (int)std::max<size_t>(1, std::min<size_t>(2048 / threads, (227 * 1024) / shbytes)) : 0;
+      const int grid2 = smem ? (int)std::min<long long>(rows, (long long)sms * per_sm) : grid;
+      const int nxi = (int)nx, mi = (int)merge, Xi = (int)X, Yi = (int)Y, Zi = (int)Z;
+      if (dtype == DT_U8) {
+        const uint8_t* v = (const uint8_t*)vol;
+        k_h2v_max<<<grid, threads, 0, s>>>(v, Xi, Yi, Zi, scratch);
+        k_h2v_gmax<<<grid, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch);
+        if (smem) {
+          e = cudaFuncSetAttribute(k_h2v_bin<uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
+          if (e != cudaSuccess) return e;
+          k_h2v_bin<uint8_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_rows);
+        } else {
+          k_h2v_bin<uint8_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0);
+        }
+      } else {
+        const uint16_t* v = (const uint16_t*)vol;
+        k_h2v_max<<<grid, threads, 0, s>>>(v, Xi, Yi, Zi, scratch);
+        k_h2v_gmax<<<grid, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch);
+        if (smem) {
+          e = cudaFuncSetAttribute(k_h2v_bin<uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
+          if (e != cudaSuccess) return e;
+          k_h2v_bin<uint16_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_rows);
+        } else {
+          k_h2v_bin<uint16_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0);
+        }
+      }
+      return cudaGetLastError();
+    }
+  }
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (dtype == DT_F32) return cudaErrorInvalidValue;
   const long long X = dims[0], Y = dims[1], Z = dims[2];

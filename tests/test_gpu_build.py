@@ -120,3 +120,46 @@ def test_constant_and_tiny_volumes(orc):
             h2, mg = orc.hist2d(vol, float(vol.max()), h1.size, f)
             g2, gmg = r.get2DHistogram()
             assert np.array_equal(g2, h2) and np.float32(gmg) == np.float32(mg)
+
+
+def _dev_hist2d(vol, max_scalar, nx, merge, offset=0):
+    import ctypes as C
+    import torch
+    from imagevis3d_gb300 import _lib as L
+    flat = torch.from_numpy(np.ascontiguousarray(vol).reshape(-1).view(np.uint8))
+    buf = torch.zeros(flat.numel() + 16, dtype=torch.uint8, device="cuda")
+    buf[offset:offset + flat.numel()] = flat.cuda()
+    hist = torch.zeros(nx * 256, dtype=torch.int64, device="cuda")
+    dims = (C.c_int64 * 3)(vol.shape[2], vol.shape[1], vol.shape[0])
+    mg = C.c_float()
+    L.call("gbvr_dev_hist2d", C.c_void_p(buf.data_ptr() + offset), 0 if vol.dtype == np.uint8 else 1, dims,
+           max_scalar, nx, merge, C.c_void_p(hist.data_ptr()), C.byref(mg), None)
+    torch.cuda.synchronize()
+    return hist.cpu().numpy().astype(np.uint64).reshape(nx, 256), mg.value
+
+
+def _hist2d_cases(orc):
+    blobs = lambda dims, dt, vmax, scale: orc.synth_blobs(
+        synth_params(dims, dt, 9, 10, (3.0, 9.0), (0.3, 1.0), scale, noise_kind=1, noise_amp=3.0, vmax=vmax))
+    z, y, x = np.meshgrid(np.arange(20), np.arange(30), np.arange(40), indexing="ij")
+    return {
+        "u8_smem": (blobs((200, 64, 48), np.uint8, 255.0, 255.0), 0),
+        "u8_periodic_flush": (blobs((16384, 64, 16), np.uint8, 255.0, 255.0), 0),
+        "u8_x4": (blobs((4, 30, 20), np.uint8, 255.0, 255.0), 0),
+        "u8_misaligned": (blobs((200, 64, 48), np.uint8, 255.0, 255.0), 1),
+        "u8_ramp_ties": (((x + y + z) % 200).astype(np.uint8), 0),
+        "u16_smem": (blobs((96, 50, 40), np.uint16, 200.0, 200.0), 0),
+        "u16_global": (blobs((128, 40, 36), np.uint16, 4095.0, 2600.0), 0),
+    }
+
+
+@pytest.mark.parametrize("case", ["u8_smem", "u8_periodic_flush", "u8_x4", "u8_misaligned", "u8_ramp_ties",
+                                  "u16_smem", "u16_global"])
+def test_dev_hist2d_paths_bit_exact(orc, case):
+    vol, offset = _hist2d_cases(orc)[case]
+    h1, f = orc.hist1d(vol)
+    ms = float(vol.max())
+    want, wmg = orc.hist2d(vol, ms, h1.size, f)
+    got, gmg = _dev_hist2d(vol, ms, h1.size, f, offset)
+    assert np.array_equal(got, want), case
+    assert np.float32(gmg) == np.float32(wmg)

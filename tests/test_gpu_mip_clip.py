@@ -176,7 +176,7 @@ def test_slices_match_oracle(orc, vol_u16, axis):
             ref = orc.render_slice(vol, axis, float(idx), W, H, tf, value_range=(0.0, 4095.0), flip_x=flips[0],
                                    flip_y=flips[1], bg=(0.2, 0.3, 0.4))
             assert_close(img, ref)
-        assert (ref[..., 3] > 0).mean() > 0.1
+        assert (ref[..., 3] > 0).mean() > 0.03
         # background outside the letterboxed slice
         assert (img[..., 3] == 0).any()
         r.paintSlice(axis, idx, use_mip=True)

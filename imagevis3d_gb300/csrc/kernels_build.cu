@@ -666,7 +666,7 @@ struct RowWalk {
 };
 
 template <typename T>
-__global__ void k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DScratch* sc) {
+__global__ void __launch_bounds__(512) k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DScratch* sc) {
   unsigned long long smax = 0;
   const long long rows = (long long)Y * Z;
   for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
@@ -688,7 +688,7 @@ __global__ void k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DSc
 }
 
 template <typename T>
-__global__ void k_h2v_gmax(const T* __restrict__ v, int X, int Y, int Z, double c, Hist2DScratch* sc) {
+__global__ void __launch_bounds__(512) k_h2v_gmax(const T* __restrict__ v, int X, int Y, int Z, double c, Hist2DScratch* sc) {
   const unsigned long long smax = sc->smax;
   if (smax == 0) return;
   const long long rows = (long long)Y * Z;
@@ -715,7 +715,7 @@ __global__ void k_h2v_gmax(const T* __restrict__ v, int X, int Y, int Z, double 
 // can reach 2^16 (flush_rows * X <= 65535).  Runs of equal bins along a
 // thread's voxels are counted in registers first either way.
 template <typename T, bool SMEM>
-__global__ void k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx, int merge,
+__global__ void __launch_bounds__(512) k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx, int merge,
                           unsigned long long* __restrict__ hist, const Hist2DScratch* sc, int flush_rows) {
   extern __shared__ unsigned sh[];
   const unsigned long long smax = sc->smax;
@@ -812,7 +812,7 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       const double c = max_scalar > 0 ? max_scalar : 1.0;
       const long long cpr = X / 4;
-      int threads = (int)std::min<long long>(1024, (cpr + 31) / 32 * 32);
+      int threads = (int)std::min<long long>(512, (cpr + 31) / 32 * 32);
       if (threads < 128) threads = 128;
       const long long rows = Y * Z;
       const int grid = (int)std::min<long long>(rows, (long long)sms * (2048 / threads));

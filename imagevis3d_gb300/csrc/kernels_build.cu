@@ -610,12 +610,13 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
   if (run) atomicAdd(hist + run_bin, run);
 }
 
-// ---- vectorised row walk: rows whose length is a multiple of 4 voxels ----
-// Each thread takes 4 consecutive voxels of a row per step: one 4-voxel load
-// from each of the row, the rows at y +- 1 and the planes at z +- 1, and two
-// scalar loads for the x neighbours.  The border rules (one-sided difference
-// x 2 on the volume's faces) are decided once per row as a pair of row
-// pointers and a multiplier.  Same integer differences as int_diffs.
+// ---- vectorised z-march: rows whose length is a multiple of 4 voxels ----
+// Each thread owns a column of 4 consecutive voxels (x0 .. x0 + 3 of row y)
+// and walks it along z, keeping the planes z - 1, z, z + 1 of the column in
+// registers: per step one 4-voxel load of the next plane, one of each of the
+// rows y - 1 and y + 1, and two scalar loads for the x neighbours.  The
+// border rules (one-sided difference x 2 on the faces) are the multipliers
+// my / mz.  Same integer differences as int_diffs.
 template <typename T> struct Quad;
 template <> struct Quad<uint8_t> { using V = uchar4; };
 template <> struct Quad<uint16_t> { using V = ushort4; };
@@ -627,110 +628,133 @@ __device__ __forceinline__ void ld4(const T* p, int q[4]) {
 }
 
 template <typename T>
-struct RowWalk {
-  const T *c, *ym, *yp, *zm, *zp;
-  int my, mz;
-  __device__ __forceinline__ RowWalk(const T* v, int X, int Y, int Z, long long row, int y, int z) {
-    const long long plane = (long long)X * Y;
-    c = v + row * X;
-    if (Y == 1) { ym = yp = c; my = 0; }
-    else if (y == 0) { ym = c; yp = c + X; my = 2; }
-    else if (y == Y - 1) { ym = c - X; yp = c; my = 2; }
-    else { ym = c - X; yp = c + X; my = 1; }
-    if (Z == 1) { zm = zp = c; mz = 0; }
-    else if (z == 0) { zm = c; zp = c + plane; mz = 2; }
-    else if (z == Z - 1) { zm = c - plane; zp = c; mz = 2; }
-    else { zm = c - plane; zp = c + plane; mz = 1; }
+struct Column {
+  const T* base;  // voxel (x0, y, 0)
+  long long plane;
+  int X, Z, x0, ym, yp, my;
+  int prv[4], cur[4], nxt[4];
+  __device__ __forceinline__ Column(const T* v, int X_, int Y, int Z_, int x0_, int y) {
+    X = X_; Z = Z_; x0 = x0_;
+    plane = (long long)X * Y;
+    base = v + (long long)y * X + x0;
+    if (Y == 1) { ym = yp = 0; my = 0; }
+    else if (y == 0) { ym = 0; yp = X; my = 2; }
+    else if (y == Y - 1) { ym = -X; yp = 0; my = 2; }
+    else { ym = -X; yp = X; my = 1; }
+    ld4(base, cur);
+    if (Z > 1) ld4(base + plane, nxt);
+    else { nxt[0] = cur[0]; nxt[1] = cur[1]; nxt[2] = cur[2]; nxt[3] = cur[3]; }
+    prv[0] = cur[0]; prv[1] = cur[1]; prv[2] = cur[2]; prv[3] = cur[3];
   }
-  // S = Dx^2 + Dy^2 + Dz^2 and the voxel values for x0 .. x0 + 3
-  __device__ __forceinline__ void quad(int x0, int X, unsigned long long S[4], int val[4]) const {
-    int a[4], b[4], e[4], f[4];
-    ld4(c + x0, val);
-    ld4(ym + x0, a);
-    ld4(yp + x0, b);
-    ld4(zm + x0, e);
-    ld4(zp + x0, f);
-    const int xl = x0 > 0 ? (int)__ldg(c + x0 - 1) : 0;
-    const int xr = x0 + 4 < X ? (int)__ldg(c + x0 + 4) : 0;
+  // S = Dx^2 + Dy^2 + Dz^2 of the 4 voxels at plane z (their values in cur)
+  __device__ __forceinline__ void diffs(int z, unsigned long long S[4]) const {
+    const T* row = base + z * plane;
+    int a[4], b[4];
+    ld4(row + ym, a);
+    ld4(row + yp, b);
+    const int xl = x0 > 0 ? (int)__ldg(row - 1) : 0;
+    const int xr = x0 + 4 < X ? (int)__ldg(row + 4) : 0;
     int dx[4];
-    dx[0] = x0 == 0 ? 2 * (val[1] - val[0]) : val[1] - xl;
-    dx[1] = val[2] - val[0];
-    dx[2] = val[3] - val[1];
-    dx[3] = x0 + 4 == X ? 2 * (val[3] - val[2]) : xr - val[2];
+    dx[0] = x0 == 0 ? 2 * (cur[1] - cur[0]) : cur[1] - xl;
+    dx[1] = cur[2] - cur[0];
+    dx[2] = cur[3] - cur[1];
+    dx[3] = x0 + 4 == X ? 2 * (cur[3] - cur[2]) : xr - cur[2];
+    const int mz = Z == 1 ? 0 : ((z == 0 || z == Z - 1) ? 2 : 1);
+    const int* zm = z == 0 ? cur : prv;
+    const int* zp = z == Z - 1 ? cur : nxt;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const long long dy = (long long)my * (b[j] - a[j]), dz = (long long)mz * (f[j] - e[j]);
+      const long long dy = (long long)my * (b[j] - a[j]), dz = (long long)mz * (zp[j] - zm[j]);
       S[j] = (unsigned long long)((long long)dx[j] * dx[j] + dy * dy + dz * dz);
     }
   }
+  // move to plane z + 1
+  __device__ __forceinline__ void step(int z) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { prv[j] = cur[j]; cur[j] = nxt[j]; }
+    if (z + 2 < Z) ld4(base + (z + 2) * plane, nxt);
+  }
 };
 
+// Pass 1: the largest S.  One thread per 4-voxel column (all of z).
 template <typename T>
-__global__ void __launch_bounds__(512) k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DScratch* sc) {
+__global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DScratch* sc) {
+  const int cpr = X >> 2;
+  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long smax = 0;
-  const long long rows = (long long)Y * Z;
-  for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
-    const int z = (int)(row / Y), y = (int)(row - (long long)z * Y);
-    const RowWalk<T> w(v, X, Y, Z, row, y, z);
-    for (int x0 = 4 * threadIdx.x; x0 < X; x0 += 4 * blockDim.x) {
+  if (col < (long long)cpr * Y) {
+    const int y = (int)(col / cpr), x0 = 4 * (int)(col - (long long)y * cpr);
+    Column<T> c(v, X, Y, Z, x0, y);
+    for (int z = 0; z < Z; ++z) {
       unsigned long long S[4];
-      int val[4];
-      w.quad(x0, X, S, val);
+      c.diffs(z, S);
 #pragma unroll
       for (int j = 0; j < 4; ++j) smax = S[j] > smax ? S[j] : smax;
+      c.step(z);
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long t = __shfl_xor_sync(0xffffffffu, smax, o);
     smax = t > smax ? t : smax;
   }
-  if ((threadIdx.x & 31) == 0) atomicMax(&sc->smax, smax);
+  if ((threadIdx.x & 31) == 0 && smax) atomicMax(&sc->smax, smax);
 }
 
+// Pass 1b: the f64 |g| over the voxels attaining Smax.
 template <typename T>
-__global__ void __launch_bounds__(512) k_h2v_gmax(const T* __restrict__ v, int X, int Y, int Z, double c, Hist2DScratch* sc) {
+__global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X, int Y, int Z, double c,
+                                                  Hist2DScratch* sc) {
   const unsigned long long smax = sc->smax;
   if (smax == 0) return;
-  const long long rows = (long long)Y * Z;
-  for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
-    const int z = (int)(row / Y), y = (int)(row - (long long)z * Y);
-    const RowWalk<T> w(v, X, Y, Z, row, y, z);
-    for (int x0 = 4 * threadIdx.x; x0 < X; x0 += 4 * blockDim.x) {
-      unsigned long long S[4];
-      int val[4];
-      w.quad(x0, X, S, val);
+  const int cpr = X >> 2;
+  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= (long long)cpr * Y) return;
+  const int y = (int)(col / cpr), x0 = 4 * (int)(col - (long long)y * cpr);
+  Column<T> cl(v, X, Y, Z, x0, y);
+  for (int z = 0; z < Z; ++z) {
+    unsigned long long S[4];
+    cl.diffs(z, S);
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
-        if (S[j] == smax) {
-          const double g = grad_f64(v, X, Y, Z, x0 + j, y, z, row * X + x0 + j, c);
-          atomicMax(&sc->gmax_bits, (unsigned long long)__double_as_longlong(g));
-        }
-    }
+    for (int j = 0; j < 4; ++j)
+      if (S[j] == smax) {
+        const double g = grad_f64(v, X, Y, Z, x0 + j, y, z, ((long long)z * Y + y) * X + x0 + j, c);
+        atomicMax(&sc->gmax_bits, (unsigned long long)__double_as_longlong(g));
+      }
+    cl.step(z);
   }
 }
 
-// Pass 2.  SMEM: the block counts into a shared copy of the whole histogram
-// (two 16-bit counters per word; nx * 256 <= 65536 bins = 128 KB) and adds it
-// to the global one every `flush_rows` rows of its own, before any counter
-// can reach 2^16 (flush_rows * X <= 65535).  Runs of equal bins along a
-// thread's voxels are counted in registers first either way.
+// Pass 2: bins.  SMEM: each block counts the gradient rows k < kshared into
+// a shared copy of that part of the histogram (two 16-bit counters per word,
+// nx * kshared bins; about 48 KB so several blocks share an SM) and adds it
+// to the global one every `flush_steps` z-steps, before any counter can
+// reach 2^16 (flush_steps * 4 * blockDim <= 65535); higher rows, rare in
+// practice, go to global memory directly.  Blocks loop over groups of
+// blockDim columns.  Runs of equal bins along a thread's voxels are counted
+// in registers first either way.
 template <typename T, bool SMEM>
-__global__ void __launch_bounds__(512) k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx, int merge,
-                          unsigned long long* __restrict__ hist, const Hist2DScratch* sc, int flush_rows) {
+__global__ void __launch_bounds__(256) k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx,
+                                                 int merge, unsigned long long* __restrict__ hist,
+                                                 const Hist2DScratch* sc, int flush_steps, int kshared) {
   extern __shared__ unsigned sh[];
   const unsigned long long smax = sc->smax;
   const double gmax = __longlong_as_double((long long)sc->gmax_bits);
   const float smax_f = (float)smax;
   const unsigned merge32 = (unsigned)merge;
-  const int words = nx * 128;
+  const int words = nx * kshared / 2;  // kshared is even
   if (SMEM) {
     for (int i = threadIdx.x; i < words; i += blockDim.x) sh[i] = 0;
     __syncthreads();
   }
   unsigned run_bin = ~0u, run = 0;
   auto add = [&](unsigned bin, unsigned cnt) {
-    if (SMEM) atomicAdd(sh + (bin >> 1), cnt << ((bin & 1u) << 4));
-    else atomicAdd(hist + bin, (unsigned long long)cnt);
+    const unsigned k = bin & 255u;
+    if (SMEM && k < (unsigned)kshared) {
+      const unsigned sb = (bin >> 8) * (unsigned)kshared + k;
+      atomicAdd(sh + (sb >> 1), cnt << ((sb & 1u) << 4));
+    } else {
+      atomicAdd(hist + bin, (unsigned long long)cnt);
+    }
   };
   auto flush = [&]() {
     if (run) add(run_bin, run);
@@ -740,54 +764,61 @@ __global__ void __launch_bounds__(512) k_h2v_bin(const T* __restrict__ v, int X,
     for (int i = threadIdx.x; i < words; i += blockDim.x) {
       const unsigned wv = sh[i];
       if (wv) {
-        if (wv & 0xffffu) atomicAdd(hist + 2 * i, (unsigned long long)(wv & 0xffffu));
-        if (wv >> 16) atomicAdd(hist + 2 * i + 1, (unsigned long long)(wv >> 16));
+        const unsigned sb = 2u * i, bx = sb / (unsigned)kshared, k = sb - bx * (unsigned)kshared;  // k even
+        if (wv & 0xffffu) atomicAdd(hist + bx * 256u + k, (unsigned long long)(wv & 0xffffu));
+        if (wv >> 16) atomicAdd(hist + bx * 256u + k + 1, (unsigned long long)(wv >> 16));
         sh[i] = 0;
       }
     }
     __syncthreads();
   };
-  const long long rows = (long long)Y * Z;
+  const int cpr = X >> 2;
+  const long long ncols = (long long)cpr * Y;
+  const long long groups = (ncols + blockDim.x - 1) / blockDim.x;
   int since = 0;
-  for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
-    const int z = (int)(row / Y), y = (int)(row - (long long)z * Y);
-    const RowWalk<T> w(v, X, Y, Z, row, y, z);
-    for (int x0 = 4 * threadIdx.x; x0 < X; x0 += 4 * blockDim.x) {
-      unsigned long long S[4];
-      int val[4];
-      w.quad(x0, X, S, val);
+  for (long long g = blockIdx.x; g < groups; g += gridDim.x) {
+    const long long col = g * blockDim.x + threadIdx.x;
+    const bool active = col < ncols;
+    const int y = active ? (int)(col / cpr) : 0, x0 = active ? 4 * (int)(col - (long long)y * cpr) : 0;
+    Column<T> cl(v, X, Y, Z, x0, y);  // inactive threads walk column 0 and count nothing
+    for (int z = 0; z < Z; ++z) {
+      if (active) {
+        unsigned long long S[4];
+        cl.diffs(z, S);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        int k = 0;
-        if (smax > 0 && S[j] > 0) {
-          const unsigned long long lhs = 65025ULL * S[j];
-          // FP32 estimate (within one of the exact bin), settled exactly
-          k = (int)(255.f * sqrtf(__fdiv_rn((float)S[j], smax_f)));
-          if (k > 255) k = 255;
-          while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
-          while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;
-          if ((unsigned long long)k * k * smax == lhs) {
-            // exact tie: the f64 formula decides
-            const double g = grad_f64(v, X, Y, Z, x0 + j, y, z, row * X + x0 + j, c);
-            k = (int)floor(__dmul_rn(__ddiv_rn(g, gmax), 255.0));
+        for (int j = 0; j < 4; ++j) {
+          int k = 0;
+          if (smax > 0 && S[j] > 0) {
+            const unsigned long long lhs = 65025ULL * S[j];
+            // FP32 estimate (within one of the exact bin), settled exactly
+            k = (int)(255.f * sqrtf(__fdiv_rn((float)S[j], smax_f)));
             if (k > 255) k = 255;
+            while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
+            while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;
+            if ((unsigned long long)k * k * smax == lhs) {
+              // exact tie: the f64 formula decides
+              const double gg = grad_f64(v, X, Y, Z, x0 + j, y, z, ((long long)z * Y + y) * X + x0 + j, c);
+              k = (int)floor(__dmul_rn(__ddiv_rn(gg, gmax), 255.0));
+              if (k > 255) k = 255;
+            }
+          }
+          int bx = merge32 == 1 ? cl.cur[j] : (int)((unsigned)cl.cur[j] / merge32);
+          if (bx >= nx) bx = nx - 1;
+          const unsigned bin = (unsigned)bx * 256u + (unsigned)k;
+          if (bin == run_bin) {
+            ++run;
+          } else {
+            if (run) add(run_bin, run);
+            run_bin = bin;
+            run = 1;
           }
         }
-        int bx = merge32 == 1 ? val[j] : (int)((unsigned)val[j] / merge32);
-        if (bx >= nx) bx = nx - 1;
-        const unsigned bin = (unsigned)bx * 256u + (unsigned)k;
-        if (bin == run_bin) {
-          ++run;
-        } else {
-          if (run) add(run_bin, run);
-          run_bin = bin;
-          run = 1;
-        }
+        cl.step(z);
       }
-    }
-    if (SMEM && ++since == flush_rows) {
-      flush();
-      since = 0;
+      if (SMEM && ++since == flush_steps) {
+        flush();
+        since = 0;
+      }
     }
   }
   if (SMEM) {
@@ -811,40 +842,42 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       const double c = max_scalar > 0 ? max_scalar : 1.0;
-      const long long cpr = X / 4;
-      int threads = (int)std::min<long long>(512, (cpr + 31) / 32 * 32);
-      if (threads < 128) threads = 128;
-      const long long rows = Y * Z;
-      const int grid = (int)std::min<long long>(rows, (long long)sms * (2048 / threads));
+      const int threads = 256;
+      const long long ncols = (X / 4) * Y;
+      const long long blocks = (ncols + threads - 1) / threads;
+      if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
       cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(Hist2DScratch), s);
       if (e != cudaSuccess) return e;
-      const bool smem = nx * 256 <= 65536 && X <= 65535;
-      const size_t shbytes = smem ? (size_t)nx * 128 * sizeof(unsigned) : 0;
-      const int flush_rows = smem ? (int)std::max<long long>(1, 65535 / X) : 0;
+      // shared counters for the gradient rows k < kshared: 2 bytes per bin, ~48 KB
+      const int kshared = (int)std::min<long long>(256, (49152 / (2 * nx)) & ~1LL);
+      const bool smem = kshared >= 2;
+      const size_t shbytes = smem ? (size_t)nx * kshared * 2 : 0;
+      // a block adds 4 * threads voxels per z-step to its shared counters
+      const int flush_steps = 65535 / (4 * threads);
       const int per_sm = smem ? (int)std::max<size_t>(1, std::min<size_t>(2048 / threads, (227 * 1024) / shbytes)) : 0;
-      const int grid2 = smem ? (int)std::min<long long>(rows, (long long)sms * per_sm) : grid;
+      const int grid2 = smem ? (int)std::min<long long>(blocks, (long long)sms * per_sm) : (int)blocks;
       const int nxi = (int)nx, mi = (int)merge, Xi = (int)X, Yi = (int)Y, Zi = (int)Z;
       if (dtype == DT_U8) {
         const uint8_t* v = (const uint8_t*)vol;
-        k_h2v_max<<<grid, threads, 0, s>>>(v, Xi, Yi, Zi, scratch);
-        k_h2v_gmax<<<grid, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch);
+        k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch);
+        k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch);
         if (smem) {
           e = cudaFuncSetAttribute(k_h2v_bin<uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
           if (e != cudaSuccess) return e;
-          k_h2v_bin<uint8_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_rows);
+          k_h2v_bin<uint8_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps, kshared);
         } else {
-          k_h2v_bin<uint8_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0);
+          k_h2v_bin<uint8_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0, 0);
         }
       } else {
         const uint16_t* v = (const uint16_t*)vol;
-        k_h2v_max<<<grid, threads, 0, s>>>(v, Xi, Yi, Zi, scratch);
-        k_h2v_gmax<<<grid, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch);
+        k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch);
+        k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch);
         if (smem) {
           e = cudaFuncSetAttribute(k_h2v_bin<uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
           if (e != cudaSuccess) return e;
-          k_h2v_bin<uint16_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_rows);
+          k_h2v_bin<uint16_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps, kshared);
         } else {
-          k_h2v_bin<uint16_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0);
+          k_h2v_bin<uint16_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0, 0);
         }
       }
       return cudaGetLastError();

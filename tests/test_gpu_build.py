@@ -150,16 +150,21 @@ def _hist2d_cases(orc):
         "u8_ramp_ties": (((x + y + z) % 200).astype(np.uint8), 0),
         "u16_smem": (blobs((96, 50, 40), np.uint16, 200.0, 200.0), 0),
         "u16_global": (blobs((128, 40, 36), np.uint16, 4095.0, 2600.0), 0),
+        "u8_deep": (blobs((64, 8, 300), np.uint8, 255.0, 255.0), 0),
+        "u16_wide_nosmem": (blobs((64, 20, 10), np.uint16, 16000.0, 16000.0), 0),
     }
 
 
 @pytest.mark.parametrize("case", ["u8_smem", "u8_periodic_flush", "u8_x4", "u8_misaligned", "u8_ramp_ties",
-                                  "u16_smem", "u16_global"])
+                                  "u16_smem", "u16_global", "u8_deep", "u16_wide_nosmem"])
 def test_dev_hist2d_paths_bit_exact(orc, case):
     vol, offset = _hist2d_cases(orc)[case]
     h1, f = orc.hist1d(vol)
+    nx = h1.size
+    if case == "u16_wide_nosmem":
+        nx, f = int(vol.max()) + 1, 1  # 16001 value bins: no gradient row fits in shared memory
     ms = float(vol.max())
-    want, wmg = orc.hist2d(vol, ms, h1.size, f)
-    got, gmg = _dev_hist2d(vol, ms, h1.size, f, offset)
+    want, wmg = orc.hist2d(vol, ms, nx, f)
+    got, gmg = _dev_hist2d(vol, ms, nx, f, offset)
     assert np.array_equal(got, want), case
     assert np.float32(gmg) == np.float32(wmg)

@@ -491,9 +491,11 @@ __device__ __forceinline__ void int_diffs(const T* __restrict__ v, long long X, 
   }
 }
 
-// The f64 formula for one voxel, operation for operation.
+// The f64 formula for one voxel, operation for operation.  Called only for
+// exact ties and the voxels attaining Smax: kept out of line so the common
+// path does not carry its registers.
 template <typename T>
-__device__ double grad_f64(const T* __restrict__ v, long long X, long long Y, long long Z, long long x, long long y,
+__device__ __noinline__ double grad_f64(const T* __restrict__ v, long long X, long long Y, long long Z, long long x, long long y,
                            long long z, long long i, double c) {
   const long long c3[3] = {x, y, z}, n[3] = {X, Y, Z}, st[3] = {1, X, X * Y};
   double g[3];
@@ -627,6 +629,11 @@ __device__ __forceinline__ void ld4(const T* p, int q[4]) {
   q[0] = w.x; q[1] = w.y; q[2] = w.z; q[3] = w.w;
 }
 
+// Squared-difference sums: below 2^20 for 8-bit voxels (32-bit arithmetic),
+// up to 3 (2 x 65535)^2 for 16-bit ones (64-bit).
+template <typename T> struct SumT { using U = unsigned long long; };
+template <> struct SumT<uint8_t> { using U = unsigned; };
+
 template <typename T>
 struct Column {
   const T* base;  // voxel (x0, y, 0)
@@ -647,7 +654,8 @@ struct Column {
     prv[0] = cur[0]; prv[1] = cur[1]; prv[2] = cur[2]; prv[3] = cur[3];
   }
   // S = Dx^2 + Dy^2 + Dz^2 of the 4 voxels at plane z (their values in cur)
-  __device__ __forceinline__ void diffs(int z, unsigned long long S[4]) const {
+  __device__ __forceinline__ void diffs(int z, typename SumT<T>::U S[4]) const {
+    using U = typename SumT<T>::U;
     const T* row = base + z * plane;
     int a[4], b[4];
     ld4(row + ym, a);
@@ -664,8 +672,8 @@ struct Column {
     const int* zp = z == Z - 1 ? cur : nxt;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const long long dy = (long long)my * (b[j] - a[j]), dz = (long long)mz * (zp[j] - zm[j]);
-      S[j] = (unsigned long long)((long long)dx[j] * dx[j] + dy * dy + dz * dz);
+      const int dy = my * (b[j] - a[j]), dz = mz * (zp[j] - zm[j]);
+      S[j] = (U)((U)((long long)dx[j] * dx[j]) + (U)((long long)dy * dy) + (U)((long long)dz * dz));
     }
   }
   // move to plane z + 1
@@ -681,12 +689,13 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DScratch* sc) {
   const int cpr = X >> 2;
   const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long smax = 0;
+  using U = typename SumT<T>::U;
+  U smax = 0;
   if (col < (long long)cpr * Y) {
     const int y = (int)(col / cpr), x0 = 4 * (int)(col - (long long)y * cpr);
     Column<T> c(v, X, Y, Z, x0, y);
     for (int z = 0; z < Z; ++z) {
-      unsigned long long S[4];
+      U S[4];
       c.diffs(z, S);
 #pragma unroll
       for (int j = 0; j < 4; ++j) smax = S[j] > smax ? S[j] : smax;
@@ -694,10 +703,10 @@ __global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X,
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long t = __shfl_xor_sync(0xffffffffu, smax, o);
+    const U t = __shfl_xor_sync(0xffffffffu, smax, o);
     smax = t > smax ? t : smax;
   }
-  if ((threadIdx.x & 31) == 0 && smax) atomicMax(&sc->smax, smax);
+  if ((threadIdx.x & 31) == 0 && smax) atomicMax(&sc->smax, (unsigned long long)smax);
 }
 
 // Pass 1b: the f64 |g| over the voxels attaining Smax.
@@ -712,11 +721,11 @@ __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X
   const int y = (int)(col / cpr), x0 = 4 * (int)(col - (long long)y * cpr);
   Column<T> cl(v, X, Y, Z, x0, y);
   for (int z = 0; z < Z; ++z) {
-    unsigned long long S[4];
+    typename SumT<T>::U S[4];
     cl.diffs(z, S);
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      if (S[j] == smax) {
+      if ((unsigned long long)S[j] == smax) {
         const double g = grad_f64(v, X, Y, Z, x0 + j, y, z, ((long long)z * Y + y) * X + x0 + j, c);
         atomicMax(&sc->gmax_bits, (unsigned long long)__double_as_longlong(g));
       }
@@ -733,7 +742,7 @@ __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X
 // blockDim columns.  Runs of equal bins along a thread's voxels are counted
 // in registers first either way.
 template <typename T, bool SMEM>
-__global__ void __launch_bounds__(256) k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx,
+__global__ void __launch_bounds__(256, 3) k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx,
                                                  int merge, unsigned long long* __restrict__ hist,
                                                  const Hist2DScratch* sc, int flush_steps, int kshared) {
   extern __shared__ unsigned sh[];
@@ -783,13 +792,13 @@ __global__ void __launch_bounds__(256) k_h2v_bin(const T* __restrict__ v, int X,
     Column<T> cl(v, X, Y, Z, x0, y);  // inactive threads walk column 0 and count nothing
     for (int z = 0; z < Z; ++z) {
       if (active) {
-        unsigned long long S[4];
+        typename SumT<T>::U S[4];
         cl.diffs(z, S);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           int k = 0;
           if (smax > 0 && S[j] > 0) {
-            const unsigned long long lhs = 65025ULL * S[j];
+            const unsigned long long lhs = 65025ULL * (unsigned long long)S[j];
             // FP32 estimate (within one of the exact bin), settled exactly
             k = (int)(255.f * sqrtf(__fdiv_rn((float)S[j], smax_f)));
             if (k > 255) k = 255;

@@ -825,7 +825,6 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
   if (!(gm > 0)) gm = 1.f;
   f.grad_scale = (float)((f.tf_h - 1) / ((double)gm * (p.hi - p.lo)));
   f.dt = (float)(1.0 / ((double)p.spv * (double)maxd));
-  f.inv_dt = 1.f / f.dt;
   f.opacity_exp = (float)(1.0 / (double)p.spv);
   f.ert = p.ert;
   f.iso = p.iso;

@@ -67,7 +67,6 @@ struct __align__(16) FrameDesc {
   float idx_scale;           // (tf_w - 1) / (value_hi - value_lo)
   float grad_scale;          // 2D: (tf_h - 1) / (grad_max * (value_hi - value_lo))
   float dt;                  // step, world units
-  float inv_dt;              // 1 / dt (float division, as the device would compute it)
   float opacity_exp;         // dt / dt0 = 1 / samples_per_voxel
   float ert;
   float iso;

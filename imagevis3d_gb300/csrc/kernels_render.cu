@@ -330,64 +330,47 @@ __device__ __forceinline__ bool composite(const FrameDesc& f, float4 c, Accum& a
   return acc.A >= f.ert;
 }
 
-// The march of one ray, as a state machine so a warp can refill lanes whose
-// rays have finished (k_render_persistent) while the per-view kernel runs it
-// to the end in one call: init once, step until done, result.  One step is
-// one iteration of the walk: at most one brick change, one macro-cell
-// decision and one run of samples.
-struct MarchState {
-  Accum acc;
-  float runmax;  // MIP: largest sample so far
-  int k, K;      // next sample, end of the ray's samples
-  int bi, bke;   // current brick and the end of the ray's run in it
-  bool done;
-  BrickView b;
-};
-
-__device__ __forceinline__ void pos_of(const FrameDesc& f, const RaySetup& r, int kk, float& px, float& py, float& pz) {
-  const float t = fmaf((float)kk + 0.5f, f.dt, r.t0);
-  px = fmaf(t, r.dv[0], r.ov[0]);
-  py = fmaf(t, r.dv[1], r.ov[1]);
-  pz = fmaf(t, r.dv[2], r.ov[2]);
-}
-
-// First sample index >= k0 + 1 whose cell leaves the box [lo, hi) (per axis,
-// on clamped floor coordinates), or K: estimated from the box's exit planes,
-// then settled by the same floor(pos) rule that assigns samples to bricks and
-// cells.  Positions are monotone in k, so members form one run and only its
-// ends need checking.
-__device__ __forceinline__ int run_end(const FrameDesc& f, const RaySetup& r, int K, int k0, int lx, int ly, int lz,
-                                       int hx, int hy, int hz) {
-  float te = INFINITY;
-  te = fminf(te, r.dv[0] > 0.f ? ((float)hx - r.ov[0]) * r.inv[0]
-                               : (r.dv[0] < 0.f ? ((float)lx - r.ov[0]) * r.inv[0] : INFINITY));
-  te = fminf(te, r.dv[1] > 0.f ? ((float)hy - r.ov[1]) * r.inv[1]
-                               : (r.dv[1] < 0.f ? ((float)ly - r.ov[1]) * r.inv[1] : INFINITY));
-  te = fminf(te, r.dv[2] > 0.f ? ((float)hz - r.ov[2]) * r.inv[2]
-                               : (r.dv[2] < 0.f ? ((float)lz - r.ov[2]) * r.inv[2] : INFINITY));
-  const float kef = ceilf((te - r.t0) * f.inv_dt - 0.5f);
-  int ke = kef >= (float)K ? K : max(k0 + 1, (int)kef);
-  auto in_box = [&](int kk) {
-    float qx, qy, qz;
-    pos_of(f, r, kk, qx, qy, qz);
-    const int cx = clamp_cell(qx, f.dims[0]), cy = clamp_cell(qy, f.dims[1]), cz = clamp_cell(qz, f.dims[2]);
-    return cx >= lx && cx < hx && cy >= ly && cy < hy && cz >= lz && cz < hz;
-  };
-  while (ke > k0 + 1 && !in_box(ke - 1)) --ke;
-  while (ke < K && in_box(ke)) ++ke;
-  return ke;
-}
-
-__device__ __forceinline__ void march_init(const FrameDesc& f, const RaySetup& r, MarchState& s) {
-  s.acc = {0.f, 0.f, 0.f, 0.f};
-  s.runmax = -INFINITY;
-  s.k = 0;
-  s.K = 0;
-  s.bi = -1;
-  s.bke = 0;
+template <typename T, int MODE, int SAMPLER>
+__device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) {
+  Accum acc = {0.f, 0.f, 0.f, 0.f};
+  float runmax = -INFINITY;  // MIP: largest sample so far
   if (r.hit) {
-    const float dt = f.dt, t0 = r.t0;
+    const float dt = f.dt;
+    const float t0 = r.t0;
     int K = max(0, (int)ceilf((r.t1 - t0) / dt - 0.5f));
+    const float V[3] = {-r.dw[0], -r.dw[1], -r.dw[2]};
+    const float inv_dt = 1.f / dt;
+    auto pos_of = [&](int kk, float& px, float& py, float& pz) {
+      const float t = fmaf((float)kk + 0.5f, dt, t0);
+      px = fmaf(t, r.dv[0], r.ov[0]);
+      py = fmaf(t, r.dv[1], r.ov[1]);
+      pz = fmaf(t, r.dv[2], r.ov[2]);
+    };
+    // First sample index >= k + 1 whose cell leaves the box [lo, hi) (per
+    // axis, on clamped floor coordinates), or K: estimated from the box's
+    // exit planes, then settled by the same floor(pos) rule that assigns
+    // samples to bricks and cells.  Positions are monotone in k, so members
+    // form one run and only its ends need checking.
+    auto run_end = [&](int k0, int lx, int ly, int lz, int hx, int hy, int hz) -> int {
+      float te = INFINITY;
+      te = fminf(te, r.dv[0] > 0.f ? ((float)hx - r.ov[0]) * r.inv[0]
+                                   : (r.dv[0] < 0.f ? ((float)lx - r.ov[0]) * r.inv[0] : INFINITY));
+      te = fminf(te, r.dv[1] > 0.f ? ((float)hy - r.ov[1]) * r.inv[1]
+                                   : (r.dv[1] < 0.f ? ((float)ly - r.ov[1]) * r.inv[1] : INFINITY));
+      te = fminf(te, r.dv[2] > 0.f ? ((float)hz - r.ov[2]) * r.inv[2]
+                                   : (r.dv[2] < 0.f ? ((float)lz - r.ov[2]) * r.inv[2] : INFINITY));
+      const float kef = ceilf((te - t0) * inv_dt - 0.5f);
+      int ke = kef >= (float)K ? K : max(k0 + 1, (int)kef);
+      auto in_box = [&](int kk) {
+        float qx, qy, qz;
+        pos_of(kk, qx, qy, qz);
+        const int cx = clamp_cell(qx, f.dims[0]), cy = clamp_cell(qy, f.dims[1]), cz = clamp_cell(qz, f.dims[2]);
+        return cx >= lx && cx < hx && cy >= ly && cy < hy && cz >= lz && cz < hz;
+      };
+      while (ke > k0 + 1 && !in_box(ke - 1)) --ke;
+      while (ke < K && in_box(ke)) ++ke;
+      return ke;
+    };
     int k = 0;
     if (f.clip_on) {
       // Clip plane: keep the samples with n . p + d <= 0.  Along the ray
@@ -403,13 +386,13 @@ __device__ __forceinline__ void march_init(const FrameDesc& f, const RaySetup& r
       }
       auto keep = [&](int kk) { return fmaf(s1, fmaf((float)kk + 0.5f, dt, t0), s0) <= 0.f; };
       if (s1 > 0.f) {
-        const float kf = floorf((-s0 / s1 - t0) * f.inv_dt - 0.5f);
+        const float kf = floorf((-s0 / s1 - t0) * inv_dt - 0.5f);
         int e = kf < 0.f ? 0 : (kf >= (float)K ? K : (int)kf + 1);
         while (e > 0 && !keep(e - 1)) --e;
         while (e < K && keep(e)) ++e;
         K = e;
       } else if (s1 < 0.f) {
-        const float kf = ceilf((-s0 / s1 - t0) * f.inv_dt - 0.5f);
+        const float kf = ceilf((-s0 / s1 - t0) * inv_dt - 0.5f);
         int e = kf <= 0.f ? 0 : (kf >= (float)K ? K : (int)kf);
         while (e < K && !keep(e)) ++e;
         while (e > 0 && keep(e - 1)) --e;
@@ -418,167 +401,151 @@ __device__ __forceinline__ void march_init(const FrameDesc& f, const RaySetup& r
         K = 0;
       }
     }
-    s.k = k;
-    s.K = K;
-  }
-  s.done = s.k >= s.K;
-}
-
-template <typename T, int MODE, int SAMPLER>
-__device__ __forceinline__ void march_step(const FrameDesc& f, const RaySetup& r, MarchState& s, unsigned& nsamp) {
-  const float dt = f.dt, t0 = r.t0;
-  const int K = s.K;
-  int k = s.k;
-  float px, py, pz;
-  pos_of(f, r, k, px, py, pz);
-  const int gx = clamp_cell(px, f.dims[0]), gy = clamp_cell(py, f.dims[1]), gz = clamp_cell(pz, f.dims[2]);
-  if (s.bi < 0 || k >= s.bke) {
-    s.bi = brick_index(f, gx, gy, gz);
-    load_brick(f, s.bi, s.b);
-    s.bke = run_end(f, r, K, k, s.b.lox, s.b.loy, s.b.loz, s.b.hix, s.b.hiy, s.b.hiz);
-    bool skip_b = f.empty_skip >= 1 && __ldg(f.skip + s.bi);
-    // MIP: a brick whose largest voxel cannot raise the maximum is skipped
-    if constexpr (MODE == MODE_MIP) skip_b = skip_b || (f.empty_skip >= 1 && __ldg(&f.bricks[s.bi].vmax) <= s.runmax);
-    if (skip_b) {
-      s.k = s.bke;
-      s.bi = -1;
-      s.done = s.k >= K;
-      return;
-    }
-    if (f.touched) f.touched[s.bi] = 1;
-  }
-  const BrickView& b = s.b;
-  int ke = s.bke;
-  if (f.empty_skip >= 2) {
-    // Macro-cells: occ holds, per cell, the Chebyshev distance (in cells,
-    // capped) to the nearest cell that may contribute; 0 = this cell may
-    // contribute.  From an empty cell at distance d the ray may leave the
-    // whole cube of 2d-1 cells around it without sampling.  Runs are
-    // estimated from exit planes only: a sample that rounding places across
-    // a face lies within a voxel of it, and every cell's min/max covers one
-    // voxel beyond its samples' footprints, so no contributing sample is ever
-    // skipped; sampling past a face is harmless.
+    bool done = false;
+    BrickView b;
+    int bi = -1, bke = 0;  // current brick and the end of the ray's run in it
     const int sh = f.cell_shift;
-    const int cx = max(gx, 0) >> sh, cy = max(gy, 0) >> sh, cz = max(gz, 0) >> sh;
-    const size_t ci = ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx;
-    int d;
-    if constexpr (MODE == MODE_MIP) d = __ldg(&f.cells[ci].y) <= s.runmax ? 1 : 0;  // one cell at a time
-    else d = __ldg(f.occ + ci);
-    const int lo_c = d > 0 ? d - 1 : 0;  // cube = cells [c - lo_c, c + lo_c]
-    const float lx = (float)(max(cx - lo_c, 0) << sh), hx = (float)min((cx + lo_c + 1) << sh, f.dims[0]);
-    const float ly = (float)(max(cy - lo_c, 0) << sh), hy = (float)min((cy + lo_c + 1) << sh, f.dims[1]);
-    const float lz = (float)(max(cz - lo_c, 0) << sh), hz = (float)min((cz + lo_c + 1) << sh, f.dims[2]);
-    float te = fminf(fminf(r.dv[0] > 0.f ? (hx - r.ov[0]) * r.inv[0] : (r.dv[0] < 0.f ? (lx - r.ov[0]) * r.inv[0] : INFINITY),
-                           r.dv[1] > 0.f ? (hy - r.ov[1]) * r.inv[1] : (r.dv[1] < 0.f ? (ly - r.ov[1]) * r.inv[1] : INFINITY)),
-                     r.dv[2] > 0.f ? (hz - r.ov[2]) * r.inv[2] : (r.dv[2] < 0.f ? (lz - r.ov[2]) * r.inv[2] : INFINITY));
-    const float kef = ceilf((te - t0) * f.inv_dt - 0.5f);
-    if (d > 0) {
-      s.k = kef >= (float)K ? K : max(k + 1, (int)kef);
-      if (s.k >= s.bke) s.bi = -1;
-      s.done = s.k >= K;
-      return;
-    }
-    ke = kef >= (float)ke ? ke : max(k + 1, (int)kef);
-    if (f.cell_touched) {
-      // algorithmic-bytes accounting: one bit per sampled cell
-      unsigned* w = f.cell_touched + (ci >> 5);
-      const unsigned bit = 1u << (ci & 31);
-      if (!(*(volatile unsigned*)w & bit)) atomicOr(w, bit);
-    }
-  }
-  bool done = false;
-  if constexpr (MODE == MODE_MIP) {
-    for (; k < ke; ++k) {
-      float ax, ay, az;
-      pos_of(f, r, k, ax, ay, az);
-      const Cell ca = make_cell(f, ax, ay, az);
-      ++nsamp;
-      s.runmax = fmaxf(s.runmax, sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz));
-    }
-    if (s.runmax >= f.level_max) done = true;
-  } else if constexpr (MODE == MODE_1D) {
-    for (; k < ke; ++k) {
-      float ax, ay, az;
-      pos_of(f, r, k, ax, ay, az);
-      const Cell ca = make_cell(f, ax, ay, az);
-      ++nsamp;
-      if (composite<MODE>(f, tf1d(f, sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz)), s.acc)) {
-        done = true;
-        break;
-      }
-    }
-  } else {
-    const float V[3] = {-r.dw[0], -r.dw[1], -r.dw[2]};
-    for (; k < ke; ++k) {
-      pos_of(f, r, k, px, py, pz);
-      const Cell c = make_cell(f, px, py, pz);
-      const float v = sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z, c.fx, c.fy, c.fz);
-      ++nsamp;
-      if (MODE == MODE_ISO) {
-        if (v >= f.iso) {
-          float tl = k == 0 ? t0 : fmaf((float)k - 0.5f, dt, t0), th = fmaf((float)k + 0.5f, dt, t0);
-#pragma unroll 1
-          for (int it = 0; it < 4; ++it) {
-            float tm = 0.5f * (tl + th);
-            const Cell mc = make_cell(f, fmaf(tm, r.dv[0], r.ov[0]), fmaf(tm, r.dv[1], r.ov[1]),
-                                      fmaf(tm, r.dv[2], r.ov[2]));
-            // within one voxel of this brick's interior its ghosts hold the
-            // neighbours' voxels, so the current brick answers (same values;
-            // an out-of-core neighbour need not be resident)
-            float vm;
-            if (mc.x >= b.lox - 1 && mc.x <= b.hix && mc.y >= b.loy - 1 && mc.y <= b.hiy && mc.z >= b.loz - 1 &&
-                mc.z <= b.hiz)
-              vm = sample_cell<T, SAMPLER>(f, b, mc.x, mc.y, mc.z, mc.fx, mc.fy, mc.fz);
-            else
-              vm = sample_anywhere<T, SAMPLER>(f, fmaf(tm, r.dv[0], r.ov[0]), fmaf(tm, r.dv[1], r.ov[1]),
-                                               fmaf(tm, r.dv[2], r.ov[2]));
-            if (vm >= f.iso) th = tm;
-            else tl = tm;
-          }
-          float th2 = 0.5f * (tl + th);
-          const Cell hc = make_cell(f, fmaf(th2, r.dv[0], r.ov[0]), fmaf(th2, r.dv[1], r.ov[1]),
-                                    fmaf(th2, r.dv[2], r.ov[2]));
-          BrickView hb;
-          load_brick(f, brick_index(f, hc.x, hc.y, hc.z), hb);
-          float g[3], col[3];
-          gradient<T, SAMPLER>(f, hb, hc, g);
-          g[0] *= f.vox_scale[0];
-          g[1] *= f.vox_scale[1];
-          g[2] *= f.vox_scale[2];
-          if (f.lighting) shade(f, g, V, f.iso_rgb, col);
-          else { col[0] = f.iso_rgb[0]; col[1] = f.iso_rgb[1]; col[2] = f.iso_rgb[2]; }
-          s.acc.C0 = col[0]; s.acc.C1 = col[1]; s.acc.C2 = col[2];
-          s.acc.A = 1.f;
-          done = true;
-          break;
+    while (k < K && !done) {
+      float px, py, pz;
+      pos_of(k, px, py, pz);
+      const int gx = clamp_cell(px, f.dims[0]), gy = clamp_cell(py, f.dims[1]), gz = clamp_cell(pz, f.dims[2]);
+      if (bi < 0 || k >= bke) {
+        bi = brick_index(f, gx, gy, gz);
+        load_brick(f, bi, b);
+        bke = run_end(k, b.lox, b.loy, b.loz, b.hix, b.hiy, b.hiz);
+        bool skip_b = f.empty_skip >= 1 && __ldg(f.skip + bi);
+        // MIP: a brick whose largest voxel cannot raise the maximum is skipped
+        if constexpr (MODE == MODE_MIP) skip_b = skip_b || (f.empty_skip >= 1 && __ldg(&f.bricks[bi].vmax) <= runmax);
+        if (skip_b) {
+          k = bke;
+          bi = -1;
+          continue;
         }
-        continue;
+        if (f.touched) f.touched[bi] = 1;
       }
-      // 2D transfer function over (value, |gradient|), Phong lit
-      float g[3];
-      gradient<T, SAMPLER>(f, b, c, g);
-      const float gm = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-      float4 cl = tf2d(f, v, gm);
-      if (f.lighting && cl.w > 0.f) {
-        float gw[3] = {g[0] * f.vox_scale[0], g[1] * f.vox_scale[1], g[2] * f.vox_scale[2]};
-        float col[3] = {cl.x, cl.y, cl.z}, lit[3];
-        shade(f, gw, V, col, lit);
-        cl.x = lit[0]; cl.y = lit[1]; cl.z = lit[2];
+      int ke = bke;
+      if (f.empty_skip >= 2) {
+        // Macro-cells: occ holds, per cell, the Chebyshev distance (in
+        // cells, capped) to the nearest cell that may contribute; 0 = this
+        // cell may contribute.  From an empty cell at distance d the ray may
+        // leave the whole cube of 2d-1 cells around it without sampling.
+        // Runs are estimated from exit planes only: a sample that rounding
+        // places across a face lies within a voxel of it, and every cell's
+        // min/max covers one voxel beyond its samples' footprints, so no
+        // contributing sample is ever skipped; sampling past a face is
+        // harmless.
+        const int cx = max(gx, 0) >> sh, cy = max(gy, 0) >> sh, cz = max(gz, 0) >> sh;
+        const size_t ci = ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx;
+        int d;
+        if constexpr (MODE == MODE_MIP) d = __ldg(&f.cells[ci].y) <= runmax ? 1 : 0;  // one cell at a time
+        else d = __ldg(f.occ + ci);
+        const int lo_c = d > 0 ? d - 1 : 0;  // cube = cells [c - lo_c, c + lo_c]
+        const float lx = (float)(max(cx - lo_c, 0) << sh), hx = (float)min((cx + lo_c + 1) << sh, f.dims[0]);
+        const float ly = (float)(max(cy - lo_c, 0) << sh), hy = (float)min((cy + lo_c + 1) << sh, f.dims[1]);
+        const float lz = (float)(max(cz - lo_c, 0) << sh), hz = (float)min((cz + lo_c + 1) << sh, f.dims[2]);
+        float te = fminf(fminf(r.dv[0] > 0.f ? (hx - r.ov[0]) * r.inv[0] : (r.dv[0] < 0.f ? (lx - r.ov[0]) * r.inv[0] : INFINITY),
+                               r.dv[1] > 0.f ? (hy - r.ov[1]) * r.inv[1] : (r.dv[1] < 0.f ? (ly - r.ov[1]) * r.inv[1] : INFINITY)),
+                         r.dv[2] > 0.f ? (hz - r.ov[2]) * r.inv[2] : (r.dv[2] < 0.f ? (lz - r.ov[2]) * r.inv[2] : INFINITY));
+        const float kef = ceilf((te - t0) * inv_dt - 0.5f);
+        if (d > 0) {
+          k = kef >= (float)K ? K : max(k + 1, (int)kef);
+          if (k >= bke) bi = -1;
+          continue;
+        }
+        ke = kef >= (float)ke ? ke : max(k + 1, (int)kef);
+        if (f.cell_touched) {
+          // algorithmic-bytes accounting: one bit per sampled cell
+          unsigned* w = f.cell_touched + (ci >> 5);
+          const unsigned bit = 1u << (ci & 31);
+          if (!(*(volatile unsigned*)w & bit)) atomicOr(w, bit);
+        }
       }
-      if (composite<MODE>(f, cl, s.acc)) { done = true; break; }
+      if constexpr (MODE == MODE_MIP) {
+        for (; k < ke; ++k) {
+          float ax, ay, az;
+          pos_of(k, ax, ay, az);
+          const Cell ca = make_cell(f, ax, ay, az);
+          ++nsamp;
+          runmax = fmaxf(runmax, sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz));
+        }
+        if (runmax >= f.level_max) done = true;
+      } else if constexpr (MODE == MODE_1D) {
+        for (; k < ke; ++k) {
+          float ax, ay, az;
+          pos_of(k, ax, ay, az);
+          const Cell ca = make_cell(f, ax, ay, az);
+          ++nsamp;
+          if (composite<MODE>(f, tf1d(f, sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz)), acc)) {
+            done = true;
+            break;
+          }
+        }
+      } else {
+      for (; k < ke; ++k) {
+        pos_of(k, px, py, pz);
+        const Cell c = make_cell(f, px, py, pz);
+        const float v = sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z, c.fx, c.fy, c.fz);
+        ++nsamp;
+        if (MODE == MODE_ISO) {
+          if (v >= f.iso) {
+            float tl = k == 0 ? t0 : fmaf((float)k - 0.5f, dt, t0), th = fmaf((float)k + 0.5f, dt, t0);
+#pragma unroll 1
+            for (int it = 0; it < 4; ++it) {
+              float tm = 0.5f * (tl + th);
+              const Cell mc = make_cell(f, fmaf(tm, r.dv[0], r.ov[0]), fmaf(tm, r.dv[1], r.ov[1]),
+                                        fmaf(tm, r.dv[2], r.ov[2]));
+              // within one voxel of this brick's interior its ghosts hold the
+              // neighbours' voxels, so the current brick answers (same values;
+              // an out-of-core neighbour need not be resident)
+              float vm;
+              if (mc.x >= b.lox - 1 && mc.x <= b.hix && mc.y >= b.loy - 1 && mc.y <= b.hiy && mc.z >= b.loz - 1 &&
+                  mc.z <= b.hiz)
+                vm = sample_cell<T, SAMPLER>(f, b, mc.x, mc.y, mc.z, mc.fx, mc.fy, mc.fz);
+              else
+                vm = sample_anywhere<T, SAMPLER>(f, fmaf(tm, r.dv[0], r.ov[0]), fmaf(tm, r.dv[1], r.ov[1]),
+                                                 fmaf(tm, r.dv[2], r.ov[2]));
+              if (vm >= f.iso) th = tm;
+              else tl = tm;
+            }
+            float th2 = 0.5f * (tl + th);
+            const Cell hc = make_cell(f, fmaf(th2, r.dv[0], r.ov[0]), fmaf(th2, r.dv[1], r.ov[1]),
+                                      fmaf(th2, r.dv[2], r.ov[2]));
+            BrickView hb;
+            load_brick(f, brick_index(f, hc.x, hc.y, hc.z), hb);
+            float g[3], col[3];
+            gradient<T, SAMPLER>(f, hb, hc, g);
+            g[0] *= f.vox_scale[0];
+            g[1] *= f.vox_scale[1];
+            g[2] *= f.vox_scale[2];
+            if (f.lighting) shade(f, g, V, f.iso_rgb, col);
+            else { col[0] = f.iso_rgb[0]; col[1] = f.iso_rgb[1]; col[2] = f.iso_rgb[2]; }
+            acc.C0 = col[0]; acc.C1 = col[1]; acc.C2 = col[2];
+            acc.A = 1.f;
+            done = true;
+            break;
+          }
+          continue;
+        }
+        // 2D transfer function over (value, |gradient|), Phong lit
+        float g[3];
+        gradient<T, SAMPLER>(f, b, c, g);
+        const float gm = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        float4 cl = tf2d(f, v, gm);
+        if (f.lighting && cl.w > 0.f) {
+          float gw[3] = {g[0] * f.vox_scale[0], g[1] * f.vox_scale[1], g[2] * f.vox_scale[2]};
+          float col[3] = {cl.x, cl.y, cl.z}, lit[3];
+          shade(f, gw, V, col, lit);
+          cl.x = lit[0]; cl.y = lit[1]; cl.z = lit[2];
+        }
+        if (composite<MODE>(f, cl, acc)) { done = true; break; }
+      }
+      }
     }
   }
-  s.k = k;
-  s.done = done || k >= K;
-}
-
-template <int MODE>
-__device__ __forceinline__ float4 march_result(const FrameDesc& f, const MarchState& s) {
-  Accum acc = s.acc;
   if constexpr (MODE == MODE_MIP) {
     // the maximum through the 1D TF, composited once (no opacity correction)
-    if (s.runmax > -INFINITY) {
-      const float4 c = tf1d(f, s.runmax);
+    if (runmax > -INFINITY) {
+      const float4 c = tf1d(f, runmax);
       acc.C0 = c.x * c.w;
       acc.C1 = c.y * c.w;
       acc.C2 = c.z * c.w;
@@ -587,14 +554,6 @@ __device__ __forceinline__ float4 march_result(const FrameDesc& f, const MarchSt
   }
   const float rem = 1.f - acc.A;
   return make_float4(fmaf(rem, f.bg[0], acc.C0), fmaf(rem, f.bg[1], acc.C1), fmaf(rem, f.bg[2], acc.C2), acc.A);
-}
-
-template <typename T, int MODE, int SAMPLER>
-__device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) {
-  MarchState s;
-  march_init(f, r, s);
-  while (!s.done) march_step<T, MODE, SAMPLER>(f, r, s, nsamp);
-  return march_result<MODE>(f, s);
 }
 
 template <typename T, int MODE, int SAMPLER>
@@ -623,9 +582,6 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
 }
 
 constexpr int RENDER_THREADS = 128;
-// Frames whose sample counters a persistent block keeps in shared memory
-// (8 B each); later frames count straight into global memory.
-constexpr int kPersistentSmemFrames = 1024;
 
 template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_plain(const __grid_constant__ FrameDesc f) {
@@ -645,98 +601,19 @@ __device__ __forceinline__ int find_frame(const int* __restrict__ prefix, int nf
   return lo;
 }
 
-// Persistent batched raycast.  Work items are (view, ray tile) pairs taken
-// from one atomic counter; a warp keeps the current item as a pool of rays
-// and hands them to lanes one by one: a lane whose ray has finished takes the
-// next ray at once (lane refill), so lanes do not idle until the slowest ray
-// of a tile ends.  Rays of different views may share a warp.  Sample counts
-// gather per lane and per frame, then in shared per-frame counters (the
-// first `smem_frames` frames) and finally in the frames' counters.
 template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
                                                          const int* __restrict__ tile_prefix, int total,
-                                                         int* __restrict__ counter, int smem_frames) {
-  extern __shared__ unsigned long long block_samples[];
-  for (int i = threadIdx.x; i < smem_frames; i += blockDim.x) block_samples[i] = 0;
-  __syncthreads();
-  const unsigned FULL = 0xffffffffu;
+                                                         int* __restrict__ counter) {
   const int lane = threadIdx.x & 31;
-  int pool_fi = 0, pool_tile = 0, pool_next = 32;  // warp-uniform: current item, its next unassigned ray
-  bool exhausted = false, have = false;
-  int fi = 0, px = 0, py = 0;
-  RaySetup r;
-  MarchState st;
-  unsigned nsamp = 0;
-  int acc_fi = -1;
-  unsigned long long acc_n = 0;
-  auto flush = [&]() {
-    if (acc_fi >= 0 && acc_n) {
-      if (acc_fi < smem_frames) atomicAdd(block_samples + acc_fi, acc_n);
-      else if (frames[acc_fi].samples) atomicAdd(frames[acc_fi].samples, acc_n);
-    }
-    acc_n = 0;
-  };
   for (;;) {
-    unsigned need = __ballot_sync(FULL, !have);
-    while (need && !exhausted) {
-      if (pool_next == 32) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(counter, 1);
-        item = __shfl_sync(FULL, item, 0);
-        if (item >= total) {
-          exhausted = true;
-          break;
-        }
-        pool_fi = find_frame(tile_prefix, nframes, item);
-        pool_tile = item - __ldg(tile_prefix + pool_fi);
-        pool_next = 0;
-      }
-      const int rank = __popc(need & ((1u << lane) - 1u));
-      const int avail = 32 - pool_next;
-      if (((need >> lane) & 1u) && rank < avail) {
-        const FrameDesc& f = frames[pool_fi];
-        const int slot = pool_next + rank;
-        const int tx = pool_tile % f.tiles_x, ty = pool_tile / f.tiles_x;
-        const int qx = tx * f.tile_w + (slot & (f.tile_w - 1)), qy = ty * (32 / f.tile_w) + slot / f.tile_w;
-        if (qx < f.width && qy < f.height) {
-          fi = pool_fi;
-          px = qx;
-          py = qy;
-          setup_ray(f, px, py, r);
-          march_init(f, r, st);
-          have = true;
-        }
-      }
-      pool_next += min(__popc(need), avail);
-      need = __ballot_sync(FULL, !have);
-    }
-    if (!__any_sync(FULL, have)) break;
-    if (have) {
-      const FrameDesc& f = frames[fi];
-      if (!st.done) march_step<T, MODE, SAMPLER>(f, r, st, nsamp);
-      if (st.done) {
-        const float4 c = march_result<MODE>(f, st);
-        const size_t o = (size_t)py * f.width + px;
-        if (f.out_f32) f.out_f32[o] = c;
-        if (f.out_rgba8)
-          f.out_rgba8[o] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
-                                       (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
-                                       (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f),
-                                       (unsigned char)__float2uint_rn(__saturatef(c.w) * 255.f));
-        if (fi != acc_fi) {
-          flush();
-          acc_fi = fi;
-        }
-        acc_n += nsamp;
-        nsamp = 0;
-        have = false;
-      }
-    }
+    int item = 0;
+    if (lane == 0) item = atomicAdd(counter, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= total) return;
+    int fi = find_frame(tile_prefix, nframes, item);
+    render_tile<T, MODE, SAMPLER>(frames[fi], item - __ldg(tile_prefix + fi));
   }
-  flush();
-  __syncthreads();
-  for (int i = threadIdx.x; i < smem_frames; i += blockDim.x)
-    if (block_samples[i] && frames[i].samples) atomicAdd(frames[i].samples, block_samples[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -970,9 +847,7 @@ template <typename T, int MODE, int SAMPLER>
 static cudaError_t persistent_t(const FrameDesc* frames, int nframes, const int* prefix, int total, int* counter,
                                 int grid, cudaStream_t s) {
   (void)cudaGetLastError();
-  const int smem_frames = nframes < kPersistentSmemFrames ? nframes : kPersistentSmemFrames;
-  k_render_persistent<T, MODE, SAMPLER><<<grid, RENDER_THREADS, sizeof(unsigned long long) * smem_frames, s>>>(
-      frames, nframes, prefix, total, counter, smem_frames);
+  k_render_persistent<T, MODE, SAMPLER><<<grid, RENDER_THREADS, 0, s>>>(frames, nframes, prefix, total, counter);
   return cudaGetLastError();
 }
 
@@ -1024,7 +899,7 @@ int persistent_grid_size(int device) {
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent<uint16_t, MODE_1D, SAMPLER_SW>,
-                                                RENDER_THREADS, 64 * sizeof(unsigned long long));
+                                                RENDER_THREADS, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }

@@ -936,7 +936,7 @@ struct gbvr_renderer {
   int last_views = 0, last_level = 0;
   float last_ms = 0.f, last_kernel_ms = 0.f;
   uint64_t last_h2d = 0;
-  int max_ctas_per_sm = 0, sm_count = 0;
+  int max_ctas_per_sm = 0, max_ctas_per_sm_u = 0, sm_count = 0;
   // graph cache for the batch launch
   struct GraphKey {
     int n, w, h, level, dtype, mode, sampler, grid;
@@ -947,10 +947,15 @@ struct gbvr_renderer {
              std::tie(o.n, o.w, o.h, o.level, o.dtype, o.mode, o.sampler, o.grid, o.fb8, o.fb32);
     }
   };
-  std::map<GraphKey, cudaGraphExec_t> graphs;
+  struct CachedGraph {
+    cudaGraphExec_t exec;
+    bool uniform;
+    FrameDesc shared;  // the batch-uniform kernel parameter baked into the graph
+  };
+  std::map<GraphKey, CachedGraph> graphs;
 
   void drop_graphs() {
-    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
     graphs.clear();
   }
   ~gbvr_renderer() {
@@ -1410,13 +1415,35 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
-    r->max_ctas_per_sm = persistent_grid_size(dev) / std::max(r->sm_count, 1);
-    if (r->max_ctas_per_sm < 1) r->max_ctas_per_sm = 1;
+    r->max_ctas_per_sm = std::max(1, persistent_grid_size(dev) / std::max(r->sm_count, 1));
+    r->max_ctas_per_sm_u = std::max(1, persistent_grid_size_uniform(dev) / std::max(r->sm_count, 1));
   }
-  const int per_sm = r->ctas_per_sm > 0 ? std::min(r->ctas_per_sm, r->max_ctas_per_sm) : r->max_ctas_per_sm;
+  // Views of one renderer batch share everything but camera, outputs and
+  // counters, unless they sample different brick layout copies: then the
+  // shared part goes to the kernel as a parameter.
+  bool uniform = true;
+  for (int v = 1; v < n; ++v)
+    if (hf[v].perm != hf[0].perm || hf[v].copy_off != hf[0].copy_off) uniform = false;
+  FrameDesc shared = hf[0];
+  if (uniform) {
+    memset(shared.inv_vp, 0, sizeof(shared.inv_vp));
+    shared.out_rgba8 = nullptr;
+    shared.out_f32 = nullptr;
+    shared.samples = nullptr;
+    shared.touched_stride = shared.touched ? r->ds.levels[level].nbricks : 0;
+    shared.cell_touched_stride = shared.cell_touched ? r->cell_words : 0;
+  }
+  const int max_per_sm = uniform ? r->max_ctas_per_sm_u : r->max_ctas_per_sm;
+  const int per_sm = r->ctas_per_sm > 0 ? std::min(r->ctas_per_sm, max_per_sm) : max_per_sm;
   const int grid = r->sm_count * per_sm;
   gbvr_renderer::GraphKey key{n, r->width, r->height, level, r->ds.dtype, r->mode, r->sampler, grid, r->d_fb8.p, r->d_fb32.p};
   auto it = r->graphs.find(key);
+  if (it != r->graphs.end() &&
+      (it->second.uniform != uniform || (uniform && memcmp(&it->second.shared, &shared, sizeof(FrameDesc)) != 0))) {
+    cudaGraphExecDestroy(it->second.exec);  // the baked-in parameter changed
+    r->graphs.erase(it);
+    it = r->graphs.end();
+  }
   if (it == r->graphs.end()) {
     // The graph holds the persistent launch; descriptor uploads and counter
     // resets are plain stream operations before it, so the kernel-only
@@ -1424,9 +1451,13 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     cudaGraph_t g;
     (void)cudaGetLastError();
     CUDA_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t le = launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), n,
-                                                    r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid,
-                                                    r->stream);
+    cudaError_t le =
+        uniform ? launch_render_persistent_uniform(r->ds.dtype, r->mode, r->sampler, shared, r->d_frames.as<FrameDesc>(),
+                                                   n, r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid,
+                                                   r->stream)
+                : launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), n,
+                                                 r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid,
+                                                 r->stream);
     cudaError_t ce = cudaStreamEndCapture(r->stream, &g);
     if (le != cudaSuccess) return cuda_fail(le, "persistent launch capture");
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
@@ -1434,7 +1465,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
-    it = r->graphs.emplace(key, ge).first;
+    it = r->graphs.emplace(key, gbvr_renderer::CachedGraph{ge, uniform, shared}).first;
   }
   CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
   CUDA_TRY(cudaMemcpyAsync(r->d_frames.p, r->h_frames.p, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, r->stream));
@@ -1444,7 +1475,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
   if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words * n, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
-  CUDA_TRY(cudaGraphLaunch(it->second, r->stream));
+  CUDA_TRY(cudaGraphLaunch(it->second.exec, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
   r->last_h2d = sizeof(FrameDesc) * n + sizeof(int) * (n + 1);

@@ -98,6 +98,9 @@ struct __align__(16) FrameDesc {
   unsigned long long* samples;  // per-frame sample counter
   unsigned char* touched;    // per-frame flag per brick of the rendered level
   unsigned* cell_touched;    // per-frame bitmap of sampled non-empty macro-cells (or null)
+  // batch-uniform descriptors only: view v's flags start at touched +
+  // v * touched_stride (cell_touched likewise); 0 in per-view descriptors
+  long long touched_stride, cell_touched_stride;
 };
 
 // A 2D slice view: screen pixels map to the plane through the slice (or to
@@ -136,6 +139,13 @@ cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, con
                                            int nframes, const int* tile_prefix, int total_tiles,
                                            int* counter, int grid, cudaStream_t s);
 int persistent_grid_size(int device);
+// Batches whose views share everything but camera, outputs and counters: the
+// shared part travels as a kernel parameter (constant bank), each view's part
+// is read from `frames` (camera, image size, outputs, sample counter).
+cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, const FrameDesc& shared,
+                                             const FrameDesc* frames, int nframes, const int* prefix, int total,
+                                             int* counter, int grid, cudaStream_t s);
+int persistent_grid_size_uniform(int device);
 cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStream_t s);
 
 // ---- launch wrappers (kernels_build.cu) ----

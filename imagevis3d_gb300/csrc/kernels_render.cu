@@ -331,7 +331,7 @@ __device__ __forceinline__ bool composite(const FrameDesc& f, float4 c, Accum& a
 }
 
 template <typename T, int MODE, int SAMPLER>
-__device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) {
+__device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, int vidx) {
   Accum acc = {0.f, 0.f, 0.f, 0.f};
   float runmax = -INFINITY;  // MIP: largest sample so far
   if (r.hit) {
@@ -421,7 +421,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
           bi = -1;
           continue;
         }
-        if (f.touched) f.touched[bi] = 1;
+        if (f.touched) f.touched[(long long)vidx * f.touched_stride + bi] = 1;
       }
       int ke = bke;
       if (f.empty_skip >= 2) {
@@ -455,7 +455,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp) 
         ke = kef >= (float)ke ? ke : max(k + 1, (int)kef);
         if (f.cell_touched) {
           // algorithmic-bytes accounting: one bit per sampled cell
-          unsigned* w = f.cell_touched + (ci >> 5);
+          unsigned* w = f.cell_touched + (long long)vidx * f.cell_touched_stride + (ci >> 5);
           const unsigned bit = 1u << (ci & 31);
           if (!(*(volatile unsigned*)w & bit)) atomicOr(w, bit);
         }
@@ -566,7 +566,7 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
   if (px < f.width && py < f.height) {
     RaySetup r;
     setup_ray(f, px, py, r);
-    float4 c = march<T, MODE, SAMPLER>(f, r, nsamp);
+    float4 c = march<T, MODE, SAMPLER>(f, r, nsamp, 0);
     size_t o = (size_t)py * f.width + px;
     if (f.out_f32) f.out_f32[o] = c;
     if (f.out_rgba8) {
@@ -581,7 +581,42 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
   if (lane == 0 && f.samples && nsamp) atomicAdd(f.samples, (unsigned long long)nsamp);
 }
 
+// The same for a batch-uniform descriptor f (kernel parameter) and the view's
+// own descriptor fv (camera, image size, outputs, counter).
+template <typename T, int MODE, int SAMPLER>
+__device__ __forceinline__ void render_tile_u(const FrameDesc& f, const FrameDesc& fv, int vidx, int tile) {
+  const int lane = threadIdx.x & 31;
+  const int tw = f.tile_w;
+  const int tx = tile % f.tiles_x, ty = tile / f.tiles_x;
+  const int px = tx * tw + (lane & (tw - 1));
+  const int py = ty * (32 / tw) + (lane / tw);
+  unsigned nsamp = 0;
+  if (px < f.width && py < f.height) {
+    RaySetup r;
+    setup_ray(fv, px, py, r);
+    float4 c = march<T, MODE, SAMPLER>(f, r, nsamp, vidx);
+    size_t o = (size_t)py * f.width + px;
+    float4* of = fv.out_f32;
+    uchar4* o8 = fv.out_rgba8;
+    if (of) of[o] = c;
+    if (o8)
+      o8[o] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
+                          (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
+                          (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f),
+                          (unsigned char)__float2uint_rn(__saturatef(c.w) * 255.f));
+  }
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) nsamp += __shfl_xor_sync(0xffffffffu, nsamp, s);
+  if (lane == 0 && nsamp) {
+    unsigned long long* cnt = fv.samples;
+    if (cnt) atomicAdd(cnt, (unsigned long long)nsamp);
+  }
+}
+
 constexpr int RENDER_THREADS = 128;
+// Resident CTAs per SM the uniform persistent kernel is compiled for (a
+// measured optimum: 10 CTAs of 128 threads, 48 registers, ahead of 6, 8, 12).
+constexpr int UNIFORM_CTAS_PER_SM = 10;
 
 template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_plain(const __grid_constant__ FrameDesc f) {
@@ -698,6 +733,24 @@ cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStr
   else if (f.dtype == DT_U16) k_render_slice<uint16_t><<<grid, 128, 0, s>>>(f, sd);
   else k_render_slice<float><<<grid, 128, 0, s>>>(f, sd);
   return cudaGetLastError();
+}
+
+// Batch-uniform variant: `shared` (a kernel parameter, so the walk reads it as
+// constant-bank operands) holds everything the views have in common; camera,
+// image size, outputs and the sample counter come from frames[view].
+template <typename T, int MODE, int SAMPLER>
+__global__ void __launch_bounds__(RENDER_THREADS, UNIFORM_CTAS_PER_SM)
+    k_render_persistent_u(const __grid_constant__ FrameDesc shared, const FrameDesc* __restrict__ frames,
+                          int nframes, const int* __restrict__ tile_prefix, int total, int* __restrict__ counter) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(counter, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= total) return;
+    int fi = find_frame(tile_prefix, nframes, item);
+    render_tile_u<T, MODE, SAMPLER>(shared, frames[fi], fi, item - __ldg(tile_prefix + fi));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -851,6 +904,15 @@ static cudaError_t persistent_t(const FrameDesc* frames, int nframes, const int*
   return cudaGetLastError();
 }
 
+template <typename T, int MODE, int SAMPLER>
+static cudaError_t persistent_u_t(const FrameDesc& shared, const FrameDesc* frames, int nframes, const int* prefix,
+                                  int total, int* counter, int grid, cudaStream_t s) {
+  (void)cudaGetLastError();
+  k_render_persistent_u<T, MODE, SAMPLER><<<grid, RENDER_THREADS, 0, s>>>(shared, frames, nframes, prefix, total,
+                                                                         counter);
+  return cudaGetLastError();
+}
+
 #define GBVR_DISPATCH(FN, dtype, mode, sampler, ...)                                          \
   do {                                                                                        \
     switch ((dtype) * 8 + (mode) * 2 + (sampler)) {                                           \
@@ -893,6 +955,22 @@ cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, con
                                            const int* prefix, int total, int* counter, int grid, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   GBVR_DISPATCH(persistent_t, dtype, mode, sampler, frames, nframes, prefix, total, counter, grid, s);
+}
+
+cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, const FrameDesc& shared,
+                                             const FrameDesc* frames, int nframes, const int* prefix, int total,
+                                             int* counter, int grid, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  GBVR_DISPATCH(persistent_u_t, dtype, mode, sampler, shared, frames, nframes, prefix, total, counter, grid, s);
+}
+
+int persistent_grid_size_uniform(int device) {
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_1D, SAMPLER_SW>,
+                                                RENDER_THREADS, 0);
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm;
 }
 
 int persistent_grid_size(int device) {

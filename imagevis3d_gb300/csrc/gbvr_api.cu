@@ -936,7 +936,7 @@ struct gbvr_renderer {
   int last_views = 0, last_level = 0;
   float last_ms = 0.f, last_kernel_ms = 0.f;
   uint64_t last_h2d = 0;
-  int max_ctas_per_sm = 0, max_ctas_per_sm_u = 0, sm_count = 0;
+  int max_ctas_per_sm = 0, max_ctas_per_sm_u[4] = {0, 0, 0, 0}, sm_count = 0;
   // graph cache for the batch launch
   struct GraphKey {
     int n, w, h, level, dtype, mode, sampler, grid;
@@ -1416,7 +1416,8 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
     r->max_ctas_per_sm = std::max(1, persistent_grid_size(dev) / std::max(r->sm_count, 1));
-    r->max_ctas_per_sm_u = std::max(1, persistent_grid_size_uniform(dev) / std::max(r->sm_count, 1));
+    for (int m = 0; m < 4; ++m)
+      r->max_ctas_per_sm_u[m] = std::max(1, persistent_grid_size_uniform(dev, m) / std::max(r->sm_count, 1));
   }
   // Views of one renderer batch share everything but camera, outputs and
   // counters, unless they sample different brick layout copies: then the
@@ -1426,14 +1427,16 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     if (hf[v].perm != hf[0].perm || hf[v].copy_off != hf[0].copy_off) uniform = false;
   FrameDesc shared = hf[0];
   if (uniform) {
+    // per-view parts, read from each view's own descriptor
     memset(shared.inv_vp, 0, sizeof(shared.inv_vp));
+    memset(shared.light_to, 0, sizeof(shared.light_to));
     shared.out_rgba8 = nullptr;
     shared.out_f32 = nullptr;
     shared.samples = nullptr;
     shared.touched_stride = shared.touched ? r->ds.levels[level].nbricks : 0;
     shared.cell_touched_stride = shared.cell_touched ? r->cell_words : 0;
   }
-  const int max_per_sm = uniform ? r->max_ctas_per_sm_u : r->max_ctas_per_sm;
+  const int max_per_sm = uniform ? r->max_ctas_per_sm_u[r->mode] : r->max_ctas_per_sm;
   const int per_sm = r->ctas_per_sm > 0 ? std::min(r->ctas_per_sm, max_per_sm) : max_per_sm;
   const int grid = r->sm_count * per_sm;
   gbvr_renderer::GraphKey key{n, r->width, r->height, level, r->ds.dtype, r->mode, r->sampler, grid, r->d_fb8.p, r->d_fb32.p};

@@ -139,13 +139,14 @@ cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, con
                                            int nframes, const int* tile_prefix, int total_tiles,
                                            int* counter, int grid, cudaStream_t s);
 int persistent_grid_size(int device);
-// Batches whose views share everything but camera, outputs and counters: the
-// shared part travels as a kernel parameter (constant bank), each view's part
-// is read from `frames` (camera, image size, outputs, sample counter).
+// Batches whose views share everything but camera, light direction, outputs
+// and counters: the shared part travels as a kernel parameter (constant
+// bank), each view's part is read from `frames` (camera, light direction,
+// outputs, sample counter).
 cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, const FrameDesc& shared,
                                              const FrameDesc* frames, int nframes, const int* prefix, int total,
                                              int* counter, int grid, cudaStream_t s);
-int persistent_grid_size_uniform(int device);
+int persistent_grid_size_uniform(int device, int mode);
 cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStream_t s);
 
 // ---- launch wrappers (kernels_build.cu) ----

@@ -215,8 +215,10 @@ __device__ __forceinline__ void gradient(const FrameDesc& f, const BrickView& b,
 }
 
 // Phong, directional light, two-sided: normal = -grad/|grad| turned towards
-// the viewer.  g is a world-space gradient, V the unit vector to the viewer.
-__device__ __forceinline__ void shade(const FrameDesc& f, const float g[3], const float V[3],
+// the viewer.  g is a world-space gradient, V the unit vector to the viewer,
+// L the unit vector towards the light in world space (it follows the view:
+// the light is fixed in eye space).
+__device__ __forceinline__ void shade(const FrameDesc& f, const float* L, const float g[3], const float V[3],
                                       const float col[3], float out[3]) {
   float gl = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
   if (!(gl > 0.f)) {
@@ -227,7 +229,6 @@ __device__ __forceinline__ void shade(const FrameDesc& f, const float g[3], cons
   }
   float n0 = -g[0] / gl, n1 = -g[1] / gl, n2 = -g[2] / gl;
   if (n0 * V[0] + n1 * V[1] + n2 * V[2] < 0.f) { n0 = -n0; n1 = -n1; n2 = -n2; }
-  const float* L = f.light_to;
   float nl = fmaxf(0.f, n0 * L[0] + n1 * L[1] + n2 * L[2]);
   float H0 = L[0] + V[0], H1 = L[1] + V[1], H2 = L[2] + V[2];
   float hl = sqrtf(H0 * H0 + H1 * H1 + H2 * H2);
@@ -331,7 +332,7 @@ __device__ __forceinline__ bool composite(const FrameDesc& f, float4 c, Accum& a
 }
 
 template <typename T, int MODE, int SAMPLER>
-__device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, int vidx) {
+__device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, int vidx, const float* light_to) {
   Accum acc = {0.f, 0.f, 0.f, 0.f};
   float runmax = -INFINITY;  // MIP: largest sample so far
   if (r.hit) {
@@ -517,7 +518,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
             g[0] *= f.vox_scale[0];
             g[1] *= f.vox_scale[1];
             g[2] *= f.vox_scale[2];
-            if (f.lighting) shade(f, g, V, f.iso_rgb, col);
+            if (f.lighting) shade(f, light_to, g, V, f.iso_rgb, col);
             else { col[0] = f.iso_rgb[0]; col[1] = f.iso_rgb[1]; col[2] = f.iso_rgb[2]; }
             acc.C0 = col[0]; acc.C1 = col[1]; acc.C2 = col[2];
             acc.A = 1.f;
@@ -534,7 +535,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
         if (f.lighting && cl.w > 0.f) {
           float gw[3] = {g[0] * f.vox_scale[0], g[1] * f.vox_scale[1], g[2] * f.vox_scale[2]};
           float col[3] = {cl.x, cl.y, cl.z}, lit[3];
-          shade(f, gw, V, col, lit);
+          shade(f, light_to, gw, V, col, lit);
           cl.x = lit[0]; cl.y = lit[1]; cl.z = lit[2];
         }
         if (composite<MODE>(f, cl, acc)) { done = true; break; }
@@ -566,7 +567,7 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
   if (px < f.width && py < f.height) {
     RaySetup r;
     setup_ray(f, px, py, r);
-    float4 c = march<T, MODE, SAMPLER>(f, r, nsamp, 0);
+    float4 c = march<T, MODE, SAMPLER>(f, r, nsamp, 0, f.light_to);
     size_t o = (size_t)py * f.width + px;
     if (f.out_f32) f.out_f32[o] = c;
     if (f.out_rgba8) {
@@ -594,7 +595,7 @@ __device__ __forceinline__ void render_tile_u(const FrameDesc& f, const FrameDes
   if (px < f.width && py < f.height) {
     RaySetup r;
     setup_ray(fv, px, py, r);
-    float4 c = march<T, MODE, SAMPLER>(f, r, nsamp, vidx);
+    float4 c = march<T, MODE, SAMPLER>(f, r, nsamp, vidx, fv.light_to);
     size_t o = (size_t)py * f.width + px;
     float4* of = fv.out_f32;
     uchar4* o8 = fv.out_rgba8;
@@ -614,9 +615,11 @@ __device__ __forceinline__ void render_tile_u(const FrameDesc& f, const FrameDes
 }
 
 constexpr int RENDER_THREADS = 128;
-// Resident CTAs per SM the uniform persistent kernel is compiled for (a
-// measured optimum: 10 CTAs of 128 threads, 48 registers, ahead of 6, 8, 12).
-constexpr int UNIFORM_CTAS_PER_SM = 10;
+// Resident CTAs per SM the uniform persistent kernel is compiled for: for the
+// 1D TF and MIP walks 10 CTAs of 128 threads (48 registers; measured ahead of
+// 6, 8 and 12), for the shaded modes 8 (64 registers, fewer spills).
+template <int MODE>
+constexpr int uniform_ctas_per_sm() { return (MODE == MODE_1D || MODE == MODE_MIP) ? 10 : 8; }
 
 template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_plain(const __grid_constant__ FrameDesc f) {
@@ -739,7 +742,7 @@ cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStr
 // constant-bank operands) holds everything the views have in common; camera,
 // image size, outputs and the sample counter come from frames[view].
 template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS, UNIFORM_CTAS_PER_SM)
+__global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
     k_render_persistent_u(const __grid_constant__ FrameDesc shared, const FrameDesc* __restrict__ frames,
                           int nframes, const int* __restrict__ tile_prefix, int total, int* __restrict__ counter) {
   const int lane = threadIdx.x & 31;
@@ -964,11 +967,15 @@ cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, c
   GBVR_DISPATCH(persistent_u_t, dtype, mode, sampler, shared, frames, nframes, prefix, total, counter, grid, s);
 }
 
-int persistent_grid_size_uniform(int device) {
+int persistent_grid_size_uniform(int device, int mode) {
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_1D, SAMPLER_SW>,
-                                                RENDER_THREADS, 0);
+  if (mode == MODE_1D || mode == MODE_MIP)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_1D, SAMPLER_SW>,
+                                                  RENDER_THREADS, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_2D, SAMPLER_SW>,
+                                                  RENDER_THREADS, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }

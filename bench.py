@@ -750,7 +750,7 @@ def main():
                     "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic_from_profile(),
-                         "kernel": "k_render_persistent<uint16,1D,SW>",
+                         "kernel": "k_render_persistent_u<uint16,1D,SW>",
                          "bytes_per_launch": cell_bytes_per_launch,
                          "bytes_rule": "sum over views of distinct non-empty 4^3 macro-cells sampled x 4^3 x 2 B",
                          "brick_bytes_per_launch": brick_bytes / args.steps,

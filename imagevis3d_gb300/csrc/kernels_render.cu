@@ -622,7 +622,8 @@ template <int MODE>
 constexpr int uniform_ctas_per_sm() { return (MODE == MODE_1D || MODE == MODE_MIP) ? 10 : 8; }
 
 template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_plain(const __grid_constant__ FrameDesc f) {
+__global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
+    k_render_plain(const __grid_constant__ FrameDesc f) {
   int warp = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (warp >= f.tiles_x * f.tiles_y) return;
   render_tile<T, MODE, SAMPLER>(f, warp);

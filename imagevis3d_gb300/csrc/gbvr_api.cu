@@ -925,7 +925,13 @@ struct gbvr_renderer {
   DevBuf d_cellbits, d_cellcount, d_occtmp, d_ooc_skip;
   // out-of-core paging state and the last paint's statistics
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t ev_copy0 = nullptr, ev_copy1 = nullptr;
+  // out-of-core paging, double-buffered for the fly-through pipeline: copy
+  // start/end events, render-done events and page-locked staging for the page
+  // table and skip table of each of two frames in flight
+  cudaEvent_t ev_c0[2] = {nullptr, nullptr}, ev_c1[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr};
+  PinnedBuf h_pt[2], h_skip[2];
+  std::vector<std::shared_ptr<DevBuf>> occ_lv;  // out of core: classified macro-cells per level
+  std::vector<char> occ_valid;
   uint64_t last_misses = 0, last_paged = 0;
   float last_page_ms = 0.f;
   long long cell_words = 0;
@@ -964,8 +970,11 @@ struct gbvr_renderer {
     if (ev1) cudaEventDestroy(ev1);
     if (evk0) cudaEventDestroy(evk0);
     if (evk1) cudaEventDestroy(evk1);
-    if (ev_copy0) cudaEventDestroy(ev_copy0);
-    if (ev_copy1) cudaEventDestroy(ev_copy1);
+    for (int k = 0; k < 2; ++k) {
+      if (ev_c0[k]) cudaEventDestroy(ev_c0[k]);
+      if (ev_c1[k]) cudaEventDestroy(ev_c1[k]);
+      if (ev_done[k]) cudaEventDestroy(ev_done[k]);
+    }
     if (copy_stream) cudaStreamDestroy(copy_stream);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -1027,6 +1036,29 @@ int upload_tf(gbvr_renderer* r, int level) {
     r->tf_dirty = false;
     r->skip_dirty = true;
   }
+  if (r->ds.ooc) {
+    // out of core: frames of a fly-through change level, so each level keeps
+    // its own classified macro-cells until the TF or mode changes
+    const size_t nl = r->ds.levels.size();
+    if (r->occ_lv.size() != nl) {
+      r->occ_lv.clear();
+      for (size_t l = 0; l < nl; ++l) r->occ_lv.push_back(std::make_shared<DevBuf>());
+      r->occ_valid.assign(nl, 0);
+    }
+    if (r->skip_dirty) {
+      r->occ_valid.assign(nl, 0);
+      r->skip_dirty = false;
+    }
+    if (!r->occ_valid[level]) {
+      double lo, hi;
+      default_range(r, lo, hi);
+      int w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4), h = two ? r->tf2d_h : 1;
+      TRY(classify_level(r->ds, level, tf, w, h, r->mode, lo, hi, r->iso, r->d_tfprefix, r->d_skip, *r->occ_lv[level],
+                         r->d_occtmp, r->stream));
+      r->occ_valid[level] = 1;
+    }
+    return GBVR_OK;
+  }
   if (r->skip_dirty || r->skip_level != level) {
     double lo, hi;
     default_range(r, lo, hi);
@@ -1074,7 +1106,7 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
   default_range(r, p.lo, p.hi);
   p.grad_max = r->tf2d_grad_max;
   p.skip = r->d_skip.as<unsigned char>();
-  p.occ = r->d_occ.as<unsigned char>();
+  p.occ = r->ds.ooc && level < (int)r->occ_lv.size() ? r->occ_lv[level]->as<unsigned char>() : r->d_occ.as<unsigned char>();
   p.clip_on = r->clip_on;
   for (int k = 0; k < 4; ++k) p.clip[k] = r->clip[k];
   if (r->ds.ooc) {
@@ -1112,7 +1144,16 @@ struct PtrSnapshot {
 // the frame's skip table: a brick is skipped when it is empty under the TF or
 // not resident.  Bricks needed at the requested level but not resident when
 // the paint began count as misses.
-int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level) {
+//
+// Nothing here waits for the GPU: the copies go to the copy stream between
+// the events ev_c0/ev_c1[stage], the render stream waits for them and then
+// takes the level's page table and the skip table from the page-locked
+// staging of `stage`.  A frame still rendering keeps its slots: `protect` is
+// its stamp (0: none), and if the new frame cannot be placed without them the
+// call first waits for `protect_done`.  The staging of `stage` must be free
+// (its previous uploads complete) when this is called.
+int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64_t protect, cudaEvent_t protect_done,
+             int stage, uint64_t* misses_out, uint64_t* bytes_out) {
   Dataset& ds = r->ds;
   ensure_tf(r);
   const bool two = r->mode == GBVR_RM_2DTRANS;
@@ -1201,10 +1242,20 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level) {
     want[bidx] = 1;
     if (ds.slot_of[bidx] >= 0) ds.slot_used[ds.slot_of[bidx]] = ds.frame;
   }
-  // victims: free slots first, then least recently used unwanted bricks
+  // victims: free slots first, then least recently used unwanted bricks; the
+  // slots of a frame still rendering only if the new frame needs the room
+  size_t missing = 0;
+  for (int bidx : needed) missing += ds.slot_of[bidx] < 0;
   std::vector<int> victims;
-  for (int sl = 0; sl < ds.nslots; ++sl)
-    if (ds.slot_brick[sl] < 0 || !want[ds.slot_brick[sl]]) victims.push_back(sl);
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool guard = protect != 0 && pass == 0;
+    victims.clear();
+    for (int sl = 0; sl < ds.nslots; ++sl)
+      if (ds.slot_brick[sl] < 0 || (!want[ds.slot_brick[sl]] && !(guard && ds.slot_used[sl] == protect)))
+        victims.push_back(sl);
+    if (victims.size() >= missing || !guard) break;
+    if (protect_done) CUDA_TRY(cudaEventSynchronize(protect_done));
+  }
   std::sort(victims.begin(), victims.end(), [&](int x, int y) {
     const bool fx = ds.slot_brick[x] < 0, fy = ds.slot_brick[y] < 0;
     if (fx != fy) return fx;
@@ -1213,10 +1264,12 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level) {
   const size_t es = dtype_size(ds.dtype);
   size_t vi = 0;
   uint64_t bytes = 0;
-  // slots are overwritten only after every earlier paint has read them
-  CUDA_TRY(cudaEventRecord(r->ev_copy0, r->stream));
-  CUDA_TRY(cudaStreamWaitEvent(r->copy_stream, r->ev_copy0, 0));
-  CUDA_TRY(cudaEventRecord(r->ev_copy0, r->copy_stream));
+  if (!protect) {
+    // slots are overwritten only after every earlier paint has read them
+    CUDA_TRY(cudaEventRecord(r->ev_c0[stage], r->stream));
+    CUDA_TRY(cudaStreamWaitEvent(r->copy_stream, r->ev_c0[stage], 0));
+  }
+  CUDA_TRY(cudaEventRecord(r->ev_c0[stage], r->copy_stream));
   for (int bidx : needed) {
     if (ds.slot_of[bidx] >= 0) continue;
     if (vi >= victims.size()) break;
@@ -1232,27 +1285,41 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level) {
                              r->copy_stream));
     bytes += nbytes;
   }
-  CUDA_TRY(cudaEventRecord(r->ev_copy1, r->copy_stream));
-  CUDA_TRY(cudaStreamWaitEvent(r->stream, r->ev_copy1, 0));
-  // page table of the rendered level and its skip table
+  CUDA_TRY(cudaEventRecord(r->ev_c1[stage], r->copy_stream));
+  CUDA_TRY(cudaStreamWaitEvent(r->stream, r->ev_c1[stage], 0));
+  // page table of the rendered level and its skip table, staged in page-locked
+  // memory so the uploads queue behind the renders already on the stream
   const Level& L = ds.levels[level];
-  std::vector<unsigned char> skip(ds.bricks.size(), 1);
+  CUDA_TRY(r->h_pt[stage].alloc(sizeof(BrickInfo) * ds.bricks.size()));
+  CUDA_TRY(r->h_skip[stage].alloc(ds.bricks.size()));
+  BrickInfo* pt = (BrickInfo*)r->h_pt[stage].p;
+  unsigned char* skip = (unsigned char*)r->h_skip[stage].p;
+  memset(skip, 1, ds.bricks.size());
   for (int i = 0; i < L.nbricks; ++i) {
     BrickInfo& b = ds.bricks[L.brick_base + i];
     const int sl = ds.slot_of[L.brick_base + i];
     b.offset = sl >= 0 ? (unsigned long long)sl * ds.slot_elems : 0;
+    pt[i] = b;
     skip[L.brick_base + i] = (sl >= 0 && nonempty(b)) ? 0 : 1;
   }
-  CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.as<BrickInfo>() + L.brick_base, ds.bricks.data() + L.brick_base,
-                           sizeof(BrickInfo) * L.nbricks, cudaMemcpyHostToDevice, r->stream));
+  CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.as<BrickInfo>() + L.brick_base, pt, sizeof(BrickInfo) * L.nbricks,
+                           cudaMemcpyHostToDevice, r->stream));
   CUDA_TRY(r->d_ooc_skip.alloc(ds.bricks.size()));
-  CUDA_TRY(cudaMemcpyAsync(r->d_ooc_skip.p, skip.data(), skip.size(), cudaMemcpyHostToDevice, r->stream));
-  CUDA_TRY(cudaEventSynchronize(r->ev_copy1));
-  CUDA_TRY(cudaEventElapsedTime(&r->last_page_ms, r->ev_copy0, r->ev_copy1));
-  // the host tables above must outlive their copies
-  CUDA_TRY(cudaStreamSynchronize(r->stream));
-  r->last_misses = misses;
-  r->last_paged = bytes;
+  CUDA_TRY(cudaMemcpyAsync(r->d_ooc_skip.p, skip, ds.bricks.size(), cudaMemcpyHostToDevice, r->stream));
+  if (misses_out) *misses_out = misses;
+  if (bytes_out) *bytes_out = bytes;
+  return GBVR_OK;
+}
+
+int ooc_streams(gbvr_renderer* r) {
+  if (!r->copy_stream) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      CUDA_TRY(cudaEventCreate(&r->ev_c0[k]));
+      CUDA_TRY(cudaEventCreate(&r->ev_c1[k]));
+      CUDA_TRY(cudaEventCreate(&r->ev_done[k]));
+    }
+  }
   return GBVR_OK;
 }
 
@@ -1261,11 +1328,7 @@ int prepare(gbvr_renderer* r, int nviews, int& level, const gbvr_view* views) {
   if (nviews <= 0) return fail(GBVR_EINVAL, "view count must be positive");
   level = render_level(r);
   if (r->ds.ooc) {
-    if (!r->copy_stream) {
-      CUDA_TRY(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
-      CUDA_TRY(cudaEventCreate(&r->ev_copy0));
-      CUDA_TRY(cudaEventCreate(&r->ev_copy1));
-    }
+    TRY(ooc_streams(r));
     std::vector<gbvr_view> vs;
     if (!views) {
       gbvr_view v;
@@ -1278,7 +1341,10 @@ int prepare(gbvr_renderer* r, int nviews, int& level, const gbvr_view* views) {
       vs.push_back(v);
       views = vs.data();
     }
-    TRY(ooc_page(r, views, views == vs.data() ? 1 : nviews, level));
+    // every earlier paint has finished (paints are synchronous): no slot is in use
+    TRY(ooc_page(r, views, views == vs.data() ? 1 : nviews, level, 0, nullptr, 0, &r->last_misses, &r->last_paged));
+    CUDA_TRY(cudaEventSynchronize(r->ev_c1[0]));
+    CUDA_TRY(cudaEventElapsedTime(&r->last_page_ms, r->ev_c0[0], r->ev_c1[0]));
     r->drop_graphs();  // the page table changes between paints
   }
   const size_t npix = (size_t)r->width * r->height;
@@ -1388,6 +1454,89 @@ int paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
   r->last_h2d = sizeof(float) * r->tf1d.size();
   return finish(r, 1, level);
+}
+
+// A sequence of frames (a fly-through) into framebuffers 0..n-1.  Out of
+// core the frames form a pipeline: while frame i renders, the host picks
+// frame i + 1's level and bricks and their copies run on the copy stream;
+// frame i's slots are kept until it is done, and at most two frames are in
+// flight (frame i is paged only after frame i - 2 has finished, which frees
+// its staging and its slots).  Each frame renders with the per-view kernel
+// at its own level.  In core the frames simply render one after the other.
+int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out, uint64_t* miss_out,
+               uint64_t* paged_out) {
+  TRY(check_loaded(r));
+  if (n <= 0 || !views) return fail(GBVR_EINVAL, "bad view list");
+  Dataset& ds = r->ds;
+  if (!ds.ooc) {
+    TRY(paint_plain(r, views, n));
+    for (int i = 0; i < n; ++i) {
+      if (lod_out) lod_out[i] = r->last_level;
+      if (miss_out) miss_out[i] = 0;
+      if (paged_out) paged_out[i] = 0;
+    }
+    return GBVR_OK;
+  }
+  TRY(ooc_streams(r));
+  const size_t npix = (size_t)r->width * r->height;
+  if (r->fb_views < n || r->fb_w != r->width || r->fb_h != r->height) {
+    CUDA_TRY(r->d_fb8.alloc(npix * 4 * n));
+    if (r->flags & 1u) CUDA_TRY(r->d_fb32.alloc(npix * 16 * n));
+    r->fb_views = n;
+    r->fb_w = r->width;
+    r->fb_h = r->height;
+    r->drop_graphs();
+  }
+  const int nb0 = ds.levels[0].nbricks;  // the finest level has the most bricks
+  CUDA_TRY(r->d_samples.alloc(sizeof(unsigned long long) * n));
+  CUDA_TRY(r->d_touched.alloc((size_t)n * nb0));
+  CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream));
+  CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * nb0, r->stream));
+  r->drop_graphs();
+  uint64_t stamp[2] = {0, 0};
+  uint64_t tot_miss = 0, tot_paged = 0;
+  float tot_page_ms = 0.f;
+  int level = 0;
+  auto page_time = [&](int st) -> int {
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, r->ev_c0[st], r->ev_c1[st]));
+    tot_page_ms += ms;
+    return GBVR_OK;
+  };
+  CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
+  CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
+  for (int i = 0; i < n; ++i) {
+    const int st = i & 1;
+    if (i >= 2) {
+      CUDA_TRY(cudaEventSynchronize(r->ev_done[st]));  // frame i - 2 is done
+      TRY(page_time(st));
+    }
+    level = render_level(r);
+    uint64_t miss = 0, bytes = 0;
+    const uint64_t protect = i >= 1 ? stamp[st ^ 1] : 0;
+    TRY(ooc_page(r, views + i, 1, level, protect, i >= 1 ? r->ev_done[st ^ 1] : nullptr, st, &miss, &bytes));
+    stamp[st] = ds.frame;
+    TRY(upload_tf(r, level));
+    FrameDesc f = make_frame(r, views[i].view, views[i].proj, level, i);
+    f.touched = r->stats_level >= 1 ? r->d_touched.as<unsigned char>() + (size_t)i * nb0 : nullptr;
+    f.cell_touched = nullptr;
+    CUDA_TRY(launch_render_plain(f, r->stream));
+    CUDA_TRY(cudaEventRecord(r->ev_done[st], r->stream));
+    if (lod_out) lod_out[i] = level;
+    if (miss_out) miss_out[i] = miss;
+    if (paged_out) paged_out[i] = bytes;
+    tot_miss += miss;
+    tot_paged += bytes;
+  }
+  CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
+  CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
+  CUDA_TRY(cudaEventSynchronize(r->ev1));
+  for (int i = std::max(0, n - 2); i < n; ++i) TRY(page_time(i & 1));
+  r->last_misses = tot_miss;
+  r->last_paged = tot_paged;
+  r->last_page_ms = tot_page_ms;
+  r->last_h2d = 0;
+  return finish(r, n, level);
 }
 
 int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
@@ -1812,6 +1961,12 @@ int gbvr_set_render_mode(gbvr_renderer* r, int mode) {
   if (mode != r->mode) { r->tf_dirty = true; r->skip_dirty = true; }
   r->mode = mode;
   return GBVR_OK;
+}
+
+int gbvr_paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod, uint64_t* misses,
+                    uint64_t* bytes_paged) {
+  TRY(check_r(r));
+  return paint_path(r, views, n, lod, misses, bytes_paged);
 }
 
 int gbvr_paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_y, int use_mip) {

@@ -237,6 +237,20 @@ class Renderer:
         """changed2DTrans from a .2dt file (rasterised on the GPU)."""
         L.call("gbvr_set_tf2d_file", self._h, path.encode(), max_grad)
 
+    def paintPath(self, views):
+        """Frames of a camera path into framebuffers 0..n-1 (out of core: paging
+        of frame i + 1 overlaps the render of frame i).  Returns per-frame
+        (lod, misses, bytes_paged) arrays."""
+        arr = self._views(views)
+        n = len(views)
+        lod = np.zeros(n, np.int32)
+        miss = np.zeros(n, np.uint64)
+        paged = np.zeros(n, np.uint64)
+        L.call("gbvr_paint_path", self._h, arr, n, lod.ctypes.data_as(C.POINTER(C.c_int32)),
+               miss.ctypes.data_as(L.U64P), paged.ctypes.data_as(L.U64P))
+        self._nviews = n
+        return lod, miss, paged
+
     def paintSlice(self, axis, index, flip_x=False, flip_y=False, use_mip=False):
         """A 2D render region: the slice `index` (finest-level voxels) across
         `axis` (0 sagittal x, 1 axial y, 2 coronal z), or the maximum along it."""

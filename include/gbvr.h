@@ -184,6 +184,15 @@ int gbvr_resize(gbvr_renderer* r, int width, int height);                 /* res
 int gbvr_set_render_mode(gbvr_renderer* r, int mode);                     /* setRenderMode */
 int gbvr_set_tf1d(gbvr_renderer* r, const float* rgba, int n);            /* changed1DTrans */
 int gbvr_set_tf2d(gbvr_renderer* r, const float* rgba, int w, int h, float max_grad); /* changed2DTrans */
+/* A camera path (the fly-through animator's frames, LuaScripts/FlyThroughAnimator.lua, painted one by one
+ * in the reference) in one call: frame i into framebuffer i (read them with gbvr_read_framebuffers).  Out of
+ * core every frame renders at the finest level whose bricks fit the device pool, as gbvr_paint does, and
+ * the bricks of frame i + 1 are paged in on a copy stream while frame i renders.  Per frame (optional arrays
+ * of n entries): the level rendered, the bricks missed at the target level, the bytes paged in.  In-core
+ * datasets render the frames one after the other.  gbvr_get_stats then reports the whole path. */
+int gbvr_paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod, uint64_t* misses,
+                    uint64_t* bytes_paged);
+
 /* 2D render region (tuvok.renderRegion2D.new(mode, sliceIndex, renderer), setSliceDepth, set2DFlipMode,
  * setUseMIP: RenderWindow.cpp:1548-1571, 235-239, 270-289) into framebuffer 0.  axis = the window mode:
  * 0 sagittal (x), 1 axial (y), 2 coronal (z), as the reference indexes getDomainSize() by it; index = the

@@ -195,3 +195,43 @@ def test_ooc_rejections(tmp_path):
             r.setSampler(GBVR_SAMPLER_TEX)
             r.paint()
 
+
+
+def test_ooc_paint_path_pipeline_matches_incore_per_frame():
+    sp, bp = CASES["u16_200x180x170_b64"]
+    slot = 64 ** 3 * 2
+    views = _inside_path(10, 128, 96)
+    with Renderer(float_fb=True) as a, Renderer(float_fb=True) as b, Renderer(float_fb=True) as c:
+        a.loadSynthetic(sp, **bp)
+        b.loadSyntheticOutOfCore(sp, 30 * slot, **bp)
+        c.loadSyntheticOutOfCore(sp, 30 * slot, **bp)
+        for r in (a, b, c):
+            _setup(r, sp, 128, 96)
+        lod, miss, paged = b.paintPath(views)
+        st = b.stats()
+        assert st["bytes_paged"] == int(paged.sum()) > 0 and st["brick_misses"] == int(miss.sum())
+        frames = [b.readFramebuffer(i, as_float=True) for i in range(len(views))]
+        for i, (view, proj) in enumerate(views):
+            # same level as a synchronous paint of the frame
+            img_c = _paint(c, view, proj)
+            assert c.stats()["lod"] == lod[i]
+            assert np.array_equal(frames[i], img_c), i
+            a.setLODLimits(int(lod[i]), int(lod[i]))
+            assert np.array_equal(frames[i], _paint(a, view, proj)), i
+        # a second pass over the same path finds most bricks resident
+        lod2, miss2, paged2 = b.paintPath(views)
+        assert paged2.sum() < paged.sum()
+        assert np.array_equal(lod2, lod)
+
+
+def test_paint_path_in_core_equals_views():
+    sp, bp = CASES["u8_131x97x203_b32"]
+    views = _inside_path(4, 96, 64)
+    with Renderer(float_fb=True) as a:
+        a.loadSynthetic(sp, **bp)
+        _setup(a, sp, 96, 64)
+        lod, miss, paged = a.paintPath(views)
+        assert (lod == 0).all() and miss.sum() == 0 and paged.sum() == 0
+        got = [a.readFramebuffer(i, as_float=True) for i in range(4)]
+        for i, (view, proj) in enumerate(views):
+            assert np.array_equal(got[i], _paint(a, view, proj))

@@ -862,6 +862,9 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
   for (int k = 0; k < 4; ++k) f.clip[k] = p.clip[k];
   f.tiles_x = (p.width + p.tile_w - 1) / p.tile_w;
   f.tiles_y = (p.height + 32 / p.tile_w - 1) / (32 / p.tile_w);
+  f.tx0 = f.ty0 = 0;
+  f.ntx = f.tiles_x;
+  f.nty = f.tiles_y;
   // layout copy: the axis whose voxel-space extent along screen x is largest
   // (row 0 of the view matrix is the camera's right vector in world space)
   f.perm = 0;
@@ -1125,6 +1128,43 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
   f.cell_touched = (r->stats_level >= 2 && r->empty_skip >= 2)
                        ? r->d_cellbits.as<unsigned>() + (size_t)vidx * r->cell_words : nullptr;
   return f;
+}
+
+// The view's ray tiles whose pixels can see the volume: the rectangle around
+// the projected corners of the volume box, one pixel wider on each side.  A
+// pixel centre outside the projected box (the convex hull of its corners when
+// all are in front of the eye) sends a ray that misses it.  With a corner at
+// or behind the eye, or a box beyond the frame, the whole frame is kept or
+// nothing (only the background).
+void cull_tiles(FrameDesc& f, const gbvr_renderer* r, const float* view, const float* proj) {
+  double V[16], P[16], M[16];
+  for (int i = 0; i < 16; ++i) { V[i] = view[i]; P[i] = proj[i]; }
+  mat_mul(P, V, M);
+  double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+  for (int k = 0; k < 8; ++k) {
+    const double c[3] = {(k & 1) ? f.half_extent[0] : -f.half_extent[0], (k & 2) ? f.half_extent[1] : -f.half_extent[1],
+                         (k & 4) ? f.half_extent[2] : -f.half_extent[2]};
+    double h[4];
+    for (int rr = 0; rr < 4; ++rr) h[rr] = M[4 * rr] * c[0] + M[4 * rr + 1] * c[1] + M[4 * rr + 2] * c[2] + M[4 * rr + 3];
+    if (!(h[3] > 1e-6)) return;  // a corner at or behind the eye: keep the whole frame
+    const double px = (h[0] / h[3] + 1.0) * 0.5 * f.width - 0.5, py = (1.0 - h[1] / h[3]) * 0.5 * f.height - 0.5;
+    x0 = std::min(x0, px); x1 = std::max(x1, px);
+    y0 = std::min(y0, py); y1 = std::max(y1, py);
+  }
+  const int th = 32 / f.tile_w;
+  const long long px0 = std::max<long long>(0, (long long)std::floor(x0) - 1);
+  const long long px1 = std::min<long long>(f.width - 1, (long long)std::ceil(x1) + 1);
+  const long long py0 = std::max<long long>(0, (long long)std::floor(y0) - 1);
+  const long long py1 = std::min<long long>(f.height - 1, (long long)std::ceil(y1) + 1);
+  if (px0 > px1 || py0 > py1) {
+    f.ntx = f.nty = 0;  // the volume is outside the frame
+    return;
+  }
+  f.tx0 = (int)(px0 / f.tile_w);
+  f.ty0 = (int)(py0 / th);
+  f.ntx = (int)(px1 / f.tile_w) - f.tx0 + 1;
+  f.nty = (int)(py1 / th) - f.ty0 + 1;
+  (void)r;
 }
 
 // Cached graphs bake in device and pinned pointers: drop them whenever a
@@ -1555,8 +1595,9 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   int total = 0;
   for (int v = 0; v < n; ++v) {
     hf[v] = make_frame(r, views[v].view, views[v].proj, level, v);
+    cull_tiles(hf[v], r, views[v].view, views[v].proj);
     hp[v] = total;
-    total += hf[v].tiles_x * hf[v].tiles_y;
+    total += hf[v].ntx * hf[v].nty;
   }
   hp[n] = total;
   if (PtrSnapshot(r) != before) r->drop_graphs();
@@ -1579,6 +1620,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     // per-view parts, read from each view's own descriptor
     memset(shared.inv_vp, 0, sizeof(shared.inv_vp));
     memset(shared.light_to, 0, sizeof(shared.light_to));
+    shared.tx0 = shared.ty0 = shared.ntx = shared.nty = 0;
     shared.out_rgba8 = nullptr;
     shared.out_f32 = nullptr;
     shared.samples = nullptr;
@@ -1588,6 +1630,30 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   const int max_per_sm = uniform ? r->max_ctas_per_sm_u[r->mode] : r->max_ctas_per_sm;
   const int per_sm = r->ctas_per_sm > 0 ? std::min(r->ctas_per_sm, max_per_sm) : max_per_sm;
   const int grid = r->sm_count * per_sm;
+  if (n == 1) {
+    // a single view (gbvr_paint): a direct launch; its descriptor changes
+    // with every dataset, TF and size, which would re-capture a graph each time
+    CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_frames.p, r->h_frames.p, sizeof(FrameDesc), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_prefix.p, r->h_prefix.p, sizeof(int) * 2, cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemsetAsync(r->d_counter.p, 0, sizeof(int), r->stream));
+    CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long), r->stream));
+    CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)r->ds.levels[level].nbricks, r->stream));
+    if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words, r->stream));
+    CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
+    CUDA_TRY(launch_fill_outside(r->d_frames.as<FrameDesc>(), 1, r->width, r->height, r->stream));
+    cudaError_t le =
+        uniform ? launch_render_persistent_uniform(r->ds.dtype, r->mode, r->sampler, shared, r->d_frames.as<FrameDesc>(),
+                                                   1, r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid,
+                                                   r->stream)
+                : launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), 1,
+                                                 r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid, r->stream);
+    if (le != cudaSuccess) return cuda_fail(le, "persistent launch");
+    CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
+    CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
+    r->last_h2d = sizeof(FrameDesc) + sizeof(int) * 2;
+    return finish(r, 1, level);
+  }
   gbvr_renderer::GraphKey key{n, r->width, r->height, level, r->ds.dtype, r->mode, r->sampler, grid, r->d_fb8.p, r->d_fb32.p};
   auto it = r->graphs.find(key);
   if (it != r->graphs.end() &&
@@ -1627,6 +1693,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
   if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words * n, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
+  CUDA_TRY(launch_fill_outside(r->d_frames.as<FrameDesc>(), n, r->width, r->height, r->stream));
   CUDA_TRY(cudaGraphLaunch(it->second.exec, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));

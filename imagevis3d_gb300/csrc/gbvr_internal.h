@@ -80,6 +80,10 @@ struct __align__(16) FrameDesc {
   float inv_vp[16];          // row-major inverse of proj*view
   int width, height;
   int tiles_x, tiles_y;
+  // the view's ray tiles that can meet the volume: tx0 .. tx0 + ntx - 1 by
+  // ty0 .. ty0 + nty - 1 (the whole frame unless a batch culls it); pixels
+  // outside hold the background
+  int tx0, ty0, ntx, nty;
   // empty-space skipping: 0 none, 1 whole bricks, 2 bricks and macro-cells
   int empty_skip;
   const unsigned char* occ; // per macro-cell: capped distance (cells) to one that may contribute
@@ -139,6 +143,9 @@ cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, con
                                            int nframes, const int* tile_prefix, int total_tiles,
                                            int* counter, int grid, cudaStream_t s);
 int persistent_grid_size(int device);
+// Background (RGBA = bg, 0) into every pixel of each frame outside its tile
+// rectangle, as a ray that misses the volume leaves it.
+cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int width, int height, cudaStream_t s);
 // Batches whose views share everything but camera, light direction, outputs
 // and counters: the shared part travels as a kernel parameter (constant
 // bank), each view's part is read from `frames` (camera, light direction,

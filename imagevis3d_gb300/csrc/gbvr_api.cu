@@ -1435,6 +1435,8 @@ int paint_plain(gbvr_renderer* r, const gbvr_view* views, int n) {
       else { default_camera(r, dv, dp); vw = dv; pj = dp; }
     }
     FrameDesc f = make_frame(r, vw, pj, level, v);
+    cull_tiles(f, r, vw, pj);
+    CUDA_TRY(launch_fill_outside_one(f, r->stream));
     CUDA_TRY(launch_render_plain(f, r->stream));
   }
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
@@ -1560,6 +1562,8 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
     FrameDesc f = make_frame(r, views[i].view, views[i].proj, level, i);
     f.touched = r->stats_level >= 1 ? r->d_touched.as<unsigned char>() + (size_t)i * nb0 : nullptr;
     f.cell_touched = nullptr;
+    cull_tiles(f, r, views[i].view, views[i].proj);
+    CUDA_TRY(launch_fill_outside_one(f, r->stream));
     CUDA_TRY(launch_render_plain(f, r->stream));
     CUDA_TRY(cudaEventRecord(r->ev_done[st], r->stream));
     if (lod_out) lod_out[i] = level;
@@ -2581,6 +2585,7 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
   struct Group { int first, count, prefix_at, total, dtype, mode; };
   std::vector<Group> groups;
   int pcur = 0;
+  long long max_pix = 0;
   for (int i = 0; i < n; ++i) {
     const ServerRequest* q = slot.reqs[i];
     const Dataset& ds = *s->datasets[q->req.dataset];
@@ -2621,6 +2626,8 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
     fill_frame(hf[i], ds, p);
     hf[i].out_rgba8 = (uchar4*)((char*)slot.d_fb.p + slot.fb_off[i]);
     hf[i].samples = slot.d_samples.as<unsigned long long>() + i;
+    cull_tiles(hf[i], nullptr, p.view, p.proj);
+    max_pix = std::max(max_pix, (long long)p.width * p.height);
     const int dt = ds.dtype, md = t.mode;
     if (groups.empty() || groups.back().dtype != dt || groups.back().mode != md) {
       if (!groups.empty()) {
@@ -2632,7 +2639,7 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
     }
     Group& g = groups.back();
     hp[g.prefix_at + g.count] = g.total;
-    g.total += hf[i].tiles_x * hf[i].tiles_y;
+    g.total += hf[i].ntx * hf[i].nty;
     ++g.count;
   }
   if (!groups.empty()) {
@@ -2646,6 +2653,9 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
   CUDA_TRY(cudaMemcpyAsync(slot.d_prefix.p, hp, sizeof(int) * pcur, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemsetAsync(slot.d_counter.p, 0, sizeof(int) * 16, st));
   CUDA_TRY(cudaMemsetAsync(slot.d_samples.p, 0, sizeof(unsigned long long) * n, st));
+  // background outside each request's tile rectangle (frames differ in size:
+  // the grid covers the largest, each thread checks its own frame)
+  CUDA_TRY(launch_fill_outside(slot.d_frames.as<FrameDesc>(), n, (int)std::min<long long>(max_pix, 1LL << 30), 1, st));
   const int grid = s->sm_count * s->max_ctas;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const Group& g = groups[gi];

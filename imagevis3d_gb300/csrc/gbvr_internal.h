@@ -146,6 +146,7 @@ int persistent_grid_size(int device);
 // Background (RGBA = bg, 0) into every pixel of each frame outside its tile
 // rectangle, as a ray that misses the volume leaves it.
 cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int width, int height, cudaStream_t s);
+cudaError_t launch_fill_outside_one(const FrameDesc& f, cudaStream_t s);
 // Batches whose views share everything but camera, light direction, outputs
 // and counters: the shared part travels as a kernel parameter (constant
 // bank), each view's part is read from `frames` (camera, light direction,

@@ -655,9 +655,7 @@ __global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const F
   }
 }
 
-__global__ void k_fill_outside(const FrameDesc* __restrict__ frames, int width, int height) {
-  const FrameDesc& f = frames[blockIdx.y];
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void fill_outside_pixel(const FrameDesc& f, long long p) {
   if (p >= (long long)f.width * f.height) return;
   const int x = (int)(p % f.width), y = (int)(p / f.width);
   const int th = 32 / f.tile_w;
@@ -668,6 +666,22 @@ __global__ void k_fill_outside(const FrameDesc* __restrict__ frames, int width, 
     f.out_rgba8[p] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
                                  (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
                                  (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f), 0);
+}
+
+__global__ void k_fill_outside(const FrameDesc* __restrict__ frames, int width, int height) {
+  fill_outside_pixel(frames[blockIdx.y], (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void k_fill_outside_one(const __grid_constant__ FrameDesc f) {
+  fill_outside_pixel(f, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+cudaError_t launch_fill_outside_one(const FrameDesc& f, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (f.ntx == f.tiles_x && f.nty == f.tiles_y) return cudaSuccess;  // nothing outside
+  const long long npix = (long long)f.width * f.height;
+  k_fill_outside_one<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(f);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int width, int height, cudaStream_t s) {
@@ -916,7 +930,7 @@ cudaError_t launch_classify_cells(const float2* cells, long long n, const int* p
 template <typename T, int MODE, int SAMPLER>
 static cudaError_t plain_t(const FrameDesc& f, cudaStream_t s) {
   (void)cudaGetLastError();
-  int tiles = f.tiles_x * f.tiles_y;
+  int tiles = f.ntx * f.nty;  // the frame's tile rectangle (the whole frame unless culled)
   int warps_per_block = RENDER_THREADS / 32;
   int blocks = (tiles + warps_per_block - 1) / warps_per_block;
   if (blocks == 0) return cudaSuccess;

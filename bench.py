@@ -138,10 +138,12 @@ def run_reference(args):
     if rank != 0:
         return 0
     import numpy as np
-    from imagevis3d_gb300 import synth_volume, workloads
+    from imagevis3d_gb300 import workloads
     from oracle import orc
     wl = workloads.config2(nviews=64)
-    vol = synth_volume(wl.synth) if not args.cpu_volume else orc.synth_blobs(wl.synth)
+    # the input volume from the CPU generator (bit-identical to the GPU one):
+    # nothing of the GPU library runs on this arm
+    vol = orc.synth_blobs(wl.synth)
     threads = orc.max_threads()
     view, proj = wl.views[0]
     for _ in range(args.warmup):

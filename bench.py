@@ -779,7 +779,7 @@ def main():
                          "kernel_ms": 1000.0 * ksec / args.steps,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if pk else "fallback"},
             "cpu_baseline": cpu,
-            "gpu_launches": args.steps,
+            "gpu_launches": 2 * args.steps,  # per step: the background fill and the persistent raycast
             "clocks": clk,
             "stats_last_step": {k: st_last[k] for k in ("samples", "bricks_touched", "bricks_skipped",
                                                          "brick_bytes")},

@@ -945,7 +945,7 @@ struct gbvr_renderer {
   int last_views = 0, last_level = 0;
   float last_ms = 0.f, last_kernel_ms = 0.f;
   uint64_t last_h2d = 0;
-  int max_ctas_per_sm = 0, max_ctas_per_sm_u[4] = {0, 0, 0, 0}, sm_count = 0;
+  int max_ctas_per_sm[4] = {0, 0, 0, 0}, max_ctas_per_sm_u[4] = {0, 0, 0, 0}, sm_count = 0;
   // graph cache for the batch launch
   struct GraphKey {
     int n, w, h, level, dtype, mode, sampler, grid;
@@ -1609,9 +1609,10 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
-    r->max_ctas_per_sm = std::max(1, persistent_grid_size(dev) / std::max(r->sm_count, 1));
-    for (int m = 0; m < 4; ++m)
+    for (int m = 0; m < 4; ++m) {
+      r->max_ctas_per_sm[m] = std::max(1, persistent_grid_size(dev, m) / std::max(r->sm_count, 1));
       r->max_ctas_per_sm_u[m] = std::max(1, persistent_grid_size_uniform(dev, m) / std::max(r->sm_count, 1));
+    }
   }
   // Views of one renderer batch share everything but camera, outputs and
   // counters, unless they sample different brick layout copies: then the
@@ -1631,7 +1632,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
     shared.touched_stride = shared.touched ? r->ds.levels[level].nbricks : 0;
     shared.cell_touched_stride = shared.cell_touched ? r->cell_words : 0;
   }
-  const int max_per_sm = uniform ? r->max_ctas_per_sm_u[r->mode] : r->max_ctas_per_sm;
+  const int max_per_sm = uniform ? r->max_ctas_per_sm_u[r->mode] : r->max_ctas_per_sm[r->mode];
   const int per_sm = r->ctas_per_sm > 0 ? std::min(r->ctas_per_sm, max_per_sm) : max_per_sm;
   const int grid = r->sm_count * per_sm;
   if (n == 1) {
@@ -2520,7 +2521,7 @@ struct BatchSlot {
 struct gbvr_server {
   gbvr_server_params params;
   int device = 0;
-  int sm_count = 0, max_ctas = 1;
+  int sm_count = 0, max_ctas[4] = {1, 1, 1, 1};
   cudaStream_t stream = nullptr;
   std::vector<std::unique_ptr<Dataset>> datasets;
   std::vector<std::unique_ptr<ServerTf>> tfs;
@@ -2656,9 +2657,9 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
   // background outside each request's tile rectangle (frames differ in size:
   // the grid covers the largest, each thread checks its own frame)
   CUDA_TRY(launch_fill_outside(slot.d_frames.as<FrameDesc>(), n, (int)std::min<long long>(max_pix, 1LL << 30), 1, st));
-  const int grid = s->sm_count * s->max_ctas;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const Group& g = groups[gi];
+    const int grid = s->sm_count * s->max_ctas[g.mode];
     CUDA_TRY(launch_render_persistent_typed(g.dtype, g.mode, GBVR_SAMPLER_SW, slot.d_frames.as<FrameDesc>() + g.first,
                                             g.count, slot.d_prefix.as<int>() + g.prefix_at, g.total,
                                             slot.d_counter.as<int>() + gi, grid, st));
@@ -2803,7 +2804,7 @@ int gbvr_server_create(const gbvr_server_params* params, gbvr_server** out) {
   s->params = p;
   CUDA_TRY(cudaGetDevice(&s->device));
   CUDA_TRY(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device));
-  s->max_ctas = std::max(1, persistent_grid_size(s->device) / std::max(s->sm_count, 1));
+  for (int m = 0; m < 4; ++m) s->max_ctas[m] = std::max(1, persistent_grid_size(s->device, m) / std::max(s->sm_count, 1));
   CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   for (auto& slot : s->slots) {
     CUDA_TRY(cudaEventCreate(&slot.ev0));

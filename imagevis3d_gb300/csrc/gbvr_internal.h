@@ -142,7 +142,7 @@ cudaError_t launch_count_bits(const unsigned* bits, long long words, int n_frame
 cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, const FrameDesc* frames,
                                            int nframes, const int* tile_prefix, int total_tiles,
                                            int* counter, int grid, cudaStream_t s);
-int persistent_grid_size(int device);
+int persistent_grid_size(int device, int mode);
 // Background (RGBA = bg, 0) into every pixel of each frame outside its tile
 // rectangle, as a ray that misses the volume leaves it.
 cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int width, int height, cudaStream_t s);

@@ -641,7 +641,8 @@ __device__ __forceinline__ int find_frame(const int* __restrict__ prefix, int nf
 }
 
 template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS, 8) k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
+__global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
+    k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
                                                          const int* __restrict__ tile_prefix, int total,
                                                          int* __restrict__ counter) {
   const int lane = threadIdx.x & 31;
@@ -1019,11 +1020,15 @@ int persistent_grid_size_uniform(int device, int mode) {
   return sms * per_sm;
 }
 
-int persistent_grid_size(int device) {
+int persistent_grid_size(int device, int mode) {
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent<uint16_t, MODE_1D, SAMPLER_SW>,
-                                                RENDER_THREADS, 0);
+  if (mode == MODE_1D || mode == MODE_MIP)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent<uint16_t, MODE_1D, SAMPLER_SW>,
+                                                  RENDER_THREADS, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent<uint16_t, MODE_2D, SAMPLER_SW>,
+                                                  RENDER_THREADS, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }

@@ -416,7 +416,7 @@ def run_c4(args):
         "cpu_baseline": {"value": cpu_pix_s / (wl.width * wl.height) if cpu_pix_s else None, "unit": "frames/s",
                          "cores": orc.max_threads(), "kind": "port",
                          "sample": "4096 seeded pixels of one frame at its resolved level"},
-        "build_s": build_s, "gpu_launches": frames * (len(passes) + 2), "clocks": clocks,
+        "build_s": build_s, "gpu_launches": 2 * frames * (len(passes) + 2), "clocks": clocks,
     }
     print(json.dumps(out))
     return 0

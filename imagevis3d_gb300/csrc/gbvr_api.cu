@@ -1190,8 +1190,9 @@ struct PtrSnapshot {
 // takes the level's page table and the skip table from the page-locked
 // staging of `stage`.  A frame still rendering keeps its slots: `protect` is
 // its stamp (0: none), and if the new frame cannot be placed without them the
-// call first waits for `protect_done`.  The staging of `stage` must be free
-// (its previous uploads complete) when this is called.
+// copies wait on the GPU for `protect_done` (that frame's end) before they
+// overwrite anything.  The staging of `stage` must be free (its previous
+// uploads complete) when this is called.
 int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64_t protect, cudaEvent_t protect_done,
              int stage, uint64_t* misses_out, uint64_t* bytes_out) {
   Dataset& ds = r->ds;
@@ -1287,6 +1288,7 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
   size_t missing = 0;
   for (int bidx : needed) missing += ds.slot_of[bidx] < 0;
   std::vector<int> victims;
+  bool wait_protected = false;
   for (int pass = 0; pass < 2; ++pass) {
     const bool guard = protect != 0 && pass == 0;
     victims.clear();
@@ -1294,7 +1296,9 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
       if (ds.slot_brick[sl] < 0 || (!want[ds.slot_brick[sl]] && !(guard && ds.slot_used[sl] == protect)))
         victims.push_back(sl);
     if (victims.size() >= missing || !guard) break;
-    if (protect_done) CUDA_TRY(cudaEventSynchronize(protect_done));
+    // no room without the frame still rendering: its slots become victims
+    // and the copies wait for it on the GPU (the host keeps going)
+    wait_protected = protect_done != nullptr;
   }
   std::sort(victims.begin(), victims.end(), [&](int x, int y) {
     const bool fx = ds.slot_brick[x] < 0, fy = ds.slot_brick[y] < 0;
@@ -1308,6 +1312,8 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
     // slots are overwritten only after every earlier paint has read them
     CUDA_TRY(cudaEventRecord(r->ev_c0[stage], r->stream));
     CUDA_TRY(cudaStreamWaitEvent(r->copy_stream, r->ev_c0[stage], 0));
+  } else if (wait_protected) {
+    CUDA_TRY(cudaStreamWaitEvent(r->copy_stream, protect_done, 0));
   }
   CUDA_TRY(cudaEventRecord(r->ev_c0[stage], r->copy_stream));
   for (int bidx : needed) {

@@ -2469,13 +2469,13 @@ int gbvr_orbit_camera(float azimuth_deg, float elevation_deg, float radius, floa
 // Serving loop: many resident datasets and transfer functions, requests from
 // any thread, continuous batching into persistent launches.
 //
-// A worker thread owns the GPU side.  Three batch slots rotate: while one
+// A worker thread owns the GPU side.  Two batch slots alternate: while one
 // batch renders, the next is assembled from the requests that arrived and
 // queued behind it on the same stream, so the GPU is not idle between
-// batches, and a finished batch can be handed back to its callers meanwhile.
-// A batch takes pending requests in arrival order until it holds max_batch
-// requests or its framebuffer area (a third of fb_budget_bytes) is full;
-// requests that do not fit wait for the next batch (admission by memory).  Within a batch, requests are grouped by voxel type and render
+// batches.  A batch takes pending requests in arrival order until it holds
+// max_batch requests or its framebuffer area (half of fb_budget_bytes) is
+// full; requests that do not fit wait for the next batch (admission by
+// memory).  Within a batch, requests are grouped by voxel type and render
 // mode (one persistent launch each, all queued back to back).  Every ray is
 // computed independently of the batch it lands in, so a request's image is
 // the same alone and in any mix.
@@ -2531,8 +2531,7 @@ struct gbvr_server {
   cudaStream_t stream = nullptr;
   std::vector<std::unique_ptr<Dataset>> datasets;
   std::vector<std::unique_ptr<ServerTf>> tfs;
-  static constexpr int kSlots = 3;  // one rendering, one queued behind it, one being retired
-  BatchSlot slots[kSlots];
+  BatchSlot slots[2];
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<ServerRequest*> pending;
@@ -2678,11 +2677,10 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
 
 void server_worker(gbvr_server* s) {
   cudaSetDevice(s->device);
-  const size_t slot_budget = s->params.fb_budget_bytes / gbvr_server::kSlots;
+  const size_t slot_budget = s->params.fb_budget_bytes / 2;
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
-    bool in_flight = false;
-    for (auto& sl : s->slots) in_flight = in_flight || sl.busy;
+    const bool in_flight = s->slots[0].busy || s->slots[1].busy;
     if (in_flight) {
       // poll the batch in flight, waking early when new requests arrive so
       // a free slot can be filled and queued behind it
@@ -2690,7 +2688,7 @@ void server_worker(gbvr_server* s) {
     } else {
       s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty(); });
     }
-    if (s->stop && s->pending.empty() && !in_flight) break;
+    if (s->stop && s->pending.empty() && !s->slots[0].busy && !s->slots[1].busy) break;
     // fill every free slot with pending requests
     for (auto& slot : s->slots) {
       if (slot.busy || s->pending.empty()) continue;
@@ -2817,8 +2815,8 @@ int gbvr_server_create(const gbvr_server_params* params, gbvr_server** out) {
   for (auto& slot : s->slots) {
     CUDA_TRY(cudaEventCreate(&slot.ev0));
     CUDA_TRY(cudaEventCreate(&slot.ev1));
-    CUDA_TRY(slot.d_fb.alloc(p.fb_budget_bytes / gbvr_server::kSlots));
-    CUDA_TRY(slot.h_fb.alloc(p.fb_budget_bytes / gbvr_server::kSlots));
+    CUDA_TRY(slot.d_fb.alloc(p.fb_budget_bytes / 2));
+    CUDA_TRY(slot.h_fb.alloc(p.fb_budget_bytes / 2));
   }
   gbvr_server* raw = s.get();
   s->worker = std::thread(server_worker, raw);

@@ -365,9 +365,9 @@ int gbvr_dev_synth_volume_noalloc(const gbvr_synth_params* p, void* dev_out, siz
  * renders requests submitted from any thread.  A worker thread batches the
  * pending requests into persistent launches: a batch takes requests in
  * arrival order until it holds max_batch of them or its framebuffer area
- * (a third of fb_budget_bytes: one batch renders, one waits behind it and
- * one is handed back) is full; the rest wait for the next batch, which is
- * assembled while the current one renders.  A request's image does not depend on the batch it lands in.
+ * (half of fb_budget_bytes; two batches are in flight) is full; the rest
+ * wait for the next batch, which is assembled while the current one
+ * renders.  A request's image does not depend on the batch it lands in.
  * No counterpart in the reference (its GUI renders one window per paint,
  * ImageVis3D/UI/RenderWindow.cpp:2453-2502). */
 typedef struct gbvr_server gbvr_server;

@@ -89,8 +89,7 @@ def test_mix_alone_and_renderer_agree(setup):
 
 def test_admission_limits(setup):
     vols, _, tfs, owners = setup
-    # three batch slots, each exactly one 64x64 RGBA8 frame
-    with Server(max_batch=4, fb_budget_bytes=3 * 64 * 64 * 4) as srv:
+    with Server(max_batch=4, fb_budget_bytes=2 * 64 * 64 * 4) as srv:
         d = srv.add_synthetic(vols[0], brick_size=64, overlap=2)
         t = srv.add_tf(d, tfs[0][0], tfs[0][1])
         cam = orbit_camera(10.0, 10.0, 2.5 * workloads.DIAG, 45.0, 64, 64)

@@ -444,7 +444,7 @@ def run_c5(args):
                                   noise_kind=2, noise_amp=0.02 * scale, vmax=vmax))
     img_sizes = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
     nreq = args.requests
-    srv = Server(max_batch=64, fb_budget_bytes=1 << 30)
+    srv = Server(max_batch=args.max_batch, fb_budget_bytes=1 << 30)
     ds, presets = [], []
     for i, sp in enumerate(specs):
         d = srv.add_synthetic(sp, brick_size=256, overlap=2, layouts=1)
@@ -543,7 +543,7 @@ def run_c5(args):
         "ms_per_step": 1000.0 / max(st["frames_per_s"], 1e-9), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded blob volumes)",
         "config": {"workload": "c5_serving_12_datasets_%d_requests" % nreq, "datasets": "64^3..1024^3 u8/u16/f32",
-                   "image_sizes": img_sizes, "arrival_rate_per_s": rate, "max_batch": 64},
+                   "image_sizes": img_sizes, "arrival_rate_per_s": rate, "max_batch": args.max_batch},
         "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"], "mean_batch": st["mean_batch"],
         "burst_capacity_fps": capacity, "burst_p99_ms": burst["p99_ms"],
         "plain_per_request_fps": plain_fps, "plain_p50_ms": lat[len(lat) // 2],
@@ -572,6 +572,7 @@ def main():
     ap.add_argument("--pool-gib", type=float, default=0.0)
     ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--plain-requests", type=int, default=600)
+    ap.add_argument("--max-batch", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -138,6 +138,9 @@ SIGNATURES = {
     "gbvr_set_clip_plane": [P, I, FP],
     "gbvr_paint_slice": [P, I, C.c_int64, I, I, I],
     "gbvr_paint_path": [P, C.POINTER(View), I, C.POINTER(C.c_int32), U64P, U64P],
+    "gbvr_paint_batch_async": [P, C.POINTER(View), I, I],
+    "gbvr_read_framebuffers_async": [P, I, I, I, P, SZ],
+    "gbvr_wait_async": [P],
     "gbvr_set_tf1d": [P, FP, I],
     "gbvr_set_tf2d": [P, FP, I, I, F],
     "gbvr_set_value_range": [P, D, D],

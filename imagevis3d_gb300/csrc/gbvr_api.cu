@@ -66,6 +66,10 @@ struct DevBuf {
     p = nullptr;
     n = 0;
   }
+  void swap(DevBuf& o) {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+  }
   cudaError_t alloc(size_t bytes) {
     if (bytes <= n && p) return cudaSuccess;
     release();
@@ -82,6 +86,10 @@ struct PinnedBuf {
   void* p = nullptr;
   size_t n = 0;
   ~PinnedBuf() { if (p) cudaFreeHost(p); }
+  void swap(PinnedBuf& o) {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+  }
   cudaError_t alloc(size_t bytes) {
     if (bytes <= n && p) return cudaSuccess;
     if (p) cudaFreeHost(p);
@@ -939,6 +947,36 @@ struct gbvr_renderer {
   float last_page_ms = 0.f;
   long long cell_words = 0;
   PinnedBuf h_frames, h_prefix;
+  // Asynchronous batches use two sets of batch buffers ("slots"): the set of
+  // the slot in use sits in the members above, the other one here, and
+  // selecting a slot swaps them.  Per slot: its render's end and its
+  // read-back's end.
+  struct SlotBufs {
+    DevBuf fb8, fb32, frames, prefix, counter, samples, touched, cellbits;
+    PinnedBuf h_frames, h_prefix;
+    int fb_views = 0, fb_w = 0, fb_h = 0;
+  } other;
+  int cur_slot = 0;
+  cudaStream_t read_stream = nullptr;
+  cudaEvent_t slot_rendered[2] = {nullptr, nullptr}, slot_read[2] = {nullptr, nullptr};
+  bool slot_render_pending[2] = {false, false}, slot_read_pending[2] = {false, false};
+  void select_slot(int slot) {
+    if (slot == cur_slot) return;
+    d_fb8.swap(other.fb8);
+    d_fb32.swap(other.fb32);
+    d_frames.swap(other.frames);
+    d_prefix.swap(other.prefix);
+    d_counter.swap(other.counter);
+    d_samples.swap(other.samples);
+    d_touched.swap(other.touched);
+    d_cellbits.swap(other.cellbits);
+    h_frames.swap(other.h_frames);
+    h_prefix.swap(other.h_prefix);
+    std::swap(fb_views, other.fb_views);
+    std::swap(fb_w, other.fb_w);
+    std::swap(fb_h, other.fb_h);
+    cur_slot = slot;
+  }
   bool tf_dirty = true, skip_dirty = true;
   int skip_level = -1;
   int fb_views = 0, fb_w = 0, fb_h = 0;
@@ -973,6 +1011,11 @@ struct gbvr_renderer {
     if (ev1) cudaEventDestroy(ev1);
     if (evk0) cudaEventDestroy(evk0);
     if (evk1) cudaEventDestroy(evk1);
+    for (int k = 0; k < 2; ++k) {
+      if (slot_rendered[k]) cudaEventDestroy(slot_rendered[k]);
+      if (slot_read[k]) cudaEventDestroy(slot_read[k]);
+    }
+    if (read_stream) cudaStreamDestroy(read_stream);
     for (int k = 0; k < 2; ++k) {
       if (ev_c0[k]) cudaEventDestroy(ev_c0[k]);
       if (ev_c1[k]) cudaEventDestroy(ev_c1[k]);
@@ -1416,6 +1459,18 @@ int prepare(gbvr_renderer* r, int nviews, int& level, const gbvr_view* views) {
   return GBVR_OK;
 }
 
+// The synchronous calls first let queued asynchronous work finish, so they
+// never overwrite framebuffers a read-back still copies.
+int settle_async(gbvr_renderer* r) {
+  if (!r->read_stream) return GBVR_OK;
+  if (r->slot_render_pending[0] || r->slot_render_pending[1] || r->slot_read_pending[0] || r->slot_read_pending[1]) {
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->read_stream));
+    for (int k = 0; k < 2; ++k) r->slot_render_pending[k] = r->slot_read_pending[k] = false;
+  }
+  return GBVR_OK;
+}
+
 int finish(gbvr_renderer* r, int nviews, int level) {
   CUDA_TRY(cudaEventSynchronize(r->ev1));
   CUDA_TRY(cudaEventElapsedTime(&r->last_ms, r->ev0, r->ev1));
@@ -1589,8 +1644,14 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
   return finish(r, n, level);
 }
 
-int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
+// async: the step of a pipeline (gbvr_paint_batch_async): returns once the
+// work is queued; the staging of the slot is reused only after the slot's
+// previous render has consumed it, and the framebuffers only after their
+// previous read-back.
+int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = false) {
   int level;
+  const int slot = r->cur_slot;
+  if (async && r->slot_read_pending[slot]) CUDA_TRY(cudaStreamWaitEvent(r->stream, r->slot_read[slot], 0));
   const PtrSnapshot before(r);
   TRY(prepare(r, n, level, views));
   CUDA_TRY(r->h_frames.alloc(sizeof(FrameDesc) * n));
@@ -1599,7 +1660,11 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   CUDA_TRY(r->d_prefix.alloc(sizeof(int) * (n + 1)));
   CUDA_TRY(r->d_counter.alloc(sizeof(int)));
   // the previous replay may still read the pinned staging buffers
-  CUDA_TRY(cudaStreamSynchronize(r->stream));
+  if (async) {
+    if (r->slot_render_pending[slot]) CUDA_TRY(cudaEventSynchronize(r->slot_rendered[slot]));
+  } else {
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+  }
   FrameDesc* hf = (FrameDesc*)r->h_frames.p;
   int* hp = (int*)r->h_prefix.p;
   int total = 0;
@@ -1709,6 +1774,13 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
   r->last_h2d = sizeof(FrameDesc) * n + sizeof(int) * (n + 1);
+  if (async) {
+    CUDA_TRY(cudaEventRecord(r->slot_rendered[slot], r->stream));
+    r->slot_render_pending[slot] = true;
+    r->last_views = n;
+    r->last_level = level;
+    return GBVR_OK;
+  }
   return finish(r, n, level);
 }
 
@@ -2044,11 +2116,13 @@ int gbvr_set_render_mode(gbvr_renderer* r, int mode) {
 int gbvr_paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod, uint64_t* misses,
                     uint64_t* bytes_paged) {
   TRY(check_r(r));
+  TRY(settle_async(r));
   return paint_path(r, views, n, lod, misses, bytes_paged);
 }
 
 int gbvr_paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_y, int use_mip) {
   TRY(check_r(r));
+  TRY(settle_async(r));
   return paint_slice(r, axis, index, flip_x, flip_y, use_mip);
 }
 
@@ -2222,26 +2296,72 @@ int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_res
 
 int gbvr_paint(gbvr_renderer* r) {
   TRY(check_loaded(r));
+  TRY(settle_async(r));
   // One view: the per-view kernel.  A one-view persistent launch measured no
   // faster (1063 vs 1109 frames/s at 1920x1080): a single frame's time is set
   // by its slowest ray tiles, which only other views' work can hide.
   return paint_plain(r, nullptr, 1);
 }
 
+int gbvr_paint_batch_async(gbvr_renderer* r, const gbvr_view* views, int n, int slot) {
+  TRY(check_loaded(r));
+  if (!views || n <= 0) return fail(GBVR_EINVAL, "bad view list");
+  if (slot < 0 || slot > 1) return fail(GBVR_EINVAL, "slot must be 0 or 1");
+  if (r->ds.ooc) return fail(GBVR_ESTATE, "asynchronous batches need an in-core dataset");
+  if (!r->read_stream) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&r->read_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      CUDA_TRY(cudaEventCreateWithFlags(&r->slot_rendered[k], cudaEventDisableTiming));
+      CUDA_TRY(cudaEventCreateWithFlags(&r->slot_read[k], cudaEventDisableTiming));
+    }
+  }
+  r->select_slot(slot);
+  return paint_batch(r, views, n, true);
+}
+
+int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, void* host, size_t bytes) {
+  TRY(check_r(r));
+  if (slot < 0 || slot > 1 || !r->read_stream || !r->slot_render_pending[slot])
+    return fail(GBVR_ESTATE, "no asynchronous batch rendered into that slot");
+  const bool cur = slot == r->cur_slot;
+  const int w = cur ? r->fb_w : r->other.fb_w, h = cur ? r->fb_h : r->other.fb_h;
+  const int views = cur ? r->fb_views : r->other.fb_views;
+  const void* fb = cur ? r->d_fb8.p : r->other.fb8.p;
+  const size_t per = (size_t)w * h * 4;
+  if (first < 0 || n <= 0 || first + n > views) return fail(GBVR_EINVAL, "view range out of range");
+  if (!host || bytes < per * n) return fail(GBVR_EINVAL, "host buffer too small");
+  CUDA_TRY(cudaStreamWaitEvent(r->read_stream, r->slot_rendered[slot], 0));
+  CUDA_TRY(cudaMemcpyAsync(host, (const char*)fb + per * first, per * n, cudaMemcpyDeviceToHost, r->read_stream));
+  CUDA_TRY(cudaEventRecord(r->slot_read[slot], r->read_stream));
+  r->slot_read_pending[slot] = true;
+  return GBVR_OK;
+}
+
+int gbvr_wait_async(gbvr_renderer* r) {
+  TRY(check_r(r));
+  CUDA_TRY(cudaStreamSynchronize(r->stream));
+  if (r->read_stream) CUDA_TRY(cudaStreamSynchronize(r->read_stream));
+  for (int k = 0; k < 2; ++k) r->slot_render_pending[k] = r->slot_read_pending[k] = false;
+  return GBVR_OK;
+}
+
 int gbvr_paint_views(gbvr_renderer* r, const gbvr_view* views, int n) {
   TRY(check_loaded(r));
+  TRY(settle_async(r));
   if (!views) return fail(GBVR_EINVAL, "null views");
   return paint_plain(r, views, n);
 }
 
 int gbvr_paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
   TRY(check_loaded(r));
+  TRY(settle_async(r));
   if (!views) return fail(GBVR_EINVAL, "null views");
   return paint_batch(r, views, n);
 }
 
 int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t bytes) {
   TRY(check_r(r));
+  TRY(settle_async(r));
   const size_t need = (size_t)r->fb_w * r->fb_h * 4;
   if (view < 0 || view >= r->last_views) return fail(GBVR_EINVAL, "view index out of range");
   if (!rgba8 || bytes < need) return fail(GBVR_EINVAL, "framebuffer buffer too small");
@@ -2252,6 +2372,7 @@ int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t byt
 
 int gbvr_read_framebuffers(gbvr_renderer* r, int first, int n, uint8_t* rgba8, size_t bytes) {
   TRY(check_r(r));
+  TRY(settle_async(r));
   const size_t per = (size_t)r->fb_w * r->fb_h * 4;
   if (first < 0 || n <= 0 || first + n > r->last_views) return fail(GBVR_EINVAL, "view range out of range");
   if (!rgba8 || bytes < per * n) return fail(GBVR_EINVAL, "framebuffer buffer too small");
@@ -2262,6 +2383,7 @@ int gbvr_read_framebuffers(gbvr_renderer* r, int first, int n, uint8_t* rgba8, s
 
 int gbvr_read_framebuffer_f32(gbvr_renderer* r, int view, float* rgba, size_t bytes) {
   TRY(check_r(r));
+  TRY(settle_async(r));
   if (!r->d_fb32.p) return fail(GBVR_ESTATE, "renderer was created without the float framebuffer flag (1)");
   const size_t need = (size_t)r->fb_w * r->fb_h * 16;
   if (view < 0 || view >= r->last_views) return fail(GBVR_EINVAL, "view index out of range");

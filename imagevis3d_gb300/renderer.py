@@ -343,6 +343,23 @@ class Renderer:
         L.call("gbvr_paint_batch", self._h, arr, len(views))
         self._nviews = len(views)
 
+    def paintBatchAsync(self, views, slot):
+        """Queue a batch into framebuffer set `slot` (0/1) without waiting."""
+        arr = self._views(views)
+        L.call("gbvr_paint_batch_async", self._h, arr, len(views), slot)
+        self._nviews = len(views)
+
+    def readFramebuffersAsync(self, slot, out, first=0, n=None):
+        """Queue the read-back of views [first, first + n) of set `slot` into
+        `out` (page-locked memory for an overlap, e.g. a pinned torch tensor)."""
+        n = self._nviews - first if n is None else n
+        ptr = out.data_ptr() if hasattr(out, "data_ptr") else out.ctypes.data
+        nbytes = out.numel() * out.element_size() if hasattr(out, "numel") else out.nbytes
+        L.call("gbvr_read_framebuffers_async", self._h, slot, first, n, C.c_void_p(ptr), nbytes)
+
+    def waitAsync(self):
+        L.call("gbvr_wait_async", self._h)
+
     def paintViews(self, views):
         arr = self._views(views)
         L.call("gbvr_paint_views", self._h, arr, len(views))

@@ -257,6 +257,17 @@ int gbvr_paint(gbvr_renderer* r);
 int gbvr_paint_batch(gbvr_renderer* r, const gbvr_view* views, int n);
 int gbvr_paint_views(gbvr_renderer* r, const gbvr_view* views, int n);
 
+/* ---- asynchronous batches (a pipeline of steps; no counterpart in the reference, whose paint is
+ * synchronous) ----
+ * gbvr_paint_batch_async renders n views into framebuffer set `slot` (0 or 1, in-core datasets) and returns
+ * once the work is queued.  gbvr_read_framebuffers_async copies views of a set into host memory
+ * (page-locked for a true overlap) after that set's render, on its own stream, so the read-back of one step
+ * overlaps the render of the next; a set is rendered again only after its read-back.  gbvr_wait_async waits
+ * for everything queued.  The synchronous calls use set 0 whenever set 0 was selected last. */
+int gbvr_paint_batch_async(gbvr_renderer* r, const gbvr_view* views, int n, int slot);
+int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, void* host, size_t bytes);
+int gbvr_wait_async(gbvr_renderer* r);
+
 /* ---- readback (captureSingleFrame, RenderWindow.cpp:1642-1671; RGBA8 model
  * StandaloneTuvok/CmdRenderer.cpp:34-56).  Row 0 is the top image row. ---- */
 int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t bytes);

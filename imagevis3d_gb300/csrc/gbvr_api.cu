@@ -1720,10 +1720,9 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     CUDA_TRY(launch_fill_outside(r->d_frames.as<FrameDesc>(), 1, r->width, r->height, r->stream));
     cudaError_t le =
         uniform ? launch_render_persistent_uniform(r->ds.dtype, r->mode, r->sampler, shared, r->d_frames.as<FrameDesc>(),
-                                                   1, r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid,
-                                                   r->stream)
+                                                   1, r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream)
                 : launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), 1,
-                                                 r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid, r->stream);
+                                                 r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream);
     if (le != cudaSuccess) return cuda_fail(le, "persistent launch");
     CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
     CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
@@ -1747,11 +1746,9 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     CUDA_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t le =
         uniform ? launch_render_persistent_uniform(r->ds.dtype, r->mode, r->sampler, shared, r->d_frames.as<FrameDesc>(),
-                                                   n, r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid,
-                                                   r->stream)
+                                                   n, r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream)
                 : launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), n,
-                                                 r->d_prefix.as<int>(), total, r->d_counter.as<int>(), grid,
-                                                 r->stream);
+                                                 r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream);
     cudaError_t ce = cudaStreamEndCapture(r->stream, &g);
     if (le != cudaSuccess) return cuda_fail(le, "persistent launch capture");
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
@@ -2789,7 +2786,7 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
     const Group& g = groups[gi];
     const int grid = s->sm_count * s->max_ctas[g.mode];
     CUDA_TRY(launch_render_persistent_typed(g.dtype, g.mode, GBVR_SAMPLER_SW, slot.d_frames.as<FrameDesc>() + g.first,
-                                            g.count, slot.d_prefix.as<int>() + g.prefix_at, g.total,
+                                            g.count, slot.d_prefix.as<int>() + g.prefix_at,
                                             slot.d_counter.as<int>() + gi, grid, st));
   }
   CUDA_TRY(cudaMemcpyAsync(slot.h_fb.p, slot.d_fb.p, slot.fb_used, cudaMemcpyDeviceToHost, st));

@@ -139,9 +139,12 @@ cudaError_t launch_render_plain(const FrameDesc& f, cudaStream_t s);
 // popcount of n_frames bitmaps of `words` words each into counts[n_frames]
 cudaError_t launch_count_bits(const unsigned* bits, long long words, int n_frames, unsigned long long* counts,
                               cudaStream_t s);
+// tile_prefix[0..nframes]: the first tile of each frame and, last, the total;
+// the kernels read the total from device memory, so a graph replay takes the
+// count of the descriptors uploaded before it
 cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, const FrameDesc* frames,
-                                           int nframes, const int* tile_prefix, int total_tiles,
-                                           int* counter, int grid, cudaStream_t s);
+                                           int nframes, const int* tile_prefix, int* counter, int grid,
+                                           cudaStream_t s);
 int persistent_grid_size(int device, int mode);
 // Background (RGBA = bg, 0) into every pixel of each frame outside its tile
 // rectangle, as a ray that misses the volume leaves it.
@@ -152,7 +155,7 @@ cudaError_t launch_fill_outside_one(const FrameDesc& f, cudaStream_t s);
 // bank), each view's part is read from `frames` (camera, light direction,
 // outputs, sample counter).
 cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, const FrameDesc& shared,
-                                             const FrameDesc* frames, int nframes, const int* prefix, int total,
+                                             const FrameDesc* frames, int nframes, const int* tile_prefix,
                                              int* counter, int grid, cudaStream_t s);
 int persistent_grid_size_uniform(int device, int mode);
 cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStream_t s);

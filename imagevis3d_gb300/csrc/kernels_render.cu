@@ -643,9 +643,10 @@ __device__ __forceinline__ int find_frame(const int* __restrict__ prefix, int nf
 template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
     k_render_persistent(const FrameDesc* __restrict__ frames, int nframes,
-                                                         const int* __restrict__ tile_prefix, int total,
+                                                         const int* __restrict__ tile_prefix,
                                                          int* __restrict__ counter) {
   const int lane = threadIdx.x & 31;
+  const int total = __ldg(tile_prefix + nframes);
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(counter, 1);
@@ -784,8 +785,9 @@ cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStr
 template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
     k_render_persistent_u(const __grid_constant__ FrameDesc shared, const FrameDesc* __restrict__ frames,
-                          int nframes, const int* __restrict__ tile_prefix, int total, int* __restrict__ counter) {
+                          int nframes, const int* __restrict__ tile_prefix, int* __restrict__ counter) {
   const int lane = threadIdx.x & 31;
+  const int total = __ldg(tile_prefix + nframes);
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(counter, 1);
@@ -940,19 +942,18 @@ static cudaError_t plain_t(const FrameDesc& f, cudaStream_t s) {
 }
 
 template <typename T, int MODE, int SAMPLER>
-static cudaError_t persistent_t(const FrameDesc* frames, int nframes, const int* prefix, int total, int* counter,
-                                int grid, cudaStream_t s) {
+static cudaError_t persistent_t(const FrameDesc* frames, int nframes, const int* prefix, int* counter, int grid,
+                                cudaStream_t s) {
   (void)cudaGetLastError();
-  k_render_persistent<T, MODE, SAMPLER><<<grid, RENDER_THREADS, 0, s>>>(frames, nframes, prefix, total, counter);
+  k_render_persistent<T, MODE, SAMPLER><<<grid, RENDER_THREADS, 0, s>>>(frames, nframes, prefix, counter);
   return cudaGetLastError();
 }
 
 template <typename T, int MODE, int SAMPLER>
 static cudaError_t persistent_u_t(const FrameDesc& shared, const FrameDesc* frames, int nframes, const int* prefix,
-                                  int total, int* counter, int grid, cudaStream_t s) {
+                                  int* counter, int grid, cudaStream_t s) {
   (void)cudaGetLastError();
-  k_render_persistent_u<T, MODE, SAMPLER><<<grid, RENDER_THREADS, 0, s>>>(shared, frames, nframes, prefix, total,
-                                                                         counter);
+  k_render_persistent_u<T, MODE, SAMPLER><<<grid, RENDER_THREADS, 0, s>>>(shared, frames, nframes, prefix, counter);
   return cudaGetLastError();
 }
 
@@ -995,16 +996,16 @@ cudaError_t launch_render_plain(const FrameDesc& f, cudaStream_t s) {
 // All frames of one persistent launch share dtype, mode and sampler (the
 // host groups a mixed batch by these and issues one launch per group).
 cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, const FrameDesc* frames, int nframes,
-                                           const int* prefix, int total, int* counter, int grid, cudaStream_t s) {
+                                           const int* prefix, int* counter, int grid, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
-  GBVR_DISPATCH(persistent_t, dtype, mode, sampler, frames, nframes, prefix, total, counter, grid, s);
+  GBVR_DISPATCH(persistent_t, dtype, mode, sampler, frames, nframes, prefix, counter, grid, s);
 }
 
 cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, const FrameDesc& shared,
-                                             const FrameDesc* frames, int nframes, const int* prefix, int total,
-                                             int* counter, int grid, cudaStream_t s) {
+                                             const FrameDesc* frames, int nframes, const int* prefix, int* counter,
+                                             int grid, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
-  GBVR_DISPATCH(persistent_u_t, dtype, mode, sampler, shared, frames, nframes, prefix, total, counter, grid, s);
+  GBVR_DISPATCH(persistent_u_t, dtype, mode, sampler, shared, frames, nframes, prefix, counter, grid, s);
 }
 
 int persistent_grid_size_uniform(int device, int mode) {

@@ -131,3 +131,20 @@ def test_large_batch_equals_per_view_launches(blobs):
         r.setView(*views[37])
         r.paint()
         assert np.array_equal(r.readFramebuffer(0), batch[37])
+
+
+def test_batches_of_new_views_replay_the_cached_graph(blobs):
+    """Same-sized batches replay one cached launch; each new set of views
+    culls to a different tile count, which the replay must follow."""
+    sp, _ = blobs
+    steps = [workloads.orbit_views(4, 96, 72, elevation=e, start=s) for e, s in ((5, 0), (25, 30), (-35, 60), (15, 90))]
+    with Renderer() as r:
+        r.loadSynthetic(sp, brick_size=32, overlap=2)
+        r.resize((96, 72))
+        r.set1DTrans(TF)
+        r.setValueRange(0.0, 255.0)
+        for views in steps:
+            r.paintBatch(views)
+            batch = r.readFramebuffers(0, 4).copy()
+            r.paintViews(views)
+            assert np.array_equal(batch, r.readFramebuffers(0, 4))

@@ -65,19 +65,26 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """Start sampling every 50 ms; returns once the first sample is in, so
+        the samples that follow fall inside the timed region.  The first one
+        (taken before the region) is dropped."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.first = threading.Event()
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=5.0)
         except Exception:
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            if self.first.is_set():
+                self.lines.append(line.strip())
+            self.first.set()
 
     def stop(self):
         if not self.proc:
@@ -557,7 +564,7 @@ def run_c5(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--views", type=int, default=64)
@@ -703,7 +710,9 @@ def main():
     h2d = r.stats()["h2d_bytes"]
     d2h = len(views) * wl.width * wl.height * 4
     # pipelined (the e2e value): step i renders into framebuffer set i % 2
-    # while step i - 1's frames are read back into their own host buffer
+    # while step i - 1's frames are read back into their own host buffer; the
+    # host waits for each step's read-back (a consumer could use the frames
+    # then) while the next render runs
     host2 = [host_fb, torch.empty_like(host_fb).pin_memory()]
     for i in range(2):
         r.paintBatchAsync(views, i)
@@ -714,6 +723,7 @@ def main():
         r.paintBatchAsync(views, i % 2)
         if i > 0:
             r.readFramebuffersAsync((i - 1) % 2, host2[(i - 1) % 2])
+            r.waitRead((i - 1) % 2)
     r.readFramebuffersAsync((args.steps - 1) % 2, host2[(args.steps - 1) % 2])
     r.waitAsync()
     barrier()

@@ -140,6 +140,7 @@ SIGNATURES = {
     "gbvr_paint_path": [P, C.POINTER(View), I, C.POINTER(C.c_int32), U64P, U64P],
     "gbvr_paint_batch_async": [P, C.POINTER(View), I, I],
     "gbvr_read_framebuffers_async": [P, I, I, I, P, SZ],
+    "gbvr_wait_read": [P, I],
     "gbvr_wait_async": [P],
     "gbvr_set_tf1d": [P, FP, I],
     "gbvr_set_tf2d": [P, FP, I, I, F],

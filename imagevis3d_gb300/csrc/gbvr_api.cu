@@ -1716,8 +1716,8 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long), r->stream));
     CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)r->ds.levels[level].nbricks, r->stream));
     if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words, r->stream));
-    CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
-    CUDA_TRY(launch_fill_outside(r->d_frames.as<FrameDesc>(), 1, r->width, r->height, r->stream));
+    CUDA_TRY(launch_fill_outside(r->d_frames.as<FrameDesc>(), 1, r->height, r->stream));
+    CUDA_TRY(cudaEventRecord(r->evk0, r->stream));  // kernel time: the raycast alone
     cudaError_t le =
         uniform ? launch_render_persistent_uniform(r->ds.dtype, r->mode, r->sampler, shared, r->d_frames.as<FrameDesc>(),
                                                    1, r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream)
@@ -1765,8 +1765,8 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
   CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream));
   CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
   if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words * n, r->stream));
-  CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
-  CUDA_TRY(launch_fill_outside(r->d_frames.as<FrameDesc>(), n, r->width, r->height, r->stream));
+  CUDA_TRY(launch_fill_outside(r->d_frames.as<FrameDesc>(), n, r->height, r->stream));
+  CUDA_TRY(cudaEventRecord(r->evk0, r->stream));  // kernel time: the raycast alone
   CUDA_TRY(cudaGraphLaunch(it->second.exec, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
@@ -2334,6 +2334,16 @@ int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, v
   return GBVR_OK;
 }
 
+int gbvr_wait_read(gbvr_renderer* r, int slot) {
+  TRY(check_r(r));
+  if (slot < 0 || slot > 1) return fail(GBVR_EINVAL, "slot must be 0 or 1");
+  if (!r->read_stream || !r->slot_read_pending[slot]) return GBVR_OK;
+  // read-backs share one stream: the slot's last event covers all of them
+  CUDA_TRY(cudaEventSynchronize(r->slot_read[slot]));
+  r->slot_read_pending[slot] = false;
+  return GBVR_OK;
+}
+
 int gbvr_wait_async(gbvr_renderer* r) {
   TRY(check_r(r));
   CUDA_TRY(cudaStreamSynchronize(r->stream));
@@ -2682,6 +2692,9 @@ struct gbvr_server {
 namespace {
 
 // Assemble and launch one batch into `slot` (worker thread, mutex released).
+// work counters per batch: one per launch group
+constexpr int kServerGroups = 16;
+
 int launch_batch(gbvr_server* s, BatchSlot& slot) {
   const int n = (int)slot.reqs.size();
   // group by voxel type and mode: one persistent launch per group
@@ -2689,7 +2702,7 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
   for (int i = 0; i < n; ++i) order[i] = i;
   auto key = [&](int i) {
     const ServerRequest* q = slot.reqs[i];
-    return s->datasets[q->req.dataset]->dtype * 3 + s->tfs[q->req.tf]->mode;
+    return s->datasets[q->req.dataset]->dtype * 4 + s->tfs[q->req.tf]->mode;  // 3 dtypes x 4 modes
   };
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key(x) < key(y); });
   std::vector<ServerRequest*> sorted(n);
@@ -2702,7 +2715,7 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
   slot.fb_off.swap(offs);
   CUDA_TRY(slot.d_frames.alloc(sizeof(FrameDesc) * s->params.max_batch));
   CUDA_TRY(slot.d_prefix.alloc(sizeof(int) * (s->params.max_batch + 8) * 2));
-  CUDA_TRY(slot.d_counter.alloc(sizeof(int) * 16));
+  CUDA_TRY(slot.d_counter.alloc(sizeof(int) * kServerGroups));
   CUDA_TRY(slot.d_samples.alloc(sizeof(unsigned long long) * s->params.max_batch));
   CUDA_TRY(slot.h_frames.alloc(sizeof(FrameDesc) * s->params.max_batch));
   CUDA_TRY(slot.h_prefix.alloc(sizeof(int) * (s->params.max_batch + 8) * 2));
@@ -2711,7 +2724,7 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
   struct Group { int first, count, prefix_at, total, dtype, mode; };
   std::vector<Group> groups;
   int pcur = 0;
-  long long max_pix = 0;
+  int max_h = 0;
   for (int i = 0; i < n; ++i) {
     const ServerRequest* q = slot.reqs[i];
     const Dataset& ds = *s->datasets[q->req.dataset];
@@ -2753,7 +2766,7 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
     hf[i].out_rgba8 = (uchar4*)((char*)slot.d_fb.p + slot.fb_off[i]);
     hf[i].samples = slot.d_samples.as<unsigned long long>() + i;
     cull_tiles(hf[i], nullptr, p.view, p.proj);
-    max_pix = std::max(max_pix, (long long)p.width * p.height);
+    max_h = std::max(max_h, p.height);
     const int dt = ds.dtype, md = t.mode;
     if (groups.empty() || groups.back().dtype != dt || groups.back().mode != md) {
       if (!groups.empty()) {
@@ -2773,15 +2786,17 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
     hp[g.prefix_at + g.count] = g.total;
     pcur = g.prefix_at + g.count + 1;
   }
+  // one group per (voxel type, mode) after the sort: at most 12
+  if (groups.size() > (size_t)kServerGroups) return fail(GBVR_ESTATE, "too many launch groups in a batch");
   cudaStream_t st = s->stream;
   CUDA_TRY(cudaEventRecord(slot.ev0, st));
   CUDA_TRY(cudaMemcpyAsync(slot.d_frames.p, hf, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(slot.d_prefix.p, hp, sizeof(int) * pcur, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemsetAsync(slot.d_counter.p, 0, sizeof(int) * 16, st));
+  CUDA_TRY(cudaMemsetAsync(slot.d_counter.p, 0, sizeof(int) * kServerGroups, st));
   CUDA_TRY(cudaMemsetAsync(slot.d_samples.p, 0, sizeof(unsigned long long) * n, st));
   // background outside each request's tile rectangle (frames differ in size:
-  // the grid covers the largest, each thread checks its own frame)
-  CUDA_TRY(launch_fill_outside(slot.d_frames.as<FrameDesc>(), n, (int)std::min<long long>(max_pix, 1LL << 30), 1, st));
+  // the grid covers the tallest, each block checks its own frame's rows)
+  CUDA_TRY(launch_fill_outside(slot.d_frames.as<FrameDesc>(), n, max_h, st));
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const Group& g = groups[gi];
     const int grid = s->sm_count * s->max_ctas[g.mode];
@@ -2974,7 +2989,7 @@ int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba,
   TRY(check_s(s));
   if (dataset < 0 || dataset >= (int)s->datasets.size()) return fail(GBVR_EINVAL, "bad dataset id");
   if (mode < 0 || mode > 3) return fail(GBVR_EINVAL, "bad render mode");
-  if (mode == GBVR_RM_1DTRANS) h = 1;
+  if (mode == GBVR_RM_1DTRANS || mode == GBVR_RM_MIP) h = 1;
   if (mode == GBVR_RM_ISOSURFACE) {
     static const float dummy[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (!rgba) { rgba = dummy; w = 2; h = 1; }

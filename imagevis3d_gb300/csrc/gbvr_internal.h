@@ -148,7 +148,8 @@ cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, con
 int persistent_grid_size(int device, int mode);
 // Background (RGBA = bg, 0) into every pixel of each frame outside its tile
 // rectangle, as a ray that misses the volume leaves it.
-cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int width, int height, cudaStream_t s);
+// (frames of different sizes: max_height is the tallest; each block checks its frame's size)
+cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int max_height, cudaStream_t s);
 cudaError_t launch_fill_outside_one(const FrameDesc& f, cudaStream_t s);
 // Batches whose views share everything but camera, light direction, outputs
 // and counters: the shared part travels as a kernel parameter (constant

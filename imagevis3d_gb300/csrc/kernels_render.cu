@@ -657,41 +657,65 @@ __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
   }
 }
 
-__device__ __forceinline__ void fill_outside_pixel(const FrameDesc& f, long long p) {
-  if (p >= (long long)f.width * f.height) return;
-  const int x = (int)(p % f.width), y = (int)(p / f.width);
+// Background outside a frame's tile rectangle.  A block covers FILL_ROWS rows
+// of one frame; its threads stride along each row (coalesced 4-byte RGBA8 or
+// 16-byte float stores) and skip the rectangle's span on the rows it crosses.
+// No division: the row and column come from the loop counters.
+constexpr int FILL_ROWS = 8;
+constexpr int FILL_THREADS = 256;
+
+__device__ __forceinline__ void fill_outside_rows(const FrameDesc& f, int row_block) {
+  const int w = f.width, h = f.height;
+  const int y0 = row_block * FILL_ROWS;
+  if (y0 >= h) return;
+  const int y1 = min(y0 + FILL_ROWS, h);
   const int th = 32 / f.tile_w;
-  if (x >= f.tx0 * f.tile_w && x < (f.tx0 + f.ntx) * f.tile_w && y >= f.ty0 * th && y < (f.ty0 + f.nty) * th) return;
+  const int rx0 = f.tx0 * f.tile_w, rx1 = (f.tx0 + f.ntx) * f.tile_w;
+  const int ry0 = f.ty0 * th, ry1 = (f.ty0 + f.nty) * th;
   const float4 c = make_float4(f.bg[0], f.bg[1], f.bg[2], 0.f);
-  if (f.out_f32) f.out_f32[p] = c;
-  if (f.out_rgba8)
-    f.out_rgba8[p] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
-                                 (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
-                                 (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f), 0);
+  const uchar4 c8 = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
+                                (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
+                                (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f), 0);
+  uchar4* o8 = f.out_rgba8;
+  float4* o32 = f.out_f32;
+  for (int y = y0; y < y1; ++y) {
+    const size_t base = (size_t)y * w;
+    const bool row_in = y >= ry0 && y < ry1;
+    // [0, a) and [b, w): the whole row, or the parts left and right of the rectangle
+    const int a = row_in ? min(rx0, w) : w, b = row_in ? max(rx1, a) : w;
+    for (int x = threadIdx.x; x < a; x += FILL_THREADS) {
+      if (o8) o8[base + x] = c8;
+      if (o32) o32[base + x] = c;
+    }
+    for (int x = b + threadIdx.x; x < w; x += FILL_THREADS) {
+      if (o8) o8[base + x] = c8;
+      if (o32) o32[base + x] = c;
+    }
+  }
 }
 
-__global__ void k_fill_outside(const FrameDesc* __restrict__ frames, int width, int height) {
-  fill_outside_pixel(frames[blockIdx.y], (long long)blockIdx.x * blockDim.x + threadIdx.x);
+__global__ void __launch_bounds__(FILL_THREADS) k_fill_outside(const FrameDesc* __restrict__ frames) {
+  fill_outside_rows(frames[blockIdx.x], blockIdx.y);
 }
 
-__global__ void k_fill_outside_one(const __grid_constant__ FrameDesc f) {
-  fill_outside_pixel(f, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+__global__ void __launch_bounds__(FILL_THREADS) k_fill_outside_one(const __grid_constant__ FrameDesc f) {
+  fill_outside_rows(f, blockIdx.x);
 }
 
 cudaError_t launch_fill_outside_one(const FrameDesc& f, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (f.ntx == f.tiles_x && f.nty == f.tiles_y) return cudaSuccess;  // nothing outside
-  const long long npix = (long long)f.width * f.height;
-  k_fill_outside_one<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(f);
+  if (f.width <= 0 || f.height <= 0) return cudaSuccess;
+  k_fill_outside_one<<<(unsigned)((f.height + FILL_ROWS - 1) / FILL_ROWS), FILL_THREADS, 0, s>>>(f);
   return cudaGetLastError();
 }
 
-cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int width, int height, cudaStream_t s) {
+cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int max_height, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
-  if (nframes <= 0) return cudaSuccess;
-  const long long npix = (long long)width * height;
-  dim3 grid((unsigned)((npix + 255) / 256), (unsigned)nframes);
-  k_fill_outside<<<grid, 256, 0, s>>>(frames, width, height);
+  if (nframes <= 0 || max_height <= 0) return cudaSuccess;
+  if ((max_height + FILL_ROWS - 1) / FILL_ROWS > 65535) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)nframes, (unsigned)((max_height + FILL_ROWS - 1) / FILL_ROWS));
+  k_fill_outside<<<grid, FILL_THREADS, 0, s>>>(frames);
   return cudaGetLastError();
 }
 

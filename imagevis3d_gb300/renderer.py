@@ -357,6 +357,10 @@ class Renderer:
         nbytes = out.numel() * out.element_size() if hasattr(out, "numel") else out.nbytes
         L.call("gbvr_read_framebuffers_async", self._h, slot, first, n, C.c_void_p(ptr), nbytes)
 
+    def waitRead(self, slot):
+        """Wait until the read-backs queued for set `slot` are in host memory."""
+        L.call("gbvr_wait_read", self._h, slot)
+
     def waitAsync(self):
         L.call("gbvr_wait_async", self._h)
 

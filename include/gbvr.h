@@ -262,10 +262,13 @@ int gbvr_paint_views(gbvr_renderer* r, const gbvr_view* views, int n);
  * gbvr_paint_batch_async renders n views into framebuffer set `slot` (0 or 1, in-core datasets) and returns
  * once the work is queued.  gbvr_read_framebuffers_async copies views of a set into host memory
  * (page-locked for a true overlap) after that set's render, on its own stream, so the read-back of one step
- * overlaps the render of the next; a set is rendered again only after its read-back.  gbvr_wait_async waits
- * for everything queued.  The synchronous calls use set 0 whenever set 0 was selected last. */
+ * overlaps the render of the next; a set is rendered again only after its read-back.  gbvr_wait_read
+ * returns once every read-back queued for `slot` has landed in host memory (the render queued since keeps
+ * running); gbvr_wait_async waits for everything queued.  The synchronous calls first let queued work
+ * finish, then render into and read the set selected last (set 0 until an asynchronous batch picks 1). */
 int gbvr_paint_batch_async(gbvr_renderer* r, const gbvr_view* views, int n, int slot);
 int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, void* host, size_t bytes);
+int gbvr_wait_read(gbvr_renderer* r, int slot);
 int gbvr_wait_async(gbvr_renderer* r);
 
 /* ---- readback (captureSingleFrame, RenderWindow.cpp:1642-1671; RGBA8 model

@@ -69,6 +69,32 @@ def test_every_step_read_back_in_a_pipeline(sp):
         assert np.array_equal(r.readFramebuffers(0, 4), want[0])
 
 
+def test_consumer_waits_for_one_read_back(sp):
+    """A consumer takes step i - 1's frames from host memory while step i
+    renders: waiting for that slot's read-back is enough."""
+    steps = [workloads.orbit_views(3, W, H, elevation=e, start=s) for e, s in
+             ((0, 0), (20, 25), (-15, 50), (35, 75), (10, 110), (-40, 140))]
+    with _renderer(sp) as r:
+        want = []
+        for views in steps:
+            r.paintBatch(views)
+            want.append(r.readFramebuffers(0, len(views)).copy())
+        host = [torch.empty((3, H, W, 4), dtype=torch.uint8).pin_memory() for _ in range(2)]
+        got = []
+        for i, views in enumerate(steps):
+            r.paintBatchAsync(views, i % 2)
+            if i > 0:
+                r.readFramebuffersAsync((i - 1) % 2, host[(i - 1) % 2])
+                r.waitRead((i - 1) % 2)
+                got.append(host[(i - 1) % 2].numpy().copy())
+        r.readFramebuffersAsync((len(steps) - 1) % 2, host[(len(steps) - 1) % 2])
+        r.waitRead((len(steps) - 1) % 2)
+        got.append(host[(len(steps) - 1) % 2].numpy().copy())
+        r.waitAsync()
+        for i in range(len(steps)):
+            assert np.array_equal(got[i], want[i]), i
+
+
 def test_async_errors(sp):
     with _renderer(sp) as r:
         with pytest.raises(GbvrError):
@@ -76,6 +102,9 @@ def test_async_errors(sp):
         views = workloads.orbit_views(2, W, H)
         with pytest.raises(GbvrError):
             r.paintBatchAsync(views, 2)
+        with pytest.raises(GbvrError):
+            r.waitRead(-1)
+        r.waitRead(0)  # nothing queued: returns at once
         r.paintBatchAsync(views, 1)
         with pytest.raises(GbvrError):
             r.readFramebuffersAsync(1, np.zeros((1, H, W, 4), np.uint8), 0, 2)  # too small

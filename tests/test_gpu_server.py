@@ -4,8 +4,8 @@ same view rendered through the renderer API, bit for bit."""
 import numpy as np
 import pytest
 
-from imagevis3d_gb300 import (GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE, GbvrError, Renderer,
-                              Server, orbit_camera, synth_params, workloads)
+from imagevis3d_gb300 import (GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE, GBVR_RM_MIP, GbvrError,
+                              Renderer, Server, orbit_camera, synth_params, workloads)
 
 pytestmark = pytest.mark.gpu
 
@@ -28,8 +28,10 @@ def setup(orc):
         (GBVR_RM_2DTRANS, workloads.tf2d_seeded(128, 64, 7, zero_cols=10), {"grad_max": 0.08}),
         (GBVR_RM_1DTRANS, workloads.tf1d_seeded(512, 8, 0.2, 1.0), {}),
         (GBVR_RM_ISOSURFACE, None, {"iso": 1200.0, "iso_rgb": (0.9, 0.6, 0.3)}),
+        # MIP on uint8 next to 1D on uint16: distinct launch groups
+        (GBVR_RM_MIP, workloads.tf1d_seeded(256, 9, 40.0, 255.0), {}),
     ]
-    owners = [0, 1, 1, 2, 1]
+    owners = [0, 1, 1, 2, 1, 0]
     return vols, hosts, tfs, owners
 
 
@@ -37,7 +39,7 @@ def _requests(n, seed):
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(n):
-        tf = int(rng.integers(0, 5))
+        tf = int(rng.integers(0, 6))
         w, h = SIZES[int(rng.integers(0, len(SIZES)))]
         cam = orbit_camera(float(rng.uniform(0, 360)), float(rng.uniform(-40, 40)),
                            float(rng.uniform(1.6, 3.0)) * workloads.DIAG, 45.0, w, h)
@@ -67,14 +69,15 @@ def test_mix_alone_and_renderer_agree(setup):
             alone.append(img)
     for i in range(12):
         assert np.array_equal(alone[i], mixed[i][0]), i
+    assert {tf for tf, *_ in reqs} == set(range(len(tfs)))
     # the renderer API draws the same pixels
-    for i, (tf, w, h, cam, spv) in enumerate(reqs[:10]):
+    for i, (tf, w, h, cam, spv) in enumerate(reqs[:14]):
         m, t, kw = tfs[tf]
         with Renderer() as r:
             r.loadVolume(hosts[owners[tf]], brick_size=64, overlap=2)
             r.resize((w, h))
             r.setRenderMode(m)
-            if m == GBVR_RM_1DTRANS:
+            if m in (GBVR_RM_1DTRANS, GBVR_RM_MIP):
                 r.set1DTrans(t)
             elif m == GBVR_RM_2DTRANS:
                 r.set2DTrans(t, kw["grad_max"])

@@ -193,7 +193,7 @@ def traffic_from_profile():
 
 
 def run_c3(args):
-    """Sparse fractal workload (BASELINE config 3): 2048^3 uint8 fBm, 2D TF +
+    """Sparse fractal workload: 2048^3 uint8 fBm, 2D TF +
     Phong DVR and isosurfaces at 2560x1440, plus the GPU 2D histogram of the
     8 GiB level.  Prints one JSON line of its own."""
     import numpy as np
@@ -307,7 +307,7 @@ def level_from_bricks(r, lod):
 
 
 def run_c4(args):
-    """Out-of-core fly-through (BASELINE config 4, scaled to the host): a
+    """Out-of-core fly-through (the 8192x8192x4096 volume scaled to the host): a
     uint8 blob volume streamed brick by brick into page-locked host memory
     (256^3 bricks, 2 ghosts, 6 levels), a device slot pool holding 3/8 of
     the volume (the 96 GiB : 256 GiB ratio), a 120-frame Bezier fly-through
@@ -430,7 +430,7 @@ def run_c4(args):
 
 
 def run_c5(args):
-    """Serving mix (BASELINE config 5): Poisson arrivals of render requests
+    """Serving mix: Poisson arrivals of render requests
     over 12 resident datasets (64^3 .. 1024^3, uint8 / uint16 / float32), image
     sizes in {256^2, 512^2, 1280x720, 1920x1080}, a random 1D or 2D TF preset
     and a random camera per request.  Capacity is measured first with a burst;

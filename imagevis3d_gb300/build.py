@@ -56,14 +56,16 @@ def build(force=False, verbose=False):
         obj = os.path.join(OBJ, u + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
+            # host code: one rounding per operation (no FMA contraction on
+            # any host CPU), so host-side FP64 geometry is reproducible
             jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "-Xptxas", "-v", "-c", src, "-o", obj])
+                         "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v", "-c", src, "-o", obj])
     for u in HOST_UNITS:
         src = os.path.join(CSRC, u)
         obj = os.path.join(OBJ, u + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-c", src, "-o", obj])
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", src, "-o", obj])
     logs = []
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:

@@ -272,7 +272,9 @@ struct Dataset {
   ~Dataset() { release(); }
 };
 
-// LOD and brick-grid rules: see the oracle (same statements) and the design doc.
+// LOD and brick-grid rules: the level count halves (ceil) until the largest
+// axis fits one brick interior (brick - 2 ghost), as UVFReader/DataSource.h:521-529
+// halves the raster until it fits; the oracle states the same rules.
 int lod_dims(const long long dims[3], int brick, int ghost, int max_lods, std::vector<std::array<long long, 3>>& out) {
   long long I = brick - 2 * ghost;
   long long n[3] = {dims[0], dims[1], dims[2]};
@@ -904,6 +906,10 @@ struct gbvr_renderer {
   int mode = GBVR_RM_1DTRANS, interp = GBVR_LINEAR, sampler = GBVR_SAMPLER_SW;
   int clip_on = 0;
   float clip[4] = {0.f, 0.f, 1.f, 0.f};
+  // bounding boxes: the dataset box and the brick boxes of the rendered level
+  int bbox_global = 0, bbox_local = 0;
+  float bbox_rgb[2][3] = {{1.f, 1.f, 1.f}, {0.6f, 0.6f, 0.6f}};
+  DevBuf d_line_keys, d_line_segs, d_line_views, d_line_list, d_line_count;
   std::vector<float> tf1d;
   std::vector<float> tf2d;
   int tf2d_w = 0, tf2d_h = 0;
@@ -1170,7 +1176,131 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
   f.touched = r->stats_level >= 1 ? r->d_touched.as<unsigned char>() + (size_t)vidx * L.nbricks : nullptr;
   f.cell_touched = (r->stats_level >= 2 && r->empty_skip >= 2)
                        ? r->d_cellbits.as<unsigned>() + (size_t)vidx * r->cell_words : nullptr;
+  if (r->bbox_global || r->bbox_local) f.lines = r->d_line_keys.as<unsigned>() + (size_t)vidx * npix;
+  memcpy(f.line_rgb, r->bbox_rgb, sizeof(f.line_rgb));
   return f;
+}
+
+// World-space segments of the bounding boxes at `level`: the 12 edges of the
+// dataset box, and the lines of the level's brick grid (interior bounds at
+// multiples of the interior size, clamped to the level) that are not edges
+// of the drawn dataset box.  A brick bound b of an axis with d voxels and
+// normalised extent e lies at (b / d) e - e/2.
+void bbox_segments(const gbvr_renderer* r, int level, std::vector<LineSeg>& segs) {
+  segs.clear();
+  const Dataset& ds = r->ds;
+  const Level& L = ds.levels[level];
+  double ext[3], h[3], mx = 0;
+  for (int a = 0; a < 3; ++a) {
+    ext[a] = (double)ds.dims[a] * ds.aspect[a];
+    mx = std::max(mx, ext[a]);
+  }
+  for (int a = 0; a < 3; ++a) {
+    ext[a] /= mx;
+    h[a] = 0.5 * ext[a];
+  }
+  auto add = [&](int a, double u, double v, int color) {
+    const int b = (a + 1) % 3, c = (a + 2) % 3;
+    LineSeg sg;
+    memset(&sg, 0, sizeof(sg));
+    sg.a[a] = -h[a];
+    sg.b[a] = h[a];
+    sg.a[b] = sg.b[b] = u;
+    sg.a[c] = sg.b[c] = v;
+    sg.color = color;
+    segs.push_back(sg);
+  };
+  for (int a = 0; a < 3; ++a) {
+    const int b = (a + 1) % 3, c = (a + 2) % 3;
+    if (r->bbox_global)
+      for (int k = 0; k < 4; ++k) add(a, (k & 1) ? h[b] : -h[b], (k & 2) ? h[c] : -h[c], 0);
+    if (!r->bbox_local) continue;
+    auto bound = [&](int ax, int j) {
+      const long long bj = std::min<long long>((long long)j * L.interior, L.dims[ax]);
+      return (double)bj / (double)L.dims[ax] * ext[ax] - h[ax];
+    };
+    for (int j = 0; j <= L.nb[b]; ++j)
+      for (int k = 0; k <= L.nb[c]; ++k) {
+        const bool edge = (j == 0 || j == L.nb[b]) && (k == 0 || k == L.nb[c]);
+        if (edge && r->bbox_global) continue;
+        add(a, bound(b, j), bound(c, k), 1);
+      }
+  }
+}
+
+int lines_on(const gbvr_renderer* r) { return r->bbox_global || r->bbox_local; }
+
+// Key buffers, the list of covered pixels and its count for n frames.
+int alloc_lines(gbvr_renderer* r, size_t npix, int n) {
+  if (!lines_on(r)) return GBVR_OK;
+  CUDA_TRY(r->d_line_keys.alloc(sizeof(unsigned) * npix * n));
+  CUDA_TRY(r->d_line_list.alloc(sizeof(unsigned long long) * npix * n));
+  CUDA_TRY(r->d_line_count.alloc(sizeof(unsigned)));
+  CUDA_TRY(r->d_frames.alloc(sizeof(FrameDesc) * n));  // plain paints copy their descriptors here
+  return GBVR_OK;
+}
+
+// Line stops and the covered-pixel list for the n frames in d_frames.
+int line_stops(gbvr_renderer* r, int n) {
+  if (!lines_on(r)) return GBVR_OK;
+  CUDA_TRY(cudaMemsetAsync(r->d_line_count.p, 0, sizeof(unsigned), r->stream));
+  CUDA_TRY(launch_line_stops(r->d_frames.as<FrameDesc>(), 0, n, r->height, r->d_line_list.as<unsigned long long>(),
+                             r->d_line_count.as<unsigned>(), r->stream));
+  return GBVR_OK;
+}
+
+// The same for one frame rendered by a plain launch (its descriptor is a
+// kernel parameter: it is copied to d_frames[v] for the line passes); `reset`
+// starts a new list.
+int line_stops_one(gbvr_renderer* r, const FrameDesc& f, int v, bool reset) {
+  if (!lines_on(r)) return GBVR_OK;
+  CUDA_TRY(cudaMemcpyAsync(r->d_frames.as<FrameDesc>() + v, &f, sizeof(FrameDesc), cudaMemcpyHostToDevice, r->stream));
+  if (reset) CUDA_TRY(cudaMemsetAsync(r->d_line_count.p, 0, sizeof(unsigned), r->stream));
+  CUDA_TRY(launch_line_stops(r->d_frames.as<FrameDesc>(), v, 1, r->height, r->d_line_list.as<unsigned long long>(),
+                             r->d_line_count.as<unsigned>(), r->stream));
+  return GBVR_OK;
+}
+
+// Re-render the listed pixels (after the frames' render).
+int render_lines(gbvr_renderer* r) {
+  if (!lines_on(r)) return GBVR_OK;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  CUDA_TRY(launch_render_lines(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(),
+                               r->d_line_list.as<unsigned long long>(), r->d_line_count.as<unsigned>(),
+                               std::max(sms, 1) * 8, r->stream));
+  return GBVR_OK;
+}
+
+// Rasterise the bounding-box lines of views [0, n) into the key buffers of
+// frames vidx0 .. vidx0 + n - 1 (on the render stream, before their render).
+int draw_lines(gbvr_renderer* r, const gbvr_view* views, int vidx0, int n, int level) {
+  if (!r->bbox_global && !r->bbox_local) return GBVR_OK;
+  std::vector<LineSeg> segs;
+  bbox_segments(r, level, segs);
+  const size_t npix = (size_t)r->width * r->height;
+  CUDA_TRY(cudaMemsetAsync(r->d_line_keys.as<unsigned>() + (size_t)vidx0 * npix, 0xff, sizeof(unsigned) * npix * n,
+                           r->stream));
+  if (segs.empty()) return GBVR_OK;
+  std::vector<LineView> lv((size_t)n);
+  for (int v = 0; v < n; ++v) {
+    memcpy(lv[v].view, views[v].view, sizeof(lv[v].view));
+    memcpy(lv[v].proj, views[v].proj, sizeof(lv[v].proj));
+    lv[v].width = r->width;
+    lv[v].height = r->height;
+    lv[v].keys = r->d_line_keys.as<unsigned>() + (size_t)(vidx0 + v) * npix;
+  }
+  CUDA_TRY(r->d_line_segs.alloc(sizeof(LineSeg) * segs.size()));
+  CUDA_TRY(r->d_line_views.alloc(sizeof(LineView) * lv.size()));
+  // pageable sources: each copy returns once its source is staged
+  CUDA_TRY(cudaMemcpyAsync(r->d_line_segs.p, segs.data(), sizeof(LineSeg) * segs.size(), cudaMemcpyHostToDevice,
+                           r->stream));
+  CUDA_TRY(cudaMemcpyAsync(r->d_line_views.p, lv.data(), sizeof(LineView) * lv.size(), cudaMemcpyHostToDevice,
+                           r->stream));
+  CUDA_TRY(launch_raster_lines(r->d_line_segs.as<LineSeg>(), (int)segs.size(), r->d_line_views.as<LineView>(), n,
+                               r->stream));
+  return GBVR_OK;
 }
 
 // The view's ray tiles whose pixels can see the volume: the rectangle around
@@ -1447,6 +1577,7 @@ int prepare(gbvr_renderer* r, int nviews, int& level, const gbvr_view* views) {
   }
   CUDA_TRY(r->d_samples.alloc(sizeof(unsigned long long) * nviews));
   CUDA_TRY(r->d_touched.alloc((size_t)nviews * r->ds.levels[level].nbricks));
+  TRY(alloc_lines(r, npix, nviews));
   {
     const Level& L = r->ds.levels[level];
     r->cell_words = ((long long)L.nc[0] * L.nc[1] * L.nc[2] + 31) / 32;
@@ -1487,19 +1618,26 @@ int paint_plain(gbvr_renderer* r, const gbvr_view* views, int n) {
   CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
   if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words * n, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
+  gbvr_view cur;
+  if (!views) {
+    if (r->view_set) {
+      memcpy(cur.view, r->view, sizeof(cur.view));
+      memcpy(cur.proj, r->proj, sizeof(cur.proj));
+    } else {
+      default_camera(r, cur.view, cur.proj);
+    }
+  }
+  TRY(draw_lines(r, views ? views : &cur, 0, n, level));
   CUDA_TRY(cudaEventRecord(r->evk0, r->stream));
   for (int v = 0; v < n; ++v) {
-    float dv[16], dp[16];
-    const float *vw = views ? views[v].view : nullptr, *pj = views ? views[v].proj : nullptr;
-    if (!views) {
-      if (r->view_set) { vw = r->view; pj = r->proj; }
-      else { default_camera(r, dv, dp); vw = dv; pj = dp; }
-    }
+    const float *vw = views ? views[v].view : cur.view, *pj = views ? views[v].proj : cur.proj;
     FrameDesc f = make_frame(r, vw, pj, level, v);
     cull_tiles(f, r, vw, pj);
+    TRY(line_stops_one(r, f, v, v == 0));
     CUDA_TRY(launch_fill_outside_one(f, r->stream));
     CUDA_TRY(launch_render_plain(f, r->stream));
   }
+  TRY(render_lines(r));
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
   r->last_h2d = 0;  // descriptors travel as kernel parameters
@@ -1593,6 +1731,7 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
   const int nb0 = ds.levels[0].nbricks;  // the finest level has the most bricks
   CUDA_TRY(r->d_samples.alloc(sizeof(unsigned long long) * n));
   CUDA_TRY(r->d_touched.alloc((size_t)n * nb0));
+  TRY(alloc_lines(r, npix, n));
   CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream));
   CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * nb0, r->stream));
   r->drop_graphs();
@@ -1624,8 +1763,11 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
     f.touched = r->stats_level >= 1 ? r->d_touched.as<unsigned char>() + (size_t)i * nb0 : nullptr;
     f.cell_touched = nullptr;
     cull_tiles(f, r, views[i].view, views[i].proj);
+    TRY(draw_lines(r, views + i, i, 1, level));
+    TRY(line_stops_one(r, f, i, true));
     CUDA_TRY(launch_fill_outside_one(f, r->stream));
     CUDA_TRY(launch_render_plain(f, r->stream));
+    TRY(render_lines(r));  // while the frame's bricks are resident
     CUDA_TRY(cudaEventRecord(r->ev_done[st], r->stream));
     if (lod_out) lod_out[i] = level;
     if (miss_out) miss_out[i] = miss;
@@ -1700,6 +1842,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     shared.out_rgba8 = nullptr;
     shared.out_f32 = nullptr;
     shared.samples = nullptr;
+    shared.lines = nullptr;
     shared.touched_stride = shared.touched ? r->ds.levels[level].nbricks : 0;
     shared.cell_touched_stride = shared.cell_touched ? r->cell_words : 0;
   }
@@ -1710,12 +1853,14 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     // a single view (gbvr_paint): a direct launch; its descriptor changes
     // with every dataset, TF and size, which would re-capture a graph each time
     CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
+    TRY(draw_lines(r, views, 0, 1, level));
     CUDA_TRY(cudaMemcpyAsync(r->d_frames.p, r->h_frames.p, sizeof(FrameDesc), cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(r->d_prefix.p, r->h_prefix.p, sizeof(int) * 2, cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemsetAsync(r->d_counter.p, 0, sizeof(int), r->stream));
     CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long), r->stream));
     CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)r->ds.levels[level].nbricks, r->stream));
     if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words, r->stream));
+    TRY(line_stops(r, 1));
     CUDA_TRY(launch_fill_outside(r->d_frames.as<FrameDesc>(), 1, r->height, r->stream));
     CUDA_TRY(cudaEventRecord(r->evk0, r->stream));  // kernel time: the raycast alone
     cudaError_t le =
@@ -1724,6 +1869,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
                 : launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), 1,
                                                  r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream);
     if (le != cudaSuccess) return cuda_fail(le, "persistent launch");
+    TRY(render_lines(r));
     CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
     CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
     r->last_h2d = sizeof(FrameDesc) + sizeof(int) * 2;
@@ -1759,15 +1905,18 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     it = r->graphs.emplace(key, gbvr_renderer::CachedGraph{ge, uniform, shared}).first;
   }
   CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
+  TRY(draw_lines(r, views, 0, n, level));
   CUDA_TRY(cudaMemcpyAsync(r->d_frames.p, r->h_frames.p, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, r->stream));
   CUDA_TRY(cudaMemcpyAsync(r->d_prefix.p, r->h_prefix.p, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, r->stream));
   CUDA_TRY(cudaMemsetAsync(r->d_counter.p, 0, sizeof(int), r->stream));
   CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long) * n, r->stream));
   CUDA_TRY(cudaMemsetAsync(r->d_touched.p, 0, (size_t)n * r->ds.levels[level].nbricks, r->stream));
   if (r->stats_level >= 2) CUDA_TRY(cudaMemsetAsync(r->d_cellbits.p, 0, sizeof(unsigned) * r->cell_words * n, r->stream));
+  TRY(line_stops(r, n));
   CUDA_TRY(launch_fill_outside(r->d_frames.as<FrameDesc>(), n, r->height, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk0, r->stream));  // kernel time: the raycast alone
   CUDA_TRY(cudaGraphLaunch(it->second.exec, r->stream));
+  TRY(render_lines(r));
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
   r->last_h2d = sizeof(FrameDesc) * n + sizeof(int) * (n + 1);
@@ -2331,6 +2480,18 @@ int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, v
   CUDA_TRY(cudaMemcpyAsync(host, (const char*)fb + per * first, per * n, cudaMemcpyDeviceToHost, r->read_stream));
   CUDA_TRY(cudaEventRecord(r->slot_read[slot], r->read_stream));
   r->slot_read_pending[slot] = true;
+  return GBVR_OK;
+}
+
+int gbvr_set_bboxes(gbvr_renderer* r, int global, int local, const float global_rgb[3], const float local_rgb[3]) {
+  TRY(check_r(r));
+  TRY(settle_async(r));
+  r->bbox_global = global ? 1 : 0;
+  r->bbox_local = local ? 1 : 0;
+  for (int k = 0; k < 3; ++k) {
+    if (global_rgb) r->bbox_rgb[0][k] = global_rgb[k];
+    if (local_rgb) r->bbox_rgb[1][k] = local_rgb[k];
+  }
   return GBVR_OK;
 }
 

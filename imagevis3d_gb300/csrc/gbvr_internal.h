@@ -11,6 +11,7 @@
 //   frames    FrameDesc[n] for the views rendered by one launch.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace gbvr {
@@ -93,6 +94,12 @@ struct __align__(16) FrameDesc {
   float level_max;           // MIP: largest voxel of the level; no sample exceeds it
   int clip_on;               // clip plane: samples with clip . (x, y, z, 1) > 0 are dropped
   float clip[4];
+  // bounding-box lines: per pixel the key of the nearest covering line (see
+  // line_key), then the ray parameter where that line ends the ray (float
+  // bits, bit 0 = colour), or 0xffffffff; null when no lines are drawn.  Per
+  // view.
+  const unsigned* lines;
+  float line_rgb[2][3];      // colour of the global box (key bit 0 = 0) and of the brick boxes (1)
   int tile_w;                // ray tile of one warp: tile_w x (32 / tile_w) pixels
   int perm;                  // brick layout copy: 0 x-fastest, 1 y-fastest, 2 z-fastest, 3 4^3 blocks
   unsigned long long copy_off;  // element offset of that copy in the pool
@@ -106,6 +113,36 @@ struct __align__(16) FrameDesc {
   // v * touched_stride (cell_touched likewise); 0 in per-view descriptors
   long long touched_stride, cell_touched_stride;
 };
+
+// Bounding-box lines (setGlobalBBox / setLocalBBox).  Segments in world
+// coordinates; a pixel is covered by a segment when its centre lies within
+// half a pixel of the segment's projection (clipped to the near plane).  The
+// covered point's NDC depth z varies linearly along the projected segment.
+// Key = bits of the float (z + 2) with bit 0 replaced by the colour index, so
+// the smallest key is the nearest line, and of two lines at one depth the
+// global box wins.
+struct LineSeg {
+  double a[3], b[3];
+  int color;  // 0 global box, 1 brick box
+  int pad;
+};
+struct LineView {
+  float view[16], proj[16];  // row-major, column vectors (as gbvr_view)
+  int width, height;
+  unsigned* keys;            // width * height, 0xffffffff where no line
+};
+
+__host__ __device__ inline unsigned line_key(float z_plus_2, int color) {
+  unsigned u;
+  memcpy(&u, &z_plus_2, 4);
+  return (u & ~1u) | (unsigned)color;
+}
+__host__ __device__ inline float line_ndc_z(unsigned key) {
+  const unsigned u = key & ~1u;
+  float z;
+  memcpy(&z, &u, 4);
+  return z - 2.f;
+}
 
 // A 2D slice view: screen pixels map to the plane through the slice (or to
 // rays along its axis for MIP).
@@ -160,6 +197,18 @@ cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, c
                                              int* counter, int grid, cudaStream_t s);
 int persistent_grid_size_uniform(int device, int mode);
 cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStream_t s);
+// then, for frames [frame0, frame0 + n) of `frames` (device), each covered
+// pixel's key <- the ray parameter where its ray ends (float bits; bit 0
+// keeps the colour), and the pixel (frame << 32 | pixel) is appended to list
+// (*count entries, zeroed beforehand)
+cudaError_t launch_line_stops(const FrameDesc* frames, int frame0, int nframes, int max_height,
+                              unsigned long long* list, unsigned* count, cudaStream_t s);
+// after the frames' render: re-render the listed pixels with the ray ending
+// at the line and the line behind (grid-stride over *count)
+cudaError_t launch_render_lines(int dtype, int mode, int sampler, const FrameDesc* frames,
+                                const unsigned long long* list, const unsigned* count, int grid, cudaStream_t s);
+// keys of every view (set to 0xffffffff beforehand) <- the nearest covering line
+cudaError_t launch_raster_lines(const LineSeg* segs, int nseg, const LineView* views, int nviews, cudaStream_t s);
 
 // ---- launch wrappers (kernels_build.cu) ----
 struct BlobTablesDev {

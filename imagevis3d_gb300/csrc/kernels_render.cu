@@ -6,7 +6,7 @@
 // Replaces the fragment-shader raycaster behind Tuvok's AbstrRenderer::Paint
 // (reached from LuaScripts/BatchRenderer.lua:35 `renderer.paint()` and
 // ImageVis3D/UI/RenderWindow.cpp:2464).  The sampling rule is the project's
-// (stated in the design doc): samples at t_k = t_entry + (k + 1/2) dt along the unit
+// own (Tuvok's shaders are absent): samples at t_k = t_entry + (k + 1/2) dt along the unit
 // world-space ray, dt = 1 / (samples_per_voxel * max level dim), trilinear on
 // cell-centred voxels with clamp-to-edge, TF index (v - lo) (N - 1) / (hi - lo)
 // with linear interpolation between entries, alpha' = 1 - (1 - alpha)^(1/s),
@@ -274,6 +274,14 @@ struct RaySetup {
   bool hit;
 };
 
+// No bounding-box line covers the pixel.
+constexpr unsigned NO_LINE = 0xffffffffu;
+
+// Per-pixel passes over whole frames (background fill, line stops): a block
+// covers FILL_ROWS rows of one frame, its threads stride along each row.
+constexpr int FILL_ROWS = 8;
+constexpr int FILL_THREADS = 256;
+
 __device__ __forceinline__ void setup_ray(const FrameDesc& f, int px, int py, RaySetup& r) {
   float nx = ((float)px + 0.5f) / (float)f.width * 2.f - 1.f;
   float ny = 1.f - ((float)py + 0.5f) / (float)f.height * 2.f;
@@ -311,6 +319,57 @@ __device__ __forceinline__ void setup_ray(const FrameDesc& f, int px, int py, Ra
   // a chord through the unit-normalised box is at most sqrt(3) long; the
   // comparison also rejects NaN rays from degenerate matrices
   r.hit = t1 > t0 && (t1 - t0) < 4.0f;
+}
+
+// The pixel is covered by a bounding-box line with key `line`: opaque
+// geometry at NDC depth z, so the ray ends where it reaches that depth (the
+// ray's point a + (z + 1) / 2 (b - a) in homogeneous world coordinates, with
+// a, b its near and far points as in setup_ray).  Returns that ray parameter.
+__device__ __forceinline__ float line_stop_t(const FrameDesc& f, int px, int py, unsigned line) {
+  RaySetup r;
+  setup_ray(f, px, py, r);
+  const float nx = ((float)px + 0.5f) / (float)f.width * 2.f - 1.f;
+  const float ny = 1.f - ((float)py + 0.5f) / (float)f.height * 2.f;
+  const float* M = f.inv_vp;
+  const float h = (line_ndc_z(line) + 1.f) * 0.5f;
+  float a[4], g[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float base = M[4 * i] * nx + M[4 * i + 1] * ny + M[4 * i + 3];
+    a[i] = base - M[4 * i + 2];
+    g[i] = fmaf(h, 2.f * M[4 * i + 2], a[i]);
+  }
+  float ts = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) ts = fmaf(g[i] / g[3] - a[i] / a[3], r.dw[i], ts);
+  return ts;
+}
+
+// After the lines are rasterised: each covered pixel's key becomes the ray
+// parameter where its ray ends (float bits, bit 0 still the colour), and the
+// pixel (frame << 32 | pixel) goes to `list`, which the line pass re-renders.
+// NO_LINE (a NaN pattern) stays.
+__device__ __forceinline__ void line_stops_rows(const FrameDesc& f, int frame, int row_block,
+                                                unsigned long long* list, unsigned* count) {
+  unsigned* keys = const_cast<unsigned*>(f.lines);
+  const int y0 = row_block * FILL_ROWS;
+  const int y1 = min(y0 + FILL_ROWS, f.height);
+  const int lane = threadIdx.x & 31;
+  for (int y = y0; y < y1; ++y)
+    for (int x0 = 0; x0 < f.width; x0 += FILL_THREADS) {
+      const int x = x0 + (int)threadIdx.x;
+      const size_t p = (size_t)y * f.width + x;
+      const unsigned k = x < f.width ? keys[p] : NO_LINE;
+      const bool on = k != NO_LINE;
+      if (on) keys[p] = (__float_as_uint(line_stop_t(f, x, y, k)) & ~1u) | (k & 1u);
+      // one atomic per warp for its covered pixels
+      const unsigned m = __ballot_sync(0xffffffffu, on);
+      if (!m) continue;
+      unsigned base = 0;
+      if (lane == __ffs(m) - 1) base = atomicAdd(count, (unsigned)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+      if (on) list[base + __popc(m & ((1u << lane) - 1u))] = ((unsigned long long)frame << 32) | (unsigned long long)p;
+    }
 }
 
 struct Accum {
@@ -553,8 +612,17 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
       acc.A = c.w;
     }
   }
-  const float rem = 1.f - acc.A;
-  return make_float4(fmaf(rem, f.bg[0], acc.C0), fmaf(rem, f.bg[1], acc.C1), fmaf(rem, f.bg[2], acc.C2), acc.A);
+  return make_float4(acc.C0, acc.C1, acc.C2, acc.A);
+}
+
+// What lies behind the volume: the background (adds no opacity), or an
+// opaque bounding-box line.
+__device__ __forceinline__ float4 behind(const FrameDesc& f, float4 c, unsigned line) {
+  const float rem = 1.f - c.w;
+  if (line == NO_LINE)
+    return make_float4(fmaf(rem, f.bg[0], c.x), fmaf(rem, f.bg[1], c.y), fmaf(rem, f.bg[2], c.z), c.w);
+  const float* lc = f.line_rgb[line & 1u];
+  return make_float4(fmaf(rem, lc[0], c.x), fmaf(rem, lc[1], c.y), fmaf(rem, lc[2], c.z), c.w + rem);
 }
 
 template <typename T, int MODE, int SAMPLER>
@@ -567,8 +635,8 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
   if (px < f.width && py < f.height) {
     RaySetup r;
     setup_ray(f, px, py, r);
-    float4 c = march<T, MODE, SAMPLER>(f, r, nsamp, 0, f.light_to);
-    size_t o = (size_t)py * f.width + px;
+    float4 c = behind(f, march<T, MODE, SAMPLER>(f, r, nsamp, 0, f.light_to), NO_LINE);
+    const size_t o = (size_t)py * f.width + px;
     if (f.out_f32) f.out_f32[o] = c;
     if (f.out_rgba8) {
       f.out_rgba8[o] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
@@ -595,8 +663,8 @@ __device__ __forceinline__ void render_tile_u(const FrameDesc& f, const FrameDes
   if (px < f.width && py < f.height) {
     RaySetup r;
     setup_ray(fv, px, py, r);
-    float4 c = march<T, MODE, SAMPLER>(f, r, nsamp, vidx, fv.light_to);
-    size_t o = (size_t)py * f.width + px;
+    float4 c = behind(f, march<T, MODE, SAMPLER>(f, r, nsamp, vidx, fv.light_to), NO_LINE);
+    const size_t o = (size_t)py * f.width + px;
     float4* of = fv.out_f32;
     uchar4* o8 = fv.out_rgba8;
     if (of) of[o] = c;
@@ -661,8 +729,6 @@ __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
 // of one frame; its threads stride along each row (coalesced 4-byte RGBA8 or
 // 16-byte float stores) and skip the rectangle's span on the rows it crosses.
 // No division: the row and column come from the loop counters.
-constexpr int FILL_ROWS = 8;
-constexpr int FILL_THREADS = 256;
 
 __device__ __forceinline__ void fill_outside_rows(const FrameDesc& f, int row_block) {
   const int w = f.width, h = f.height;
@@ -710,12 +776,168 @@ cudaError_t launch_fill_outside_one(const FrameDesc& f, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(FILL_THREADS) k_line_stops(const FrameDesc* __restrict__ frames, int frame0,
+                                                              unsigned long long* list, unsigned* count) {
+  const FrameDesc& f = frames[blockIdx.x];
+  if (f.lines) line_stops_rows(f, frame0 + (int)blockIdx.x, blockIdx.y, list, count);
+}
+
+cudaError_t launch_line_stops(const FrameDesc* frames, int frame0, int nframes, int max_height,
+                              unsigned long long* list, unsigned* count, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (nframes <= 0 || max_height <= 0) return cudaSuccess;
+  if ((max_height + FILL_ROWS - 1) / FILL_ROWS > 65535) return cudaErrorInvalidValue;
+  k_line_stops<<<dim3((unsigned)nframes, (unsigned)((max_height + FILL_ROWS - 1) / FILL_ROWS)), FILL_THREADS, 0, s>>>(
+      frames + frame0, frame0, list, count);
+  return cudaGetLastError();
+}
+
+// Re-render the pixels a bounding-box line covers (after the frame's render):
+// the ray ends at the line's stop, and the line lies behind what the ray
+// composited.  One thread per listed pixel; the sample counters keep the
+// main render's counts.
+template <typename T, int MODE, int SAMPLER>
+__global__ void __launch_bounds__(128) k_render_lines(const FrameDesc* __restrict__ frames,
+                                                      const unsigned long long* __restrict__ list,
+                                                      const unsigned* __restrict__ count) {
+  const unsigned n = *count;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long e = list[i];
+    const FrameDesc& f = frames[e >> 32];
+    const size_t p = (size_t)(e & 0xffffffffull);
+    const int px = (int)(p % (size_t)f.width), py = (int)(p / (size_t)f.width);
+    const unsigned stop = f.lines[p];
+    RaySetup r;
+    setup_ray(f, px, py, r);
+    r.t1 = fminf(r.t1, __uint_as_float(stop));
+    r.hit = r.t1 > r.t0 && (r.t1 - r.t0) < 4.0f;
+    unsigned nsamp = 0;
+    const float4 c = behind(f, march<T, MODE, SAMPLER>(f, r, nsamp, 0, f.light_to), stop);
+    if (f.out_f32) f.out_f32[p] = c;
+    if (f.out_rgba8)
+      f.out_rgba8[p] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
+                                   (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
+                                   (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f),
+                                   (unsigned char)__float2uint_rn(__saturatef(c.w) * 255.f));
+  }
+}
+
 cudaError_t launch_fill_outside(const FrameDesc* frames, int nframes, int max_height, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (nframes <= 0 || max_height <= 0) return cudaSuccess;
   if ((max_height + FILL_ROWS - 1) / FILL_ROWS > 65535) return cudaErrorInvalidValue;
   dim3 grid((unsigned)nframes, (unsigned)((max_height + FILL_ROWS - 1) / FILL_ROWS));
   k_fill_outside<<<grid, FILL_THREADS, 0, s>>>(frames);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Bounding-box lines (Tuvok draws them as GL lines, depth-tested against the
+// volume: RenderWindow.cpp:2208-2225 setGlobalBBox / setLocalBBox).  One block
+// per (segment, view).  The coverage test and the key are FP64 expressions
+// with every operation rounded on its own (no contraction), in the order the
+// oracle evaluates them, so both pick the same pixels and keys bit for bit;
+// the candidate pixels (a band around the projected segment) only need to
+// include every covered one.
+namespace {
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dd(double a, double b) { return __ddiv_rn(a, b); }
+
+struct SegScreen {
+  double sx0, sy0, z0, dx, dy, dz, inv_l2;
+  int ok;
+};
+
+__device__ void project_segment(const LineSeg& s, const LineView& v, SegScreen& o) {
+  double M[16];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j)
+      M[4 * i + j] = da(da(da(dm(v.proj[4 * i], v.view[j]), dm(v.proj[4 * i + 1], v.view[4 + j])),
+                           dm(v.proj[4 * i + 2], v.view[8 + j])),
+                        dm(v.proj[4 * i + 3], v.view[12 + j]));
+  double c0[4], c1[4];
+  for (int i = 0; i < 4; ++i) {
+    c0[i] = da(da(da(dm(M[4 * i], s.a[0]), dm(M[4 * i + 1], s.a[1])), dm(M[4 * i + 2], s.a[2])), M[4 * i + 3]);
+    c1[i] = da(da(da(dm(M[4 * i], s.b[0]), dm(M[4 * i + 1], s.b[1])), dm(M[4 * i + 2], s.b[2])), M[4 * i + 3]);
+  }
+  // clip to the near plane z >= -w
+  const double n0 = da(c0[2], c0[3]), n1 = da(c1[2], c1[3]);
+  o.ok = !(n0 < 0.0 && n1 < 0.0);
+  double p0[4], p1[4];
+  for (int k = 0; k < 4; ++k) { p0[k] = c0[k]; p1[k] = c1[k]; }
+  if (n0 < 0.0) {
+    const double u = dd(n0, ds(n0, n1));
+    for (int k = 0; k < 4; ++k) p0[k] = da(c0[k], dm(u, ds(c1[k], c0[k])));
+  } else if (n1 < 0.0) {
+    const double u = dd(n1, ds(n1, n0));
+    for (int k = 0; k < 4; ++k) p1[k] = da(c1[k], dm(u, ds(c0[k], c1[k])));
+  }
+  if (!(p0[3] > 0.0 && p1[3] > 0.0)) o.ok = 0;
+  const double hw = 0.5 * (double)v.width, hh = 0.5 * (double)v.height;
+  const double sx0 = dm(da(dd(p0[0], p0[3]), 1.0), hw), sy0 = dm(ds(1.0, dd(p0[1], p0[3])), hh);
+  const double sx1 = dm(da(dd(p1[0], p1[3]), 1.0), hw), sy1 = dm(ds(1.0, dd(p1[1], p1[3])), hh);
+  const double z0 = dd(p0[2], p0[3]), z1 = dd(p1[2], p1[3]);
+  o.sx0 = sx0;
+  o.sy0 = sy0;
+  o.z0 = z0;
+  o.dx = ds(sx1, sx0);
+  o.dy = ds(sy1, sy0);
+  o.dz = ds(z1, z0);
+  const double l2 = da(dm(o.dx, o.dx), dm(o.dy, o.dy));
+  o.inv_l2 = l2 > 0.0 ? dd(1.0, l2) : 0.0;
+  // projections beyond 1e8 pixels (a segment grazing the eye plane) are not drawn
+  if (!(fabs(sx0) < 1e8 && fabs(sy0) < 1e8 && fabs(sx1) < 1e8 && fabs(sy1) < 1e8)) o.ok = 0;
+}
+
+__device__ __forceinline__ void cover_pixel(const SegScreen& g, int color, const LineView& v, int px, int py) {
+  const double cx = (double)px + 0.5, cy = (double)py + 0.5;
+  double s = dm(da(dm(ds(cx, g.sx0), g.dx), dm(ds(cy, g.sy0), g.dy)), g.inv_l2);
+  s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+  const double ex = ds(cx, da(g.sx0, dm(s, g.dx))), ey = ds(cy, da(g.sy0, dm(s, g.dy)));
+  const double d2 = da(dm(ex, ex), dm(ey, ey));
+  if (!(d2 <= 0.25)) return;
+  const double zz = da(da(g.z0, dm(s, g.dz)), 2.0);
+  if (!(zz > 0.0)) return;
+  atomicMin(v.keys + (size_t)py * v.width + px, line_key(__double2float_rn(zz), color));
+}
+}  // namespace
+
+__global__ void __launch_bounds__(128) k_raster_lines(const LineSeg* __restrict__ segs,
+                                                      const LineView* __restrict__ views) {
+  __shared__ SegScreen g;
+  const LineView& v = views[blockIdx.y];
+  const int color = segs[blockIdx.x].color;
+  if (threadIdx.x == 0) project_segment(segs[blockIdx.x], v, g);
+  __syncthreads();
+  if (!g.ok) return;
+  const int W = v.width, H = v.height;
+  // march along the major axis; per step the band of 5 pixels around the
+  // segment (a covered pixel's centre is within one pixel of the segment's
+  // point at its column or row)
+  const bool xmaj = fabs(g.dx) >= fabs(g.dy);
+  const double a0 = xmaj ? g.sx0 : g.sy0, da_ = xmaj ? g.dx : g.dy;
+  const double b0 = xmaj ? g.sy0 : g.sx0, db = xmaj ? g.dy : g.dx;
+  const int na = xmaj ? W : H, nb = xmaj ? H : W;
+  const double lo = fmax(fmin(a0, a0 + da_) - 1.0, -1.0), hi = fmin(fmax(a0, a0 + da_) + 1.0, (double)na);
+  const int i0 = max(0, (int)floor(lo)), i1 = min(na - 1, (int)floor(hi));
+  for (int i = i0 + (int)threadIdx.x; i <= i1; i += blockDim.x) {
+    double t = da_ != 0.0 ? ((double)i + 0.5 - a0) / da_ : 0.0;
+    t = fmin(fmax(t, 0.0), 1.0);
+    const int j0 = (int)floor(b0 + t * db) - 2;
+    for (int j = max(j0, 0); j <= min(j0 + 4, nb - 1); ++j) {
+      if (xmaj) cover_pixel(g, color, v, i, j);
+      else cover_pixel(g, color, v, j, i);
+    }
+  }
+}
+
+cudaError_t launch_raster_lines(const LineSeg* segs, int nseg, const LineView* views, int nviews, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (nseg <= 0 || nviews <= 0) return cudaSuccess;
+  if (nviews > 65535) return cudaErrorInvalidValue;
+  k_raster_lines<<<dim3((unsigned)nseg, (unsigned)nviews), 128, 0, s>>>(segs, views);
   return cudaGetLastError();
 }
 
@@ -1011,6 +1233,20 @@ static cudaError_t persistent_u_t(const FrameDesc& shared, const FrameDesc* fram
       default: return cudaErrorInvalidValue;                                                  \
     }                                                                                         \
   } while (0)
+
+template <typename T, int MODE, int SAMPLER>
+static cudaError_t lines_t(const FrameDesc* frames, const unsigned long long* list, const unsigned* count, int grid,
+                           cudaStream_t s) {
+  k_render_lines<T, MODE, SAMPLER><<<grid, 128, 0, s>>>(frames, list, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render_lines(int dtype, int mode, int sampler, const FrameDesc* frames,
+                                const unsigned long long* list, const unsigned* count, int grid, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (grid <= 0) return cudaSuccess;
+  GBVR_DISPATCH(lines_t, dtype, mode, sampler, frames, list, count, grid, s);
+}
 
 cudaError_t launch_render_plain(const FrameDesc& f, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call

@@ -266,6 +266,21 @@ class Renderer:
         pl, pp = _fp(plane)
         L.call("gbvr_set_clip_plane", self._h, 1 if enabled else 0, pp)
 
+    def setGlobalBBox(self, enabled, rgb=None):
+        """setGlobalBBox: draw the dataset box's edges (opaque one-pixel lines
+        at their depth)."""
+        self._bbox = getattr(self, "_bbox", [False, False])
+        self._bbox[0] = bool(enabled)
+        keep, gp = _fp(rgb) if rgb is not None else (None, None)
+        L.call("gbvr_set_bboxes", self._h, int(self._bbox[0]), int(self._bbox[1]), gp, None)
+
+    def setLocalBBox(self, enabled, rgb=None):
+        """setLocalBBox: draw the brick grid of the rendered level."""
+        self._bbox = getattr(self, "_bbox", [False, False])
+        self._bbox[1] = bool(enabled)
+        keep, lp = _fp(rgb) if rgb is not None else (None, None)
+        L.call("gbvr_set_bboxes", self._h, int(self._bbox[0]), int(self._bbox[1]), None, lp)
+
     def setValueRange(self, lo, hi):
         L.call("gbvr_set_value_range", self._h, lo, hi)
 

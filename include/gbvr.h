@@ -206,6 +206,13 @@ int gbvr_paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int 
  * points p (the normalised volume box) with plane[0..2] . p + plane[3] > 0 are dropped; enabled = 0 turns the
  * plane off (plane may then be NULL). */
 int gbvr_set_clip_plane(gbvr_renderer* r, int enabled, const float plane[4]);
+/* setGlobalBBox / setLocalBBox (RenderWindow.cpp:2208-2225, RenderWindow.h:165-166): global draws the 12
+ * edges of the dataset box, local the lines of the rendered level's brick grid (brick interior bounds).
+ * Lines are opaque, one pixel wide (a pixel whose centre lies within half a pixel of a line's projection,
+ * after clipping to the near plane), at their depth: the volume in front of a line composites over it, and
+ * the line replaces the background behind the ray (alpha 1).  Of two lines at one depth the global box
+ * wins.  rgb may be NULL (keep; defaults: global (1, 1, 1), local (0.6, 0.6, 0.6)).  3D views only. */
+int gbvr_set_bboxes(gbvr_renderer* r, int global, int local, const float global_rgb[3], const float local_rgb[3]);
 int gbvr_set_value_range(gbvr_renderer* r, double lo, double hi);         /* TF domain (biasScaleTF) */
 int gbvr_set_iso(gbvr_renderer* r, float value, const float rgb[3]);      /* setIsoValue, setIsosurfaceColor */
 int gbvr_set_lighting(gbvr_renderer* r, int enabled, const float amb[4], const float diff[4],

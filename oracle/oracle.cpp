@@ -504,6 +504,12 @@ struct orc_render_params {
   int width, height;
   int clip_on;              // clip plane: samples with clip . (x, y, z, 1) > 0 (world) are dropped
   double clip[4];
+  // bounding-box lines (the renderer's setGlobalBBox / setLocalBBox)
+  int bbox_global, bbox_local;
+  double line_rgb[2][3];    // global box, brick boxes
+  double view[16], proj[16];  // the float32 view and projection matrices (row-major)
+  i64 brick_interior;       // brick edge minus two ghost layers (the level is one brick if it fits)
+  const uint32_t* line_keys;  // filled by orc_render: per pixel the nearest line's key or 0xffffffff
 };
 
 struct Vol {
@@ -596,6 +602,123 @@ static void shade(const orc_render_params* p, const double g[3], const double vd
   for (int k = 0; k < 3; ++k) out[k] = col[k] * (p->amb[k] + p->diff[k] * nl) + p->spec[k] * sp;
 }
 
+// ---------------------------------------------------------------------------
+// Bounding-box lines.  Segments: the 12 edges of the box [-extent/2,
+// extent/2] and the lines of the level's brick grid (bounds at multiples of
+// the interior size, clamped to the level, at (b / dims) extent - extent/2)
+// that are not edges of the drawn box.  A pixel is covered by a segment when
+// its centre lies within half a pixel of the segment's projection: the
+// segment in clip space (P V x), clipped to the near plane z >= -w, divided
+// by w, mapped to pixels (x + 1) W/2, (1 - y) H/2; the covered point's NDC
+// depth is interpolated linearly along the projected segment.  Key = the
+// float bits of (z + 2) with bit 0 = colour (0 global, 1 brick); the nearest
+// line has the smallest key.  Every expression below is evaluated in the
+// order written, one rounding per operation (-ffp-contract=off), so the keys
+// are reproducible bit for bit.  Projections beyond 1e8 pixels are dropped.
+// ---------------------------------------------------------------------------
+struct OrcSeg {
+  double a[3], b[3];
+  int color;
+};
+
+static void bbox_segments(const orc_render_params* p, std::vector<OrcSeg>& segs) {
+  double h[3];
+  for (int a = 0; a < 3; ++a) h[a] = 0.5 * p->extent[a];
+  const i64 mx = std::max(p->dims[0], std::max(p->dims[1], p->dims[2]));
+  const bool single = mx <= p->brick_interior;
+  const i64 I = single ? mx : p->brick_interior;
+  i64 nb[3];
+  for (int a = 0; a < 3; ++a) nb[a] = single ? 1 : (p->dims[a] + I - 1) / I;
+  auto add = [&](int a, double u, double v, int color) {
+    const int b = (a + 1) % 3, c = (a + 2) % 3;
+    OrcSeg s;
+    s.a[a] = -h[a];
+    s.b[a] = h[a];
+    s.a[b] = s.b[b] = u;
+    s.a[c] = s.b[c] = v;
+    s.color = color;
+    segs.push_back(s);
+  };
+  for (int a = 0; a < 3; ++a) {
+    const int b = (a + 1) % 3, c = (a + 2) % 3;
+    if (p->bbox_global)
+      for (int k = 0; k < 4; ++k) add(a, (k & 1) ? h[b] : -h[b], (k & 2) ? h[c] : -h[c], 0);
+    if (!p->bbox_local) continue;
+    auto bound = [&](int ax, i64 j) {
+      const i64 bj = std::min(j * I, p->dims[ax]);
+      return (double)bj / (double)p->dims[ax] * p->extent[ax] - h[ax];
+    };
+    for (i64 j = 0; j <= nb[b]; ++j)
+      for (i64 k = 0; k <= nb[c]; ++k) {
+        const bool edge = (j == 0 || j == nb[b]) && (k == 0 || k == nb[c]);
+        if (edge && p->bbox_global) continue;
+        add(a, bound(b, j), bound(c, k), 1);
+      }
+  }
+}
+
+static void line_keys(const orc_render_params* p, std::vector<uint32_t>& keys) {
+  const int W = p->width, H = p->height;
+  keys.assign((size_t)W * H, 0xffffffffu);
+  std::vector<OrcSeg> segs;
+  bbox_segments(p, segs);
+  const double* Pm = p->proj;
+  const double* Vm = p->view;
+  double M[16];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j)
+      M[4 * i + j] = Pm[4 * i] * Vm[j] + Pm[4 * i + 1] * Vm[4 + j] + Pm[4 * i + 2] * Vm[8 + j] + Pm[4 * i + 3] * Vm[12 + j];
+  for (const OrcSeg& s : segs) {
+    double c0[4], c1[4];
+    for (int i = 0; i < 4; ++i) {
+      c0[i] = M[4 * i] * s.a[0] + M[4 * i + 1] * s.a[1] + M[4 * i + 2] * s.a[2] + M[4 * i + 3];
+      c1[i] = M[4 * i] * s.b[0] + M[4 * i + 1] * s.b[1] + M[4 * i + 2] * s.b[2] + M[4 * i + 3];
+    }
+    const double n0 = c0[2] + c0[3], n1 = c1[2] + c1[3];
+    if (n0 < 0.0 && n1 < 0.0) continue;
+    double p0[4], p1[4];
+    for (int k = 0; k < 4; ++k) { p0[k] = c0[k]; p1[k] = c1[k]; }
+    if (n0 < 0.0) {
+      const double u = n0 / (n0 - n1);
+      for (int k = 0; k < 4; ++k) p0[k] = c0[k] + u * (c1[k] - c0[k]);
+    } else if (n1 < 0.0) {
+      const double u = n1 / (n1 - n0);
+      for (int k = 0; k < 4; ++k) p1[k] = c1[k] + u * (c0[k] - c1[k]);
+    }
+    if (!(p0[3] > 0.0 && p1[3] > 0.0)) continue;
+    const double hw = 0.5 * (double)W, hh = 0.5 * (double)H;
+    const double sx0 = (p0[0] / p0[3] + 1.0) * hw, sy0 = (1.0 - p0[1] / p0[3]) * hh;
+    const double sx1 = (p1[0] / p1[3] + 1.0) * hw, sy1 = (1.0 - p1[1] / p1[3]) * hh;
+    if (!(std::fabs(sx0) < 1e8 && std::fabs(sy0) < 1e8 && std::fabs(sx1) < 1e8 && std::fabs(sy1) < 1e8)) continue;
+    const double z0 = p0[2] / p0[3], z1 = p1[2] / p1[3];
+    const double dx = sx1 - sx0, dy = sy1 - sy0, dz = z1 - z0;
+    const double l2 = dx * dx + dy * dy;
+    const double inv = l2 > 0.0 ? 1.0 / l2 : 0.0;
+    // every pixel of the segment's bounding box, one pixel wider
+    const i64 x0 = std::max<i64>(0, (i64)std::floor(std::min(sx0, sx1) - 1.0));
+    const i64 x1 = std::min<i64>(W - 1, (i64)std::floor(std::max(sx0, sx1) + 1.0));
+    const i64 y0 = std::max<i64>(0, (i64)std::floor(std::min(sy0, sy1) - 1.0));
+    const i64 y1 = std::min<i64>(H - 1, (i64)std::floor(std::max(sy0, sy1) + 1.0));
+    for (i64 py = y0; py <= y1; ++py)
+      for (i64 px = x0; px <= x1; ++px) {
+        const double cx = (double)px + 0.5, cy = (double)py + 0.5;
+        double t = ((cx - sx0) * dx + (cy - sy0) * dy) * inv;
+        t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+        const double ex = cx - (sx0 + t * dx), ey = cy - (sy0 + t * dy);
+        const double d2 = ex * ex + ey * ey;
+        if (!(d2 <= 0.25)) continue;
+        const double zz = (z0 + t * dz) + 2.0;
+        if (!(zz > 0.0)) continue;
+        const float zf = (float)zz;
+        uint32_t u;
+        memcpy(&u, &zf, 4);
+        u = (u & ~1u) | (uint32_t)s.color;
+        uint32_t& k = keys[(size_t)py * W + px];
+        if (u < k) k = u;
+      }
+  }
+}
+
 static void render_pixel(const orc_render_params* p, int px, int py, double* out,
                          i64* nsamples) {
   Vol V{p};
@@ -621,6 +744,18 @@ static void render_pixel(const orc_render_params* p, int px, int py, double* out
     double ta = (lo - o[k]) / d[k], tb = (hi - o[k]) / d[k];
     t0 = std::max(t0, std::min(ta, tb));
     t1 = std::min(t1, std::max(ta, tb));
+  }
+  // a bounding-box line covering the pixel ends the ray at the line's depth
+  const uint32_t line = p->line_keys ? p->line_keys[(size_t)py * p->width + px] : 0xffffffffu;
+  if (line != 0xffffffffu) {
+    const uint32_t u = line & ~1u;
+    float zf;
+    memcpy(&zf, &u, 4);
+    double g[4], gh[4] = {ndc_x, ndc_y, (double)zf - 2.0, 1.0};
+    mat_vec4(p->inv_viewproj, gh, g);
+    double ts = 0.0;
+    for (int k = 0; k < 3; ++k) ts += (g[k] / g[3] - o[k]) * d[k];
+    t1 = std::min(t1, ts);
   }
   double C[3] = {0, 0, 0}, A = 0;
   // light: travels along light_dir_eye, transformed to world by the inverse view
@@ -728,8 +863,15 @@ static void render_pixel(const orc_render_params* p, int px, int py, double* out
       A = c[3];
     }
   }
-  for (int k = 0; k < 3; ++k) out[k] = C[k] + (1.0 - A) * p->bg[k];
-  out[3] = A;
+  if (line != 0xffffffffu) {
+    // the opaque line behind the volume's samples
+    const double* lc = p->line_rgb[line & 1u];
+    for (int k = 0; k < 3; ++k) out[k] = C[k] + (1.0 - A) * lc[k];
+    out[3] = A + (1.0 - A);
+  } else {
+    for (int k = 0; k < 3; ++k) out[k] = C[k] + (1.0 - A) * p->bg[k];
+    out[3] = A;
+  }
   if (nsamples) *nsamples = ns;
 }
 
@@ -779,7 +921,16 @@ void orc_render_slice(const orc_render_params* p, int axis, double coord, int fl
 // Render `npix` pixels (indices into the width*height image, row 0 = top) or
 // the whole image when pixels == null.  out: [npix][4] doubles.  Returns the
 // number of samples taken.
-i64 orc_render(const orc_render_params* p, const int64_t* pixels, i64 npix, double* out, int threads) {
+i64 orc_render(const orc_render_params* pin, const int64_t* pixels, i64 npix, double* out, int threads) {
+  orc_render_params pc = *pin;
+  const orc_render_params* p = &pc;
+  std::vector<uint32_t> keys;
+  if (pc.bbox_global || pc.bbox_local) {
+    line_keys(p, keys);
+    pc.line_keys = keys.data();
+  } else {
+    pc.line_keys = nullptr;
+  }
   i64 total = pixels ? npix : (i64)p->width * p->height;
   i64 ns_total = 0;
 #ifdef _OPENMP
@@ -793,6 +944,13 @@ i64 orc_render(const orc_render_params* p, const int64_t* pixels, i64 npix, doub
     ns_total += ns;
   }
   return ns_total;
+}
+
+// The per-pixel line keys alone (for the tests of the GPU rasteriser).
+void orc_line_keys(const orc_render_params* p, uint32_t* out) {
+  std::vector<uint32_t> keys;
+  line_keys(p, keys);
+  memcpy(out, keys.data(), sizeof(uint32_t) * keys.size());
 }
 
 int orc_max_threads(void) {

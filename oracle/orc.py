@@ -26,6 +26,8 @@ class RenderParams(C.Structure):
         ("amb", D * 3), ("diff", D * 3), ("spec", D * 3), ("shininess", D),
         ("light_dir_eye", D * 3), ("bg", D * 3), ("inv_viewproj", D * 16), ("inv_view", D * 16),
         ("width", C.c_int), ("height", C.c_int), ("clip_on", C.c_int), ("clip", D * 4),
+        ("bbox_global", C.c_int), ("bbox_local", C.c_int), ("line_rgb", D * 6), ("view", D * 16),
+        ("proj", D * 16), ("brick_interior", I64), ("line_keys", C.c_void_p),
     ]
 
 
@@ -144,11 +146,13 @@ def synth_blobs(params):
 def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0), mode=0,
            interp=1, ert=0.99, extent=None, grad_max=1.0, iso=0.0, iso_rgb=(1, 1, 1), lighting=1,
            amb=(0.1, 0.1, 0.1), diff=(1, 1, 1), spec=(1, 1, 1), shininess=8.0,
-           light_dir=(0, 0, -1), bg=(0, 0, 0), pixels=None, threads=0, clip=None):
+           light_dir=(0, 0, -1), bg=(0, 0, 0), pixels=None, threads=0, clip=None, bbox=None):
     """FP64 render of `vol` (the flat level, (z, y, x)).  mode 0 1D TF, 1 2D TF
     + Phong, 2 isosurface, 3 maximum-intensity projection; clip = plane
-    (a, b, c, d) dropping samples with a x + b y + c z + d > 0.  Returns
-    (rgba float64 [n, 4] or [h, w, 4], samples)."""
+    (a, b, c, d) dropping samples with a x + b y + c z + d > 0; bbox = dict
+    (global_, local, interior = brick edge minus two ghosts, rgb = (global,
+    local) colours) for bounding-box lines.  Returns (rgba float64 [n, 4] or
+    [h, w, 4], samples)."""
     vol = np.ascontiguousarray(vol)
     tf = np.ascontiguousarray(tf, np.float32)
     p = RenderParams()
@@ -187,6 +191,7 @@ def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0)
         p.clip_on = 1
         for i in range(4):
             p.clip[i] = clip[i]
+    _set_lines(p, view, proj, bbox)
     if pixels is None:
         out = np.zeros((height * width, 4), np.float64)
         ns = lib().orc_render(C.byref(p), None, I64(0), out.ctypes.data_as(C.POINTER(D)), threads)
@@ -196,6 +201,37 @@ def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0)
     ns = lib().orc_render(C.byref(p), pix.ctypes.data_as(C.POINTER(I64)), I64(pix.size),
                           out.ctypes.data_as(C.POINTER(D)), threads)
     return out, ns
+
+
+def _set_lines(p, view, proj, bbox):
+    if not bbox:
+        return
+    p.bbox_global = 1 if bbox.get("global_") else 0
+    p.bbox_local = 1 if bbox.get("local") else 0
+    rgb = bbox.get("rgb", ((1.0, 1.0, 1.0), (0.6, 0.6, 0.6)))
+    for c in range(2):
+        for k in range(3):
+            p.line_rgb[3 * c + k] = float(np.float32(rgb[c][k]))
+    v32 = np.asarray(view, np.float32).ravel()
+    p32 = np.asarray(proj, np.float32).ravel()
+    for i in range(16):
+        p.view[i] = float(v32[i])
+        p.proj[i] = float(p32[i])
+    p.brick_interior = int(bbox.get("interior", 1 << 40))
+
+
+def line_keys(dims, extent, view, proj, width, height, bbox):
+    """Per-pixel keys of the nearest bounding-box line ([h, w] uint32,
+    0xffffffff where none) for a level of `dims` (x, y, z)."""
+    p = RenderParams()
+    for i in range(3):
+        p.dims[i] = dims[i]
+        p.extent[i] = extent[i]
+    p.width, p.height = width, height
+    _set_lines(p, view, proj, bbox)
+    out = np.empty((height, width), np.uint32)
+    lib().orc_line_keys(C.byref(p), out.ctypes.data_as(C.c_void_p))
+    return out
 
 
 def render_slice(vol, axis, coord, width, height, tf, value_range=(0.0, 255.0), flip_x=False, flip_y=False,

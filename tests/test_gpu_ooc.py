@@ -235,3 +235,25 @@ def test_paint_path_in_core_equals_views():
         got = [a.readFramebuffer(i, as_float=True) for i in range(4)]
         for i, (view, proj) in enumerate(views):
             assert np.array_equal(got[i], _paint(a, view, proj))
+
+
+def test_ooc_paint_path_with_bboxes_matches_incore():
+    """Bounding-box lines on the pipelined out-of-core path: each frame equals
+    the in-core render at its resolved level with the same lines (the brick
+    grid of that level)."""
+    sp, bp = CASES["u16_200x180x170_b64"]
+    slot = 64 ** 3 * 2
+    views = _inside_path(6, 128, 96)
+    with Renderer(float_fb=True) as a, Renderer(float_fb=True) as b:
+        a.loadSynthetic(sp, **bp)
+        b.loadSyntheticOutOfCore(sp, 30 * slot, **bp)
+        for r in (a, b):
+            _setup(r, sp, 128, 96)
+            r.setGlobalBBox(True)
+            r.setLocalBBox(True, (0.2, 0.8, 0.4))
+        lod, _, _ = b.paintPath(views)
+        frames = [b.readFramebuffer(i, as_float=True) for i in range(len(views))]
+        for i, (view, proj) in enumerate(views):
+            a.setLODLimits(int(lod[i]), int(lod[i]))
+            assert np.array_equal(frames[i], _paint(a, view, proj)), i
+        assert any((f[..., 3] == 1.0).sum() > 50 for f in frames)

@@ -137,6 +137,7 @@ SIGNATURES = {
     "gbvr_set_render_mode": [P, I],
     "gbvr_set_clip_plane": [P, I, FP],
     "gbvr_set_bboxes": [P, I, I, FP, FP],
+    "gbvr_set_clearview": [P, I, F, FP, F, F, F, F, F],
     "gbvr_paint_slice": [P, I, C.c_int64, I, I, I],
     "gbvr_paint_path": [P, C.POINTER(View), I, C.POINTER(C.c_int32), U64P, U64P],
     "gbvr_paint_batch_async": [P, C.POINTER(View), I, I],

@@ -910,6 +910,12 @@ struct gbvr_renderer {
   int bbox_global = 0, bbox_local = 0;
   float bbox_rgb[2][3] = {{1.f, 1.f, 1.f}, {0.6f, 0.6f, 0.6f}};
   DevBuf d_line_keys, d_line_segs, d_line_views, d_line_list, d_line_count;
+  // ClearView (isosurface mode): focus iso value and colour, lens size
+  // (radius = size * min(width, height) / 2 pixels), context and border
+  // scales, focus point in pixels (row 0 = top)
+  int cv_on = 0;
+  float cv_iso = 0.f, cv_rgb[3] = {1.f, 1.f, 1.f}, cv_size = 0.5f, cv_context = 1.f, cv_border = 1.f;
+  float cv_fx = -1.f, cv_fy = -1.f;
   std::vector<float> tf1d;
   std::vector<float> tf2d;
   int tf2d_w = 0, tf2d_h = 0;
@@ -1077,6 +1083,12 @@ void ensure_tf(gbvr_renderer* r) {
   }
 }
 
+// The iso value that empty-space classification uses: with ClearView the
+// march also looks for the focus surface, so the lower of the two.
+float skip_iso(const gbvr_renderer* r) {
+  return r->cv_on && r->mode == GBVR_RM_ISOSURFACE ? std::min(r->iso, r->cv_iso) : r->iso;
+}
+
 int upload_tf(gbvr_renderer* r, int level) {
   ensure_tf(r);
   const bool two = r->mode == GBVR_RM_2DTRANS;
@@ -1105,7 +1117,7 @@ int upload_tf(gbvr_renderer* r, int level) {
       double lo, hi;
       default_range(r, lo, hi);
       int w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4), h = two ? r->tf2d_h : 1;
-      TRY(classify_level(r->ds, level, tf, w, h, r->mode, lo, hi, r->iso, r->d_tfprefix, r->d_skip, *r->occ_lv[level],
+      TRY(classify_level(r->ds, level, tf, w, h, r->mode, lo, hi, skip_iso(r), r->d_tfprefix, r->d_skip, *r->occ_lv[level],
                          r->d_occtmp, r->stream));
       r->occ_valid[level] = 1;
     }
@@ -1115,7 +1127,7 @@ int upload_tf(gbvr_renderer* r, int level) {
     double lo, hi;
     default_range(r, lo, hi);
     int w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4), h = two ? r->tf2d_h : 1;
-    TRY(classify_level(r->ds, level, tf, w, h, r->mode, lo, hi, r->iso, r->d_tfprefix, r->d_skip, r->d_occ,
+    TRY(classify_level(r->ds, level, tf, w, h, r->mode, lo, hi, skip_iso(r), r->d_tfprefix, r->d_skip, r->d_occ,
                        r->d_occtmp, r->stream));
     r->skip_dirty = false;
     r->skip_level = level;
@@ -1178,7 +1190,27 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
                        ? r->d_cellbits.as<unsigned>() + (size_t)vidx * r->cell_words : nullptr;
   if (r->bbox_global || r->bbox_local) f.lines = r->d_line_keys.as<unsigned>() + (size_t)vidx * npix;
   memcpy(f.line_rgb, r->bbox_rgb, sizeof(f.line_rgb));
+  f.cv_iso = r->cv_iso;
+  memcpy(f.cv_rgb, r->cv_rgb, sizeof(f.cv_rgb));
+  f.cv_context = r->cv_context;
+  f.cv_border = r->cv_border;
   return f;
+}
+
+// ClearView lens pass of one frame (after its render and line pass).
+int render_cv(gbvr_renderer* r, const FrameDesc& f) {
+  if (!r->cv_on || r->mode != GBVR_RM_ISOSURFACE) return GBVR_OK;
+  CvLens L;
+  L.fx = r->cv_fx;
+  L.fy = r->cv_fy;
+  L.radius = r->cv_size * 0.5f * (float)std::min(r->width, r->height);
+  if (!(L.radius > 0.f)) return GBVR_OK;
+  L.x0 = (int)std::max(0.f, std::floor(L.fx - L.radius));
+  L.y0 = (int)std::max(0.f, std::floor(L.fy - L.radius));
+  L.x1 = (int)std::min((float)r->width, std::ceil(L.fx + L.radius) + 1.f);
+  L.y1 = (int)std::min((float)r->height, std::ceil(L.fy + L.radius) + 1.f);
+  CUDA_TRY(launch_render_cv(f, L, r->stream));
+  return GBVR_OK;
 }
 
 // World-space segments of the bounding boxes at `level`: the 12 edges of the
@@ -1384,7 +1416,7 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
   default_range(r, vlo, vhi);
   const float idx_scale = (float)((w - 1) / (vhi - vlo)), lo_f = (float)vlo;
   auto nonempty = [&](const BrickInfo& b) {
-    if (r->mode == GBVR_RM_ISOSURFACE) return b.vmax >= r->iso;
+    if (r->mode == GBVR_RM_ISOSURFACE) return b.vmax >= skip_iso(r);
     if (r->mode == GBVR_RM_MIP) return true;
     float ilo = std::min(std::max((b.vmin - lo_f) * idx_scale, 0.f), (float)(w - 1));
     float ihi = std::min(std::max((b.vmax - lo_f) * idx_scale, 0.f), (float)(w - 1));
@@ -1636,8 +1668,14 @@ int paint_plain(gbvr_renderer* r, const gbvr_view* views, int n) {
     TRY(line_stops_one(r, f, v, v == 0));
     CUDA_TRY(launch_fill_outside_one(f, r->stream));
     CUDA_TRY(launch_render_plain(f, r->stream));
+    if (!lines_on(r)) TRY(render_cv(r, f));
   }
   TRY(render_lines(r));
+  if (lines_on(r))
+    for (int v = 0; v < n; ++v) {
+      const float *vw = views ? views[v].view : cur.view, *pj = views ? views[v].proj : cur.proj;
+      TRY(render_cv(r, make_frame(r, vw, pj, level, v)));
+    }
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
   r->last_h2d = 0;  // descriptors travel as kernel parameters
@@ -1768,6 +1806,7 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
     CUDA_TRY(launch_fill_outside_one(f, r->stream));
     CUDA_TRY(launch_render_plain(f, r->stream));
     TRY(render_lines(r));  // while the frame's bricks are resident
+    TRY(render_cv(r, f));
     CUDA_TRY(cudaEventRecord(r->ev_done[st], r->stream));
     if (lod_out) lod_out[i] = level;
     if (miss_out) miss_out[i] = miss;
@@ -1870,6 +1909,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
                                                  r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream);
     if (le != cudaSuccess) return cuda_fail(le, "persistent launch");
     TRY(render_lines(r));
+    TRY(render_cv(r, hf[0]));
     CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
     CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
     r->last_h2d = sizeof(FrameDesc) + sizeof(int) * 2;
@@ -1917,6 +1957,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
   CUDA_TRY(cudaEventRecord(r->evk0, r->stream));  // kernel time: the raycast alone
   CUDA_TRY(cudaGraphLaunch(it->second.exec, r->stream));
   TRY(render_lines(r));
+  for (int v = 0; v < n; ++v) TRY(render_cv(r, hf[v]));
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
   r->last_h2d = sizeof(FrameDesc) * n + sizeof(int) * (n + 1);
@@ -2480,6 +2521,24 @@ int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, v
   CUDA_TRY(cudaMemcpyAsync(host, (const char*)fb + per * first, per * n, cudaMemcpyDeviceToHost, r->read_stream));
   CUDA_TRY(cudaEventRecord(r->slot_read[slot], r->read_stream));
   r->slot_read_pending[slot] = true;
+  return GBVR_OK;
+}
+
+int gbvr_set_clearview(gbvr_renderer* r, int enabled, float iso, const float rgb[3], float size, float context_scale,
+                       float border_scale, float focus_x, float focus_y) {
+  TRY(check_r(r));
+  TRY(settle_async(r));
+  if (enabled && !(size > 0.f)) return fail(GBVR_EINVAL, "lens size must be positive");
+  r->cv_on = enabled ? 1 : 0;
+  r->cv_iso = iso;
+  if (rgb) for (int k = 0; k < 3; ++k) r->cv_rgb[k] = rgb[k];
+  r->cv_size = size;
+  r->cv_context = context_scale;
+  r->cv_border = border_scale;
+  r->cv_fx = focus_x;
+  r->cv_fy = focus_y;
+  r->skip_dirty = true;  // classification uses the lower iso value while on
+  r->drop_graphs();
   return GBVR_OK;
 }
 

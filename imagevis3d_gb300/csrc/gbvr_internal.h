@@ -100,6 +100,10 @@ struct __align__(16) FrameDesc {
   // view.
   const unsigned* lines;
   float line_rgb[2][3];      // colour of the global box (key bit 0 = 0) and of the brick boxes (1)
+  // ClearView (isosurface mode, the lens pass only): the focus surface's
+  // iso value and colour, the context and border scales of the context
+  // surface's opacity
+  float cv_iso, cv_rgb[3], cv_context, cv_border;
   int tile_w;                // ray tile of one warp: tile_w x (32 / tile_w) pixels
   int perm;                  // brick layout copy: 0 x-fastest, 1 y-fastest, 2 z-fastest, 3 4^3 blocks
   unsigned long long copy_off;  // element offset of that copy in the pool
@@ -207,6 +211,13 @@ cudaError_t launch_line_stops(const FrameDesc* frames, int frame0, int nframes, 
 // at the line and the line behind (grid-stride over *count)
 cudaError_t launch_render_lines(int dtype, int mode, int sampler, const FrameDesc* frames,
                                 const unsigned long long* list, const unsigned* count, int grid, cudaStream_t s);
+// ClearView lens: the pixel rectangle [x0, x1) x [y0, y1) around the focus
+// point (fx, fy) (pixels, row 0 = top) and the lens radius in pixels
+struct CvLens {
+  int x0, y0, x1, y1;
+  float fx, fy, radius;
+};
+cudaError_t launch_render_cv(const FrameDesc& f, const CvLens& L, cudaStream_t s);
 // keys of every view (set to 0xffffffff beforehand) <- the nearest covering line
 cudaError_t launch_raster_lines(const LineSeg* segs, int nseg, const LineView* views, int nviews, cudaStream_t s);
 

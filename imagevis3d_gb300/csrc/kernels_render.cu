@@ -390,10 +390,18 @@ __device__ __forceinline__ bool composite(const FrameDesc& f, float4 c, Accum& a
   return acc.A >= f.ert;
 }
 
-template <typename T, int MODE, int SAMPLER>
-__device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, int vidx, const float* light_to) {
+// CV (isosurface mode only): ClearView.  The first hit of f.iso is the
+// context surface; inside the lens (cv_rho < 1: distance to the focus point
+// over the lens radius) it gets opacity clamp(cv_context (1 - |n.v|) +
+// cv_border rho^2, 0, 1), and the march goes on to the first hit of f.cv_iso
+// (the focus surface, from the context hit's sample on), which lies behind.
+template <typename T, int MODE, int SAMPLER, bool CV = false>
+__device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, int vidx, const float* light_to,
+                        float cv_rho = 2.f) {
   Accum acc = {0.f, 0.f, 0.f, 0.f};
   float runmax = -INFINITY;  // MIP: largest sample so far
+  int cv_phase = 0;          // ClearView: 0 looking for the context surface, 1 for the focus surface
+  float cv_a = 1.f, cv_c[3] = {0.f, 0.f, 0.f};
   if (r.hit) {
     const float dt = f.dt;
     const float t0 = r.t0;
@@ -547,7 +555,8 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
         const float v = sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z, c.fx, c.fy, c.fz);
         ++nsamp;
         if (MODE == MODE_ISO) {
-          if (v >= f.iso) {
+          const float thr = (CV && cv_phase) ? f.cv_iso : f.iso;
+          if (v >= thr) {
             float tl = k == 0 ? t0 : fmaf((float)k - 0.5f, dt, t0), th = fmaf((float)k + 0.5f, dt, t0);
 #pragma unroll 1
             for (int it = 0; it < 4; ++it) {
@@ -564,7 +573,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
               else
                 vm = sample_anywhere<T, SAMPLER>(f, fmaf(tm, r.dv[0], r.ov[0]), fmaf(tm, r.dv[1], r.ov[1]),
                                                  fmaf(tm, r.dv[2], r.ov[2]));
-              if (vm >= f.iso) th = tm;
+              if (vm >= thr) th = tm;
               else tl = tm;
             }
             float th2 = 0.5f * (tl + th);
@@ -577,8 +586,28 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
             g[0] *= f.vox_scale[0];
             g[1] *= f.vox_scale[1];
             g[2] *= f.vox_scale[2];
-            if (f.lighting) shade(f, light_to, g, V, f.iso_rgb, col);
-            else { col[0] = f.iso_rgb[0]; col[1] = f.iso_rgb[1]; col[2] = f.iso_rgb[2]; }
+            const float* rgb = (CV && cv_phase) ? f.cv_rgb : f.iso_rgb;
+            if (f.lighting) shade(f, light_to, g, V, rgb, col);
+            else { col[0] = rgb[0]; col[1] = rgb[1]; col[2] = rgb[2]; }
+            if constexpr (CV) {
+              if (cv_phase == 0) {
+                const float gl = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+                const float nv = gl > 0.f ? fabsf(g[0] * V[0] + g[1] * V[1] + g[2] * V[2]) / gl : 1.f;
+                const float a = cv_rho < 1.f ? __saturatef(fmaf(f.cv_border * cv_rho, cv_rho, f.cv_context * (1.f - nv)))
+                                             : 1.f;
+                if (a < 1.f) {
+                  cv_a = a;
+                  cv_c[0] = col[0]; cv_c[1] = col[1]; cv_c[2] = col[2];
+                  cv_phase = 1;
+                  --k;  // the focus surface may cross at this sample too
+                  continue;
+                }
+              } else {
+                // the context over the focus surface
+#pragma unroll
+                for (int q = 0; q < 3; ++q) col[q] = fmaf(cv_a, cv_c[q], (1.f - cv_a) * col[q]);
+              }
+            }
             acc.C0 = col[0]; acc.C1 = col[1]; acc.C2 = col[2];
             acc.A = 1.f;
             done = true;
@@ -600,6 +629,15 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
         if (composite<MODE>(f, cl, acc)) { done = true; break; }
       }
       }
+    }
+  }
+  if constexpr (CV) {
+    if (cv_phase == 1 && acc.A < 1.f) {
+      // no focus surface behind the context surface
+      acc.C0 = cv_a * cv_c[0];
+      acc.C1 = cv_a * cv_c[1];
+      acc.C2 = cv_a * cv_c[2];
+      acc.A = cv_a;
     }
   }
   if constexpr (MODE == MODE_MIP) {
@@ -1233,6 +1271,58 @@ static cudaError_t persistent_u_t(const FrameDesc& shared, const FrameDesc* fram
       default: return cudaErrorInvalidValue;                                                  \
     }                                                                                         \
   } while (0)
+
+// ClearView lens pass (isosurface mode), after the frame's render and line
+// pass: the pixels inside the lens circle are rendered again with the
+// context surface made partly transparent over the focus surface (see march);
+// pixels outside keep the main render.  One warp per 8x4 pixel tile of the
+// lens's bounding rectangle.
+template <typename T, int SAMPLER>
+__global__ void __launch_bounds__(128) k_render_cv(const __grid_constant__ FrameDesc f, const CvLens L) {
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  const int tw = (L.x1 - L.x0 + 7) / 8;
+  const int px = L.x0 + (warp % tw) * 8 + (lane & 7), py = L.y0 + (warp / tw) * 4 + (lane >> 3);
+  if (px >= L.x1 || py >= L.y1) return;
+  const float dx = (float)px + 0.5f - L.fx, dy = (float)py + 0.5f - L.fy;
+  const float rho = sqrtf(dx * dx + dy * dy) / L.radius;
+  if (!(rho < 1.f)) return;
+  const size_t p = (size_t)py * f.width + px;
+  RaySetup r;
+  setup_ray(f, px, py, r);
+  unsigned stop = NO_LINE;
+  if (f.lines) {
+    stop = f.lines[p];
+    r.t1 = fminf(r.t1, __uint_as_float(stop));
+    r.hit = r.t1 > r.t0 && (r.t1 - r.t0) < 4.0f;
+  }
+  unsigned nsamp = 0;
+  const float4 c = behind(f, march<T, MODE_ISO, SAMPLER, true>(f, r, nsamp, 0, f.light_to, rho), stop);
+  if (f.out_f32) f.out_f32[p] = c;
+  if (f.out_rgba8)
+    f.out_rgba8[p] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
+                                 (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
+                                 (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f),
+                                 (unsigned char)__float2uint_rn(__saturatef(c.w) * 255.f));
+}
+
+template <typename T, int SAMPLER>
+static cudaError_t cv_t(const FrameDesc& f, const CvLens& L, cudaStream_t s) {
+  const long long tiles = (long long)((L.x1 - L.x0 + 7) / 8) * ((L.y1 - L.y0 + 3) / 4);
+  k_render_cv<T, SAMPLER><<<(unsigned)((tiles + 3) / 4), 128, 0, s>>>(f, L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render_cv(const FrameDesc& f, const CvLens& L, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (L.x1 <= L.x0 || L.y1 <= L.y0 || !(L.radius > 0.f)) return cudaSuccess;
+  const bool tex = f.sampler == SAMPLER_TEX;
+  switch (f.dtype) {
+    case 0: return tex ? cv_t<uint8_t, SAMPLER_TEX>(f, L, s) : cv_t<uint8_t, SAMPLER_SW>(f, L, s);
+    case 1: return tex ? cv_t<uint16_t, SAMPLER_TEX>(f, L, s) : cv_t<uint16_t, SAMPLER_SW>(f, L, s);
+    case 2: return tex ? cv_t<float, SAMPLER_TEX>(f, L, s) : cv_t<float, SAMPLER_SW>(f, L, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 template <typename T, int MODE, int SAMPLER>
 static cudaError_t lines_t(const FrameDesc* frames, const unsigned long long* list, const unsigned* count, int grid,

@@ -281,6 +281,46 @@ class Renderer:
         keep, lp = _fp(rgb) if rgb is not None else (None, None)
         L.call("gbvr_set_bboxes", self._h, int(self._bbox[0]), int(self._bbox[1]), None, lp)
 
+    # ---- ClearView (setCV, setCVIsoValue, setCVColor, setCVSize,
+    # setCVContextScale, setCVBorderScale, setCVFocusPos) ----
+    def _cv_state(self):
+        if not hasattr(self, "_cv"):
+            self._cv = dict(on=False, iso=0.0, rgb=(1.0, 1.0, 1.0), size=0.5, context=1.0, border=1.0,
+                            fx=-1.0, fy=-1.0)
+        return self._cv
+
+    def _cv_apply(self):
+        c = self._cv
+        keep, rp = _fp(c["rgb"])
+        L.call("gbvr_set_clearview", self._h, int(c["on"]), c["iso"], rp, c["size"], c["context"], c["border"],
+               c["fx"], c["fy"])
+
+    def _cv_set(self, **kw):
+        self._cv_state().update(kw)
+        self._cv_apply()
+
+    def setCV(self, enabled):
+        self._cv_set(on=bool(enabled))
+
+    def setCVIsoValue(self, value):
+        self._cv_set(iso=float(value))
+
+    def setCVColor(self, rgb):
+        self._cv_set(rgb=tuple(float(x) for x in rgb))
+
+    def setCVSize(self, size):
+        self._cv_set(size=float(size))
+
+    def setCVContextScale(self, scale):
+        self._cv_set(context=float(scale))
+
+    def setCVBorderScale(self, scale):
+        self._cv_set(border=float(scale))
+
+    def setCVFocusPos(self, x, y):
+        """Focus point in pixels (row 0 = top), as the mouse position."""
+        self._cv_set(fx=float(x), fy=float(y))
+
     def setValueRange(self, lo, hi):
         L.call("gbvr_set_value_range", self._h, lo, hi)
 

@@ -213,6 +213,17 @@ int gbvr_set_clip_plane(gbvr_renderer* r, int enabled, const float plane[4]);
  * the line replaces the background behind the ray (alpha 1).  Of two lines at one depth the global box
  * wins.  rgb may be NULL (keep; defaults: global (1, 1, 1), local (0.6, 0.6, 0.6)).  3D views only. */
 int gbvr_set_bboxes(gbvr_renderer* r, int global, int local, const float global_rgb[3], const float local_rgb[3]);
+/* ClearView (setCV, setCVIsoValue, setCVColor, setCVSize, setCVContextScale, setCVBorderScale, setCVFocusPos:
+ * RenderWindow.cpp:2155-2206,2337-2367; the focus-and-context technique of Krueger, Schneider and Westermann,
+ * IEEE Vis 2006), isosurface mode only.  The first hit of the iso value (gbvr_set_iso) is the context
+ * surface, the first hit of `iso` behind it the focus surface (colour rgb, shaded alike).  Inside the lens,
+ * a circle of radius size * min(width, height) / 2 pixels around the focus point (focus_x, focus_y in pixels,
+ * row 0 = top), the context surface gets opacity a = clamp(context_scale (1 - |n.v|) + border_scale rho^2,
+ * 0, 1) (n its normal, v the view direction, rho the distance to the focus point over the radius) and is
+ * composited over the focus surface (or the background); elsewhere it is opaque.  Rays that meet no
+ * context surface show the background, as in isosurface mode.  rgb may be NULL (keep). */
+int gbvr_set_clearview(gbvr_renderer* r, int enabled, float iso, const float rgb[3], float size, float context_scale,
+                       float border_scale, float focus_x, float focus_y);
 int gbvr_set_value_range(gbvr_renderer* r, double lo, double hi);         /* TF domain (biasScaleTF) */
 int gbvr_set_iso(gbvr_renderer* r, float value, const float rgb[3]);      /* setIsoValue, setIsosurfaceColor */
 int gbvr_set_lighting(gbvr_renderer* r, int enabled, const float amb[4], const float diff[4],

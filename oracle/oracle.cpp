@@ -510,6 +510,11 @@ struct orc_render_params {
   double view[16], proj[16];  // the float32 view and projection matrices (row-major)
   i64 brick_interior;       // brick edge minus two ghost layers (the level is one brick if it fits)
   const uint32_t* line_keys;  // filled by orc_render: per pixel the nearest line's key or 0xffffffff
+  // ClearView (mode 2): the first hit of iso is the context surface; inside the lens (distance to the
+  // focus point in pixels over cv_radius < 1) it gets opacity clamp(cv_context (1 - |n.v|) + cv_border
+  // rho^2, 0, 1) over the first hit of cv_iso from the context hit's sample on (colour cv_rgb)
+  int cv_on;
+  double cv_iso, cv_rgb[3], cv_context, cv_border, cv_focus[2], cv_radius;
 };
 
 struct Vol {
@@ -787,6 +792,14 @@ static void render_pixel(const orc_render_params* p, int px, int py, double* out
     double prev_t = t0;
     double vmax = -std::numeric_limits<double>::infinity();
     bool any = false;
+    // ClearView state: phase 0 looks for the context surface, 1 for the focus surface
+    int cv_phase = 0;
+    double cv_a = 1.0, cv_c[3] = {0, 0, 0};
+    double cv_rho = 2.0;
+    if (p->cv_on && p->mode == 2) {
+      const double dx = px + 0.5 - p->cv_focus[0], dy = py + 0.5 - p->cv_focus[1];
+      cv_rho = std::sqrt(dx * dx + dy * dy) / p->cv_radius;
+    }
     for (i64 k = 0; k < nk; ++k) {
       double t = t0 + (k + 0.5) * dt;
       if (p->clip_on) {
@@ -809,20 +822,37 @@ static void render_pixel(const orc_render_params* p, int px, int py, double* out
         continue;
       }
       if (p->mode == 2) {
-        if (v >= p->iso) {
+        const double thr = cv_phase ? p->cv_iso : p->iso;
+        if (v >= thr) {
           double tl = (k == 0) ? t0 : prev_t, th = t;
           for (int it = 0; it < 4; ++it) {
             double tm = 0.5 * (tl + th), xm[3];
             to_vox(tm, xm);
-            if (V.sample(xm[0], xm[1], xm[2]) >= p->iso) th = tm;
+            if (V.sample(xm[0], xm[1], xm[2]) >= thr) th = tm;
             else tl = tm;
           }
           double th_hit = 0.5 * (tl + th), xh[3], g[3], col[3];
           to_vox(th_hit, xh);
           V.gradient(xh[0], xh[1], xh[2], g);
           for (int c = 0; c < 3; ++c) g[c] *= scale_v[c];  // world-space direction
-          if (p->lighting) shade(p, g, d, L, p->iso_rgb, col);
-          else for (int c = 0; c < 3; ++c) col[c] = p->iso_rgb[c];
+          const double* rgb = cv_phase ? p->cv_rgb : p->iso_rgb;
+          if (p->lighting) shade(p, g, d, L, rgb, col);
+          else for (int c = 0; c < 3; ++c) col[c] = rgb[c];
+          if (p->cv_on && cv_phase == 0) {
+            const double gl = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+            const double nv = gl > 0 ? std::fabs(g[0] * d[0] + g[1] * d[1] + g[2] * d[2]) / gl : 1.0;
+            double a = 1.0;
+            if (cv_rho < 1.0) a = std::min(1.0, std::max(0.0, p->cv_border * cv_rho * cv_rho + p->cv_context * (1.0 - nv)));
+            if (a < 1.0) {
+              cv_a = a;
+              for (int c = 0; c < 3; ++c) cv_c[c] = col[c];
+              cv_phase = 1;
+              --k;  // the focus surface may cross at this sample too
+              continue;
+            }
+          } else if (p->cv_on) {
+            for (int c = 0; c < 3; ++c) col[c] = cv_a * cv_c[c] + (1.0 - cv_a) * col[c];
+          }
           for (int c = 0; c < 3; ++c) C[c] = col[c];
           A = 1.0;
           break;
@@ -854,6 +884,11 @@ static void render_pixel(const orc_render_params* p, int px, int py, double* out
       C[2] += w * c[2];
       A += w;
       if (A >= p->ert) break;
+    }
+    if (cv_phase == 1 && A < 1.0) {
+      // no focus surface behind the context surface
+      for (int c = 0; c < 3; ++c) C[c] = cv_a * cv_c[c];
+      A = cv_a;
     }
     if (p->mode == 3 && any) {
       // maximum-intensity projection: the maximum through the 1D TF, once

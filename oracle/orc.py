@@ -28,6 +28,8 @@ class RenderParams(C.Structure):
         ("width", C.c_int), ("height", C.c_int), ("clip_on", C.c_int), ("clip", D * 4),
         ("bbox_global", C.c_int), ("bbox_local", C.c_int), ("line_rgb", D * 6), ("view", D * 16),
         ("proj", D * 16), ("brick_interior", I64), ("line_keys", C.c_void_p),
+        ("cv_on", C.c_int), ("cv_iso", D), ("cv_rgb", D * 3), ("cv_context", D), ("cv_border", D),
+        ("cv_focus", D * 2), ("cv_radius", D),
     ]
 
 
@@ -146,13 +148,14 @@ def synth_blobs(params):
 def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0), mode=0,
            interp=1, ert=0.99, extent=None, grad_max=1.0, iso=0.0, iso_rgb=(1, 1, 1), lighting=1,
            amb=(0.1, 0.1, 0.1), diff=(1, 1, 1), spec=(1, 1, 1), shininess=8.0,
-           light_dir=(0, 0, -1), bg=(0, 0, 0), pixels=None, threads=0, clip=None, bbox=None):
+           light_dir=(0, 0, -1), bg=(0, 0, 0), pixels=None, threads=0, clip=None, bbox=None, cv=None):
     """FP64 render of `vol` (the flat level, (z, y, x)).  mode 0 1D TF, 1 2D TF
     + Phong, 2 isosurface, 3 maximum-intensity projection; clip = plane
     (a, b, c, d) dropping samples with a x + b y + c z + d > 0; bbox = dict
     (global_, local, interior = brick edge minus two ghosts, rgb = (global,
-    local) colours) for bounding-box lines.  Returns (rgba float64 [n, 4] or
-    [h, w, 4], samples)."""
+    local) colours) for bounding-box lines; cv = dict(iso, rgb, context,
+    border, focus = (x, y) pixels, radius pixels) for ClearView (mode 2).
+    Returns (rgba float64 [n, 4] or [h, w, 4], samples)."""
     vol = np.ascontiguousarray(vol)
     tf = np.ascontiguousarray(tf, np.float32)
     p = RenderParams()
@@ -192,6 +195,15 @@ def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0)
         for i in range(4):
             p.clip[i] = clip[i]
     _set_lines(p, view, proj, bbox)
+    if cv:
+        p.cv_on = 1
+        p.cv_iso = cv["iso"]
+        for k in range(3):
+            p.cv_rgb[k] = float(np.float32(cv.get("rgb", (1, 1, 1))[k]))
+        p.cv_context = float(np.float32(cv.get("context", 1.0)))
+        p.cv_border = float(np.float32(cv.get("border", 1.0)))
+        p.cv_focus[0], p.cv_focus[1] = (float(np.float32(x)) for x in cv["focus"])
+        p.cv_radius = float(np.float32(cv["radius"]))
     if pixels is None:
         out = np.zeros((height * width, 4), np.float64)
         ns = lib().orc_render(C.byref(p), None, I64(0), out.ctypes.data_as(C.POINTER(D)), threads)

@@ -9,7 +9,12 @@ TOL_RMS = 0.5 / 255.0
 
 
 def image_error(gpu, ref):
-    d = np.abs(np.asarray(gpu, np.float64) - np.asarray(ref, np.float64))
+    """Max and RMS per-channel error of the images: both saturated to [0, 1]
+    first, as the RGBA8 framebuffer stores them (lit colours can exceed 1 in
+    the float framebuffer, e.g. on specular highlights)."""
+    g = np.clip(np.asarray(gpu, np.float64), 0.0, 1.0)
+    r = np.clip(np.asarray(ref, np.float64), 0.0, 1.0)
+    d = np.abs(g - r)
     return float(d.max()), float(np.sqrt(np.mean(d * d)))
 
 

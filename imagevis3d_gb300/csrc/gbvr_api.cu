@@ -700,10 +700,38 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
     ds.hist1d.assign((size + ds.merge - 1) / ds.merge, 0);
     for (long long i = 0; i < size; ++i) ds.hist1d[i / ds.merge] += full[i];
     ds.bit_width = dtype == DT_U8 ? 8 : 16;
+    // 2D histogram (the in-core rule, bit for bit): its three passes (Smax,
+    // f64 max |grad| at Smax, binning) each regenerate the finest level in
+    // z-slabs with one halo plane on each side for the z differences
+    const long long outsize = (long long)ds.hist1d.size();
+    const size_t n2 = (size_t)outsize * 256;
+    DevBuf d2, dsc, slab;
+    CUDA_TRY(d2.alloc(sizeof(uint64_t) * n2));
+    CUDA_TRY(dsc.alloc(sizeof(Hist2DScratch)));
+    CUDA_TRY(cudaMemsetAsync(d2.p, 0, sizeof(uint64_t) * n2, s));
+    CUDA_TRY(cudaMemsetAsync(dsc.p, 0, sizeof(Hist2DScratch), s));
+    const long long SZ = std::min<long long>(32, dims[2]);
+    CUDA_TRY(slab.alloc(w0.plane * (size_t)(SZ + 2)));
+    for (int pass = 1; pass <= 3; ++pass)
+      for (long long z = 0; z < dims[2]; z += SZ) {
+        const long long ze = std::min(z + SZ, dims[2]);
+        const long long zlo = std::max<long long>(z - 1, 0), zhi = std::min(ze + 1, dims[2]);
+        CUDA_TRY(launch_synth_blobs_planes(td, dims, dtype, zlo, zhi - zlo, slab.p, s));
+        CUDA_TRY(launch_hist2d_slab(slab.p, dtype, dims, z, ze, zlo, ds.gmax, outsize, ds.merge, pass,
+                                    d2.as<unsigned long long>(), dsc.as<Hist2DScratch>(), s));
+      }
+    ds.hist2d.resize(n2);
+    Hist2DScratch hs;
+    CUDA_TRY(cudaMemcpyAsync(ds.hist2d.data(), d2.p, sizeof(uint64_t) * n2, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(&hs, dsc.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    double gm;
+    memcpy(&gm, &hs.gmax_bits, 8);
+    ds.max_grad = (float)gm;
   } else {
     ds.bit_width = 32;
+    ds.max_grad = 0.f;
   }
-  ds.max_grad = 0.f;  // the 2D histogram is not built out of core
   ds.layouts = 1;
   ds.copy_stride = 0;
   ds.ooc = true;

@@ -277,5 +277,13 @@ struct Hist2DScratch {
 cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], double max_scalar,
                           long long nx, long long merge, unsigned long long* hist,
                           Hist2DScratch* scratch, cudaStream_t s);
+// One of the three passes (1: Smax, 2: f64 max |grad| at Smax, 3: binning)
+// over the planes [zb, ze) of a volume streamed in z: `slab` holds planes
+// zlo .. (zlo <= zb - 1 unless zb = 0, and plane ze unless ze = Z).  The
+// scratch is zeroed once before the first slab of pass 1; every slab of a
+// pass before the next pass.
+cudaError_t launch_hist2d_slab(const void* slab, int dtype, const long long dims[3], long long zb, long long ze,
+                               long long zlo, double max_scalar, long long nx, long long merge, int pass,
+                               unsigned long long* hist, Hist2DScratch* scratch, cudaStream_t s);
 
 }  // namespace gbvr

@@ -514,13 +514,18 @@ __device__ __noinline__ double grad_f64(const T* __restrict__ v, long long X, lo
 
 // The three passes walk the volume row by row (one CTA per z-slab of rows,
 // threads along x) so no voxel pays for a 64-bit division of its index.
+// They cover the planes [zb, ze) of a Z-plane volume of which `v` holds the
+// planes from zlo on (a slab of a volume streamed in z: the planes zb - 1
+// and ze, where they exist, must be present for the z differences); the
+// whole volume is zb = zlo = 0, ze = Z.
 template <typename T>
-__global__ void k_hist2d_pass1(const T* __restrict__ v, long long X, long long Y, long long Z, Hist2DScratch* sc) {
+__global__ void k_hist2d_pass1(const T* __restrict__ v, long long X, long long Y, long long Z, long long zb,
+                               long long ze, long long zlo, Hist2DScratch* sc) {
   unsigned long long smax = 0;
-  for (long long row = blockIdx.x; row < Y * Z; row += gridDim.x) {
-    const long long z = row / Y, y = row - z * Y;
+  for (long long row = blockIdx.x; row < Y * (ze - zb); row += gridDim.x) {
+    const long long zr = row / Y, y = row - zr * Y, z = zb + zr;
     for (long long x = threadIdx.x; x < X; x += blockDim.x) {
-      const long long i = row * X + x;
+      const long long i = ((z - zlo) * Y + y) * X + x;
       int D[3];
       int_diffs(v, X, Y, Z, x, y, z, i, D);
       const unsigned long long S =
@@ -538,14 +543,14 @@ __global__ void k_hist2d_pass1(const T* __restrict__ v, long long X, long long Y
 // f64 max |g| over the voxels with S == Smax (positive doubles order like
 // their bit patterns).
 template <typename T>
-__global__ void k_hist2d_pass1b(const T* __restrict__ v, long long X, long long Y, long long Z, double c,
-                                Hist2DScratch* sc) {
+__global__ void k_hist2d_pass1b(const T* __restrict__ v, long long X, long long Y, long long Z, long long zb,
+                                long long ze, long long zlo, double c, Hist2DScratch* sc) {
   const unsigned long long smax = sc->smax;
   if (smax == 0) return;
-  for (long long row = blockIdx.x; row < Y * Z; row += gridDim.x) {
-    const long long z = row / Y, y = row - z * Y;
+  for (long long row = blockIdx.x; row < Y * (ze - zb); row += gridDim.x) {
+    const long long zr = row / Y, y = row - zr * Y, z = zb + zr;
     for (long long x = threadIdx.x; x < X; x += blockDim.x) {
-      const long long i = row * X + x;
+      const long long i = ((z - zlo) * Y + y) * X + x;
       int D[3];
       int_diffs(v, X, Y, Z, x, y, z, i, D);
       const unsigned long long S =
@@ -559,8 +564,9 @@ __global__ void k_hist2d_pass1b(const T* __restrict__ v, long long X, long long 
 }
 
 template <typename T>
-__global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y, long long Z, double c, long long nx,
-                               long long merge, unsigned long long* __restrict__ hist, const Hist2DScratch* sc) {
+__global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y, long long Z, long long zb,
+                               long long ze, long long zlo, double c, long long nx, long long merge,
+                               unsigned long long* __restrict__ hist, const Hist2DScratch* sc) {
   const unsigned long long smax = sc->smax;
   const double gmax = __longlong_as_double((long long)sc->gmax_bits);
   const float smax_f = (float)smax;
@@ -568,10 +574,10 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
   // values are below 2^16, so any merge above 2^16 bins like 2^16
   const unsigned merge32 = (unsigned)(merge < 1 ? 1 : merge > 65536 ? 65536 : merge);
   unsigned long long run_bin = ~0ULL, run = 0;
-  for (long long row = blockIdx.x; row < Y * Z; row += gridDim.x) {
-    const long long z = row / Y, y = row - z * Y;
+  for (long long row = blockIdx.x; row < Y * (ze - zb); row += gridDim.x) {
+    const long long zr = row / Y, y = row - zr * Y, z = zb + zr;
     for (long long x = threadIdx.x; x < X; x += blockDim.x) {
-      const long long i = row * X + x;
+      const long long i = ((z - zlo) * Y + y) * X + x;
       int D[3];
       int_diffs(v, X, Y, Z, x, y, z, i, D);
       const unsigned long long S =
@@ -903,14 +909,39 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
   if (e != cudaSuccess) return e;
   if (dtype == DT_U8) {
     const uint8_t* v = (const uint8_t*)vol;
-    k_hist2d_pass1<<<blocks, threads, 0, s>>>(v, X, Y, Z, scratch);
-    k_hist2d_pass1b<<<blocks, threads, 0, s>>>(v, X, Y, Z, c, scratch);
-    k_hist2d_pass2<<<blocks, threads, 0, s>>>(v, X, Y, Z, c, nx, merge, hist, scratch);
+    k_hist2d_pass1<<<blocks, threads, 0, s>>>(v, X, Y, Z, 0, Z, 0, scratch);
+    k_hist2d_pass1b<<<blocks, threads, 0, s>>>(v, X, Y, Z, 0, Z, 0, c, scratch);
+    k_hist2d_pass2<<<blocks, threads, 0, s>>>(v, X, Y, Z, 0, Z, 0, c, nx, merge, hist, scratch);
   } else {
     const uint16_t* v = (const uint16_t*)vol;
-    k_hist2d_pass1<<<blocks, threads, 0, s>>>(v, X, Y, Z, scratch);
-    k_hist2d_pass1b<<<blocks, threads, 0, s>>>(v, X, Y, Z, c, scratch);
-    k_hist2d_pass2<<<blocks, threads, 0, s>>>(v, X, Y, Z, c, nx, merge, hist, scratch);
+    k_hist2d_pass1<<<blocks, threads, 0, s>>>(v, X, Y, Z, 0, Z, 0, scratch);
+    k_hist2d_pass1b<<<blocks, threads, 0, s>>>(v, X, Y, Z, 0, Z, 0, c, scratch);
+    k_hist2d_pass2<<<blocks, threads, 0, s>>>(v, X, Y, Z, 0, Z, 0, c, nx, merge, hist, scratch);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hist2d_slab(const void* slab, int dtype, const long long dims[3], long long zb, long long ze,
+                               long long zlo, double max_scalar, long long nx, long long merge, int pass,
+                               unsigned long long* hist, Hist2DScratch* scratch, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (dtype == DT_F32 || pass < 1 || pass > 3) return cudaErrorInvalidValue;
+  const long long X = dims[0], Y = dims[1], Z = dims[2];
+  if (zb < 0 || ze > Z || zb >= ze || zlo > zb || (zb > 0 && zlo > zb - 1)) return cudaErrorInvalidValue;
+  const double c = max_scalar > 0 ? max_scalar : 1.0;
+  const int threads = X >= 256 ? 256 : 128;
+  const long long rows = Y * (ze - zb);
+  const int blocks = (int)(rows < 152LL * 64 ? rows : 152LL * 64);
+  if (dtype == DT_U8) {
+    const uint8_t* v = (const uint8_t*)slab;
+    if (pass == 1) k_hist2d_pass1<<<blocks, threads, 0, s>>>(v, X, Y, Z, zb, ze, zlo, scratch);
+    else if (pass == 2) k_hist2d_pass1b<<<blocks, threads, 0, s>>>(v, X, Y, Z, zb, ze, zlo, c, scratch);
+    else k_hist2d_pass2<<<blocks, threads, 0, s>>>(v, X, Y, Z, zb, ze, zlo, c, nx, merge, hist, scratch);
+  } else {
+    const uint16_t* v = (const uint16_t*)slab;
+    if (pass == 1) k_hist2d_pass1<<<blocks, threads, 0, s>>>(v, X, Y, Z, zb, ze, zlo, scratch);
+    else if (pass == 2) k_hist2d_pass1b<<<blocks, threads, 0, s>>>(v, X, Y, Z, zb, ze, zlo, c, scratch);
+    else k_hist2d_pass2<<<blocks, threads, 0, s>>>(v, X, Y, Z, zb, ze, zlo, c, nx, merge, hist, scratch);
   }
   return cudaGetLastError();
 }

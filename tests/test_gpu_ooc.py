@@ -63,6 +63,11 @@ def test_ooc_build_matches_incore(case):
         assert ib["host_bytes"] > 0 and ib["device_slots"] == ib["total_bricks"]
         if sp.dtype != 2:
             assert np.array_equal(a.getHistogram(), b.getHistogram())
+            # the 2D histogram, streamed in z-slabs out of core, bit for bit
+            h2a, ga = a.get2DHistogram()
+            h2b, gb = b.get2DHistogram()
+            assert ga == gb > 0 and np.array_equal(h2a, h2b)
+            assert ia["hist2d_max_grad"] == ib["hist2d_max_grad"]
         for lod in range(ia["lod_count"]):
             assert np.array_equal(a.brickMinMax(lod), b.brickMinMax(lod))
             nb = ia["lod_bricks"][lod]

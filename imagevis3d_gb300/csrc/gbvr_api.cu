@@ -927,6 +927,14 @@ int set_error(int code, const std::string& msg) { return fail(code, msg); }
 // ---------------------------------------------------------------------------
 // Renderer
 // ---------------------------------------------------------------------------
+// A 2D slice paint (gbvr_paint_slice) out of core: the bricks it needs
+// instead of the views' frusta.  index: slice of the finest level.
+struct SliceSel {
+  int axis;
+  long long index;
+  bool mip;
+};
+
 struct gbvr_renderer {
   Dataset ds;
   uint32_t flags = 0;
@@ -935,6 +943,7 @@ struct gbvr_renderer {
   int clip_on = 0;
   float clip[4] = {0.f, 0.f, 1.f, 0.f};
   // bounding boxes: the dataset box and the brick boxes of the rendered level
+  const SliceSel* slice_sel = nullptr;  // during an out-of-core slice paint
   int bbox_global = 0, bbox_local = 0;
   float bbox_rgb[2][3] = {{1.f, 1.f, 1.f}, {0.6f, 0.6f, 0.6f}};
   DevBuf d_line_keys, d_line_segs, d_line_views, d_line_list, d_line_count;
@@ -1427,10 +1436,11 @@ struct PtrSnapshot {
 // overwrite anything.  The staging of `stage` must be free (its previous
 // uploads complete) when this is called.
 int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64_t protect, cudaEvent_t protect_done,
-             int stage, uint64_t* misses_out, uint64_t* bytes_out) {
+             int stage, uint64_t* misses_out, uint64_t* bytes_out, const SliceSel* slice = nullptr) {
   Dataset& ds = r->ds;
   ensure_tf(r);
-  const bool two = r->mode == GBVR_RM_2DTRANS;
+  // a slice is classified with the 1D TF, whatever the render mode
+  const bool two = r->mode == GBVR_RM_2DTRANS && !slice;
   if (two && r->tf2d.empty()) return fail(GBVR_ESTATE, "2D transfer function not set");
   const std::vector<float>& tf = two ? r->tf2d : r->tf1d;
   const int w = two ? r->tf2d_w : (int)(r->tf1d.size() / 4), h = two ? r->tf2d_h : 1;
@@ -1444,8 +1454,9 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
   default_range(r, vlo, vhi);
   const float idx_scale = (float)((w - 1) / (vhi - vlo)), lo_f = (float)vlo;
   auto nonempty = [&](const BrickInfo& b) {
-    if (r->mode == GBVR_RM_ISOSURFACE) return b.vmax >= skip_iso(r);
-    if (r->mode == GBVR_RM_MIP) return true;
+    if (slice && slice->mip) return true;  // the column maximum needs every brick
+    if (!slice && r->mode == GBVR_RM_ISOSURFACE) return b.vmax >= skip_iso(r);
+    if (!slice && r->mode == GBVR_RM_MIP) return true;
     float ilo = std::min(std::max((b.vmin - lo_f) * idx_scale, 0.f), (float)(w - 1));
     float ihi = std::min(std::max((b.vmax - lo_f) * idx_scale, 0.f), (float)(w - 1));
     int a0 = std::max((int)std::floor(ilo) - 1, 0), a1 = std::min((int)std::floor(ihi) + 2, w - 1);
@@ -1467,6 +1478,15 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
   // far plane does not cull.
   auto visible = [&](const Level& L, const BrickInfo& b) {
     const int lo[3] = {b.lox, b.loy, b.loz}, hi[3] = {b.hix, b.hiy, b.hiz};
+    if (slice) {
+      if (slice->mip) return true;
+      // the brick holding the slice's cell (one cell either side for
+      // rounding): the sampler reads the footprint from that brick
+      const int a = slice->axis;
+      const double wpos = ((double)slice->index + 0.5) / (double)ds.dims[a];
+      const long long cell = (long long)std::floor(wpos * (double)L.dims[a] - 0.5);
+      return lo[a] <= cell + 1 && cell - 1 < hi[a];
+    }
     double c[8][4];
     for (int k = 0; k < 8; ++k)
       for (int a = 0; a < 3; ++a) {
@@ -1621,7 +1641,8 @@ int prepare(gbvr_renderer* r, int nviews, int& level, const gbvr_view* views) {
       views = vs.data();
     }
     // every earlier paint has finished (paints are synchronous): no slot is in use
-    TRY(ooc_page(r, views, views == vs.data() ? 1 : nviews, level, 0, nullptr, 0, &r->last_misses, &r->last_paged));
+    TRY(ooc_page(r, views, views == vs.data() ? 1 : nviews, level, 0, nullptr, 0, &r->last_misses, &r->last_paged,
+                 r->slice_sel));
     CUDA_TRY(cudaEventSynchronize(r->ev_c1[0]));
     CUDA_TRY(cudaEventElapsedTime(&r->last_page_ms, r->ev_c0[0], r->ev_c1[0]));
     r->drop_graphs();  // the page table changes between paints
@@ -1716,9 +1737,16 @@ int paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_
   const Dataset& ds = r->ds;
   if (axis < 0 || axis > 2) return fail(GBVR_EINVAL, "slice axis must be 0, 1 or 2");
   if (index < 0 || index >= ds.dims[axis]) return fail(GBVR_EINVAL, "slice index outside the volume");
-  if (ds.ooc) return fail(GBVR_ESTATE, "2D slices of out-of-core datasets are not supported");
   int level;
-  TRY(prepare(r, 1, level, nullptr));
+  {
+    // out of core, the slice's bricks are paged in (every brick for MIP;
+    // a coarser level when they do not fit the device slots)
+    const SliceSel sel{axis, (long long)index, use_mip != 0};
+    r->slice_sel = &sel;
+    const int rc = prepare(r, 1, level, nullptr);
+    r->slice_sel = nullptr;
+    TRY(rc);
+  }
   ensure_tf(r);
   CUDA_TRY(r->d_tf_slice.alloc(sizeof(float) * r->tf1d.size()));
   CUDA_TRY(cudaMemcpyAsync(r->d_tf_slice.p, r->tf1d.data(), sizeof(float) * r->tf1d.size(), cudaMemcpyHostToDevice,
@@ -1753,6 +1781,7 @@ int paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_
   sd.flip_x = flip_x ? 1 : 0;
   sd.flip_y = flip_y ? 1 : 0;
   sd.mip = use_mip ? 1 : 0;
+  sd.use_skip = ds.ooc ? 1 : 0;
   CUDA_TRY(cudaMemsetAsync(r->d_samples.p, 0, sizeof(unsigned long long), r->stream));
   CUDA_TRY(cudaEventRecord(r->ev0, r->stream));
   CUDA_TRY(cudaEventRecord(r->evk0, r->stream));

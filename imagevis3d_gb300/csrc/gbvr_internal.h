@@ -158,6 +158,7 @@ struct SliceDesc {
   float ext_u, ext_v;  // world extents of the in-plane axes (u = lower-numbered, v = higher)
   float scale_u, scale_v;  // level voxels per world unit along u, v
   int flip_x, flip_y, mip;
+  int use_skip;        // out of core: a brick flagged in f.skip (empty under the TF, or not resident) is background
 };
 
 // Default ray tile handled by one warp: 8 x 4 pixels.

@@ -1009,10 +1009,16 @@ __global__ void k_render_slice(const __grid_constant__ FrameDesc f, const __grid
         z = s.axis == 2 ? pa : pv;
       };
       float v, x, y, z;
+      bool empty = false;
       if (!s.mip) {
         pos(s.coord, x, y, z);
-        v = sample_anywhere<T, SAMPLER_SW>(f, x, y, z);
-        ns = 1;
+        if (s.use_skip) {
+          // the in-core pixel of a brick empty under the TF is the background
+          const Cell c = make_cell(f, x, y, z);
+          empty = __ldg(f.skip + brick_index(f, c.x, c.y, c.z)) != 0;
+        }
+        v = empty ? 0.f : sample_anywhere<T, SAMPLER_SW>(f, x, y, z);
+        ns = empty ? 0 : 1;
       } else {
         v = -INFINITY;
         const int n = f.dims[s.axis];
@@ -1024,7 +1030,7 @@ __global__ void k_render_slice(const __grid_constant__ FrameDesc f, const __grid
           BrickView b;
           load_brick(f, bi, b);
           const int hi = s.axis == 0 ? b.hix : (s.axis == 1 ? b.hiy : b.hiz);
-          if (__ldg(&f.bricks[bi].vmax) > v) {
+          if (__ldg(&f.bricks[bi].vmax) > v && !(s.use_skip && __ldg(f.skip + bi))) {
             for (; k < hi; ++k) {
               const int cx = s.axis == 0 ? k : c.x, cy = s.axis == 1 ? k : c.y, cz = s.axis == 2 ? k : c.z;
               v = fmaxf(v, sample_cell<T, SAMPLER_SW>(f, b, cx, cy, cz, s.axis == 0 ? 0.f : c.fx,
@@ -1037,9 +1043,11 @@ __global__ void k_render_slice(const __grid_constant__ FrameDesc f, const __grid
           if (v >= f.level_max) break;
         }
       }
-      const float4 c = tf1d(f, v);
-      out = make_float4(fmaf(c.w, c.x, (1.f - c.w) * f.bg[0]), fmaf(c.w, c.y, (1.f - c.w) * f.bg[1]),
-                        fmaf(c.w, c.z, (1.f - c.w) * f.bg[2]), c.w);
+      if (!empty) {
+        const float4 c = tf1d(f, v);
+        out = make_float4(fmaf(c.w, c.x, (1.f - c.w) * f.bg[0]), fmaf(c.w, c.y, (1.f - c.w) * f.bg[1]),
+                          fmaf(c.w, c.z, (1.f - c.w) * f.bg[2]), c.w);
+      }
     }
     const size_t o = (size_t)py * f.width + px;
     if (f.out_f32) f.out_f32[o] = out;

@@ -200,7 +200,8 @@ int gbvr_paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lo
  * at its aspect ratio, centred, background around it; screen x follows the lower-numbered in-plane axis,
  * screen y the higher one upwards; flip_x / flip_y mirror them.  Each pixel: the trilinear value at the
  * slice through the 1D TF over the background.  use_mip: the maximum along the axis instead (maximum-
- * intensity projection of the whole volume).  Not for out-of-core datasets. */
+ * intensity projection of the whole volume).  Out of core, the bricks the slice needs are paged in first
+ * (every brick for use_mip), on a coarser level when they do not fit the device slots. */
 int gbvr_paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_y, int use_mip);
 /* setClipPlane / setClipPlaneEnabled (RenderWindow.cpp:1920-1927, RenderWindow.h:131,168): samples at world
  * points p (the normalised volume box) with plane[0..2] . p + plane[3] > 0 are dropped; enabled = 0 turns the

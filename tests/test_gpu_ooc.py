@@ -262,3 +262,37 @@ def test_ooc_paint_path_with_bboxes_matches_incore():
             a.setLODLimits(int(lod[i]), int(lod[i]))
             assert np.array_equal(frames[i], _paint(a, view, proj)), i
         assert any((f[..., 3] == 1.0).sum() > 50 for f in frames)
+
+
+@pytest.mark.parametrize("mip", [False, True])
+def test_ooc_slices_equal_incore(mip):
+    """2D slices of an out-of-core dataset page in the slice's bricks (every
+    brick for slice MIP, on a coarser level when they do not fit) and equal
+    the in-core slice at that level bit for bit."""
+    sp, bp = CASES["u8_131x97x203_b32"]
+    slot = 32 ** 3
+    with Renderer(float_fb=True) as a, Renderer(float_fb=True) as b:
+        a.loadSynthetic(sp, **bp)
+        b.loadSyntheticOutOfCore(sp, 48 * slot, **bp)
+        for r in (a, b):
+            _setup(r, sp, 160, 120)
+        lods, visible = set(), 0
+        # a sparse TF (empty bricks are skipped) and a dense one
+        ramp = np.linspace(0.0, 1.0, 256, dtype=np.float32)
+        dense = np.stack([ramp, ramp[::-1], np.full(256, 0.5, np.float32), np.full(256, 0.6, np.float32)], -1)
+        dense[0, 3] = 0.0
+        for tf in (workloads.tf1d_seeded(256, 5, 40.0, 255.0), dense):
+            for r in (a, b):
+                r.set1DTrans(tf)
+            for axis, idx, fx in ((0, 5, False), (1, 48, True), (2, 150, False), (2, 0, False), (0, 130, True)):
+                b.paintSlice(axis, idx, flip_x=fx, use_mip=mip)
+                got = b.readFramebuffer(0, as_float=True)
+                lod = b.stats()["lod"]
+                lods.add(lod)
+                a.setLODLimits(lod, lod)
+                a.paintSlice(axis, idx, flip_x=fx, use_mip=mip)
+                assert np.array_equal(got, a.readFramebuffer(0, as_float=True)), (axis, idx)
+                visible += int((got[..., 3] > 0).sum())
+        assert visible > 20000
+        # slice MIP needs all 160 bricks of level 0: it falls back; a slice fits
+        assert lods == ({1} if mip else {0})

@@ -1905,14 +1905,16 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
   }
   FrameDesc* hf = (FrameDesc*)r->h_frames.p;
   int* hp = (int*)r->h_prefix.p;
-  int total = 0;
+  long long total = 0;
   for (int v = 0; v < n; ++v) {
     hf[v] = make_frame(r, views[v].view, views[v].proj, level, v);
     cull_tiles(hf[v], r, views[v].view, views[v].proj);
-    hp[v] = total;
-    total += hf[v].ntx * hf[v].nty;
+    hp[v] = (int)total;
+    total += (long long)hf[v].ntx * hf[v].nty;
+    // work items are 32-bit (the atomic counter runs up to total + grid)
+    if (total > (long long)INT32_MAX - (1 << 24)) return fail(GBVR_EINVAL, "batch too large: split it");
   }
-  hp[n] = total;
+  hp[n] = (int)total;
   if (PtrSnapshot(r) != before) r->drop_graphs();
   if (!r->sm_count) {
     int dev = 0;

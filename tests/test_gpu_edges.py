@@ -1,8 +1,8 @@
 """Edge cases of the raycaster against the FP64 oracle: non-unit voxel aspect,
 ragged and tiny framebuffers, a one-voxel-thick slab, sampling rates below
 and above one sample per voxel, early-termination thresholds, a coloured
-background, orthographic projection, and a batch of many views against the
-per-view launches."""
+background, orthographic projection, batches of 100 and 4096 views against
+the per-view launches, and an 8192 x 8192 framebuffer."""
 import numpy as np
 import pytest
 
@@ -148,3 +148,42 @@ def test_batches_of_new_views_replay_the_cached_graph(blobs):
             batch = r.readFramebuffers(0, 4).copy()
             r.paintViews(views)
             assert np.array_equal(batch, r.readFramebuffers(0, 4))
+
+
+def test_many_small_views_in_one_batch(blobs):
+    """4096 views in one persistent launch equal the per-view launches."""
+    sp, _ = blobs
+    views = workloads.orbit_views(4096, 32, 24, elevation=25.0)
+    with Renderer() as r:
+        r.loadSynthetic(sp, brick_size=32, overlap=2)
+        r.resize((32, 24))
+        r.set1DTrans(TF)
+        r.setValueRange(0.0, 255.0)
+        r.paintBatch(views)
+        batch = r.readFramebuffers(0, 4096)
+        r.paintViews(views)
+        assert np.array_equal(batch, r.readFramebuffers(0, 4096))
+        assert (batch[..., 3] > 0).any(axis=(1, 2)).all()
+
+
+def test_large_framebuffer(orc, blobs):
+    """One 8192 x 8192 view: the persistent and the per-view kernel agree bit
+    for bit, and seeded pixels match the oracle."""
+    sp, vol = blobs
+    w = h = 8192
+    view, proj = orbit_camera(70.0, 20.0, 1.8 * workloads.DIAG, 45.0, w, h)
+    with Renderer(float_fb=True) as r:
+        r.loadSynthetic(sp, brick_size=32, overlap=2)
+        r.resize((w, h))
+        r.set1DTrans(TF)
+        r.setValueRange(0.0, 255.0)
+        r.paintBatch([(view, proj)])
+        batch = r.readFramebuffer(0, as_float=True)
+        r.setView(view, proj)
+        r.paint()
+        img = r.readFramebuffer(0, as_float=True)
+    assert np.array_equal(batch, img)
+    pix = np.random.default_rng(3).choice(w * h, 20000, replace=False)
+    ref, _ = orc.render(vol, view, proj, w, h, TF, value_range=(0.0, 255.0), pixels=pix)
+    assert_close(img.reshape(-1, 4)[pix], ref)
+    assert (ref[:, 3] > 0).sum() > 1000

@@ -947,6 +947,7 @@ struct gbvr_renderer {
   int bbox_global = 0, bbox_local = 0;
   float bbox_rgb[2][3] = {{1.f, 1.f, 1.f}, {0.6f, 0.6f, 0.6f}};
   DevBuf d_line_keys, d_line_segs, d_line_views, d_line_list, d_line_count;
+  DevBuf d_tf_col;  // 2D TF: per value column, 1 if any gradient row has opacity
   // ClearView (isosurface mode): focus iso value and colour, lens size
   // (radius = size * min(width, height) / 2 pixels), context and border
   // scales, focus point in pixels (row 0 = top)
@@ -1134,6 +1135,15 @@ int upload_tf(gbvr_renderer* r, int level) {
   if (r->tf_dirty) {
     CUDA_TRY(r->d_tf.alloc(sizeof(float) * tf.size()));
     CUDA_TRY(cudaMemcpyAsync(r->d_tf.p, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice, r->stream));
+    if (two) {
+      const int w = r->tf2d_w, h = r->tf2d_h;
+      std::vector<unsigned char> live((size_t)w, 0);
+      for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) live[x] |= tf[4 * ((size_t)y * w + x) + 3] != 0.f;
+      CUDA_TRY(r->d_tf_col.alloc(live.size()));
+      // pageable source: the copy returns once it is staged
+      CUDA_TRY(cudaMemcpyAsync(r->d_tf_col.p, live.data(), live.size(), cudaMemcpyHostToDevice, r->stream));
+    }
     r->tf_dirty = false;
     r->skip_dirty = true;
   }
@@ -1227,6 +1237,7 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
                        ? r->d_cellbits.as<unsigned>() + (size_t)vidx * r->cell_words : nullptr;
   if (r->bbox_global || r->bbox_local) f.lines = r->d_line_keys.as<unsigned>() + (size_t)vidx * npix;
   memcpy(f.line_rgb, r->bbox_rgb, sizeof(f.line_rgb));
+  f.tf_col_live = r->mode == GBVR_RM_2DTRANS ? r->d_tf_col.as<unsigned char>() : nullptr;
   f.cv_iso = r->cv_iso;
   memcpy(f.cv_rgb, r->cv_rgb, sizeof(f.cv_rgb));
   f.cv_context = r->cv_context;

@@ -67,6 +67,7 @@ struct __align__(16) FrameDesc {
   float value_lo;
   float idx_scale;           // (tf_w - 1) / (value_hi - value_lo)
   float grad_scale;          // 2D: (tf_h - 1) / (grad_max * (value_hi - value_lo))
+  const unsigned char* tf_col_live;  // 2D: per value column, 1 if any gradient row has opacity (or null)
   float dt;                  // step, world units
   float opacity_exp;         // dt / dt0 = 1 / samples_per_voxel
   float ert;

@@ -615,7 +615,14 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
           }
           continue;
         }
-        // 2D transfer function over (value, |gradient|), Phong lit
+        // 2D transfer function over (value, |gradient|), Phong lit.  A value
+        // between two columns without opacity in any gradient row composites
+        // nothing (alpha 0 whatever the gradient): its gradient is skipped.
+        if (f.tf_col_live) {
+          const float ix = fminf(fmaxf((v - f.value_lo) * f.idx_scale, 0.f), (float)(f.tf_w - 1));
+          const int x0 = (int)ix;
+          if (!(__ldg(f.tf_col_live + x0) | __ldg(f.tf_col_live + min(x0 + 1, f.tf_w - 1)))) continue;
+        }
         float g[3];
         gradient<T, SAMPLER>(f, b, c, g);
         const float gm = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);

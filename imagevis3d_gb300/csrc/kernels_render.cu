@@ -214,6 +214,85 @@ __device__ __forceinline__ void gradient(const FrameDesc& f, const BrickView& b,
           sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z - 1, c.fx, c.fy, c.fz)) * 0.5f;
 }
 
+// Trilinear interpolation of 8 voxels in sample_cell's order of operations.
+__device__ __forceinline__ float trilin(float v000, float v100, float v010, float v110, float v001, float v101,
+                                        float v011, float v111, float fx, float fy, float fz) {
+  const float c00 = fmaf(fx, v100 - v000, v000);
+  const float c10 = fmaf(fx, v110 - v010, v010);
+  const float c01 = fmaf(fx, v101 - v001, v001);
+  const float c11 = fmaf(fx, v111 - v011, v011);
+  const float c0 = fmaf(fy, c10 - c00, c00);
+  const float c1 = fmaf(fy, c11 - c01, c01);
+  return fmaf(fz, c1 - c0, c0);
+}
+
+// A cell's value and central-difference gradient together (software
+// trilinear sampler): the six gradient taps, the same fractions one cell
+// over, share half their voxels with the cell's own sample, so 32 voxels are
+// loaded instead of 56.  Voxel addresses are the sum of per-axis offsets of
+// the coordinates -1 .. +2 around the cell; values and arithmetic are those
+// of sample_cell and gradient, bit for bit.
+struct Taps {
+  long long base;
+  int X[4], Y[4], Z[4];
+};
+
+__device__ __forceinline__ void make_taps(const FrameDesc& f, const BrickView& b, const Cell& c, Taps& t) {
+  const int lx = c.x - b.ox - 1, ly = c.y - b.oy - 1, lz = c.z - b.oz - 1;
+  if (f.perm == 3) {
+    t.base = b.base;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int x = lx + i, y = ly + i, z = lz + i;
+      t.X[i] = ((x >> 2) << 6) + (x & 3);
+      t.Y[i] = (y >> 2) * b.s1 + ((y & 3) << 2);
+      t.Z[i] = (z >> 2) * b.s2 + ((z & 3) << 4);
+    }
+  } else {
+    t.base = b.base + (long long)b.ox * b.s0 + (long long)b.oy * b.s1 + (long long)b.oz * b.s2;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      t.X[i] = (lx + i) * b.s0;
+      t.Y[i] = (ly + i) * b.s1;
+      t.Z[i] = (lz + i) * b.s2;
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ float tap(const FrameDesc& f, const Taps& t, int i, int j, int k) {
+  return ldv(reinterpret_cast<const T*>(f.pool) + (t.base + (long long)(t.Z[k] + t.Y[j] + t.X[i])));
+}
+
+// m: the cell's 8 voxels in sample_cell's order (v000, v100, v010, v110, v001, v101, v011, v111)
+template <typename T>
+__device__ __forceinline__ float sample_taps(const FrameDesc& f, const Taps& t, const Cell& c, float m[8]) {
+  m[0] = tap<T>(f, t, 1, 1, 1); m[1] = tap<T>(f, t, 2, 1, 1); m[2] = tap<T>(f, t, 1, 2, 1); m[3] = tap<T>(f, t, 2, 2, 1);
+  m[4] = tap<T>(f, t, 1, 1, 2); m[5] = tap<T>(f, t, 2, 1, 2); m[6] = tap<T>(f, t, 1, 2, 2); m[7] = tap<T>(f, t, 2, 2, 2);
+  return trilin(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], c.fx, c.fy, c.fz);
+}
+
+template <typename T>
+__device__ __forceinline__ void gradient_taps(const FrameDesc& f, const Taps& t, const Cell& c, const float m[8],
+                                              float g[3]) {
+  const float fx = c.fx, fy = c.fy, fz = c.fz;
+  const float xp = trilin(m[1], tap<T>(f, t, 3, 1, 1), m[3], tap<T>(f, t, 3, 2, 1), m[5], tap<T>(f, t, 3, 1, 2), m[7],
+                          tap<T>(f, t, 3, 2, 2), fx, fy, fz);
+  const float xm = trilin(tap<T>(f, t, 0, 1, 1), m[0], tap<T>(f, t, 0, 2, 1), m[2], tap<T>(f, t, 0, 1, 2), m[4],
+                          tap<T>(f, t, 0, 2, 2), m[6], fx, fy, fz);
+  g[0] = (xp - xm) * 0.5f;
+  const float yp = trilin(m[2], m[3], tap<T>(f, t, 1, 3, 1), tap<T>(f, t, 2, 3, 1), m[6], m[7], tap<T>(f, t, 1, 3, 2),
+                          tap<T>(f, t, 2, 3, 2), fx, fy, fz);
+  const float ym = trilin(tap<T>(f, t, 1, 0, 1), tap<T>(f, t, 2, 0, 1), m[0], m[1], tap<T>(f, t, 1, 0, 2),
+                          tap<T>(f, t, 2, 0, 2), m[4], m[5], fx, fy, fz);
+  g[1] = (yp - ym) * 0.5f;
+  const float zp = trilin(m[4], m[5], m[6], m[7], tap<T>(f, t, 1, 1, 3), tap<T>(f, t, 2, 1, 3), tap<T>(f, t, 1, 2, 3),
+                          tap<T>(f, t, 2, 2, 3), fx, fy, fz);
+  const float zm = trilin(tap<T>(f, t, 1, 1, 0), tap<T>(f, t, 2, 1, 0), tap<T>(f, t, 1, 2, 0), tap<T>(f, t, 2, 2, 0),
+                          m[0], m[1], m[2], m[3], fx, fy, fz);
+  g[2] = (zp - zm) * 0.5f;
+}
+
 // Phong, directional light, two-sided: normal = -grad/|grad| turned towards
 // the viewer.  g is a world-space gradient, V the unit vector to the viewer,
 // L the unit vector towards the light in world space (it follows the view:
@@ -552,7 +631,17 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
       for (; k < ke; ++k) {
         pos_of(k, px, py, pz);
         const Cell c = make_cell(f, px, py, pz);
-        const float v = sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z, c.fx, c.fy, c.fz);
+        // 2D TF, software trilinear: the value and later its gradient from shared taps
+        constexpr bool kTaps = MODE == MODE_2D && SAMPLER == SAMPLER_SW;
+        Taps tp;
+        float m[8];
+        float v;
+        if (kTaps && f.interp) {
+          make_taps(f, b, c, tp);
+          v = sample_taps<T>(f, tp, c, m);
+        } else {
+          v = sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z, c.fx, c.fy, c.fz);
+        }
         ++nsamp;
         if (MODE == MODE_ISO) {
           const float thr = (CV && cv_phase) ? f.cv_iso : f.iso;
@@ -624,7 +713,8 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
           if (!(__ldg(f.tf_col_live + x0) | __ldg(f.tf_col_live + min(x0 + 1, f.tf_w - 1)))) continue;
         }
         float g[3];
-        gradient<T, SAMPLER>(f, b, c, g);
+        if (kTaps && f.interp) gradient_taps<T>(f, tp, c, m, g);
+        else gradient<T, SAMPLER>(f, b, c, g);
         const float gm = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
         float4 cl = tf2d(f, v, gm);
         if (f.lighting && cl.w > 0.f) {
@@ -728,11 +818,12 @@ __device__ __forceinline__ void render_tile_u(const FrameDesc& f, const FrameDes
 }
 
 constexpr int RENDER_THREADS = 128;
-// Resident CTAs per SM the uniform persistent kernel is compiled for: for the
-// 1D TF and MIP walks 10 CTAs of 128 threads (48 registers; measured ahead of
-// 6, 8 and 12), for the shaded modes 8 (64 registers, fewer spills).
+// Resident CTAs per SM each mode's kernels are compiled for (registers =
+// 65536 / (128 x this)): the 1D TF and MIP walks 10 (48 registers; measured
+// ahead of 6, 8 and 12); the 2D TF path 6 (80 registers: it keeps a sample's
+// 8 voxels and 12 tap offsets for its gradient); the isosurface path 8 (64).
 template <int MODE>
-constexpr int uniform_ctas_per_sm() { return (MODE == MODE_1D || MODE == MODE_MIP) ? 10 : 8; }
+constexpr int uniform_ctas_per_sm() { return (MODE == MODE_1D || MODE == MODE_MIP) ? 10 : (MODE == MODE_2D ? 6 : 8); }
 
 template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
@@ -1376,11 +1467,15 @@ cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, c
 int persistent_grid_size_uniform(int device, int mode) {
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  // each mode's own kernel: their launch bounds differ
   if (mode == MODE_1D || mode == MODE_MIP)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_1D, SAMPLER_SW>,
                                                   RENDER_THREADS, 0);
-  else
+  else if (mode == MODE_2D)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_2D, SAMPLER_SW>,
+                                                  RENDER_THREADS, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_ISO, SAMPLER_SW>,
                                                   RENDER_THREADS, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
@@ -1389,11 +1484,15 @@ int persistent_grid_size_uniform(int device, int mode) {
 int persistent_grid_size(int device, int mode) {
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  // each mode's own kernel: their launch bounds differ
   if (mode == MODE_1D || mode == MODE_MIP)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent<uint16_t, MODE_1D, SAMPLER_SW>,
                                                   RENDER_THREADS, 0);
-  else
+  else if (mode == MODE_2D)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent<uint16_t, MODE_2D, SAMPLER_SW>,
+                                                  RENDER_THREADS, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent<uint16_t, MODE_ISO, SAMPLER_SW>,
                                                   RENDER_THREADS, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;

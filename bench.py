@@ -604,7 +604,8 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    from imagevis3d_gb300 import GBVR_SAMPLER_SW, GBVR_SAMPLER_TEX, Renderer, synth_volume, workloads
+    from imagevis3d_gb300 import (GBVR_RM_1DTRANS, GBVR_RM_MIP, GBVR_SAMPLER_SW, GBVR_SAMPLER_TEX, Renderer,
+                                  synth_volume, workloads)
     from imagevis3d_gb300.replicas import shard
 
     wl = workloads.config2(size=args.size, nviews=args.views)
@@ -695,6 +696,25 @@ def main():
         tex_fps = len(views) * args.steps / (sum(tms) / 1000.0)
         r.setSampler(GBVR_SAMPLER_SW)
         r.setLaunchShape(tune["tile_w"], tune["ctas_per_sm"])
+
+    # ---- the same batch in MIP mode, and with both bounding boxes drawn ----
+    def batch_fps():
+        for _ in range(2):
+            r.paintBatch(views)
+        ms_ = []
+        for _ in range(args.steps):
+            r.paintBatch(views)
+            ms_.append(r.stats()["gpu_ms"])
+        return len(views) * args.steps / (sum(ms_) / 1000.0)
+
+    r.setRenderMode(GBVR_RM_MIP)
+    mip_fps = batch_fps()
+    r.setRenderMode(GBVR_RM_1DTRANS)
+    r.setGlobalBBox(True)
+    r.setLocalBBox(True)
+    bbox_fps = batch_fps()
+    r.setGlobalBBox(False)
+    r.setLocalBBox(False)
 
     # ---- end to end through the public API with host buffers ----
     # (the caller's destination is page-locked host memory, one copy per step)
@@ -796,6 +816,8 @@ def main():
             "per_view_paint_fps": paint_fps,
             "batched_vs_per_view": value / plain_fps,
             "texture_trilinear_fps": tex_fps,
+            "mip_fps": mip_fps,
+            "with_bboxes_fps": bbox_fps,
             "autotune": {"sw": tune, "tex": tune_tex},
             "e2e_per_view_fps": e2e_plain,
             "image_error_vs_fp64": err,

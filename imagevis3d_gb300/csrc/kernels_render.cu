@@ -984,6 +984,10 @@ __device__ __forceinline__ double dd(double a, double b) { return __ddiv_rn(a, b
 struct SegScreen {
   double sx0, sy0, z0, dx, dy, dz, inv_l2;
   int ok;
+  // FP32 copies for rejecting far candidates: used when every coordinate is
+  // below 65536 pixels, where the FP32 squared distance errs by under 0.02
+  int fast;
+  float fx0, fy0, fdx, fdy, finv;
 };
 
 __device__ void project_segment(const LineSeg& s, const LineView& v, SegScreen& o) {
@@ -1025,9 +1029,23 @@ __device__ void project_segment(const LineSeg& s, const LineView& v, SegScreen& 
   o.inv_l2 = l2 > 0.0 ? dd(1.0, l2) : 0.0;
   // projections beyond 1e8 pixels (a segment grazing the eye plane) are not drawn
   if (!(fabs(sx0) < 1e8 && fabs(sy0) < 1e8 && fabs(sx1) < 1e8 && fabs(sy1) < 1e8)) o.ok = 0;
+  o.fast = fabs(sx0) < 65536.0 && fabs(sy0) < 65536.0 && fabs(sx1) < 65536.0 && fabs(sy1) < 65536.0;
+  o.fx0 = (float)sx0;
+  o.fy0 = (float)sy0;
+  o.fdx = (float)o.dx;
+  o.fdy = (float)o.dy;
+  o.finv = (float)o.inv_l2;
 }
 
 __device__ __forceinline__ void cover_pixel(const SegScreen& g, int color, const LineView& v, int px, int py) {
+  if (g.fast) {
+    // far from the segment in FP32 (squared distance > 0.3): not covered
+    const float cxf = (float)px + 0.5f, cyf = (float)py + 0.5f;
+    float sf = ((cxf - g.fx0) * g.fdx + (cyf - g.fy0) * g.fdy) * g.finv;
+    sf = fminf(fmaxf(sf, 0.f), 1.f);
+    const float exf = cxf - (g.fx0 + sf * g.fdx), eyf = cyf - (g.fy0 + sf * g.fdy);
+    if (exf * exf + eyf * eyf > 0.3f) return;
+  }
   const double cx = (double)px + 0.5, cy = (double)py + 0.5;
   double s = dm(da(dm(ds(cx, g.sx0), g.dx), dm(ds(cy, g.sy0), g.dy)), g.inv_l2);
   s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);

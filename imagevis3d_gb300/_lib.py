@@ -25,7 +25,7 @@ ERRORS = {
 
 class BrickParams(C.Structure):
     _fields_ = [("brick_size", C.c_int32), ("overlap", C.c_int32), ("max_lods", C.c_int32),
-                ("build_texture", C.c_int32), ("layouts", C.c_int32), ("reserved", C.c_int32),
+                ("build_texture", C.c_int32), ("layouts", C.c_int32), ("compression", C.c_int32),
                 ("aspect", C.c_double * 3)]
 
 
@@ -36,7 +36,7 @@ class DatasetInfo(C.Structure):
                 ("lod_bricks", (C.c_int32 * 3) * 16), ("total_bricks", C.c_int64),
                 ("device_bytes", C.c_uint64), ("hist1d_size", C.c_int32),
                 ("hist2d_max_grad", C.c_float), ("host_bytes", C.c_uint64), ("device_slots", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("compression", C.c_int32), ("host_raw_bytes", C.c_uint64)]
 
 
 class View(C.Structure):
@@ -49,7 +49,7 @@ class Stats(C.Structure):
                 ("brick_misses", C.c_uint64), ("bytes_paged", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("lod", C.c_int32), ("subframes", C.c_int32), ("gpu_ms", C.c_double),
                 ("kernel_ms", C.c_double), ("cells_touched", C.c_uint64), ("cell_bytes", C.c_uint64),
-                ("page_ms", C.c_double)]
+                ("page_ms", C.c_double), ("bytes_paged_compressed", C.c_uint64)]
 
 
 class TuneResult(C.Structure):
@@ -137,6 +137,9 @@ SIGNATURES = {
     "gbvr_set_render_mode": [P, I],
     "gbvr_set_clip_plane": [P, I, FP],
     "gbvr_set_bboxes": [P, I, I, FP, FP],
+    "gbvr_lz4_bound": [SZ],
+    "gbvr_lz4_compress": [P, SZ, P, SZ],
+    "gbvr_lz4_decompress": [P, SZ, P, SZ],
     "gbvr_set_clearview": [P, I, F, FP, F, F, F, F, F],
     "gbvr_paint_slice": [P, I, C.c_int64, I, I, I],
     "gbvr_paint_path": [P, C.POINTER(View), I, C.POINTER(C.c_int32), U64P, U64P],
@@ -214,6 +217,10 @@ class GbvrError(RuntimeError):
 _lib = None
 
 
+# functions that return something other than a status
+RESTYPES = {"gbvr_lz4_bound": SZ, "gbvr_lz4_compress": SZ}
+
+
 def lib():
     """Load libgbvr.so once and attach the signatures; raise if it is absent."""
     global _lib
@@ -225,7 +232,7 @@ def lib():
     for name, args in SIGNATURES.items():
         fn = getattr(L, name)
         fn.argtypes = args
-        fn.restype = C.c_int
+        fn.restype = RESTYPES.get(name, C.c_int)
     _lib = L
     return L
 

@@ -20,7 +20,10 @@
 
 #include "../../include/gbvr.h"
 #include "gbvr_internal.h"
+#include "lz4.h"
 #include "uvf.h"
+
+#include <thread>
 
 namespace gbvr {
 bool write_image(const std::string& path, const unsigned char* rgba, int w, int h, bool alpha);
@@ -240,6 +243,16 @@ struct Dataset {
   bool ooc = false;
   PinnedBuf host_store;
   std::vector<unsigned long long> host_off;
+  // Compressed store (brick_params.compression = 3, LZ4): brick b's chunks
+  // (LZ_CHUNK raw bytes each, the last one shorter) lie back to back from
+  // byte host_coff[b]; chunk_size[chunk_first[b] + k] is chunk k's compressed
+  // size (bit 31: stored uncompressed).  Paged bricks are decoded on the
+  // device from d_stage into their slots.
+  int compression = 0;
+  std::vector<unsigned long long> host_coff;
+  std::vector<unsigned> chunk_first, chunk_size;
+  uint64_t raw_store_bytes = 0;
+  DevBuf d_stage, d_chunks, d_lz_err;
   size_t slot_elems = 0;
   int nslots = 0;
   std::vector<int> slot_of;                  // per brick, -1 = not resident
@@ -259,6 +272,14 @@ struct Dataset {
     host_store.n = 0;
     ooc = false;
     host_off.clear();
+    compression = 0;
+    host_coff.clear();
+    chunk_first.clear();
+    chunk_size.clear();
+    raw_store_bytes = 0;
+    d_stage.release();
+    d_chunks.release();
+    d_lz_err.release();
     slot_of.clear();
     slot_brick.clear();
     slot_used.clear();
@@ -490,6 +511,8 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
 // memory is O(plane area x brick size), independent of the volume depth.
 // ---------------------------------------------------------------------------
 constexpr int OOC_CELL_SHIFT = 3;
+// raw bytes per compressed chunk of a brick (one LZ4 block; offsets reach 64 KiB back)
+constexpr size_t LZ_CHUNK = 65536;
 
 int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_params* bp, uint64_t pool_bytes,
                     cudaStream_t s) {
@@ -538,11 +561,22 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
   ds.slot_brick.assign(ds.nslots, -1);
   ds.slot_used.assign(ds.nslots, 0);
   for (auto& b : ds.bricks) b.offset = 0;
-  {
+  ds.compression = bp ? bp->compression : 0;
+  if (ds.compression != 0 && ds.compression != 3) return fail(GBVR_EINVAL, "compression must be 0 (none) or 3 (LZ4)");
+  ds.raw_store_bytes = cursor * es;
+  if (!ds.compression) {
     cudaError_t e = cudaMallocHost(&ds.host_store.p, cursor * es);
     if (e != cudaSuccess) return fail(GBVR_ENOMEM, "page-locked host brick store of " + std::to_string(cursor * es) + " bytes");
     ds.host_store.n = cursor * es;
+  } else {
+    ds.host_coff.assign(nb, 0);
+    ds.chunk_first.assign(nb, 0);
   }
+  // compressed store: each layer of bricks comes to page-locked staging in
+  // one copy and is compressed by host threads
+  std::vector<uint8_t> comp;
+  PinnedBuf h_layer;
+  const unsigned nthreads = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
   // generator tables
   BlobTablesHost tab;
   make_blob_tables(*p, tab);
@@ -612,13 +646,51 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
       CUDA_TRY(launch_gather_bricks_window(w.a.p, dtype, d3, w.z0, tmp_info.as<BrickInfo>(), per, tmp.p, 0, s));
       CUDA_TRY(launch_brick_minmax(tmp.p, dtype, tmp_info.as<BrickInfo>(), per, s));
       CUDA_TRY(cudaMemcpyAsync(layer.data(), tmp_info.p, sizeof(BrickInfo) * per, cudaMemcpyDeviceToHost, s));
-      for (int j = 0; j < per; ++j) {
-        const BrickInfo& b = ds.bricks[first + j];
-        CUDA_TRY(cudaMemcpyAsync((char*)ds.host_store.p + ds.host_off[first + j] * es,
-                                 (const char*)tmp.p + (size_t)j * slot_bytes, (size_t)b.sx * b.sy * b.sz * es,
-                                 cudaMemcpyDeviceToHost, s));
+      if (!ds.compression) {
+        for (int j = 0; j < per; ++j) {
+          const BrickInfo& b = ds.bricks[first + j];
+          CUDA_TRY(cudaMemcpyAsync((char*)ds.host_store.p + ds.host_off[first + j] * es,
+                                   (const char*)tmp.p + (size_t)j * slot_bytes, (size_t)b.sx * b.sy * b.sz * es,
+                                   cudaMemcpyDeviceToHost, s));
+        }
+        CUDA_TRY(cudaStreamSynchronize(s));
+      } else {
+        CUDA_TRY(h_layer.alloc((size_t)per * slot_bytes));
+        CUDA_TRY(cudaMemcpyAsync(h_layer.p, tmp.p, (size_t)per * slot_bytes, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        // per brick its chunks (compressed, or raw when that is not smaller)
+        std::vector<std::vector<uint8_t>> out(per);
+        std::vector<std::vector<unsigned>> sizes(per);
+        auto work = [&](unsigned t) {
+          std::vector<uint8_t> buf(lz4_bound(LZ_CHUNK));
+          for (int j = (int)t; j < per; j += (int)nthreads) {
+            const BrickInfo& b = ds.bricks[first + j];
+            const size_t nbytes = (size_t)b.sx * b.sy * b.sz * es;
+            const uint8_t* src = (const uint8_t*)h_layer.p + (size_t)j * slot_bytes;
+            for (size_t o = 0; o < nbytes; o += LZ_CHUNK) {
+              const size_t rn = std::min(LZ_CHUNK, nbytes - o);
+              const size_t cn = lz4_compress(src + o, rn, buf.data(), buf.size());
+              if (cn > 0 && cn < rn) {
+                out[j].insert(out[j].end(), buf.data(), buf.data() + cn);
+                sizes[j].push_back((unsigned)cn);
+              } else {
+                out[j].insert(out[j].end(), src + o, src + o + rn);
+                sizes[j].push_back((unsigned)rn | 0x80000000u);
+              }
+            }
+          }
+        };
+        std::vector<std::thread> pool_t;
+        for (unsigned t = 1; t < nthreads; ++t) pool_t.emplace_back(work, t);
+        work(0);
+        for (auto& th : pool_t) th.join();
+        for (int j = 0; j < per; ++j) {
+          ds.host_coff[first + j] = comp.size();
+          ds.chunk_first[first + j] = (unsigned)ds.chunk_size.size();
+          comp.insert(comp.end(), out[j].begin(), out[j].end());
+          ds.chunk_size.insert(ds.chunk_size.end(), sizes[j].begin(), sizes[j].end());
+        }
       }
-      CUDA_TRY(cudaStreamSynchronize(s));
       for (int j = 0; j < per; ++j) {
         ds.bricks[first + j].vmin = layer[j].vmin;
         ds.bricks[first + j].vmax = layer[j].vmax;
@@ -682,6 +754,19 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
   for (int l = 0; l < nlev; ++l)
     if (st[l].next_bz != ds.levels[l].nb[2] || st[l].next_cz != ds.levels[l].nc[2])
       return fail(GBVR_ECUDA, "out-of-core build did not complete level " + std::to_string(l));
+  if (ds.compression) {
+    // the compressed store, page-locked for asynchronous paging
+    if (h_layer.p) cudaFreeHost(h_layer.p);
+    h_layer.p = nullptr;
+    h_layer.n = 0;
+    cudaError_t e = cudaMallocHost(&ds.host_store.p, std::max<size_t>(comp.size(), 16));
+    if (e != cudaSuccess) return fail(GBVR_ENOMEM, "page-locked compressed brick store of " + std::to_string(comp.size()) + " bytes");
+    ds.host_store.n = comp.size();
+    memcpy(ds.host_store.p, comp.data(), comp.size());
+    std::vector<uint8_t>().swap(comp);
+    CUDA_TRY(ds.d_lz_err.alloc(sizeof(int)));
+    CUDA_TRY(cudaMemsetAsync(ds.d_lz_err.p, 0, sizeof(int), s));
+  }
   CUDA_TRY(ds.d_bricks.alloc(sizeof(BrickInfo) * nb));
   CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * nb, cudaMemcpyHostToDevice, s));
   ds.gmin = INFINITY;
@@ -994,6 +1079,7 @@ struct gbvr_renderer {
   std::vector<std::shared_ptr<DevBuf>> occ_lv;  // out of core: classified macro-cells per level
   std::vector<char> occ_valid;
   uint64_t last_misses = 0, last_paged = 0;
+  uint64_t last_paged_comp = 0;  // compressed store: bytes copied host to device by the last paint
   float last_page_ms = 0.f;
   long long cell_words = 0;
   PinnedBuf h_frames, h_prefix;
@@ -1580,6 +1666,7 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
     CUDA_TRY(cudaStreamWaitEvent(r->copy_stream, protect_done, 0));
   }
   CUDA_TRY(cudaEventRecord(r->ev_c0[stage], r->copy_stream));
+  std::vector<std::pair<int, int>> paged;  // compressed store: (brick, slot) to decode
   for (int bidx : needed) {
     if (ds.slot_of[bidx] >= 0) continue;
     if (vi >= victims.size()) break;
@@ -1590,11 +1677,57 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
     ds.slot_used[sl] = ds.frame;
     const BrickInfo& b = ds.bricks[bidx];
     const size_t nbytes = (size_t)b.sx * b.sy * b.sz * es;
-    CUDA_TRY(cudaMemcpyAsync((char*)ds.pool.p + (size_t)sl * ds.slot_elems * es,
-                             (const char*)ds.host_store.p + ds.host_off[bidx] * es, nbytes, cudaMemcpyHostToDevice,
-                             r->copy_stream));
+    if (ds.compression) {
+      paged.emplace_back(bidx, sl);
+    } else {
+      CUDA_TRY(cudaMemcpyAsync((char*)ds.pool.p + (size_t)sl * ds.slot_elems * es,
+                               (const char*)ds.host_store.p + ds.host_off[bidx] * es, nbytes, cudaMemcpyHostToDevice,
+                               r->copy_stream));
+    }
     bytes += nbytes;
   }
+  uint64_t comp_bytes = 0;
+  if (!paged.empty()) {
+    // compressed runs to the device staging, then one decode of all their
+    // chunks into the slots (both on the copy stream)
+    std::vector<Lz4Chunk> jobs;
+    std::vector<size_t> run(paged.size());
+    size_t total = 0;
+    for (size_t q = 0; q < paged.size(); ++q) {
+      const int bidx = paged[q].first;
+      const BrickInfo& b = ds.bricks[bidx];
+      const size_t nbytes = (size_t)b.sx * b.sy * b.sz * es;
+      const unsigned c0 = ds.chunk_first[bidx], nc = (unsigned)((nbytes + LZ_CHUNK - 1) / LZ_CHUNK);
+      size_t cb = 0;
+      for (unsigned k = 0; k < nc; ++k) {
+        const unsigned cs = ds.chunk_size[c0 + k];
+        Lz4Chunk ch;
+        ch.src = total + cb;
+        ch.dst = (unsigned long long)paged[q].second * ds.slot_elems * es + (unsigned long long)k * LZ_CHUNK;
+        ch.comp = cs;
+        ch.raw = (unsigned)std::min(LZ_CHUNK, nbytes - (size_t)k * LZ_CHUNK);
+        jobs.push_back(ch);
+        cb += cs & 0x7fffffffu;
+      }
+      run[q] = cb;
+      total += cb;
+    }
+    CUDA_TRY(ds.d_stage.alloc(std::max<size_t>(total, 16)));
+    CUDA_TRY(ds.d_chunks.alloc(sizeof(Lz4Chunk) * jobs.size()));
+    size_t at = 0;
+    for (size_t q = 0; q < paged.size(); ++q) {
+      CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + at, (const char*)ds.host_store.p + ds.host_coff[paged[q].first],
+                               run[q], cudaMemcpyHostToDevice, r->copy_stream));
+      at += run[q];
+    }
+    // pageable source: the copy returns once it is staged
+    CUDA_TRY(cudaMemcpyAsync(ds.d_chunks.p, jobs.data(), sizeof(Lz4Chunk) * jobs.size(), cudaMemcpyHostToDevice,
+                             r->copy_stream));
+    CUDA_TRY(launch_lz4_decode(ds.d_stage.p, ds.pool.p, ds.d_chunks.as<Lz4Chunk>(), (int)jobs.size(),
+                               ds.d_lz_err.as<int>(), r->copy_stream));
+    comp_bytes = total;
+  }
+  r->last_paged_comp += comp_bytes;
   CUDA_TRY(cudaEventRecord(r->ev_c1[stage], r->copy_stream));
   CUDA_TRY(cudaStreamWaitEvent(r->stream, r->ev_c1[stage], 0));
   // page table of the rendered level and its skip table, staged in page-locked
@@ -1633,6 +1766,17 @@ int ooc_streams(gbvr_renderer* r) {
   return GBVR_OK;
 }
 
+// Out of core with a compressed store: a chunk the device decoder found
+// malformed (the store is written by lz4_compress, so only a corrupted store
+// does this) fails the paint.
+int check_decode(gbvr_renderer* r) {
+  if (!r->ds.ooc || !r->ds.compression) return GBVR_OK;
+  int e = 0;
+  CUDA_TRY(cudaMemcpy(&e, r->ds.d_lz_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return fail(GBVR_EFORMAT, "corrupt compressed brick in the out-of-core store");
+  return GBVR_OK;
+}
+
 int prepare(gbvr_renderer* r, int nviews, int& level, const gbvr_view* views) {
   TRY(check_loaded(r));
   if (nviews <= 0) return fail(GBVR_EINVAL, "view count must be positive");
@@ -1652,9 +1796,11 @@ int prepare(gbvr_renderer* r, int nviews, int& level, const gbvr_view* views) {
       views = vs.data();
     }
     // every earlier paint has finished (paints are synchronous): no slot is in use
+    r->last_paged_comp = 0;
     TRY(ooc_page(r, views, views == vs.data() ? 1 : nviews, level, 0, nullptr, 0, &r->last_misses, &r->last_paged,
                  r->slice_sel));
     CUDA_TRY(cudaEventSynchronize(r->ev_c1[0]));
+    TRY(check_decode(r));
     CUDA_TRY(cudaEventElapsedTime(&r->last_page_ms, r->ev_c0[0], r->ev_c1[0]));
     r->drop_graphs();  // the page table changes between paints
   }
@@ -1825,6 +1971,7 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
     return GBVR_OK;
   }
   TRY(ooc_streams(r));
+  r->last_paged_comp = 0;
   const size_t npix = (size_t)r->width * r->height;
   if (r->fb_views < n || r->fb_w != r->width || r->fb_h != r->height) {
     CUDA_TRY(r->d_fb8.alloc(npix * 4 * n));
@@ -1889,6 +2036,7 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
   r->last_misses = tot_miss;
   r->last_paged = tot_paged;
   r->last_page_ms = tot_page_ms;
+  TRY(check_decode(r));
   r->last_h2d = 0;
   return finish(r, n, level);
 }
@@ -2298,8 +2446,10 @@ int gbvr_get_dataset_info(gbvr_renderer* r, gbvr_dataset_info* info) {
     }
   info->total_bricks = (int64_t)ds.bricks.size();
   info->device_bytes = ds.ooc ? (uint64_t)ds.nslots * ds.slot_elems * dtype_size(ds.dtype) : ds.stored_bytes;
-  info->host_bytes = ds.ooc ? ds.stored_bytes : 0;
+  info->host_bytes = ds.ooc ? (ds.compression ? ds.host_store.n : ds.stored_bytes) : 0;
   info->device_slots = ds.ooc ? ds.nslots : 0;
+  info->compression = ds.ooc ? ds.compression : 0;
+  info->host_raw_bytes = ds.ooc ? ds.stored_bytes : 0;
   info->hist1d_size = (int)ds.hist1d.size();
   info->hist2d_max_grad = ds.max_grad;
   return GBVR_OK;
@@ -2346,6 +2496,19 @@ int gbvr_get_brick(gbvr_renderer* r, int lod, const int32_t brick[3], void* out,
   if (stored_dims) { stored_dims[0] = b.sx; stored_dims[1] = b.sy; stored_dims[2] = b.sz; }
   if (!out) return GBVR_OK;
   if (bytes < need) return fail(GBVR_EINVAL, "brick buffer too small");
+  if (r->ds.ooc && r->ds.compression) {
+    // decode the brick's chunks on the host
+    const size_t bidx = &b - r->ds.bricks.data();
+    const uint8_t* src = (const uint8_t*)r->ds.host_store.p + r->ds.host_coff[bidx];
+    for (size_t k = 0, o = 0; o < need; ++k, o += LZ_CHUNK) {
+      const unsigned cs = r->ds.chunk_size[r->ds.chunk_first[bidx] + k];
+      const size_t rn = std::min(LZ_CHUNK, need - o), cn = cs & 0x7fffffffu;
+      if (cs & 0x80000000u) memcpy((uint8_t*)out + o, src, rn);
+      else if (!lz4_decompress(src, cn, (uint8_t*)out + o, rn)) return fail(GBVR_EFORMAT, "corrupt compressed brick");
+      src += cn;
+    }
+    return GBVR_OK;
+  }
   if (r->ds.ooc) {
     memcpy(out, (const char*)r->ds.host_store.p + r->ds.host_off[&b - r->ds.bricks.data()] * es, need);
     return GBVR_OK;
@@ -2721,9 +2884,10 @@ int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out) {
   out->subframes = 1;
   out->gpu_ms = r->last_ms;
   out->kernel_ms = r->last_kernel_ms;
-  out->h2d_bytes = r->last_h2d + r->last_paged;
+  out->h2d_bytes = r->last_h2d + (r->ds.compression ? r->last_paged_comp : r->last_paged);
   out->brick_misses = r->last_misses;
   out->bytes_paged = r->last_paged;
+  out->bytes_paged_compressed = r->last_paged_comp;
   out->page_ms = r->last_page_ms;
   if (r->last_views < 1 || !r->ds.loaded) return GBVR_OK;
   const int n = r->last_views;

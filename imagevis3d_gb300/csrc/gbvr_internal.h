@@ -279,6 +279,17 @@ struct Hist2DScratch {
 cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], double max_scalar,
                           long long nx, long long merge, unsigned long long* hist,
                           Hist2DScratch* scratch, cudaStream_t s);
+// LZ4-compressed brick chunks to decode on the device: the compressed bytes
+// at stage + src (comp bytes; bit 31 set: stored uncompressed) become raw
+// bytes at pool + dst.
+struct Lz4Chunk {
+  unsigned long long src, dst;
+  unsigned comp, raw;
+};
+// one warp per chunk; a malformed chunk sets *err (nonzero) and is left partly written
+cudaError_t launch_lz4_decode(const void* stage, void* pool, const Lz4Chunk* chunks, int nchunks, int* err,
+                              cudaStream_t s);
+
 // One of the three passes (1: Smax, 2: f64 max |grad| at Smax, 3: binning)
 // over the planes [zb, ze) of a volume streamed in z: `slab` holds planes
 // zlo .. (zlo <= zb - 1 unless zb = 0, and plane ze unless ze = Z).  The

@@ -946,4 +946,121 @@ cudaError_t launch_hist2d_slab(const void* slab, int dtype, const long long dims
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// LZ4 block decoding of paged bricks (out-of-core store compressed with the
+// codec of lz4.cpp, one block per 64 KiB chunk of a brick).  One warp per
+// chunk: lane 0 parses each sequence header (every read and write bound
+// checked), the warp copies the literals, then the match.  A match reads only
+// output before its start: with offset >= 32 a 32-byte step reads bytes
+// written by earlier steps; a shorter offset repeats its pattern, so byte i
+// of the match is output[start - offset + i mod offset].  __syncwarp orders
+// the lanes' writes between steps.  A malformed block sets *err and stops.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restrict__ stage,
+                                                    unsigned char* __restrict__ pool,
+                                                    const Lz4Chunk* __restrict__ chunks, int nchunks,
+                                                    int* __restrict__ err) {
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= nchunks) return;
+  const Lz4Chunk c = chunks[w];
+  const unsigned char* in = stage + c.src;
+  unsigned char* out = pool + c.dst;
+  const unsigned n = c.comp & 0x7fffffffu, raw = c.raw;
+  if (c.comp & 0x80000000u) {  // stored uncompressed
+    if (n != raw) {
+      if (lane == 0) atomicOr(err, 1);
+      return;
+    }
+    for (unsigned i = lane; i < raw; i += 32) out[i] = __ldg(in + i);
+    return;
+  }
+  unsigned ip = 0, op = 0;
+  for (;;) {
+    // 0: literals then a match; 1: literals only (the last sequence); 2: malformed
+    unsigned state = 0, nlit = 0, lit_at = 0, off = 0, mlen = 0;
+    if (lane == 0) {
+      if (ip >= n) {
+        state = 2;
+      } else {
+        const unsigned token = __ldg(in + ip++);
+        nlit = token >> 4;
+        if (nlit == 15) {
+          unsigned b = 255;
+          while (b == 255) {
+            if (ip >= n) { state = 2; break; }
+            b = __ldg(in + ip++);
+            nlit += b;
+          }
+        }
+        if (state == 0 && (nlit > n - ip || nlit > raw - op)) state = 2;
+        if (state == 0) {
+          lit_at = ip;
+          ip += nlit;
+          if (ip == n) {
+            state = op + nlit == raw ? 1 : 2;
+          } else if (n - ip < 2) {
+            state = 2;
+          } else {
+            off = (unsigned)__ldg(in + ip) | ((unsigned)__ldg(in + ip + 1) << 8);
+            ip += 2;
+            mlen = token & 15;
+            if (mlen == 15) {
+              unsigned b = 255;
+              while (b == 255) {
+                if (ip >= n) { state = 2; break; }
+                b = __ldg(in + ip++);
+                mlen += b;
+              }
+            }
+            mlen += 4;
+            if (state == 0 && (off == 0 || off > op + nlit || mlen > raw - op - nlit)) state = 2;
+          }
+        }
+      }
+    }
+    state = __shfl_sync(0xffffffffu, state, 0);
+    if (state == 2) {
+      if (lane == 0) atomicOr(err, 1);
+      return;
+    }
+    nlit = __shfl_sync(0xffffffffu, nlit, 0);
+    lit_at = __shfl_sync(0xffffffffu, lit_at, 0);
+    for (unsigned i = lane; i < nlit; i += 32) out[op + i] = __ldg(in + lit_at + i);
+    op += nlit;
+    if (state == 1) return;
+    off = __shfl_sync(0xffffffffu, off, 0);
+    mlen = __shfl_sync(0xffffffffu, mlen, 0);
+    ip = __shfl_sync(0xffffffffu, ip, 0);
+    __syncwarp();
+    if (off >= 32) {
+      for (unsigned base = 0; base < mlen; base += 32) {
+        const unsigned i = base + lane;
+        if (i < mlen) out[op + i] = out[op - off + i];
+        __syncwarp();
+      }
+    } else {
+      // i mod off, stepped by 32 mod off
+      unsigned r = lane % off;
+      const unsigned step = 32 % off;
+      for (unsigned i = lane; i < mlen; i += 32) {
+        out[op + i] = out[op - off + r];
+        r += step;
+        if (r >= off) r -= off;
+      }
+      __syncwarp();
+    }
+    op += mlen;
+  }
+}
+
+cudaError_t launch_lz4_decode(const void* stage, void* pool, const Lz4Chunk* chunks, int nchunks, int* err,
+                              cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (nchunks <= 0) return cudaSuccess;
+  const unsigned blocks = (unsigned)((nchunks + 3) / 4);
+  k_lz4_decode<<<blocks, 128, 0, s>>>((const unsigned char*)stage, (unsigned char*)pool, chunks, nchunks, err);
+  return cudaGetLastError();
+}
+
 }  // namespace gbvr

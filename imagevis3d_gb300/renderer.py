@@ -23,13 +23,15 @@ def _fp(a):
 
 
 def brick_params(brick_size=256, overlap=2, max_lods=0, build_texture=False, layouts=1,
-                 aspect=(1, 1, 1)):
+                 aspect=(1, 1, 1), compression=0):
+    """compression: out-of-core host store codec, 0 raw or 3 (LZ4)."""
     bp = L.BrickParams()
     bp.brick_size = brick_size
     bp.overlap = overlap
     bp.max_lods = max_lods
     bp.build_texture = 1 if build_texture else 0
     bp.layouts = layouts
+    bp.compression = compression
     for i in range(3):
         bp.aspect[i] = aspect[i]
     return bp
@@ -184,7 +186,8 @@ class Renderer:
                     lod_bricks=[tuple(info.lod_bricks[i]) for i in range(n)],
                     total_bricks=info.total_bricks, device_bytes=info.device_bytes,
                     hist1d_size=info.hist1d_size, hist2d_max_grad=info.hist2d_max_grad,
-                    host_bytes=info.host_bytes, device_slots=info.device_slots)
+                    host_bytes=info.host_bytes, device_slots=info.device_slots,
+                    compression=info.compression, host_raw_bytes=info.host_raw_bytes)
 
     def getHistogram(self):
         n = self.datasetInfo()["hist1d_size"]

@@ -93,7 +93,9 @@ typedef struct gbvr_brick_params {
                            whose fastest axis is closest to its screen x axis;
                            4: also a copy in 4x4x4 voxel blocks (2x memory),
                            sampled by every view */
-  int32_t reserved;
+  int32_t compression;  /* out-of-core host store: 0 raw, 3 LZ4 (the UVF codec id CT_LZ4,
+                           CmdLineConverter/main.cpp:175-178): 64 KiB chunks compressed by host
+                           threads at build, decoded on the GPU when paged */
   double aspect[3];     /* voxel spacing; 0 = (1,1,1) */
 } gbvr_brick_params;
 
@@ -112,7 +114,8 @@ typedef struct gbvr_dataset_info {
   float hist2d_max_grad;  /* max gradient magnitude of the 2D histogram */
   uint64_t host_bytes;    /* out of core: bytes of the page-locked host brick store */
   int32_t device_slots;   /* out of core: bricks the device pool holds at once */
-  int32_t reserved;
+  int32_t compression;    /* out of core: the store's codec (0 raw, 3 LZ4) */
+  uint64_t host_raw_bytes;/* out of core: the store's bytes uncompressed */
 } gbvr_dataset_info;
 
 /* One view of a batch: camera, output size and (optionally) its own TF. */
@@ -137,6 +140,7 @@ typedef struct gbvr_stats {
   uint64_t cells_touched;      /* stats level 2: sum over views of distinct non-empty macro-cells sampled */
   uint64_t cell_bytes;         /* ... times the cell's voxel bytes (4^3 voxels) */
   double page_ms;              /* out of core: device time of the last paint's brick uploads */
+  uint64_t bytes_paged_compressed; /* out of core, compressed store: host->device bytes of those bricks */
 } gbvr_stats;
 
 /* ---- errors / device ---- */
@@ -558,6 +562,14 @@ int gbvr_uvf_write_raster(const char* path, const char* raster_id, const void* v
                           const int64_t dims[3], int dtype, int32_t brick_size, int32_t overlap,
                           const uint64_t* hist1d, size_t n1, const uint64_t* hist2d, size_t nx,
                           size_t ny, float max_grad, const double* minmax, size_t nminmax);
+
+/* ---- LZ4 block codec (UVF brick compression id 3, CT_LZ4: UVFReader/BlockInfo.h:60-93), host side.  The
+ * out-of-core brick store compresses with it (gbvr_brick_params.compression) and the GPU decodes paged
+ * bricks.  gbvr_lz4_compress returns the compressed size (0: does not fit in cap); gbvr_lz4_decompress
+ * decodes into exactly out_n bytes (GBVR_EFORMAT when malformed). ---- */
+size_t gbvr_lz4_bound(size_t n);
+size_t gbvr_lz4_compress(const void* src, size_t n, void* dst, size_t cap);
+int gbvr_lz4_decompress(const void* src, size_t n, void* dst, size_t out_n);
 
 #ifdef __cplusplus
 }

@@ -988,6 +988,47 @@ void orc_line_keys(const orc_render_params* p, uint32_t* out) {
   memcpy(out, keys.data(), sizeof(uint32_t) * keys.size());
 }
 
+// LZ4 block decoding, restated from the published block format (test
+// oracle for the library's codec): sequences of a token (literal count in
+// the high nibble, match length - 4 in the low one, 15 = continued by bytes
+// added until one below 255), the literals, a 2-byte little-endian offset
+// and the match; the last sequence carries literals only.  Returns the
+// decoded size, or -1 when the block is malformed or exceeds out_n.
+i64 orc_lz4_decompress(const uint8_t* in, i64 n, uint8_t* out, i64 out_n) {
+  i64 ip = 0, op = 0;
+  while (ip < n) {
+    const int token = in[ip++];
+    i64 lit = token >> 4;
+    if (lit == 15) {
+      int b;
+      do {
+        if (ip >= n) return -1;
+        b = in[ip++];
+        lit += b;
+      } while (b == 255);
+    }
+    if (ip + lit > n || op + lit > out_n) return -1;
+    for (i64 i = 0; i < lit; ++i) out[op++] = in[ip++];
+    if (ip == n) return op;
+    if (ip + 2 > n) return -1;
+    const i64 off = in[ip] + 256 * (i64)in[ip + 1];
+    ip += 2;
+    i64 len = (token & 15);
+    if (len == 15) {
+      int b;
+      do {
+        if (ip >= n) return -1;
+        b = in[ip++];
+        len += b;
+      } while (b == 255);
+    }
+    len += 4;
+    if (off < 1 || off > op || op + len > out_n) return -1;
+    for (i64 i = 0; i < len; ++i, ++op) out[op] = out[op - off];
+  }
+  return -1;  // a block ends with a literal-only sequence
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -246,6 +246,16 @@ def line_keys(dims, extent, view, proj, width, height, bbox):
     return out
 
 
+def lz4_decompress(block, out_n):
+    """Oracle LZ4 block decoder: bytes, or None when malformed."""
+    src = np.frombuffer(bytes(block), np.uint8) if len(block) else np.zeros(1, np.uint8)
+    out = np.zeros(max(out_n, 1), np.uint8)
+    f = lib().orc_lz4_decompress
+    f.restype = I64
+    n = f(src.ctypes.data_as(C.c_void_p), I64(len(block)), out.ctypes.data_as(C.c_void_p), I64(out_n))
+    return None if n < 0 else out[:n].tobytes()
+
+
 def render_slice(vol, axis, coord, width, height, tf, value_range=(0.0, 255.0), flip_x=False, flip_y=False,
                  mip=False, interp=1, extent=None, bg=(0, 0, 0)):
     """FP64 2D slice view of the flat level `vol` ((z, y, x)): [h, w, 4]."""

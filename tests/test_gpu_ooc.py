@@ -296,3 +296,54 @@ def test_ooc_slices_equal_incore(mip):
         assert visible > 20000
         # slice MIP needs all 160 bricks of level 0: it falls back; a slice fits
         assert lods == ({1} if mip else {0})
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_ooc_compressed_store_equals_raw_store(case):
+    """The LZ4-compressed host store holds the same bricks (decoded on the
+    host) and pages the same bricks (decoded on the GPU): images of a paged
+    fly-through equal the raw store's bit for bit."""
+    sp, bp = CASES[case]
+    slot = (bp["brick_size"] ** 3) * (1 if sp.dtype == 0 else 2 if sp.dtype == 1 else 4)
+    views = _inside_path(6, 128, 96)
+    with Renderer(float_fb=True) as a, Renderer(float_fb=True) as b:
+        a.loadSyntheticOutOfCore(sp, 30 * slot, **bp)
+        b.loadSyntheticOutOfCore(sp, 30 * slot, compression=3, **bp)
+        ia, ib = a.datasetInfo(), b.datasetInfo()
+        assert ib["compression"] == 3 and ib["host_raw_bytes"] == ia["host_bytes"] > 0
+        assert 0 < ib["host_bytes"] <= ib["host_raw_bytes"] * 1.01
+        for lod in range(ia["lod_count"]):
+            nb = ia["lod_bricks"][lod]
+            for bz in range(nb[2]):
+                for by in range(nb[1]):
+                    for bx in range(nb[0]):
+                        va, oa = a.getBrick(lod, (bx, by, bz))
+                        vb, ob = b.getBrick(lod, (bx, by, bz))
+                        assert oa == ob and np.array_equal(va, vb), (lod, bx, by, bz)
+        for r in (a, b):
+            _setup(r, sp, 128, 96)
+        la, _, pa = a.paintPath(views)
+        lb, _, pb = b.paintPath(views)
+        assert np.array_equal(la, lb) and np.array_equal(pa, pb)
+        st = b.stats()
+        assert st["bytes_paged_compressed"] > 0
+        for i in range(len(views)):
+            assert np.array_equal(a.readFramebuffer(i, as_float=True), b.readFramebuffer(i, as_float=True)), i
+        # synchronous paints and a slice page through the same decoder
+        a.setView(*views[3])
+        b.setView(*views[3])
+        a.paint()
+        b.paint()
+        assert np.array_equal(a.readFramebuffer(0, as_float=True), b.readFramebuffer(0, as_float=True))
+        a.paintSlice(2, 40)
+        b.paintSlice(2, 40)
+        assert np.array_equal(a.readFramebuffer(0, as_float=True), b.readFramebuffer(0, as_float=True))
+
+
+def test_ooc_compression_shrinks_smooth_volumes():
+    sp = synth_params((192, 160, 144), np.uint8, 33, 10, (10.0, 30.0), (0.4, 1.0), 255.0, vmax=255.0,
+                      bg_freq=1.0, bg_level=0.1, bg_amp=0.1)
+    with Renderer() as r:
+        r.loadSyntheticOutOfCore(sp, 1 << 28, brick_size=64, overlap=2, compression=3)
+        info = r.datasetInfo()
+    assert info["host_bytes"] * 2 < info["host_raw_bytes"]

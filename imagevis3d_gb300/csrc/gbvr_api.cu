@@ -248,11 +248,17 @@ struct Dataset {
   // byte host_coff[b]; chunk_size[chunk_first[b] + k] is chunk k's compressed
   // size (bit 31: stored uncompressed).  Paged bricks are decoded on the
   // device from d_stage into their slots.
+  // The compressed store is a list of page-locked segments (a brick's run
+  // lies in one): segment host_cseg[b], byte host_coff[b].
   int compression = 0;
+  std::vector<void*> seg_p;
+  std::vector<size_t> seg_used;
+  std::vector<int> host_cseg;
   std::vector<unsigned long long> host_coff;
   std::vector<unsigned> chunk_first, chunk_size;
-  uint64_t raw_store_bytes = 0;
+  uint64_t raw_store_bytes = 0, comp_store_bytes = 0;
   DevBuf d_stage, d_chunks, d_lz_err;
+  const uint8_t* comp_run(size_t b) const { return (const uint8_t*)seg_p[host_cseg[b]] + host_coff[b]; }
   size_t slot_elems = 0;
   int nslots = 0;
   std::vector<int> slot_of;                  // per brick, -1 = not resident
@@ -273,6 +279,11 @@ struct Dataset {
     ooc = false;
     host_off.clear();
     compression = 0;
+    for (void* q : seg_p) cudaFreeHost(q);
+    seg_p.clear();
+    seg_used.clear();
+    host_cseg.clear();
+    comp_store_bytes = 0;
     host_coff.clear();
     chunk_first.clear();
     chunk_size.clear();
@@ -511,8 +522,9 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
 // memory is O(plane area x brick size), independent of the volume depth.
 // ---------------------------------------------------------------------------
 constexpr int OOC_CELL_SHIFT = 3;
-// raw bytes per compressed chunk of a brick (one LZ4 block; offsets reach 64 KiB back)
-constexpr size_t LZ_CHUNK = 65536;
+// raw bytes per compressed chunk of a brick (one LZ4 block): small enough that
+// a paged frame gives the decoder thousands of warps
+constexpr size_t LZ_CHUNK = 16384;
 
 int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_params* bp, uint64_t pool_bytes,
                     cudaStream_t s) {
@@ -570,11 +582,28 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
     ds.host_store.n = cursor * es;
   } else {
     ds.host_coff.assign(nb, 0);
+    ds.host_cseg.assign(nb, 0);
     ds.chunk_first.assign(nb, 0);
   }
   // compressed store: each layer of bricks comes to page-locked staging in
-  // one copy and is compressed by host threads
-  std::vector<uint8_t> comp;
+  // one copy and is compressed by host threads into page-locked segments of
+  // 16 MiB .. 4 GiB (no copy of the whole store: it is built in place)
+  const size_t kSeg = std::min<size_t>((size_t)1 << 32, std::max<size_t>((size_t)1 << 24, ds.raw_store_bytes / 8));
+  auto seg_append = [&](const uint8_t* data, size_t n, int& seg, unsigned long long& off) -> int {
+    if (ds.seg_p.empty() || ds.seg_used.back() + n > kSeg) {
+      void* q = nullptr;
+      if (cudaMallocHost(&q, std::max(kSeg, n)) != cudaSuccess)
+        return fail(GBVR_ENOMEM, "page-locked compressed brick store segment");
+      ds.seg_p.push_back(q);
+      ds.seg_used.push_back(0);
+    }
+    seg = (int)ds.seg_p.size() - 1;
+    off = ds.seg_used.back();
+    memcpy((uint8_t*)ds.seg_p.back() + off, data, n);
+    ds.seg_used.back() += n;
+    ds.comp_store_bytes += n;
+    return GBVR_OK;
+  };
   PinnedBuf h_layer;
   const unsigned nthreads = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
   // generator tables
@@ -685,9 +714,8 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
         work(0);
         for (auto& th : pool_t) th.join();
         for (int j = 0; j < per; ++j) {
-          ds.host_coff[first + j] = comp.size();
+          TRY(seg_append(out[j].data(), out[j].size(), ds.host_cseg[first + j], ds.host_coff[first + j]));
           ds.chunk_first[first + j] = (unsigned)ds.chunk_size.size();
-          comp.insert(comp.end(), out[j].begin(), out[j].end());
           ds.chunk_size.insert(ds.chunk_size.end(), sizes[j].begin(), sizes[j].end());
         }
       }
@@ -755,15 +783,9 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
     if (st[l].next_bz != ds.levels[l].nb[2] || st[l].next_cz != ds.levels[l].nc[2])
       return fail(GBVR_ECUDA, "out-of-core build did not complete level " + std::to_string(l));
   if (ds.compression) {
-    // the compressed store, page-locked for asynchronous paging
     if (h_layer.p) cudaFreeHost(h_layer.p);
     h_layer.p = nullptr;
     h_layer.n = 0;
-    cudaError_t e = cudaMallocHost(&ds.host_store.p, std::max<size_t>(comp.size(), 16));
-    if (e != cudaSuccess) return fail(GBVR_ENOMEM, "page-locked compressed brick store of " + std::to_string(comp.size()) + " bytes");
-    ds.host_store.n = comp.size();
-    memcpy(ds.host_store.p, comp.data(), comp.size());
-    std::vector<uint8_t>().swap(comp);
     CUDA_TRY(ds.d_lz_err.alloc(sizeof(int)));
     CUDA_TRY(cudaMemsetAsync(ds.d_lz_err.p, 0, sizeof(int), s));
   }
@@ -1716,8 +1738,8 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
     CUDA_TRY(ds.d_chunks.alloc(sizeof(Lz4Chunk) * jobs.size()));
     size_t at = 0;
     for (size_t q = 0; q < paged.size(); ++q) {
-      CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + at, (const char*)ds.host_store.p + ds.host_coff[paged[q].first],
-                               run[q], cudaMemcpyHostToDevice, r->copy_stream));
+      CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + at, ds.comp_run(paged[q].first), run[q], cudaMemcpyHostToDevice,
+                               r->copy_stream));
       at += run[q];
     }
     // pageable source: the copy returns once it is staged
@@ -2446,7 +2468,7 @@ int gbvr_get_dataset_info(gbvr_renderer* r, gbvr_dataset_info* info) {
     }
   info->total_bricks = (int64_t)ds.bricks.size();
   info->device_bytes = ds.ooc ? (uint64_t)ds.nslots * ds.slot_elems * dtype_size(ds.dtype) : ds.stored_bytes;
-  info->host_bytes = ds.ooc ? (ds.compression ? ds.host_store.n : ds.stored_bytes) : 0;
+  info->host_bytes = ds.ooc ? (ds.compression ? ds.comp_store_bytes : ds.stored_bytes) : 0;
   info->device_slots = ds.ooc ? ds.nslots : 0;
   info->compression = ds.ooc ? ds.compression : 0;
   info->host_raw_bytes = ds.ooc ? ds.stored_bytes : 0;
@@ -2499,7 +2521,7 @@ int gbvr_get_brick(gbvr_renderer* r, int lod, const int32_t brick[3], void* out,
   if (r->ds.ooc && r->ds.compression) {
     // decode the brick's chunks on the host
     const size_t bidx = &b - r->ds.bricks.data();
-    const uint8_t* src = (const uint8_t*)r->ds.host_store.p + r->ds.host_coff[bidx];
+    const uint8_t* src = r->ds.comp_run(bidx);
     for (size_t k = 0, o = 0; o < need; ++k, o += LZ_CHUNK) {
       const unsigned cs = r->ds.chunk_size[r->ds.chunk_first[bidx] + k];
       const size_t rn = std::min(LZ_CHUNK, need - o), cn = cs & 0x7fffffffu;

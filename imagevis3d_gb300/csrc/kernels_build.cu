@@ -948,7 +948,7 @@ cudaError_t launch_hist2d_slab(const void* slab, int dtype, const long long dims
 
 // ---------------------------------------------------------------------------
 // LZ4 block decoding of paged bricks (out-of-core store compressed with the
-// codec of lz4.cpp, one block per 64 KiB chunk of a brick).  One warp per
+// codec of lz4.cpp, one block per 16 KiB chunk of a brick).  One warp per
 // chunk: lane 0 parses each sequence header (every read and write bound
 // checked), the warp copies the literals, then the match.  A match reads only
 // output before its start: with offset >= 32 a 32-byte step reads bytes

@@ -218,13 +218,14 @@ def flythrough_views(keys, frames, width, height, fov=45.0, znear=0.01, zfar=10.
 
 
 def config4(size=(8192, 8192, 4096), width=1920, height=1080, frames=120, brick=256, lods=6, seed=SEED + 4):
-    """Out-of-core volume: 192 seeded blobs over a low-frequency background
-    layer, uint8, 256^3 bricks with 2 ghosts and `lods` levels, a fly-through
-    of `frames` frames at width x height (from outside the volume into it and
-    through), 1D TF with 256 entries (alpha 0 below 60)."""
+    """Out-of-core volume: layered seeded blobs, 192 of them over a
+    low-frequency background layer (no per-voxel noise), uint8, 256^3 bricks
+    with 2 ghosts and `lods` levels, a fly-through of `frames` frames at
+    width x height (from outside the volume into it and through), 1D TF with
+    256 entries (alpha 0 below 60)."""
     n = max(size)
-    sp = synth_params(size, np.uint8, seed, 192, (0.01 * n, 0.04 * n), (0.3, 1.0), 255.0, noise_kind=1,
-                      noise_amp=4.0, vmax=255.0, bg_freq=1.5, bg_level=0.08, bg_amp=0.1)
+    sp = synth_params(size, np.uint8, seed, 192, (0.01 * n, 0.04 * n), (0.3, 1.0), 255.0, vmax=255.0,
+                      bg_freq=1.5, bg_level=0.08, bg_amp=0.1)
     tf = tf1d_seeded(256, seed, 60.0, 255.0)
     m = [s / n for s in size]  # normalised half extents are m / 2
     keys = [((-0.9 * m[0], 0.1, -0.6 * m[2]), (0.0, 0.0, 0.0), (0, 1, 0)),

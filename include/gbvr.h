@@ -94,7 +94,7 @@ typedef struct gbvr_brick_params {
                            4: also a copy in 4x4x4 voxel blocks (2x memory),
                            sampled by every view */
   int32_t compression;  /* out-of-core host store: 0 raw, 3 LZ4 (the UVF codec id CT_LZ4,
-                           CmdLineConverter/main.cpp:175-178): 64 KiB chunks compressed by host
+                           CmdLineConverter/main.cpp:175-178): 16 KiB chunks compressed by host
                            threads at build, decoded on the GPU when paged */
   double aspect[3];     /* voxel spacing; 0 = (1,1,1) */
 } gbvr_brick_params;

@@ -949,8 +949,8 @@ cudaError_t launch_hist2d_slab(const void* slab, int dtype, const long long dims
 // ---------------------------------------------------------------------------
 // LZ4 block decoding of paged bricks (out-of-core store compressed with the
 // codec of lz4.cpp, one block per 16 KiB chunk of a brick).  One warp per
-// chunk: lane 0 parses each sequence header (every read and write bound
-// checked), the warp copies the literals, then the match.  A match reads only
+// chunk parses each sequence header in lockstep (every read and write bound
+// checked), copies the literals, then the match.  A match reads only
 // output before its start: with offset >= 32 a 32-byte step reads bytes
 // written by earlier steps; a shorter offset repeats its pattern, so byte i
 // of the match is output[start - offset + i mod offset].  __syncwarp orders
@@ -975,63 +975,54 @@ __global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restr
     for (unsigned i = lane; i < raw; i += 32) out[i] = __ldg(in + i);
     return;
   }
+  // The warp parses in lockstep from a 32-byte window of the input, one byte
+  // per lane (refilled with one coalesced load when the parse leaves it):
+  // header bytes come by shuffle, not by dependent loads.
+  unsigned wbase = 0xffffffffu, wbyte = 0;
+  auto byte_at = [&](unsigned pos) -> unsigned {
+    if (pos < wbase || pos >= wbase + 32) {
+      wbase = pos;
+      wbyte = pos + lane < n ? (unsigned)__ldg(in + pos + lane) : 0u;
+    }
+    return __shfl_sync(0xffffffffu, wbyte, (int)(pos - wbase));
+  };
   unsigned ip = 0, op = 0;
   for (;;) {
-    // 0: literals then a match; 1: literals only (the last sequence); 2: malformed
-    unsigned state = 0, nlit = 0, lit_at = 0, off = 0, mlen = 0;
-    if (lane == 0) {
-      if (ip >= n) {
-        state = 2;
-      } else {
-        const unsigned token = __ldg(in + ip++);
-        nlit = token >> 4;
-        if (nlit == 15) {
-          unsigned b = 255;
-          while (b == 255) {
-            if (ip >= n) { state = 2; break; }
-            b = __ldg(in + ip++);
-            nlit += b;
-          }
-        }
-        if (state == 0 && (nlit > n - ip || nlit > raw - op)) state = 2;
-        if (state == 0) {
-          lit_at = ip;
-          ip += nlit;
-          if (ip == n) {
-            state = op + nlit == raw ? 1 : 2;
-          } else if (n - ip < 2) {
-            state = 2;
-          } else {
-            off = (unsigned)__ldg(in + ip) | ((unsigned)__ldg(in + ip + 1) << 8);
-            ip += 2;
-            mlen = token & 15;
-            if (mlen == 15) {
-              unsigned b = 255;
-              while (b == 255) {
-                if (ip >= n) { state = 2; break; }
-                b = __ldg(in + ip++);
-                mlen += b;
-              }
-            }
-            mlen += 4;
-            if (state == 0 && (off == 0 || off > op + nlit || mlen > raw - op - nlit)) state = 2;
-          }
-        }
+    if (ip >= n) break;  // malformed: the block ended after a match
+    const unsigned token = byte_at(ip++);
+    unsigned nlit = token >> 4;
+    bool bad = false;
+    if (nlit == 15) {
+      unsigned b = 255;
+      while (b == 255) {
+        if (ip >= n) { bad = true; break; }
+        b = byte_at(ip++);
+        nlit += b;
       }
     }
-    state = __shfl_sync(0xffffffffu, state, 0);
-    if (state == 2) {
-      if (lane == 0) atomicOr(err, 1);
-      return;
-    }
-    nlit = __shfl_sync(0xffffffffu, nlit, 0);
-    lit_at = __shfl_sync(0xffffffffu, lit_at, 0);
+    if (bad || nlit > n - ip || nlit > raw - op) break;
+    const unsigned lit_at = ip;
+    ip += nlit;
     for (unsigned i = lane; i < nlit; i += 32) out[op + i] = __ldg(in + lit_at + i);
     op += nlit;
-    if (state == 1) return;
-    off = __shfl_sync(0xffffffffu, off, 0);
-    mlen = __shfl_sync(0xffffffffu, mlen, 0);
-    ip = __shfl_sync(0xffffffffu, ip, 0);
+    if (ip == n) {
+      if (op == raw) return;  // the last sequence: done
+      break;
+    }
+    if (n - ip < 2) break;
+    const unsigned off = byte_at(ip) | (byte_at(ip + 1) << 8);
+    ip += 2;
+    unsigned mlen = token & 15;
+    if (mlen == 15) {
+      unsigned b = 255;
+      while (b == 255) {
+        if (ip >= n) { bad = true; break; }
+        b = byte_at(ip++);
+        mlen += b;
+      }
+    }
+    mlen += 4;
+    if (bad || off == 0 || off > op || mlen > raw - op) break;
     __syncwarp();
     if (off >= 32) {
       for (unsigned base = 0; base < mlen; base += 32) {
@@ -1052,6 +1043,7 @@ __global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restr
     }
     op += mlen;
   }
+  if (lane == 0) atomicOr(err, 1);
 }
 
 cudaError_t launch_lz4_decode(const void* stage, void* pool, const Lz4Chunk* chunks, int nchunks, int* err,

@@ -1736,12 +1736,25 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
     }
     CUDA_TRY(ds.d_stage.alloc(std::max<size_t>(total, 16)));
     CUDA_TRY(ds.d_chunks.alloc(sizeof(Lz4Chunk) * jobs.size()));
-    size_t at = 0;
+    // bricks page in index order and the store holds them in build order, so
+    // runs of consecutive bricks are adjacent: one copy per adjacent stretch
+    size_t at = 0, cp_at = 0, cp_n = 0;
+    const uint8_t* cp_src = nullptr;
     for (size_t q = 0; q < paged.size(); ++q) {
-      CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + at, ds.comp_run(paged[q].first), run[q], cudaMemcpyHostToDevice,
-                               r->copy_stream));
+      const uint8_t* h = ds.comp_run(paged[q].first);
+      if (cp_n && h == cp_src + cp_n) {
+        cp_n += run[q];
+      } else {
+        if (cp_n)
+          CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + cp_at, cp_src, cp_n, cudaMemcpyHostToDevice, r->copy_stream));
+        cp_src = h;
+        cp_at = at;
+        cp_n = run[q];
+      }
       at += run[q];
     }
+    if (cp_n)
+      CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + cp_at, cp_src, cp_n, cudaMemcpyHostToDevice, r->copy_stream));
     // pageable source: the copy returns once it is staged
     CUDA_TRY(cudaMemcpyAsync(ds.d_chunks.p, jobs.data(), sizeof(Lz4Chunk) * jobs.size(), cudaMemcpyHostToDevice,
                              r->copy_stream));

@@ -1538,6 +1538,66 @@ struct PtrSnapshot {
   bool operator!=(const PtrSnapshot& o) const { return memcmp(p, o.p, sizeof(p)) != 0; }
 };
 
+// Out of core, compressed store: the compressed runs of the paged bricks
+// (brick, slot) to the device staging, then one decode of all their chunks
+// into the slots, both on the copy stream.  comp_bytes: bytes copied.
+int page_compressed(gbvr_renderer* r, const std::vector<std::pair<int, int>>& paged, uint64_t& comp_bytes) {
+  Dataset& ds = r->ds;
+  const size_t es = dtype_size(ds.dtype);
+  // compressed runs to the device staging, then one decode of all their
+  // chunks into the slots (both on the copy stream)
+  std::vector<Lz4Chunk> jobs;
+  std::vector<size_t> run(paged.size());
+  size_t total = 0;
+  for (size_t q = 0; q < paged.size(); ++q) {
+    const int bidx = paged[q].first;
+    const BrickInfo& b = ds.bricks[bidx];
+    const size_t nbytes = (size_t)b.sx * b.sy * b.sz * es;
+    const unsigned c0 = ds.chunk_first[bidx], nc = (unsigned)((nbytes + LZ_CHUNK - 1) / LZ_CHUNK);
+    size_t cb = 0;
+    for (unsigned k = 0; k < nc; ++k) {
+      const unsigned cs = ds.chunk_size[c0 + k];
+      Lz4Chunk ch;
+      ch.src = total + cb;
+      ch.dst = (unsigned long long)paged[q].second * ds.slot_elems * es + (unsigned long long)k * LZ_CHUNK;
+      ch.comp = cs;
+      ch.raw = (unsigned)std::min(LZ_CHUNK, nbytes - (size_t)k * LZ_CHUNK);
+      jobs.push_back(ch);
+      cb += cs & 0x7fffffffu;
+    }
+    run[q] = cb;
+    total += cb;
+  }
+  CUDA_TRY(ds.d_stage.alloc(std::max<size_t>(total, 16)));
+  CUDA_TRY(ds.d_chunks.alloc(sizeof(Lz4Chunk) * jobs.size()));
+  // bricks page in index order and the store holds them in build order, so
+  // runs of consecutive bricks are adjacent: one copy per adjacent stretch
+  size_t at = 0, cp_at = 0, cp_n = 0;
+  const uint8_t* cp_src = nullptr;
+  for (size_t q = 0; q < paged.size(); ++q) {
+    const uint8_t* h = ds.comp_run(paged[q].first);
+    if (cp_n && h == cp_src + cp_n) {
+      cp_n += run[q];
+    } else {
+      if (cp_n)
+        CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + cp_at, cp_src, cp_n, cudaMemcpyHostToDevice, r->copy_stream));
+      cp_src = h;
+      cp_at = at;
+      cp_n = run[q];
+    }
+    at += run[q];
+  }
+  if (cp_n)
+    CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + cp_at, cp_src, cp_n, cudaMemcpyHostToDevice, r->copy_stream));
+  // pageable source: the copy returns once it is staged
+  CUDA_TRY(cudaMemcpyAsync(ds.d_chunks.p, jobs.data(), sizeof(Lz4Chunk) * jobs.size(), cudaMemcpyHostToDevice,
+                           r->copy_stream));
+  CUDA_TRY(launch_lz4_decode(ds.d_stage.p, ds.pool.p, ds.d_chunks.as<Lz4Chunk>(), (int)jobs.size(),
+                             ds.d_lz_err.as<int>(), r->copy_stream));
+  comp_bytes = total;
+  return GBVR_OK;
+}
+
 // Out-of-core paging for the views of one paint: pick the finest level (from
 // the LOD limit down) whose bricks that may contribute and intersect a view
 // frustum fit the device slots, upload the missing ones on the copy stream
@@ -1710,57 +1770,19 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
   }
   uint64_t comp_bytes = 0;
   if (!paged.empty()) {
-    // compressed runs to the device staging, then one decode of all their
-    // chunks into the slots (both on the copy stream)
-    std::vector<Lz4Chunk> jobs;
-    std::vector<size_t> run(paged.size());
-    size_t total = 0;
-    for (size_t q = 0; q < paged.size(); ++q) {
-      const int bidx = paged[q].first;
-      const BrickInfo& b = ds.bricks[bidx];
-      const size_t nbytes = (size_t)b.sx * b.sy * b.sz * es;
-      const unsigned c0 = ds.chunk_first[bidx], nc = (unsigned)((nbytes + LZ_CHUNK - 1) / LZ_CHUNK);
-      size_t cb = 0;
-      for (unsigned k = 0; k < nc; ++k) {
-        const unsigned cs = ds.chunk_size[c0 + k];
-        Lz4Chunk ch;
-        ch.src = total + cb;
-        ch.dst = (unsigned long long)paged[q].second * ds.slot_elems * es + (unsigned long long)k * LZ_CHUNK;
-        ch.comp = cs;
-        ch.raw = (unsigned)std::min(LZ_CHUNK, nbytes - (size_t)k * LZ_CHUNK);
-        jobs.push_back(ch);
-        cb += cs & 0x7fffffffu;
+    // a failure below leaves these bricks undecoded: they go back to not
+    // resident (their slots free), so a later paint pages them again
+    auto rollback = [&]() {
+      for (const auto& pr : paged) {
+        ds.slot_of[pr.first] = -1;
+        ds.slot_brick[pr.second] = -1;
       }
-      run[q] = cb;
-      total += cb;
+    };
+    const int rc = page_compressed(r, paged, comp_bytes);
+    if (rc != GBVR_OK) {
+      rollback();
+      return rc;
     }
-    CUDA_TRY(ds.d_stage.alloc(std::max<size_t>(total, 16)));
-    CUDA_TRY(ds.d_chunks.alloc(sizeof(Lz4Chunk) * jobs.size()));
-    // bricks page in index order and the store holds them in build order, so
-    // runs of consecutive bricks are adjacent: one copy per adjacent stretch
-    size_t at = 0, cp_at = 0, cp_n = 0;
-    const uint8_t* cp_src = nullptr;
-    for (size_t q = 0; q < paged.size(); ++q) {
-      const uint8_t* h = ds.comp_run(paged[q].first);
-      if (cp_n && h == cp_src + cp_n) {
-        cp_n += run[q];
-      } else {
-        if (cp_n)
-          CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + cp_at, cp_src, cp_n, cudaMemcpyHostToDevice, r->copy_stream));
-        cp_src = h;
-        cp_at = at;
-        cp_n = run[q];
-      }
-      at += run[q];
-    }
-    if (cp_n)
-      CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + cp_at, cp_src, cp_n, cudaMemcpyHostToDevice, r->copy_stream));
-    // pageable source: the copy returns once it is staged
-    CUDA_TRY(cudaMemcpyAsync(ds.d_chunks.p, jobs.data(), sizeof(Lz4Chunk) * jobs.size(), cudaMemcpyHostToDevice,
-                             r->copy_stream));
-    CUDA_TRY(launch_lz4_decode(ds.d_stage.p, ds.pool.p, ds.d_chunks.as<Lz4Chunk>(), (int)jobs.size(),
-                               ds.d_lz_err.as<int>(), r->copy_stream));
-    comp_bytes = total;
   }
   r->last_paged_comp += comp_bytes;
   CUDA_TRY(cudaEventRecord(r->ev_c1[stage], r->copy_stream));

@@ -1003,10 +1003,9 @@ __global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restr
     if (bad || nlit > n - ip || nlit > raw - op) break;
     const unsigned lit_at = ip;
     ip += nlit;
-    for (unsigned i = lane; i < nlit; i += 32) out[op + i] = __ldg(in + lit_at + i);
-    op += nlit;
     if (ip == n) {
-      if (op == raw) return;  // the last sequence: done
+      for (unsigned i = lane; i < nlit; i += 32) out[op + i] = __ldg(in + lit_at + i);
+      if (op + nlit == raw) return;  // the last sequence: done
       break;
     }
     if (n - ip < 2) break;
@@ -1022,7 +1021,38 @@ __global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restr
       }
     }
     mlen += 4;
-    if (bad || off == 0 || off > op || mlen > raw - op) break;
+    if (bad || off == 0 || off > op + nlit || mlen > raw - op - nlit) break;
+    if (nlit + mlen <= 32) {
+      // the whole sequence in one step: lane j writes its byte j.  A match
+      // byte's source, nlit - off + ((j - nlit) mod off), lies before the
+      // match: a literal of this step (taken from its lane) or earlier
+      // output (in memory, ordered by the last __syncwarp).
+      const unsigned j = lane;
+      const unsigned lit = j < nlit ? (unsigned)__ldg(in + lit_at + j) : 0u;
+      int src = 0;
+      if (j >= nlit) {
+        int d = (int)(j - nlit);
+        if (d >= (int)off) {
+          // d mod off for d, off < 32: a float quotient within one of the
+          // exact one, then settled
+          const int q = (int)((float)d * __frcp_rn((float)off));
+          d -= q * (int)off;
+          if (d < 0) d += (int)off;
+          else if (d >= (int)off) d -= (int)off;
+        }
+        src = (int)nlit - (int)off + d;
+      }
+      const unsigned from_lane = __shfl_sync(0xffffffffu, lit, src > 0 ? src : 0);
+      if (j < nlit + mlen) {
+        const unsigned v = j < nlit ? lit : (src >= 0 ? from_lane : (unsigned)out[(int)op + src]);
+        out[op + j] = (unsigned char)v;
+      }
+      op += nlit + mlen;
+      __syncwarp();
+      continue;
+    }
+    for (unsigned i = lane; i < nlit; i += 32) out[op + i] = __ldg(in + lit_at + i);
+    op += nlit;
     __syncwarp();
     if (off >= 32) {
       for (unsigned base = 0; base < mlen; base += 32) {

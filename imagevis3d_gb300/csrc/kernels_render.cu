@@ -1,7 +1,8 @@
 // Raycasting kernels: ray setup, bricked front-to-back walk with empty-brick
-// skipping, SW or texture trilinear sampling, 1D / 2D transfer functions with
-// opacity correction, FP32 compositing with early ray termination, and the
-// isosurface first-hit mode with central-difference Phong shading.
+// and macro-cell skipping, SW or texture trilinear sampling, 1D / 2D transfer
+// functions with opacity correction, FP32 compositing with early ray
+// termination, the isosurface first-hit mode with central-difference Phong
+// shading, maximum-intensity projection, and a clip plane.
 //
 // Replaces the fragment-shader raycaster behind Tuvok's AbstrRenderer::Paint
 // (reached from LuaScripts/BatchRenderer.lua:35 `renderer.paint()` and
@@ -13,12 +14,19 @@
 // C += (1 - A) alpha' c, A += (1 - A) alpha', stop at A >= ert, background
 // composited last.
 //
-// One warp renders one 8x4 ray tile.  Two launch forms share render_tile():
-//   k_render_plain        one launch per view, one warp per tile (the drop-in
-//                         per-view form of AbstrRenderer::Paint)
-//   k_render_persistent   grid = SMs x resident CTAs; warps pull (view, tile)
-//                         items from one atomic counter spanning every view
-//                         of the batch, so views and uneven rays share the GPU.
+// One warp renders one 8x4 ray tile.  Launch forms sharing march():
+//   k_render_plain          one launch per view, one warp per tile (the drop-in
+//                           per-view form of AbstrRenderer::Paint)
+//   k_render_persistent     grid = SMs x resident CTAs; warps pull (view, tile)
+//                           items from one atomic counter spanning every view
+//                           of the batch, so views and uneven rays share the GPU
+//   k_render_persistent_u   the same for batches whose views share all but the
+//                           camera: the shared descriptor is a kernel parameter
+// Around them: the background outside each view's projected volume
+// rectangle (k_fill_outside), bounding-box lines (k_raster_lines,
+// k_line_stops, k_render_lines: FP64 coverage, covered rays re-rendered),
+// the ClearView lens pass (k_render_cv), 2D slice views (k_render_slice) and
+// TF classification of bricks and macro-cells.
 #include <algorithm>
 
 #include "gbvr_internal.h"

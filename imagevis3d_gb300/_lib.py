@@ -137,6 +137,8 @@ SIGNATURES = {
     "gbvr_set_render_mode": [P, I],
     "gbvr_set_clip_plane": [P, I, FP],
     "gbvr_set_bboxes": [P, I, I, FP, FP],
+    "gbvr_set_iso_relative": [P, F, FP],
+    "gbvr_set_blend_precision": [P, I],
     "gbvr_lz4_bound": [SZ],
     "gbvr_lz4_compress": [P, SZ, P, SZ],
     "gbvr_lz4_decompress": [P, SZ, P, SZ],

@@ -2656,6 +2656,20 @@ int gbvr_set_iso(gbvr_renderer* r, float value, const float rgb[3]) {
   return GBVR_OK;
 }
 
+int gbvr_set_iso_relative(gbvr_renderer* r, float fraction, const float rgb[3]) {
+  TRY(check_loaded(r));
+  double lo, hi;
+  default_range(r, lo, hi);
+  const float f = std::min(std::max(fraction, 0.f), 1.f);
+  return gbvr_set_iso(r, f * (float)(long long)hi, rgb);
+}
+
+int gbvr_set_blend_precision(gbvr_renderer* r, int bits) {
+  TRY(check_r(r));
+  if (bits != 8 && bits != 16 && bits != 32) return fail(GBVR_EINVAL, "blend precision must be 8, 16 or 32 bits");
+  return GBVR_OK;  // compositing is FP32 for every setting
+}
+
 int gbvr_set_lighting(gbvr_renderer* r, int enabled, const float amb[4], const float diff[4], const float spec[4],
                       const float dir[3]) {
   TRY(check_r(r));

@@ -333,6 +333,17 @@ class Renderer:
             arr, c = _fp(rgb)
         L.call("gbvr_set_iso", self._h, value, c)
 
+    def setIsoValueRelative(self, fraction, rgb=None):
+        """setIsoValueRelative: the isovalue as a fraction of the value range's top."""
+        c = None
+        if rgb is not None:
+            arr, c = _fp(rgb)
+        L.call("gbvr_set_iso_relative", self._h, fraction, c)
+
+    def setBlendPrecision(self, bits):
+        """setBlendPrecision (8, 16 or 32): compositing stays FP32."""
+        L.call("gbvr_set_blend_precision", self._h, bits)
+
     def setLightColors(self, ambient, diffuse, specular, direction, enabled=True):
         a, pa = _fp(ambient)
         d, pd = _fp(diffuse)

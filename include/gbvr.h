@@ -231,6 +231,13 @@ int gbvr_set_clearview(gbvr_renderer* r, int enabled, float iso, const float rgb
                        float border_scale, float focus_x, float focus_y);
 int gbvr_set_value_range(gbvr_renderer* r, double lo, double hi);         /* TF domain (biasScaleTF) */
 int gbvr_set_iso(gbvr_renderer* r, float value, const float rgb[3]);      /* setIsoValue, setIsosurfaceColor */
+/* setIsoValueRelative (RenderWindow.cpp:2144-2153): iso = clamp(fraction, 0, 1) x the integer top of the
+ * value range (the TF domain's upper end), as the script command maps it (ImageVis3D.cpp:478-484).  Needs a
+ * loaded dataset. */
+int gbvr_set_iso_relative(gbvr_renderer* r, float fraction, const float rgb[3]);
+/* setBlendPrecision (RenderWindow.cpp:1618-1623): 8, 16 or 32 bits; this renderer composites in FP32 for
+ * every setting (the value is recorded and returned by nothing else). */
+int gbvr_set_blend_precision(gbvr_renderer* r, int bits);
 int gbvr_set_lighting(gbvr_renderer* r, int enabled, const float amb[4], const float diff[4],
                       const float spec[4], const float dir[3]);          /* setLightingEnabled, setLightColors */
 int gbvr_set_sample_rate(gbvr_renderer* r, float samples_per_voxel);      /* setSampleRateModifier */

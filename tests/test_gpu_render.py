@@ -210,6 +210,34 @@ def test_isosurface_matches_oracle(orc, multibrick, iso):
     assert hit_r.mean() > 0.003
 
 
+def test_relative_isovalue_and_blend_precision(multibrick):
+    """setIsoValueRelative(f) renders as setIsoValue(clamp(f, 0, 1) x the
+    range top); every blend precision composites the same FP32 image."""
+    vol, _, _ = multibrick
+    top_value = float(vol.max())  # the range top: the histogram's last non-empty bin
+    view, proj = orbit_camera(120.0, 10.0, 2.5 * workloads.DIAG, 45.0, 96, 72)
+    with Renderer() as r:
+        r.loadVolume(vol, brick_size=64, overlap=2)
+        r.resize((96, 72))
+        r.setRenderMode(GBVR_RM_ISOSURFACE)
+        r.setIsoValue(float(np.float32(0.3) * np.float32(top_value)))
+        absolute = gpu_render(r, view, proj)
+        r.setIsoValueRelative(0.3)
+        relative = gpu_render(r, view, proj)
+        r.setIsoValueRelative(1.7)
+        clamped = gpu_render(r, view, proj)
+        r.setIsoValue(top_value)
+        top = gpu_render(r, view, proj)
+        for bits in (8, 16, 32):
+            r.setBlendPrecision(bits)
+            assert np.array_equal(gpu_render(r, view, proj), top)
+        with pytest.raises(GbvrError):
+            r.setBlendPrecision(12)
+    assert np.array_equal(relative, absolute)
+    assert np.array_equal(clamped, top)
+    assert (absolute[..., 3] > 0.5).mean() > 0.003
+
+
 def test_texture_sampler_matches_oracle(orc, multibrick):
     vol, _, tf = multibrick
     view, proj = orbit_camera(35.0, 20.0, 2.5 * workloads.DIAG, 45.0, 200, 150)

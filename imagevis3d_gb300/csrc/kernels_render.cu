@@ -495,6 +495,24 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
     int K = max(0, (int)ceilf((r.t1 - t0) / dt - 0.5f));
     const float V[3] = {-r.dw[0], -r.dw[1], -r.dw[2]};
     const float inv_dt = 1.f / dt;
+    // Crossing of the plane x_i = p, in sample-index units: the k with
+    // t_k = (p - ov_i) / dv_i, i.e. fma(p, ka_i, kb_i) (the -1/2 of the
+    // sample centres included).  Per axis the ray leaves a box through its
+    // upper plane when dv_i > 0 and its lower plane otherwise; an axis the ray
+    // runs parallel to gives +inf.
+    float ka[3], kb[3];
+    {
+      const float kt = fmaf(t0, inv_dt, 0.5f);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const bool par = !(fabsf(r.dv[i]) > 1e-30f);
+        ka[i] = par ? 0.f : r.inv[i] * inv_dt;
+        kb[i] = par ? INFINITY : -fmaf(r.ov[i], ka[i], kt);
+      }
+    }
+    auto exit_k = [&](int ex, int ey, int ez) {
+      return fminf(fminf(fmaf((float)ex, ka[0], kb[0]), fmaf((float)ey, ka[1], kb[1])), fmaf((float)ez, ka[2], kb[2]));
+    };
     auto pos_of = [&](int kk, float& px, float& py, float& pz) {
       const float t = fmaf((float)kk + 0.5f, dt, t0);
       px = fmaf(t, r.dv[0], r.ov[0]);
@@ -507,14 +525,7 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
     // samples to bricks and cells.  Positions are monotone in k, so members
     // form one run and only its ends need checking.
     auto run_end = [&](int k0, int lx, int ly, int lz, int hx, int hy, int hz) -> int {
-      float te = INFINITY;
-      te = fminf(te, r.dv[0] > 0.f ? ((float)hx - r.ov[0]) * r.inv[0]
-                                   : (r.dv[0] < 0.f ? ((float)lx - r.ov[0]) * r.inv[0] : INFINITY));
-      te = fminf(te, r.dv[1] > 0.f ? ((float)hy - r.ov[1]) * r.inv[1]
-                                   : (r.dv[1] < 0.f ? ((float)ly - r.ov[1]) * r.inv[1] : INFINITY));
-      te = fminf(te, r.dv[2] > 0.f ? ((float)hz - r.ov[2]) * r.inv[2]
-                                   : (r.dv[2] < 0.f ? ((float)lz - r.ov[2]) * r.inv[2] : INFINITY));
-      const float kef = ceilf((te - t0) * inv_dt - 0.5f);
+      const float kef = ceilf(exit_k(r.dv[0] > 0.f ? hx : lx, r.dv[1] > 0.f ? hy : ly, r.dv[2] > 0.f ? hz : lz));
       int ke = kef >= (float)K ? K : max(k0 + 1, (int)kef);
       auto in_box = [&](int kk) {
         float qx, qy, qz;
@@ -595,13 +606,9 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
         if constexpr (MODE == MODE_MIP) d = __ldg(&f.cells[ci].y) <= runmax ? 1 : 0;  // one cell at a time
         else d = __ldg(f.occ + ci);
         const int lo_c = d > 0 ? d - 1 : 0;  // cube = cells [c - lo_c, c + lo_c]
-        const float lx = (float)(max(cx - lo_c, 0) << sh), hx = (float)min((cx + lo_c + 1) << sh, f.dims[0]);
-        const float ly = (float)(max(cy - lo_c, 0) << sh), hy = (float)min((cy + lo_c + 1) << sh, f.dims[1]);
-        const float lz = (float)(max(cz - lo_c, 0) << sh), hz = (float)min((cz + lo_c + 1) << sh, f.dims[2]);
-        float te = fminf(fminf(r.dv[0] > 0.f ? (hx - r.ov[0]) * r.inv[0] : (r.dv[0] < 0.f ? (lx - r.ov[0]) * r.inv[0] : INFINITY),
-                               r.dv[1] > 0.f ? (hy - r.ov[1]) * r.inv[1] : (r.dv[1] < 0.f ? (ly - r.ov[1]) * r.inv[1] : INFINITY)),
-                         r.dv[2] > 0.f ? (hz - r.ov[2]) * r.inv[2] : (r.dv[2] < 0.f ? (lz - r.ov[2]) * r.inv[2] : INFINITY));
-        const float kef = ceilf((te - t0) * inv_dt - 0.5f);
+        const float kef = ceilf(exit_k(r.dv[0] > 0.f ? min((cx + lo_c + 1) << sh, f.dims[0]) : max(cx - lo_c, 0) << sh,
+                                       r.dv[1] > 0.f ? min((cy + lo_c + 1) << sh, f.dims[1]) : max(cy - lo_c, 0) << sh,
+                                       r.dv[2] > 0.f ? min((cz + lo_c + 1) << sh, f.dims[2]) : max(cz - lo_c, 0) << sh));
         if (d > 0) {
           k = kef >= (float)K ? K : max(k + 1, (int)kef);
           if (k >= bke) bi = -1;

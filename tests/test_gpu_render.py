@@ -216,7 +216,7 @@ def test_relative_isovalue_and_blend_precision(multibrick):
     vol, _, _ = multibrick
     top_value = float(vol.max())  # the range top: the histogram's last non-empty bin
     view, proj = orbit_camera(120.0, 10.0, 2.5 * workloads.DIAG, 45.0, 96, 72)
-    with Renderer() as r:
+    with Renderer(float_fb=True) as r:
         r.loadVolume(vol, brick_size=64, overlap=2)
         r.resize((96, 72))
         r.setRenderMode(GBVR_RM_ISOSURFACE)

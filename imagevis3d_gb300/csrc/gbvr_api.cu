@@ -1216,6 +1216,21 @@ void default_range(gbvr_renderer* r, double& lo, double& hi) {
 }
 
 // Default TF: a linear ramp, as a freshly opened dataset gets in the reference.
+// The device form of a 1D TF of w RGBA entries: per entry the entry and its
+// FP32 difference to the next one (zero for the last), read by the kernels'
+// tf1d.
+std::vector<float> tf1d_pairs(const float* rgba, int w) {
+  std::vector<float> out(8 * (size_t)w);
+  for (int i = 0; i < w; ++i) {
+    const int j = std::min(i + 1, w - 1);
+    for (int c = 0; c < 4; ++c) {
+      out[8 * (size_t)i + c] = rgba[4 * (size_t)i + c];
+      out[8 * (size_t)i + 4 + c] = rgba[4 * (size_t)j + c] - rgba[4 * (size_t)i + c];
+    }
+  }
+  return out;
+}
+
 void ensure_tf(gbvr_renderer* r) {
   if (r->tf1d.empty()) {
     int n = r->ds.hist1d.empty() ? 256 : (int)std::min<size_t>(r->ds.hist1d.size(), 4096);
@@ -1241,8 +1256,10 @@ int upload_tf(gbvr_renderer* r, int level) {
   if (two && r->tf2d.empty()) return fail(GBVR_ESTATE, "2D transfer function not set");
   const std::vector<float>& tf = two ? r->tf2d : r->tf1d;
   if (r->tf_dirty) {
-    CUDA_TRY(r->d_tf.alloc(sizeof(float) * tf.size()));
-    CUDA_TRY(cudaMemcpyAsync(r->d_tf.p, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice, r->stream));
+    // pageable sources: each copy returns once it is staged
+    const std::vector<float> dev = two ? tf : tf1d_pairs(tf.data(), (int)(tf.size() / 4));
+    CUDA_TRY(r->d_tf.alloc(sizeof(float) * dev.size()));
+    CUDA_TRY(cudaMemcpyAsync(r->d_tf.p, dev.data(), sizeof(float) * dev.size(), cudaMemcpyHostToDevice, r->stream));
     if (two) {
       const int w = r->tf2d_w, h = r->tf2d_h;
       std::vector<unsigned char> live((size_t)w, 0);
@@ -1962,8 +1979,9 @@ int paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_
     TRY(rc);
   }
   ensure_tf(r);
-  CUDA_TRY(r->d_tf_slice.alloc(sizeof(float) * r->tf1d.size()));
-  CUDA_TRY(cudaMemcpyAsync(r->d_tf_slice.p, r->tf1d.data(), sizeof(float) * r->tf1d.size(), cudaMemcpyHostToDevice,
+  const std::vector<float> slice_tf = tf1d_pairs(r->tf1d.data(), (int)(r->tf1d.size() / 4));
+  CUDA_TRY(r->d_tf_slice.alloc(sizeof(float) * slice_tf.size()));
+  CUDA_TRY(cudaMemcpyAsync(r->d_tf_slice.p, slice_tf.data(), sizeof(float) * slice_tf.size(), cudaMemcpyHostToDevice,
                            r->stream));
   float dv[16], dp[16];
   default_camera(r, dv, dp);
@@ -3540,8 +3558,9 @@ int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba,
     t->lo = 0;
     t->hi = std::max(1.0, (double)((long long)ds.hist1d.size() * ds.merge - 1));
   }
-  CUDA_TRY(t->d_tf.alloc(sizeof(float) * t->host.size()));
-  CUDA_TRY(cudaMemcpyAsync(t->d_tf.p, t->host.data(), sizeof(float) * t->host.size(), cudaMemcpyHostToDevice, s->stream));
+  const std::vector<float> dev = mode == GBVR_RM_2DTRANS ? t->host : tf1d_pairs(t->host.data(), w);
+  CUDA_TRY(t->d_tf.alloc(sizeof(float) * dev.size()));
+  CUDA_TRY(cudaMemcpyAsync(t->d_tf.p, dev.data(), sizeof(float) * dev.size(), cudaMemcpyHostToDevice, s->stream));
   TRY(classify_level(ds, t->level, t->host, w, h, mode, t->lo, t->hi, t->iso, t->d_prefix, t->d_skip, t->d_occ,
                      t->d_occtmp, s->stream));
   std::lock_guard<std::mutex> lk(s->mu);

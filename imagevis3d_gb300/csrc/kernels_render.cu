@@ -325,15 +325,16 @@ __device__ __forceinline__ void shade(const FrameDesc& f, const float* L, const 
   for (int k = 0; k < 3; ++k) out[k] = col[k] * (f.amb[k] + f.diff[k] * nl) + f.spec[k] * sp;
 }
 
+// A 1D TF lives on the device as pairs (entry i, entry min(i + 1, w - 1) -
+// entry i), the difference taken in FP32 on the host: the lerp reads one
+// 32-byte pair and gives exactly a + fr (b - a) as computed here.
 __device__ __forceinline__ float4 tf1d(const FrameDesc& f, float v) {
   float idx = fminf(fmaxf((v - f.value_lo) * f.idx_scale, 0.f), (float)(f.tf_w - 1));
   float i0f = floorf(idx);
-  int i0 = (int)i0f;
-  int i1 = min(i0 + 1, f.tf_w - 1);
   float fr = idx - i0f;
-  float4 a = __ldg(f.tf + i0), b = __ldg(f.tf + i1);
-  return make_float4(fmaf(fr, b.x - a.x, a.x), fmaf(fr, b.y - a.y, a.y), fmaf(fr, b.z - a.z, a.z),
-                     fmaf(fr, b.w - a.w, a.w));
+  const float4* p = f.tf + 2 * (int)i0f;
+  float4 a = __ldg(p), d = __ldg(p + 1);
+  return make_float4(fmaf(fr, d.x, a.x), fmaf(fr, d.y, a.y), fmaf(fr, d.z, a.z), fmaf(fr, d.w, a.w));
 }
 
 __device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {

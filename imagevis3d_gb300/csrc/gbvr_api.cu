@@ -208,7 +208,19 @@ struct Level {
   int nc[3];                          // macro-cell grid
   int cell_shift = 2;                 // macro-cell edge = 1 << cell_shift voxels
   std::shared_ptr<DevBuf> cells;      // float2 min/max per macro-cell
+  int nsc[3] = {0, 0, 0};             // super-cell grid (4^3 macro-cells each)
+  std::shared_ptr<DevBuf> smax;       // float: largest cell maximum per super-cell (MIP skipping)
 };
+
+// The super-cell maxima of a level whose macro-cell min/max is complete.
+int build_supercells(Level& L, cudaStream_t s) {
+  constexpr int E = 1 << SUPERCELL_SHIFT;
+  for (int a = 0; a < 3; ++a) L.nsc[a] = (L.nc[a] + E - 1) / E;
+  L.smax = std::make_shared<DevBuf>();
+  CUDA_TRY(L.smax->alloc(sizeof(float) * (size_t)L.nsc[0] * L.nsc[1] * L.nsc[2]));
+  CUDA_TRY(launch_supercell_max(L.cells->as<float2>(), L.nc, L.smax->as<float>(), L.nsc, s));
+  return GBVR_OK;
+}
 
 // macro-cell edge (voxels) for empty-space skipping inside bricks, and the
 // cap of the empty-cell distance field
@@ -451,6 +463,7 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
     L.cells = std::make_shared<DevBuf>();
     CUDA_TRY(L.cells->alloc(sizeof(float2) * (size_t)L.nc[0] * L.nc[1] * L.nc[2]));
     CUDA_TRY(launch_cell_minmax(lv[l]->p, dtype, d, CELL_SHIFT, L.nc, L.cells->as<float2>(), s));
+    TRY(build_supercells(L, s));
     for (int c = 0; c < (ds.layouts == 4 ? 2 : ds.layouts); ++c) {
       const int perm = (ds.layouts == 4 && c == 1) ? 3 : c;
       CUDA_TRY(launch_gather_bricks(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks,
@@ -839,6 +852,7 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
     ds.bit_width = 32;
     ds.max_grad = 0.f;
   }
+  for (Level& L : ds.levels) TRY(build_supercells(L, s));
   ds.layouts = 1;
   ds.copy_stride = 0;
   ds.ooc = true;
@@ -1001,6 +1015,8 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
   for (int a = 0; a < 3; ++a) f.nc[a] = L.nc[a];
   f.cell_shift = L.cell_shift;
   f.cells = L.cells ? L.cells->as<float2>() : nullptr;
+  f.smax = L.smax ? L.smax->as<float>() : nullptr;
+  for (int a = 0; a < 3; ++a) f.nsc[a] = L.nsc[a];
   f.level_max = -INFINITY;
   for (int i = 0; i < L.nbricks; ++i) f.level_max = std::max(f.level_max, ds.bricks[L.brick_base + i].vmax);
   f.clip_on = p.clip_on;

@@ -92,6 +92,8 @@ struct __align__(16) FrameDesc {
   int nc[3];                 // macro-cell grid of the level
   int cell_shift;            // macro-cell edge = 1 << cell_shift voxels
   const float2* cells;       // MIP: per macro-cell min/max of the level (footprint + 1 voxel)
+  const float* smax;         // MIP: per super-cell (4^3 macro-cells) the largest cell maximum, or null
+  int nsc[3];                // super-cell grid
   float level_max;           // MIP: largest voxel of the level; no sample exceeds it
   int clip_on;               // clip plane: samples with clip . (x, y, z, 1) > 0 are dropped
   float clip[4];
@@ -269,6 +271,10 @@ cudaError_t launch_cell_minmax(const void* level, int dtype, const long long dim
 // layers' footprints must lie in the window)
 cudaError_t launch_cell_minmax_layers(const void* level, int dtype, const long long dims[3], long long vz0,
                                       int cell_shift, const int nc[3], int cz0, int cz1, float2* out, cudaStream_t s);
+// Super-cells of 4^3 macro-cells (clamped at the grid's end): the largest
+// cell maximum of each, out[(sz nsc1 + sy) nsc0 + sx].
+constexpr int SUPERCELL_SHIFT = 2;
+cudaError_t launch_supercell_max(const float2* cells, const int nc[3], float* out, const int nsc[3], cudaStream_t s);
 cudaError_t launch_hist1d(const void* vol, int dtype, long long n, unsigned long long* hist,
                           int nbins, cudaStream_t s);
 // 2D histogram passes; scratch holds the pass-1 reduction state.

@@ -396,6 +396,29 @@ cudaError_t launch_cell_minmax_layers(const void* level, int dtype, const long l
   return cudaGetLastError();
 }
 
+__global__ void k_supercell_max(const float2* __restrict__ cells, int ncx, int ncy, int ncz, float* __restrict__ out,
+                                int nsx, int nsy, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sx = (int)(i % nsx);
+  const long long t = i / nsx;
+  const int sy = (int)(t % nsy), sz = (int)(t / nsy);
+  constexpr int E = 1 << SUPERCELL_SHIFT;
+  float m = -INFINITY;
+  for (int z = sz * E; z < min(sz * E + E, ncz); ++z)
+    for (int y = sy * E; y < min(sy * E + E, ncy); ++y)
+      for (int x = sx * E; x < min(sx * E + E, ncx); ++x) m = fmaxf(m, cells[((size_t)z * ncy + y) * ncx + x].y);
+  out[i] = m;
+}
+
+cudaError_t launch_supercell_max(const float2* cells, const int nc[3], float* out, const int nsc[3], cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  const long long n = (long long)nsc[0] * nsc[1] * nsc[2];
+  if (n <= 0) return cudaSuccess;
+  k_supercell_max<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(cells, nc[0], nc[1], nc[2], out, nsc[0], nsc[1], n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cell_minmax(const void* level, int dtype, const long long dims[3], int sh, const int nc[3],
                                float2* out, cudaStream_t s) {
   return launch_cell_minmax_layers(level, dtype, dims, 0, sh, nc, 0, nc[2], out, s);

@@ -602,6 +602,23 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
         // contributing sample is ever skipped; sampling past a face is
         // harmless.
         const int cx = max(gx, 0) >> sh, cy = max(gy, 0) >> sh, cz = max(gz, 0) >> sh;
+        if constexpr (MODE == MODE_MIP) {
+          // a super-cell (4^3 macro-cells) whose largest cell maximum cannot
+          // raise the maximum is left through its exit face at once
+          if (f.smax) {
+            constexpr int SS = SUPERCELL_SHIFT;
+            const int sx = cx >> SS, sy = cy >> SS, sz = cz >> SS;
+            if (__ldg(f.smax + ((size_t)sz * f.nsc[1] + sy) * f.nsc[0] + sx) <= runmax) {
+              const int s2 = sh + SS;
+              const float kef = ceilf(exit_k(r.dv[0] > 0.f ? min((sx + 1) << s2, f.dims[0]) : sx << s2,
+                                             r.dv[1] > 0.f ? min((sy + 1) << s2, f.dims[1]) : sy << s2,
+                                             r.dv[2] > 0.f ? min((sz + 1) << s2, f.dims[2]) : sz << s2));
+              k = kef >= (float)K ? K : max(k + 1, (int)kef);
+              if (k >= bke) bi = -1;
+              continue;
+            }
+          }
+        }
         const size_t ci = ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx;
         int d;
         if constexpr (MODE == MODE_MIP) d = __ldg(&f.cells[ci].y) <= runmax ? 1 : 0;  // one cell at a time

@@ -66,6 +66,35 @@ def test_errors_without_gpu_are_statuses():
     assert rc == -1
 
 
+def test_renderer_calls_reject_a_null_handle():
+    """Every renderer call checks its handle before anything else: a null
+    renderer is GBVR_EINVAL with a message, and no CUDA call is made."""
+    lib = L.lib()
+    rgb = (C.c_float * 3)(1.0, 0.5, 0.25)
+    plane = (C.c_float * 4)(1.0, 0.0, 0.0, 0.0)
+    calls = [
+        ("gbvr_set_render_mode", (None, 0)),
+        ("gbvr_set_iso", (None, C.c_float(0.5), rgb)),
+        ("gbvr_set_iso_relative", (None, C.c_float(0.5), rgb)),
+        ("gbvr_set_blend_precision", (None, 32)),
+        ("gbvr_set_sample_rate", (None, C.c_float(1.0))),
+        ("gbvr_set_interpolant", (None, 1)),
+        ("gbvr_set_lod_limits", (None, 0, 4)),
+        ("gbvr_set_background", (None, rgb, rgb)),
+        ("gbvr_set_empty_skipping", (None, 2)),
+        ("gbvr_set_clip_plane", (None, 1, plane)),
+        ("gbvr_set_bboxes", (None, 1, 1, rgb, rgb)),
+        ("gbvr_set_clearview", (None, 1, C.c_float(0.5), rgb, C.c_float(0.5), C.c_float(1.0), C.c_float(1.0),
+                                C.c_float(0.0), C.c_float(0.0))),
+        ("gbvr_wait_read", (None, 0)),
+        ("gbvr_paint", (None,)),
+    ]
+    for name, args in calls:
+        rc = getattr(lib, name)(*args)
+        assert rc == -1, name
+        assert "null renderer" in L.last_error(), name
+
+
 def test_orbit_camera_is_host_math():
     v = np.zeros(16, np.float32)
     p = np.zeros(16, np.float32)

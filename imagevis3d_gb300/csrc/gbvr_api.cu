@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/gbvr.h"
+#include "abi_guard.h"
 #include "gbvr_internal.h"
 #include "lz4.h"
 #include "uvf.h"
@@ -2330,14 +2331,17 @@ void default_camera(gbvr_renderer* r, float view[16], float proj[16]) {
 extern "C" {
 
 int gbvr_last_error(char* buf, size_t size) {
+  GBVR_ABI_TRY
   if (!buf || size == 0) return GBVR_EINVAL;
   size_t n = std::min(size - 1, g_err.size());
   memcpy(buf, g_err.data(), n);
   buf[n] = 0;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes) {
+  GBVR_ABI_TRY
   int dev = 0;
   CUDA_TRY(cudaGetDevice(&dev));
   if (sm_count) CUDA_TRY(cudaDeviceGetAttribute(sm_count, cudaDevAttrMultiProcessorCount, dev));
@@ -2346,9 +2350,11 @@ int gbvr_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes) {
   if (free_bytes) *free_bytes = f;
   if (total_bytes) *total_bytes = t;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_create(int renderer_type, uint32_t flags, gbvr_renderer** out) {
+  GBVR_ABI_TRY
   if (!out) return fail(GBVR_EINVAL, "null output handle");
   *out = nullptr;
   if (renderer_type != GBVR_CUDA_RAYCASTER)
@@ -2365,16 +2371,20 @@ int gbvr_create(int renderer_type, uint32_t flags, gbvr_renderer** out) {
   CUDA_TRY(cudaEventCreate(&r->evk1));
   *out = r.release();
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_destroy(gbvr_renderer* r) {
+  GBVR_ABI_TRY
   if (!r) return GBVR_OK;
   if (r->stream) cudaStreamSynchronize(r->stream);
   delete r;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_load_volume(gbvr_renderer* r, const void* host, const int64_t dims[3], int dtype, const gbvr_brick_params* bp) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!host || !dims || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return fail(GBVR_EINVAL, "bad volume");
   if (dtype < 0 || dtype > 2) return fail(GBVR_EINVAL, "bad dtype");
@@ -2388,9 +2398,11 @@ int gbvr_load_volume(gbvr_renderer* r, const void* host, const int64_t dims[3], 
   r->tf_dirty = true;
   TRY(build_dataset(r->ds, lv, dtype, d, bp, r->stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_load_synthetic(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr_brick_params* bp) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   DevBuf lv;
   TRY(synth_to_device(p, lv, r->stream));
@@ -2400,9 +2412,11 @@ int gbvr_load_synthetic(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr
   long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
   TRY(build_dataset(r->ds, lv, p->dtype, d, bp, r->stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_synth_volume(const gbvr_synth_params* p, void* host_out, size_t bytes) {
+  GBVR_ABI_TRY
   if (!p || !host_out) return fail(GBVR_EINVAL, "null argument");
   const size_t need = (size_t)p->dims[0] * p->dims[1] * p->dims[2] * dtype_size(p->dtype);
   if (bytes < need) return fail(GBVR_EINVAL, "output buffer too small");
@@ -2433,6 +2447,7 @@ int gbvr_synth_volume(const gbvr_synth_params* p, void* host_out, size_t bytes) 
   CUDA_TRY(cudaMemcpyAsync(host_out, lv.p, need, cudaMemcpyDeviceToHost, tmp.stream));
   CUDA_TRY(cudaStreamSynchronize(tmp.stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 static int check_fbm(const gbvr_fbm_params* p) {
@@ -2444,6 +2459,7 @@ static int check_fbm(const gbvr_fbm_params* p) {
 }
 
 int gbvr_synth_fbm_volume(const gbvr_fbm_params* p, void* host_out, size_t bytes) {
+  GBVR_ABI_TRY
   TRY(check_fbm(p));
   if (!host_out) return fail(GBVR_EINVAL, "null output");
   const size_t need = (size_t)p->dims[0] * p->dims[1] * p->dims[2] * dtype_size(p->dtype);
@@ -2457,9 +2473,11 @@ int gbvr_synth_fbm_volume(const gbvr_fbm_params* p, void* host_out, size_t bytes
   CUDA_TRY(cudaMemcpyAsync(host_out, lv.p, need, cudaMemcpyDeviceToHost, tmp.stream));
   CUDA_TRY(cudaStreamSynchronize(tmp.stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_load_synthetic_fbm(gbvr_renderer* r, const gbvr_fbm_params* p, const gbvr_brick_params* bp) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   TRY(check_fbm(p));
   long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
@@ -2471,10 +2489,12 @@ int gbvr_load_synthetic_fbm(gbvr_renderer* r, const gbvr_fbm_params* p, const gb
   r->tf_dirty = true;
   TRY(build_dataset(r->ds, lv, p->dtype, d, bp, r->stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_load_synthetic_ooc(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr_brick_params* bp,
                             uint64_t device_pool_bytes) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!p || p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 || p->nblobs < 0)
     return fail(GBVR_EINVAL, "bad synthetic parameters");
@@ -2483,9 +2503,11 @@ int gbvr_load_synthetic_ooc(gbvr_renderer* r, const gbvr_synth_params* p, const 
   r->tf_dirty = true;
   TRY(build_ooc_synth(r->ds, p, bp, device_pool_bytes, r->stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_load_uvf(gbvr_renderer* r, const char* path, int verify, const gbvr_brick_params* bp) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!path) return fail(GBVR_EINVAL, "null path");
   UvfFile uf;
@@ -2515,9 +2537,11 @@ int gbvr_load_uvf(gbvr_renderer* r, const char* path, int verify, const gbvr_bri
   TRY(gbvr_load_volume(r, host.data(), dims, dtype, &p));
   r->ds.raster_id = ra.id;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_get_dataset_info(gbvr_renderer* r, gbvr_dataset_info* info) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   if (!info) return fail(GBVR_EINVAL, "null info");
   memset(info, 0, sizeof(*info));
@@ -2544,24 +2568,30 @@ int gbvr_get_dataset_info(gbvr_renderer* r, gbvr_dataset_info* info) {
   info->hist1d_size = (int)ds.hist1d.size();
   info->hist2d_max_grad = ds.max_grad;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_get_hist1d(gbvr_renderer* r, uint64_t* out, size_t n) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   if (!out || n < r->ds.hist1d.size()) return fail(GBVR_EINVAL, "histogram buffer too small");
   memcpy(out, r->ds.hist1d.data(), sizeof(uint64_t) * r->ds.hist1d.size());
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_get_hist2d(gbvr_renderer* r, uint64_t* out, size_t nx, size_t ny, float* max_grad) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   if (!out || nx * ny < r->ds.hist2d.size() || ny != 256) return fail(GBVR_EINVAL, "histogram buffer too small");
   memcpy(out, r->ds.hist2d.data(), sizeof(uint64_t) * r->ds.hist2d.size());
   if (max_grad) *max_grad = r->ds.max_grad;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_get_brick_minmax(gbvr_renderer* r, int lod, double* out, size_t nbricks) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   if (lod < 0 || lod >= (int)r->ds.levels.size()) return fail(GBVR_EINVAL, "bad lod");
   const Level& L = r->ds.levels[lod];
@@ -2571,10 +2601,12 @@ int gbvr_get_brick_minmax(gbvr_renderer* r, int lod, double* out, size_t nbricks
     out[2 * i + 1] = r->ds.bricks[L.brick_base + i].vmax;
   }
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_get_brick(gbvr_renderer* r, int lod, const int32_t brick[3], void* out, size_t bytes, int64_t origin[3],
                    int64_t stored_dims[3]) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   if (lod < 0 || lod >= (int)r->ds.levels.size() || !brick) return fail(GBVR_EINVAL, "bad lod");
   const Level& L = r->ds.levels[lod];
@@ -2606,38 +2638,48 @@ int gbvr_get_brick(gbvr_renderer* r, int lod, const int32_t brick[3], void* out,
   }
   CUDA_TRY(cudaMemcpy(out, (const char*)r->ds.pool.p + b.offset * es, need, cudaMemcpyDeviceToHost));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_resize(gbvr_renderer* r, int width, int height) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (width <= 0 || height <= 0 || width > 16384 || height > 16384) return fail(GBVR_EINVAL, "bad framebuffer size");
   r->width = width;
   r->height = height;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_render_mode(gbvr_renderer* r, int mode) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (mode < 0 || mode > 3) return fail(GBVR_EINVAL, "bad render mode");
   if (mode != r->mode) { r->tf_dirty = true; r->skip_dirty = true; }
   r->mode = mode;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod, uint64_t* misses,
                     uint64_t* bytes_paged) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   TRY(settle_async(r));
   return paint_path(r, views, n, lod, misses, bytes_paged);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_y, int use_mip) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   TRY(settle_async(r));
   return paint_slice(r, axis, index, flip_x, flip_y, use_mip);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_clip_plane(gbvr_renderer* r, int enabled, const float plane[4]) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (enabled) {
     if (!plane) return fail(GBVR_EINVAL, "null plane");
@@ -2648,18 +2690,22 @@ int gbvr_set_clip_plane(gbvr_renderer* r, int enabled, const float plane[4]) {
   r->clip_on = enabled ? 1 : 0;
   r->drop_graphs();
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_tf1d(gbvr_renderer* r, const float* rgba, int n) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!rgba || n < 2 || n > 65536) return fail(GBVR_EINVAL, "1D transfer function needs 2..65536 entries");
   r->tf1d.assign(rgba, rgba + 4 * (size_t)n);
   r->tf_dirty = true;
   r->skip_dirty = true;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_tf2d(gbvr_renderer* r, const float* rgba, int w, int h, float max_grad) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!rgba || w < 2 || h < 2 || w > 4096 || h > 4096) return fail(GBVR_EINVAL, "bad 2D transfer function size");
   r->tf2d.assign(rgba, rgba + 4 * (size_t)w * h);
@@ -2669,9 +2715,11 @@ int gbvr_set_tf2d(gbvr_renderer* r, const float* rgba, int w, int h, float max_g
   r->tf_dirty = true;
   r->skip_dirty = true;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_value_range(gbvr_renderer* r, double lo, double hi) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!(hi > lo)) return fail(GBVR_EINVAL, "value range must have hi > lo");
   r->range_set = true;
@@ -2679,33 +2727,41 @@ int gbvr_set_value_range(gbvr_renderer* r, double lo, double hi) {
   r->vhi = hi;
   r->skip_dirty = true;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_iso(gbvr_renderer* r, float value, const float rgb[3]) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   r->iso = value;
   r->iso_set = true;
   if (rgb) for (int k = 0; k < 3; ++k) r->iso_rgb[k] = rgb[k];
   r->skip_dirty = true;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_iso_relative(gbvr_renderer* r, float fraction, const float rgb[3]) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   double lo, hi;
   default_range(r, lo, hi);
   const float f = std::min(std::max(fraction, 0.f), 1.f);
   return gbvr_set_iso(r, f * (float)(long long)hi, rgb);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_blend_precision(gbvr_renderer* r, int bits) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (bits != 8 && bits != 16 && bits != 32) return fail(GBVR_EINVAL, "blend precision must be 8, 16 or 32 bits");
   return GBVR_OK;  // compositing is FP32 for every setting
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_lighting(gbvr_renderer* r, int enabled, const float amb[4], const float diff[4], const float spec[4],
                       const float dir[3]) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   r->lighting = enabled != 0;
   for (int k = 0; k < 3; ++k) {
@@ -2715,81 +2771,101 @@ int gbvr_set_lighting(gbvr_renderer* r, int enabled, const float amb[4], const f
     if (dir) r->light_dir[k] = dir[k];
   }
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_sample_rate(gbvr_renderer* r, float spv) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!(spv >= 0.05f && spv <= 64.f)) return fail(GBVR_EINVAL, "samples per voxel must be in [0.05, 64]");
   r->spv = spv;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_interpolant(gbvr_renderer* r, int interp) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (interp != GBVR_NEAREST && interp != GBVR_LINEAR) return fail(GBVR_EINVAL, "bad interpolant");
   r->interp = interp;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_sampler(gbvr_renderer* r, int sampler) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (sampler != GBVR_SAMPLER_SW && sampler != GBVR_SAMPLER_TEX) return fail(GBVR_EINVAL, "bad sampler");
   if (sampler == GBVR_SAMPLER_TEX && r->ds.loaded && (r->ds.texs.empty() || r->ds.ooc))
     return fail(GBVR_ESTATE, "dataset was loaded without build_texture");
   r->sampler = sampler;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_lod_limits(gbvr_renderer* r, int min_lod, int max_lod) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (min_lod < 0 || max_lod < min_lod) return fail(GBVR_EINVAL, "bad LOD limits");
   r->lod_min = min_lod;
   r->lod_max = max_lod;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_view(gbvr_renderer* r, const float view[16], const float proj[16]) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!view || !proj) return fail(GBVR_EINVAL, "null matrix");
   memcpy(r->view, view, sizeof(r->view));
   memcpy(r->proj, proj, sizeof(r->proj));
   r->view_set = true;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_background(gbvr_renderer* r, const float top[3], const float bottom[3]) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   for (int k = 0; k < 3; ++k) {
     if (top) r->bg_top[k] = top[k];
     if (bottom) r->bg_bot[k] = bottom[k];
   }
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_early_termination(gbvr_renderer* r, float alpha) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!(alpha > 0.f && alpha <= 1.0f)) return fail(GBVR_EINVAL, "termination alpha must be in (0, 1]");
   r->ert = alpha;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_launch_shape(gbvr_renderer* r, int tile_w, int ctas_per_sm) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (tile_w != 4 && tile_w != 8 && tile_w != 16 && tile_w != 32) return fail(GBVR_EINVAL, "tile_w must be 4, 8, 16 or 32");
   if (ctas_per_sm < 0 || ctas_per_sm > 64) return fail(GBVR_EINVAL, "bad ctas_per_sm");
   r->tile_w = tile_w;
   r->ctas_per_sm = ctas_per_sm;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_empty_skipping(gbvr_renderer* r, int mode) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (mode < 0 || mode > 2) return fail(GBVR_EINVAL, "empty skipping mode must be 0, 1 or 2");
   r->empty_skip = mode;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_result* out) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   if (!views || n <= 0) return fail(GBVR_EINVAL, "no tuning views");
   const int tiles[] = {4, 8, 16, 32};
@@ -2817,18 +2893,22 @@ int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_res
     out->default_ms = def;
   }
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_paint(gbvr_renderer* r) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   TRY(settle_async(r));
   // One view: the per-view kernel.  A one-view persistent launch measured no
   // faster (1063 vs 1109 frames/s at 1920x1080): a single frame's time is set
   // by its slowest ray tiles, which only other views' work can hide.
   return paint_plain(r, nullptr, 1);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_paint_batch_async(gbvr_renderer* r, const gbvr_view* views, int n, int slot) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   if (!views || n <= 0) return fail(GBVR_EINVAL, "bad view list");
   if (slot < 0 || slot > 1) return fail(GBVR_EINVAL, "slot must be 0 or 1");
@@ -2842,9 +2922,11 @@ int gbvr_paint_batch_async(gbvr_renderer* r, const gbvr_view* views, int n, int 
   }
   r->select_slot(slot);
   return paint_batch(r, views, n, true);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, void* host, size_t bytes) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (slot < 0 || slot > 1 || !r->read_stream || !r->slot_render_pending[slot])
     return fail(GBVR_ESTATE, "no asynchronous batch rendered into that slot");
@@ -2860,10 +2942,12 @@ int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, v
   CUDA_TRY(cudaEventRecord(r->slot_read[slot], r->read_stream));
   r->slot_read_pending[slot] = true;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_clearview(gbvr_renderer* r, int enabled, float iso, const float rgb[3], float size, float context_scale,
                        float border_scale, float focus_x, float focus_y) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   TRY(settle_async(r));
   if (enabled && !(size > 0.f)) return fail(GBVR_EINVAL, "lens size must be positive");
@@ -2878,9 +2962,11 @@ int gbvr_set_clearview(gbvr_renderer* r, int enabled, float iso, const float rgb
   r->skip_dirty = true;  // classification uses the lower iso value while on
   r->drop_graphs();
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_bboxes(gbvr_renderer* r, int global, int local, const float global_rgb[3], const float local_rgb[3]) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   TRY(settle_async(r));
   r->bbox_global = global ? 1 : 0;
@@ -2890,9 +2976,11 @@ int gbvr_set_bboxes(gbvr_renderer* r, int global, int local, const float global_
     if (local_rgb) r->bbox_rgb[1][k] = local_rgb[k];
   }
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_wait_read(gbvr_renderer* r, int slot) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (slot < 0 || slot > 1) return fail(GBVR_EINVAL, "slot must be 0 or 1");
   if (!r->read_stream || !r->slot_read_pending[slot]) return GBVR_OK;
@@ -2900,31 +2988,39 @@ int gbvr_wait_read(gbvr_renderer* r, int slot) {
   CUDA_TRY(cudaEventSynchronize(r->slot_read[slot]));
   r->slot_read_pending[slot] = false;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_wait_async(gbvr_renderer* r) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   CUDA_TRY(cudaStreamSynchronize(r->stream));
   if (r->read_stream) CUDA_TRY(cudaStreamSynchronize(r->read_stream));
   for (int k = 0; k < 2; ++k) r->slot_render_pending[k] = r->slot_read_pending[k] = false;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_paint_views(gbvr_renderer* r, const gbvr_view* views, int n) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   TRY(settle_async(r));
   if (!views) return fail(GBVR_EINVAL, "null views");
   return paint_plain(r, views, n);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_paint_batch(gbvr_renderer* r, const gbvr_view* views, int n) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   TRY(settle_async(r));
   if (!views) return fail(GBVR_EINVAL, "null views");
   return paint_batch(r, views, n);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t bytes) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   TRY(settle_async(r));
   const size_t need = (size_t)r->fb_w * r->fb_h * 4;
@@ -2933,9 +3029,11 @@ int gbvr_read_framebuffer(gbvr_renderer* r, int view, uint8_t* rgba8, size_t byt
   CUDA_TRY(cudaMemcpyAsync(rgba8, (const char*)r->d_fb8.p + need * view, need, cudaMemcpyDeviceToHost, r->stream));
   CUDA_TRY(cudaStreamSynchronize(r->stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_read_framebuffers(gbvr_renderer* r, int first, int n, uint8_t* rgba8, size_t bytes) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   TRY(settle_async(r));
   const size_t per = (size_t)r->fb_w * r->fb_h * 4;
@@ -2944,9 +3042,11 @@ int gbvr_read_framebuffers(gbvr_renderer* r, int first, int n, uint8_t* rgba8, s
   CUDA_TRY(cudaMemcpyAsync(rgba8, (const char*)r->d_fb8.p + per * first, per * n, cudaMemcpyDeviceToHost, r->stream));
   CUDA_TRY(cudaStreamSynchronize(r->stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_read_framebuffer_f32(gbvr_renderer* r, int view, float* rgba, size_t bytes) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   TRY(settle_async(r));
   if (!r->d_fb32.p) return fail(GBVR_ESTATE, "renderer was created without the float framebuffer flag (1)");
@@ -2956,9 +3056,11 @@ int gbvr_read_framebuffer_f32(gbvr_renderer* r, int view, float* rgba, size_t by
   CUDA_TRY(cudaMemcpyAsync(rgba, (const char*)r->d_fb32.p + need * view, need, cudaMemcpyDeviceToHost, r->stream));
   CUDA_TRY(cudaStreamSynchronize(r->stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_capture_single_frame(gbvr_renderer* r, const char* path, int preserve_transparency) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!path) return fail(GBVR_EINVAL, "null path");
   if (r->last_views < 1) return fail(GBVR_ESTATE, "nothing painted yet");
@@ -2967,9 +3069,11 @@ int gbvr_capture_single_frame(gbvr_renderer* r, const char* path, int preserve_t
   if (!write_image(path, px.data(), r->fb_w, r->fb_h, preserve_transparency != 0))
     return fail(GBVR_EIO, std::string("cannot write ") + path);
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_capture_view(gbvr_renderer* r, int view, const char* path, int preserve_transparency) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!path) return fail(GBVR_EINVAL, "null path");
   if (view < 0 || view >= r->last_views) return fail(GBVR_EINVAL, "view index out of range");
@@ -2978,9 +3082,11 @@ int gbvr_capture_view(gbvr_renderer* r, int view, const char* path, int preserve
   if (!write_image(path, px.data(), r->fb_w, r->fb_h, preserve_transparency != 0))
     return fail(GBVR_EIO, std::string("cannot write ") + path);
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (!out) return fail(GBVR_EINVAL, "null stats");
   memset(out, 0, sizeof(*out));
@@ -3028,16 +3134,20 @@ int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out) {
     }
   }
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_stats_level(gbvr_renderer* r, int level) {
+  GBVR_ABI_TRY
   TRY(check_r(r));
   if (level < 0 || level > 2) return fail(GBVR_EINVAL, "stats level must be 0, 1 or 2");
   r->stats_level = level;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_write_uvf(gbvr_renderer* r, const char* path) {
+  GBVR_ABI_TRY
   TRY(check_loaded(r));
   if (!path) return fail(GBVR_EINVAL, "null path");
   if (r->ds.ooc) return fail(GBVR_EINVAL, "out-of-core datasets are not written back as one raster");
@@ -3089,24 +3199,30 @@ int gbvr_write_uvf(gbvr_renderer* r, const char* path) {
   int rc = uvf_write(path, s, msg);
   if (rc) return fail(rc, msg);
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_build_uvf(const void* host, const int64_t dims[3], int dtype, const gbvr_brick_params* bp, const char* out_path) {
+  GBVR_ABI_TRY
   gbvr_renderer* r = nullptr;
   TRY(gbvr_create(GBVR_CUDA_RAYCASTER, 0, &r));
   std::unique_ptr<gbvr_renderer> hold(r);
   TRY(gbvr_load_volume(r, host, dims, dtype, bp));
   return gbvr_write_uvf(r, out_path);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_dev_hist1d(const void* dev_vol, int dtype, int64_t n, uint64_t* dev_hist, int nbins, void* stream) {
+  GBVR_ABI_TRY
   if (!dev_vol || !dev_hist || n < 0 || nbins <= 0) return fail(GBVR_EINVAL, "bad argument");
   CUDA_TRY(launch_hist1d(dev_vol, dtype, n, (unsigned long long*)dev_hist, nbins, (cudaStream_t)stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_dev_hist2d(const void* dev_vol, int dtype, const int64_t dims[3], double max_scalar, int64_t nx,
                     int64_t merge, uint64_t* dev_hist, float* max_grad, void* stream) {
+  GBVR_ABI_TRY
   if (!dev_vol || !dev_hist || !dims || nx <= 0 || merge <= 0) return fail(GBVR_EINVAL, "bad argument");
   DevBuf sc;
   CUDA_TRY(sc.alloc(sizeof(Hist2DScratch)));
@@ -3120,17 +3236,21 @@ int gbvr_dev_hist2d(const void* dev_vol, int dtype, const int64_t dims[3], doubl
   memcpy(&g, &hs.gmax_bits, 8);
   if (max_grad) *max_grad = (float)g;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_dev_downsample(const void* dev_in, int dtype, const int64_t dims[3], void* dev_out, void* stream) {
+  GBVR_ABI_TRY
   if (!dev_in || !dev_out || !dims) return fail(GBVR_EINVAL, "bad argument");
   long long d[3] = {dims[0], dims[1], dims[2]};
   CUDA_TRY(launch_downsample(dev_in, dtype, d, dev_out, (cudaStream_t)stream));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_look_at_camera(const float eye[3], const float ref[3], const float up[3], float fov_deg, float znear,
                         float zfar, int width, int height, float view[16], float proj[16]) {
+  GBVR_ABI_TRY
   if (!eye || !ref || !up || !view || !proj || width <= 0 || height <= 0 || !(znear > 0) || !(zfar > znear))
     return fail(GBVR_EINVAL, "bad camera");
   double e[3] = {eye[0], eye[1], eye[2]}, c[3] = {ref[0], ref[1], ref[2]}, u[3] = {up[0], up[1], up[2]};
@@ -3142,13 +3262,16 @@ int gbvr_look_at_camera(const float eye[3], const float ref[3], const float up[3
   perspective(fov_deg, (double)width / height, znear, zfar, P);
   for (int i = 0; i < 16; ++i) { view[i] = (float)V[i]; proj[i] = (float)P[i]; }
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_orbit_camera(float azimuth_deg, float elevation_deg, float radius, float fov_deg, int width, int height,
                       float view[16], float proj[16]) {
+  GBVR_ABI_TRY
   if (!view || !proj || width <= 0 || height <= 0 || !(radius > 0)) return fail(GBVR_EINVAL, "bad camera");
   orbit(azimuth_deg, elevation_deg, radius, fov_deg, width, height, view, proj);
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 }  // extern "C"
@@ -3488,6 +3611,7 @@ int server_add_dataset(gbvr_server* s, DevBuf& lv, int dtype, const long long d[
 extern "C" {
 
 int gbvr_server_create(const gbvr_server_params* params, gbvr_server** out) {
+  GBVR_ABI_TRY
   if (!out) return fail(GBVR_EINVAL, "null output handle");
   *out = nullptr;
   int ndev = 0;
@@ -3515,15 +3639,19 @@ int gbvr_server_create(const gbvr_server_params* params, gbvr_server** out) {
   s->worker = std::thread(server_worker, raw);
   *out = s.release();
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_server_destroy(gbvr_server* s) {
+  GBVR_ABI_TRY
   delete s;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_server_add_volume(gbvr_server* s, const void* host, const int64_t dims[3], int dtype,
                            const gbvr_brick_params* bp, int* id) {
+  GBVR_ABI_TRY
   TRY(check_s(s));
   if (!host || !dims || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0 || dtype < 0 || dtype > 2)
     return fail(GBVR_EINVAL, "bad volume");
@@ -3533,18 +3661,22 @@ int gbvr_server_add_volume(gbvr_server* s, const void* host, const int64_t dims[
   CUDA_TRY(lv.alloc(bytes));
   CUDA_TRY(cudaMemcpyAsync(lv.p, host, bytes, cudaMemcpyHostToDevice, s->stream));
   return server_add_dataset(s, lv, dtype, d, bp, id);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_server_add_synthetic(gbvr_server* s, const gbvr_synth_params* p, const gbvr_brick_params* bp, int* id) {
+  GBVR_ABI_TRY
   TRY(check_s(s));
   DevBuf lv;
   TRY(synth_to_device(p, lv, s->stream));
   long long d[3] = {p->dims[0], p->dims[1], p->dims[2]};
   return server_add_dataset(s, lv, p->dtype, d, bp, id);
+  GBVR_ABI_CATCH
 }
 
 int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba, int w, int h, float grad_max,
                        float iso, const float iso_rgb[3], double lo, double hi, int* tf_id) {
+  GBVR_ABI_TRY
   TRY(check_s(s));
   if (dataset < 0 || dataset >= (int)s->datasets.size()) return fail(GBVR_EINVAL, "bad dataset id");
   if (mode < 0 || mode > 3) return fail(GBVR_EINVAL, "bad render mode");
@@ -3583,9 +3715,11 @@ int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba,
   s->tfs.push_back(std::move(t));
   if (tf_id) *tf_id = (int)s->tfs.size() - 1;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_server_submit(gbvr_server* s, const gbvr_request* req, uint64_t* ticket) {
+  GBVR_ABI_TRY
   TRY(check_s(s));
   if (!req || !req->out_rgba8 || req->width <= 0 || req->height <= 0 || req->width > 16384 || req->height > 16384)
     return fail(GBVR_EINVAL, "bad request");
@@ -3606,9 +3740,11 @@ int gbvr_server_submit(gbvr_server* s, const gbvr_request* req, uint64_t* ticket
   }
   s->cv_work.notify_one();
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_server_wait(gbvr_server* s, uint64_t ticket, double timeout_s, gbvr_request_result* out) {
+  GBVR_ABI_TRY
   TRY(check_s(s));
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->reqs.find(ticket);
@@ -3633,9 +3769,11 @@ int gbvr_server_wait(gbvr_server* s, uint64_t ticket, double timeout_s, gbvr_req
   s->reqs.erase(it);
   if (st != GBVR_OK) return fail(st, s->worker_error.empty() ? "request failed" : s->worker_error);
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_server_get_stats(gbvr_server* s, gbvr_server_stats* out) {
+  GBVR_ABI_TRY
   TRY(check_s(s));
   if (!out) return fail(GBVR_EINVAL, "null stats");
   std::lock_guard<std::mutex> lk(s->mu);
@@ -3654,9 +3792,11 @@ int gbvr_server_get_stats(gbvr_server* s, gbvr_server_stats* out) {
   }
   if (s->completed && s->t_last > s->t_first) out->frames_per_s = s->completed / ((s->t_last - s->t_first) / 1000.0);
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_server_reset_stats(gbvr_server* s) {
+  GBVR_ABI_TRY
   TRY(check_s(s));
   std::lock_guard<std::mutex> lk(s->mu);
   s->latencies.clear();
@@ -3664,6 +3804,7 @@ int gbvr_server_reset_stats(gbvr_server* s) {
   s->t_first = -1;
   s->t_last = 0;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 }  // extern "C"

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/gbvr.h"
+#include "abi_guard.h"
 
 namespace gbvr {
 
@@ -148,13 +149,17 @@ extern "C" {
 size_t gbvr_lz4_bound(size_t n) { return gbvr::lz4_bound(n); }
 
 size_t gbvr_lz4_compress(const void* src, size_t n, void* dst, size_t cap) {
+  GBVR_ABI_TRY
   if (!src || !dst) return 0;
   return gbvr::lz4_compress((const uint8_t*)src, n, (uint8_t*)dst, cap);
+  GBVR_ABI_CATCH_SIZE
 }
 
 int gbvr_lz4_decompress(const void* src, size_t n, void* dst, size_t out_n) {
+  GBVR_ABI_TRY
   if (!src || !dst) return GBVR_EINVAL;
   return gbvr::lz4_decompress((const uint8_t*)src, n, (uint8_t*)dst, out_n) ? GBVR_OK : GBVR_EFORMAT;
+  GBVR_ABI_CATCH
 }
 
 }  // extern "C"

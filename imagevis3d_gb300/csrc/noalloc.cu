@@ -18,6 +18,7 @@
 #include <string>
 
 #include "../../include/gbvr.h"
+#include "abi_guard.h"
 #include "gbvr_internal.h"
 
 namespace gbvr {
@@ -90,6 +91,7 @@ void fill_tables(const gbvr_synth_params& p, float* t) {
 }  // namespace
 
 extern "C" int gbvr_dev_synth_volume_noalloc(const gbvr_synth_params* p, void* dev_out, size_t bytes, void* stream) {
+  GBVR_ABI_TRY
   if (!p || !dev_out) return set_error(GBVR_EINVAL, "null argument");
   if (p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 || p->nblobs < 0)
     return set_error(GBVR_EINVAL, "bad synthetic parameters");
@@ -135,4 +137,5 @@ extern "C" int gbvr_dev_synth_volume_noalloc(const gbvr_synth_params* p, void* d
   e = launch_synth_blobs(td, d, p->dtype, dev_out, s);
   if (e != cudaSuccess) return set_error(GBVR_ECUDA, std::string("synth launch: ") + cudaGetErrorString(e));
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }

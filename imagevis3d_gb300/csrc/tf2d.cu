@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "../../include/gbvr.h"
+#include "abi_guard.h"
 #include "gbvr_internal.h"
 
 namespace gbvr {
@@ -132,6 +133,7 @@ extern "C" {
 
 int gbvr_tf2d_rasterize(const gbvr_tf2d_swatch* swatches, int nswatches, const float* tf1d, int tf1d_n, int width,
                         int height, float* out_rgba) {
+  GBVR_ABI_TRY
   if (!out_rgba || width <= 0 || height <= 0 || width > 16384 || height > 16384 || nswatches < 0 || tf1d_n < 0 ||
       (nswatches > 0 && !swatches) || (tf1d_n > 0 && !tf1d))
     return set_error(GBVR_EINVAL, "bad argument");
@@ -165,9 +167,11 @@ int gbvr_tf2d_rasterize(const gbvr_tf2d_swatch* swatches, int nswatches, const f
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "k_raster_tf2d");
   if ((e = cudaMemcpy(out_rgba, dout.p, nout, cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_fail(e, "readback");
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_set_tf2d_file(gbvr_renderer* r, const char* path, float max_grad) {
+  GBVR_ABI_TRY
   if (!r) return set_error(GBVR_EINVAL, "null renderer");
   int w = 0, h = 0, n1 = 0, ns = 0;
   int st = gbvr_load_tf2d_file(path, &w, &h, nullptr, 0, &n1, nullptr, 0, &ns);
@@ -180,6 +184,7 @@ int gbvr_set_tf2d_file(gbvr_renderer* r, const char* path, float max_grad) {
   st = gbvr_tf2d_rasterize(sw.data(), ns, tf1d.data(), n1, w, h, table.data());
   if (st != GBVR_OK) return st;
   return gbvr_set_tf2d(r, table.data(), w, h, max_grad);
+  GBVR_ABI_CATCH
 }
 
 }  // extern "C"

@@ -1,10 +1,13 @@
 // UVF container I/O and MD5 (RFC 1321).  See uvf.h for the layout notes.
 #include "uvf.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <new>
+#include <stdexcept>
 
 #include "../../include/gbvr.h"
 
@@ -105,7 +108,21 @@ bool rd64(FILE* f, uint64_t off, uint64_t& v) {
 }
 }  // namespace
 
-int uvf_read(const std::string& path, bool verify, UvfFile& out, std::string& msg) {
+namespace {
+// a * b, false when it does not fit 64 bits
+bool mul_ok(uint64_t a, uint64_t b, uint64_t& r) { return !__builtin_mul_overflow(a, b, &r); }
+// count items of `each` bytes fit in [from, end)
+bool fits(uint64_t from, uint64_t end, uint64_t count, uint64_t each) {
+  if (from > end) return false;
+  uint64_t bytes;
+  return mul_ok(count, each, bytes) && bytes <= end - from;
+}
+
+// The parse proper.  Every read of a block's fields stays inside the block,
+// every count read from the file is checked against the bytes that remain
+// before anything is allocated, so a truncated or corrupted file ends in a
+// status.
+int uvf_parse(const std::string& path, bool verify, UvfFile& out, std::string& msg) {
   File fh(path, "rb");
   if (!fh.f) { msg = "cannot open " + path; return GBVR_EIO; }
   FILE* f = fh.f;
@@ -116,7 +133,7 @@ int uvf_read(const std::string& path, bool verify, UvfFile& out, std::string& ms
     msg = "not a UVF file: " + path;
     return GBVR_EFORMAT;
   }
-  unsigned char endian;
+  unsigned char endian = 1;
   rd(f, 8, &endian, 1);
   if (endian != 0) { msg = "big-endian UVF is not supported"; return GBVR_EFORMAT; }
   uint64_t p = 9, cs_len = 0;
@@ -131,7 +148,7 @@ int uvf_read(const std::string& path, bool verify, UvfFile& out, std::string& ms
   const uint64_t md5_from = p + cs_len;
   p += cs_len;
   uint64_t addl = 0;
-  if (!rd64(f, p, addl)) { msg = "truncated UVF global header"; return GBVR_EFORMAT; }
+  if (!rd64(f, p, addl) || addl > size - (p + 8)) { msg = "truncated UVF global header"; return GBVR_EFORMAT; }
   p += 8 + addl;
   if (verify && out.checksum_semantic == 2) {
     if (cs_len != 16) { msg = "MD5 checksum must be 16 bytes"; return GBVR_EFORMAT; }
@@ -149,18 +166,29 @@ int uvf_read(const std::string& path, bool verify, UvfFile& out, std::string& ms
   for (int guard = 0; guard < 4096; ++guard) {
     UvfBlock b;
     b.start = p;
-    uint64_t slen;
-    if (!rd64(f, p, slen) || slen > 1 << 20 || p + 8 + slen + 24 > size) { msg = "truncated block header"; return GBVR_EFORMAT; }
+    uint64_t slen = 0;
+    if (p > size || !rd64(f, p, slen) || slen > (1 << 20) || slen + 32 > size - p) {
+      msg = "truncated block header";
+      return GBVR_EFORMAT;
+    }
     b.id.resize(slen);
     if (slen) rd(f, p + 8, &b.id[0], slen);
     uint64_t q = p + 8 + slen;
+    b.semantic = b.compression = b.next = 0;
     rd64(f, q, b.semantic);
     rd64(f, q + 8, b.compression);
     rd64(f, q + 16, b.next);
     b.payload = q + 24;
     out.blocks.push_back(b);
+    if (b.next > size - b.start) { msg = "block extends past end of file"; return GBVR_EFORMAT; }
     const uint64_t end = b.next ? b.start + b.next : size;
-    if (end > size || end < b.payload) { msg = "block extends past end of file"; return GBVR_EFORMAT; }
+    if (end < b.payload) { msg = "block extends past end of file"; return GBVR_EFORMAT; }
+    // reads of the block's fields: inside [payload, end) or the parse fails
+    bool ok = true;
+    auto get = [&](uint64_t off, uint64_t& v) {
+      v = 0;
+      if (!(off >= b.payload && off <= end && end - off >= 8 && rd64(f, off, v))) ok = false;
+    };
     if (b.compression != 0 && (b.semantic == 1 || b.semantic == 5 || b.semantic == 6 || b.semantic == 7)) {
       msg = "compressed UVF blocks are not supported";
       return GBVR_EFORMAT;
@@ -168,66 +196,89 @@ int uvf_read(const std::string& path, bool verify, UvfFile& out, std::string& ms
     if (b.semantic == 1 && !out.has_raster) {
       UvfRaster& r = out.raster;
       r.id = b.id;
-      uint64_t w = b.payload, nd;
-      rd64(f, w, nd);
-      if (nd != 3) { msg = "raster block is not 3-dimensional"; return GBVR_EFORMAT; }
+      uint64_t w = b.payload, nd = 0;
+      get(w, nd);
+      if (!ok || nd != 3) { msg = "raster block is not 3-dimensional"; return GBVR_EFORMAT; }
       w += 8 + 3 * 8;  // domain semantics
       for (int i = 0; i < 16; ++i) {
         uint64_t bits;
-        rd64(f, w + 8 * i, bits);
+        get(w + 8 * i, bits);
         memcpy(&r.transform[i], &bits, 8);
       }
       w += 16 * 8;
-      for (int i = 0; i < 3; ++i) rd64(f, w + 8 * i, r.dims[i]);
+      for (int i = 0; i < 3; ++i) get(w + 8 * i, r.dims[i]);
       w += 24;
-      for (int i = 0; i < 3; ++i) rd64(f, w + 8 * i, r.brick_size[i]);
+      for (int i = 0; i < 3; ++i) get(w + 8 * i, r.brick_size[i]);
       w += 24;
-      for (int i = 0; i < 3; ++i) rd64(f, w + 8 * i, r.overlap[i]);
+      for (int i = 0; i < 3; ++i) get(w + 8 * i, r.overlap[i]);
       w += 24;
-      for (int i = 0; i < 3; ++i) rd64(f, w + 8 * i, r.lod_factor[i]);
+      for (int i = 0; i < 3; ++i) get(w + 8 * i, r.lod_factor[i]);
       w += 24;
       uint64_t ngroups = 0;
       for (int i = 0; i < 3; ++i) {
-        rd64(f, w + 8 * i, r.lod_groups[i]);
+        get(w + 8 * i, r.lod_groups[i]);
+        if (r.lod_groups[i] >= 64) { msg = "bad LOD groups in the raster block"; return GBVR_EFORMAT; }
         if (r.lod_groups[i] + 1 > ngroups) ngroups = r.lod_groups[i] + 1;
       }
       w += 24;
+      if (!ok) { msg = "truncated raster block"; return GBVR_EFORMAT; }
       r.lod_counts.assign(ngroups, 1);
-      for (uint64_t g = 0; g < ngroups; ++g) rd64(f, w + 8 * g, r.lod_counts[g]);
+      for (uint64_t g = 0; g < ngroups; ++g) get(w + 8 * g, r.lod_counts[g]);
       w += 8 * ngroups;
-      uint64_t nel, eldim;
-      rd64(f, w, nel);
-      rd64(f, w + 8, eldim);
+      uint64_t nel = 0, eldim = 0;
+      get(w, nel);
+      get(w + 8, eldim);
+      if (!ok) { msg = "truncated raster block"; return GBVR_EFORMAT; }
       if (nel != 1 || eldim != 1) { msg = "only scalar raster data is supported"; return GBVR_EFORMAT; }
       w += 16;
-      rd64(f, w, r.elem_semantic);
-      rd64(f, w + 8, r.bit_size);
-      rd64(f, w + 16, r.mantissa);
+      get(w, r.elem_semantic);
+      get(w + 8, r.bit_size);
+      get(w + 16, r.mantissa);
       w += 24;
-      unsigned char sg;
-      rd(f, w, &sg, 1);
+      unsigned char sg = 0;
+      if (!(w < end && rd(f, w, &sg, 1))) ok = false;
       r.is_signed = sg != 0;
       w += 1;
-      rd64(f, w, r.data_offset_field);
+      get(w, r.data_offset_field);
       w += 8;
+      if (!ok) { msg = "truncated raster block"; return GBVR_EFORMAT; }
+      if (r.bit_size != 8 && r.bit_size != 16 && r.bit_size != 32) {
+        msg = "unsupported raster element size";
+        return GBVR_EFORMAT;
+      }
+      // the voxels (finest level) must lie inside the file
+      uint64_t nvox = 1, nbytes = 0;
+      for (int i = 0; i < 3; ++i)
+        if (r.dims[i] == 0 || !mul_ok(nvox, r.dims[i], nvox)) { msg = "bad raster dimensions"; return GBVR_EFORMAT; }
+      if (!mul_ok(nvox, r.bit_size / 8, nbytes) || r.data_offset_field > size - w) {
+        msg = "bad raster dimensions";
+        return GBVR_EFORMAT;
+      }
       r.data_pos = w + r.data_offset_field;
+      if (nbytes > size - r.data_pos) { msg = "truncated raster data"; return GBVR_EFORMAT; }
       r.is_float = r.bit_size == 32 && r.mantissa == 23;
       out.has_raster = true;
     } else if (b.semantic == 5) {
-      uint64_t n;
-      rd64(f, b.payload, n);
-      if (b.payload + 8 + 8 * n > end) { msg = "truncated 1D histogram"; return GBVR_EFORMAT; }
+      uint64_t n = 0;
+      get(b.payload, n);
+      if (!ok || !fits(b.payload + 8, end, n, 8)) { msg = "truncated 1D histogram"; return GBVR_EFORMAT; }
       out.hist1d.resize(n);
-      for (uint64_t i = 0; i < n; ++i) rd64(f, b.payload + 8 + 8 * i, out.hist1d[i]);
+      for (uint64_t i = 0; i < n; ++i) get(b.payload + 8 + 8 * i, out.hist1d[i]);
+      if (!ok) { msg = "truncated 1D histogram"; return GBVR_EFORMAT; }
     } else if (b.semantic == 6) {
-      rd(f, b.payload, &out.hist2d_max_grad, 4);
-      rd64(f, b.payload + 4, out.hist2d_nx);
-      rd64(f, b.payload + 12, out.hist2d_ny);
-      const uint64_t n = out.hist2d_nx * out.hist2d_ny;
-      if (b.payload + 20 + 8 * n > end) { msg = "truncated 2D histogram"; return GBVR_EFORMAT; }
+      uint64_t nx = 0, ny = 0, n = 0;
+      if (!(end - b.payload >= 4 && rd(f, b.payload, &out.hist2d_max_grad, 4))) ok = false;
+      get(b.payload + 4, nx);
+      get(b.payload + 12, ny);
+      if (!ok || !mul_ok(nx, ny, n) || !fits(b.payload + 20, end, n, 8)) {
+        msg = "truncated 2D histogram";
+        return GBVR_EFORMAT;
+      }
+      out.hist2d_nx = nx;
+      out.hist2d_ny = ny;
       out.hist2d.resize(n);
       std::vector<unsigned char> raw(8 * n);
-      rd(f, b.payload + 20, raw.data(), raw.size());
+      if (n && !rd(f, b.payload + 20, raw.data(), raw.size())) { msg = "truncated 2D histogram"; return GBVR_EFORMAT; }
       for (uint64_t i = 0; i < n; ++i) {
         uint64_t v = 0;
         for (int k = 7; k >= 0; --k) v = (v << 8) | raw[8 * i + k];
@@ -235,35 +286,55 @@ int uvf_read(const std::string& path, bool verify, UvfFile& out, std::string& ms
       }
       out.hist2d_id = b.id;
     } else if (b.semantic == 7) {
-      uint64_t nb, nc;
-      rd64(f, b.payload, nb);
-      rd64(f, b.payload + 8, nc);
-      if (b.payload + 16 + 32 * nb * nc > end) { msg = "truncated min/max block"; return GBVR_EFORMAT; }
+      uint64_t nb = 0, nc = 0, n = 0;
+      get(b.payload, nb);
+      get(b.payload + 8, nc);
+      if (!ok || !mul_ok(nb, nc, n) || !fits(b.payload + 16, end, n, 32)) {
+        msg = "truncated min/max block";
+        return GBVR_EFORMAT;
+      }
       out.minmax_components = nc;
-      out.minmax.resize(nb * nc);
-      for (uint64_t i = 0; i < nb * nc; ++i) rd(f, b.payload + 16 + 32 * i, &out.minmax[i], 32);
+      out.minmax.resize(n);
+      for (uint64_t i = 0; i < n; ++i)
+        if (!rd(f, b.payload + 16 + 32 * i, &out.minmax[i], 32)) { msg = "truncated min/max block"; return GBVR_EFORMAT; }
     } else if (b.semantic == 4) {
-      uint64_t n, w = b.payload;
-      rd64(f, w, n);
+      uint64_t n = 0, w = b.payload;
+      get(w, n);
       w += 8;
-      for (uint64_t i = 0; i < n && i < 4096; ++i) {
-        uint64_t kl, vl;
-        rd64(f, w, kl);
+      for (uint64_t i = 0; ok && i < n && i < 4096; ++i) {
+        uint64_t kl = 0, vl = 0;
+        get(w, kl);
+        if (!ok || kl > end - (w + 8)) break;
         std::string k(kl, '\0');
         if (kl) rd(f, w + 8, &k[0], kl);
         w += 8 + kl;
-        rd64(f, w, vl);
+        get(w, vl);
+        if (!ok || vl > end - (w + 8)) break;
         std::string v(vl, '\0');
         if (vl) rd(f, w + 8, &v[0], vl);
         w += 8 + vl;
         out.kv.emplace_back(k, v);
       }
+      if (!ok || out.kv.size() < std::min<uint64_t>(n, 4096)) { msg = "truncated key/value block"; return GBVR_EFORMAT; }
     }
     if (b.next == 0) break;
     p = b.start + b.next;
   }
   if (!out.has_raster) { msg = "UVF file holds no raster data block"; return GBVR_EFORMAT; }
   return GBVR_OK;
+}
+}  // namespace
+
+int uvf_read(const std::string& path, bool verify, UvfFile& out, std::string& msg) {
+  try {
+    return uvf_parse(path, verify, out, msg);
+  } catch (const std::bad_alloc&) {
+    msg = "out of host memory reading " + path;
+    return GBVR_ENOMEM;
+  } catch (const std::exception& e) {
+    msg = std::string("UVF read failed: ") + e.what();
+    return GBVR_EFORMAT;
+  }
 }
 
 int uvf_read_voxels(const std::string& path, const UvfFile& uf, void* out, size_t bytes, std::string& msg) {

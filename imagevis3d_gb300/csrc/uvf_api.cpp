@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/gbvr.h"
+#include "abi_guard.h"
 #include "uvf.h"
 
 namespace gbvr {
@@ -17,6 +18,7 @@ using namespace gbvr;
 extern "C" {
 
 int gbvr_uvf_inspect(const char* path, int verify, gbvr_uvf_summary* out) {
+  GBVR_ABI_TRY
   if (!path || !out) return set_error(GBVR_EINVAL, "null argument");
   UvfFile f;
   std::string msg;
@@ -25,7 +27,7 @@ int gbvr_uvf_inspect(const char* path, int verify, gbvr_uvf_summary* out) {
   memset(out, 0, sizeof(*out));
   out->version = f.version;
   out->checksum_semantic = f.checksum_semantic;
-  memcpy(out->checksum, f.checksum.data(), f.checksum.size() < 16 ? f.checksum.size() : 16);
+  if (!f.checksum.empty()) memcpy(out->checksum, f.checksum.data(), f.checksum.size() < 16 ? f.checksum.size() : 16);
   out->checksum_verified = verify && f.checksum_ok;
   out->nblocks = (int)f.blocks.size();
   for (size_t i = 0; i < f.blocks.size() && i < 32; ++i) out->block_semantics[i] = f.blocks[i].semantic;
@@ -50,9 +52,11 @@ int gbvr_uvf_inspect(const char* path, int verify, gbvr_uvf_summary* out) {
     out->minmax_first[3] = f.minmax[0].max_grad;
   }
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_uvf_read_volume(const char* path, void* out, size_t bytes) {
+  GBVR_ABI_TRY
   if (!path || !out) return set_error(GBVR_EINVAL, "null argument");
   UvfFile f;
   std::string msg;
@@ -64,32 +68,38 @@ int gbvr_uvf_read_volume(const char* path, void* out, size_t bytes) {
   rc = uvf_read_voxels(path, f, out, need, msg);
   if (rc) return set_error(rc, msg);
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_uvf_read_hist1d(const char* path, uint64_t* out, size_t n) {
+  GBVR_ABI_TRY
   UvfFile f;
   std::string msg;
   int rc = uvf_read(path ? path : "", false, f, msg);
   if (rc) return set_error(rc, msg);
   if (!out || n < f.hist1d.size()) return set_error(GBVR_EINVAL, "buffer too small");
-  memcpy(out, f.hist1d.data(), 8 * f.hist1d.size());
+  if (!f.hist1d.empty()) memcpy(out, f.hist1d.data(), 8 * f.hist1d.size());
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_uvf_read_hist2d(const char* path, uint64_t* out, size_t n, float* max_grad) {
+  GBVR_ABI_TRY
   UvfFile f;
   std::string msg;
   int rc = uvf_read(path ? path : "", false, f, msg);
   if (rc) return set_error(rc, msg);
   if (!out || n < f.hist2d.size()) return set_error(GBVR_EINVAL, "buffer too small");
-  memcpy(out, f.hist2d.data(), 8 * f.hist2d.size());
+  if (!f.hist2d.empty()) memcpy(out, f.hist2d.data(), 8 * f.hist2d.size());
   if (max_grad) *max_grad = f.hist2d_max_grad;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_uvf_write_raster(const char* path, const char* raster_id, const void* voxels, const int64_t dims[3], int dtype,
                           int32_t brick_size, int32_t overlap, const uint64_t* hist1d, size_t n1, const uint64_t* hist2d,
                           size_t nx, size_t ny, float max_grad, const double* minmax, size_t nminmax) {
+  GBVR_ABI_TRY
   if (!path || !voxels || !dims || dtype < 0 || dtype > 2) return set_error(GBVR_EINVAL, "bad argument");
   UvfWriteSpec s;
   s.raster.id = raster_id ? raster_id : "";
@@ -117,9 +127,11 @@ int gbvr_uvf_write_raster(const char* path, const char* raster_id, const void* v
   int rc = uvf_write(path, s, msg);
   if (rc) return set_error(rc, msg);
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_load_tf1d_file(const char* path, int target_size, float* rgba_out, int capacity, int* n_out) {
+  GBVR_ABI_TRY
   if (!path || !rgba_out || capacity <= 0) return set_error(GBVR_EINVAL, "bad argument");
   FILE* f = fopen(path, "r");
   if (!f) return set_error(GBVR_EIO, std::string("cannot open ") + path);
@@ -145,10 +157,12 @@ int gbvr_load_tf1d_file(const char* path, int target_size, float* rgba_out, int 
   }
   if (n_out) *n_out = (int)m;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 int gbvr_load_tf2d_file(const char* path, int* width, int* height, float* tf1d, int tf1d_cap, int* tf1d_n,
                         gbvr_tf2d_swatch* swatches, int swatch_cap, int* nswatches) {
+  GBVR_ABI_TRY
   if (!path) return set_error(GBVR_EINVAL, "bad argument");
   FILE* f = fopen(path, "r");
   if (!f) return set_error(GBVR_EIO, std::string("cannot open ") + path);
@@ -190,6 +204,7 @@ int gbvr_load_tf2d_file(const char* path, int* width, int* height, float* tf1d, 
   if (tf1d_n) *tf1d_n = (int)n;
   if (nswatches) *nswatches = ns;
   return GBVR_OK;
+  GBVR_ABI_CATCH
 }
 
 }  // extern "C"

@@ -3,6 +3,7 @@
 // RGBA8 readback model of StandaloneTuvok/CmdRenderer.cpp:34-56.
 // PNG is written with stored (uncompressed) deflate blocks, so no zlib is
 // needed; .bmp and .ppm are also accepted.
+#include <cctype>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -11,19 +12,21 @@
 
 namespace gbvr {
 
-static uint32_t crc_table[256];
-static bool crc_ready = false;
-static void crc_init() {
-  if (crc_ready) return;
-  for (uint32_t n = 0; n < 256; ++n) {
-    uint32_t c = n;
-    for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-    crc_table[n] = c;
+// CRC-32 (the PNG chunk checksum), table built once on first use (a
+// function-local static: safe when several threads capture at once)
+struct CrcTable {
+  uint32_t t[256];
+  CrcTable() {
+    for (uint32_t n = 0; n < 256; ++n) {
+      uint32_t c = n;
+      for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+      t[n] = c;
+    }
   }
-  crc_ready = true;
-}
+};
 static uint32_t crc32(const unsigned char* p, size_t n, uint32_t c = 0xFFFFFFFFu) {
-  for (size_t i = 0; i < n; ++i) c = crc_table[(c ^ p[i]) & 0xFF] ^ (c >> 8);
+  static const CrcTable table;
+  for (size_t i = 0; i < n; ++i) c = table.t[(c ^ p[i]) & 0xFF] ^ (c >> 8);
   return c;
 }
 
@@ -46,7 +49,7 @@ static void chunk(std::vector<unsigned char>& out, const char* type, const std::
 // rgba: width*height*4 bytes, row 0 = top.  alpha == false drops alpha.
 bool write_image(const std::string& path, const unsigned char* rgba, int w, int h, bool alpha) {
   std::string ext = path.size() >= 4 ? path.substr(path.size() - 4) : "";
-  for (auto& ch : ext) ch = (char)tolower(ch);
+  for (auto& ch : ext) ch = (char)tolower((unsigned char)ch);
   FILE* f = fopen(path.c_str(), "wb");
   if (!f) return false;
   bool ok = true;
@@ -71,7 +74,6 @@ bool write_image(const std::string& path, const unsigned char* rgba, int w, int 
       ok = fwrite(line.data(), 1, row, f) == (size_t)row;
     }
   } else {
-    crc_init();
     std::vector<unsigned char> png = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1A, '\n'};
     std::vector<unsigned char> ihdr;
     be32(ihdr, (uint32_t)w);

@@ -1,7 +1,8 @@
-// The library's host-side parsers and codec under AddressSanitizer and
-// UndefinedBehaviorSanitizer: the UVF reader and writer, the .1dt / .2dt
-// parsers and the LZ4 block codec, on valid inputs and on truncated,
-// bit-flipped and overwritten ones.  A malformed input must come back as a
+// The library's host-side parsers, codec and image writer under
+// AddressSanitizer and UndefinedBehaviorSanitizer: the UVF reader and writer,
+// the .1dt / .2dt parsers and the LZ4 block codec on valid inputs and on
+// truncated, bit-flipped and overwritten ones, and the PNG / BMP / PPM frame
+// writer at odd sizes.  A malformed input must come back as a
 // status: no crash, no out-of-bounds access, no undefined behaviour.  Built
 // and run by test_host_sanitizers.py (no GPU); usage: sanitize_host DIR SEED.
 #include <algorithm>
@@ -18,6 +19,7 @@
 namespace gbvr {
 // the renderer's error store lives in the CUDA part of the library
 int set_error(int code, const std::string&) { return code; }
+bool write_image(const std::string& path, const unsigned char* rgba, int w, int h, bool alpha);
 }  // namespace gbvr
 
 namespace {
@@ -240,6 +242,61 @@ void tf_cases(const std::string& dir) {
   }
 }
 
+uint32_t be32(const uint8_t* p) { return (uint32_t)p[0] << 24 | (uint32_t)p[1] << 16 | (uint32_t)p[2] << 8 | p[3]; }
+
+// PNG (stored deflate blocks), BMP and PPM frames of odd sizes: the PNG is
+// decoded back (chunks, stored blocks, filter bytes) and must give the pixels
+void image_cases(const std::string& dir) {
+  const int sizes[][2] = {{1, 1}, {3, 5}, {100, 7}, {7, 300}, {200, 200}};
+  for (const auto& sz : sizes)
+    for (int alpha = 0; alpha < 2; ++alpha) {
+      const int w = sz[0], h = sz[1], ch = alpha ? 4 : 3;
+      Heap rgba((size_t)w * h * 4);
+      for (size_t i = 0; i < (size_t)w * h * 4; ++i) rgba.data()[i] = (uint8_t)rnd();
+      const std::string png = dir + "/frame.png";
+      CHECK(gbvr::write_image(png, rgba.data(), w, h, alpha != 0));
+      const std::vector<uint8_t> f = slurp(png);
+      CHECK(f.size() > 33 && std::memcmp(f.data() + 12, "IHDR", 4) == 0);
+      if (f.size() <= 33) continue;
+      CHECK(be32(f.data() + 16) == (uint32_t)w && be32(f.data() + 20) == (uint32_t)h && f[25] == (alpha ? 6 : 2));
+      std::vector<uint8_t> z;  // the IDAT payloads
+      for (size_t at = 8; at + 12 <= f.size();) {
+        const uint32_t n = be32(f.data() + at);
+        if (at + 12 + n > f.size()) break;
+        if (std::memcmp(f.data() + at + 4, "IDAT", 4) == 0) z.insert(z.end(), f.begin() + at + 8, f.begin() + at + 8 + n);
+        at += 12 + n;
+      }
+      std::vector<uint8_t> raw;  // stored blocks after the 2-byte zlib header
+      size_t q = 2;
+      bool last = false;
+      while (!last && q + 5 <= z.size()) {
+        last = z[q] & 1;
+        const size_t n = z[q + 1] | (size_t)z[q + 2] << 8;
+        CHECK((z[q + 3] | (size_t)z[q + 4] << 8) == (~n & 0xffff));
+        if (q + 5 + n > z.size()) break;
+        raw.insert(raw.end(), z.begin() + q + 5, z.begin() + q + 5 + n);
+        q += 5 + n;
+      }
+      CHECK(last && raw.size() == (size_t)h * (1 + (size_t)w * ch));
+      bool same = raw.size() == (size_t)h * (1 + (size_t)w * ch);
+      for (int y = 0; same && y < h; ++y) {
+        same = raw[(size_t)y * (1 + w * ch)] == 0;
+        for (int x = 0; same && x < w; ++x)
+          same = std::memcmp(&raw[(size_t)y * (1 + w * ch) + 1 + (size_t)x * ch], rgba.data() + 4 * ((size_t)y * w + x),
+                             ch) == 0;
+      }
+      CHECK(same);
+      const std::string bmp = dir + "/frame.BMP", ppm = dir + "/frame.ppm";
+      CHECK(gbvr::write_image(bmp, rgba.data(), w, h, false));
+      CHECK(slurp(bmp).size() == 54 + (size_t)((w * 3 + 3) & ~3) * h);
+      CHECK(gbvr::write_image(ppm, rgba.data(), w, h, false));
+      char hdr[64];
+      std::snprintf(hdr, sizeof(hdr), "P6\n%d %d\n255\n", w, h);
+      CHECK(slurp(ppm).size() == std::strlen(hdr) + (size_t)w * h * 3);
+    }
+  CHECK(!gbvr::write_image(dir + "/no/such/dir/frame.png", nullptr, 0, 0, false));
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -252,6 +309,7 @@ int main(int argc, char** argv) {
   lz4_cases();
   uvf_cases(dir);
   tf_cases(dir);
+  image_cases(dir);
   std::printf("%s: %d failed checks\n", g_failures ? "FAILED" : "ok", g_failures);
   return g_failures ? 1 : 0;
 }

@@ -1,9 +1,9 @@
-"""The host-side UVF reader and writer, the .1dt / .2dt parsers and the LZ4
-codec, built from the library's own sources with AddressSanitizer and
-UndefinedBehaviorSanitizer and run on valid, truncated, bit-flipped and
-overwritten inputs (tests/sanitize_host.cpp).  A malformed file must come
-back as a status, never as a crash, an out-of-bounds access or undefined
-behaviour.  No GPU."""
+"""The host-side UVF reader and writer, the .1dt / .2dt parsers, the LZ4
+codec and the frame image writer, built from the library's own sources with
+AddressSanitizer, UndefinedBehaviorSanitizer and LeakSanitizer and run on
+valid, truncated, bit-flipped and overwritten inputs
+(tests/sanitize_host.cpp).  A malformed file must come back as a status,
+never as a crash, an out-of-bounds access or undefined behaviour.  No GPU."""
 import os
 import shutil
 import subprocess
@@ -23,7 +23,8 @@ def sanitized(tmp_path_factory):
     cmd = ["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
            "-fno-omit-frame-pointer", "-I", os.path.join(ROOT, "include"), "-I", CSRC,
            os.path.join(ROOT, "tests", "sanitize_host.cpp"), os.path.join(CSRC, "uvf.cpp"),
-           os.path.join(CSRC, "uvf_api.cpp"), os.path.join(CSRC, "lz4.cpp"), "-o", exe]
+           os.path.join(CSRC, "uvf_api.cpp"), os.path.join(CSRC, "lz4.cpp"), os.path.join(CSRC, "image_io.cpp"),
+           "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0 and ("asan" in r.stderr.lower() or "ubsan" in r.stderr.lower()):
         pytest.skip("sanitizer runtime not available: " + r.stderr.strip().splitlines()[-1])

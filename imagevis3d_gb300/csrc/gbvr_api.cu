@@ -3539,7 +3539,14 @@ void server_worker(gbvr_server* s) {
         q->batch_size = (int)slot.reqs.size();
       }
       lk.unlock();
-      int rc = launch_batch(s, slot);
+      int rc;
+      try {  // the worker thread must not end on an exception: the batch fails instead
+        rc = launch_batch(s, slot);
+      } catch (const std::bad_alloc&) {
+        rc = fail(GBVR_ENOMEM, "out of host memory");
+      } catch (const std::exception& e) {
+        rc = fail(GBVR_EINVAL, e.what());
+      }
       lk.lock();
       if (rc != GBVR_OK) {
         s->worker_error = g_err;

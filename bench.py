@@ -140,16 +140,15 @@ def cpu_sample(wl, vol, view, proj, seconds, threads, rng_seed):
 def run_reference(args):
     """The reference's CPU implementation of the path (the FP64 oracle port:
     Tuvok's raycaster is unbuildable here), all host threads, per step a
-    bounded pixel sample of view 0 of the same workload."""
+    bounded pixel sample of view 0 of the same workload.  Nothing of the GPU
+    library is imported or loaded on this arm: the scene (volume parameters,
+    TF, cameras) comes from oracle.scenes, the cameras from the oracle's own
+    FP64 camera code."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
-    import numpy as np
-    from imagevis3d_gb300 import workloads
-    from oracle import orc
-    wl = workloads.config2(nviews=64)
-    # the input volume from the CPU generator (bit-identical to the GPU one):
-    # nothing of the GPU library runs on this arm
+    from oracle import orc, scenes
+    wl = scenes.config2(size=args.size, nviews=64)
     vol = orc.synth_blobs(wl.synth)
     threads = orc.max_threads()
     view, proj = wl.views[0]
@@ -175,7 +174,7 @@ def run_reference(args):
         "gsamples_per_s": statistics.mean(srates) / 1e9,
         "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
                          "sample": "seeded pixel subsets of view 0, %.1f s of CPU work per step, "
-                                   "frames/s = pixels/s / (1920*1080)" % per},
+                                   "frames/s = pixels/s / (%d*%d)" % (per, wl.width, wl.height)},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))

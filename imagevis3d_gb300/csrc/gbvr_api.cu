@@ -9,6 +9,8 @@
 
 #include <algorithm>
 #include <array>
+#include <climits>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -22,6 +24,7 @@
 #include "abi_guard.h"
 #include "gbvr_internal.h"
 #include "lz4.h"
+#include "synth_tables.h"
 #include "uvf.h"
 
 #include <thread>
@@ -157,43 +160,29 @@ void philox_host(uint32_t c[4], uint32_t k0, uint32_t k1) {
 
 // Per-axis blob / background tables of a synthetic volume (host math, double,
 // rounded to float): the device kernel then combines them in a fixed float32
-// order.
+// order.  One flat array (fill_blob_tables), split here into the uploads.
 struct BlobTablesHost {
   std::vector<float> amp, ex, ey, ez, bgx, bgy, bgz;
 };
 
 void make_blob_tables(const gbvr_synth_params& p, BlobTablesHost& t) {
-  const uint32_t k0 = p.seed, k1 = 0x70617261u;
-  const int nb = p.nblobs;
-  const long long dims[3] = {p.dims[0], p.dims[1], p.dims[2]};
-  t.amp.resize(nb);
-  std::vector<float>* tabs[3] = {&t.ex, &t.ey, &t.ez};
-  for (int a = 0; a < 3; ++a) tabs[a]->resize((size_t)nb * dims[a]);
-  for (int k = 0; k < nb; ++k) {
-    uint32_t c0[4] = {(uint32_t)k, 0u, 0x626c6f62u, 0u}, c1[4] = {(uint32_t)k, 1u, 0x626c6f62u, 0u};
-    philox_host(c0, k0, k1);
-    philox_host(c1, k0, k1);
-    double cen[3];
-    for (int a = 0; a < 3; ++a) cen[a] = (double)(c0[a] >> 8) / 16777216.0 * (double)dims[a];
-    double sig = p.sigma_lo + (double)(c1[0] >> 8) / 16777216.0 * ((double)p.sigma_hi - p.sigma_lo);
-    double am = p.amp_lo + (double)(c1[1] >> 8) / 16777216.0 * ((double)p.amp_hi - p.amp_lo);
-    t.amp[k] = (float)am;
-    for (int a = 0; a < 3; ++a)
-      for (long long i = 0; i < dims[a]; ++i) {
-        double dd = (double)i - cen[a];
-        (*tabs[a])[(size_t)k * dims[a] + i] = (float)std::exp(-(dd * dd) / (2.0 * sig * sig));
-      }
-  }
-  if (p.bg_freq > 0) {
-    uint32_t c[4] = {0xffffffffu, 2u, 0x626c6f62u, 0u};
-    philox_host(c, k0, k1);
-    std::vector<float>* bt[3] = {&t.bgx, &t.bgy, &t.bgz};
-    for (int a = 0; a < 3; ++a) {
-      double ph = (double)(c[a] >> 8) / 16777216.0;
-      bt[a]->resize(dims[a]);
-      for (long long i = 0; i < dims[a]; ++i)
-        (*bt[a])[i] = (float)std::cos(2.0 * M_PI * ((double)p.bg_freq * ((double)i + 0.5) / (double)dims[a] + ph));
-    }
+  const size_t nb = (size_t)p.nblobs, X = (size_t)p.dims[0], Y = (size_t)p.dims[1], Z = (size_t)p.dims[2];
+  const size_t bg = p.bg_freq > 0 ? X + Y + Z : 0;
+  std::vector<float> flat(nb * (1 + X + Y + Z) + bg);
+  fill_blob_tables(p, flat.data());
+  const float* q = flat.data();
+  auto take = [&](std::vector<float>& v, size_t n) {
+    v.assign(q, q + n);
+    q += n;
+  };
+  take(t.amp, nb);
+  take(t.ex, nb * X);
+  take(t.ey, nb * Y);
+  take(t.ez, nb * Z);
+  if (bg) {
+    take(t.bgx, X);
+    take(t.bgy, Y);
+    take(t.bgz, Z);
   }
 }
 
@@ -897,8 +886,7 @@ int classify_level(const Dataset& ds, int level, const std::vector<float>& tf, i
 // Generate a seeded blob volume into a new device buffer (tables built on
 // the host, combined on the device in a fixed float32 order).
 int synth_to_device(const gbvr_synth_params* p, DevBuf& lv, cudaStream_t s) {
-  if (!p || p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 || p->nblobs < 0)
-    return fail(GBVR_EINVAL, "bad synthetic parameters");
+  TRY(check_synth_params(p, true, nullptr, nullptr));
   BlobTablesHost t;
   make_blob_tables(*p, t);
   DevBuf amp, ex, ey, ez, bx, by, bz;
@@ -1046,6 +1034,66 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
 
 namespace gbvr {
 int set_error(int code, const std::string& msg) { return fail(code, msg); }
+
+int check_synth_params(const gbvr_synth_params* p, bool whole_volume, long long* table_floats, size_t* volume_bytes) {
+  if (!p) return fail(GBVR_EINVAL, "null synthetic parameters");
+  if (p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2)
+    return fail(GBVR_EINVAL, "bad synthetic parameters (dims must be positive, dtype 0, 1 or 2)");
+  if (p->nblobs < 0 || p->nblobs > kMaxSynthBlobs)
+    return fail(GBVR_EINVAL, "nblobs must lie in [0, " + std::to_string(kMaxSynthBlobs) +
+                                 "] (the generator keeps a row of blob weights in 48 KiB of shared memory)");
+  const unsigned long long X = (unsigned long long)p->dims[0], Y = (unsigned long long)p->dims[1],
+                           Z = (unsigned long long)p->dims[2];
+  if (Y > 0x7fffffffull) return fail(GBVR_EINVAL, "dims[1] must be below 2^31 (one block per row)");
+  if (whole_volume && Z > 65535) return fail(GBVR_EINVAL, "dims[2] must be at most 65535 (one block row per plane)");
+  unsigned long long vox = 0, bytes = 0, axes = 0, tab = 0;
+  if (__builtin_mul_overflow(X, Y, &vox) || __builtin_mul_overflow(vox, Z, &vox) ||
+      __builtin_mul_overflow(vox, (unsigned long long)dtype_size(p->dtype), &bytes) || bytes > (unsigned long long)SIZE_MAX)
+    return fail(GBVR_EINVAL, "the volume's byte count overflows");
+  // each axis is below 2^63 and their product fits 64 bits, so at most one
+  // axis exceeds 2^32 and 1 + X + Y + Z cannot wrap
+  axes = 1 + X + Y + Z;
+  if (__builtin_mul_overflow((unsigned long long)p->nblobs, axes, &tab) ||
+      __builtin_add_overflow(tab, p->bg_freq > 0 ? X + Y + Z : 0ull, &tab) || tab > (unsigned long long)LLONG_MAX)
+    return fail(GBVR_EINVAL, "the generator tables' size overflows");
+  if (table_floats) *table_floats = (long long)tab;
+  if (volume_bytes) *volume_bytes = (size_t)bytes;
+  return GBVR_OK;
+}
+
+void fill_blob_tables(const gbvr_synth_params& p, float* t) {
+  const uint32_t k0 = p.seed, k1 = 0x70617261u;
+  const long long nb = p.nblobs;
+  const long long dims[3] = {p.dims[0], p.dims[1], p.dims[2]};
+  float* amp = t;
+  float* tab[3] = {t + nb, t + nb + nb * dims[0], t + nb + nb * (dims[0] + dims[1])};
+  for (long long k = 0; k < nb; ++k) {
+    uint32_t c0[4] = {(uint32_t)k, 0u, 0x626c6f62u, 0u}, c1[4] = {(uint32_t)k, 1u, 0x626c6f62u, 0u};
+    philox_host(c0, k0, k1);
+    philox_host(c1, k0, k1);
+    double cen[3];
+    for (int a = 0; a < 3; ++a) cen[a] = (double)(c0[a] >> 8) / 16777216.0 * (double)dims[a];
+    double sig = p.sigma_lo + (double)(c1[0] >> 8) / 16777216.0 * ((double)p.sigma_hi - p.sigma_lo);
+    double am = p.amp_lo + (double)(c1[1] >> 8) / 16777216.0 * ((double)p.amp_hi - p.amp_lo);
+    amp[k] = (float)am;
+    for (int a = 0; a < 3; ++a)
+      for (long long i = 0; i < dims[a]; ++i) {
+        double dd = (double)i - cen[a];
+        tab[a][k * dims[a] + i] = (float)std::exp(-(dd * dd) / (2.0 * sig * sig));
+      }
+  }
+  if (p.bg_freq > 0) {
+    uint32_t c[4] = {0xffffffffu, 2u, 0x626c6f62u, 0u};
+    philox_host(c, k0, k1);
+    float* bg = t + nb * (1 + dims[0] + dims[1] + dims[2]);
+    for (int a = 0; a < 3; ++a) {
+      double ph = (double)(c[a] >> 8) / 16777216.0;
+      for (long long i = 0; i < dims[a]; ++i)
+        bg[i] = (float)std::cos(2.0 * M_PI * ((double)p.bg_freq * ((double)i + 0.5) / (double)dims[a] + ph));
+      bg += dims[a];
+    }
+  }
+}
 }  // namespace gbvr
 
 // ---------------------------------------------------------------------------
@@ -2418,7 +2466,8 @@ int gbvr_load_synthetic(gbvr_renderer* r, const gbvr_synth_params* p, const gbvr
 int gbvr_synth_volume(const gbvr_synth_params* p, void* host_out, size_t bytes) {
   GBVR_ABI_TRY
   if (!p || !host_out) return fail(GBVR_EINVAL, "null argument");
-  const size_t need = (size_t)p->dims[0] * p->dims[1] * p->dims[2] * dtype_size(p->dtype);
+  size_t need = 0;
+  TRY(check_synth_params(p, true, nullptr, &need));
   if (bytes < need) return fail(GBVR_EINVAL, "output buffer too small");
   gbvr_renderer tmp;
   CUDA_TRY(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking));
@@ -2496,8 +2545,7 @@ int gbvr_load_synthetic_ooc(gbvr_renderer* r, const gbvr_synth_params* p, const 
                             uint64_t device_pool_bytes) {
   GBVR_ABI_TRY
   TRY(check_r(r));
-  if (!p || p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 || p->nblobs < 0)
-    return fail(GBVR_EINVAL, "bad synthetic parameters");
+  TRY(check_synth_params(p, false, nullptr, nullptr));
   r->drop_graphs();
   r->skip_dirty = true;
   r->tf_dirty = true;

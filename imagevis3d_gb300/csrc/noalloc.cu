@@ -12,7 +12,6 @@
 // every GPU that loads this library holds until the process exits.
 #include <cuda_runtime.h>
 
-#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -20,6 +19,7 @@
 #include "../../include/gbvr.h"
 #include "abi_guard.h"
 #include "gbvr_internal.h"
+#include "synth_tables.h"
 
 namespace gbvr {
 int set_error(int code, const std::string& msg);
@@ -36,97 +36,76 @@ namespace {
 
 std::mutex g_mu;
 constexpr int kMaxDevices = 64;
-float* g_scratch_dev[kMaxDevices] = {nullptr};  // device address of g_synth_scratch, per device
+struct DeviceSetup {
+  float* scratch = nullptr;     // device address of g_synth_scratch on this device
+  cudaEvent_t copied = nullptr; // recorded after the last table copy queued on this device
+  bool pending = false;         // a copy from g_tables_host may still be reading it
+};
+DeviceSetup g_dev[kMaxDevices];
 // Host staging for the tables: static, so the call allocates no host heap
-// either.  Guarded by g_mu.
+// either.  Guarded by g_mu; refilled only after the copy that last read it
+// has completed (its event).
 float g_tables_host[kSynthScratchFloats];
-
-void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
-  for (int r = 0; r < 10; ++r) {
-    uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
-    uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
-    c[0] = n0; c[1] = (uint32_t)p1; c[2] = n2; c[3] = (uint32_t)p0;
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
-  }
-}
-
-// The generator's tables, the same draws and the same double-precision math
-// as the allocating entry points, written into `t` as
-// amp[nb] | ex[nb X] | ey[nb Y] | ez[nb Z] | bgx[X] | bgy[Y] | bgz[Z].
-void fill_tables(const gbvr_synth_params& p, float* t) {
-  const uint32_t k0 = p.seed, k1 = 0x70617261u;
-  const int nb = p.nblobs;
-  const long long d[3] = {p.dims[0], p.dims[1], p.dims[2]};
-  float* amp = t;
-  float* tab[3] = {t + nb, t + nb + (long long)nb * d[0], t + nb + (long long)nb * (d[0] + d[1])};
-  for (int k = 0; k < nb; ++k) {
-    uint32_t c0[4] = {(uint32_t)k, 0u, 0x626c6f62u, 0u}, c1[4] = {(uint32_t)k, 1u, 0x626c6f62u, 0u};
-    philox(c0, k0, k1);
-    philox(c1, k0, k1);
-    double cen[3];
-    for (int a = 0; a < 3; ++a) cen[a] = (double)(c0[a] >> 8) / 16777216.0 * (double)d[a];
-    double sig = p.sigma_lo + (double)(c1[0] >> 8) / 16777216.0 * ((double)p.sigma_hi - p.sigma_lo);
-    double am = p.amp_lo + (double)(c1[1] >> 8) / 16777216.0 * ((double)p.amp_hi - p.amp_lo);
-    amp[k] = (float)am;
-    for (int a = 0; a < 3; ++a)
-      for (long long i = 0; i < d[a]; ++i) {
-        double dd = (double)i - cen[a];
-        tab[a][(long long)k * d[a] + i] = (float)std::exp(-(dd * dd) / (2.0 * sig * sig));
-      }
-  }
-  if (p.bg_freq > 0) {
-    uint32_t c[4] = {0xffffffffu, 2u, 0x626c6f62u, 0u};
-    philox(c, k0, k1);
-    float* bg = t + nb + (long long)nb * (d[0] + d[1] + d[2]);
-    for (int a = 0; a < 3; ++a) {
-      double ph = (double)(c[a] >> 8) / 16777216.0;
-      for (long long i = 0; i < d[a]; ++i)
-        bg[i] = (float)std::cos(2.0 * M_PI * ((double)p.bg_freq * ((double)i + 0.5) / (double)d[a] + ph));
-      bg += d[a];
-    }
-  }
-}
 
 }  // namespace
 
 extern "C" int gbvr_dev_synth_volume_noalloc(const gbvr_synth_params* p, void* dev_out, size_t bytes, void* stream) {
   GBVR_ABI_TRY
   if (!p || !dev_out) return set_error(GBVR_EINVAL, "null argument");
-  if (p->dims[0] <= 0 || p->dims[1] <= 0 || p->dims[2] <= 0 || p->dtype < 0 || p->dtype > 2 || p->nblobs < 0)
-    return set_error(GBVR_EINVAL, "bad synthetic parameters");
-  const long long X = p->dims[0], Y = p->dims[1], Z = p->dims[2];
-  const long long need = (long long)p->nblobs * (1 + X + Y + Z) + (p->bg_freq > 0 ? X + Y + Z : 0);
+  long long need = 0;
+  size_t out_bytes = 0;
+  int rc = check_synth_params(p, true, &need, &out_bytes);
+  if (rc != GBVR_OK) return rc;
   if (need > kSynthScratchFloats)
     return set_error(GBVR_EINVAL, "the generator tables need " + std::to_string(need) +
                                       " floats; the no-allocation entry point holds at most " +
                                       std::to_string(kSynthScratchFloats) +
                                       " (nblobs x (1 + X + Y + Z) + X + Y + Z)");
-  const size_t out_bytes = (size_t)X * Y * Z * dtype_size(p->dtype);
   if (bytes < out_bytes) return set_error(GBVR_EINVAL, "output buffer too small");
   cudaStream_t s = (cudaStream_t)stream;
+  // a captured copy would read the static host tables when the graph is
+  // replayed, by then holding another call's parameters
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cap);
+  if (e != cudaSuccess) return set_error(GBVR_ECUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+  if (cap != cudaStreamCaptureStatusNone)
+    return set_error(GBVR_EINVAL, "gbvr_dev_synth_volume_noalloc cannot be called while its stream is being captured");
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return set_error(GBVR_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return set_error(GBVR_EINVAL, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_dev[dev]) {
+  DeviceSetup& ds = g_dev[dev];
+  if (!ds.scratch) {
     // Set-up, once per device, with that device current: resolve the device
     // address of the scratch array (the first call on a device also loads
-    // the library's device code there).
+    // the library's device code there) and create the copy event.
     void* ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_synth_scratch);
     if (e != cudaSuccess) return set_error(GBVR_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_scratch_dev[dev] = (float*)ptr;
+    cudaEvent_t ev = nullptr;
+    e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return set_error(GBVR_ECUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e));
+    ds.copied = ev;
+    ds.scratch = (float*)ptr;
   }
-  float* dt = g_scratch_dev[dev];
+  float* dt = ds.scratch;
   if (need > 0) {
-    fill_tables(*p, g_tables_host);
-    // from pageable memory: returns once the source has been staged, so the
-    // static host tables may be refilled by the next call
+    // the previous table copy (on any device) must have read the host staging
+    for (int d = 0; d < kMaxDevices; ++d)
+      if (g_dev[d].pending) {
+        e = cudaEventSynchronize(g_dev[d].copied);
+        if (e != cudaSuccess) return set_error(GBVR_ECUDA, std::string("cudaEventSynchronize: ") + cudaGetErrorString(e));
+        g_dev[d].pending = false;
+      }
+    fill_blob_tables(*p, g_tables_host);
     e = cudaMemcpyAsync(dt, g_tables_host, sizeof(float) * (size_t)need, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return set_error(GBVR_ECUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    e = cudaEventRecord(ds.copied, s);
+    if (e != cudaSuccess) return set_error(GBVR_ECUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
+    ds.pending = true;
   }
+  const long long X = p->dims[0], Y = p->dims[1], Z = p->dims[2];
   const int nb = p->nblobs;
   const bool bg = p->bg_freq > 0;
   float* bgt = dt + nb + (long long)nb * (X + Y + Z);

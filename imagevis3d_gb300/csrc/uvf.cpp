@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -22,11 +23,13 @@ static const int md5_r[64] = {7, 12, 17, 22, 7, 12, 17, 22, 7, 12, 17, 22, 7, 12
                               5, 9,  14, 20, 5, 9,  14, 20, 5, 9,  14, 20, 5, 9,  14, 20,
                               4, 11, 16, 23, 4, 11, 16, 23, 4, 11, 16, 23, 4, 11, 16, 23,
                               6, 10, 15, 21, 6, 10, 15, 21, 6, 10, 15, 21, 6, 10, 15, 21};
-static bool md5_init_done = false;
+static std::once_flag md5_once;
+// Filled once, by whichever thread opens or writes a UVF file first.
 static void md5_init_table() {
-  if (md5_init_done) return;
-  for (int i = 0; i < 64; ++i) md5_k[i] = (uint32_t)(uint64_t)std::floor(std::fabs(std::sin((double)(i + 1))) * 4294967296.0);
-  md5_init_done = true;
+  std::call_once(md5_once, [] {
+    for (int i = 0; i < 64; ++i)
+      md5_k[i] = (uint32_t)(uint64_t)std::floor(std::fabs(std::sin((double)(i + 1))) * 4294967296.0);
+  });
 }
 
 static inline uint32_t rotl(uint32_t x, int c) { return (x << c) | (x >> (32 - c)); }

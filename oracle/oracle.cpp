@@ -1127,4 +1127,77 @@ void orc_raster_tf2d(const orc_swatch* sw, int ns, const float* tf1d, int n1d, i
     }
 }
 
+// ---------------------------------------------------------------------------
+// Cameras, restated in FP64 for the CPU reference arm and as an independent
+// check of the library's camera code: the look-at view matrix and the OpenGL
+// perspective projection (gluLookAt / gluPerspective, row-major, column
+// vectors), and the orbit of the 360-degree capture
+// (ImageVis3D/UI/ImageVis3D_Capturing.cpp:170: angle i / N * 360 about +y;
+// RenderWindow.cpp:207-214) at an elevation above the xz plane, looking at
+// the volume centre, clip planes one unit either side of the centre's depth.
+// Results are rounded to float32 once, at the end.
+// ---------------------------------------------------------------------------
+static void cam_look_at(const double eye[3], const double at[3], const double up[3], double V[16]) {
+  double fwd[3], side[3], upv[3];
+  for (int i = 0; i < 3; ++i) fwd[i] = at[i] - eye[i];
+  const double fn = std::sqrt(fwd[0] * fwd[0] + fwd[1] * fwd[1] + fwd[2] * fwd[2]);
+  for (double& v : fwd) v /= fn;
+  side[0] = fwd[1] * up[2] - fwd[2] * up[1];
+  side[1] = fwd[2] * up[0] - fwd[0] * up[2];
+  side[2] = fwd[0] * up[1] - fwd[1] * up[0];
+  const double sn = std::sqrt(side[0] * side[0] + side[1] * side[1] + side[2] * side[2]);
+  for (double& v : side) v /= sn;
+  upv[0] = side[1] * fwd[2] - side[2] * fwd[1];
+  upv[1] = side[2] * fwd[0] - side[0] * fwd[2];
+  upv[2] = side[0] * fwd[1] - side[1] * fwd[0];
+  const double* axes[3] = {side, upv, fwd};
+  for (int r = 0; r < 3; ++r) {
+    const double sg = r == 2 ? -1.0 : 1.0;  // the camera looks down -z
+    double dot = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      V[4 * r + k] = sg * axes[r][k];
+      dot += V[4 * r + k] * eye[k];
+    }
+    V[4 * r + 3] = -dot;
+  }
+  V[12] = V[13] = V[14] = 0.0;
+  V[15] = 1.0;
+}
+
+static void cam_perspective(double fovy_deg, double aspect, double zn, double zf, double P[16]) {
+  const double f = 1.0 / std::tan(fovy_deg * M_PI / 360.0);
+  for (int i = 0; i < 16; ++i) P[i] = 0.0;
+  P[0] = f / aspect;
+  P[5] = f;
+  P[10] = (zf + zn) / (zn - zf);
+  P[11] = 2.0 * zf * zn / (zn - zf);
+  P[14] = -1.0;
+}
+
+void orc_orbit_camera(double az_deg, double el_deg, double radius, double fov_deg, int w, int h, float view[16],
+                      float proj[16]) {
+  const double az = az_deg * M_PI / 180.0, el = el_deg * M_PI / 180.0;
+  const double eye[3] = {radius * std::cos(el) * std::sin(az), radius * std::sin(el),
+                         radius * std::cos(el) * std::cos(az)};
+  const double at[3] = {0.0, 0.0, 0.0}, up[3] = {0.0, 1.0, 0.0};
+  double V[16], P[16];
+  cam_look_at(eye, at, up, V);
+  cam_perspective(fov_deg, (double)w / (double)h, std::max(0.01, radius - 2.0), radius + 2.0, P);
+  for (int i = 0; i < 16; ++i) {
+    view[i] = (float)V[i];
+    proj[i] = (float)P[i];
+  }
+}
+
+void orc_look_at_camera(const double eye[3], const double at[3], const double up[3], double fov_deg, double zn,
+                        double zf, int w, int h, float view[16], float proj[16]) {
+  double V[16], P[16];
+  cam_look_at(eye, at, up, V);
+  cam_perspective(fov_deg, (double)w / (double)h, zn, zf, P);
+  for (int i = 0; i < 16; ++i) {
+    view[i] = (float)V[i];
+    proj[i] = (float)P[i];
+  }
+}
+
 }  // extern "C"

@@ -287,6 +287,32 @@ def max_threads():
     return lib().orc_max_threads()
 
 
+def orbit_camera(azimuth_deg, elevation_deg, radius, fov_deg, width, height):
+    """FP64 orbit camera (orc_orbit_camera), rounded to float32 row-major
+    (view, proj) as the library takes them.  The angles, radius and field of
+    view are float32 numbers, as the library's camera call receives them."""
+    v = np.zeros(16, np.float32)
+    p = np.zeros(16, np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    f32 = lambda x: D(float(np.float32(x)))
+    lib().orc_orbit_camera(f32(azimuth_deg), f32(elevation_deg), f32(radius), f32(fov_deg), int(width), int(height),
+                           fp(v), fp(p))
+    return v.reshape(4, 4), p.reshape(4, 4)
+
+
+def look_at_camera(eye, ref, up, fov_deg, znear, zfar, width, height):
+    """FP64 look-at camera (orc_look_at_camera), rounded to float32; inputs
+    are float32 numbers, as the library's camera call receives them."""
+    v = np.zeros(16, np.float32)
+    p = np.zeros(16, np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    f32 = lambda x: D(float(np.float32(x)))
+    d3 = lambda a: (D * 3)(*[float(np.float32(x)) for x in a])
+    lib().orc_look_at_camera(d3(eye), d3(ref), d3(up), f32(fov_deg), f32(znear), f32(zfar), int(width), int(height),
+                             fp(v), fp(p))
+    return v.reshape(4, 4), p.reshape(4, 4)
+
+
 def synth_fbm(params):
     """CPU restatement of the seeded fractal generator (gbvr_fbm_params)."""
     dims = [params.dims[i] for i in range(3)]

@@ -7,7 +7,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = "/root/reference"
+# Root of an ImageVis3D source tree (for the one test that reads the
+# reference's own DemoData/c60.uvf); unset: that test is skipped.  The other
+# parity tests use the fixtures under tests/golden/.
+REFERENCE = os.environ.get("IMAGEVIS3D_REFERENCE", "")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
@@ -29,7 +32,9 @@ def orc():
 
 
 def reference_file(rel):
+    if not REFERENCE:
+        pytest.skip("IMAGEVIS3D_REFERENCE (an ImageVis3D source tree) is not set")
     p = os.path.join(REFERENCE, rel)
     if not os.path.exists(p):
-        pytest.skip("reference tree not present (only in the build container)")
+        pytest.skip("%s is not in the ImageVis3D tree at IMAGEVIS3D_REFERENCE" % rel)
     return p

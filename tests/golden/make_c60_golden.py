@@ -1,7 +1,7 @@
 """Generate the c60 golden fixture from the reference's own demo dataset.
 
 Reads ``DemoData/c60.uvf``, ``DemoData/c60.1dt`` and ``DemoData/c60.2dt`` from the
-reference tree (path given on the command line, default the read-only mount) and
+reference tree (path given on the command line or in IMAGEVIS3D_REFERENCE) and
 writes ``c60.npz`` beside this script.  The fixture holds what the reference's
 UVF writer stored: the 128^3 uint8 voxels, the 256-bin 1D histogram, the
 256x256 2D histogram with its float32 max-gradient, the min/max block, the
@@ -9,6 +9,7 @@ global-header checksum and every header field needed to re-emit the file byte
 for byte.  Tests use it on machines where the reference tree is absent.
 
 Usage: python tests/golden/make_c60_golden.py [REFERENCE_ROOT]
+(REFERENCE_ROOT: an ImageVis3D source tree; default: $IMAGEVIS3D_REFERENCE)
 """
 import hashlib
 import os
@@ -53,7 +54,9 @@ def parse_1dt(text):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("IMAGEVIS3D_REFERENCE", "")
+    if not root:
+        sys.exit("usage: make_c60_golden.py REFERENCE_ROOT (or set IMAGEVIS3D_REFERENCE)")
     demo = os.path.join(root, "DemoData")
     f = open(os.path.join(demo, "c60.uvf"), "rb").read()
     info = parse_blocks(f)

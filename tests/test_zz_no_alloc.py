@@ -48,6 +48,52 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls_in_a_row():
     assert np.array_equal(_host(ga2, a), synth_volume(a))
 
 
+def test_noalloc_allocates_no_device_memory():
+    """The defining property: after the first call on the device (its set-up),
+    further calls leave the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    a = workloads.config1().synth
+    b = synth_params((96, 80, 72), np.uint16, 77, 16, (5.0, 20.0), (0.3, 1.0), 2600.0, noise_kind=2,
+                     noise_amp=20.0, vmax=4095.0, bg_freq=1.0, bg_level=0.15, bg_amp=0.1)
+    outs = []
+    for p in (a, b):  # outputs owned by the caller, allocated before measuring
+        dims = [p.dims[i] for i in range(3)]
+        dt = torch.uint8 if p.dtype == L.GBVR_U8 else torch.int16
+        outs.append(torch.empty((dims[2], dims[1], dims[0]), dtype=dt, device="cuda"))
+
+    def call(p, out):
+        L.call("gbvr_dev_synth_volume_noalloc", C.byref(p), C.c_void_p(out.data_ptr()),
+               out.numel() * out.element_size(), None)
+
+    call(a, outs[0])  # warm-up: set-up on this device, kernel loaded
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        call(a, outs[0])
+        call(b, outs[1])
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert np.array_equal(_host(outs[1], b), synth_volume(b))
+
+
+def test_noalloc_is_refused_during_stream_capture():
+    """A captured call would read the shared host tables at replay time; it
+    is refused, and nothing is queued into the capture."""
+    torch = pytest.importorskip("torch")
+    a = workloads.config1().synth
+    out = torch.empty((128, 128, 128), dtype=torch.uint8, device="cuda")
+    _noalloc(a, torch)  # set-up before any capture
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            rc = L.lib().gbvr_dev_synth_volume_noalloc(C.byref(a), C.c_void_p(out.data_ptr()),
+                                                       out.numel(), C.c_void_p(s.cuda_stream))
+    assert rc == -1 and "captured" in L.last_error()
+
+
 def test_noalloc_rejects_tables_beyond_its_capacity():
     torch = pytest.importorskip("torch")
     big = synth_params((1024, 1024, 1024), np.uint16, 1, 200, (5.0, 20.0), (0.3, 1.0), 2600.0,

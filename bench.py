@@ -181,17 +181,28 @@ def run_reference(args):
     return 0
 
 
-def traffic_from_profile():
-    """DRAM bytes per launch of the persistent kernel from the committed ncu
-    summary, scaled to this workload (see the summary for the capture)."""
-    p = os.path.join(ROOT, "profiles", "raycast_persistent_1024cube_u16.md")
+PROFILE_CSV = os.path.join(ROOT, "profiles", "raycast_persistent_1024cube_u16_8views.ncu.csv")
+
+
+def profile_counters():
+    """Counters of one ncu capture of the persistent raycast kernel on the
+    8-view case of this workload (profiles/*.ncu.csv: the raw page of the
+    capture, base units, reduced to the columns used here).  None when the
+    file is absent.  The bench scales them to its own launch by ratios it
+    measures itself (algorithmic bytes and samples of the same 8 views)."""
+    import csv
     try:
-        for line in open(p):
-            if line.startswith("traffic_bytes_per_launch_full:"):
-                return float(line.split(":")[1])
+        rows = list(csv.reader(open(PROFILE_CSV)))
     except OSError:
-        pass
-    return None
+        return None
+    hdr, vals = rows[0], rows[-1]
+    out = {}
+    for k, v in zip(hdr, vals):
+        try:
+            out[k] = float(v.replace(",", ""))
+        except ValueError:
+            out[k] = v
+    return out
 
 
 def run_c3(args):
@@ -229,9 +240,36 @@ def run_c3(args):
         r.paintViews(wl.views)
         pms.append(r.stats()["gpu_ms"])
     dvr_plain = len(wl.views) * args.steps / (sum(pms) / 1000.0)
+    # error against the FP64 oracle (voxels evaluated on demand from the
+    # fractal's rule): seeded pixel subsets of one view's RGBA8 frame, so the
+    # 8-bit rounding is included
+    from oracle import orc
+    proc = orc.ProceduralFbm(wl.synth)
+    erng = np.random.default_rng(workloads.SEED + 33)
+    errs = {}
+
+    def frame_error(key, view_idx, kw, covered_thr):
+        img = r.readFramebuffer(view_idx).reshape(-1, 4).astype(np.float64) / 255.0
+        cov = np.flatnonzero(img[:, 3] > covered_thr)
+        pix = np.concatenate([erng.choice(cov, min(200, cov.size), replace=False) if cov.size else
+                              np.zeros(0, np.int64), erng.integers(0, img.shape[0], 60)])
+        v, p = wl.views[view_idx]
+        ref, _ = orc.render(proc, v, p, wl.width, wl.height, wl.tf, value_range=wl.value_range, pixels=pix,
+                            threads=orc.max_threads(), **kw)
+        g = np.clip(img[pix], 0, 1)
+        rr = np.clip(ref, 0, 1)
+        if kw.get("mode") == 2:
+            same = (g[:, 3] > 0.5) == (rr[:, 3] > 0.5)  # silhouette rays may hit on one side only
+            errs[key + "_hit_mismatch"] = float(1.0 - same.mean())
+            g, rr = g[same], rr[same]
+        d = np.abs(g - rr)
+        errs[key] = {"max": float(d.max()), "rms": float(np.sqrt((d * d).mean())), "pixels": int(len(g))}
+
+    r.paintBatch(wl.views)
+    frame_error("dvr_2dtf_phong", 0, dict(mode=1, grad_max=info["hist2d_max_grad"] * 0.5), 0.02)
     r.setRenderMode(GBVR_RM_ISOSURFACE)
     iso_fps = []
-    for iso in wl.isovalues:
+    for ii, iso in enumerate(wl.isovalues):
         r.setIsoValue(iso, (0.8, 0.8, 0.9))
         r.paintBatch(wl.views)
         ims = []
@@ -239,6 +277,9 @@ def run_c3(args):
             r.paintBatch(wl.views)
             ims.append(r.stats()["kernel_ms"])
         iso_fps.append(len(wl.views) * args.steps / (sum(ims) / 1000.0))
+        frame_error("iso_%d" % ii, 3, dict(mode=2, iso=iso, iso_rgb=(0.8, 0.8, 0.9)), 0.5)
+    errs["tol_max"], errs["tol_rms"] = 2 / 255, 0.5 / 255
+    errs["note"] = "RGBA8 frames (8-bit rounding included) vs the FP64 oracle, seeded pixel subsets"
     r.cleanup()
     # GPU 2D histogram of the 8 GiB level, device resident
     n = wl.synth.dims[0] * wl.synth.dims[1] * wl.synth.dims[2]
@@ -278,6 +319,7 @@ def run_c3(args):
         "isosurface_fps": dict(zip(["%.1f" % v for v in wl.isovalues], iso_fps)),
         "gsamples_per_s": st["samples"] / (ms[-1] / 1000.0) / 1e9,
         "uvf_build_s": build_s,
+        "image_error_vs_fp64": errs,
         "hist2d": {"ms": hist_ms, "gbps_read_3_passes": 3 * n / (hist_ms / 1000.0) / 1e9,
                    "peak_gbps": pk["hbm_gbs"] if pk else None},
         "autotune": tune,
@@ -445,18 +487,25 @@ def run_c4(args):
     return 0
 
 
-def run_c5(args):
-    """Serving mix: Poisson arrivals of render requests
-    over 12 resident datasets (64^3 .. 1024^3, uint8 / uint16 / float32), image
-    sizes in {256^2, 512^2, 1280x720, 1920x1080}, a random 1D or 2D TF preset
-    and a random camera per request.  Capacity is measured first with a burst;
-    the Poisson stream then runs at 70% of it.  The plain per-request path
-    (one renderer paint + readback per request) is timed on the same requests."""
+def serving_run(nreq, plain_requests, max_batch, err_requests=6, seed_offset=5, slots=3, pool_fraction=0.0):
+    """Serving mix: Poisson arrivals of render requests over 12 resident
+    datasets (64^3 .. 1024^3, uint8 / uint16 / float32), image sizes in
+    {256^2, 512^2, 1280x720, 1920x1080}, a random 1D or 2D TF preset and a
+    random camera per request.  Capacity is measured first with a burst; the
+    Poisson stream then runs at 70% of it.  The plain per-request path (one
+    renderer paint + readback per request) is timed on the same requests.
+    The image error against the FP64 oracle is taken on `err_requests`
+    requests of the datasets up to 384^3 (their RGBA8 images as served, so the
+    8-bit rounding is included).  `slots` batches are in flight at once; the
+    launch shapes come from the server's autotuner; pool_fraction > 0 caps the
+    device brick-pool memory at that fraction of all datasets' pools
+    (admission by memory: pools evicted and uploaded on demand).  Returns a
+    dict."""
     import threading as th
     import numpy as np
     from imagevis3d_gb300 import (GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, Renderer, Server, orbit_camera,
                                   synth_params, workloads)
-    rng = np.random.default_rng(workloads.SEED + 5)
+    rng = np.random.default_rng(workloads.SEED + seed_offset)
     sizes_vol = [64, 96, 128, 192, 256, 320, 384, 512, 640, 768, 896, 1024]
     dtypes = [np.uint8, np.uint16, np.float32]
     specs = []
@@ -466,8 +515,18 @@ def run_c5(args):
         specs.append(synth_params((n, n, n), dt, 500 + i, 24, (0.03 * n, 0.09 * n), (0.3, 1.0), scale,
                                   noise_kind=2, noise_amp=0.02 * scale, vmax=vmax))
     img_sizes = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
-    nreq = args.requests
-    srv = Server(max_batch=args.max_batch, fb_budget_bytes=1 << 30)
+    pools = []
+    if pool_fraction > 0:
+        # the datasets' pool sizes, from an unbudgeted server's resident bytes
+        with Server(max_batch=max_batch, fb_budget_bytes=64 << 20, slots=1) as probe:
+            prev = 0
+            for sp in specs:
+                probe.add_synthetic(sp, brick_size=256, overlap=2, layouts=1)
+                cur = probe.stats()["resident_bytes"]
+                pools.append(cur - prev)
+                prev = cur
+    budget = max(max(pools), int(pool_fraction * sum(pools))) if pools else 0
+    srv = Server(max_batch=max_batch, fb_budget_bytes=1 << 30, slots=slots, device_pool_bytes=budget)
     ds, presets = [], []
     for i, sp in enumerate(specs):
         d = srv.add_synthetic(sp, brick_size=256, overlap=2, layouts=1)
@@ -486,8 +545,8 @@ def run_c5(args):
                            float(rng.uniform(1.8, 3.0)) * workloads.DIAG, 45.0, w, h)
         reqs.append((di, pi, w, h, cam))
 
-    def run_stream(arrivals):
-        tickets, done = [], []
+    def run_stream(arrivals, outs=None):
+        tickets = []
         q = []
         lock = th.Lock()
         finished = th.Event()
@@ -496,10 +555,7 @@ def run_c5(args):
             k = 0
             while k < len(arrivals):
                 with lock:
-                    if k >= len(q):
-                        t = None
-                    else:
-                        t = q[k]
+                    t = q[k] if k < len(q) else None
                 if t is None:
                     time.sleep(0.0002)
                     continue
@@ -509,16 +565,18 @@ def run_c5(args):
         wt = th.Thread(target=waiter, daemon=True)
         wt.start()
         t0 = time.perf_counter()
-        for (di, pi, w, h, cam), ta in zip(reqs, arrivals):
+        for j, ((di, pi, w, h, cam), ta) in enumerate(zip(reqs, arrivals)):
             delay = ta - (time.perf_counter() - t0)
             if delay > 0:
                 time.sleep(delay)
-            t = srv.submit(ds[di], presets[di][pi][0], w, h, cam[0], cam[1])
+            out = outs[j] if outs is not None and j in outs else None
+            t = srv.submit(ds[di], presets[di][pi][0], w, h, cam[0], cam[1], out=out)
             with lock:
                 q.append(t)
         finished.wait()
         return time.perf_counter() - t0
 
+    tune = srv.autotune(512, 512, 16)
     # warm-up and capacity (burst)
     srv.reset_stats()
     run_stream([0.0] * min(200, nreq))
@@ -526,53 +584,107 @@ def run_c5(args):
     wall = run_stream([0.0] * nreq)
     burst = srv.stats()
     capacity = burst["completed"] / wall
-    # Poisson arrivals at 70% of capacity
+    # Poisson arrivals at 70% of capacity; the images of a few small requests kept for the error check
     rate = 0.7 * capacity
     arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq)).tolist()
+    err_idx = [j for j, rq in enumerate(reqs) if sizes_vol[rq[0]] <= 384][:err_requests]
+    outs = {j: np.zeros((reqs[j][3], reqs[j][2], 4), np.uint8) for j in err_idx}
     srv.reset_stats()
-    wall = run_stream(arrivals)
+    wall = run_stream(arrivals, outs)
     st = srv.stats()
     srv.close()
     # plain per-request path: one renderer per dataset, paint + readback
-    rends = []
-    for i, sp in enumerate(specs):
-        r = Renderer()
-        r.loadSynthetic(sp, brick_size=256, overlap=2)
-        rends.append(r)
-    sample = reqs[:min(len(reqs), args.plain_requests)]
-    lat = []
-    t0 = time.perf_counter()
-    for di, pi, w, h, cam in sample:
-        t1 = time.perf_counter()
-        r = rends[di]
-        _, mode, tf = presets[di][pi]
-        r.resize((w, h))
-        r.setRenderMode(mode)
-        if mode == GBVR_RM_1DTRANS:
-            r.set1DTrans(tf)
-        else:
-            r.set2DTrans(tf, 0.05)
-        r.setView(*cam)
-        r.paint()
-        r.readFramebuffer(0)
-        lat.append((time.perf_counter() - t1) * 1000.0)
-    plain_fps = len(sample) / (time.perf_counter() - t0)
-    for r in rends:
-        r.cleanup()
-    lat.sort()
+    plain_fps, lat = None, []
+    if plain_requests > 0:
+        rends = []
+        for i, sp in enumerate(specs):
+            r = Renderer()
+            r.loadSynthetic(sp, brick_size=256, overlap=2)
+            rends.append(r)
+        sample = reqs[:min(len(reqs), plain_requests)]
+        t0 = time.perf_counter()
+        for di, pi, w, h, cam in sample:
+            t1 = time.perf_counter()
+            r = rends[di]
+            _, mode, tf = presets[di][pi]
+            r.resize((w, h))
+            r.setRenderMode(mode)
+            if mode == GBVR_RM_1DTRANS:
+                r.set1DTrans(tf)
+            else:
+                r.set2DTrans(tf, 0.05)
+            r.setView(*cam)
+            r.paint()
+            r.readFramebuffer(0)
+            lat.append((time.perf_counter() - t1) * 1000.0)
+        plain_fps = len(sample) / (time.perf_counter() - t0)
+        for r in rends:
+            r.cleanup()
+        lat.sort()
+    # error of served images against the FP64 oracle (pixel subsets; the
+    # servers's default value range: [0, max] for integers, [min, max] for float32)
+    err = None
+    if err_idx:
+        from oracle import orc
+        worst_max, sq, n = 0.0, 0.0, 0
+        vols = {}
+        prng = np.random.default_rng(workloads.SEED + 55)
+        for j in err_idx:
+            di, pi, w, h, cam = reqs[j]
+            if di not in vols:
+                vols[di] = orc.synth_blobs(specs[di])
+            vol = vols[di]
+            _, mode, tf = presets[di][pi]
+            vr = (float(vol.min()), float(vol.max())) if vol.dtype == np.float32 else (0.0, max(1.0, float(vol.max())))
+            img = outs[j].reshape(-1, 4).astype(np.float64) / 255.0
+            cov = np.flatnonzero(img[:, 3] > 0.02)
+            pix = np.concatenate([prng.choice(cov, min(300, cov.size), replace=False) if cov.size else
+                                  np.zeros(0, np.int64), prng.integers(0, w * h, 100)])
+            kw = dict(mode=1, grad_max=0.05) if mode == GBVR_RM_2DTRANS else dict(mode=0)
+            ref, _ = orc.render(vol, cam[0], cam[1], w, h, tf, value_range=vr, pixels=pix, **kw)
+            d = np.abs(np.clip(img[pix], 0, 1) - np.clip(ref, 0, 1))
+            worst_max = max(worst_max, float(d.max()))
+            sq += float((d * d).sum())
+            n += d.size
+        err = {"max": worst_max, "rms": math.sqrt(sq / n), "requests": len(err_idx),
+               "pixels": n // 4, "tol_max": 2 / 255, "tol_rms": 0.5 / 255,
+               "note": "RGBA8 images as served (8-bit rounding included), seeded pixel subsets"}
+    return {
+        "frames_per_s": st["frames_per_s"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+        "mean_batch": st["mean_batch"], "requests": nreq, "arrival_rate_per_s": rate,
+        "burst_capacity_fps": capacity, "burst_p99_ms": burst["p99_ms"], "plain_per_request_fps": plain_fps,
+        "plain_p50_ms": lat[len(lat) // 2] if lat else None,
+        "plain_p99_ms": lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))] if lat else None,
+        "serving_vs_plain": capacity / plain_fps if plain_fps else None, "max_batch": max_batch, "image_error_vs_fp64": err,
+        "slots": slots, "batches": st["batches"], "overlapped_batch_pairs": st["overlapped"],
+        "checked_batch_pairs": st["overlap_checked"], "burst_overlapped_pairs": burst["overlapped"],
+        "device_pool_bytes": budget, "pool_uploads": st["uploads"], "pool_evictions": st["evictions"],
+        "pool_upload_bytes": st["upload_bytes"], "all_pools_bytes": sum(pools) if pools else None,
+        "autotune": tune,
+    }
+
+
+def run_c5(args):
+    """Serving mix at full length (10k requests by default); prints one JSON line of its own."""
+    sv = serving_run(args.requests, args.plain_requests, args.max_batch, slots=args.slots)
+    # the same stream under a brick-pool budget of half the datasets' pools
+    svm = serving_run(min(args.requests, 2000), 0, args.max_batch, err_requests=0, slots=args.slots,
+                      pool_fraction=0.5) if args.pool_pass else None
     out = {
         "metric": "serving frames/s & p50/p99 latency (Poisson arrivals, continuous batching)",
-        "value": st["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": nreq, "warmup": 200,
-        "ms_per_step": 1000.0 / max(st["frames_per_s"], 1e-9), "higher_is_better": True, "scaling": "weak",
+        "value": sv["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "steps": args.requests, "warmup": 200,
+        "ms_per_step": 1000.0 / max(sv["frames_per_s"], 1e-9), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded blob volumes)",
-        "config": {"workload": "c5_serving_12_datasets_%d_requests" % nreq, "datasets": "64^3..1024^3 u8/u16/f32",
-                   "image_sizes": img_sizes, "arrival_rate_per_s": rate, "max_batch": args.max_batch},
-        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"], "mean_batch": st["mean_batch"],
-        "burst_capacity_fps": capacity, "burst_p99_ms": burst["p99_ms"],
-        "plain_per_request_fps": plain_fps, "plain_p50_ms": lat[len(lat) // 2],
-        "plain_p99_ms": lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))],
-        "serving_vs_plain": capacity / plain_fps,
+        "config": {"workload": "c5_serving_12_datasets_%d_requests" % args.requests,
+                   "datasets": "64^3..1024^3 u8/u16/f32",
+                   "image_sizes": [(256, 256), (512, 512), (1280, 720), (1920, 1080)],
+                   "arrival_rate_per_s": sv["arrival_rate_per_s"], "max_batch": args.max_batch},
     }
+    out.update({k: v for k, v in sv.items() if k not in ("frames_per_s", "arrival_rate_per_s")})
+    if svm:
+        out["memory_budget_pass"] = {k: svm[k] for k in ("frames_per_s", "p50_ms", "p99_ms", "burst_capacity_fps",
+                                                          "device_pool_bytes", "all_pools_bytes", "pool_uploads",
+                                                          "pool_evictions", "pool_upload_bytes", "requests")}
     print(json.dumps(out))
     return 0
 
@@ -597,6 +709,10 @@ def main():
     ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--plain-requests", type=int, default=600)
     ap.add_argument("--max-batch", type=int, default=64)
+    ap.add_argument("--slots", type=int, default=3, help="serving: batches in flight")
+    ap.add_argument("--pool-pass", type=int, default=1, help="c5: also run under a half-size brick-pool budget")
+    ap.add_argument("--serve-requests", type=int, default=400,
+                    help="c2: requests of the short serving run giving p50/p99 (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -628,6 +744,7 @@ def main():
     views = [wl.views[i] for i in mine]
     r = Renderer()
     r.loadSynthetic(wl.synth, **wl.brick, build_texture=not args.no_texture, layouts=4)
+    build = r.buildStats()  # the GPU UVF build of the volume just loaded (device time per phase)
     r.resize((wl.width, wl.height))
     r.set1DTrans(wl.tf)
     r.setValueRange(*wl.value_range)
@@ -670,6 +787,9 @@ def main():
     r.setStatsLevel(2)
     r.paintBatch(views)
     st2 = r.stats()
+    # the 8-view orbit the committed ncu capture rendered (bench.py --views 8)
+    r.paintBatch(workloads.config2(size=args.size, nviews=8).views)
+    st8 = r.stats()
     r.setStatsLevel(1)
     cell_bytes_per_launch = st2["cell_bytes"]
     dev_s = maxover(sum(step_ms) / 1000.0)
@@ -677,7 +797,7 @@ def main():
     value = frames_total / dev_s
     ksec = sum(kernel_ms) / 1000.0
     achieved = None
-    st_last = r.stats()
+    st_last = st  # the last timed step
 
     # ---- per-view plain kernel (64 launches) ----
     plain_ms = []
@@ -777,22 +897,44 @@ def main():
             r.readFramebuffer(0)
     e2e_plain = len(views) * max(1, args.steps // 2) / (time.perf_counter() - t0)
 
+    r.cleanup()
+    # ---- short serving run (the metric's p99): Poisson arrivals at 70% of capacity ----
+    sv = serving_run(args.serve_requests, 100, args.max_batch, err_requests=4) if args.serve_requests > 0 else None
+
     out = None
     if rank == 0:
         pk = peaks()
         peak = pk["hbm_gbs"] if pk else 6800.0
         cpu = None
         err = None
+        cpu_build = None
         if not args.no_cpu:
             from oracle import orc
             vol = synth_volume(wl.synth)
             threads = orc.max_threads()
             v0, p0 = wl.views[0]
             pr, sr, n, ref, pix, el = cpu_sample(wl, vol, v0, p0, args.cpu_seconds, threads, 7)
+            pr1, sr1, n1, _, _, el1 = cpu_sample(wl, vol, v0, p0, args.cpu_seconds / 3.0, 1, 8)
             cpu = {"value": pr / (wl.width * wl.height), "unit": "frames/s", "cores": threads,
                    "kind": "port", "gsamples_per_s": sr / 1e9,
-                   "sample": "%d seeded pixels of view 0 (%.1f s, FP64 oracle, %d threads); "
-                             "frames/s = pixels/s / (%d*%d)" % (n, el, threads, wl.width, wl.height)}
+                   "value_1core": pr1 / (wl.width * wl.height), "gsamples_per_s_1core": sr1 / 1e9,
+                   "sample": "%d seeded pixels of view 0 (%.1f s, FP64 oracle, %d threads; 1 thread: %d "
+                             "pixels in %.1f s); frames/s = pixels/s / (%d*%d)" %
+                             (n, el, threads, n1, el1, wl.width, wl.height)}
+            # the CPU UVF build restatement on the same generator at 1/8 of the voxels
+            # (512^3), all threads and 1 thread, scaled to the full volume by voxel count
+            from oracle import scenes
+            small = orc.synth_blobs(scenes.config2(size=args.size // 2, nviews=1).synth)
+            scale = float(vol.size) / float(small.size)
+            tb_all, ph_all = orc.uvf_build_timed(small, threads=threads)
+            tb_1, ph_1 = orc.uvf_build_timed(small, threads=1)
+            del small
+            cpu_build = {"kind": "port", "cores": threads, "seconds": tb_all * scale, "seconds_1core": tb_1 * scale,
+                         "phases_s": {k: v * scale for k, v in ph_all.items()},
+                         "phases_s_1core": {k: v * scale for k, v in ph_1.items()},
+                         "sample": "the oracle's CPU build (pyramid, bricks + min/max, 1D and 2D histograms) of "
+                                   "the %d^3 volume of the same generator, times scaled by voxel count x%.0f"
+                                   % (args.size // 2, scale)}
             # image error of the GPU frame on the same pixels
             r2 = Renderer(float_fb=True)
             r2.loadSynthetic(wl.synth, **wl.brick)
@@ -809,6 +951,38 @@ def main():
                    "pixels": int(pix.size), "tol_max": 2 / 255, "tol_rms": 0.5 / 255}
         gs = samples / (sum(kernel_ms) / 1000.0) / 1e9
         achieved = cell_bytes_per_launch / (ksec / args.steps) / 1e9
+        # traffic and issue: the committed 8-view ncu capture, scaled to this
+        # launch by the algorithmic bytes / samples measured here on both
+        prof = profile_counters()
+        traffic = issue = None
+        if prof and st8["cell_bytes"] > 0 and st8["samples"] > 0:
+            dram8 = prof.get("dram__bytes_read.sum", 0.0) + prof.get("dram__bytes_write.sum", 0.0)
+            traffic = dram8 * cell_bytes_per_launch / st8["cell_bytes"]
+            inst = prof.get("smsp__inst_executed.sum", 0.0) * st_last["samples"] / st8["samples"]
+            sm_hz = (clk.get("sm_mhz") or 2070.0) * 1e6
+            nsm = int(prof.get("device__attribute_multiprocessor_count", 152))
+            issue_peak = 4.0 * nsm * sm_hz  # one warp instruction per SMSP per cycle, 4 SMSPs per SM
+            issue_ach = inst / (ksec / args.steps)
+            issue = {"bound": "issue", "achieved": issue_ach, "peak": issue_peak, "unit": "warp-inst/s",
+                     "frac": issue_ach / issue_peak,
+                     "capture_issue_active_pct": prof.get("smsp__issue_active.avg.pct_of_peak_sustained_active"),
+                     "capture_threads_per_inst": prof.get("smsp__thread_inst_executed_per_inst_executed.ratio"),
+                     "how": "warp instructions of the 8-view capture x (samples here / samples of the 8 views "
+                            "here), over this launch's kernel time; peak = 4 x SMs x SM clock"}
+        bgbps = build["total_bytes"] / (build["total_ms"] / 1000.0) / 1e9 if build["total_ms"] > 0 else None
+        uvf_build = {
+            "workload": "GPU UVF build of the %d^3 uint16 volume: %d LODs, 256^3 bricks with 2 ghosts, %d layout "
+                        "copies, macro-cell min/max, per-brick min/max, 1D and 2D histograms (synthesis and "
+                        "textures excluded)" % (args.size, build["lod_count"], build["layout_copies"]),
+            "ms": build["total_ms"], "bytes": build["total_bytes"], "gbps": bgbps,
+            "roofline": {"bound": "hbm", "achieved": bgbps, "peak": peak, "unit": "GB/s",
+                         "frac": bgbps / peak if bgbps else None},
+            "phases_ms": {k[:-3]: build[k] for k in ("pyramid_ms", "cells_ms", "bricks_ms", "minmax_ms",
+                                                     "hist1d_ms", "hist2d_ms")},
+            "phases_bytes": {k[:-6]: build[k] for k in ("pyramid_bytes", "cells_bytes", "bricks_bytes",
+                                                        "minmax_bytes", "hist1d_bytes", "hist2d_bytes")},
+            "cpu_baseline": cpu_build,
+        }
         out = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -841,21 +1015,27 @@ def main():
                            "read-back of step i overlapping the render of step i + 1; every step's frames read back"},
             "e2e_sync_fps": e2e_sync,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic_from_profile(),
+                         "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_render_persistent_u<uint16,1D,SW>",
                          "bytes_per_launch": cell_bytes_per_launch,
                          "bytes_rule": "sum over views of distinct non-empty 4^3 macro-cells sampled x 4^3 x 2 B",
                          "brick_bytes_per_launch": brick_bytes / args.steps,
                          "kernel_ms": 1000.0 * ksec / args.steps,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if pk else "fallback"},
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if pk else "fallback",
+                         "traffic_how": "DRAM bytes of the committed 8-view ncu capture x (algorithmic bytes here / "
+                                        "algorithmic bytes of the same 8 views here)",
+                         "issue": issue},
             "cpu_baseline": cpu,
+            "uvf_build": uvf_build,
+            "p50_ms": sv["p50_ms"] if sv else None,
+            "p99_ms": sv["p99_ms"] if sv else None,
+            "serving": sv,
             "gpu_launches": 2 * args.steps,  # per step: the background fill and the persistent raycast
             "clocks": clk,
             "stats_last_step": {k: st_last[k] for k in ("samples", "bricks_touched", "bricks_skipped",
                                                          "brick_bytes")},
         }
         print(json.dumps(out))
-    r.cleanup()
     if dist is not None:
         dist.destroy_process_group()
     return 0

@@ -57,8 +57,28 @@ class TuneResult(C.Structure):
                 ("best_ms", C.c_float), ("default_ms", C.c_float)]
 
 
+class BuildStats(C.Structure):
+    _fields_ = [("total_ms", C.c_double), ("pyramid_ms", C.c_double), ("cells_ms", C.c_double),
+                ("bricks_ms", C.c_double), ("minmax_ms", C.c_double), ("hist1d_ms", C.c_double),
+                ("hist2d_ms", C.c_double), ("total_bytes", C.c_uint64), ("pyramid_bytes", C.c_uint64),
+                ("cells_bytes", C.c_uint64), ("bricks_bytes", C.c_uint64), ("minmax_bytes", C.c_uint64),
+                ("hist1d_bytes", C.c_uint64), ("hist2d_bytes", C.c_uint64), ("level0_bytes", C.c_uint64),
+                ("lod_count", C.c_int32), ("layout_copies", C.c_int32)]
+
+
+class TuneParams(C.Structure):
+    _fields_ = [("brick_sizes", C.c_int32 * 4), ("samples_per_step", C.c_int32 * 2), ("reserved", C.c_int32 * 2)]
+
+
+class TuneResultEx(C.Structure):
+    _fields_ = [("tile_w", C.c_int32), ("ctas_per_sm", C.c_int32), ("brick_size", C.c_int32),
+                ("samples_per_step", C.c_int32), ("candidates", C.c_int32), ("best_ms", C.c_float),
+                ("default_ms", C.c_float), ("worst_ms", C.c_float)]
+
+
 class ServerParams(C.Structure):
-    _fields_ = [("max_batch", C.c_int32), ("tile_w", C.c_int32), ("fb_budget_bytes", C.c_uint64)]
+    _fields_ = [("max_batch", C.c_int32), ("tile_w", C.c_int32), ("fb_budget_bytes", C.c_uint64),
+                ("slots", C.c_int32), ("reserved", C.c_int32), ("device_pool_bytes", C.c_uint64)]
 
 
 class Request(C.Structure):
@@ -80,7 +100,14 @@ class Tf2dSwatch(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("batches", C.c_uint64),
                 ("mean_batch", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
-                ("max_ms", C.c_double), ("frames_per_s", C.c_double)]
+                ("max_ms", C.c_double), ("frames_per_s", C.c_double), ("overlap_checked", C.c_uint64),
+                ("overlapped", C.c_uint64), ("uploads", C.c_uint64), ("evictions", C.c_uint64),
+                ("upload_bytes", C.c_uint64), ("resident_bytes", C.c_uint64)]
+
+
+class ServerTune(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("mode", C.c_int32), ("tile_w", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("candidates", C.c_int32), ("best_ms", C.c_float), ("default_ms", C.c_float)]
 
 
 class SynthParams(C.Structure):
@@ -128,6 +155,9 @@ SIGNATURES = {
     "gbvr_load_uvf": [P, CP, I, C.POINTER(BrickParams)],
     "gbvr_load_volume": [P, P, I64P, I, C.POINTER(BrickParams)],
     "gbvr_get_dataset_info": [P, C.POINTER(DatasetInfo)],
+    "gbvr_get_build_stats": [P, C.POINTER(BuildStats)],
+    "gbvr_set_samples_per_step": [P, I],
+    "gbvr_autotune_ex": [P, C.POINTER(View), I, C.POINTER(TuneParams), C.POINTER(TuneResultEx)],
     "gbvr_get_hist1d": [P, U64P, SZ],
     "gbvr_get_hist2d": [P, U64P, SZ, SZ, FP],
     "gbvr_get_brick_minmax": [P, I, C.POINTER(D), SZ],
@@ -200,6 +230,7 @@ SIGNATURES = {
     "gbvr_server_wait": [P, C.c_uint64, D, C.POINTER(RequestResult)],
     "gbvr_server_get_stats": [P, C.POINTER(ServerStats)],
     "gbvr_server_reset_stats": [P],
+    "gbvr_server_autotune": [P, I, I, I, C.POINTER(ServerTune), I, C.POINTER(I)],
     "gbvr_uvf_inspect": [CP, I, C.POINTER(UvfSummary)],
     "gbvr_uvf_read_volume": [CP, P, SZ],
     "gbvr_uvf_read_hist1d": [CP, U64P, SZ],

@@ -10,6 +10,8 @@
 #include <algorithm>
 #include <array>
 #include <climits>
+#include <stdexcept>
+#include <cstdlib>
 #include <cstdint>
 #include <cmath>
 #include <cstdio>
@@ -89,6 +91,24 @@ struct DevBuf {
   T* as() const { return (T*)p; }
 };
 
+// Host-side failure injection for the error-path tests: the environment
+// variable GBVR_FAULT_INJECT names one failure site -- "pinned_alloc" (every
+// page-locked allocation fails as if host memory were exhausted) or
+// "server_launch" (the serving worker's batch launch throws).  Unset in
+// normal use; nothing on the GPU is made to fail.
+bool fault_injected(const char* site) {
+  const char* v = std::getenv("GBVR_FAULT_INJECT");
+  return v && std::strcmp(v, site) == 0;
+}
+
+cudaError_t host_alloc_pinned(void** p, size_t bytes) {
+  if (fault_injected("pinned_alloc")) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocHost(p, bytes);
+}
+
 struct PinnedBuf {
   void* p = nullptr;
   size_t n = 0;
@@ -102,7 +122,7 @@ struct PinnedBuf {
     if (p) cudaFreeHost(p);
     p = nullptr;
     n = 0;
-    cudaError_t e = cudaMallocHost(&p, bytes ? bytes : 16);
+    cudaError_t e = host_alloc_pinned(&p, bytes ? bytes : 16);
     if (e == cudaSuccess) n = bytes;
     return e;
   }
@@ -238,6 +258,7 @@ struct Dataset {
   std::vector<cudaArray_t> arrays;
   std::vector<cudaTextureObject_t> texs;
   std::string raster_id = "GB300 volume raster";
+  gbvr_build_stats build{};  // the last in-core build's phase times and bytes
   // Out of core: every brick lives in page-locked host memory (host_store,
   // element offsets host_off); the device pool is a cache of nslots
   // fixed-size slots, and BrickInfo.offset points at a brick's slot while
@@ -273,6 +294,7 @@ struct Dataset {
     for (auto a : arrays) cudaFreeArray(a);
     texs.clear();
     arrays.clear();
+    build = gbvr_build_stats{};
     pool.release();
     d_bricks.release();
     if (host_store.p) cudaFreeHost(host_store.p);
@@ -402,9 +424,38 @@ int build_textures(Dataset& ds, cudaStream_t s) {
 
 // GPU UVF build: LOD pyramid, bricks with ghosts, per-brick min/max, 1D and
 // 2D histograms.  d_level0 (device, flat, x fastest) is consumed.
+// Device time of one build phase: events recorded right before and after
+// its launches on the build stream; read once the build has synchronised.
+struct PhaseTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  double* acc;
+  explicit PhaseTimer(double* out) : acc(out) {}
+  ~PhaseTimer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+  cudaError_t start(cudaStream_t s) {
+    cudaError_t e = a ? cudaSuccess : cudaEventCreate(&a);
+    if (e == cudaSuccess && !b) e = cudaEventCreate(&b);
+    return e == cudaSuccess ? cudaEventRecord(a, s) : e;
+  }
+  cudaError_t stop(cudaStream_t s) { return cudaEventRecord(b, s); }
+  // after a synchronisation of the stream
+  cudaError_t add() {
+    float ms = 0.f;
+    cudaError_t e = cudaEventElapsedTime(&ms, a, b);
+    if (e == cudaSuccess) *acc += ms;
+    return e;
+  }
+};
+
 int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims[3], const gbvr_brick_params* bp,
                   cudaStream_t s) {
   ds.release();
+  gbvr_build_stats& bs = ds.build;
+  bs = gbvr_build_stats{};
+  PhaseTimer t_pyr(&bs.pyramid_ms), t_cells(&bs.cells_ms), t_bricks(&bs.bricks_ms), t_mm(&bs.minmax_ms),
+      t_h1(&bs.hist1d_ms), t_h2(&bs.hist2d_ms);
   ds.dtype = dtype;
   for (int a = 0; a < 3; ++a) ds.dims[a] = dims[a];
   ds.brick = bp && bp->brick_size > 0 ? bp->brick_size : 256;
@@ -422,12 +473,18 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   lv.emplace_back(new DevBuf());
   std::swap(lv[0]->p, d_level0.p);
   std::swap(lv[0]->n, d_level0.n);
+  auto level_bytes = [&](size_t l) { return (uint64_t)ld[l][0] * ld[l][1] * ld[l][2] * es; };
   for (size_t l = 1; l < ld.size(); ++l) {
     lv.emplace_back(new DevBuf());
-    CUDA_TRY(lv[l]->alloc((size_t)ld[l][0] * ld[l][1] * ld[l][2] * es));
+    CUDA_TRY(lv[l]->alloc((size_t)level_bytes(l)));
+  }
+  CUDA_TRY(t_pyr.start(s));
+  for (size_t l = 1; l < ld.size(); ++l) {
     long long pd[3] = {ld[l - 1][0], ld[l - 1][1], ld[l - 1][2]};
     CUDA_TRY(launch_downsample(lv[l - 1]->p, dtype, pd, lv[l]->p, s));
+    bs.pyramid_bytes += level_bytes(l - 1) + level_bytes(l);
   }
+  CUDA_TRY(t_pyr.stop(s));
   // page table
   unsigned long long cursor = 0;
   for (size_t l = 0; l < ld.size(); ++l) {
@@ -447,20 +504,46 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyHostToDevice, s));
   for (size_t l = 0; l < ld.size(); ++l) {
     Level& L = ds.levels[l];
-    long long d[3] = {ld[l][0], ld[l][1], ld[l][2]};
     L.cell_shift = CELL_SHIFT;
-    for (int a = 0; a < 3; ++a) L.nc[a] = (int)((d[a] + (1 << CELL_SHIFT) - 1) >> CELL_SHIFT);
+    for (int a = 0; a < 3; ++a) L.nc[a] = (int)((ld[l][a] + (1 << CELL_SHIFT) - 1) >> CELL_SHIFT);
     L.cells = std::make_shared<DevBuf>();
     CUDA_TRY(L.cells->alloc(sizeof(float2) * (size_t)L.nc[0] * L.nc[1] * L.nc[2]));
+    L.smax = std::make_shared<DevBuf>();
+    for (int a = 0; a < 3; ++a) L.nsc[a] = (L.nc[a] + (1 << SUPERCELL_SHIFT) - 1) >> SUPERCELL_SHIFT;
+    CUDA_TRY(L.smax->alloc(sizeof(float) * (size_t)L.nsc[0] * L.nsc[1] * L.nsc[2]));
+  }
+  // macro-cell min/max (and the MIP super-cells) of every level
+  CUDA_TRY(t_cells.start(s));
+  for (size_t l = 0; l < ld.size(); ++l) {
+    Level& L = ds.levels[l];
+    long long d[3] = {ld[l][0], ld[l][1], ld[l][2]};
     CUDA_TRY(launch_cell_minmax(lv[l]->p, dtype, d, CELL_SHIFT, L.nc, L.cells->as<float2>(), s));
-    TRY(build_supercells(L, s));
+    CUDA_TRY(launch_supercell_max(L.cells->as<float2>(), L.nc, L.smax->as<float>(), L.nsc, s));
+    bs.cells_bytes += level_bytes(l);
+  }
+  CUDA_TRY(t_cells.stop(s));
+  // bricks (interior + ghosts) of every level, per layout copy
+  CUDA_TRY(t_bricks.start(s));
+  for (size_t l = 0; l < ld.size(); ++l) {
+    Level& L = ds.levels[l];
+    long long d[3] = {ld[l][0], ld[l][1], ld[l][2]};
+    uint64_t stored = 0;
+    for (int i = 0; i < L.nbricks; ++i) {
+      const BrickInfo& b = ds.bricks[L.brick_base + i];
+      stored += (uint64_t)b.sx * b.sy * b.sz * es;
+    }
     for (int c = 0; c < (ds.layouts == 4 ? 2 : ds.layouts); ++c) {
       const int perm = (ds.layouts == 4 && c == 1) ? 3 : c;
       CUDA_TRY(launch_gather_bricks(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks,
                                     (char*)ds.pool.p + (size_t)c * cursor * es, perm, s));
+      bs.bricks_bytes += level_bytes(l) + stored;
     }
   }
+  CUDA_TRY(t_bricks.stop(s));
+  CUDA_TRY(t_mm.start(s));
   CUDA_TRY(launch_brick_minmax(ds.pool.p, dtype, ds.d_bricks.as<BrickInfo>(), (int)ds.bricks.size(), s));
+  CUDA_TRY(t_mm.stop(s));
+  bs.minmax_bytes = ds.stored_bytes;
   CUDA_TRY(cudaMemcpyAsync(ds.bricks.data(), ds.d_bricks.p, sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   ds.gmin = INFINITY;
@@ -476,7 +559,10 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
     DevBuf dh;
     CUDA_TRY(dh.alloc(sizeof(uint64_t) * nbins));
     CUDA_TRY(cudaMemsetAsync(dh.p, 0, sizeof(uint64_t) * nbins, s));
+    CUDA_TRY(t_h1.start(s));
     CUDA_TRY(launch_hist1d(lv[0]->p, dtype, n0, dh.as<unsigned long long>(), nbins, s));
+    CUDA_TRY(t_h1.stop(s));
+    bs.hist1d_bytes = level_bytes(0);
     std::vector<uint64_t> full(nbins);
     CUDA_TRY(cudaMemcpyAsync(full.data(), dh.p, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
@@ -493,8 +579,11 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
     CUDA_TRY(d2.alloc(sizeof(uint64_t) * n2));
     CUDA_TRY(dsc.alloc(sizeof(Hist2DScratch)));
     CUDA_TRY(cudaMemsetAsync(d2.p, 0, sizeof(uint64_t) * n2, s));
+    CUDA_TRY(t_h2.start(s));
     CUDA_TRY(launch_hist2d(lv[0]->p, dtype, dims, ds.gmax, outsize, ds.merge, d2.as<unsigned long long>(),
                            dsc.as<Hist2DScratch>(), s));
+    CUDA_TRY(t_h2.stop(s));
+    bs.hist2d_bytes = 3 * level_bytes(0);
     ds.hist2d.resize(n2);
     Hist2DScratch hs;
     CUDA_TRY(cudaMemcpyAsync(ds.hist2d.data(), d2.p, sizeof(uint64_t) * n2, cudaMemcpyDeviceToHost, s));
@@ -504,9 +593,21 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
     memcpy(&g, &hs.gmax_bits, 8);
     ds.max_grad = (float)g;
     ds.bit_width = dtype == DT_U8 ? 8 : 16;
+    CUDA_TRY(t_h1.add());
+    CUDA_TRY(t_h2.add());
   } else {
     ds.bit_width = 32;
   }
+  CUDA_TRY(t_pyr.add());
+  CUDA_TRY(t_cells.add());
+  CUDA_TRY(t_bricks.add());
+  CUDA_TRY(t_mm.add());
+  bs.total_ms = bs.pyramid_ms + bs.cells_ms + bs.bricks_ms + bs.minmax_ms + bs.hist1d_ms + bs.hist2d_ms;
+  bs.total_bytes = bs.pyramid_bytes + bs.cells_bytes + bs.bricks_bytes + bs.minmax_bytes + bs.hist1d_bytes +
+                   bs.hist2d_bytes;
+  bs.level0_bytes = level_bytes(0);
+  bs.lod_count = (int32_t)ld.size();
+  bs.layout_copies = ds.layouts == 4 ? 2 : ds.layouts;
   if (bp && bp->build_texture) TRY(build_textures(ds, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   ds.loaded = true;
@@ -580,7 +681,7 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
   if (ds.compression != 0 && ds.compression != 3) return fail(GBVR_EINVAL, "compression must be 0 (none) or 3 (LZ4)");
   ds.raw_store_bytes = cursor * es;
   if (!ds.compression) {
-    cudaError_t e = cudaMallocHost(&ds.host_store.p, cursor * es);
+    cudaError_t e = host_alloc_pinned(&ds.host_store.p, cursor * es);
     if (e != cudaSuccess) return fail(GBVR_ENOMEM, "page-locked host brick store of " + std::to_string(cursor * es) + " bytes");
     ds.host_store.n = cursor * es;
   } else {
@@ -595,7 +696,7 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
   auto seg_append = [&](const uint8_t* data, size_t n, int& seg, unsigned long long& off) -> int {
     if (ds.seg_p.empty() || ds.seg_used.back() + n > kSeg) {
       void* q = nullptr;
-      if (cudaMallocHost(&q, std::max(kSeg, n)) != cudaSuccess)
+      if (host_alloc_pinned(&q, std::max(kSeg, n)) != cudaSuccess)
         return fail(GBVR_ENOMEM, "page-locked compressed brick store segment");
       ds.seg_p.push_back(q);
       ds.seg_used.push_back(0);
@@ -927,6 +1028,7 @@ struct FrameParams {
   float iso_rgb[3];
   int lighting;
   float amb[3], diff[3], spec[3], shininess, light_dir[3], bg[3];
+  float bg_top[3];  // with bg: a vertical gradient when they differ
   int tile_w, empty_skip;
   const float4* tf;
   int tf_w, tf_h;
@@ -982,6 +1084,8 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
     f.diff[k] = p.diff[k];
     f.spec[k] = p.spec[k];
     f.bg[k] = p.bg[k];
+    f.bg_top[k] = p.bg_top[k];
+    if (p.bg_top[k] != p.bg[k]) f.bg_grad = 1;
   }
   f.lighting = p.lighting;
   f.shininess = p.shininess;
@@ -1207,14 +1311,16 @@ struct gbvr_renderer {
   float last_ms = 0.f, last_kernel_ms = 0.f;
   uint64_t last_h2d = 0;
   int max_ctas_per_sm[4] = {0, 0, 0, 0}, max_ctas_per_sm_u[4] = {0, 0, 0, 0}, sm_count = 0;
+  int max_ctas_per_sm_sps2 = 0;  // the batch kernel's two-samples-per-step variant
+  int samples_per_step = 1;
   // graph cache for the batch launch
   struct GraphKey {
-    int n, w, h, level, dtype, mode, sampler, grid;
+    int n, w, h, level, dtype, mode, sampler, grid, sps;
     void* fb8;
     void* fb32;
     bool operator<(const GraphKey& o) const {
-      return std::tie(n, w, h, level, dtype, mode, sampler, grid, fb8, fb32) <
-             std::tie(o.n, o.w, o.h, o.level, o.dtype, o.mode, o.sampler, o.grid, o.fb8, o.fb32);
+      return std::tie(n, w, h, level, dtype, mode, sampler, grid, sps, fb8, fb32) <
+             std::tie(o.n, o.w, o.h, o.level, o.dtype, o.mode, o.sampler, o.grid, o.sps, o.fb8, o.fb32);
     }
   };
   struct CachedGraph {
@@ -1397,6 +1503,7 @@ FrameDesc make_frame(gbvr_renderer* r, const float* view, const float* proj, int
     p.spec[k] = r->spec[k];
     p.light_dir[k] = r->light_dir[k];
     p.bg[k] = r->bg_bot[k];
+    p.bg_top[k] = r->bg_top[k];
   }
   p.tile_w = r->tile_w;
   p.empty_skip = r->empty_skip;
@@ -2223,6 +2330,7 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
       r->max_ctas_per_sm[m] = std::max(1, persistent_grid_size(dev, m) / std::max(r->sm_count, 1));
       r->max_ctas_per_sm_u[m] = std::max(1, persistent_grid_size_uniform(dev, m) / std::max(r->sm_count, 1));
     }
+    r->max_ctas_per_sm_sps2 = persistent_ctas_per_sm_sps2();
   }
   // Views of one renderer batch share everything but camera, outputs and
   // counters, unless they sample different brick layout copies: then the
@@ -2243,7 +2351,10 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     shared.touched_stride = shared.touched ? r->ds.levels[level].nbricks : 0;
     shared.cell_touched_stride = shared.cell_touched ? r->cell_words : 0;
   }
-  const int max_per_sm = uniform ? r->max_ctas_per_sm_u[r->mode] : r->max_ctas_per_sm[r->mode];
+  const int sps = uniform && r->samples_per_step == 2 && r->mode == GBVR_RM_1DTRANS && r->sampler == GBVR_SAMPLER_SW
+                      ? 2 : 1;
+  const int max_per_sm = sps == 2 ? r->max_ctas_per_sm_sps2
+                                  : (uniform ? r->max_ctas_per_sm_u[r->mode] : r->max_ctas_per_sm[r->mode]);
   const int per_sm = r->ctas_per_sm > 0 ? std::min(r->ctas_per_sm, max_per_sm) : max_per_sm;
   const int grid = r->sm_count * per_sm;
   if (n == 1) {
@@ -2262,7 +2373,8 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     CUDA_TRY(cudaEventRecord(r->evk0, r->stream));  // kernel time: the raycast alone
     cudaError_t le =
         uniform ? launch_render_persistent_uniform(r->ds.dtype, r->mode, r->sampler, shared, r->d_frames.as<FrameDesc>(),
-                                                   1, r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream)
+                                                   1, r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream,
+                                                   sps)
                 : launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), 1,
                                                  r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream);
     if (le != cudaSuccess) return cuda_fail(le, "persistent launch");
@@ -2273,7 +2385,8 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     r->last_h2d = sizeof(FrameDesc) + sizeof(int) * 2;
     return finish(r, 1, level);
   }
-  gbvr_renderer::GraphKey key{n, r->width, r->height, level, r->ds.dtype, r->mode, r->sampler, grid, r->d_fb8.p, r->d_fb32.p};
+  gbvr_renderer::GraphKey key{n,    r->width, r->height, level,       r->ds.dtype, r->mode,
+                              r->sampler, grid,  sps,     r->d_fb8.p, r->d_fb32.p};
   auto it = r->graphs.find(key);
   if (it != r->graphs.end() &&
       (it->second.uniform != uniform || (uniform && memcmp(&it->second.shared, &shared, sizeof(FrameDesc)) != 0))) {
@@ -2290,7 +2403,8 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     CUDA_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t le =
         uniform ? launch_render_persistent_uniform(r->ds.dtype, r->mode, r->sampler, shared, r->d_frames.as<FrameDesc>(),
-                                                   n, r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream)
+                                                   n, r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream,
+                                                   sps)
                 : launch_render_persistent_typed(r->ds.dtype, r->mode, r->sampler, r->d_frames.as<FrameDesc>(), n,
                                                  r->d_prefix.as<int>(), r->d_counter.as<int>(), grid, r->stream);
     cudaError_t ce = cudaStreamEndCapture(r->stream, &g);
@@ -2584,6 +2698,16 @@ int gbvr_load_uvf(gbvr_renderer* r, const char* path, int verify, const gbvr_bri
   int64_t dims[3] = {(int64_t)ra.dims[0], (int64_t)ra.dims[1], (int64_t)ra.dims[2]};
   TRY(gbvr_load_volume(r, host.data(), dims, dtype, &p));
   r->ds.raster_id = ra.id;
+  return GBVR_OK;
+  GBVR_ABI_CATCH
+}
+
+int gbvr_get_build_stats(gbvr_renderer* r, gbvr_build_stats* out) {
+  GBVR_ABI_TRY
+  TRY(check_loaded(r));
+  if (!out) return fail(GBVR_EINVAL, "null output");
+  if (r->ds.ooc) return fail(GBVR_ESTATE, "build statistics are kept for in-core builds only");
+  *out = r->ds.build;
   return GBVR_OK;
   GBVR_ABI_CATCH
 }
@@ -2939,6 +3063,108 @@ int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_res
     out->candidates = count;
     out->best_ms = best;
     out->default_ms = def;
+  }
+  return GBVR_OK;
+  GBVR_ABI_CATCH
+}
+
+int gbvr_set_samples_per_step(gbvr_renderer* r, int sps) {
+  GBVR_ABI_TRY
+  TRY(check_r(r));
+  if (sps != 1 && sps != 2) return fail(GBVR_EINVAL, "samples per step must be 1 or 2");
+  r->samples_per_step = sps;
+  return GBVR_OK;
+  GBVR_ABI_CATCH
+}
+
+int gbvr_autotune_ex(gbvr_renderer* r, const gbvr_view* views, int n, const gbvr_tune_params* tp,
+                     gbvr_tune_result_ex* out) {
+  GBVR_ABI_TRY
+  TRY(check_loaded(r));
+  if (!views || n <= 0) return fail(GBVR_EINVAL, "no tuning views");
+  if (r->ds.ooc) return fail(GBVR_ESTATE, "the extended autotuner rebuilds the dataset: in-core datasets only");
+  TRY(settle_async(r));
+  std::vector<int> bricks, spss;
+  for (int i = 0; i < 4 && tp && tp->brick_sizes[i] > 0; ++i) bricks.push_back(tp->brick_sizes[i]);
+  for (int i = 0; i < 2 && tp && tp->samples_per_step[i] > 0; ++i) spss.push_back(tp->samples_per_step[i]);
+  for (int b : bricks)
+    if (b - 2 * r->ds.ghost < 8 || b > 2048) return fail(GBVR_EINVAL, "brick size out of range");
+  for (int v : spss)
+    if (v != 1 && v != 2) return fail(GBVR_EINVAL, "samples per step must be 1 or 2");
+  const int brick0 = r->ds.brick;
+  if (bricks.empty()) bricks.push_back(brick0);
+  if (spss.empty()) spss.push_back(r->samples_per_step);
+  // the finest level, reassembled from the bricks' interiors, for the rebuilds
+  DevBuf level0;
+  gbvr_brick_params bp = {};
+  const long long dims[3] = {r->ds.dims[0], r->ds.dims[1], r->ds.dims[2]};
+  const size_t lbytes = (size_t)dims[0] * dims[1] * dims[2] * dtype_size(r->ds.dtype);
+  const bool rebuild = bricks.size() > 1 || bricks[0] != brick0;
+  if (rebuild) {
+    const Level& L0 = r->ds.levels[0];
+    CUDA_TRY(level0.alloc(lbytes));
+    CUDA_TRY(launch_scatter_interiors(r->ds.pool.p, r->ds.dtype, r->ds.d_bricks.as<BrickInfo>() + L0.brick_base,
+                                      L0.nbricks, dims, level0.p, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    bp.overlap = r->ds.ghost;
+    bp.layouts = r->ds.layouts;
+    bp.build_texture = r->ds.texs.empty() ? 0 : 1;
+    for (int a = 0; a < 3; ++a) bp.aspect[a] = r->ds.aspect[a];
+  }
+  auto build_at = [&](int b) -> int {
+    if (r->ds.brick == b && r->ds.loaded) return GBVR_OK;
+    DevBuf lv;
+    CUDA_TRY(lv.alloc(lbytes));
+    CUDA_TRY(cudaMemcpyAsync(lv.p, level0.p, lbytes, cudaMemcpyDeviceToDevice, r->stream));
+    bp.brick_size = b;
+    r->drop_graphs();
+    r->skip_dirty = true;
+    r->tf_dirty = true;
+    r->occ_valid.clear();
+    return build_dataset(r->ds, lv, r->ds.dtype, dims, &bp, r->stream);
+  };
+  const int tiles[] = {4, 8, 16, 32};
+  const int ctas[] = {0, 4, 6};
+  float best = INFINITY, def = INFINITY, worst = 0.f;
+  int bt = TILE_W, bc = 0, bb = brick0, bs = 1, count = 0;
+  // the current brick size first, so the default combination is measured on it
+  std::stable_partition(bricks.begin(), bricks.end(), [&](int b) { return b == brick0; });
+  for (int b : bricks) {
+    TRY(build_at(b));
+    for (int v : spss)
+      for (int tw : tiles)
+        for (int c : ctas) {
+          r->samples_per_step = v;
+          r->tile_w = tw;
+          r->ctas_per_sm = c;
+          TRY(paint_batch(r, views, n));  // warm-up (and graph instantiation)
+          TRY(paint_batch(r, views, n));
+          const float ms = r->last_kernel_ms;
+          ++count;
+          if (b == brick0 && v == 1 && tw == TILE_W && c == 0) def = ms;
+          worst = std::max(worst, ms);
+          if (ms < best) {
+            best = ms;
+            bt = tw;
+            bc = c;
+            bb = b;
+            bs = v;
+          }
+        }
+  }
+  TRY(build_at(bb));
+  r->tile_w = bt;
+  r->ctas_per_sm = bc;
+  r->samples_per_step = bs;
+  if (out) {
+    out->tile_w = bt;
+    out->ctas_per_sm = bc;
+    out->brick_size = bb;
+    out->samples_per_step = bs;
+    out->candidates = count;
+    out->best_ms = best;
+    out->default_ms = def;
+    out->worst_ms = worst;
   }
   return GBVR_OK;
   GBVR_ABI_CATCH
@@ -3325,23 +3551,38 @@ int gbvr_orbit_camera(float azimuth_deg, float elevation_deg, float radius, floa
 }  // extern "C"
 
 // ===========================================================================
-// Serving loop: many resident datasets and transfer functions, requests from
-// any thread, continuous batching into persistent launches.
+// Serving loop: many datasets and transfer functions, requests from any
+// thread, continuous batching into graph-replayed persistent launches.
 //
-// A worker thread owns the GPU side.  Two batch slots alternate: while one
-// batch renders, the next is assembled from the requests that arrived and
-// queued behind it on the same stream, so the GPU is not idle between
-// batches.  A batch takes pending requests in arrival order until it holds
-// max_batch requests or its framebuffer area (half of fb_budget_bytes) is
-// full; requests that do not fit wait for the next batch (admission by
-// memory).  Within a batch, requests are grouped by voxel type and render
-// mode (one persistent launch each, all queued back to back).  Every ray is
-// computed independently of the batch it lands in, so a request's image is
-// the same alone and in any mix.
+// A worker thread owns the GPU side and keeps up to `slots` batches in
+// flight, each on its own stream.  Whenever a slot is free and requests are
+// pending it assembles a batch and launches it at once, so a batch starts
+// while earlier ones still run and its ray tiles take the SMs their tails
+// leave idle.  A batch takes pending requests in arrival order until it holds
+// max_batch of them or its framebuffer share (fb_budget_bytes / slots) is
+// full.  Its requests are grouped by (voxel type, mode) -- group index
+// dtype * 4 + mode -- and each group is one persistent launch
+// (k_render_persistent_g) whose frames, count and tile prefix come from a
+// device table, so the launches of a slot are captured once per set of
+// groups and replayed.  Each group has its own launch shape (tile width, CTAs
+// per SM; gbvr_server_autotune).  A host function queued behind a slot's
+// read-back wakes the worker when it is done (no polling).
+//
+// Admission by memory: with device_pool_bytes > 0 every dataset's brick pool
+// is copied to page-locked host memory when it is added and made resident on
+// demand: a request whose dataset is not resident is admitted once the pool
+// fits the budget, evicting idle datasets (no batch in flight uses them)
+// least recently used first; the upload runs on the batch's stream ahead of
+// its kernels, and later batches on other streams wait for it by event.
+// Requests behind one that must wait are not held up.  Every ray is computed
+// independently of its batch, so a request's image is the same alone and in
+// any mix.
 // ===========================================================================
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <list>
+#include <map>
 #include <thread>
 #include <unordered_map>
 
@@ -3351,6 +3592,10 @@ double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+constexpr int kServerGroups = 12;     // 3 voxel types x 4 render modes
+constexpr int kMaxServerSlots = 8;
+constexpr int kEventRing = 64;        // per-batch kernel-span events, reused every kEventRing batches
+
 struct ServerTf {
   int dataset = 0;
   int mode = GBVR_RM_1DTRANS, w = 0, h = 1, level = 0;
@@ -3358,6 +3603,18 @@ struct ServerTf {
   DevBuf d_tf, d_prefix, d_skip, d_occ, d_occtmp;
   double lo = 0, hi = 1;
   float grad_max = 0.f, iso = 0.f, iso_rgb[3] = {1, 1, 1};
+};
+
+struct ServerDataset {
+  std::unique_ptr<Dataset> ds;
+  size_t pool_bytes = 0;
+  bool resident = true;
+  bool async_pool = false;        // the device pool came from cudaMallocAsync
+  PinnedBuf host_pool;            // page-locked copy of the pool (under a memory budget)
+  int inflight = 0;               // batches in flight that use it
+  uint64_t last_use = 0;          // sequence number of the last batch that used it
+  cudaEvent_t uploaded = nullptr; // recorded behind its last upload
+  bool ever_uploaded = false;
 };
 
 struct ServerRequest {
@@ -3370,15 +3627,33 @@ struct ServerRequest {
   double gpu_ms = 0;
 };
 
+struct GroupShape {
+  int tile_w = TILE_W;
+  int ctas_per_sm = 0;  // 0 = as many as fit
+};
+
 struct BatchSlot {
-  DevBuf d_frames, d_prefix, d_counter, d_samples, d_fb;
-  PinnedBuf h_frames, h_prefix, h_fb;
+  gbvr_server* server = nullptr;
+  int index = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf d_frames, d_prefix, d_counter, d_samples, d_fb, d_groups;
+  PinnedBuf h_frames, h_prefix, h_fb, h_groups;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<ServerRequest*> reqs;
   std::vector<size_t> fb_off;
+  // per request, taken under the server's mutex (the worker then reads no
+  // server container): its dataset, TF preset and group (dtype * 4 + mode)
+  std::vector<const Dataset*> req_ds;
+  std::vector<const ServerTf*> req_tf;
+  std::vector<int> req_gi;
+  std::vector<int> datasets;      // distinct datasets of the batch
+  std::vector<ServerDataset*> dsets;  // ... and their records (upload events)
   size_t fb_used = 0;
   bool busy = false;
+  bool done = false;              // set by the host function behind the batch
   uint64_t seq = 0;
+  unsigned shape_version = 0;
+  std::map<unsigned, cudaGraphExec_t> graphs;  // by set of groups present (bit gi)
 };
 
 }  // namespace
@@ -3387,21 +3662,33 @@ struct gbvr_server {
   gbvr_server_params params;
   int device = 0;
   int sm_count = 0, max_ctas[4] = {1, 1, 1, 1};
-  cudaStream_t stream = nullptr;
-  std::vector<std::unique_ptr<Dataset>> datasets;
+  int nslots = 3;
+  cudaStream_t stream = nullptr;          // dataset builds, TF classification
+  cudaStream_t capture_stream = nullptr;  // graph capture only
+  std::vector<std::unique_ptr<ServerDataset>> datasets;
   std::vector<std::unique_ptr<ServerTf>> tfs;
-  BatchSlot slots[2];
+  std::vector<std::unique_ptr<BatchSlot>> slots;
+  GroupShape shape[kServerGroups];
+  unsigned shape_version = 1;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<ServerRequest*> pending;
   std::unordered_map<uint64_t, std::unique_ptr<ServerRequest>> reqs;
   uint64_t next_ticket = 1, next_batch = 1;
   bool stop = false;
+  bool blocked = false;   // the pending requests cannot be admitted until something changes
+  bool tuning = false;    // the autotuner owns the slots
   std::string worker_error;
   std::thread worker;
+  size_t resident_bytes = 0;
+  // kernel spans per batch (ring by sequence number) for the overlap count
+  cudaEvent_t k0[kEventRing] = {}, k1[kEventRing] = {};
+  bool span_done[kEventRing] = {};
+  uint64_t span_seq[kEventRing] = {};
   // statistics since the last reset
   std::vector<double> latencies;
   uint64_t submitted = 0, completed = 0, batches = 0, batched_requests = 0;
+  uint64_t overlap_checked = 0, overlapped = 0, uploads = 0, evictions = 0, upload_bytes = 0;
   double t_first = -1, t_last = 0;
 
   ~gbvr_server() {
@@ -3411,54 +3698,130 @@ struct gbvr_server {
     }
     cv_work.notify_all();
     if (worker.joinable()) worker.join();
-    for (auto& s : slots) {
-      if (s.ev0) cudaEventDestroy(s.ev0);
-      if (s.ev1) cudaEventDestroy(s.ev1);
+    for (auto& sl : slots) {
+      if (sl->stream) cudaStreamSynchronize(sl->stream);
+      for (auto& g : sl->graphs) cudaGraphExecDestroy(g.second);
+      if (sl->ev0) cudaEventDestroy(sl->ev0);
+      if (sl->ev1) cudaEventDestroy(sl->ev1);
     }
+    for (auto& d : datasets) {
+      if (d->async_pool && d->ds->pool.p) {
+        cudaFreeAsync(d->ds->pool.p, stream);
+        d->ds->pool.p = nullptr;
+        d->ds->pool.n = 0;
+      }
+      if (d->uploaded) cudaEventDestroy(d->uploaded);
+    }
+    if (stream) cudaStreamSynchronize(stream);
+    for (int i = 0; i < kEventRing; ++i) {
+      if (k0[i]) cudaEventDestroy(k0[i]);
+      if (k1[i]) cudaEventDestroy(k1[i]);
+    }
+    for (auto& sl : slots)
+      if (sl->stream) cudaStreamDestroy(sl->stream);
+    if (capture_stream) cudaStreamDestroy(capture_stream);
     if (stream) cudaStreamDestroy(stream);
   }
 };
 
 namespace {
 
-// Assemble and launch one batch into `slot` (worker thread, mutex released).
-// work counters per batch: one per launch group
-constexpr int kServerGroups = 16;
+int group_of(const gbvr_server* s, const ServerRequest* q) {
+  return s->datasets[q->req.dataset]->ds->dtype * 4 + s->tfs[q->req.tf]->mode;
+}
 
-int launch_batch(gbvr_server* s, BatchSlot& slot) {
-  const int n = (int)slot.reqs.size();
-  // group by voxel type and mode: one persistent launch per group
-  std::vector<int> order(n);
-  for (int i = 0; i < n; ++i) order[i] = i;
-  auto key = [&](int i) {
-    const ServerRequest* q = slot.reqs[i];
-    return s->datasets[q->req.dataset]->dtype * 4 + s->tfs[q->req.tf]->mode;  // 3 dtypes x 4 modes
-  };
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key(x) < key(y); });
-  std::vector<ServerRequest*> sorted(n);
-  std::vector<size_t> offs(n);
-  for (int i = 0; i < n; ++i) {
-    sorted[i] = slot.reqs[order[i]];
-    offs[i] = slot.fb_off[order[i]];
+int group_grid(const gbvr_server* s, int gi, const GroupShape& sh) {
+  const int m = gi & 3;
+  const int ctas = sh.ctas_per_sm > 0 ? std::min(sh.ctas_per_sm, s->max_ctas[m]) : s->max_ctas[m];
+  return s->sm_count * std::max(1, ctas);
+}
+
+// Host function queued behind a slot's read-back: the slot may be retired.
+void CUDART_CB slot_done_cb(void* arg) {
+  BatchSlot* sl = static_cast<BatchSlot*>(arg);
+  gbvr_server* s = sl->server;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    sl->done = true;
   }
-  slot.reqs.swap(sorted);
-  slot.fb_off.swap(offs);
-  CUDA_TRY(slot.d_frames.alloc(sizeof(FrameDesc) * s->params.max_batch));
-  CUDA_TRY(slot.d_prefix.alloc(sizeof(int) * (s->params.max_batch + 8) * 2));
+  s->cv_work.notify_all();
+}
+
+// Evict idle datasets (least recently used first, none of `keep`) until
+// `need` more bytes fit the budget; then allocate and upload the pool of D on
+// stream st.  Worker thread, mutex held.  Returns false when it cannot fit now.
+bool make_resident(gbvr_server* s, ServerDataset& D, cudaStream_t st, const std::vector<int>& keep, int& rc) {
+  rc = GBVR_OK;
+  const size_t budget = s->params.device_pool_bytes;
+  while (s->resident_bytes + D.pool_bytes > budget) {
+    ServerDataset* victim = nullptr;
+    for (size_t i = 0; i < s->datasets.size(); ++i) {
+      ServerDataset& c = *s->datasets[i];
+      if (!c.resident || c.inflight > 0 || &c == &D) continue;
+      if (std::find(keep.begin(), keep.end(), (int)i) != keep.end()) continue;
+      if (!victim || c.last_use < victim->last_use) victim = &c;
+    }
+    if (!victim) return false;
+    // stream-ordered: no batch in flight reads it, and no device-wide synchronisation
+    cudaError_t e = cudaFreeAsync(victim->ds->pool.p, st);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "cudaFreeAsync"); return false; }
+    victim->ds->pool.p = nullptr;
+    victim->ds->pool.n = 0;
+    victim->resident = false;
+    s->resident_bytes -= victim->pool_bytes;
+    ++s->evictions;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, D.pool_bytes, st);
+  if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMallocAsync (brick pool)"); return false; }
+  e = cudaMemcpyAsync(p, D.host_pool.p, D.pool_bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaEventRecord(D.uploaded, st);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(p, st);
+    rc = cuda_fail(e, "brick pool upload");
+    return false;
+  }
+  D.ds->pool.p = p;
+  D.ds->pool.n = D.pool_bytes;
+  D.async_pool = true;
+  D.resident = true;
+  D.ever_uploaded = true;
+  s->resident_bytes += D.pool_bytes;
+  ++s->uploads;
+  s->upload_bytes += D.pool_bytes;
+  return true;
+}
+
+// Queue the batch of `slot` on its stream: descriptors, background fill, one
+// persistent launch per group present (captured once per set of groups and
+// replayed; `force` launches every group with one shape directly instead, for
+// the autotuner), the read-back and the completion host function.  Worker
+// thread (or the autotuner), mutex released.  gpu_spans: record the kernel
+// span events of the batch's ring entry.
+int launch_batch(gbvr_server* s, BatchSlot& slot, const GroupShape* force, bool gpu_spans) {
+  const int n = (int)slot.reqs.size();
+  if (!force && fault_injected("server_launch")) throw std::runtime_error("injected failure of a batch launch");
+  const int mb = std::max(s->params.max_batch, n);
+  CUDA_TRY(slot.d_frames.alloc(sizeof(FrameDesc) * mb));
+  CUDA_TRY(slot.d_prefix.alloc(sizeof(int) * (mb + kServerGroups)));
   CUDA_TRY(slot.d_counter.alloc(sizeof(int) * kServerGroups));
-  CUDA_TRY(slot.d_samples.alloc(sizeof(unsigned long long) * s->params.max_batch));
-  CUDA_TRY(slot.h_frames.alloc(sizeof(FrameDesc) * s->params.max_batch));
-  CUDA_TRY(slot.h_prefix.alloc(sizeof(int) * (s->params.max_batch + 8) * 2));
+  CUDA_TRY(slot.d_samples.alloc(sizeof(unsigned long long) * mb));
+  CUDA_TRY(slot.d_groups.alloc(sizeof(LaunchGroup) * kServerGroups));
+  CUDA_TRY(slot.h_frames.alloc(sizeof(FrameDesc) * mb));
+  CUDA_TRY(slot.h_prefix.alloc(sizeof(int) * (mb + kServerGroups)));
+  CUDA_TRY(slot.h_groups.alloc(sizeof(LaunchGroup) * kServerGroups));
   FrameDesc* hf = (FrameDesc*)slot.h_frames.p;
   int* hp = (int*)slot.h_prefix.p;
-  struct Group { int first, count, prefix_at, total, dtype, mode; };
-  std::vector<Group> groups;
-  int pcur = 0;
-  int max_h = 0;
+  LaunchGroup* hg = (LaunchGroup*)slot.h_groups.p;
+  for (int g = 0; g < kServerGroups; ++g) hg[g] = LaunchGroup{0, 0, 0, 0};
+  unsigned mask = 0;
+  int pcur = 0, max_h = 0, cur = -1, total = 0;
   for (int i = 0; i < n; ++i) {
     const ServerRequest* q = slot.reqs[i];
-    const Dataset& ds = *s->datasets[q->req.dataset];
-    const ServerTf& t = *s->tfs[q->req.tf];
+    const Dataset& ds = *slot.req_ds[i];
+    const ServerTf& t = *slot.req_tf[i];
+    const int gi = slot.req_gi[i];
+    const GroupShape& sh = force ? *force : s->shape[gi];
     FrameParams p;
     memset(&p, 0, sizeof(p));
     p.view = q->req.view;
@@ -3481,8 +3844,9 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
       p.spec[k] = 1.f;
       p.light_dir[k] = k == 2 ? -1.f : 0.f;
       p.bg[k] = 0.f;
+      p.bg_top[k] = 0.f;
     }
-    p.tile_w = s->params.tile_w;
+    p.tile_w = sh.tile_w;
     p.empty_skip = 2;
     p.tf = t.d_tf.as<float4>();
     p.tf_w = t.w;
@@ -3497,88 +3861,230 @@ int launch_batch(gbvr_server* s, BatchSlot& slot) {
     hf[i].samples = slot.d_samples.as<unsigned long long>() + i;
     cull_tiles(hf[i], nullptr, p.view, p.proj);
     max_h = std::max(max_h, p.height);
-    const int dt = ds.dtype, md = t.mode;
-    if (groups.empty() || groups.back().dtype != dt || groups.back().mode != md) {
-      if (!groups.empty()) {
-        Group& g = groups.back();
-        hp[g.prefix_at + g.count] = g.total;
-        pcur = g.prefix_at + g.count + 1;
+    if (gi != cur) {
+      if (cur >= 0) {
+        hp[pcur++] = total;  // closing entry of the previous group
       }
-      groups.push_back({i, 0, pcur, 0, dt, md});
+      cur = gi;
+      mask |= 1u << gi;
+      hg[gi] = LaunchGroup{i, 0, pcur, 0};
+      total = 0;
     }
-    Group& g = groups.back();
-    hp[g.prefix_at + g.count] = g.total;
-    g.total += hf[i].ntx * hf[i].nty;
-    ++g.count;
+    hp[pcur++] = total;
+    total += hf[i].ntx * hf[i].nty;
+    ++hg[gi].count;
   }
-  if (!groups.empty()) {
-    Group& g = groups.back();
-    hp[g.prefix_at + g.count] = g.total;
-    pcur = g.prefix_at + g.count + 1;
-  }
-  // one group per (voxel type, mode) after the sort: at most 12
-  if (groups.size() > (size_t)kServerGroups) return fail(GBVR_ESTATE, "too many launch groups in a batch");
-  cudaStream_t st = s->stream;
+  if (cur >= 0) hp[pcur++] = total;
+  cudaStream_t st = slot.stream;
+  // the batch's pools: uploads queued on other streams finish first
+  for (const ServerDataset* D : slot.dsets)
+    if (D->ever_uploaded) CUDA_TRY(cudaStreamWaitEvent(st, D->uploaded, 0));
   CUDA_TRY(cudaEventRecord(slot.ev0, st));
   CUDA_TRY(cudaMemcpyAsync(slot.d_frames.p, hf, sizeof(FrameDesc) * n, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(slot.d_prefix.p, hp, sizeof(int) * pcur, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(slot.d_groups.p, hg, sizeof(LaunchGroup) * kServerGroups, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemsetAsync(slot.d_counter.p, 0, sizeof(int) * kServerGroups, st));
   CUDA_TRY(cudaMemsetAsync(slot.d_samples.p, 0, sizeof(unsigned long long) * n, st));
   // background outside each request's tile rectangle (frames differ in size:
   // the grid covers the tallest, each block checks its own frame's rows)
   CUDA_TRY(launch_fill_outside(slot.d_frames.as<FrameDesc>(), n, max_h, st));
-  for (size_t gi = 0; gi < groups.size(); ++gi) {
-    const Group& g = groups[gi];
-    const int grid = s->sm_count * s->max_ctas[g.mode];
-    CUDA_TRY(launch_render_persistent_typed(g.dtype, g.mode, GBVR_SAMPLER_SW, slot.d_frames.as<FrameDesc>() + g.first,
-                                            g.count, slot.d_prefix.as<int>() + g.prefix_at,
-                                            slot.d_counter.as<int>() + gi, grid, st));
+  const int ring = (int)(slot.seq % kEventRing);
+  if (gpu_spans) CUDA_TRY(cudaEventRecord(s->k0[ring], st));
+  auto launch_groups = [&](cudaStream_t ls) -> int {
+    for (int gi = 0; gi < kServerGroups; ++gi) {
+      if (!(mask >> gi & 1)) continue;
+      const GroupShape& sh = force ? *force : s->shape[gi];
+      CUDA_TRY(launch_render_persistent_group(gi >> 2, gi & 3, slot.d_frames.as<FrameDesc>(),
+                                              slot.d_groups.as<LaunchGroup>(), gi, slot.d_prefix.as<int>(),
+                                              slot.d_counter.as<int>(), group_grid(s, gi, sh), ls));
+    }
+    return GBVR_OK;
+  };
+  if (force) {
+    TRY(launch_groups(st));
+  } else {
+    if (slot.shape_version != s->shape_version) {
+      for (auto& g : slot.graphs) cudaGraphExecDestroy(g.second);
+      slot.graphs.clear();
+      slot.shape_version = s->shape_version;
+    }
+    auto it = slot.graphs.find(mask);
+    if (it == slot.graphs.end()) {
+      CUDA_TRY(cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal));
+      const int rc = launch_groups(s->capture_stream);
+      cudaGraph_t g = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(s->capture_stream, &g);
+      if (rc != GBVR_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      CUDA_TRY(ce);
+      cudaGraphExec_t ge = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      CUDA_TRY(ie);
+      it = slot.graphs.emplace(mask, ge).first;
+    }
+    CUDA_TRY(cudaGraphLaunch(it->second, st));
   }
+  if (gpu_spans) CUDA_TRY(cudaEventRecord(s->k1[ring], st));
   CUDA_TRY(cudaMemcpyAsync(slot.h_fb.p, slot.d_fb.p, slot.fb_used, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaEventRecord(slot.ev1, st));
+  CUDA_TRY(cudaLaunchHostFunc(st, slot_done_cb, &slot));
+  return GBVR_OK;
+}
+
+// Compare the kernel spans of batches a < b (consecutive sequence numbers,
+// both complete): overlapped when b's kernels started before a's ended.
+void count_overlap(gbvr_server* s, uint64_t a) {
+  const int ra = (int)(a % kEventRing), rb = (int)((a + 1) % kEventRing);
+  if (!s->span_done[ra] || !s->span_done[rb] || s->span_seq[ra] != a || s->span_seq[rb] != a + 1) return;
+  float to_b = 0.f, span_a = 0.f;
+  if (cudaEventElapsedTime(&to_b, s->k0[ra], s->k0[rb]) != cudaSuccess) return;
+  if (cudaEventElapsedTime(&span_a, s->k0[ra], s->k1[ra]) != cudaSuccess) return;
+  ++s->overlap_checked;
+  if (to_b < span_a) ++s->overlapped;
+}
+
+// Retire a finished slot: pixels to the callers' buffers, statistics.
+// Worker thread, mutex held on entry and exit.
+void retire(gbvr_server* s, BatchSlot& slot, std::unique_lock<std::mutex>& lk) {
+  const cudaError_t e = cudaEventQuery(slot.ev1);
+  float ms = 0.f;
+  lk.unlock();
+  if (e == cudaSuccess) {
+    cudaEventElapsedTime(&ms, slot.ev0, slot.ev1);
+    for (size_t i = 0; i < slot.reqs.size(); ++i) {
+      const ServerRequest* q = slot.reqs[i];
+      memcpy(q->req.out_rgba8, (const char*)slot.h_fb.p + slot.fb_off[i], (size_t)q->req.width * q->req.height * 4);
+    }
+  }
+  lk.lock();
+  const double t = now_ms();
+  for (ServerRequest* q : slot.reqs) {
+    q->status = e == cudaSuccess ? GBVR_OK : GBVR_ECUDA;
+    q->t_done = t;
+    q->gpu_ms = ms;
+    if (e == cudaSuccess) {
+      s->latencies.push_back(t - q->t_submit);
+      ++s->completed;
+      s->t_last = t;
+    }
+  }
+  if (e != cudaSuccess) s->worker_error = cudaGetErrorString(e);
+  for (int d : slot.datasets) {
+    --s->datasets[d]->inflight;
+    s->datasets[d]->last_use = std::max(s->datasets[d]->last_use, slot.seq);
+  }
+  const int ring = (int)(slot.seq % kEventRing);
+  s->span_done[ring] = e == cudaSuccess;
+  s->span_seq[ring] = slot.seq;
+  if (slot.seq > 1) count_overlap(s, slot.seq - 1);
+  count_overlap(s, slot.seq);
+  ++s->batches;
+  s->batched_requests += slot.reqs.size();
+  slot.busy = false;
+  slot.done = false;
+  slot.reqs.clear();
+  slot.datasets.clear();
+  s->blocked = false;
+  s->cv_done.notify_all();
+}
+
+// Order the batch's requests by group (each group one contiguous run of
+// frames) and take the per-request pointers the launch reads.  Mutex held.
+void snapshot_batch(gbvr_server* s, BatchSlot& slot) {
+  const int n = (int)slot.reqs.size();
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return group_of(s, slot.reqs[x]) < group_of(s, slot.reqs[y]); });
+  std::vector<ServerRequest*> sorted(n);
+  std::vector<size_t> offs(n);
+  for (int i = 0; i < n; ++i) {
+    sorted[i] = slot.reqs[order[i]];
+    offs[i] = slot.fb_off[order[i]];
+  }
+  slot.reqs.swap(sorted);
+  slot.fb_off.swap(offs);
+  slot.req_ds.resize(n);
+  slot.req_tf.resize(n);
+  slot.req_gi.resize(n);
+  for (int i = 0; i < n; ++i) {
+    const ServerRequest* q = slot.reqs[i];
+    slot.req_ds[i] = s->datasets[q->req.dataset]->ds.get();
+    slot.req_tf[i] = s->tfs[q->req.tf].get();
+    slot.req_gi[i] = group_of(s, q);
+  }
+  slot.dsets.clear();
+  for (int d : slot.datasets) slot.dsets.push_back(s->datasets[d].get());
+}
+
+// Fill `slot` from the pending requests (arrival order; a request whose
+// dataset cannot be made resident now is passed over and stays pending).
+// Worker thread, mutex held.  Returns the status of an upload failure.
+int assemble(gbvr_server* s, BatchSlot& slot) {
+  slot.reqs.clear();
+  slot.fb_off.clear();
+  slot.datasets.clear();
+  const size_t slot_budget = s->params.fb_budget_bytes / s->nslots;
+  size_t used = 0;
+  for (auto it = s->pending.begin(); it != s->pending.end() && (int)slot.reqs.size() < s->params.max_batch;) {
+    ServerRequest* q = *it;
+    const size_t aligned = ((size_t)q->req.width * q->req.height * 4 + 255) & ~(size_t)255;
+    if (used + aligned > slot_budget) break;  // the framebuffer share is full: the rest wait
+    const int d = q->req.dataset;
+    ServerDataset& D = *s->datasets[d];
+    if (!D.resident) {
+      int rc = GBVR_OK;
+      if (!make_resident(s, D, slot.stream, slot.datasets, rc)) {
+        if (rc != GBVR_OK) return rc;
+        ++it;  // waits until its pool fits
+        continue;
+      }
+    }
+    it = s->pending.erase(it);
+    if (std::find(slot.datasets.begin(), slot.datasets.end(), d) == slot.datasets.end()) slot.datasets.push_back(d);
+    slot.reqs.push_back(q);
+    slot.fb_off.push_back(used);
+    used += aligned;
+  }
+  slot.fb_used = used;
+  snapshot_batch(s, slot);
   return GBVR_OK;
 }
 
 void server_worker(gbvr_server* s) {
   cudaSetDevice(s->device);
-  const size_t slot_budget = s->params.fb_budget_bytes / 2;
   std::unique_lock<std::mutex> lk(s->mu);
-  for (;;) {
-    const bool in_flight = s->slots[0].busy || s->slots[1].busy;
-    if (in_flight) {
-      // poll the batch in flight, waking early when new requests arrive so
-      // a free slot can be filled and queued behind it
-      s->cv_work.wait_for(lk, std::chrono::microseconds(100));
-    } else {
-      s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty(); });
+  auto any_busy = [&] {
+    for (auto& sl : s->slots)
+      if (sl->busy) return true;
+    return false;
+  };
+  auto ready = [&] {
+    if (s->stop) return true;
+    for (auto& sl : s->slots) {
+      if (sl->busy && sl->done) return true;
+      if (!sl->busy && !s->pending.empty() && !s->blocked && !s->tuning) return true;
     }
-    if (s->stop && s->pending.empty() && !s->slots[0].busy && !s->slots[1].busy) break;
-    // fill every free slot with pending requests
-    for (auto& slot : s->slots) {
-      if (slot.busy || s->pending.empty()) continue;
-      slot.reqs.clear();
-      slot.fb_off.clear();
-      size_t used = 0;
-      while (!s->pending.empty() && (int)slot.reqs.size() < s->params.max_batch) {
-        ServerRequest* q = s->pending.front();
-        const size_t bytes = (size_t)q->req.width * q->req.height * 4;
-        const size_t aligned = (bytes + 255) & ~(size_t)255;
-        if (aligned > slot_budget) {  // can never be admitted
-          s->pending.pop_front();
-          q->status = GBVR_EINVAL;
-          q->t_done = now_ms();
-          s->cv_done.notify_all();
-          continue;
-        }
-        if (used + aligned > slot_budget) break;  // waits for the next batch
-        s->pending.pop_front();
-        slot.reqs.push_back(q);
-        slot.fb_off.push_back(used);
-        used += aligned;
+    return false;
+  };
+  for (;;) {
+    s->cv_work.wait(lk, ready);
+    if (s->stop && s->pending.empty() && !any_busy()) break;
+    for (auto& sl : s->slots)
+      if (sl->busy && sl->done) retire(s, *sl, lk);
+    for (auto& slp : s->slots) {
+      BatchSlot& slot = *slp;
+      if (slot.busy || s->pending.empty() || s->tuning || s->blocked) continue;
+      int rc = assemble(s, slot);
+      if (rc == GBVR_OK && slot.reqs.empty()) {
+        s->blocked = true;  // nothing admissible until a batch retires or a request arrives
+        continue;
       }
-      if (slot.reqs.empty()) continue;
-      slot.fb_used = used;
       slot.busy = true;
+      slot.done = false;
       slot.seq = s->next_batch++;
       const double t = now_ms();
       for (ServerRequest* q : slot.reqs) {
@@ -3586,60 +4092,38 @@ void server_worker(gbvr_server* s) {
         q->batch = slot.seq;
         q->batch_size = (int)slot.reqs.size();
       }
-      lk.unlock();
-      int rc;
-      try {  // the worker thread must not end on an exception: the batch fails instead
-        rc = launch_batch(s, slot);
-      } catch (const std::bad_alloc&) {
-        rc = fail(GBVR_ENOMEM, "out of host memory");
-      } catch (const std::exception& e) {
-        rc = fail(GBVR_EINVAL, e.what());
+      for (int d : slot.datasets) ++s->datasets[d]->inflight;
+      if (rc == GBVR_OK) {
+        lk.unlock();
+        try {  // the worker thread must not end on an exception: the batch fails instead
+          rc = launch_batch(s, slot, nullptr, true);
+        } catch (const std::bad_alloc&) {
+          rc = fail(GBVR_ENOMEM, "out of host memory");
+        } catch (const std::exception& e) {
+          rc = fail(GBVR_EINVAL, e.what());
+        }
+        lk.lock();
       }
-      lk.lock();
       if (rc != GBVR_OK) {
+        // the batch never reached the GPU (or only its uploads did): fail its requests
+        if (slot.stream) {
+          lk.unlock();
+          cudaStreamSynchronize(slot.stream);
+          lk.lock();
+        }
         s->worker_error = g_err;
         for (ServerRequest* q : slot.reqs) {
           q->status = rc;
           q->t_done = now_ms();
         }
+        for (int d : slot.datasets) --s->datasets[d]->inflight;
+        slot.reqs.clear();
+        slot.datasets.clear();
         slot.busy = false;
+        slot.done = false;
         s->cv_done.notify_all();
       }
     }
-    // retire the oldest batch in flight once its copies have landed
-    BatchSlot* oldest = nullptr;
-    for (auto& slot : s->slots)
-      if (slot.busy && (!oldest || slot.seq < oldest->seq)) oldest = &slot;
-    if (!oldest) continue;
-    cudaError_t e = cudaEventQuery(oldest->ev1);
-    if (e == cudaErrorNotReady) continue;
-    lk.unlock();
-    float ms = 0.f;
-    if (e == cudaSuccess) cudaEventElapsedTime(&ms, oldest->ev0, oldest->ev1);
-    if (e == cudaSuccess)
-      for (size_t i = 0; i < oldest->reqs.size(); ++i) {
-        const ServerRequest* q = oldest->reqs[i];
-        memcpy(q->req.out_rgba8, (const char*)oldest->h_fb.p + oldest->fb_off[i],
-               (size_t)q->req.width * q->req.height * 4);
-      }
-    lk.lock();
-    const double t = now_ms();
-    for (ServerRequest* q : oldest->reqs) {
-      q->status = e == cudaSuccess ? GBVR_OK : GBVR_ECUDA;
-      q->t_done = t;
-      q->gpu_ms = ms;
-      if (e == cudaSuccess) {
-        s->latencies.push_back(t - q->t_submit);
-        ++s->completed;
-        s->t_last = t;
-      }
-    }
-    if (e != cudaSuccess) s->worker_error = cudaGetErrorString(e);
-    ++s->batches;
-    s->batched_requests += oldest->reqs.size();
-    oldest->busy = false;
-    oldest->reqs.clear();
-    s->cv_done.notify_all();
   }
 }
 
@@ -3650,15 +4134,43 @@ int check_s(gbvr_server* s) {
 
 int server_add_dataset(gbvr_server* s, DevBuf& lv, int dtype, const long long d[3], const gbvr_brick_params* bp,
                        int* id) {
-  std::unique_ptr<Dataset> ds(new Dataset());
+  std::unique_ptr<ServerDataset> sd(new ServerDataset());
+  sd->ds.reset(new Dataset());
   gbvr_brick_params b = {};
   if (bp) b = *bp;
   if (b.layouts == 0) b.layouts = 4;
-  TRY(build_dataset(*ds, lv, dtype, d, &b, s->stream));
+  b.build_texture = 0;  // the serving launches sample in software
+  TRY(build_dataset(*sd->ds, lv, dtype, d, &b, s->stream));
+  sd->pool_bytes = sd->ds->pool.n;
+  CUDA_TRY(cudaEventCreateWithFlags(&sd->uploaded, cudaEventDisableTiming));
+  if (s->params.device_pool_bytes > 0) {
+    if (sd->pool_bytes > s->params.device_pool_bytes)
+      return fail(GBVR_EINVAL, "the dataset's brick pool (" + std::to_string(sd->pool_bytes) +
+                                   " bytes) exceeds the server's device_pool_bytes");
+    // a page-locked copy of the pool; it is made resident when a request needs it
+    CUDA_TRY(sd->host_pool.alloc(sd->pool_bytes));
+    CUDA_TRY(cudaMemcpyAsync(sd->host_pool.p, sd->ds->pool.p, sd->pool_bytes, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    sd->ds->pool.release();
+    sd->resident = false;
+  }
   std::lock_guard<std::mutex> lk(s->mu);
-  s->datasets.push_back(std::move(ds));
+  if (sd->resident) s->resident_bytes += sd->pool_bytes;
+  s->datasets.push_back(std::move(sd));
   if (id) *id = (int)s->datasets.size() - 1;
   return GBVR_OK;
+}
+
+// Wait until no batch is in flight and keep the worker from launching
+// (autotuner); mutex held on entry and exit.
+void pause_worker(gbvr_server* s, std::unique_lock<std::mutex>& lk) {
+  s->tuning = true;
+  for (;;) {
+    bool busy = false;
+    for (auto& sl : s->slots) busy = busy || sl->busy;
+    if (!busy) break;
+    s->cv_done.wait(lk);
+  }
 }
 
 }  // namespace
@@ -3679,16 +4191,30 @@ int gbvr_server_create(const gbvr_server_params* params, gbvr_server** out) {
   if (p.tile_w == 0) p.tile_w = TILE_W;
   if (p.tile_w != 4 && p.tile_w != 8 && p.tile_w != 16 && p.tile_w != 32) return fail(GBVR_EINVAL, "bad tile_w");
   if (p.fb_budget_bytes == 0) p.fb_budget_bytes = (uint64_t)2 << 30;
+  if (p.slots == 0) p.slots = 3;
+  if (p.slots < 1 || p.slots > kMaxServerSlots) return fail(GBVR_EINVAL, "slots must lie in [1, 8]");
   s->params = p;
+  s->nslots = p.slots;
+  for (auto& g : s->shape) g.tile_w = p.tile_w;
   CUDA_TRY(cudaGetDevice(&s->device));
   CUDA_TRY(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device));
-  for (int m = 0; m < 4; ++m) s->max_ctas[m] = std::max(1, persistent_grid_size(s->device, m) / std::max(s->sm_count, 1));
+  for (int m = 0; m < 4; ++m) s->max_ctas[m] = persistent_group_ctas_per_sm(m);
   CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
-  for (auto& slot : s->slots) {
-    CUDA_TRY(cudaEventCreate(&slot.ev0));
-    CUDA_TRY(cudaEventCreate(&slot.ev1));
-    CUDA_TRY(slot.d_fb.alloc(p.fb_budget_bytes / 2));
-    CUDA_TRY(slot.h_fb.alloc(p.fb_budget_bytes / 2));
+  CUDA_TRY(cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking));
+  for (int i = 0; i < kEventRing; ++i) {
+    CUDA_TRY(cudaEventCreate(&s->k0[i]));
+    CUDA_TRY(cudaEventCreate(&s->k1[i]));
+  }
+  for (int i = 0; i < s->nslots; ++i) {
+    std::unique_ptr<BatchSlot> sl(new BatchSlot());
+    sl->server = s.get();
+    sl->index = i;
+    CUDA_TRY(cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&sl->ev0));
+    CUDA_TRY(cudaEventCreate(&sl->ev1));
+    CUDA_TRY(sl->d_fb.alloc(p.fb_budget_bytes / s->nslots));
+    CUDA_TRY(sl->h_fb.alloc(p.fb_budget_bytes / s->nslots));
+    s->slots.push_back(std::move(sl));
   }
   gbvr_server* raw = s.get();
   s->worker = std::thread(server_worker, raw);
@@ -3711,10 +4237,14 @@ int gbvr_server_add_volume(gbvr_server* s, const void* host, const int64_t dims[
   if (!host || !dims || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0 || dtype < 0 || dtype > 2)
     return fail(GBVR_EINVAL, "bad volume");
   long long d[3] = {dims[0], dims[1], dims[2]};
-  const size_t bytes = (size_t)d[0] * d[1] * d[2] * dtype_size(dtype);
+  unsigned long long bytes = 0;
+  if (__builtin_mul_overflow((unsigned long long)d[0], (unsigned long long)d[1], &bytes) ||
+      __builtin_mul_overflow(bytes, (unsigned long long)d[2], &bytes) ||
+      __builtin_mul_overflow(bytes, (unsigned long long)dtype_size(dtype), &bytes))
+    return fail(GBVR_EINVAL, "the volume's byte count overflows");
   DevBuf lv;
-  CUDA_TRY(lv.alloc(bytes));
-  CUDA_TRY(cudaMemcpyAsync(lv.p, host, bytes, cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(lv.alloc((size_t)bytes));
+  CUDA_TRY(cudaMemcpyAsync(lv.p, host, (size_t)bytes, cudaMemcpyHostToDevice, s->stream));
   return server_add_dataset(s, lv, dtype, d, bp, id);
   GBVR_ABI_CATCH
 }
@@ -3733,7 +4263,12 @@ int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba,
                        float iso, const float iso_rgb[3], double lo, double hi, int* tf_id) {
   GBVR_ABI_TRY
   TRY(check_s(s));
-  if (dataset < 0 || dataset >= (int)s->datasets.size()) return fail(GBVR_EINVAL, "bad dataset id");
+  const Dataset* dsp = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (dataset < 0 || dataset >= (int)s->datasets.size()) return fail(GBVR_EINVAL, "bad dataset id");
+    dsp = s->datasets[dataset]->ds.get();
+  }
   if (mode < 0 || mode > 3) return fail(GBVR_EINVAL, "bad render mode");
   if (mode == GBVR_RM_1DTRANS || mode == GBVR_RM_MIP) h = 1;
   if (mode == GBVR_RM_ISOSURFACE) {
@@ -3741,7 +4276,7 @@ int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba,
     if (!rgba) { rgba = dummy; w = 2; h = 1; }
   }
   if (!rgba || w < 2 || h < 1 || w > 65536 || h > 4096) return fail(GBVR_EINVAL, "bad transfer function size");
-  const Dataset& ds = *s->datasets[dataset];
+  const Dataset& ds = *dsp;
   std::unique_ptr<ServerTf> t(new ServerTf());
   t->dataset = dataset;
   t->mode = mode;
@@ -3764,6 +4299,7 @@ int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba,
   const std::vector<float> dev = mode == GBVR_RM_2DTRANS ? t->host : tf1d_pairs(t->host.data(), w);
   CUDA_TRY(t->d_tf.alloc(sizeof(float) * dev.size()));
   CUDA_TRY(cudaMemcpyAsync(t->d_tf.p, dev.data(), sizeof(float) * dev.size(), cudaMemcpyHostToDevice, s->stream));
+  // classification reads the per-level macro-cell grids, which stay resident
   TRY(classify_level(ds, t->level, t->host, w, h, mode, t->lo, t->hi, t->iso, t->d_prefix, t->d_skip, t->d_occ,
                      t->d_occtmp, s->stream));
   std::lock_guard<std::mutex> lk(s->mu);
@@ -3778,6 +4314,7 @@ int gbvr_server_submit(gbvr_server* s, const gbvr_request* req, uint64_t* ticket
   TRY(check_s(s));
   if (!req || !req->out_rgba8 || req->width <= 0 || req->height <= 0 || req->width > 16384 || req->height > 16384)
     return fail(GBVR_EINVAL, "bad request");
+  const size_t fb = ((size_t)req->width * req->height * 4 + 255) & ~(size_t)255;
   std::unique_ptr<ServerRequest> q(new ServerRequest());
   q->req = *req;
   {
@@ -3785,6 +4322,8 @@ int gbvr_server_submit(gbvr_server* s, const gbvr_request* req, uint64_t* ticket
     if (req->dataset < 0 || req->dataset >= (int)s->datasets.size() || req->tf < 0 || req->tf >= (int)s->tfs.size() ||
         s->tfs[req->tf]->dataset != req->dataset)
       return fail(GBVR_EINVAL, "request names an unknown dataset or a transfer function of another dataset");
+    if (fb > s->params.fb_budget_bytes / s->nslots)
+      return fail(GBVR_EINVAL, "the request's framebuffer exceeds a batch slot's share of fb_budget_bytes");
     q->ticket = s->next_ticket++;
     q->t_submit = now_ms();
     if (s->t_first < 0) s->t_first = q->t_submit;
@@ -3792,8 +4331,9 @@ int gbvr_server_submit(gbvr_server* s, const gbvr_request* req, uint64_t* ticket
     if (ticket) *ticket = q->ticket;
     s->pending.push_back(q.get());
     s->reqs.emplace(q->ticket, std::move(q));
+    s->blocked = false;
   }
-  s->cv_work.notify_one();
+  s->cv_work.notify_all();
   return GBVR_OK;
   GBVR_ABI_CATCH
 }
@@ -3846,6 +4386,12 @@ int gbvr_server_get_stats(gbvr_server* s, gbvr_server_stats* out) {
     out->max_ms = l.back();
   }
   if (s->completed && s->t_last > s->t_first) out->frames_per_s = s->completed / ((s->t_last - s->t_first) / 1000.0);
+  out->overlap_checked = s->overlap_checked;
+  out->overlapped = s->overlapped;
+  out->uploads = s->uploads;
+  out->evictions = s->evictions;
+  out->upload_bytes = s->upload_bytes;
+  out->resident_bytes = s->resident_bytes;
   return GBVR_OK;
   GBVR_ABI_CATCH
 }
@@ -3856,9 +4402,126 @@ int gbvr_server_reset_stats(gbvr_server* s) {
   std::lock_guard<std::mutex> lk(s->mu);
   s->latencies.clear();
   s->submitted = s->completed = s->batches = s->batched_requests = 0;
+  s->overlap_checked = s->overlapped = s->uploads = s->evictions = s->upload_bytes = 0;
   s->t_first = -1;
   s->t_last = 0;
   return GBVR_OK;
+  GBVR_ABI_CATCH
+}
+
+int gbvr_server_autotune(gbvr_server* s, int width, int height, int n, gbvr_server_tune* out, int cap, int* n_out) {
+  GBVR_ABI_TRY
+  TRY(check_s(s));
+  if (width <= 0 || height <= 0 || n <= 0 || n > s->params.max_batch || (cap > 0 && !out))
+    return fail(GBVR_EINVAL, "bad tuning batch (width, height > 0; 0 < n <= max_batch)");
+  const size_t fb = ((size_t)width * height * 4 + 255) & ~(size_t)255;
+  if (fb * n > s->params.fb_budget_bytes / s->nslots)
+    return fail(GBVR_EINVAL, "the tuning batch exceeds a batch slot's framebuffer share");
+  std::unique_lock<std::mutex> lk(s->mu);
+  pause_worker(s, lk);
+  BatchSlot& slot = *s->slots[0];
+  // per group: one dataset (the first of the group that fits the memory
+  // budget) and its presets in turn
+  struct Plan { int gi, dataset; std::vector<int> tfs; };
+  std::vector<Plan> plans;
+  for (int gi = 0; gi < kServerGroups; ++gi) {
+    Plan pl{gi, -1, {}};
+    for (size_t t = 0; t < s->tfs.size(); ++t) {
+      const ServerTf& tf = *s->tfs[t];
+      const ServerDataset& D = *s->datasets[tf.dataset];
+      if (D.ds->dtype * 4 + tf.mode != gi) continue;
+      if (pl.dataset < 0) pl.dataset = tf.dataset;
+      if (tf.dataset == pl.dataset) pl.tfs.push_back((int)t);
+    }
+    if (pl.dataset >= 0) plans.push_back(pl);
+  }
+  int rc = GBVR_OK;
+  int count = 0;
+  std::vector<uint8_t> sink(fb);
+  std::vector<ServerRequest> fake(n);
+  const int tiles[] = {4, 8, 16};
+  for (const Plan& pl : plans) {
+    ServerDataset& D = *s->datasets[pl.dataset];
+    slot.datasets.assign(1, pl.dataset);
+    if (!D.resident && !make_resident(s, D, slot.stream, slot.datasets, rc)) {
+      if (rc != GBVR_OK) break;
+      continue;  // does not fit next to the pinned datasets: keep its default shape
+    }
+    ++D.inflight;
+    for (int i = 0; i < n; ++i) {
+      ServerRequest& q = fake[i];
+      memset(&q.req, 0, sizeof(q.req));
+      q.req.dataset = pl.dataset;
+      q.req.tf = pl.tfs[i % pl.tfs.size()];
+      q.req.width = width;
+      q.req.height = height;
+      q.req.samples_per_voxel = 1.f;
+      q.req.out_rgba8 = sink.data();
+      orbit(360.0 * i / n, 25.0 * std::sin(0.7 * i), 2.5 * std::sqrt(3.0), 45.0, width, height, q.req.view,
+            q.req.proj);
+    }
+    slot.reqs.clear();
+    slot.fb_off.clear();
+    for (int i = 0; i < n; ++i) {
+      slot.reqs.push_back(&fake[i]);
+      slot.fb_off.push_back((size_t)i * fb);
+    }
+    slot.fb_used = fb * n;
+    snapshot_batch(s, slot);
+    lk.unlock();
+    const int m = pl.gi & 3;
+    const GroupShape def{s->params.tile_w, 0};
+    std::vector<GroupShape> cands;
+    cands.push_back(def);
+    for (int tw : tiles)
+      for (int c : {s->max_ctas[m], std::max(1, s->max_ctas[m] - 2), std::max(1, s->max_ctas[m] / 2)})
+        if (!(tw == def.tile_w && c == s->max_ctas[m])) cands.push_back(GroupShape{tw, c});
+    float best = 1e30f, def_ms = 0.f;
+    GroupShape best_shape = def;
+    for (size_t ci = 0; ci < cands.size() && rc == GBVR_OK; ++ci) {
+      float ms_best = 1e30f;
+      for (int rep = 0; rep < 3 && rc == GBVR_OK; ++rep) {  // one warm-up, best of two
+        rc = launch_batch(s, slot, &cands[ci], false);
+        if (rc == GBVR_OK) {
+          cudaError_t e = cudaStreamSynchronize(slot.stream);
+          float ms = 0.f;
+          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, slot.ev0, slot.ev1);
+          if (e != cudaSuccess) rc = cuda_fail(e, "tuning batch");
+          else if (rep > 0) ms_best = std::min(ms_best, ms);
+        }
+      }
+      if (ci == 0) def_ms = ms_best;
+      if (ms_best < best) {
+        best = ms_best;
+        best_shape = cands[ci];
+      }
+    }
+    lk.lock();
+    --D.inflight;
+    if (rc != GBVR_OK) break;
+    s->shape[pl.gi] = best_shape;
+    if (out && count < cap) {
+      gbvr_server_tune& r = out[count];
+      r.dtype = pl.gi >> 2;
+      r.mode = m;
+      r.tile_w = best_shape.tile_w;
+      r.ctas_per_sm = best_shape.ctas_per_sm > 0 ? best_shape.ctas_per_sm : s->max_ctas[m];
+      r.candidates = (int)cands.size();
+      r.best_ms = best;
+      r.default_ms = def_ms;
+    }
+    ++count;
+  }
+  slot.reqs.clear();
+  slot.datasets.clear();
+  slot.dsets.clear();
+  slot.done = false;
+  ++s->shape_version;  // the slots re-capture their graphs with the new shapes
+  s->tuning = false;
+  lk.unlock();
+  s->cv_work.notify_all();
+  if (n_out) *n_out = std::min(count, cap);
+  return rc;
   GBVR_ABI_CATCH
 }
 

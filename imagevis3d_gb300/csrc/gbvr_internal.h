@@ -77,7 +77,9 @@ struct __align__(16) FrameDesc {
   float amb[3], diff[3], spec[3];
   float shininess;
   float light_to[3];         // unit vector towards the light, world space
-  float bg[3];
+  float bg[3];               // background; with bg_grad the bottom edge's colour
+  float bg_top[3];           // bg_grad: the top edge's colour (setBGColors' top)
+  int bg_grad;               // 1: vertical gradient from bg_top (top edge) to bg (bottom edge)
   // camera
   float inv_vp[16];          // row-major inverse of proj*view
   int width, height;
@@ -191,6 +193,14 @@ cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, con
                                            int nframes, const int* tile_prefix, int* counter, int grid,
                                            cudaStream_t s);
 int persistent_grid_size(int device, int mode);
+// One (voxel type, mode) group of a serving batch: frames [first, first +
+// count) of the batch's descriptor array, tile prefix at prefix_at.
+struct LaunchGroup {
+  int first, count, prefix_at, pad;
+};
+cudaError_t launch_render_persistent_group(int dtype, int mode, const FrameDesc* frames, const LaunchGroup* groups,
+                                           int gi, const int* prefix, int* counters, int grid, cudaStream_t s);
+int persistent_group_ctas_per_sm(int mode);
 // Background (RGBA = bg, 0) into every pixel of each frame outside its tile
 // rectangle, as a ray that misses the volume leaves it.
 // (frames of different sizes: max_height is the tallest; each block checks its frame's size)
@@ -200,9 +210,12 @@ cudaError_t launch_fill_outside_one(const FrameDesc& f, cudaStream_t s);
 // and counters: the shared part travels as a kernel parameter (constant
 // bank), each view's part is read from `frames` (camera, light direction,
 // outputs, sample counter).
+// sps: samples per step of the inner loop (2 only for the 1D TF with the
+// software sampler; otherwise 1)
 cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, const FrameDesc& shared,
-                                             const FrameDesc* frames, int nframes, const int* tile_prefix,
-                                             int* counter, int grid, cudaStream_t s);
+                                             const FrameDesc* frames, int nframes, const int* prefix, int* counter,
+                                             int grid, cudaStream_t s, int sps = 1);
+int persistent_ctas_per_sm_sps2();
 int persistent_grid_size_uniform(int device, int mode);
 cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStream_t s);
 // then, for frames [frame0, frame0 + n) of `frames` (device), each covered
@@ -256,6 +269,9 @@ cudaError_t launch_gather_bricks(const void* level, int dtype, const long long d
                                  int perm, cudaStream_t s);
 // bricks from a window of the level holding planes vz0.. (their stored boxes,
 // clamped to the level, must lie in the window)
+// The flat level back from the interiors of its bricks (x-fastest copy).
+cudaError_t launch_scatter_interiors(const void* pool, int dtype, const BrickInfo* bricks, int nbricks,
+                                     const long long dims[3], void* level, cudaStream_t s);
 cudaError_t launch_gather_bricks_window(const void* level, int dtype, const long long dims[3], long long vz0,
                                         const BrickInfo* bricks_dev, int nbricks, void* pool, int perm,
                                         cudaStream_t s);

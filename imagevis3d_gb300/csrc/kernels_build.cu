@@ -281,6 +281,44 @@ __global__ void k_gather(const T* __restrict__ level, long long X, long long Y, 
   }
 }
 
+// The inverse of k_gather for the x-fastest copy: every brick's interior
+// voxels (its [max(lo, 0), min(hi, dims)) box) back into the flat level.  The
+// interiors tile the level, so every voxel is written once.  One block per
+// brick, plane by plane.
+template <typename T>
+__global__ void k_scatter_interiors(const T* __restrict__ pool, const BrickInfo* __restrict__ bricks, long long X,
+                                    long long Y, long long Z, T* __restrict__ level) {
+  const BrickInfo b = bricks[blockIdx.x];
+  const long long x0 = max(b.lox, 0), x1 = min((long long)b.hix, X);
+  const long long y0 = max(b.loy, 0), y1 = min((long long)b.hiy, Y);
+  const long long z0 = max(b.loz, 0), z1 = min((long long)b.hiz, Z);
+  const long long nx = x1 - x0;
+  for (long long z = z0 + blockIdx.y; z < z1; z += gridDim.y)
+    for (long long y = y0; y < y1; ++y)
+      for (long long i = threadIdx.x; i < nx; i += blockDim.x) {
+        const long long x = x0 + i;
+        const long long src = ((z - b.oz) * b.sy + (y - b.oy)) * b.sx + (x - b.ox);
+        level[(z * Y + y) * X + x] = __ldg(pool + b.offset + src);
+      }
+}
+
+cudaError_t launch_scatter_interiors(const void* pool, int dtype, const BrickInfo* bricks, int nbricks,
+                                     const long long dims[3], void* level, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (nbricks <= 0) return cudaSuccess;
+  dim3 grid((unsigned)nbricks, 16);
+  if (dtype == DT_U8)
+    k_scatter_interiors<uint8_t><<<grid, 256, 0, s>>>((const uint8_t*)pool, bricks, dims[0], dims[1], dims[2],
+                                                      (uint8_t*)level);
+  else if (dtype == DT_U16)
+    k_scatter_interiors<uint16_t><<<grid, 256, 0, s>>>((const uint16_t*)pool, bricks, dims[0], dims[1], dims[2],
+                                                       (uint16_t*)level);
+  else
+    k_scatter_interiors<float><<<grid, 256, 0, s>>>((const float*)pool, bricks, dims[0], dims[1], dims[2],
+                                                    (float*)level);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_gather_bricks_window(const void* level, int dtype, const long long dims[3], long long vz0,
                                         const BrickInfo* bricks_dev, int nbricks, void* pool, int perm,
                                         cudaStream_t s) {

@@ -483,7 +483,11 @@ __device__ __forceinline__ bool composite(const FrameDesc& f, float4 c, Accum& a
 // over the lens radius) it gets opacity clamp(cv_context (1 - |n.v|) +
 // cv_border rho^2, 0, 1), and the march goes on to the first hit of f.cv_iso
 // (the focus surface, from the context hit's sample on), which lies behind.
-template <typename T, int MODE, int SAMPLER, bool CV = false>
+// SPS (1D TF, software sampler only): samples per step of the inner loop.
+// With 2, a step evaluates two consecutive samples -- both samples' voxel and
+// TF loads in flight together -- and composites them in order, stopping after
+// the first if it ends the ray: the same pixels as one sample per step.
+template <typename T, int MODE, int SAMPLER, bool CV = false, int SPS = 1>
 __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, int vidx, const float* light_to,
                         float cv_rho = 2.f) {
   Accum acc = {0.f, 0.f, 0.f, 0.f};
@@ -650,7 +654,29 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
         }
         if (runmax >= f.level_max) done = true;
       } else if constexpr (MODE == MODE_1D) {
-        for (; k < ke; ++k) {
+        if constexpr (SPS == 2) {
+          for (; k + 1 < ke; k += 2) {
+            float ax, ay, az, bx, by, bz;
+            pos_of(k, ax, ay, az);
+            pos_of(k + 1, bx, by, bz);
+            const Cell ca = make_cell(f, ax, ay, az);
+            const Cell cb = make_cell(f, bx, by, bz);
+            const float va = sample_cell<T, SAMPLER>(f, b, ca.x, ca.y, ca.z, ca.fx, ca.fy, ca.fz);
+            const float vb = sample_cell<T, SAMPLER>(f, b, cb.x, cb.y, cb.z, cb.fx, cb.fy, cb.fz);
+            const float4 ta = tf1d(f, va), tb = tf1d(f, vb);
+            ++nsamp;
+            if (composite<MODE>(f, ta, acc)) {
+              done = true;
+              break;
+            }
+            ++nsamp;
+            if (composite<MODE>(f, tb, acc)) {
+              done = true;
+              break;
+            }
+          }
+        }
+        for (; k < ke && !done; ++k) {
           float ax, ay, az;
           pos_of(k, ax, ay, az);
           const Cell ca = make_cell(f, ax, ay, az);
@@ -783,12 +809,24 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
   return make_float4(acc.C0, acc.C1, acc.C2, acc.A);
 }
 
+// Background colour of pixel row py (row 0 = top): f.bg, or with a gradient
+// (setBGColors with two colours) the colour at the row's centre, linear from
+// bg_top at the top edge to bg at the bottom edge.
+__device__ __forceinline__ float3 bg_at(const FrameDesc& f, int py) {
+  if (!f.bg_grad) return make_float3(f.bg[0], f.bg[1], f.bg[2]);
+  const float t = ((float)py + 0.5f) / (float)f.height;
+  return make_float3(fmaf(t, f.bg[0] - f.bg_top[0], f.bg_top[0]), fmaf(t, f.bg[1] - f.bg_top[1], f.bg_top[1]),
+                     fmaf(t, f.bg[2] - f.bg_top[2], f.bg_top[2]));
+}
+
 // What lies behind the volume: the background (adds no opacity), or an
 // opaque bounding-box line.
-__device__ __forceinline__ float4 behind(const FrameDesc& f, float4 c, unsigned line) {
+__device__ __forceinline__ float4 behind(const FrameDesc& f, float4 c, unsigned line, int py) {
   const float rem = 1.f - c.w;
-  if (line == NO_LINE)
-    return make_float4(fmaf(rem, f.bg[0], c.x), fmaf(rem, f.bg[1], c.y), fmaf(rem, f.bg[2], c.z), c.w);
+  if (line == NO_LINE) {
+    const float3 bg = bg_at(f, py);
+    return make_float4(fmaf(rem, bg.x, c.x), fmaf(rem, bg.y, c.y), fmaf(rem, bg.z, c.z), c.w);
+  }
   const float* lc = f.line_rgb[line & 1u];
   return make_float4(fmaf(rem, lc[0], c.x), fmaf(rem, lc[1], c.y), fmaf(rem, lc[2], c.z), c.w + rem);
 }
@@ -803,7 +841,7 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
   if (px < f.width && py < f.height) {
     RaySetup r;
     setup_ray(f, px, py, r);
-    float4 c = behind(f, march<T, MODE, SAMPLER>(f, r, nsamp, 0, f.light_to), NO_LINE);
+    float4 c = behind(f, march<T, MODE, SAMPLER>(f, r, nsamp, 0, f.light_to), NO_LINE, py);
     const size_t o = (size_t)py * f.width + px;
     if (f.out_f32) f.out_f32[o] = c;
     if (f.out_rgba8) {
@@ -820,7 +858,7 @@ __device__ __forceinline__ void render_tile(const FrameDesc& f, int tile) {
 
 // The same for a batch-uniform descriptor f (kernel parameter) and the view's
 // own descriptor fv (camera, image size, outputs, counter).
-template <typename T, int MODE, int SAMPLER>
+template <typename T, int MODE, int SAMPLER, int SPS = 1>
 __device__ __forceinline__ void render_tile_u(const FrameDesc& f, const FrameDesc& fv, int vidx, int tile) {
   const int lane = threadIdx.x & 31;
   const int tw = f.tile_w;
@@ -831,7 +869,7 @@ __device__ __forceinline__ void render_tile_u(const FrameDesc& f, const FrameDes
   if (px < f.width && py < f.height) {
     RaySetup r;
     setup_ray(fv, px, py, r);
-    float4 c = behind(f, march<T, MODE, SAMPLER>(f, r, nsamp, vidx, fv.light_to), NO_LINE);
+    float4 c = behind(f, march<T, MODE, SAMPLER, false, SPS>(f, r, nsamp, vidx, fv.light_to), NO_LINE, py);
     const size_t o = (size_t)py * f.width + px;
     float4* of = fv.out_f32;
     uchar4* o8 = fv.out_rgba8;
@@ -857,6 +895,9 @@ constexpr int RENDER_THREADS = 128;
 // 8 voxels and 12 tap offsets for its gradient); the isosurface path 8 (64).
 template <int MODE>
 constexpr int uniform_ctas_per_sm() { return (MODE == MODE_1D || MODE == MODE_MIP) ? 10 : (MODE == MODE_2D ? 6 : 8); }
+// Two samples per step keep two samples' voxels live: 8 CTAs/SM (64 registers).
+template <int MODE, int SPS>
+constexpr int uniform_ctas_per_sm_sps() { return SPS == 2 ? 8 : uniform_ctas_per_sm<MODE>(); }
 
 template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
@@ -894,6 +935,74 @@ __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
   }
 }
 
+// Serving batches: the group's frames, frame count and tile prefix come from
+// a table in device memory (written before each launch), so one captured
+// launch per (voxel type, mode) group serves every batch; a group with no
+// frames in a batch returns at once.
+template <typename T, int MODE, int SAMPLER>
+__global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
+    k_render_persistent_g(const FrameDesc* __restrict__ frames, const LaunchGroup* __restrict__ groups, int gi,
+                          const int* __restrict__ tile_prefix, int* __restrict__ counters) {
+  const LaunchGroup g = groups[gi];
+  if (g.count <= 0) return;
+  const FrameDesc* fr = frames + g.first;
+  const int* prefix = tile_prefix + g.prefix_at;
+  int* counter = counters + gi;
+  const int lane = threadIdx.x & 31;
+  const int total = __ldg(prefix + g.count);
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(counter, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= total) return;
+    int fi = find_frame(prefix, g.count, item);
+    render_tile<T, MODE, SAMPLER>(fr[fi], item - __ldg(prefix + fi));
+  }
+}
+
+template <typename T, int MODE>
+static cudaError_t persistent_g_t(const FrameDesc* frames, const LaunchGroup* groups, int gi, const int* prefix,
+                                  int* counters, int grid, cudaStream_t s) {
+  k_render_persistent_g<T, MODE, SAMPLER_SW><<<grid, RENDER_THREADS, 0, s>>>(frames, groups, gi, prefix, counters);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render_persistent_group(int dtype, int mode, const FrameDesc* frames, const LaunchGroup* groups,
+                                           int gi, const int* prefix, int* counters, int grid, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (grid <= 0) return cudaErrorInvalidValue;
+  switch (dtype * 4 + mode) {
+    case 0: return persistent_g_t<uint8_t, MODE_1D>(frames, groups, gi, prefix, counters, grid, s);
+    case 1: return persistent_g_t<uint8_t, MODE_2D>(frames, groups, gi, prefix, counters, grid, s);
+    case 2: return persistent_g_t<uint8_t, MODE_ISO>(frames, groups, gi, prefix, counters, grid, s);
+    case 3: return persistent_g_t<uint8_t, MODE_MIP>(frames, groups, gi, prefix, counters, grid, s);
+    case 4: return persistent_g_t<uint16_t, MODE_1D>(frames, groups, gi, prefix, counters, grid, s);
+    case 5: return persistent_g_t<uint16_t, MODE_2D>(frames, groups, gi, prefix, counters, grid, s);
+    case 6: return persistent_g_t<uint16_t, MODE_ISO>(frames, groups, gi, prefix, counters, grid, s);
+    case 7: return persistent_g_t<uint16_t, MODE_MIP>(frames, groups, gi, prefix, counters, grid, s);
+    case 8: return persistent_g_t<float, MODE_1D>(frames, groups, gi, prefix, counters, grid, s);
+    case 9: return persistent_g_t<float, MODE_2D>(frames, groups, gi, prefix, counters, grid, s);
+    case 10: return persistent_g_t<float, MODE_ISO>(frames, groups, gi, prefix, counters, grid, s);
+    case 11: return persistent_g_t<float, MODE_MIP>(frames, groups, gi, prefix, counters, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// Resident CTAs per SM of the group kernel of a mode (its launch bounds).
+int persistent_group_ctas_per_sm(int mode) {
+  int per_sm = 0;
+  if (mode == MODE_1D || mode == MODE_MIP)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_g<uint16_t, MODE_1D, SAMPLER_SW>,
+                                                  RENDER_THREADS, 0);
+  else if (mode == MODE_2D)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_g<uint16_t, MODE_2D, SAMPLER_SW>,
+                                                  RENDER_THREADS, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_g<uint16_t, MODE_ISO, SAMPLER_SW>,
+                                                  RENDER_THREADS, 0);
+  return per_sm < 1 ? 1 : per_sm;
+}
+
 // Background outside a frame's tile rectangle.  A block covers FILL_ROWS rows
 // of one frame; its threads stride along each row (coalesced 4-byte RGBA8 or
 // 16-byte float stores) and skip the rectangle's span on the rows it crosses.
@@ -907,13 +1016,14 @@ __device__ __forceinline__ void fill_outside_rows(const FrameDesc& f, int row_bl
   const int th = 32 / f.tile_w;
   const int rx0 = f.tx0 * f.tile_w, rx1 = (f.tx0 + f.ntx) * f.tile_w;
   const int ry0 = f.ty0 * th, ry1 = (f.ty0 + f.nty) * th;
-  const float4 c = make_float4(f.bg[0], f.bg[1], f.bg[2], 0.f);
-  const uchar4 c8 = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
-                                (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
-                                (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f), 0);
   uchar4* o8 = f.out_rgba8;
   float4* o32 = f.out_f32;
   for (int y = y0; y < y1; ++y) {
+    const float3 bg = bg_at(f, y);
+    const float4 c = make_float4(bg.x, bg.y, bg.z, 0.f);
+    const uchar4 c8 = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
+                                  (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
+                                  (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f), 0);
     const size_t base = (size_t)y * w;
     const bool row_in = y >= ry0 && y < ry1;
     // [0, a) and [b, w): the whole row, or the parts left and right of the rectangle
@@ -981,7 +1091,7 @@ __global__ void __launch_bounds__(128) k_render_lines(const FrameDesc* __restric
     r.t1 = fminf(r.t1, __uint_as_float(stop));
     r.hit = r.t1 > r.t0 && (r.t1 - r.t0) < 4.0f;
     unsigned nsamp = 0;
-    const float4 c = behind(f, march<T, MODE, SAMPLER>(f, r, nsamp, 0, f.light_to), stop);
+    const float4 c = behind(f, march<T, MODE, SAMPLER>(f, r, nsamp, 0, f.light_to), stop, py);
     if (f.out_f32) f.out_f32[p] = c;
     if (f.out_rgba8)
       f.out_rgba8[p] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
@@ -1148,7 +1258,8 @@ __global__ void k_render_slice(const __grid_constant__ FrameDesc f, const __grid
     float vw = (s.half_h - ((float)py + 0.5f)) * s.inv_s;
     if (s.flip_x) uw = -uw;
     if (s.flip_y) vw = -vw;
-    float4 out = make_float4(f.bg[0], f.bg[1], f.bg[2], 0.f);
+    const float3 bg = bg_at(f, py);
+    float4 out = make_float4(bg.x, bg.y, bg.z, 0.f);
     if (fabsf(uw) <= 0.5f * s.ext_u && fabsf(vw) <= 0.5f * s.ext_v) {
       const float pu = (uw + 0.5f * s.ext_u) * s.scale_u - 0.5f;
       const float pv = (vw + 0.5f * s.ext_v) * s.scale_v - 0.5f;
@@ -1194,8 +1305,8 @@ __global__ void k_render_slice(const __grid_constant__ FrameDesc f, const __grid
       }
       if (!empty) {
         const float4 c = tf1d(f, v);
-        out = make_float4(fmaf(c.w, c.x, (1.f - c.w) * f.bg[0]), fmaf(c.w, c.y, (1.f - c.w) * f.bg[1]),
-                          fmaf(c.w, c.z, (1.f - c.w) * f.bg[2]), c.w);
+        out = make_float4(fmaf(c.w, c.x, (1.f - c.w) * bg.x), fmaf(c.w, c.y, (1.f - c.w) * bg.y),
+                          fmaf(c.w, c.z, (1.f - c.w) * bg.z), c.w);
       }
     }
     const size_t o = (size_t)py * f.width + px;
@@ -1223,8 +1334,8 @@ cudaError_t launch_render_slice(const FrameDesc& f, const SliceDesc& sd, cudaStr
 // Batch-uniform variant: `shared` (a kernel parameter, so the walk reads it as
 // constant-bank operands) holds everything the views have in common; camera,
 // image size, outputs and the sample counter come from frames[view].
-template <typename T, int MODE, int SAMPLER>
-__global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
+template <typename T, int MODE, int SAMPLER, int SPS = 1>
+__global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm_sps<MODE, SPS>())
     k_render_persistent_u(const __grid_constant__ FrameDesc shared, const FrameDesc* __restrict__ frames,
                           int nframes, const int* __restrict__ tile_prefix, int* __restrict__ counter) {
   const int lane = threadIdx.x & 31;
@@ -1235,7 +1346,7 @@ __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= total) return;
     int fi = find_frame(tile_prefix, nframes, item);
-    render_tile_u<T, MODE, SAMPLER>(shared, frames[fi], fi, item - __ldg(tile_prefix + fi));
+    render_tile_u<T, MODE, SAMPLER, SPS>(shared, frames[fi], fi, item - __ldg(tile_prefix + fi));
   }
 }
 
@@ -1453,7 +1564,7 @@ __global__ void __launch_bounds__(128) k_render_cv(const __grid_constant__ Frame
     r.hit = r.t1 > r.t0 && (r.t1 - r.t0) < 4.0f;
   }
   unsigned nsamp = 0;
-  const float4 c = behind(f, march<T, MODE_ISO, SAMPLER, true>(f, r, nsamp, 0, f.light_to, rho), stop);
+  const float4 c = behind(f, march<T, MODE_ISO, SAMPLER, true>(f, r, nsamp, 0, f.light_to, rho), stop, py);
   if (f.out_f32) f.out_f32[p] = c;
   if (f.out_rgba8)
     f.out_rgba8[p] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
@@ -1508,11 +1619,32 @@ cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, con
   GBVR_DISPATCH(persistent_t, dtype, mode, sampler, frames, nframes, prefix, counter, grid, s);
 }
 
+template <typename T>
+static cudaError_t persistent_u_sps2_t(const FrameDesc& shared, const FrameDesc* frames, int nframes, const int* prefix,
+                                       int* counter, int grid, cudaStream_t s) {
+  k_render_persistent_u<T, MODE_1D, SAMPLER_SW, 2><<<grid, RENDER_THREADS, 0, s>>>(shared, frames, nframes, prefix,
+                                                                                    counter);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, const FrameDesc& shared,
                                              const FrameDesc* frames, int nframes, const int* prefix, int* counter,
-                                             int grid, cudaStream_t s) {
+                                             int grid, cudaStream_t s, int sps) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (sps == 2 && mode == MODE_1D && sampler == SAMPLER_SW) {
+    if (dtype == DT_U8) return persistent_u_sps2_t<uint8_t>(shared, frames, nframes, prefix, counter, grid, s);
+    if (dtype == DT_U16) return persistent_u_sps2_t<uint16_t>(shared, frames, nframes, prefix, counter, grid, s);
+    return persistent_u_sps2_t<float>(shared, frames, nframes, prefix, counter, grid, s);
+  }
   GBVR_DISPATCH(persistent_u_t, dtype, mode, sampler, shared, frames, nframes, prefix, counter, grid, s);
+}
+
+// Resident CTAs per SM of the batch kernel's two-samples-per-step variant.
+int persistent_ctas_per_sm_sps2() {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_1D, SAMPLER_SW, 2>,
+                                                RENDER_THREADS, 0);
+  return per_sm < 1 ? 1 : per_sm;
 }
 
 int persistent_grid_size_uniform(int device, int mode) {

@@ -189,6 +189,12 @@ class Renderer:
                     host_bytes=info.host_bytes, device_slots=info.device_slots,
                     compression=info.compression, host_raw_bytes=info.host_raw_bytes)
 
+    def buildStats(self):
+        """Device time (ms) and bytes of the last in-core UVF build, per phase."""
+        b = L.BuildStats()
+        L.call("gbvr_get_build_stats", self._h, C.byref(b))
+        return {f: getattr(b, f) for f, _ in L.BuildStats._fields_}
+
     def getHistogram(self):
         n = self.datasetInfo()["hist1d_size"]
         out = np.zeros(n, np.uint64)
@@ -390,6 +396,21 @@ class Renderer:
         res = L.TuneResult()
         L.call("gbvr_autotune", self._h, arr, len(views), C.byref(res))
         return {k: getattr(res, k) for k, _ in L.TuneResult._fields_}
+
+    def setSamplesPerStep(self, sps):
+        L.call("gbvr_set_samples_per_step", self._h, sps)
+
+    def autotuneEx(self, views, brick_sizes=(128, 256, 512), samples_per_step=(1, 2)):
+        """Launch shape x brick size x samples per step: the fastest stays set."""
+        vs = self._views(views)
+        p = L.TuneParams()
+        for k, b in enumerate(brick_sizes[:4]):
+            p.brick_sizes[k] = b
+        for k, v in enumerate(samples_per_step[:2]):
+            p.samples_per_step[k] = v
+        out = L.TuneResultEx()
+        L.call("gbvr_autotune_ex", self._h, vs, len(views), C.byref(p), C.byref(out))
+        return {f: getattr(out, f) for f, _ in L.TuneResultEx._fields_}
 
     # -- paint / readback ---------------------------------------------------
     def paint(self):

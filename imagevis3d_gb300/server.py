@@ -8,10 +8,13 @@ from .renderer import _DT, brick_params
 
 
 class Server:
-    """Resident datasets + TF presets; requests batched into persistent launches."""
+    """Datasets + TF presets; requests batched into graph-replayed persistent
+    launches, up to `slots` batches in flight on their own streams; with
+    device_pool_bytes > 0 the datasets' brick pools share that budget and are
+    made resident on demand (least recently used idle ones evicted)."""
 
-    def __init__(self, max_batch=64, fb_budget_bytes=2 << 30, tile_w=8):
-        p = L.ServerParams(max_batch, tile_w, fb_budget_bytes)
+    def __init__(self, max_batch=64, fb_budget_bytes=2 << 30, tile_w=8, slots=3, device_pool_bytes=0):
+        p = L.ServerParams(max_batch, tile_w, fb_budget_bytes, slots, 0, device_pool_bytes)
         h = C.c_void_p()
         L.call("gbvr_server_create", C.byref(p), C.byref(h))
         self._h = h
@@ -60,8 +63,13 @@ class Server:
                    value_range[0], value_range[1], C.byref(i))
         return i.value
 
-    def submit(self, dataset, tf, width, height, view, proj, spv=1.0):
-        out = np.empty((height, width, 4), np.uint8)
+    def submit(self, dataset, tf, width, height, view, proj, spv=1.0, out=None):
+        """Queue a request; its RGBA8 image lands in `out` (a C-contiguous
+        (height, width, 4) uint8 array, or a new one) once waited for."""
+        if out is None:
+            out = np.empty((height, width, 4), np.uint8)
+        elif out.shape != (height, width, 4) or out.dtype != np.uint8 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous (height, width, 4) uint8 array")
         r = L.Request()
         r.dataset, r.tf, r.width, r.height = dataset, tf, width, height
         v = np.ascontiguousarray(view, np.float32).ravel()
@@ -91,6 +99,14 @@ class Server:
         s = L.ServerStats()
         L.call("gbvr_server_get_stats", self._h, C.byref(s))
         return {k: getattr(s, k) for k, _ in L.ServerStats._fields_}
+
+    def autotune(self, width=512, height=512, n=16):
+        """Per (voxel type, mode) group: the fastest launch shape on a batch of
+        n requests (list of dicts)."""
+        out = (L.ServerTune * 12)()
+        k = C.c_int()
+        L.call("gbvr_server_autotune", self._h, width, height, n, out, 12, C.byref(k))
+        return [{f: getattr(out[i], f) for f, _ in L.ServerTune._fields_} for i in range(k.value)]
 
     def reset_stats(self):
         L.call("gbvr_server_reset_stats", self._h)

@@ -37,22 +37,29 @@ def tf1d_seeded(n, seed, zero_below, value_max, points=4):
 
 def tf2d_seeded(w, h, seed, widgets=3, zero_cols=0, x_range=(0.25, 0.85)):
     """w x h RGBA table over (value, gradient magnitude) with seeded Gaussian
-    ellipse widgets; row = gradient bin, column = value bin.  The first
-    `zero_cols` value columns are transparent (empty space stays empty)."""
+    ellipse widgets; row = gradient bin, column = value bin.  Alpha is the
+    largest widget's Gaussian; the colour is the widgets' colours mixed by
+    their Gaussians, so colour and alpha are continuous over the table (a
+    colour step where the alpha is near zero would turn sub-voxel position
+    differences into colour differences).  The first `zero_cols` value
+    columns are transparent (empty space stays empty)."""
     rng = np.random.default_rng(seed)
     x = (np.arange(w) + 0.5) / w
     y = (np.arange(h) + 0.5) / h
     X, Y = np.meshgrid(x, y)
     tf = np.zeros((h, w, 4), np.float64)
+    rgb = np.zeros((h, w, 3), np.float64)
+    wsum = np.zeros((h, w), np.float64)
     for _ in range(widgets):
         cx, cy = rng.uniform(*x_range), rng.uniform(0.1, 0.6)
         sx, sy = rng.uniform(0.03, 0.12), rng.uniform(0.08, 0.3)
         col = rng.uniform(0.2, 1.0, 3)
         amax = rng.uniform(0.3, 0.9)
         g = np.exp(-0.5 * (((X - cx) / sx) ** 2 + ((Y - cy) / sy) ** 2)) * amax
-        for c in range(3):
-            tf[..., c] = np.maximum(tf[..., c], col[c] * (g > 1e-3))
-        tf[..., 3] = np.maximum(tf[..., 3], np.where(g > 1e-3, g, 0.0))
+        rgb += g[..., None] * col[None, None, :]
+        wsum += g
+        tf[..., 3] = np.maximum(tf[..., 3], g)
+    tf[..., :3] = rgb / np.maximum(wsum, 1e-300)[..., None]
     tf[:, :zero_cols, 3] = 0.0
     return tf.astype(np.float32)
 

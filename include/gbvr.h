@@ -274,6 +274,38 @@ typedef struct gbvr_tune_result {
  * The frame content does not depend on the shape (rays are independent). */
 int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_result* out);
 
+/* Samples per step of the batched kernel's inner loop (1D TF, software
+ * sampler): 1 (default) or 2.  With 2 each step evaluates two consecutive
+ * samples -- both samples' voxel and TF loads in flight together -- and
+ * composites them in order, stopping after the first if it ends the ray:
+ * the same pixels either way.  No counterpart in the reference. */
+int gbvr_set_samples_per_step(gbvr_renderer* r, int sps);
+
+/* Extended autotuner: the launch-shape sweep of gbvr_autotune (tile width x
+ * CTAs per SM) for every brick size in brick_sizes (the dataset is rebuilt at
+ * each from its finest level: same pixels, other bricks; the uvfconvert
+ * -bricksize setting, CmdLineConverter/main.cpp:172-174, and the max brick
+ * size of ImageVis3D/UI/ImageVis3D_Settings.cpp:516-520) and every value in
+ * samples_per_step (gbvr_set_samples_per_step).  The fastest combination on
+ * `views` stays set (the dataset left at its brick size).  Zero entries end
+ * each list; an empty list keeps the current setting.  In-core datasets only. */
+typedef struct gbvr_tune_params {
+  int32_t brick_sizes[4];
+  int32_t samples_per_step[2];
+  int32_t reserved[2];
+} gbvr_tune_params;
+
+typedef struct gbvr_tune_result_ex {
+  int32_t tile_w, ctas_per_sm, brick_size, samples_per_step;
+  int32_t candidates;
+  float best_ms;     /* kernel time of the chosen combination on the tuning batch */
+  float default_ms;  /* ... of the settings at the call (tile 8, CTAs as fit, 1 sample per step, its brick size) */
+  float worst_ms;    /* ... of the slowest candidate */
+} gbvr_tune_result_ex;
+
+int gbvr_autotune_ex(gbvr_renderer* r, const gbvr_view* views, int n, const gbvr_tune_params* p,
+                     gbvr_tune_result_ex* out);
+
 /* ---- paint ----
  * gbvr_paint replaces renderer.paint() (BatchRenderer.lua:35,
  *   RenderWindow.cpp:2464): one plain launch for the current view.
@@ -371,6 +403,27 @@ typedef struct gbvr_fbm_params {
 int gbvr_synth_fbm_volume(const gbvr_fbm_params* p, void* host_out, size_t bytes);
 int gbvr_load_synthetic_fbm(gbvr_renderer* r, const gbvr_fbm_params* p, const gbvr_brick_params* bp);
 
+/* Device time and bytes of the last in-core UVF build of a renderer's dataset
+ * (gbvr_load_volume, gbvr_load_synthetic, gbvr_load_uvf), phase by phase:
+ * the work of TOCBlock::FlatDataToBrickedLOD and the histogram blocks
+ * (UVFReader/DataSource.h:475-500, 601-616), timed with CUDA events around
+ * each phase's launches.  Synthesis, host uploads and texture building are
+ * not part of it.  bytes = what each phase must read and write at least:
+ * pyramid: every level read once and the next written; cells: every level
+ * read; bricks: every level read and its stored bricks written, per layout
+ * copy; minmax: the stored bricks of copy 0 read; hist1d: level 0 read;
+ * hist2d: level 0 read three times (maximum, maximum gradient, binning). */
+typedef struct gbvr_build_stats {
+  double total_ms;
+  double pyramid_ms, cells_ms, bricks_ms, minmax_ms, hist1d_ms, hist2d_ms;
+  uint64_t total_bytes;
+  uint64_t pyramid_bytes, cells_bytes, bricks_bytes, minmax_bytes, hist1d_bytes, hist2d_bytes;
+  uint64_t level0_bytes;   /* bytes of the finest level */
+  int32_t lod_count;
+  int32_t layout_copies;
+} gbvr_build_stats;
+int gbvr_get_build_stats(gbvr_renderer* r, gbvr_build_stats* out);
+
 /* ---- GPU UVF build without a renderer (uvfconvert, CmdLineConverter/main.cpp:406-408):
  * host volume in, UVF v2 file out. ---- */
 int gbvr_build_uvf(const void* host, const int64_t dims[3], int dtype, const gbvr_brick_params* bp,
@@ -405,21 +458,33 @@ int gbvr_dev_downsample(const void* dev_in, int dtype, const int64_t dims[3], vo
 int gbvr_dev_synth_volume_noalloc(const gbvr_synth_params* p, void* dev_out, size_t bytes, void* stream);
 
 /* ---- serving (continuous batching) ----
- * A server keeps many datasets and transfer-function presets resident and
- * renders requests submitted from any thread.  A worker thread batches the
- * pending requests into persistent launches: a batch takes requests in
- * arrival order until it holds max_batch of them or its framebuffer area
- * (half of fb_budget_bytes; two batches are in flight) is full; the rest
- * wait for the next batch, which is assembled while the current one
- * renders.  A request's image does not depend on the batch it lands in.
- * No counterpart in the reference (its GUI renders one window per paint,
+ * A server keeps many datasets and transfer-function presets and renders
+ * requests submitted from any thread.  A worker thread keeps up to `slots`
+ * batches in flight, each on its own CUDA stream: whenever a slot is free and
+ * requests are pending it launches a batch of them at once, so batches
+ * overlap on the device (a new batch's ray tiles fill the SMs that earlier
+ * batches' tails leave idle).  A batch takes pending requests in arrival
+ * order until it holds max_batch of them or its framebuffer share
+ * (fb_budget_bytes / slots) is full.  Its requests are grouped by (voxel
+ * type, render mode); each group is one persistent launch over the group's
+ * ray tiles, replayed from a CUDA graph, with the group's launch shape from
+ * gbvr_server_autotune.  Admission by memory: with device_pool_bytes > 0 the
+ * datasets' brick pools share that budget; a request whose dataset is not
+ * resident waits until its pool fits (idle datasets are evicted, least
+ * recently used first, and the pool is uploaded from page-locked host memory
+ * ahead of the batch), while requests for resident datasets go ahead.  A
+ * request's image does not depend on the batch it lands in.  No counterpart
+ * in the reference (its GUI renders one window per paint,
  * ImageVis3D/UI/RenderWindow.cpp:2453-2502). */
 typedef struct gbvr_server gbvr_server;
 
 typedef struct gbvr_server_params {
   int32_t max_batch;          /* requests per batch (0 = 64) */
-  int32_t tile_w;             /* warp tile width (0 = 8) */
-  uint64_t fb_budget_bytes;   /* device + pinned framebuffer memory (0 = 2 GiB) */
+  int32_t tile_w;             /* default warp tile width (0 = 8) */
+  uint64_t fb_budget_bytes;   /* device + pinned framebuffer memory, shared by the slots (0 = 2 GiB) */
+  int32_t slots;              /* batches in flight, one stream each (0 = 3; at most 8) */
+  int32_t reserved;
+  uint64_t device_pool_bytes; /* brick-pool memory the datasets share (0 = no limit: all stay resident) */
 } gbvr_server_params;
 
 typedef struct gbvr_request {
@@ -446,6 +511,11 @@ typedef struct gbvr_server_stats {
   double mean_batch;
   double p50_ms, p99_ms, max_ms;  /* request latency percentiles */
   double frames_per_s;            /* completed requests / (last completion - first submit) */
+  uint64_t overlap_checked;       /* pairs of consecutive batches whose kernel spans were compared */
+  uint64_t overlapped;            /* ... of which the later batch's kernels started before the earlier's ended */
+  uint64_t uploads, evictions;    /* brick pools made resident / evicted under device_pool_bytes */
+  uint64_t upload_bytes;
+  uint64_t resident_bytes;        /* brick-pool bytes resident now */
 } gbvr_server_stats;
 
 int gbvr_server_create(const gbvr_server_params* params, gbvr_server** out);
@@ -461,12 +531,33 @@ int gbvr_server_add_synthetic(gbvr_server* s, const gbvr_synth_params* p, const 
  * the dataset's default). */
 int gbvr_server_add_tf(gbvr_server* s, int dataset, int mode, const float* rgba, int w, int h, float grad_max,
                        float iso, const float iso_rgb[3], double lo, double hi, int* tf_id);
+/* Fails with GBVR_EINVAL for a request that can never be admitted (unknown
+ * ids, a framebuffer above the slot's share, a brick pool above
+ * device_pool_bytes). */
 int gbvr_server_submit(gbvr_server* s, const gbvr_request* req, uint64_t* ticket);
-/* Blocks until the request is done (timeout_s <= 0: no limit); its pixels are
- * then in req.out_rgba8.  A ticket can be waited for once. */
+/* Blocks until the request is done (timeout_s <= 0: no limit; GBVR_ETIMEOUT
+ * when it runs out, the ticket then stays valid); its pixels are then in
+ * req.out_rgba8.  A ticket can be waited for once. */
 int gbvr_server_wait(gbvr_server* s, uint64_t ticket, double timeout_s, gbvr_request_result* out);
 int gbvr_server_get_stats(gbvr_server* s, gbvr_server_stats* out);
 int gbvr_server_reset_stats(gbvr_server* s);
+
+/* Launch shape of one (voxel type, render mode) group of the server. */
+typedef struct gbvr_server_tune {
+  int32_t dtype, mode;
+  int32_t tile_w, ctas_per_sm;  /* chosen */
+  int32_t candidates;
+  float best_ms, default_ms;    /* kernel time of the tuning batch: chosen shape, default shape */
+} gbvr_server_tune;
+
+/* Autotuner of the serving launches: for every (voxel type, mode) group that
+ * has a transfer-function preset, renders a batch of `n` requests of
+ * width x height (orbit cameras around one dataset of the group, its presets
+ * in turn) with every candidate tile width and CTAs-per-SM, keeps the
+ * fastest, and writes one entry per group to out (up to cap; count to
+ * *n_out).  Waits for the batches in flight first; requests submitted
+ * meanwhile wait.  The pixels do not depend on the shape. */
+int gbvr_server_autotune(gbvr_server* s, int width, int height, int n, gbvr_server_tune* out, int cap, int* n_out);
 
 /* Orbit camera around the volume centre: the rotation the 360-degree capture
  * applies per frame (ImageVis3D_Capturing.cpp:170 fAngle = i/N * 360,

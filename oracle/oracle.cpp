@@ -454,6 +454,18 @@ float orc_fbm_value(const i64 dims[3], uint32_t seed, int octaves, int base_peri
   return acc / norm;
 }
 
+// One voxel of the seeded fractal volume as stored (u8 / u16 rounded to
+// nearest, f32 as is): the thresholded, rescaled fBm value.  inv = 1 / (1 - thr).
+static inline float fbm_voxel(const i64 dims[3], int dt, uint32_t seed, int octaves, int base_period, float thr,
+                              float inv, float vmax, i64 x, i64 y, i64 z) {
+  float f = orc_fbm_value(dims, seed, octaves, base_period, x, y, z);
+  float v = f - thr;
+  v = v * inv;
+  v = std::min(std::max(v, 0.0f), 1.0f);
+  v = v * vmax;
+  return dt == DT_F32 ? v : (float)std::nearbyint(v);
+}
+
 void orc_synth_fbm(const i64 dims[3], int dt, uint32_t seed, int octaves, int base_period, float thr, float vmax,
                    void* out) {
   const i64 X = dims[0], Y = dims[1], Z = dims[2];
@@ -462,15 +474,11 @@ void orc_synth_fbm(const i64 dims[3], int dt, uint32_t seed, int octaves, int ba
   for (i64 z = 0; z < Z; ++z)
     for (i64 y = 0; y < Y; ++y)
       for (i64 x = 0; x < X; ++x) {
-        float f = orc_fbm_value(dims, seed, octaves, base_period, x, y, z);
-        float v = f - thr;
-        v = v * inv;
-        v = std::min(std::max(v, 0.0f), 1.0f);
-        v = v * vmax;
+        const float v = fbm_voxel(dims, dt, seed, octaves, base_period, thr, inv, vmax, x, y, z);
         i64 idx = (z * Y + y) * X + x;
         if (dt == DT_F32) ((float*)out)[idx] = v;
-        else if (dt == DT_U8) ((uint8_t*)out)[idx] = (uint8_t)std::nearbyint(v);
-        else ((uint16_t*)out)[idx] = (uint16_t)std::nearbyint(v);
+        else if (dt == DT_U8) ((uint8_t*)out)[idx] = (uint8_t)v;
+        else ((uint16_t*)out)[idx] = (uint16_t)v;
       }
 }
 
@@ -515,16 +523,44 @@ struct orc_render_params {
   // rho^2, 0, 1) over the first hit of cv_iso from the context hit's sample on (colour cv_rgb)
   int cv_on;
   double cv_iso, cv_rgb[3], cv_context, cv_border, cv_focus[2], cv_radius;
+  // Background gradient (setBGColors with two colours): bg is the bottom
+  // edge's colour, bg_top the top edge's; each pixel row takes the colour at
+  // its centre, linear in between.
+  int bg_grad;
+  double bg_top[3];
+  // Procedural volume: with proc_fbm set, vol is not read; every voxel is the
+  // seeded fractal volume's (orc_synth_fbm with these parameters and dtype),
+  // evaluated where a sample needs it.  Lets a pixel subset of a volume too
+  // large for host memory be rendered.
+  int proc_fbm;
+  uint32_t fbm_seed;
+  int fbm_octaves, fbm_base_period;
+  float fbm_threshold, fbm_vmax;
 };
+
+static void bg_row(const orc_render_params* p, int py, double out[3]) {
+  if (!p->bg_grad) {
+    for (int k = 0; k < 3; ++k) out[k] = p->bg[k];
+    return;
+  }
+  const double t = ((double)py + 0.5) / (double)p->height;
+  for (int k = 0; k < 3; ++k) out[k] = p->bg_top[k] + t * (p->bg[k] - p->bg_top[k]);
+}
 
 struct Vol {
   const orc_render_params* p;
+  double vox(i64 x, i64 y, i64 z) const {
+    if (p->proc_fbm)
+      return fbm_voxel(p->dims, p->dtype, p->fbm_seed, p->fbm_octaves, p->fbm_base_period, p->fbm_threshold,
+                       1.0f / (1.0f - p->fbm_threshold), p->fbm_vmax, x, y, z);
+    return load_voxel(p->vol, p->dtype, (z * p->dims[1] + y) * p->dims[0] + x);
+  }
   double sample_nearest(double x, double y, double z) const {
     i64 ix = (i64)std::floor(x + 0.5), iy = (i64)std::floor(y + 0.5), iz = (i64)std::floor(z + 0.5);
     ix = std::min(std::max<i64>(ix, 0), p->dims[0] - 1);
     iy = std::min(std::max<i64>(iy, 0), p->dims[1] - 1);
     iz = std::min(std::max<i64>(iz, 0), p->dims[2] - 1);
-    return load_voxel(p->vol, p->dtype, (iz * p->dims[1] + iy) * p->dims[0] + ix);
+    return vox(ix, iy, iz);
   }
   double sample(double x, double y, double z) const {
     if (!p->interp) return sample_nearest(x, y, z);
@@ -535,7 +571,7 @@ struct Vol {
     auto cl = [](i64 v, i64 n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); };
     i64 xa = cl(x0, X), xb = cl(x0 + 1, X), ya = cl(y0, Y), yb = cl(y0 + 1, Y);
     i64 za = cl(z0, Z), zb = cl(z0 + 1, Z);
-    auto v = [&](i64 xi, i64 yi, i64 zi) { return load_voxel(p->vol, p->dtype, (zi * Y + yi) * X + xi); };
+    auto v = [&](i64 xi, i64 yi, i64 zi) { return vox(xi, yi, zi); };
     auto lerp = [](double a, double b, double t) { return a + t * (b - a); };
     double c00 = lerp(v(xa, ya, za), v(xb, ya, za), fx);
     double c10 = lerp(v(xa, yb, za), v(xb, yb, za), fx);
@@ -904,7 +940,9 @@ static void render_pixel(const orc_render_params* p, int px, int py, double* out
     for (int k = 0; k < 3; ++k) out[k] = C[k] + (1.0 - A) * lc[k];
     out[3] = A + (1.0 - A);
   } else {
-    for (int k = 0; k < 3; ++k) out[k] = C[k] + (1.0 - A) * p->bg[k];
+    double bg[3];
+    bg_row(p, py, bg);
+    for (int k = 0; k < 3; ++k) out[k] = C[k] + (1.0 - A) * bg[k];
     out[3] = A;
   }
   if (nsamples) *nsamples = ns;
@@ -930,7 +968,9 @@ void orc_render_slice(const orc_render_params* p, int axis, double coord, int fl
       if (flip_x) uw = -uw;
       if (flip_y) vw = -vw;
       double* o = out + 4 * ((i64)py * p->width + px);
-      o[0] = p->bg[0]; o[1] = p->bg[1]; o[2] = p->bg[2]; o[3] = 0.0;
+      double bg[3];
+      bg_row(p, py, bg);
+      o[0] = bg[0]; o[1] = bg[1]; o[2] = bg[2]; o[3] = 0.0;
       if (std::fabs(uw) > 0.5 * eu || std::fabs(vw) > 0.5 * ev) continue;
       double x[3];
       x[ua] = (uw + 0.5 * eu) * (double)p->dims[ua] / eu - 0.5;
@@ -948,7 +988,7 @@ void orc_render_slice(const orc_render_params* p, int axis, double coord, int fl
       }
       double c[4];
       tf1d_lookup(p, (v - p->value_lo) * vscale * (p->tf_w - 1), c);
-      for (int q = 0; q < 3; ++q) o[q] = c[3] * c[q] + (1.0 - c[3]) * p->bg[q];
+      for (int q = 0; q < 3; ++q) o[q] = c[3] * c[q] + (1.0 - c[3]) * bg[q];
       o[3] = c[3];
     }
 }
@@ -1198,6 +1238,82 @@ void orc_look_at_camera(const double eye[3], const double at[3], const double up
     view[i] = (float)V[i];
     proj[i] = (float)P[i];
   }
+}
+
+// ---------------------------------------------------------------------------
+// The CPU UVF build of a flat level-0 volume, timed phase by phase for the
+// CPU baseline: the LOD pyramid (orc_downsample), every level's bricks with
+// ghosts (orc_extract_brick) and their min/max, the 1D histogram and the 2D
+// histogram -- the converter's sequence (UVFReader/DataSource.h:475-616) on
+// `threads` OpenMP threads (bricks in parallel; the histograms as written
+// above).  phase_s[4]: pyramid, bricks + min/max, hist1d, hist2d seconds.
+// Returns the total seconds.
+// ---------------------------------------------------------------------------
+double orc_uvf_build_timed(const void* vol, int dt, const i64 dims[3], int brick, int ghost, int threads,
+                           double* phase_s) {
+#ifdef _OPENMP
+  const int saved = omp_get_max_threads();
+  omp_set_num_threads(threads > 0 ? threads : saved);
+#endif
+  auto now = [] {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+  };
+  const size_t es = dt_size(dt);
+  i64 ld[16 * 3];
+  const int nl = orc_lod_dims(dims, brick, ghost, 0, ld);
+  std::vector<std::vector<char>> lv(nl);
+  double t0 = now();
+  for (int l = 1; l < nl; ++l) {
+    lv[l].resize((size_t)ld[3 * l] * ld[3 * l + 1] * ld[3 * l + 2] * es);
+    orc_downsample(l == 1 ? vol : lv[l - 1].data(), dt, ld + 3 * (l - 1), lv[l].data());
+  }
+  double t1 = now();
+  double sink = 0.0;
+  for (int l = 0; l < nl; ++l) {
+    const void* src = l == 0 ? vol : lv[l].data();
+    i64 nb[3], I;
+    orc_brick_grid(ld + 3 * l, brick, ghost, nb, &I);
+    const i64 n = nb[0] * nb[1] * nb[2];
+#pragma omp parallel reduction(+ : sink)
+    {
+      std::vector<char> buf;
+#pragma omp for schedule(dynamic, 1)
+      for (i64 i = 0; i < n; ++i) {
+        const i64 b[3] = {i % nb[0], (i / nb[0]) % nb[1], i / (nb[0] * nb[1])};
+        i64 o[3], sd[3];
+        orc_brick_extent(ld + 3 * l, brick, ghost, b, o, sd);
+        buf.resize((size_t)sd[0] * sd[1] * sd[2] * es);
+        orc_extract_brick(src, dt, ld + 3 * l, brick, ghost, b, buf.data());
+        double mn, mx;
+        orc_minmax(buf.data(), dt, sd[0] * sd[1] * sd[2], &mn, &mx);
+        sink += mn + mx;
+      }
+    }
+  }
+  double t2 = now();
+  std::vector<u64> h1(65536);
+  i64 merge = 1, nx = 1;
+  if (dt != DT_F32) nx = orc_hist1d(vol, dt, dims[0] * dims[1] * dims[2], 4096, h1.data(), &merge);
+  double t3 = now();
+  if (dt != DT_F32) {
+    double mn, mx;
+    orc_minmax(vol, dt, dims[0] * dims[1] * dims[2], &mn, &mx);
+    std::vector<u64> h2((size_t)nx * 256);
+    orc_hist2d(vol, dt, dims, mx, nx, merge, h2.data());
+  }
+  double t4 = now();
+#ifdef _OPENMP
+  omp_set_num_threads(saved);
+#endif
+  phase_s[0] = t1 - t0;
+  phase_s[1] = t2 - t1;
+  phase_s[2] = t3 - t2;
+  phase_s[3] = t4 - t3;
+  return (t4 - t0) + 0.0 * sink;
 }
 
 }  // extern "C"

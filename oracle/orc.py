@@ -30,6 +30,9 @@ class RenderParams(C.Structure):
         ("proj", D * 16), ("brick_interior", I64), ("line_keys", C.c_void_p),
         ("cv_on", C.c_int), ("cv_iso", D), ("cv_rgb", D * 3), ("cv_context", D), ("cv_border", D),
         ("cv_focus", D * 2), ("cv_radius", D),
+        ("bg_grad", C.c_int), ("bg_top", D * 3),
+        ("proc_fbm", C.c_int), ("fbm_seed", C.c_uint32), ("fbm_octaves", C.c_int), ("fbm_base_period", C.c_int),
+        ("fbm_threshold", C.c_float), ("fbm_vmax", C.c_float),
     ]
 
 
@@ -145,27 +148,58 @@ def synth_blobs(params):
     return out
 
 
+class ProceduralFbm:
+    """The seeded fractal volume (gbvr_fbm_params) as a render input whose
+    voxels the oracle evaluates where its samples need them."""
+
+    def __init__(self, params):
+        self.dims = [int(params.dims[i]) for i in range(3)]
+        self.dtype = int(params.dtype)
+        self.seed = int(params.seed)
+        self.octaves = int(params.octaves)
+        self.base_period = int(params.base_period)
+        self.threshold = float(np.float32(params.threshold))
+        self.vmax = float(np.float32(params.vmax))
+
+
 def render(vol, view, proj, width, height, tf, spv=1.0, value_range=(0.0, 255.0), mode=0,
            interp=1, ert=0.99, extent=None, grad_max=1.0, iso=0.0, iso_rgb=(1, 1, 1), lighting=1,
            amb=(0.1, 0.1, 0.1), diff=(1, 1, 1), spec=(1, 1, 1), shininess=8.0,
-           light_dir=(0, 0, -1), bg=(0, 0, 0), pixels=None, threads=0, clip=None, bbox=None, cv=None):
-    """FP64 render of `vol` (the flat level, (z, y, x)).  mode 0 1D TF, 1 2D TF
+           light_dir=(0, 0, -1), bg=(0, 0, 0), pixels=None, threads=0, clip=None, bbox=None, cv=None,
+           bg_top=None):
+    """FP64 render of `vol` (the flat level, (z, y, x)), or of a procedural
+    fractal volume when `vol` is a ProceduralFbm (voxels evaluated on demand,
+    for volumes too large for host memory).  mode 0 1D TF, 1 2D TF
     + Phong, 2 isosurface, 3 maximum-intensity projection; clip = plane
     (a, b, c, d) dropping samples with a x + b y + c z + d > 0; bbox = dict
     (global_, local, interior = brick edge minus two ghosts, rgb = (global,
     local) colours) for bounding-box lines; cv = dict(iso, rgb, context,
-    border, focus = (x, y) pixels, radius pixels) for ClearView (mode 2).
+    border, focus = (x, y) pixels, radius pixels) for ClearView (mode 2);
+    bg_top: the top edge's background colour (a vertical gradient down to
+    `bg`, as setBGColors draws two colours).
     Returns (rgba float64 [n, 4] or [h, w, 4], samples)."""
-    vol = np.ascontiguousarray(vol)
     tf = np.ascontiguousarray(tf, np.float32)
     p = RenderParams()
-    p.vol = vol.ctypes.data
-    p.dtype = _DT[vol.dtype]
-    for i, d in enumerate((vol.shape[2], vol.shape[1], vol.shape[0])):
+    if isinstance(vol, ProceduralFbm):
+        shape = (vol.dims[2], vol.dims[1], vol.dims[0])
+        p.vol = None
+        p.dtype = vol.dtype
+        p.proc_fbm, p.fbm_seed, p.fbm_octaves, p.fbm_base_period = 1, vol.seed, vol.octaves, vol.base_period
+        p.fbm_threshold, p.fbm_vmax = vol.threshold, vol.vmax
+    else:
+        vol = np.ascontiguousarray(vol)
+        shape = vol.shape
+        p.vol = vol.ctypes.data
+        p.dtype = _DT[vol.dtype]
+    for i, d in enumerate((shape[2], shape[1], shape[0])):
         p.dims[i] = d
+    if bg_top is not None:
+        p.bg_grad = 1
+        for i in range(3):
+            p.bg_top[i] = bg_top[i]
     if extent is None:
-        m = max(vol.shape)
-        extent = (vol.shape[2] / m, vol.shape[1] / m, vol.shape[0] / m)
+        m = max(shape)
+        extent = (shape[2] / m, shape[1] / m, shape[0] / m)
     for i in range(3):
         p.extent[i] = extent[i]
     p.tf = tf.ctypes.data_as(C.POINTER(C.c_float))
@@ -257,8 +291,9 @@ def lz4_decompress(block, out_n):
 
 
 def render_slice(vol, axis, coord, width, height, tf, value_range=(0.0, 255.0), flip_x=False, flip_y=False,
-                 mip=False, interp=1, extent=None, bg=(0, 0, 0)):
-    """FP64 2D slice view of the flat level `vol` ((z, y, x)): [h, w, 4]."""
+                 mip=False, interp=1, extent=None, bg=(0, 0, 0), bg_top=None):
+    """FP64 2D slice view of the flat level `vol` ((z, y, x)): [h, w, 4];
+    bg_top: the top edge's background colour of a vertical gradient."""
     vol = np.ascontiguousarray(vol)
     tf = np.ascontiguousarray(tf, np.float32)
     p = RenderParams()
@@ -272,6 +307,10 @@ def render_slice(vol, axis, coord, width, height, tf, value_range=(0.0, 255.0), 
     for i in range(3):
         p.extent[i] = extent[i]
         p.bg[i] = bg[i]
+    if bg_top is not None:
+        p.bg_grad = 1
+        for i in range(3):
+            p.bg_top[i] = bg_top[i]
     p.tf = tf.ctypes.data_as(C.POINTER(C.c_float))
     p.tf_w, p.tf_h = tf.shape[0], 1
     p.interp = interp
@@ -285,6 +324,17 @@ def render_slice(vol, axis, coord, width, height, tf, value_range=(0.0, 255.0), 
 
 def max_threads():
     return lib().orc_max_threads()
+
+
+def uvf_build_timed(vol, brick=256, ghost=2, threads=0):
+    """The CPU UVF build of `vol` on `threads` threads (0 = all): returns
+    (total seconds, {pyramid, bricks, hist1d, hist2d} seconds)."""
+    vol = np.ascontiguousarray(vol)
+    ph = (D * 4)()
+    lib().orc_uvf_build_timed.restype = D
+    t = lib().orc_uvf_build_timed(vol.ctypes.data_as(C.c_void_p), _DT[vol.dtype], _dims(vol), int(brick),
+                                  int(ghost), int(threads), ph)
+    return t, dict(zip(("pyramid", "bricks", "hist1d", "hist2d"), list(ph)))
 
 
 def orbit_camera(azimuth_deg, elevation_deg, radius, fov_deg, width, height):

@@ -1,0 +1,85 @@
+"""The sparse fractal workload at its full size: 2048^3 uint8 fBm, 256^3
+bricks with 2 ghosts (and the 4x4x4-blocked copy the benchmark samples),
+2560x1440 views, the 2D TF + Phong path and the isosurface path at the three
+seeded isovalues, against the FP64 oracle on seeded pixel subsets.  The
+oracle evaluates the fractal's voxels where its samples need them
+(orc.ProceduralFbm), so no 8 GiB host copy of the volume is made."""
+import numpy as np
+import pytest
+
+from imagevis3d_gb300 import GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE, Renderer, workloads
+from tests.gpu_util import assert_close
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def c3():
+    wl = workloads.config3()
+    assert [wl.synth.dims[i] for i in range(3)] == [2048] * 3 and (wl.width, wl.height) == (2560, 1440)
+    r = Renderer(float_fb=True)
+    r.loadSynthetic(wl.synth, **wl.brick, layouts=4)
+    r.resize((wl.width, wl.height))
+    r.setValueRange(*wl.value_range)
+    r.setSampleRateModifier(wl.spv)
+    yield wl, r
+    r.cleanup()
+
+
+def _subset(img, rng, covered, anywhere, thr):
+    alpha = img[:, 3]
+    cov = np.flatnonzero(alpha > thr)
+    assert cov.size >= covered
+    return np.concatenate([rng.choice(cov, covered, replace=False), rng.integers(0, img.shape[0], anywhere)])
+
+
+def test_c3_full_size_build(c3):
+    wl, r = c3
+    info = r.datasetInfo()
+    assert info["lod_dims"][0] == (2048,) * 3 and info["lod_bricks"][0] == (9, 9, 9)
+    mm = r.brickMinMax(0)
+    empty = float((mm[:, 1] == 0).mean())
+    assert 0.5 < empty < 0.9  # sparse structures: most bricks are skipped
+    h1 = r.getHistogram()
+    assert int(h1.sum()) == 2048 ** 3
+    h2, mg = r.get2DHistogram()
+    assert np.array_equal(h2.sum(axis=1), h1) and mg > 0
+
+
+def test_c3_full_size_2d_tf_phong_matches_oracle(orc, c3):
+    wl, r = c3
+    gmax = r.datasetInfo()["hist2d_max_grad"] * 0.5
+    r.setRenderMode(GBVR_RM_2DTRANS)
+    r.set2DTrans(wl.tf, gmax)
+    views = [wl.views[0], wl.views[5]]
+    r.paintBatch(views)
+    vol = orc.ProceduralFbm(wl.synth)
+    rng = np.random.default_rng(wl.synth.seed)
+    for i, (v, p) in enumerate(views):
+        img = r.readFramebuffer(i, as_float=True).reshape(-1, 4)
+        pix = _subset(img, rng, 240, 80, 0.02)
+        ref, _ = orc.render(vol, v, p, wl.width, wl.height, wl.tf, mode=1, grad_max=gmax,
+                            value_range=wl.value_range, pixels=pix)
+        assert_close(img[pix], ref)
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_c3_full_size_isosurfaces_match_oracle(orc, c3, k):
+    wl, r = c3
+    iso = wl.isovalues[k]
+    r.setRenderMode(GBVR_RM_ISOSURFACE)
+    r.setIsoValue(iso, (0.8, 0.8, 0.9))
+    v, p = wl.views[3]
+    r.setView(v, p)
+    r.paint()
+    img = r.readFramebuffer(0, as_float=True).reshape(-1, 4)
+    rng = np.random.default_rng(wl.synth.seed + k)
+    pix = _subset(img, rng, 240, 80, 0.5)
+    ref, _ = orc.render(orc.ProceduralFbm(wl.synth), v, p, wl.width, wl.height, np.zeros((2, 4), np.float32),
+                        mode=2, iso=iso, iso_rgb=(0.8, 0.8, 0.9), value_range=wl.value_range, pixels=pix)
+    hit_g, hit_r = img[pix, 3] > 0.5, ref[:, 3] > 0.5
+    # silhouette rays that graze the surface may hit on one side only
+    assert (hit_g != hit_r).mean() <= 0.01
+    both = hit_g & hit_r
+    assert both.sum() >= 200
+    assert_close(img[pix][both], ref[both])

@@ -60,3 +60,18 @@ def test_reference_arm_runs_without_the_library():
     rec = json.loads(lines[0])
     assert rec["impl"] == "reference" and rec["value"] > 0 and rec["cpu_baseline"]["kind"] == "port"
     assert lines[-1] == "LOADED 0 0"
+
+
+def test_procedural_fbm_render_equals_flat_volume_render(orc):
+    """The oracle's on-demand fractal voxels give the same FP64 image as the
+    generated volume, in every mode that reads voxels differently."""
+    from imagevis3d_gb300 import workloads
+    wl = workloads.config3(size=48, width=40, height=30, nviews=2)
+    vol = orc.synth_fbm(wl.synth)
+    proc = orc.ProceduralFbm(wl.synth)
+    v, p = workloads.orbit_views(1, 40, 30, radius=1.5 * workloads.DIAG, start=30.0)[0]
+    for kw in (dict(mode=1, grad_max=0.02), dict(mode=2, iso=20.0), dict(mode=0, interp=0)):
+        tf = wl.tf if kw["mode"] == 1 else np.tile(np.float32([[0.5, 0.6, 0.7, 0.05]]), (256, 1))
+        a, na = orc.render(vol, v, p, 40, 30, tf, value_range=wl.value_range, **kw)
+        b, nb = orc.render(proc, v, p, 40, 30, tf, value_range=wl.value_range, **kw)
+        assert np.array_equal(a, b) and na == nb

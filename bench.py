@@ -373,7 +373,8 @@ def run_c4(args):
     pool = int(args.pool_gib * (1 << 30)) if args.pool_gib > 0 else vol_bytes * 3 // 8
     r = Renderer()
     t0 = time.perf_counter()
-    r.loadSyntheticOutOfCore(wl.synth, pool, compression=0 if args.no_compress else 3, **wl.brick)
+    codec = 0 if args.no_compress else {"lz4": 3, "zlib": 1}[args.codec]
+    r.loadSyntheticOutOfCore(wl.synth, pool, compression=codec, **wl.brick)
     build_s = time.perf_counter() - t0
     info = r.datasetInfo()
     r.resize((wl.width, wl.height))
@@ -461,7 +462,8 @@ def run_c4(args):
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded blob volume, streamed from seed)",
         "config": {"workload": wl.name, "volume_bytes": vol_bytes, "host_store_bytes": info["host_bytes"],
                    "host_store_raw_bytes": info["host_raw_bytes"],
-                   "store_compression": "lz4 (16 KiB chunks, decoded on the GPU)" if info["compression"] else "none",
+                   "store_compression": ({3: "lz4", 1: "zlib"}[info["compression"]] + " (16 KiB chunks, decoded on "
+                                         "the GPU)") if info["compression"] else "none",
                    "device_pool_bytes": pool, "device_slots": info["device_slots"], "bricks": info["total_bricks"],
                    "lods": info["lod_count"], "frames_per_step": frames, "width": wl.width, "height": wl.height,
                    "l2": "volume and pool larger than L2", "step": "gbvr_paint_path over the 120-frame path"},
@@ -706,10 +708,12 @@ def main():
     ap.add_argument("--frames", type=int, default=120)
     ap.add_argument("--pool-gib", type=float, default=0.0)
     ap.add_argument("--no-compress", action="store_true", help="c4: raw host brick store")
+    ap.add_argument("--codec", default="lz4", choices=["lz4", "zlib"], help="c4: codec of the host brick store")
     ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--plain-requests", type=int, default=600)
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--slots", type=int, default=3, help="serving: batches in flight")
+    ap.add_argument("--no-tune-ex", action="store_true", help="c2: skip the extended autotuner")
     ap.add_argument("--pool-pass", type=int, default=1, help="c5: also run under a half-size brick-pool budget")
     ap.add_argument("--serve-requests", type=int, default=400,
                     help="c2: requests of the short serving run giving p50/p99 (0: skip)")
@@ -897,6 +901,15 @@ def main():
             r.readFramebuffer(0)
     e2e_plain = len(views) * max(1, args.steps // 2) / (time.perf_counter() - t0)
 
+    # ---- the extended autotuner (untimed, after every measurement above): launch
+    # shape x brick size (the dataset rebuilt from its finest level, same pixels)
+    # x samples per inner-loop step.  The headline keeps the configuration's 256^3
+    # bricks; this reports what the tuner would choose and the spread.
+    tune_ex = None
+    if not args.no_tune_ex:
+        r.setLaunchShape(8, 0)
+        tune_ex = r.autotuneEx(views, brick_sizes=(128, 256, 512), samples_per_step=(1, 2))
+        tune_ex["gain_vs_default"] = tune_ex["default_ms"] / tune_ex["best_ms"] if tune_ex["best_ms"] > 0 else None
     r.cleanup()
     # ---- short serving run (the metric's p99): Poisson arrivals at 70% of capacity ----
     sv = serving_run(args.serve_requests, 100, args.max_batch, err_requests=4) if args.serve_requests > 0 else None
@@ -1006,7 +1019,7 @@ def main():
             "texture_trilinear_fps": tex_fps,
             "mip_fps": mip_fps,
             "with_bboxes_fps": bbox_fps,
-            "autotune": {"sw": tune, "tex": tune_tex},
+            "autotune": {"sw": tune, "tex": tune_tex, "extended": tune_ex},
             "e2e_per_view_fps": e2e_plain,
             "image_error_vs_fp64": err,
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d,

@@ -172,6 +172,10 @@ SIGNATURES = {
     "gbvr_lz4_bound": [SZ],
     "gbvr_lz4_compress": [P, SZ, P, SZ],
     "gbvr_lz4_decompress": [P, SZ, P, SZ],
+    "gbvr_zlib_bound": [SZ],
+    "gbvr_zlib_compress": [P, SZ, P, SZ],
+    "gbvr_zlib_decompress": [P, SZ, P, SZ],
+    "gbvr_dev_zlib_decode": [P, P, P, I, P, P],
     "gbvr_set_clearview": [P, I, F, FP, F, F, F, F, F],
     "gbvr_paint_slice": [P, I, C.c_int64, I, I, I],
     "gbvr_paint_path": [P, C.POINTER(View), I, C.POINTER(C.c_int32), U64P, U64P],
@@ -251,7 +255,7 @@ _lib = None
 
 
 # functions that return something other than a status
-RESTYPES = {"gbvr_lz4_bound": SZ, "gbvr_lz4_compress": SZ}
+RESTYPES = {"gbvr_lz4_bound": SZ, "gbvr_lz4_compress": SZ, "gbvr_zlib_bound": SZ, "gbvr_zlib_compress": SZ}
 
 
 def lib():

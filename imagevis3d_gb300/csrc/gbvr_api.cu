@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <array>
 #include <climits>
+#include <cstddef>
 #include <stdexcept>
 #include <cstdlib>
 #include <cstdint>
@@ -25,6 +26,7 @@
 #include "../../include/gbvr.h"
 #include "abi_guard.h"
 #include "gbvr_internal.h"
+#include "deflate.h"
 #include "lz4.h"
 #include "synth_tables.h"
 #include "uvf.h"
@@ -678,7 +680,8 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
   ds.slot_used.assign(ds.nslots, 0);
   for (auto& b : ds.bricks) b.offset = 0;
   ds.compression = bp ? bp->compression : 0;
-  if (ds.compression != 0 && ds.compression != 3) return fail(GBVR_EINVAL, "compression must be 0 (none) or 3 (LZ4)");
+  if (ds.compression != 0 && ds.compression != 1 && ds.compression != 3)
+    return fail(GBVR_EINVAL, "compression must be 0 (none), 1 (zlib) or 3 (LZ4)");
   ds.raw_store_bytes = cursor * es;
   if (!ds.compression) {
     cudaError_t e = host_alloc_pinned(&ds.host_store.p, cursor * es);
@@ -795,14 +798,15 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
         std::vector<std::vector<uint8_t>> out(per);
         std::vector<std::vector<unsigned>> sizes(per);
         auto work = [&](unsigned t) {
-          std::vector<uint8_t> buf(lz4_bound(LZ_CHUNK));
+          std::vector<uint8_t> buf(std::max(lz4_bound(LZ_CHUNK), zlib_bound(LZ_CHUNK)));
           for (int j = (int)t; j < per; j += (int)nthreads) {
             const BrickInfo& b = ds.bricks[first + j];
             const size_t nbytes = (size_t)b.sx * b.sy * b.sz * es;
             const uint8_t* src = (const uint8_t*)h_layer.p + (size_t)j * slot_bytes;
             for (size_t o = 0; o < nbytes; o += LZ_CHUNK) {
               const size_t rn = std::min(LZ_CHUNK, nbytes - o);
-              const size_t cn = lz4_compress(src + o, rn, buf.data(), buf.size());
+              const size_t cn = ds.compression == 1 ? zlib_compress(src + o, rn, buf.data(), buf.size(), 16)
+                                                    : lz4_compress(src + o, rn, buf.data(), buf.size());
               if (cn > 0 && cn < rn) {
                 out[j].insert(out[j].end(), buf.data(), buf.data() + cn);
                 sizes[j].push_back((unsigned)cn);
@@ -1781,8 +1785,12 @@ int page_compressed(gbvr_renderer* r, const std::vector<std::pair<int, int>>& pa
   // pageable source: the copy returns once it is staged
   CUDA_TRY(cudaMemcpyAsync(ds.d_chunks.p, jobs.data(), sizeof(Lz4Chunk) * jobs.size(), cudaMemcpyHostToDevice,
                            r->copy_stream));
-  CUDA_TRY(launch_lz4_decode(ds.d_stage.p, ds.pool.p, ds.d_chunks.as<Lz4Chunk>(), (int)jobs.size(),
-                             ds.d_lz_err.as<int>(), r->copy_stream));
+  if (ds.compression == 1)
+    CUDA_TRY(launch_inflate(ds.d_stage.p, ds.pool.p, ds.d_chunks.as<Lz4Chunk>(), (int)jobs.size(),
+                            ds.d_lz_err.as<int>(), r->copy_stream));
+  else
+    CUDA_TRY(launch_lz4_decode(ds.d_stage.p, ds.pool.p, ds.d_chunks.as<Lz4Chunk>(), (int)jobs.size(),
+                               ds.d_lz_err.as<int>(), r->copy_stream));
   comp_bytes = total;
   return GBVR_OK;
 }
@@ -2013,8 +2021,8 @@ int ooc_streams(gbvr_renderer* r) {
 }
 
 // Out of core with a compressed store: a chunk the device decoder found
-// malformed (the store is written by lz4_compress, so only a corrupted store
-// does this) fails the paint.
+// malformed (the store is written by this library's compressors, so only a
+// corrupted store does this) fails the paint.
 int check_decode(gbvr_renderer* r) {
   if (!r->ds.ooc || !r->ds.compression) return GBVR_OK;
   int e = 0;
@@ -2799,7 +2807,9 @@ int gbvr_get_brick(gbvr_renderer* r, int lod, const int32_t brick[3], void* out,
       const unsigned cs = r->ds.chunk_size[r->ds.chunk_first[bidx] + k];
       const size_t rn = std::min(LZ_CHUNK, need - o), cn = cs & 0x7fffffffu;
       if (cs & 0x80000000u) memcpy((uint8_t*)out + o, src, rn);
-      else if (!lz4_decompress(src, cn, (uint8_t*)out + o, rn)) return fail(GBVR_EFORMAT, "corrupt compressed brick");
+      else if (!(r->ds.compression == 1 ? zlib_decompress(src, cn, (uint8_t*)out + o, rn)
+                                        : lz4_decompress(src, cn, (uint8_t*)out + o, rn)))
+        return fail(GBVR_EFORMAT, "corrupt compressed brick");
       src += cn;
     }
     return GBVR_OK;
@@ -3483,6 +3493,19 @@ int gbvr_build_uvf(const void* host, const int64_t dims[3], int dtype, const gbv
   std::unique_ptr<gbvr_renderer> hold(r);
   TRY(gbvr_load_volume(r, host, dims, dtype, bp));
   return gbvr_write_uvf(r, out_path);
+  GBVR_ABI_CATCH
+}
+
+static_assert(sizeof(gbvr_zchunk) == sizeof(Lz4Chunk) && offsetof(gbvr_zchunk, comp) == offsetof(Lz4Chunk, comp),
+              "gbvr_zchunk is the decoders' chunk record");
+
+int gbvr_dev_zlib_decode(const void* dev_src, void* dev_dst, const gbvr_zchunk* dev_chunks, int n, int* dev_err,
+                         void* stream) {
+  GBVR_ABI_TRY
+  if (n < 0 || (n > 0 && (!dev_src || !dev_dst || !dev_chunks || !dev_err))) return fail(GBVR_EINVAL, "bad arguments");
+  CUDA_TRY(launch_inflate(dev_src, dev_dst, reinterpret_cast<const Lz4Chunk*>(dev_chunks), n, dev_err,
+                          (cudaStream_t)stream));
+  return GBVR_OK;
   GBVR_ABI_CATCH
 }
 

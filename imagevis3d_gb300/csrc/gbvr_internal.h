@@ -312,6 +312,11 @@ struct Lz4Chunk {
 cudaError_t launch_lz4_decode(const void* stage, void* pool, const Lz4Chunk* chunks, int nchunks, int* err,
                               cudaStream_t s);
 
+// zlib-compressed chunks (the same table; comp bit 31: stored raw): one warp
+// per chunk; a malformed chunk or a wrong Adler-32 sets *err (nonzero)
+cudaError_t launch_inflate(const void* stage, void* pool, const Lz4Chunk* chunks, int nchunks, int* err,
+                           cudaStream_t s);
+
 // One of the three passes (1: Smax, 2: f64 max |grad| at Smax, 3: binning)
 // over the planes [zb, ze) of a volume streamed in z: `slab` holds planes
 // zlo .. (zlo <= zb - 1 unless zb = 0, and plane ze unless ze = Z).  The

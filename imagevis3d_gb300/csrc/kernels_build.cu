@@ -1146,4 +1146,401 @@ cudaError_t launch_lz4_decode(const void* stage, void* pool, const Lz4Chunk* chu
   return cudaGetLastError();
 }
 
+
+// DEFLATE's length / distance tables and the order of the code-length code
+// lengths (RFC 1951 3.2.5, 3.2.7), for the device decoder
+__constant__ uint16_t kLenBaseDev[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                                         31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+__constant__ uint8_t kLenExtraDev[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                                         2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+__constant__ uint16_t kDistBaseDev[30] = {1,    2,    3,    4,    5,    7,     9,     13,    17,  25,
+                                          33,   49,   65,   97,   129,  193,   257,   385,   513, 769,
+                                          1025, 1537, 2049, 3073, 4097, 6145,  8193,  12289, 16385, 24577};
+__constant__ uint8_t kDistExtraDev[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
+                                          6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+__constant__ uint8_t kClOrderDev[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+
+// ---------------------------------------------------------------------------
+// zlib (RFC 1950) / DEFLATE (RFC 1951) decoding of paged brick chunks: one
+// warp per chunk (a zlib stream of one chunk's raw bytes, or the raw bytes
+// when bit 31 of comp is set).  Lane 0 reads the bit stream: block headers,
+// code lengths and symbols, writing literals itself; a match is handed to the
+// whole warp, which copies it in steps of min(distance, 32) bytes with
+// __syncwarp between steps (a step reads only bytes written before it).  The
+// warp builds each block's decode tables together: per code a 10-bit (literal
+// / length) or 8-bit (distance) direct table entry (symbol << 4 | length) for
+// codes that short, canonical decoding by length for the rest.  After the last
+// block the warp sums the Adler-32 of the output and checks it.  Every read
+// and write is bounds-checked; a malformed chunk sets *err and stops.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kInfLitFast = 10, kInfDistFast = 8;
+constexpr int kInfWarps = 4;
+
+struct InflateSmem {
+  uint16_t lit_fast[1 << kInfLitFast];
+  uint16_t dist_fast[1 << kInfDistFast];
+  uint16_t code[320];                   // canonical code of each symbol (most significant bit first)
+  uint16_t lit_sym[288], dist_sym[32];  // symbols in code order
+  uint16_t lit_count[16], dist_count[16];
+  // literal/length lengths [0, 288), distance lengths [288, 320); while a
+  // dynamic header is read, the code-length code's lengths [0, 19) and the
+  // decoded HLIT + HDIST <= 316 lengths from 19 on
+  uint8_t lens[19 + 316 + 1];
+};
+
+struct InflateBits {
+  const unsigned char* in;
+  unsigned n, pos, past;
+  unsigned long long acc;
+  int bits;
+  __device__ void fill() {
+    while (bits <= 56) {
+      unsigned long long b = 0;
+      if (pos < n) b = in[pos];
+      else ++past;
+      ++pos;
+      acc |= b << bits;
+      bits += 8;
+    }
+  }
+  __device__ unsigned get(int k) {  // k <= 32
+    if (k == 0) return 0;
+    if (bits < k) fill();
+    const unsigned v = (unsigned)(acc & ((1ull << k) - 1ull));
+    acc >>= k;
+    bits -= k;
+    return v;
+  }
+  // bits beyond the input were consumed
+  __device__ bool over() const { return past > 0 && (unsigned long long)bits < 8ull * past; }
+};
+
+__device__ __forceinline__ unsigned rev_bits(unsigned c, int len) { return __brev(c) >> (32 - len); }
+
+// Count, validate (not over-subscribed), order the symbols and fill the
+// direct table of one code (lane 0 counts and orders; the warp fills).
+// Returns false (warp-uniform) for a malformed code.
+__device__ bool inflate_table(InflateSmem& sm, const uint8_t* lens, int n, uint16_t* count, uint16_t* sym,
+                              uint16_t* fast, int fast_bits, int lane) {
+  int ok = 1;
+  if (lane == 0) {
+    for (int b = 0; b < 16; ++b) count[b] = 0;
+    for (int i = 0; i < n; ++i) ++count[lens[i]];
+    count[0] = 0;
+    int left = 1;
+    for (int b = 1; b < 16; ++b) {
+      left = 2 * left - count[b];
+      if (left < 0) ok = 0;
+    }
+    if (ok) {
+      int offs[16], next[16];
+      offs[1] = 0;
+      for (int b = 1; b < 15; ++b) offs[b + 1] = offs[b] + count[b];
+      int c = 0;
+      next[0] = 0;
+      for (int b = 1; b < 16; ++b) {
+        c = (c + count[b - 1]) << 1;
+        next[b] = c;
+      }
+      for (int i = 0; i < n; ++i)
+        if (lens[i]) {
+          sym[offs[lens[i]]++] = (uint16_t)i;
+          sm.code[i] = (uint16_t)next[lens[i]]++;
+        }
+    }
+  }
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  if (!ok) return false;
+  const int size = 1 << fast_bits;
+  for (int i = lane; i < size; i += 32) fast[i] = 0;
+  __syncwarp();
+  for (int s = lane; s < n; s += 32) {
+    const int l = lens[s];
+    if (l == 0 || l > fast_bits) continue;
+    const unsigned r = rev_bits(sm.code[s], l);
+    const uint16_t e = (uint16_t)((s << 4) | l);
+    for (int k = (int)r; k < size; k += 1 << l) fast[k] = e;
+  }
+  __syncwarp();
+  return true;
+}
+
+// One symbol (lane 0): the direct table, else canonical decoding bit by bit.
+__device__ int inflate_symbol(InflateBits& br, const uint16_t* fast, int fast_bits, const uint16_t* count,
+                              const uint16_t* sym) {
+  if (br.bits < 15) br.fill();
+  const uint16_t e = fast[br.acc & ((1u << fast_bits) - 1u)];
+  if (e) {
+    br.get(e & 15);
+    return e >> 4;
+  }
+  int code = 0, first = 0, index = 0;
+  for (int b = 1; b < 16; ++b) {
+    code |= (int)br.get(1);
+    const int c = count[b];
+    if (code - first < c) return sym[index + code - first];
+    index += c;
+    first = (first + c) << 1;
+    code <<= 1;
+  }
+  return -1;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(32 * kInfWarps) k_inflate(const unsigned char* __restrict__ stage,
+                                                            unsigned char* __restrict__ pool,
+                                                            const Lz4Chunk* __restrict__ chunks, int nchunks,
+                                                            int* __restrict__ err) {
+  __shared__ InflateSmem smem[kInfWarps];
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= nchunks) return;
+  InflateSmem& sm = smem[threadIdx.x >> 5];
+  const Lz4Chunk c = chunks[w];
+  const unsigned char* in = stage + c.src;
+  unsigned char* out = pool + c.dst;
+  const unsigned n = c.comp & 0x7fffffffu, raw = c.raw;
+  if (c.comp & 0x80000000u) {  // stored uncompressed
+    if (n != raw) {
+      if (lane == 0) atomicOr(err, 1);
+      return;
+    }
+    for (unsigned i = lane; i < raw; i += 32) out[i] = in[i];
+    return;
+  }
+  int bad = 0;
+  if (lane == 0) {
+    const unsigned cmf = n >= 6 ? in[0] : 0, flg = n >= 6 ? in[1] : 0;
+    bad = n < 6 || (cmf & 15) != 8 || (cmf >> 4) > 7 || (cmf * 256 + flg) % 31 != 0 || (flg & 0x20);
+  }
+  if (__shfl_sync(0xffffffffu, bad, 0)) {
+    if (lane == 0) atomicOr(err, 1);
+    return;
+  }
+  // the last 4 bytes (the Adler-32) are not DEFLATE input
+  InflateBits br{in + 2, n - 6, 0, 0, 0ull, 0};
+  unsigned o = 0;
+  int last = 0;
+  while (!last && !bad) {
+    int type = 0;
+    if (lane == 0) {
+      last = (int)br.get(1);
+      type = (int)br.get(2);
+      if (br.over() || type == 3) bad = 1;
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    type = __shfl_sync(0xffffffffu, type, 0);
+    bad = __shfl_sync(0xffffffffu, bad, 0);
+    if (bad) break;
+    if (type == 0) {
+      // stored: to the byte boundary, LEN, NLEN, then LEN bytes (the warp copies)
+      unsigned L = 0, src = 0;
+      if (lane == 0) {
+        br.get(br.bits & 7);
+        const unsigned len = br.get(16), nlen = br.get(16);
+        const bool short_in = br.over();  // before the buffer is emptied below
+        // the whole bytes left in the bit buffer go back to the input
+        src = br.pos - (unsigned)(br.bits >> 3);
+        br.acc = 0;
+        br.bits = 0;
+        if (short_in || (len ^ 0xffffu) != nlen || o + len > raw || src + len > br.n) bad = 1;
+        L = len;
+        br.pos = src + len;
+        br.past = 0;
+      }
+      bad = __shfl_sync(0xffffffffu, bad, 0);
+      L = __shfl_sync(0xffffffffu, L, 0);
+      src = __shfl_sync(0xffffffffu, src, 0);
+      const unsigned o0 = __shfl_sync(0xffffffffu, o, 0);
+      if (bad) break;
+      for (unsigned i = lane; i < L; i += 32) out[o0 + i] = br.in[src + i];
+      o = o0 + L;
+      __syncwarp();
+      continue;
+    }
+    // the block's code lengths
+    if (type == 1) {
+      for (int i = lane; i < 320; i += 32) sm.lens[i] = i < 288 ? (i < 144 ? 8 : i < 256 ? 9 : i < 280 ? 7 : 8) : 5;
+      __syncwarp();
+    } else {
+      int hlit = 0, hdist = 0;
+      if (lane == 0) {
+        hlit = (int)br.get(5) + 257;
+        hdist = (int)br.get(5) + 1;
+        const int hclen = (int)br.get(4) + 4;
+        if (hlit > 286 || hdist > 30) bad = 1;
+        for (int i = 0; i < 19; ++i) sm.lens[i] = 0;
+        for (int k = 0; k < hclen; ++k) sm.lens[kClOrderDev[k]] = (uint8_t)br.get(3);
+        if (br.over()) bad = 1;
+      }
+      bad = __shfl_sync(0xffffffffu, bad, 0);
+      __syncwarp();
+      if (bad) break;
+      // the code-length code (in the distance slots of the tables, rebuilt below)
+      if (!inflate_table(sm, sm.lens, 19, sm.dist_count, sm.dist_sym, sm.dist_fast, kInfDistFast, lane)) {
+        bad = 1;
+        break;
+      }
+      if (lane == 0) {
+        uint8_t* lens = sm.lens + 19;  // decoded lengths, moved into place afterwards
+        const int total = hlit + hdist;
+        for (int k = 0; k < total && !bad;) {
+          const int sy = inflate_symbol(br, sm.dist_fast, kInfDistFast, sm.dist_count, sm.dist_sym);
+          if (sy < 0 || br.over()) {
+            bad = 1;
+            break;
+          }
+          if (sy < 16) {
+            lens[k++] = (uint8_t)sy;
+          } else {
+            int rep, val = 0;
+            if (sy == 16) {
+              if (k == 0) {
+                bad = 1;
+                break;
+              }
+              val = lens[k - 1];
+              rep = 3 + (int)br.get(2);
+            } else if (sy == 17) {
+              rep = 3 + (int)br.get(3);
+            } else {
+              rep = 11 + (int)br.get(7);
+            }
+            if (k + rep > total) {
+              bad = 1;
+              break;
+            }
+            while (rep--) lens[k++] = (uint8_t)val;
+          }
+        }
+        if (!bad) {
+          // literal/length lengths to [0, 288), distance lengths to [288, 320)
+          uint8_t tmp[32];
+          for (int i = 0; i < hdist; ++i) tmp[i] = lens[hlit + i];
+          for (int i = 0; i < hlit; ++i) sm.lens[i] = lens[i];  // moves down: no overlap hazard
+          for (int i = hlit; i < 288; ++i) sm.lens[i] = 0;
+          for (int i = 0; i < 32; ++i) sm.lens[288 + i] = i < hdist ? tmp[i] : 0;
+          if (sm.lens[256] == 0) bad = 1;
+        }
+      }
+      bad = __shfl_sync(0xffffffffu, bad, 0);
+      __syncwarp();
+      if (bad) break;
+    }
+    if (!inflate_table(sm, sm.lens, 288, sm.lit_count, sm.lit_sym, sm.lit_fast, kInfLitFast, lane) ||
+        !inflate_table(sm, sm.lens + 288, 32, sm.dist_count, sm.dist_sym, sm.dist_fast, kInfDistFast, lane)) {
+      bad = 1;
+      break;
+    }
+    // symbols: lane 0 writes literals; a match goes to the warp
+    for (;;) {
+      int op = 0;  // 1 match, 2 end of block, 3 malformed
+      unsigned L = 0, D = 0;
+      if (lane == 0) {
+        for (;;) {
+          const int sy = inflate_symbol(br, sm.lit_fast, kInfLitFast, sm.lit_count, sm.lit_sym);
+          if (sy < 0 || br.over()) {
+            op = 3;
+            break;
+          }
+          if (sy < 256) {
+            if (o >= raw) {
+              op = 3;
+              break;
+            }
+            out[o++] = (unsigned char)sy;
+            continue;
+          }
+          if (sy == 256) {
+            op = 2;
+            break;
+          }
+          const int li = sy - 257;
+          if (li >= 29) {
+            op = 3;
+            break;
+          }
+          L = kLenBaseDev[li] + br.get(kLenExtraDev[li]);
+          const int ds = inflate_symbol(br, sm.dist_fast, kInfDistFast, sm.dist_count, sm.dist_sym);
+          if (ds < 0 || ds >= 30) {
+            op = 3;
+            break;
+          }
+          D = kDistBaseDev[ds] + br.get(kDistExtraDev[ds]);
+          if (br.over() || D > o || o + L > raw) {
+            op = 3;
+            break;
+          }
+          op = 1;
+          break;
+        }
+      }
+      op = __shfl_sync(0xffffffffu, op, 0);
+      if (op == 3) {
+        bad = 1;
+        break;
+      }
+      if (op == 2) break;
+      L = __shfl_sync(0xffffffffu, L, 0);
+      D = __shfl_sync(0xffffffffu, D, 0);
+      const unsigned o0 = __shfl_sync(0xffffffffu, o, 0);
+      __syncwarp();  // lane 0's literals are visible to the copy
+      const unsigned step = D < 32 ? D : 32;
+      for (unsigned base = 0; base < L; base += step) {
+        const unsigned i = base + (unsigned)lane;
+        if ((unsigned)lane < step && i < L) out[o0 + i] = out[o0 - D + i];
+        __syncwarp();
+      }
+      o = o0 + L;
+    }
+  }
+  bad = __shfl_sync(0xffffffffu, bad, 0);
+  o = __shfl_sync(0xffffffffu, o, 0);
+  if (bad || o != raw) {
+    if (lane == 0) atomicOr(err, 1);
+    return;
+  }
+  // Adler-32 of the output against the stream's, at the byte after the last block
+  unsigned stored = 0;
+  int ok = 1;
+  if (lane == 0) {
+    const unsigned used = br.pos - (unsigned)(br.bits >> 3);
+    if (used + 4 > n - 2) {
+      ok = 0;
+    } else {
+      const unsigned char* a = in + 2 + used;
+      stored = ((unsigned)a[0] << 24) | ((unsigned)a[1] << 16) | ((unsigned)a[2] << 8) | a[3];
+    }
+  }
+  __syncwarp();
+  unsigned long long sa = 0, sb = 0;  // sum of bytes, sum of (raw - i) * byte
+  for (unsigned i = lane; i < raw; i += 32) {
+    const unsigned v = out[i];
+    sa += v;
+    sb += (unsigned long long)(raw - i) * v;
+  }
+  for (int k = 16; k > 0; k >>= 1) {
+    sa += __shfl_xor_sync(0xffffffffu, sa, k);
+    sb += __shfl_xor_sync(0xffffffffu, sb, k);
+  }
+  if (lane == 0) {
+    const unsigned A = (unsigned)((1ull + sa) % 65521ull), B = (unsigned)((sb + raw) % 65521ull);
+    if (!ok || ((B << 16) | A) != stored) atomicOr(err, 1);
+  }
+}
+
+cudaError_t launch_inflate(const void* stage, void* pool, const Lz4Chunk* chunks, int nchunks, int* err,
+                           cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (nchunks <= 0) return cudaSuccess;
+  const unsigned blocks = (unsigned)((nchunks + kInfWarps - 1) / kInfWarps);
+  k_inflate<<<blocks, 32 * kInfWarps, 0, s>>>((const unsigned char*)stage, (unsigned char*)pool, chunks, nchunks,
+                                              err);
+  return cudaGetLastError();
+}
+
 }  // namespace gbvr

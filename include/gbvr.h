@@ -93,9 +93,10 @@ typedef struct gbvr_brick_params {
                            whose fastest axis is closest to its screen x axis;
                            4: also a copy in 4x4x4 voxel blocks (2x memory),
                            sampled by every view */
-  int32_t compression;  /* out-of-core host store: 0 raw, 3 LZ4 (the UVF codec id CT_LZ4,
-                           CmdLineConverter/main.cpp:175-178): 16 KiB chunks compressed by host
-                           threads at build, decoded on the GPU when paged */
+  int32_t compression;  /* out-of-core host store: 0 raw, 1 zlib, 3 LZ4 (the UVF codec ids
+                           CT_ZLIB and CT_LZ4, UVFReader/BlockInfo.h:60-93; zlib is the
+                           converter's default, CmdLineConverter/main.cpp:146): 16 KiB chunks
+                           compressed by host threads at build, decoded on the GPU when paged */
   double aspect[3];     /* voxel spacing; 0 = (1,1,1) */
 } gbvr_brick_params;
 
@@ -114,7 +115,7 @@ typedef struct gbvr_dataset_info {
   float hist2d_max_grad;  /* max gradient magnitude of the 2D histogram */
   uint64_t host_bytes;    /* out of core: bytes of the page-locked host brick store */
   int32_t device_slots;   /* out of core: bricks the device pool holds at once */
-  int32_t compression;    /* out of core: the store's codec (0 raw, 3 LZ4) */
+  int32_t compression;    /* out of core: the store's codec (0 raw, 1 zlib, 3 LZ4) */
   uint64_t host_raw_bytes;/* out of core: the store's bytes uncompressed */
 } gbvr_dataset_info;
 
@@ -668,6 +669,33 @@ int gbvr_uvf_write_raster(const char* path, const char* raster_id, const void* v
 size_t gbvr_lz4_bound(size_t n);
 size_t gbvr_lz4_compress(const void* src, size_t n, void* dst, size_t cap);
 int gbvr_lz4_decompress(const void* src, size_t n, void* dst, size_t out_n);
+
+/* ---- zlib streams (RFC 1950) of DEFLATE data (RFC 1951): UVF brick compression id 1, CT_ZLIB
+ * (UVFReader/BlockInfo.h:60-93), the converter's default (CmdLineConverter/main.cpp:146).  The
+ * out-of-core brick store compresses with it when gbvr_brick_params.compression = 1 and the GPU
+ * decodes paged bricks.  gbvr_zlib_compress writes one zlib stream (dynamic Huffman blocks, or stored
+ * blocks where smaller) and returns its size (0: does not fit cap); gbvr_zlib_decompress decodes any
+ * zlib stream (stored, fixed and dynamic blocks) into exactly out_n bytes, checking its Adler-32
+ * (GBVR_EFORMAT when malformed).  Host only. ---- */
+size_t gbvr_zlib_bound(size_t n);
+size_t gbvr_zlib_compress(const void* src, size_t n, void* dst, size_t cap);
+int gbvr_zlib_decompress(const void* src, size_t n, void* dst, size_t out_n);
+
+/* One chunk of a batch of zlib streams for the GPU decoder: the stream at byte
+ * src of the source buffer, decoded to `raw` bytes at byte dst of the output
+ * buffer; bit 31 of comp marks a chunk stored raw (comp & 0x7fffffff == raw). */
+typedef struct gbvr_zchunk {
+  uint64_t src, dst;
+  uint32_t comp, raw;
+} gbvr_zchunk;
+
+/* GPU decoding of many zlib streams at once, the decoder of paged bricks: one
+ * warp per chunk (device pointers: dev_src, dev_dst, the chunk table
+ * dev_chunks and the flag dev_err, which a malformed stream or a wrong
+ * Adler-32 sets nonzero; the call neither clears nor reads it).  The call
+ * returns once the work is queued on `stream` (a cudaStream_t, or null). */
+int gbvr_dev_zlib_decode(const void* dev_src, void* dev_dst, const gbvr_zchunk* dev_chunks, int n, int* dev_err,
+                         void* stream);
 
 #ifdef __cplusplus
 }

@@ -298,19 +298,20 @@ def test_ooc_slices_equal_incore(mip):
         assert lods == ({1} if mip else {0})
 
 
+@pytest.mark.parametrize("codec", [3, 1], ids=["lz4", "zlib"])
 @pytest.mark.parametrize("case", sorted(CASES))
-def test_ooc_compressed_store_equals_raw_store(case):
-    """The LZ4-compressed host store holds the same bricks (decoded on the
-    host) and pages the same bricks (decoded on the GPU): images of a paged
-    fly-through equal the raw store's bit for bit."""
+def test_ooc_compressed_store_equals_raw_store(case, codec):
+    """The compressed host store (LZ4, codec id 3, or zlib, codec id 1) holds
+    the same bricks (decoded on the host) and pages the same bricks (decoded on
+    the GPU): images of a paged fly-through equal the raw store's bit for bit."""
     sp, bp = CASES[case]
     slot = (bp["brick_size"] ** 3) * (1 if sp.dtype == 0 else 2 if sp.dtype == 1 else 4)
     views = _inside_path(6, 128, 96)
     with Renderer(float_fb=True) as a, Renderer(float_fb=True) as b:
         a.loadSyntheticOutOfCore(sp, 30 * slot, **bp)
-        b.loadSyntheticOutOfCore(sp, 30 * slot, compression=3, **bp)
+        b.loadSyntheticOutOfCore(sp, 30 * slot, compression=codec, **bp)
         ia, ib = a.datasetInfo(), b.datasetInfo()
-        assert ib["compression"] == 3 and ib["host_raw_bytes"] == ia["host_bytes"] > 0
+        assert ib["compression"] == codec and ib["host_raw_bytes"] == ia["host_bytes"] > 0
         assert 0 < ib["host_bytes"] <= ib["host_raw_bytes"] * 1.01
         for lod in range(ia["lod_count"]):
             nb = ia["lod_bricks"][lod]
@@ -340,10 +341,11 @@ def test_ooc_compressed_store_equals_raw_store(case):
         assert np.array_equal(a.readFramebuffer(0, as_float=True), b.readFramebuffer(0, as_float=True))
 
 
-def test_ooc_compression_shrinks_smooth_volumes():
+@pytest.mark.parametrize("codec", [3, 1], ids=["lz4", "zlib"])
+def test_ooc_compression_shrinks_smooth_volumes(codec):
     sp = synth_params((192, 160, 144), np.uint8, 33, 10, (10.0, 30.0), (0.4, 1.0), 255.0, vmax=255.0,
                       bg_freq=1.0, bg_level=0.1, bg_amp=0.1)
     with Renderer() as r:
-        r.loadSyntheticOutOfCore(sp, 1 << 28, brick_size=64, overlap=2, compression=3)
+        r.loadSyntheticOutOfCore(sp, 1 << 28, brick_size=64, overlap=2, compression=codec)
         info = r.datasetInfo()
     assert info["host_bytes"] * 2 < info["host_raw_bytes"]

@@ -251,7 +251,8 @@ def run_c3(args):
     def frame_error(key, view_idx, kw, covered_thr):
         img = r.readFramebuffer(view_idx).reshape(-1, 4).astype(np.float64) / 255.0
         cov = np.flatnonzero(img[:, 3] > covered_thr)
-        pix = np.concatenate([erng.choice(cov, min(200, cov.size), replace=False) if cov.size else
+        ncov = 800 if kw.get("mode") == 2 else 200
+        pix = np.concatenate([erng.choice(cov, min(ncov, cov.size), replace=False) if cov.size else
                               np.zeros(0, np.int64), erng.integers(0, img.shape[0], 60)])
         v, p = wl.views[view_idx]
         ref, _ = orc.render(proc, v, p, wl.width, wl.height, wl.tf, value_range=wl.value_range, pixels=pix,
@@ -259,9 +260,22 @@ def run_c3(args):
         g = np.clip(img[pix], 0, 1)
         rr = np.clip(ref, 0, 1)
         if kw.get("mode") == 2:
-            same = (g[:, 3] > 0.5) == (rr[:, 3] > 0.5)  # silhouette rays may hit on one side only
-            errs[key + "_hit_mismatch"] = float(1.0 - same.mean())
-            g, rr = g[same], rr[same]
+            # silhouette rays may hit on one side only; where both hit, a pixel
+            # beyond tolerance is matched against the oracle at cameras
+            # perturbed by FP32-rounding-sized amounts (the isosurface of the
+            # fractal is ill-conditioned at a few pixels)
+            same = np.flatnonzero((g[:, 3] > 0.5) == (rr[:, 3] > 0.5))
+            errs[key + "_hit_mismatch"] = float(1.0 - same.size / len(g))
+            from tests.gpu_util import backward_error
+
+            def oracle(view, sub):
+                return orc.render(proc, view, p, wl.width, wl.height, wl.tf, value_range=wl.value_range,
+                                  pixels=pix[same[sub]], threads=orc.max_threads(), **kw)[0]
+
+            e = backward_error(g[same], rr[same], oracle, v)
+            errs[key] = {k: e[k] for k in ("max", "rms", "pixels", "beyond_tol", "backward_max", "backward_rms")}
+            errs[key]["unresolved"] = len(e["unresolved"])
+            return
         d = np.abs(g - rr)
         errs[key] = {"max": float(d.max()), "rms": float(np.sqrt((d * d).mean())), "pixels": int(len(g))}
 
@@ -279,7 +293,9 @@ def run_c3(args):
         iso_fps.append(len(wl.views) * args.steps / (sum(ims) / 1000.0))
         frame_error("iso_%d" % ii, 3, dict(mode=2, iso=iso, iso_rgb=(0.8, 0.8, 0.9)), 0.5)
     errs["tol_max"], errs["tol_rms"] = 2 / 255, 0.5 / 255
-    errs["note"] = "RGBA8 frames (8-bit rounding included) vs the FP64 oracle, seeded pixel subsets"
+    errs["note"] = ("RGBA8 frames (8-bit rounding included) vs the FP64 oracle, seeded pixel subsets; iso_*: "
+                    "max/rms forward, beyond_tol pixels, backward_max/rms against the oracle at cameras perturbed "
+                    "by <= 2e-6 relative per view-matrix entry")
     r.cleanup()
     # GPU 2D histogram of the 8 GiB level, device resident
     n = wl.synth.dims[0] * wl.synth.dims[1] * wl.synth.dims[2]
@@ -908,7 +924,7 @@ def main():
     tune_ex = None
     if not args.no_tune_ex:
         r.setLaunchShape(8, 0)
-        tune_ex = r.autotuneEx(views, brick_sizes=(128, 256, 512), samples_per_step=(1, 2))
+        tune_ex = r.autotuneEx(views, brick_sizes=(128, 256, 512), samples_per_step=(1, 4))
         tune_ex["gain_vs_default"] = tune_ex["default_ms"] / tune_ex["best_ms"] if tune_ex["best_ms"] > 0 else None
     r.cleanup()
     # ---- short serving run (the metric's p99): Poisson arrivals at 70% of capacity ----

@@ -67,7 +67,7 @@ class BuildStats(C.Structure):
 
 
 class TuneParams(C.Structure):
-    _fields_ = [("brick_sizes", C.c_int32 * 4), ("samples_per_step", C.c_int32 * 2), ("reserved", C.c_int32 * 2)]
+    _fields_ = [("brick_sizes", C.c_int32 * 4), ("samples_per_step", C.c_int32 * 4)]
 
 
 class TuneResultEx(C.Structure):

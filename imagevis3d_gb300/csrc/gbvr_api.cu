@@ -497,10 +497,13 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   }
   ds.stored_bytes = 0;
   for (auto& b : ds.bricks) ds.stored_bytes += (uint64_t)b.sx * b.sy * b.sz * es;
-  // layout copies: 1 = x-fastest only; 3 = + y- and z-fastest; 4 = + 4^3-blocked
-  ds.layouts = (bp && (bp->layouts == 3 || bp->layouts == 4)) ? bp->layouts : 1;
+  // layout copies: 1 = x-fastest only; 3 = + y- and z-fastest; 4 = + 4^3-blocked;
+  // 5 = + 4^3 blocks that also hold their +1 neighbours (5^3 voxels in 128
+  // elements: twice the room of the blocked copy, which each brick's share of
+  // the cursor already rounds to 4^3 blocks)
+  ds.layouts = (bp && (bp->layouts == 3 || bp->layouts == 4 || bp->layouts == 5)) ? bp->layouts : 1;
   ds.copy_stride = cursor;
-  const int ncopies = ds.layouts == 4 ? 2 : ds.layouts;
+  const int ncopies = ds.layouts == 5 ? 3 : ds.layouts == 4 ? 2 : ds.layouts;
   CUDA_TRY(ds.pool.alloc(cursor * es * ncopies));
   CUDA_TRY(ds.d_bricks.alloc(sizeof(BrickInfo) * ds.bricks.size()));
   CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyHostToDevice, s));
@@ -534,8 +537,8 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
       const BrickInfo& b = ds.bricks[L.brick_base + i];
       stored += (uint64_t)b.sx * b.sy * b.sz * es;
     }
-    for (int c = 0; c < (ds.layouts == 4 ? 2 : ds.layouts); ++c) {
-      const int perm = (ds.layouts == 4 && c == 1) ? 3 : c;
+    for (int c = 0; c < (ds.layouts >= 4 ? 2 : ds.layouts); ++c) {
+      const int perm = c == 1 && ds.layouts >= 4 ? ds.layouts - 1 : c;
       CUDA_TRY(launch_gather_bricks(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks,
                                     (char*)ds.pool.p + (size_t)c * cursor * es, perm, s));
       bs.bricks_bytes += level_bytes(l) + stored;
@@ -609,7 +612,7 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
                    bs.hist2d_bytes;
   bs.level0_bytes = level_bytes(0);
   bs.lod_count = (int32_t)ld.size();
-  bs.layout_copies = ds.layouts == 4 ? 2 : ds.layouts;
+  bs.layout_copies = ds.layouts >= 4 ? 2 : ds.layouts;
   if (bp && bp->build_texture) TRY(build_textures(ds, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   ds.loaded = true;
@@ -1126,8 +1129,8 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
   // layout copy: the axis whose voxel-space extent along screen x is largest
   // (row 0 of the view matrix is the camera's right vector in world space)
   f.perm = 0;
-  if (ds.layouts == 4) {
-    f.perm = 3;  // blocked copy, independent of the view direction
+  if (ds.layouts >= 4) {
+    f.perm = ds.layouts - 1;  // blocked copy, independent of the view direction
   } else if (ds.layouts == 3) {
     double best = -1;
     for (int a = 0; a < 3; ++a) {
@@ -1135,7 +1138,7 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
       if (w > best) { best = w; f.perm = a; }
     }
   }
-  f.copy_off = (unsigned long long)(f.perm == 3 ? 1 : f.perm) * ds.copy_stride;
+  f.copy_off = (unsigned long long)(f.perm >= 3 ? 1 : f.perm) * ds.copy_stride;
 }
 
 }  // namespace
@@ -2359,9 +2362,8 @@ int paint_batch(gbvr_renderer* r, const gbvr_view* views, int n, bool async = fa
     shared.touched_stride = shared.touched ? r->ds.levels[level].nbricks : 0;
     shared.cell_touched_stride = shared.cell_touched ? r->cell_words : 0;
   }
-  const int sps = uniform && r->samples_per_step == 2 && r->mode == GBVR_RM_1DTRANS && r->sampler == GBVR_SAMPLER_SW
-                      ? 2 : 1;
-  const int max_per_sm = sps == 2 ? r->max_ctas_per_sm_sps2
+  const int sps = uniform && r->mode == GBVR_RM_1DTRANS && r->sampler == GBVR_SAMPLER_SW ? r->samples_per_step : 1;
+  const int max_per_sm = sps >= 2 ? r->max_ctas_per_sm_sps2
                                   : (uniform ? r->max_ctas_per_sm_u[r->mode] : r->max_ctas_per_sm[r->mode]);
   const int per_sm = r->ctas_per_sm > 0 ? std::min(r->ctas_per_sm, max_per_sm) : max_per_sm;
   const int grid = r->sm_count * per_sm;
@@ -3081,7 +3083,7 @@ int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_res
 int gbvr_set_samples_per_step(gbvr_renderer* r, int sps) {
   GBVR_ABI_TRY
   TRY(check_r(r));
-  if (sps != 1 && sps != 2) return fail(GBVR_EINVAL, "samples per step must be 1 or 2");
+  if (sps != 1 && sps != 2 && sps != 4 && sps != 8) return fail(GBVR_EINVAL, "samples per step must be 1, 2, 4 or 8");
   r->samples_per_step = sps;
   return GBVR_OK;
   GBVR_ABI_CATCH
@@ -3096,11 +3098,11 @@ int gbvr_autotune_ex(gbvr_renderer* r, const gbvr_view* views, int n, const gbvr
   TRY(settle_async(r));
   std::vector<int> bricks, spss;
   for (int i = 0; i < 4 && tp && tp->brick_sizes[i] > 0; ++i) bricks.push_back(tp->brick_sizes[i]);
-  for (int i = 0; i < 2 && tp && tp->samples_per_step[i] > 0; ++i) spss.push_back(tp->samples_per_step[i]);
+  for (int i = 0; i < 4 && tp && tp->samples_per_step[i] > 0; ++i) spss.push_back(tp->samples_per_step[i]);
   for (int b : bricks)
     if (b - 2 * r->ds.ghost < 8 || b > 2048) return fail(GBVR_EINVAL, "brick size out of range");
   for (int v : spss)
-    if (v != 1 && v != 2) return fail(GBVR_EINVAL, "samples per step must be 1 or 2");
+    if (v != 1 && v != 2 && v != 4 && v != 8) return fail(GBVR_EINVAL, "samples per step must be 1, 2, 4 or 8");
   const int brick0 = r->ds.brick;
   if (bricks.empty()) bricks.push_back(brick0);
   if (spss.empty()) spss.push_back(r->samples_per_step);

@@ -281,6 +281,40 @@ __global__ void k_gather(const T* __restrict__ level, long long X, long long Y, 
   }
 }
 
+// Brick gather into overlapped 4^3 blocks (layout copy 4): block (bx, by, bz)
+// of a brick's stored box holds the 5^3 voxels 4 b + (0..4) per axis, x
+// fastest, in 128 elements (the last 3 zero), blocks in x, y, z order, the
+// brick's blocks at twice its offset of the x-fastest copy.  Voxel 4 of a
+// block repeats voxel 0 of the next one, so every trilinear footprint of a
+// cell in the block lies in the block; the footprint of a cell inside the
+// stored box never reaches past it, and slots past the box hold its edge.
+// One thread per destination element, consecutive threads along x.
+template <typename T>
+__global__ void k_gather_ov(const T* __restrict__ level, long long X, long long Y, long long Z, long long vz0,
+                            const BrickInfo* __restrict__ bricks, T* __restrict__ pool) {
+  const BrickInfo b = bricks[blockIdx.y];
+  const long long nbx = (b.sx + 3) >> 2, nby = (b.sy + 3) >> 2, nbz = (b.sz + 3) >> 2;
+  const long long n = nbx * nby * nbz * 128;
+  T* dst = pool + 2 * (long long)b.offset;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int slot = (int)(e & 127);
+    if (slot >= 125) {
+      dst[e] = T(0);
+      continue;
+    }
+    const long long blk = e >> 7;
+    const long long bx = blk % nbx, by = (blk / nbx) % nby, bz = blk / (nbx * nby);
+    const long long xs = min(4 * bx + slot % 5, (long long)b.sx - 1);
+    const long long ys = min(4 * by + (slot / 5) % 5, (long long)b.sy - 1);
+    const long long zs = min(4 * bz + slot / 25, (long long)b.sz - 1);
+    // ghosts outside the level replicate its edge voxels
+    const long long x = min(max((long long)b.ox + xs, 0LL), X - 1);
+    const long long y = min(max((long long)b.oy + ys, 0LL), Y - 1);
+    const long long z = min(max((long long)b.oz + zs, 0LL), Z - 1);
+    dst[e] = __ldg(level + ((z - vz0) * Y + y) * X + x);
+  }
+}
+
 // The inverse of k_gather for the x-fastest copy: every brick's interior
 // voxels (its [max(lo, 0), min(hi, dims)) box) back into the flat level.  The
 // interiors tile the level, so every voxel is written once.  One block per
@@ -326,6 +360,18 @@ cudaError_t launch_gather_bricks_window(const void* level, int dtype, const long
   if (nbricks <= 0) return cudaSuccess;
   dim3 grid((unsigned)(dims[2] < 256 ? dims[2] : 256), (unsigned)nbricks);
   int threads = 256;
+  if (perm == 4) {
+    if (dtype == DT_U8)
+      k_gather_ov<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], vz0, bricks_dev,
+                                                    (uint8_t*)pool);
+    else if (dtype == DT_U16)
+      k_gather_ov<uint16_t><<<grid, threads, 0, s>>>((const uint16_t*)level, dims[0], dims[1], dims[2], vz0,
+                                                     bricks_dev, (uint16_t*)pool);
+    else
+      k_gather_ov<float><<<grid, threads, 0, s>>>((const float*)level, dims[0], dims[1], dims[2], vz0, bricks_dev,
+                                                  (float*)pool);
+    return cudaGetLastError();
+  }
   if (dtype == DT_U8)
     k_gather<uint8_t><<<grid, threads, 0, s>>>((const uint8_t*)level, dims[0], dims[1], dims[2], vz0, bricks_dev, (uint8_t*)pool, perm);
   else if (dtype == DT_U16)

@@ -66,8 +66,8 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v,
 // the pool in the frame's layout copy; the texture coordinate of its centre
 // is g + t.
 struct BrickView {
-  long long base;    // perm 3: element offset of the brick's first block
-  int s0, s1, s2;    // perm 3: 64 * blocks per row, 64 * blocks per slab (s1, s2)
+  long long base;    // perm 3, 4: element offset of the brick's first block
+  int s0, s1, s2;    // perm 3 (4): 64 (128) * blocks per row, per slab (s1, s2)
   int ox, oy, oz;    // perm 3: stored origin
   unsigned long long tex;
   float tx, ty, tz;
@@ -89,6 +89,11 @@ __device__ __forceinline__ void load_brick(const FrameDesc& f, int bi, BrickView
     b.s1 = ((sx + 3) >> 2) << 6;
     b.s2 = b.s1 * ((sy + 3) >> 2);
     b.base = (long long)f.copy_off + off;
+  } else if (f.perm == 4) {
+    b.s0 = 128;
+    b.s1 = ((sx + 3) >> 2) << 7;
+    b.s2 = b.s1 * ((sy + 3) >> 2);
+    b.base = (long long)f.copy_off + 2 * off;
   } else {
     if (f.perm == 0) { b.s0 = 1; b.s1 = sx; b.s2 = sx * sy; }
     else if (f.perm == 1) { b.s1 = 1; b.s2 = sy; b.s0 = sy * sz; }
@@ -140,6 +145,28 @@ __device__ __forceinline__ float sample_cell(const FrameDesc& f, const BrickView
                         (float)(gz + (fz >= 0.5f)) + b.tz) * VoxelTraits<T>::tex_scale;
   }
   const T* pool = reinterpret_cast<const T*>(f.pool);
+  if (f.perm == 4) {
+    // 4^3 blocks that hold their +1 neighbours: voxel (lx, ly, lz) at
+    // (lz & 3) 25 + (ly & 3) 5 + (lx & 3) of block l >> 2, and the cell's
+    // other 7 voxels at fixed offsets from it
+    int lx = gx - b.ox, ly = gy - b.oy, lz = gz - b.oz;
+    if (!f.interp) {
+      lx += fx >= 0.5f; ly += fy >= 0.5f; lz += fz >= 0.5f;
+      return ldv(pool + (b.base + (long long)(lz >> 2) * b.s2 + (ly >> 2) * b.s1 + ((lx >> 2) << 7) +
+                         ((lz & 3) * 25 + (ly & 3) * 5 + (lx & 3))));
+    }
+    const T* p0 = pool + (b.base + (long long)(lz >> 2) * b.s2 + (ly >> 2) * b.s1 + ((lx >> 2) << 7) +
+                          ((lz & 3) * 25 + (ly & 3) * 5 + (lx & 3)));
+    float v000 = ldv(p0), v100 = ldv(p0 + 1), v010 = ldv(p0 + 5), v110 = ldv(p0 + 6);
+    float v001 = ldv(p0 + 25), v101 = ldv(p0 + 26), v011 = ldv(p0 + 30), v111 = ldv(p0 + 31);
+    float c00 = fmaf(fx, v100 - v000, v000);
+    float c10 = fmaf(fx, v110 - v010, v010);
+    float c01 = fmaf(fx, v101 - v001, v001);
+    float c11 = fmaf(fx, v111 - v011, v011);
+    float c0 = fmaf(fy, c10 - c00, c00);
+    float c1 = fmaf(fy, c11 - c01, c01);
+    return fmaf(fz, c1 - c0, c0);
+  }
   if (f.perm == 3) {
     // 4^3 blocks: voxel (lx, ly, lz) of the stored box sits in block
     // (l >> 2) at position (lz & 3) 16 + (ly & 3) 4 + (lx & 3)
@@ -255,6 +282,15 @@ __device__ __forceinline__ void make_taps(const FrameDesc& f, const BrickView& b
       t.X[i] = ((x >> 2) << 6) + (x & 3);
       t.Y[i] = (y >> 2) * b.s1 + ((y & 3) << 2);
       t.Z[i] = (z >> 2) * b.s2 + ((z & 3) << 4);
+    }
+  } else if (f.perm == 4) {
+    t.base = b.base;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int x = lx + i, y = ly + i, z = lz + i;
+      t.X[i] = ((x >> 2) << 7) + (x & 3);
+      t.Y[i] = (y >> 2) * b.s1 + (y & 3) * 5;
+      t.Z[i] = (z >> 2) * b.s2 + (z & 3) * 25;
     }
   } else {
     t.base = b.base + (long long)b.ox * b.s0 + (long long)b.oy * b.s1 + (long long)b.oz * b.s2;
@@ -483,10 +519,102 @@ __device__ __forceinline__ bool composite(const FrameDesc& f, float4 c, Accum& a
 // over the lens radius) it gets opacity clamp(cv_context (1 - |n.v|) +
 // cv_border rho^2, 0, 1), and the march goes on to the first hit of f.cv_iso
 // (the focus surface, from the context hit's sample on), which lies behind.
+// The walk along one ray, in sample-index units: K samples, the first kept
+// sample k (after the clip plane), and the crossing of the plane x_i = p as
+// fma(p, ka_i, kb_i) -- the k with t_k = (p - ov_i) / dv_i, the -1/2 of the
+// sample centres included.  Per axis the ray leaves a box through its upper
+// plane when dv_i > 0 and its lower plane otherwise; an axis the ray runs
+// parallel to gives +inf.
+struct Walk {
+  int K, k;
+  float ka[3], kb[3];
+};
+
+__device__ __forceinline__ void walk_setup(const FrameDesc& f, const RaySetup& r, Walk& w) {
+  const float dt = f.dt;
+  const float t0 = r.t0;
+  w.K = max(0, (int)ceilf((r.t1 - t0) / dt - 0.5f));
+  const float inv_dt = 1.f / dt;
+  {
+    const float kt = fmaf(t0, inv_dt, 0.5f);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const bool par = !(fabsf(r.dv[i]) > 1e-30f);
+      w.ka[i] = par ? 0.f : r.inv[i] * inv_dt;
+      w.kb[i] = par ? INFINITY : -fmaf(r.ov[i], w.ka[i], kt);
+    }
+  }
+  w.k = 0;
+  if (f.clip_on) {
+    // Clip plane: keep the samples with n . p + d <= 0.  Along the ray
+    // n . p + d = s0 + s1 t is monotone, so the kept samples are a prefix
+    // or a suffix of [0, K): estimated from the crossing, then settled with
+    // the per-sample test itself.  Sample positions do not move.
+    float s0 = f.clip[3], s1 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float o = (r.ov[i] + 0.5f) / f.vox_scale[i] - f.half_extent[i];
+      s0 = fmaf(f.clip[i], o, s0);
+      s1 = fmaf(f.clip[i], r.dw[i], s1);
+    }
+    auto keep = [&](int kk) { return fmaf(s1, fmaf((float)kk + 0.5f, dt, t0), s0) <= 0.f; };
+    if (s1 > 0.f) {
+      const float kf = floorf((-s0 / s1 - t0) * inv_dt - 0.5f);
+      int e = kf < 0.f ? 0 : (kf >= (float)w.K ? w.K : (int)kf + 1);
+      while (e > 0 && !keep(e - 1)) --e;
+      while (e < w.K && keep(e)) ++e;
+      w.K = e;
+    } else if (s1 < 0.f) {
+      const float kf = ceilf((-s0 / s1 - t0) * inv_dt - 0.5f);
+      int e = kf <= 0.f ? 0 : (kf >= (float)w.K ? w.K : (int)kf);
+      while (e < w.K && !keep(e)) ++e;
+      while (e > 0 && keep(e - 1)) --e;
+      w.k = e;
+    } else if (!(s0 <= 0.f)) {
+      w.K = 0;
+    }
+  }
+}
+
+__device__ __forceinline__ float walk_exit(const Walk& w, int ex, int ey, int ez) {
+  return fminf(fminf(fmaf((float)ex, w.ka[0], w.kb[0]), fmaf((float)ey, w.ka[1], w.kb[1])),
+               fmaf((float)ez, w.ka[2], w.kb[2]));
+}
+
+__device__ __forceinline__ void walk_pos(const FrameDesc& f, const RaySetup& r, int kk, float& px, float& py,
+                                         float& pz) {
+  const float t = fmaf((float)kk + 0.5f, f.dt, r.t0);
+  px = fmaf(t, r.dv[0], r.ov[0]);
+  py = fmaf(t, r.dv[1], r.ov[1]);
+  pz = fmaf(t, r.dv[2], r.ov[2]);
+}
+
+// First sample index >= k0 + 1 whose cell leaves the box [lo, hi) (per axis,
+// on clamped floor coordinates), or K: estimated from the box's exit planes,
+// then settled by the same floor(pos) rule that assigns samples to bricks and
+// cells.  Positions are monotone in k, so members form one run and only its
+// ends need checking.
+__device__ __forceinline__ int walk_run_end(const FrameDesc& f, const RaySetup& r, const Walk& w, int k0, int lx,
+                                            int ly, int lz, int hx, int hy, int hz) {
+  const float kef =
+      ceilf(walk_exit(w, r.dv[0] > 0.f ? hx : lx, r.dv[1] > 0.f ? hy : ly, r.dv[2] > 0.f ? hz : lz));
+  int ke = kef >= (float)w.K ? w.K : max(k0 + 1, (int)kef);
+  auto in_box = [&](int kk) {
+    float qx, qy, qz;
+    walk_pos(f, r, kk, qx, qy, qz);
+    const int cx = clamp_cell(qx, f.dims[0]), cy = clamp_cell(qy, f.dims[1]), cz = clamp_cell(qz, f.dims[2]);
+    return cx >= lx && cx < hx && cy >= ly && cy < hy && cz >= lz && cz < hz;
+  };
+  while (ke > k0 + 1 && !in_box(ke - 1)) --ke;
+  while (ke < w.K && in_box(ke)) ++ke;
+  return ke;
+}
+
 // SPS (1D TF, software sampler only): samples per step of the inner loop.
 // With 2, a step evaluates two consecutive samples -- both samples' voxel and
 // TF loads in flight together -- and composites them in order, stopping after
 // the first if it ends the ray: the same pixels as one sample per step.
+// (4 and 8: march_1d_shared.)
 template <typename T, int MODE, int SAMPLER, bool CV = false, int SPS = 1>
 __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, int vidx, const float* light_to,
                         float cv_rho = 2.f) {
@@ -497,81 +625,16 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
   if (r.hit) {
     const float dt = f.dt;
     const float t0 = r.t0;
-    int K = max(0, (int)ceilf((r.t1 - t0) / dt - 0.5f));
     const float V[3] = {-r.dw[0], -r.dw[1], -r.dw[2]};
-    const float inv_dt = 1.f / dt;
-    // Crossing of the plane x_i = p, in sample-index units: the k with
-    // t_k = (p - ov_i) / dv_i, i.e. fma(p, ka_i, kb_i) (the -1/2 of the
-    // sample centres included).  Per axis the ray leaves a box through its
-    // upper plane when dv_i > 0 and its lower plane otherwise; an axis the ray
-    // runs parallel to gives +inf.
-    float ka[3], kb[3];
-    {
-      const float kt = fmaf(t0, inv_dt, 0.5f);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        const bool par = !(fabsf(r.dv[i]) > 1e-30f);
-        ka[i] = par ? 0.f : r.inv[i] * inv_dt;
-        kb[i] = par ? INFINITY : -fmaf(r.ov[i], ka[i], kt);
-      }
-    }
-    auto exit_k = [&](int ex, int ey, int ez) {
-      return fminf(fminf(fmaf((float)ex, ka[0], kb[0]), fmaf((float)ey, ka[1], kb[1])), fmaf((float)ez, ka[2], kb[2]));
-    };
-    auto pos_of = [&](int kk, float& px, float& py, float& pz) {
-      const float t = fmaf((float)kk + 0.5f, dt, t0);
-      px = fmaf(t, r.dv[0], r.ov[0]);
-      py = fmaf(t, r.dv[1], r.ov[1]);
-      pz = fmaf(t, r.dv[2], r.ov[2]);
-    };
-    // First sample index >= k + 1 whose cell leaves the box [lo, hi) (per
-    // axis, on clamped floor coordinates), or K: estimated from the box's
-    // exit planes, then settled by the same floor(pos) rule that assigns
-    // samples to bricks and cells.  Positions are monotone in k, so members
-    // form one run and only its ends need checking.
+    Walk wk;
+    walk_setup(f, r, wk);
+    const int K = wk.K;
+    auto exit_k = [&](int ex, int ey, int ez) { return walk_exit(wk, ex, ey, ez); };
+    auto pos_of = [&](int kk, float& px, float& py, float& pz) { walk_pos(f, r, kk, px, py, pz); };
     auto run_end = [&](int k0, int lx, int ly, int lz, int hx, int hy, int hz) -> int {
-      const float kef = ceilf(exit_k(r.dv[0] > 0.f ? hx : lx, r.dv[1] > 0.f ? hy : ly, r.dv[2] > 0.f ? hz : lz));
-      int ke = kef >= (float)K ? K : max(k0 + 1, (int)kef);
-      auto in_box = [&](int kk) {
-        float qx, qy, qz;
-        pos_of(kk, qx, qy, qz);
-        const int cx = clamp_cell(qx, f.dims[0]), cy = clamp_cell(qy, f.dims[1]), cz = clamp_cell(qz, f.dims[2]);
-        return cx >= lx && cx < hx && cy >= ly && cy < hy && cz >= lz && cz < hz;
-      };
-      while (ke > k0 + 1 && !in_box(ke - 1)) --ke;
-      while (ke < K && in_box(ke)) ++ke;
-      return ke;
+      return walk_run_end(f, r, wk, k0, lx, ly, lz, hx, hy, hz);
     };
-    int k = 0;
-    if (f.clip_on) {
-      // Clip plane: keep the samples with n . p + d <= 0.  Along the ray
-      // n . p + d = s0 + s1 t is monotone, so the kept samples are a prefix
-      // or a suffix of [0, K): estimated from the crossing, then settled with
-      // the per-sample test itself.  Sample positions do not move.
-      float s0 = f.clip[3], s1 = 0.f;
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        const float o = (r.ov[i] + 0.5f) / f.vox_scale[i] - f.half_extent[i];
-        s0 = fmaf(f.clip[i], o, s0);
-        s1 = fmaf(f.clip[i], r.dw[i], s1);
-      }
-      auto keep = [&](int kk) { return fmaf(s1, fmaf((float)kk + 0.5f, dt, t0), s0) <= 0.f; };
-      if (s1 > 0.f) {
-        const float kf = floorf((-s0 / s1 - t0) * inv_dt - 0.5f);
-        int e = kf < 0.f ? 0 : (kf >= (float)K ? K : (int)kf + 1);
-        while (e > 0 && !keep(e - 1)) --e;
-        while (e < K && keep(e)) ++e;
-        K = e;
-      } else if (s1 < 0.f) {
-        const float kf = ceilf((-s0 / s1 - t0) * inv_dt - 0.5f);
-        int e = kf <= 0.f ? 0 : (kf >= (float)K ? K : (int)kf);
-        while (e < K && !keep(e)) ++e;
-        while (e > 0 && keep(e - 1)) --e;
-        k = e;
-      } else if (!(s0 <= 0.f)) {
-        K = 0;
-      }
-    }
+    int k = wk.k;
     bool done = false;
     BrickView b;
     int bi = -1, bke = 0;  // current brick and the end of the ray's run in it
@@ -819,6 +882,160 @@ __device__ __forceinline__ float3 bg_at(const FrameDesc& f, int py) {
                      fmaf(t, f.bg[2] - f.bg_top[2], f.bg_top[2]));
 }
 
+// 1D TF, software sampler, warp-shared sampling (SPS = CAP = 4 or 8).  Each
+// lane walks its own ray -- brick changes, skipped bricks and empty-cell
+// jumps, one head step per loop step as march does -- and composites its own
+// samples in order; but evaluating the samples (position, cell, 8 voxels,
+// trilinear, TF, opacity correction) is shared: every step, the pending
+// samples of all lanes' current runs, up to CAP per lane, are laid out one
+// after another and the warp evaluates them 32 at a time, each lane fetching
+// its task's ray and brick from the owning lane by shuffle.  The owners then
+// take their results back by shuffle and composite them in sample order,
+// stopping at early termination.  Sample positions, values, compositing order
+// and the termination sample are those of march: the same pixels.  All 32
+// lanes of the warp must call it together (`live` false for a lane without a
+// pixel).
+template <typename T, int CAP>
+__device__ float4 march_1d_shared(const FrameDesc& f, const RaySetup& r, bool live, unsigned& nsamp, int vidx) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  Accum acc = {0.f, 0.f, 0.f, 0.f};
+  Walk wk;
+  bool active = live && r.hit;
+  if (active) walk_setup(f, r, wk);
+  else wk.K = wk.k = 0;
+  int k = wk.k, kr = wk.k;  // pending samples of the current run: [k, kr)
+  BrickView b;
+  b.base = 0;
+  b.s0 = b.s1 = b.s2 = 0;
+  b.ox = b.oy = b.oz = 0;
+  int bi = -1, bke = 0;
+  const int sh = f.cell_shift;
+  for (;;) {
+    // one head step for a lane without pending samples (as an outer step of march)
+    if (active && k >= kr) {
+      if (k >= wk.K) {
+        active = false;
+      } else {
+        float px, py, pz;
+        walk_pos(f, r, k, px, py, pz);
+        const int gx = clamp_cell(px, f.dims[0]), gy = clamp_cell(py, f.dims[1]), gz = clamp_cell(pz, f.dims[2]);
+        bool run = true;
+        if (bi < 0 || k >= bke) {
+          bi = brick_index(f, gx, gy, gz);
+          load_brick(f, bi, b);
+          bke = walk_run_end(f, r, wk, k, b.lox, b.loy, b.loz, b.hix, b.hiy, b.hiz);
+          if (f.empty_skip >= 1 && __ldg(f.skip + bi)) {
+            k = bke;
+            bi = -1;
+            run = false;
+          } else if (f.touched) {
+            f.touched[(long long)vidx * f.touched_stride + bi] = 1;
+          }
+        }
+        if (run) {
+          int ke = bke;
+          if (f.empty_skip >= 2) {
+            const int cx = max(gx, 0) >> sh, cy = max(gy, 0) >> sh, cz = max(gz, 0) >> sh;
+            const size_t ci = ((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx;
+            const int d = __ldg(f.occ + ci);
+            const int lo_c = d > 0 ? d - 1 : 0;  // cube = cells [c - lo_c, c + lo_c]
+            const float kef =
+                ceilf(walk_exit(wk, r.dv[0] > 0.f ? min((cx + lo_c + 1) << sh, f.dims[0]) : max(cx - lo_c, 0) << sh,
+                                r.dv[1] > 0.f ? min((cy + lo_c + 1) << sh, f.dims[1]) : max(cy - lo_c, 0) << sh,
+                                r.dv[2] > 0.f ? min((cz + lo_c + 1) << sh, f.dims[2]) : max(cz - lo_c, 0) << sh));
+            if (d > 0) {
+              k = kef >= (float)wk.K ? wk.K : max(k + 1, (int)kef);
+              if (k >= bke) bi = -1;
+              run = false;
+            } else {
+              ke = kef >= (float)ke ? ke : max(k + 1, (int)kef);
+              if (f.cell_touched) {
+                unsigned* w = f.cell_touched + (long long)vidx * f.cell_touched_stride + (ci >> 5);
+                const unsigned bit = 1u << (ci & 31);
+                if (!(*(volatile unsigned*)w & bit)) atomicOr(w, bit);
+              }
+            }
+          }
+          if (run) kr = ke;
+        }
+      }
+    }
+    // this step's tasks: up to CAP pending samples per lane, laid out lane after lane
+    const int n = active && k < kr ? min(kr - k, CAP) : 0;
+    int off = n;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(FULL, off, d);
+      if (lane >= d) off += y;
+    }
+    off -= n;  // exclusive prefix
+    const int total = __shfl_sync(FULL, off + n, 31);
+    if (total == 0) {
+      if (!__any_sync(FULL, active)) break;
+      continue;
+    }
+    bool stop = false;  // this lane's ray ended within this step
+    for (int base = 0; base < total; base += 32) {
+      const int t = base + lane;
+      // the task's owner: the last lane whose tasks start at or before t
+      int own = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = own + step;
+        if (__shfl_sync(FULL, off, cand) <= t) own = cand;
+      }
+      const int o_k = __shfl_sync(FULL, k, own), o_off = __shfl_sync(FULL, off, own);
+      const float o_t0 = __shfl_sync(FULL, r.t0, own);
+      const float ovx = __shfl_sync(FULL, r.ov[0], own), ovy = __shfl_sync(FULL, r.ov[1], own),
+                  ovz = __shfl_sync(FULL, r.ov[2], own);
+      const float dvx = __shfl_sync(FULL, r.dv[0], own), dvy = __shfl_sync(FULL, r.dv[1], own),
+                  dvz = __shfl_sync(FULL, r.dv[2], own);
+      BrickView ob;
+      ob.base = __shfl_sync(FULL, b.base, own);
+      ob.s0 = __shfl_sync(FULL, b.s0, own);
+      ob.s1 = __shfl_sync(FULL, b.s1, own);
+      ob.s2 = __shfl_sync(FULL, b.s2, own);
+      ob.ox = __shfl_sync(FULL, b.ox, own);
+      ob.oy = __shfl_sync(FULL, b.oy, own);
+      ob.oz = __shfl_sync(FULL, b.oz, own);
+      float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (t < total) {
+        const int ks = o_k + (t - o_off);
+        const float tt = fmaf((float)ks + 0.5f, f.dt, o_t0);
+        const Cell c = make_cell(f, fmaf(tt, dvx, ovx), fmaf(tt, dvy, ovy), fmaf(tt, dvz, ovz));
+        const float4 tc = tf1d(f, sample_cell<T, SAMPLER_SW>(f, ob, c.x, c.y, c.z, c.fx, c.fy, c.fz));
+        float al = tc.w;
+        if (f.opacity_exp != 1.f) al = 1.f - __powf(1.f - al, f.opacity_exp);
+        res = make_float4(tc.x, tc.y, tc.z, al);
+      }
+      // the owners take their tasks of this round back, in sample order
+      const int first = max(off - base, 0), last = min(off + n - base, 32);
+      const int cnt = last > first ? last - first : 0;
+      const int maxcnt = __reduce_max_sync(FULL, (unsigned)cnt);
+      for (int j = 0; j < maxcnt; ++j) {
+        const int src = (first + j) & 31;
+        const float cx = __shfl_sync(FULL, res.x, src), cy = __shfl_sync(FULL, res.y, src),
+                    cz = __shfl_sync(FULL, res.z, src), al = __shfl_sync(FULL, res.w, src);
+        if (j < cnt && !stop) {
+          ++nsamp;
+          const float w = (1.f - acc.A) * al;
+          acc.C0 = fmaf(w, cx, acc.C0);
+          acc.C1 = fmaf(w, cy, acc.C1);
+          acc.C2 = fmaf(w, cz, acc.C2);
+          acc.A += w;
+          if (acc.A >= f.ert) stop = true;
+        }
+      }
+    }
+    if (active) {
+      if (stop) active = false;
+      else k += n;
+    }
+  }
+  return make_float4(acc.C0, acc.C1, acc.C2, acc.A);
+}
+
 // What lies behind the volume: the background (adds no opacity), or an
 // opaque bounding-box line.
 __device__ __forceinline__ float4 behind(const FrameDesc& f, float4 c, unsigned line, int py) {
@@ -866,7 +1083,25 @@ __device__ __forceinline__ void render_tile_u(const FrameDesc& f, const FrameDes
   const int px = tx * tw + (lane & (tw - 1));
   const int py = ty * (32 / tw) + (lane / tw);
   unsigned nsamp = 0;
-  if (px < f.width && py < f.height) {
+  if constexpr (SPS >= 4) {
+    // warp-shared sampling: every lane of the warp takes part
+    const bool in = px < f.width && py < f.height;
+    RaySetup r{};  // lanes without a pixel still hand their (zero) ray to the shuffles
+    r.hit = false;
+    if (in) setup_ray(fv, px, py, r);
+    const float4 c = behind(f, march_1d_shared<T, SPS>(f, r, in, nsamp, vidx), NO_LINE, py);
+    if (in) {
+      const size_t o = (size_t)py * f.width + px;
+      float4* of = fv.out_f32;
+      uchar4* o8 = fv.out_rgba8;
+      if (of) of[o] = c;
+      if (o8)
+        o8[o] = make_uchar4((unsigned char)__float2uint_rn(__saturatef(c.x) * 255.f),
+                            (unsigned char)__float2uint_rn(__saturatef(c.y) * 255.f),
+                            (unsigned char)__float2uint_rn(__saturatef(c.z) * 255.f),
+                            (unsigned char)__float2uint_rn(__saturatef(c.w) * 255.f));
+    }
+  } else if (px < f.width && py < f.height) {
     RaySetup r;
     setup_ray(fv, px, py, r);
     float4 c = behind(f, march<T, MODE, SAMPLER, false, SPS>(f, r, nsamp, vidx, fv.light_to), NO_LINE, py);
@@ -895,9 +1130,10 @@ constexpr int RENDER_THREADS = 128;
 // 8 voxels and 12 tap offsets for its gradient); the isosurface path 8 (64).
 template <int MODE>
 constexpr int uniform_ctas_per_sm() { return (MODE == MODE_1D || MODE == MODE_MIP) ? 10 : (MODE == MODE_2D ? 6 : 8); }
-// Two samples per step keep two samples' voxels live: 8 CTAs/SM (64 registers).
+// Two samples per step keep two samples' voxels live, and warp-shared
+// sampling (4, 8) keeps a task's owner data live: 8 CTAs/SM (64 registers).
 template <int MODE, int SPS>
-constexpr int uniform_ctas_per_sm_sps() { return SPS == 2 ? 8 : uniform_ctas_per_sm<MODE>(); }
+constexpr int uniform_ctas_per_sm_sps() { return SPS >= 2 ? 8 : uniform_ctas_per_sm<MODE>(); }
 
 template <typename T, int MODE, int SAMPLER>
 __global__ void __launch_bounds__(RENDER_THREADS, uniform_ctas_per_sm<MODE>())
@@ -1619,30 +1855,39 @@ cudaError_t launch_render_persistent_typed(int dtype, int mode, int sampler, con
   GBVR_DISPATCH(persistent_t, dtype, mode, sampler, frames, nframes, prefix, counter, grid, s);
 }
 
-template <typename T>
-static cudaError_t persistent_u_sps2_t(const FrameDesc& shared, const FrameDesc* frames, int nframes, const int* prefix,
-                                       int* counter, int grid, cudaStream_t s) {
-  k_render_persistent_u<T, MODE_1D, SAMPLER_SW, 2><<<grid, RENDER_THREADS, 0, s>>>(shared, frames, nframes, prefix,
-                                                                                    counter);
+template <typename T, int SPS>
+static cudaError_t persistent_u_sps_t(const FrameDesc& shared, const FrameDesc* frames, int nframes, const int* prefix,
+                                      int* counter, int grid, cudaStream_t s) {
+  k_render_persistent_u<T, MODE_1D, SAMPLER_SW, SPS><<<grid, RENDER_THREADS, 0, s>>>(shared, frames, nframes, prefix,
+                                                                                      counter);
   return cudaGetLastError();
+}
+
+template <int SPS>
+static cudaError_t persistent_u_sps(int dtype, const FrameDesc& shared, const FrameDesc* frames, int nframes,
+                                    const int* prefix, int* counter, int grid, cudaStream_t s) {
+  if (dtype == DT_U8) return persistent_u_sps_t<uint8_t, SPS>(shared, frames, nframes, prefix, counter, grid, s);
+  if (dtype == DT_U16) return persistent_u_sps_t<uint16_t, SPS>(shared, frames, nframes, prefix, counter, grid, s);
+  return persistent_u_sps_t<float, SPS>(shared, frames, nframes, prefix, counter, grid, s);
 }
 
 cudaError_t launch_render_persistent_uniform(int dtype, int mode, int sampler, const FrameDesc& shared,
                                              const FrameDesc* frames, int nframes, const int* prefix, int* counter,
                                              int grid, cudaStream_t s, int sps) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
-  if (sps == 2 && mode == MODE_1D && sampler == SAMPLER_SW) {
-    if (dtype == DT_U8) return persistent_u_sps2_t<uint8_t>(shared, frames, nframes, prefix, counter, grid, s);
-    if (dtype == DT_U16) return persistent_u_sps2_t<uint16_t>(shared, frames, nframes, prefix, counter, grid, s);
-    return persistent_u_sps2_t<float>(shared, frames, nframes, prefix, counter, grid, s);
+  if (mode == MODE_1D && sampler == SAMPLER_SW) {
+    if (sps == 2) return persistent_u_sps<2>(dtype, shared, frames, nframes, prefix, counter, grid, s);
+    if (sps == 4) return persistent_u_sps<4>(dtype, shared, frames, nframes, prefix, counter, grid, s);
+    if (sps == 8) return persistent_u_sps<8>(dtype, shared, frames, nframes, prefix, counter, grid, s);
   }
   GBVR_DISPATCH(persistent_u_t, dtype, mode, sampler, shared, frames, nframes, prefix, counter, grid, s);
 }
 
-// Resident CTAs per SM of the batch kernel's two-samples-per-step variant.
+// Resident CTAs per SM of the batch kernel's variants with 2, 4 or 8 samples
+// per step (one launch bound: 8 CTAs of 128 threads, 64 registers).
 int persistent_ctas_per_sm_sps2() {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_1D, SAMPLER_SW, 2>,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_persistent_u<uint16_t, MODE_1D, SAMPLER_SW, 4>,
                                                 RENDER_THREADS, 0);
   return per_sm < 1 ? 1 : per_sm;
 }

@@ -400,13 +400,13 @@ class Renderer:
     def setSamplesPerStep(self, sps):
         L.call("gbvr_set_samples_per_step", self._h, sps)
 
-    def autotuneEx(self, views, brick_sizes=(128, 256, 512), samples_per_step=(1, 2)):
+    def autotuneEx(self, views, brick_sizes=(128, 256, 512), samples_per_step=(1, 2, 4, 8)):
         """Launch shape x brick size x samples per step: the fastest stays set."""
         vs = self._views(views)
         p = L.TuneParams()
         for k, b in enumerate(brick_sizes[:4]):
             p.brick_sizes[k] = b
-        for k, v in enumerate(samples_per_step[:2]):
+        for k, v in enumerate(samples_per_step[:4]):
             p.samples_per_step[k] = v
         out = L.TuneResultEx()
         L.call("gbvr_autotune_ex", self._h, vs, len(views), C.byref(p), C.byref(out))

@@ -92,7 +92,10 @@ typedef struct gbvr_brick_params {
                            copies (3x device memory), each view samples the copy
                            whose fastest axis is closest to its screen x axis;
                            4: also a copy in 4x4x4 voxel blocks (2x memory),
-                           sampled by every view */
+                           sampled by every view; 5: the blocks of that copy
+                           also hold their +1 neighbours (5x5x5 voxels in 128
+                           elements, 3x memory), so a trilinear footprint is
+                           read at fixed offsets from one address */
   int32_t compression;  /* out-of-core host store: 0 raw, 1 zlib, 3 LZ4 (the UVF codec ids
                            CT_ZLIB and CT_LZ4, UVFReader/BlockInfo.h:60-93; zlib is the
                            converter's default, CmdLineConverter/main.cpp:146): 16 KiB chunks
@@ -276,10 +279,14 @@ typedef struct gbvr_tune_result {
 int gbvr_autotune(gbvr_renderer* r, const gbvr_view* views, int n, gbvr_tune_result* out);
 
 /* Samples per step of the batched kernel's inner loop (1D TF, software
- * sampler): 1 (default) or 2.  With 2 each step evaluates two consecutive
- * samples -- both samples' voxel and TF loads in flight together -- and
- * composites them in order, stopping after the first if it ends the ray:
- * the same pixels either way.  No counterpart in the reference. */
+ * sampler): 1 (default), 2, 4 or 8.  With 2 each lane evaluates two
+ * consecutive samples of its ray per step -- both samples' voxel and TF loads
+ * in flight together.  With 4 or 8 the warp shares the work: each lane still
+ * walks its own ray and composites its own samples, but the pending samples of
+ * all the warp's rays (up to 4 or 8 per ray per step) are evaluated by the
+ * whole warp, 32 at a time.  Every setting composites the same samples in the
+ * same order and stops at the same one: the same pixels.  No counterpart in
+ * the reference. */
 int gbvr_set_samples_per_step(gbvr_renderer* r, int sps);
 
 /* Extended autotuner: the launch-shape sweep of gbvr_autotune (tile width x
@@ -292,8 +299,7 @@ int gbvr_set_samples_per_step(gbvr_renderer* r, int sps);
  * each list; an empty list keeps the current setting.  In-core datasets only. */
 typedef struct gbvr_tune_params {
   int32_t brick_sizes[4];
-  int32_t samples_per_step[2];
-  int32_t reserved[2];
+  int32_t samples_per_step[4];
 } gbvr_tune_params;
 
 typedef struct gbvr_tune_result_ex {

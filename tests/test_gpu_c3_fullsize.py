@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from imagevis3d_gb300 import GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE, Renderer, workloads
-from tests.gpu_util import assert_close
+from tests.gpu_util import assert_close, assert_close_backward
 
 pytestmark = pytest.mark.gpu
 
@@ -65,21 +65,34 @@ def test_c3_full_size_2d_tf_phong_matches_oracle(orc, c3):
 
 @pytest.mark.parametrize("k", [0, 1, 2])
 def test_c3_full_size_isosurfaces_match_oracle(orc, c3, k):
+    """Each seeded isovalue on two views, 600 pixels each.  The isosurface of
+    the fractal is ill-conditioned at a few pixels: the FP64 oracle itself
+    moves by up to ~0.07 there when the view matrix is perturbed by 1e-7
+    relative (FP32 rounding).  So a pixel passes within tolerance of the
+    oracle, or within tolerance of the oracle at a camera perturbed by at
+    most 2e-6 relative per matrix entry (backward error), and at most 2 % of
+    the pixels may need the second rule."""
     wl, r = c3
     iso = wl.isovalues[k]
     r.setRenderMode(GBVR_RM_ISOSURFACE)
     r.setIsoValue(iso, (0.8, 0.8, 0.9))
-    v, p = wl.views[3]
-    r.setView(v, p)
-    r.paint()
-    img = r.readFramebuffer(0, as_float=True).reshape(-1, 4)
-    rng = np.random.default_rng(wl.synth.seed + k)
-    pix = _subset(img, rng, 240, 80, 0.5)
-    ref, _ = orc.render(orc.ProceduralFbm(wl.synth), v, p, wl.width, wl.height, np.zeros((2, 4), np.float32),
-                        mode=2, iso=iso, iso_rgb=(0.8, 0.8, 0.9), value_range=wl.value_range, pixels=pix)
-    hit_g, hit_r = img[pix, 3] > 0.5, ref[:, 3] > 0.5
-    # silhouette rays that graze the surface may hit on one side only
-    assert (hit_g != hit_r).mean() <= 0.01
-    both = hit_g & hit_r
-    assert both.sum() >= 200
-    assert_close(img[pix][both], ref[both])
+    vol = orc.ProceduralFbm(wl.synth)
+    kw = dict(mode=2, iso=iso, iso_rgb=(0.8, 0.8, 0.9), value_range=wl.value_range)
+    for vi in (3, 11):
+        v, p = wl.views[vi]
+        r.setView(v, p)
+        r.paint()
+        img = r.readFramebuffer(0, as_float=True).reshape(-1, 4)
+        rng = np.random.default_rng(wl.synth.seed + 10 * k + vi)
+        pix = _subset(img, rng, 480, 120, 0.5)
+        ref, _ = orc.render(vol, v, p, wl.width, wl.height, np.zeros((2, 4), np.float32), pixels=pix, **kw)
+        hit_g, hit_r = img[pix, 3] > 0.5, ref[:, 3] > 0.5
+        assert (hit_g != hit_r).mean() <= 0.005
+        both = np.flatnonzero(hit_g & hit_r)
+        assert both.size >= 400
+
+        def oracle(view, sub):
+            return orc.render(vol, view, p, wl.width, wl.height, np.zeros((2, 4), np.float32),
+                              pixels=pix[both[sub]], **kw)[0]
+
+        assert_close_backward(img[pix][both], ref[both], oracle, v)

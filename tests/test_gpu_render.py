@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from imagevis3d_gb300 import (GBVR_LINEAR, GBVR_NEAREST, GBVR_RM_1DTRANS, GBVR_RM_2DTRANS,
-                              GBVR_RM_ISOSURFACE, GBVR_SAMPLER_SW, GBVR_SAMPLER_TEX, GbvrError,
+                              GBVR_RM_ISOSURFACE, GBVR_RM_MIP, GBVR_SAMPLER_SW, GBVR_SAMPLER_TEX, GbvrError,
                               Renderer, orbit_camera, synth_params, workloads)
 from tests.gpu_util import assert_close
 
@@ -276,7 +276,7 @@ def test_layout_copies_and_launch_shapes_do_not_change_pixels(multibrick):
     views = workloads.orbit_views(4, 96, 80, elevation=35.0, start=10.0)
     views.append(orbit_camera(0.0, 89.0, 2.5 * workloads.DIAG, 45.0, 96, 80))  # looking down y
     imgs = {}
-    for layouts in (1, 3, 4):
+    for layouts in (1, 3, 4, 5):
         with Renderer(float_fb=True) as r:
             r.loadVolume(vol, brick_size=64, overlap=2, layouts=layouts)
             r.resize((96, 80))
@@ -297,6 +297,35 @@ def test_layout_copies_and_launch_shapes_do_not_change_pixels(multibrick):
     for key, got in imgs.items():
         for i in range(len(views)):
             assert np.array_equal(got[i], ref[i]), (key, i)
+
+
+@pytest.mark.parametrize("mode", [GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE, GBVR_RM_MIP])
+@pytest.mark.parametrize("interp", [True, False])
+def test_overlapped_blocks_give_the_same_pixels(multibrick, mode, interp):
+    """The copy in 4^3 blocks that hold their +1 neighbours (layouts 5) reads
+    the same voxels as the x-fastest copy in every mode, with trilinear and
+    nearest sampling: the same pixels bit for bit."""
+    vol, _, tf = multibrick
+    views = workloads.orbit_views(3, 112, 96, elevation=25.0, start=40.0)
+    out = {}
+    for layouts in (1, 5):
+        with Renderer(float_fb=True) as r:
+            r.loadVolume(vol, brick_size=64, overlap=2, layouts=layouts)
+            r.resize((112, 96))
+            r.set1DTrans(tf)
+            r.setValueRange(0.0, 4095.0)
+            r.setSampleRateModifier(1.5)
+            r.setInterpolant(GBVR_LINEAR if interp else GBVR_NEAREST)
+            r.setRenderMode(mode)
+            if mode == GBVR_RM_2DTRANS:
+                r.set2DTrans(workloads.tf2d_seeded(256, 64, 5, widgets=3), r.datasetInfo()["hist2d_max_grad"])
+            if mode == GBVR_RM_ISOSURFACE:
+                r.setIsoValue(1500.0, (0.8, 0.8, 0.9))
+            r.paintBatch(views)
+            out[layouts] = [r.readFramebuffer(i, as_float=True) for i in range(len(views))]
+    assert max(float(a[..., 3].max()) for a in out[1]) > 0.2
+    for a, b in zip(out[1], out[5]):
+        assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("mode", [GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE])

@@ -161,6 +161,7 @@ SIGNATURES = {
     "gbvr_get_hist1d": [P, U64P, SZ],
     "gbvr_get_hist2d": [P, U64P, SZ, SZ, FP],
     "gbvr_get_brick_minmax": [P, I, C.POINTER(D), SZ],
+    "gbvr_get_cell_minmax": [P, I, C.POINTER(C.c_float), SZ, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "gbvr_get_brick": [P, I, C.POINTER(C.c_int32), P, SZ, I64P, I64P],
     "gbvr_write_uvf": [P, CP],
     "gbvr_resize": [P, I, I],

@@ -442,8 +442,9 @@ struct PhaseTimer {
     return e == cudaSuccess ? cudaEventRecord(a, s) : e;
   }
   cudaError_t stop(cudaStream_t s) { return cudaEventRecord(b, s); }
-  // after a synchronisation of the stream
+  // after a synchronisation of the stream (a phase never started adds 0)
   cudaError_t add() {
+    if (!a) return cudaSuccess;
     float ms = 0.f;
     cudaError_t e = cudaEventElapsedTime(&ms, a, b);
     if (e == cudaSuccess) *acc += ms;
@@ -500,11 +501,16 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
   // layout copies: 1 = x-fastest only; 3 = + y- and z-fastest; 4 = + 4^3-blocked;
   // 5 = + 4^3 blocks that also hold their +1 neighbours (5^3 voxels in 128
   // elements: twice the room of the blocked copy, which each brick's share of
-  // the cursor already rounds to 4^3 blocks)
-  ds.layouts = (bp && (bp->layouts == 3 || bp->layouts == 4 || bp->layouts == 5)) ? bp->layouts : 1;
+  // the cursor already rounds to 4^3 blocks); 6 = + both blocked copies
+  ds.layouts = (bp && bp->layouts >= 3 && bp->layouts <= 6) ? bp->layouts : 1;
   ds.copy_stride = cursor;
-  const int ncopies = ds.layouts == 5 ? 3 : ds.layouts == 4 ? 2 : ds.layouts;
+  const int ncopies = ds.layouts == 6 ? 4 : ds.layouts == 5 ? 3 : ds.layouts == 4 ? 2 : ds.layouts;
   CUDA_TRY(ds.pool.alloc(cursor * es * ncopies));
+  // the gather reduces each brick's min/max into these
+  for (BrickInfo& b : ds.bricks) {
+    b.vmin = INFINITY;
+    b.vmax = -INFINITY;
+  }
   CUDA_TRY(ds.d_bricks.alloc(sizeof(BrickInfo) * ds.bricks.size()));
   CUDA_TRY(cudaMemcpyAsync(ds.d_bricks.p, ds.bricks.data(), sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyHostToDevice, s));
   for (size_t l = 0; l < ld.size(); ++l) {
@@ -537,18 +543,29 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
       const BrickInfo& b = ds.bricks[L.brick_base + i];
       stored += (uint64_t)b.sx * b.sy * b.sz * es;
     }
-    for (int c = 0; c < (ds.layouts >= 4 ? 2 : ds.layouts); ++c) {
-      const int perm = c == 1 && ds.layouts >= 4 ? ds.layouts - 1 : c;
+    // the x-fastest copy (0), the blocked copy (1) when there is one, and
+    // the bricks' min/max in one pass over the level
+    int max_sz = 1;
+    for (int i = 0; i < L.nbricks; ++i) max_sz = std::max(max_sz, ds.bricks[L.brick_base + i].sz);
+    const bool blocked = ds.layouts == 4 || ds.layouts == 6;
+    CUDA_TRY(launch_gather_fused(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks, max_sz,
+                                 ds.pool.p, blocked ? (char*)ds.pool.p + (size_t)cursor * es : nullptr, s));
+    bs.bricks_bytes += level_bytes(l) + stored * (blocked ? 2 : 1);
+    // the other copies: (copy, layout) 1 and 2 y- and z-fastest, 4
+    // overlapped blocks (two copies' room)
+    std::vector<std::pair<int, int>> copies;
+    if (ds.layouts == 3) copies = {{1, 1}, {2, 2}};
+    else if (ds.layouts == 5) copies = {{1, 4}};
+    else if (ds.layouts == 6) copies = {{2, 4}};
+    for (const auto& cp : copies) {
       CUDA_TRY(launch_gather_bricks(lv[l]->p, dtype, d, ds.d_bricks.as<BrickInfo>() + L.brick_base, L.nbricks,
-                                    (char*)ds.pool.p + (size_t)c * cursor * es, perm, s));
-      bs.bricks_bytes += level_bytes(l) + stored;
+                                    (char*)ds.pool.p + (size_t)cp.first * cursor * es, cp.second, s));
+      bs.bricks_bytes += level_bytes(l) + stored * (cp.second == 4 ? 2 : 1);
     }
   }
   CUDA_TRY(t_bricks.stop(s));
-  CUDA_TRY(t_mm.start(s));
-  CUDA_TRY(launch_brick_minmax(ds.pool.p, dtype, ds.d_bricks.as<BrickInfo>(), (int)ds.bricks.size(), s));
-  CUDA_TRY(t_mm.stop(s));
-  bs.minmax_bytes = ds.stored_bytes;
+  // per-brick min/max: reduced by the gather above
+  bs.minmax_bytes = 0;
   CUDA_TRY(cudaMemcpyAsync(ds.bricks.data(), ds.d_bricks.p, sizeof(BrickInfo) * ds.bricks.size(), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   ds.gmin = INFINITY;
@@ -612,7 +629,7 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
                    bs.hist2d_bytes;
   bs.level0_bytes = level_bytes(0);
   bs.lod_count = (int32_t)ld.size();
-  bs.layout_copies = ds.layouts >= 4 ? 2 : ds.layouts;
+  bs.layout_copies = ds.layouts == 6 ? 3 : ds.layouts >= 4 ? 2 : ds.layouts;
   if (bp && bp->build_texture) TRY(build_textures(ds, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   ds.loaded = true;
@@ -1129,7 +1146,11 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
   // layout copy: the axis whose voxel-space extent along screen x is largest
   // (row 0 of the view matrix is the camera's right vector in world space)
   f.perm = 0;
-  if (ds.layouts >= 4) {
+  if (ds.layouts == 6) {
+    // both blocked copies: isosurfaces sample the overlapped blocks (a cell's
+    // voxels at fixed offsets), the other modes the compact 4^3 blocks
+    f.perm = p.mode == GBVR_RM_ISOSURFACE ? 4 : 3;
+  } else if (ds.layouts >= 4) {
     f.perm = ds.layouts - 1;  // blocked copy, independent of the view direction
   } else if (ds.layouts == 3) {
     double best = -1;
@@ -1138,7 +1159,7 @@ void fill_frame(FrameDesc& f, const Dataset& ds, const FrameParams& p) {
       if (w > best) { best = w; f.perm = a; }
     }
   }
-  f.copy_off = (unsigned long long)(f.perm >= 3 ? 1 : f.perm) * ds.copy_stride;
+  f.copy_off = (unsigned long long)(f.perm == 4 && ds.layouts == 6 ? 2 : f.perm >= 3 ? 1 : f.perm) * ds.copy_stride;
 }
 
 }  // namespace
@@ -2013,7 +2034,12 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
 
 int ooc_streams(gbvr_renderer* r) {
   if (!r->copy_stream) {
-    CUDA_TRY(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
+    // the copies and decodes of frame i + 1 run at the highest priority, so
+    // their CTAs are dispatched as frame i's render CTAs retire instead of
+    // after the whole render
+    int least = 0, greatest = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CUDA_TRY(cudaStreamCreateWithPriority(&r->copy_stream, cudaStreamNonBlocking, greatest));
     for (int k = 0; k < 2; ++k) {
       CUDA_TRY(cudaEventCreate(&r->ev_c0[k]));
       CUDA_TRY(cudaEventCreate(&r->ev_c1[k]));
@@ -2782,6 +2808,23 @@ int gbvr_get_brick_minmax(gbvr_renderer* r, int lod, double* out, size_t nbricks
     out[2 * i] = r->ds.bricks[L.brick_base + i].vmin;
     out[2 * i + 1] = r->ds.bricks[L.brick_base + i].vmax;
   }
+  return GBVR_OK;
+  GBVR_ABI_CATCH
+}
+
+int gbvr_get_cell_minmax(gbvr_renderer* r, int lod, float* out, size_t ncells, int32_t nc[3], int32_t* cell_edge) {
+  GBVR_ABI_TRY
+  TRY(check_loaded(r));
+  TRY(settle_async(r));
+  if (lod < 0 || lod >= (int)r->ds.levels.size()) return fail(GBVR_EINVAL, "bad lod");
+  const Level& L = r->ds.levels[lod];
+  const size_t n = (size_t)L.nc[0] * L.nc[1] * L.nc[2];
+  if (nc)
+    for (int a = 0; a < 3; ++a) nc[a] = L.nc[a];
+  if (cell_edge) *cell_edge = 1 << L.cell_shift;
+  if (!out) return GBVR_OK;
+  if (ncells < n || !L.cells) return fail(GBVR_EINVAL, "buffer too small");
+  CUDA_TRY(cudaMemcpy(out, L.cells->p, n * sizeof(float2), cudaMemcpyDeviceToHost));
   return GBVR_OK;
   GBVR_ABI_CATCH
 }

@@ -277,6 +277,12 @@ cudaError_t launch_gather_bricks_window(const void* level, int dtype, const long
                                         cudaStream_t s);
 cudaError_t launch_brick_minmax(const void* pool, int dtype, BrickInfo* bricks_dev, int nbricks,
                                 cudaStream_t s);
+// In one pass over a whole level: its bricks into the x-fastest copy (pool0),
+// into the 4x4x4-blocked copy when pool1 is not null (the same offsets), and
+// each brick's vmin / vmax (which must be +inf / -inf on entry).  max_sz: the
+// largest stored z extent of the bricks.
+cudaError_t launch_gather_fused(const void* level, int dtype, const long long dims[3], BrickInfo* bricks_dev,
+                                int nbricks, int max_sz, void* pool0, void* pool1, cudaStream_t s);
 // Macro-cell min/max of a flat level: cell c covers sample cells [c M, c M + M)
 // per axis, whose trilinear footprints span voxels [c M, c M + M]; the range
 // is taken over [c M - 1, c M + M + 1] (clamped) so that a sample rounded

@@ -8,6 +8,7 @@
 // integer-exact (or a fixed float32 operation order with round-to-nearest
 // intrinsics), so results are bit-identical to the CPU restatement.
 #include <algorithm>
+#include <type_traits>
 #include <cstdint>
 
 #include "gbvr_internal.h"
@@ -288,30 +289,45 @@ __global__ void k_gather(const T* __restrict__ level, long long X, long long Y, 
 // block repeats voxel 0 of the next one, so every trilinear footprint of a
 // cell in the block lies in the block; the footprint of a cell inside the
 // stored box never reaches past it, and slots past the box hold its edge.
-// One thread per destination element, consecutive threads along x.
+// One warp per destination block (its 128 elements, 4 per lane, written in
+// order); a lane's slots, and so their offsets inside a block, are the same
+// for every block.
 template <typename T>
-__global__ void k_gather_ov(const T* __restrict__ level, long long X, long long Y, long long Z, long long vz0,
-                            const BrickInfo* __restrict__ bricks, T* __restrict__ pool) {
+__global__ void __launch_bounds__(256) k_gather_ov(const T* __restrict__ level, long long X, long long Y, long long Z,
+                                                   long long vz0, const BrickInfo* __restrict__ bricks,
+                                                   T* __restrict__ pool) {
   const BrickInfo b = bricks[blockIdx.y];
-  const long long nbx = (b.sx + 3) >> 2, nby = (b.sy + 3) >> 2, nbz = (b.sz + 3) >> 2;
-  const long long n = nbx * nby * nbz * 128;
+  const int nbx = (b.sx + 3) >> 2, nby = (b.sy + 3) >> 2, nbz = (b.sz + 3) >> 2;
+  const int nblk = nbx * nby * nbz;
   T* dst = pool + 2 * (long long)b.offset;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-    const int slot = (int)(e & 127);
-    if (slot >= 125) {
-      dst[e] = T(0);
-      continue;
+  const int lane = threadIdx.x & 31;
+  int si[4], sj[4], sk[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int slot = lane + 32 * q;
+    si[q] = slot % 5;
+    sj[q] = (slot / 5) % 5;
+    sk[q] = slot / 25;  // 5 for the 3 padding slots
+  }
+  const int warps = (int)(blockDim.x >> 5);
+  for (int blk = (int)blockIdx.x * warps + (int)(threadIdx.x >> 5); blk < nblk; blk += (int)gridDim.x * warps) {
+    const int bx = blk % nbx, t = blk / nbx, by = t % nby, bz = t / nby;
+    T* d = dst + ((long long)blk << 7);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int slot = lane + 32 * q;
+      T val = T(0);
+      if (slot < 125) {
+        // ghosts outside the level replicate its edge voxels
+        const int xs = min(4 * bx + si[q], b.sx - 1), ys = min(4 * by + sj[q], b.sy - 1),
+                  zs = min(4 * bz + sk[q], b.sz - 1);
+        const long long x = min(max((long long)b.ox + xs, 0LL), X - 1);
+        const long long y = min(max((long long)b.oy + ys, 0LL), Y - 1);
+        const long long z = min(max((long long)b.oz + zs, 0LL), Z - 1);
+        val = __ldg(level + ((z - vz0) * Y + y) * X + x);
+      }
+      d[slot] = val;
     }
-    const long long blk = e >> 7;
-    const long long bx = blk % nbx, by = (blk / nbx) % nby, bz = blk / (nbx * nby);
-    const long long xs = min(4 * bx + slot % 5, (long long)b.sx - 1);
-    const long long ys = min(4 * by + (slot / 5) % 5, (long long)b.sy - 1);
-    const long long zs = min(4 * bz + slot / 25, (long long)b.sz - 1);
-    // ghosts outside the level replicate its edge voxels
-    const long long x = min(max((long long)b.ox + xs, 0LL), X - 1);
-    const long long y = min(max((long long)b.oy + ys, 0LL), Y - 1);
-    const long long z = min(max((long long)b.oz + zs, 0LL), Z - 1);
-    dst[e] = __ldg(level + ((z - vz0) * Y + y) * X + x);
   }
 }
 
@@ -384,6 +400,101 @@ cudaError_t launch_gather_bricks_window(const void* level, int dtype, const long
 cudaError_t launch_gather_bricks(const void* level, int dtype, const long long dims[3], const BrickInfo* bricks_dev,
                                  int nbricks, void* pool, int perm, cudaStream_t s) {
   return launch_gather_bricks_window(level, dtype, dims, 0, bricks_dev, nbricks, pool, perm, s);
+}
+
+// ---------------------------------------------------------------------------
+// Brick gather of the in-core build in one pass over the level: every brick's
+// stored box into the x-fastest copy and, with `blocked`, into the 4x4x4-
+// blocked copy, and the brick's min/max over those voxels (ghosts included),
+// reduced per CTA and combined with float atomics.  A CTA of 8 warps takes
+// z-slices of one brick; a warp takes rows, its lanes consecutive x, so the
+// level is read and the x-fastest copy written in whole rows.  vmin / vmax of
+// every brick must be +inf / -inf on entry.
+// ---------------------------------------------------------------------------
+// Float min / max through integer atomics: non-negative floats order as
+// their bit patterns read as signed ints, negative floats in reverse as
+// unsigned ints.
+__device__ __forceinline__ void atomic_min_float(float* a, float v) {
+  if (v >= 0.f) atomicMin(reinterpret_cast<int*>(a), __float_as_int(v));
+  else atomicMax(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_float(float* a, float v) {
+  if (v >= 0.f) atomicMax(reinterpret_cast<int*>(a), __float_as_int(v));
+  else atomicMin(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+
+constexpr int GATHER_WARPS = 8;
+
+template <typename T, bool BLOCKED>
+__global__ void __launch_bounds__(32 * GATHER_WARPS) k_gather_fused(const T* __restrict__ level, long long X,
+                                                                    long long Y, long long Z,
+                                                                    BrickInfo* __restrict__ bricks,
+                                                                    T* __restrict__ pool0, T* __restrict__ pool1) {
+  BrickInfo* bp = bricks + blockIdx.y;
+  const int ox = bp->ox, oy = bp->oy, oz = bp->oz, sx = bp->sx, sy = bp->sy, sz = bp->sz;
+  const long long off = (long long)bp->offset;
+  const int nbx = (sx + 3) >> 2, nby = (sy + 3) >> 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float mn = INFINITY, mx = -INFINITY;
+  for (int zs = blockIdx.x; zs < sz; zs += gridDim.x) {
+    const long long z = min(max((long long)oz + zs, 0LL), Z - 1);
+    for (int r = warp; r < sy; r += GATHER_WARPS) {
+      // ghosts outside the level replicate its edge voxels
+      const long long y = min(max((long long)oy + r, 0LL), Y - 1);
+      const T* src = level + (z * Y + y) * X;
+      T* d0 = pool0 + off + ((long long)zs * sy + r) * sx;
+      T* d1 = BLOCKED ? pool1 + off + ((((long long)(zs >> 2) * nby + (r >> 2)) * nbx) << 6) + ((zs & 3) << 4) +
+                            ((r & 3) << 2)
+                      : nullptr;
+#pragma unroll 4
+      for (int xs = lane; xs < sx; xs += 32) {
+        const long long x = min(max((long long)ox + xs, 0LL), X - 1);
+        const T v = __ldg(src + x);
+        d0[xs] = v;
+        if (BLOCKED) d1[((xs >> 2) << 6) + (xs & 3)] = v;
+        const float f = (float)v;
+        mn = fminf(mn, f);
+        mx = fmaxf(mx, f);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  __shared__ float smn[GATHER_WARPS], smx[GATHER_WARPS];
+  if (lane == 0) { smn[warp] = mn; smx[warp] = mx; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < GATHER_WARPS; ++w) {
+      mn = fminf(mn, smn[w]);
+      mx = fmaxf(mx, smx[w]);
+    }
+    if (mn <= mx) {  // the CTA saw at least one voxel
+      atomic_min_float(&bp->vmin, mn);
+      atomic_max_float(&bp->vmax, mx);
+    }
+  }
+}
+
+cudaError_t launch_gather_fused(const void* level, int dtype, const long long dims[3], BrickInfo* bricks_dev,
+                                int nbricks, int max_sz, void* pool0, void* pool1, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
+  if (nbricks <= 0) return cudaSuccess;
+  dim3 grid((unsigned)std::max(1, std::min(max_sz, 64)), (unsigned)nbricks);
+  const int threads = 32 * GATHER_WARPS;
+#define GBVR_GATHER(TT)                                                                                         \
+  if (pool1)                                                                                                     \
+    k_gather_fused<TT, true><<<grid, threads, 0, s>>>((const TT*)level, dims[0], dims[1], dims[2], bricks_dev,  \
+                                                      (TT*)pool0, (TT*)pool1);                                   \
+  else                                                                                                           \
+    k_gather_fused<TT, false><<<grid, threads, 0, s>>>((const TT*)level, dims[0], dims[1], dims[2], bricks_dev, \
+                                                       (TT*)pool0, nullptr);
+  if (dtype == DT_U8) { GBVR_GATHER(uint8_t) }
+  else if (dtype == DT_U16) { GBVR_GATHER(uint16_t) }
+  else { GBVR_GATHER(float) }
+#undef GBVR_GATHER
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -464,11 +575,127 @@ __global__ void k_cell_minmax(const T* __restrict__ v, long long X, long long Y,
   }
 }
 
+// The same ranges for 4^3 cells (shift 2) from a shared-memory tile: a CTA
+// takes CX x 4 x 2 cells (CX = 15 for 8- and 16-bit voxels, 7 for float, so
+// a tile row of 4 CX + 3 voxels fills whole warps), loads the voxels their
+// ranges cover row by row (edge-replicated where the level ends, which
+// leaves every range as the clamped one), and reduces along x (7 voxels per
+// cell and row), then y, then z, keeping the partial minima and maxima as
+// voxel values.  Each voxel is read from memory about 1.6 times instead of
+// 5.4, with one 64-bit row address per row.
+template <typename T> struct CellTile {
+  static constexpr int CX = 15;
+  __device__ static T mn(T a, T b) { return a < b ? a : b; }
+  __device__ static T mx(T a, T b) { return a > b ? a : b; }
+};
+// float: fminf / fmaxf from +inf / -inf, as k_cell_minmax (NaN voxels are
+// passed over)
+template <> struct CellTile<float> {
+  static constexpr int CX = 7;
+  __device__ static float mn(float a, float b) { return fminf(a, b); }
+  __device__ static float mx(float a, float b) { return fmaxf(a, b); }
+};
+constexpr int CT_Y = 4, CT_Z = 2;
+constexpr int CV_Y = 4 * CT_Y + 3, CV_Z = 4 * CT_Z + 3;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_cell_minmax_tiled(const T* __restrict__ v, long long X, long long Y,
+                                                           long long Z, long long vz0, int ncx, int ncy, int cz0,
+                                                           int cz1, int tiles_x, int tiles_y, float2* __restrict__ out) {
+  constexpr int CX = CellTile<T>::CX, VX = 4 * CX + 3;
+  __shared__ T tile[CV_Z][CV_Y][VX];
+  __shared__ T rmn[CV_Z][CV_Y][CX], rmx[CV_Z][CV_Y][CX];
+  __shared__ T qmn[CV_Z][CT_Y][CX], qmx[CV_Z][CT_Y][CX];
+  const int tx = blockIdx.x % tiles_x, ty = (blockIdx.x / tiles_x) % tiles_y, tz = blockIdx.x / (tiles_x * tiles_y);
+  const int cx0 = tx * CX, cy0 = ty * CT_Y, cz0t = cz0 + tz * CT_Z;
+  const long long vx0 = 4LL * cx0 - 1, vy0 = 4LL * cy0 - 1, vzz0 = 4LL * cz0t - 1;
+  // planes the requested layers' ranges cover (the window holds them); a
+  // tile reaching past the last layer reads clamped planes for cells it does
+  // not write
+  const long long zlo = max(4LL * cz0 - 1, 0LL), zhi = min(4LL * cz1 + 1, Z - 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // a row is at most two warp-wide loads (VX <= 64); four rows per step so
+  // that eight loads of a lane are in flight together
+  static_assert(VX <= 64, "a tile row is at most two warps wide");
+  const int xa = (int)min(max(vx0 + lane, 0LL), X - 1), xb = (int)min(max(vx0 + lane + 32, 0LL), X - 1);
+  const bool hb = lane + 32 < VX;
+  constexpr int ROWS = CV_Y * CV_Z;
+#pragma unroll 4
+  for (int row = warp; row < ROWS; row += 8) {
+    const int ly = row % CV_Y, lz = row / CV_Y;
+    const long long y = min(max(vy0 + ly, 0LL), Y - 1), z = min(max(vzz0 + lz, zlo), zhi);
+    const T* src = v + ((z - vz0) * Y + y) * X;
+    const T a = __ldg(src + xa);
+    const T b = hb ? __ldg(src + xb) : T(0);
+    if (lane < VX) tile[lz][ly][lane] = a;
+    if (hb) tile[lz][ly][lane + 32] = b;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < CX * CV_Y * CV_Z; i += blockDim.x) {
+    const int c = i % CX, r = i / CX, ly = r % CV_Y, lz = r / CV_Y;
+    using C = CellTile<T>;
+    T mn = std::is_same<T, float>::value ? T(INFINITY) : tile[lz][ly][4 * c];
+    T mx = std::is_same<T, float>::value ? T(-INFINITY) : mn;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      const T a = tile[lz][ly][4 * c + k];
+      mn = C::mn(mn, a);
+      mx = C::mx(mx, a);
+    }
+    rmn[lz][ly][c] = mn;
+    rmx[lz][ly][c] = mx;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < CX * CT_Y * CV_Z; i += blockDim.x) {
+    const int c = i % CX, r = i / CX, cy = r % CT_Y, lz = r / CT_Y;
+    using C = CellTile<T>;
+    T mn = rmn[lz][4 * cy][c], mx = rmx[lz][4 * cy][c];
+#pragma unroll
+    for (int k = 1; k < 7; ++k) {
+      mn = C::mn(mn, rmn[lz][4 * cy + k][c]);
+      mx = C::mx(mx, rmx[lz][4 * cy + k][c]);
+    }
+    qmn[lz][cy][c] = mn;
+    qmx[lz][cy][c] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x < CX * CT_Y * CT_Z) {
+    const int c = threadIdx.x % CX, r = threadIdx.x / CX, cy = r % CT_Y, cz = r / CT_Y;
+    const int gx = cx0 + c, gy = cy0 + cy, gz = cz0t + cz;
+    if (gx < ncx && gy < ncy && gz < cz1) {
+      using C = CellTile<T>;
+      T mn = qmn[4 * cz][cy][c], mx = qmx[4 * cz][cy][c];
+#pragma unroll
+      for (int k = 1; k < 7; ++k) {
+        mn = C::mn(mn, qmn[4 * cz + k][cy][c]);
+        mx = C::mx(mx, qmx[4 * cz + k][cy][c]);
+      }
+      out[((long long)gz * ncy + gy) * ncx + gx] = make_float2((float)mn, (float)mx);
+    }
+  }
+}
+
 cudaError_t launch_cell_minmax_layers(const void* level, int dtype, const long long dims[3], long long vz0, int sh,
                                       const int nc[3], int cz0, int cz1, float2* out, cudaStream_t s) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   const long long n = (long long)nc[0] * nc[1] * (cz1 - cz0);
   if (n <= 0) return cudaSuccess;
+  if (sh == 2) {
+    const int cx = dtype == DT_F32 ? CellTile<float>::CX : CellTile<uint8_t>::CX;
+    const int tiles_x = (nc[0] + cx - 1) / cx, tiles_y = (nc[1] + CT_Y - 1) / CT_Y,
+              tiles_z = (cz1 - cz0 + CT_Z - 1) / CT_Z;
+    const long long nt = (long long)tiles_x * tiles_y * tiles_z;
+    if (nt < (1LL << 31)) {
+#define GBVR_CELLS(TT)                                                                                         \
+  k_cell_minmax_tiled<TT><<<(unsigned)nt, 256, 0, s>>>((const TT*)level, dims[0], dims[1], dims[2], vz0, nc[0], \
+                                                        nc[1], cz0, cz1, tiles_x, tiles_y, out);
+      if (dtype == DT_U8) { GBVR_CELLS(uint8_t) }
+      else if (dtype == DT_U16) { GBVR_CELLS(uint16_t) }
+      else { GBVR_CELLS(float) }
+#undef GBVR_CELLS
+      return cudaGetLastError();
+    }
+  }
   int threads = 128;
   int blocks = grid_for(n, threads);
   if (dtype == DT_U8)
@@ -797,9 +1024,20 @@ struct Column {
   }
 };
 
-// Pass 1: the largest S.  One thread per 4-voxel column (all of z).
+// Pass 1: the largest S.  One thread per 4-voxel column (all of z), which
+// also records where its column attains its own largest S (the first
+// COL_KEEP voxels as 4 z + j, and how many there are), so that the f64 pass
+// revisits only those voxels.
+constexpr int COL_KEEP = 3;
+struct ColMax {
+  unsigned long long s;
+  unsigned cnt;
+  unsigned pos[COL_KEEP];
+};
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DScratch* sc) {
+__global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DScratch* sc,
+                                                 ColMax* __restrict__ cols) {
   const int cpr = X >> 2;
   const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   using U = typename SumT<T>::U;
@@ -807,13 +1045,31 @@ __global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X,
   if (col < (long long)cpr * Y) {
     const int y = (int)(col / cpr), x0 = 4 * (int)(col - (long long)y * cpr);
     Column<T> c(v, X, Y, Z, x0, y);
+    unsigned cnt = 0, pos[COL_KEEP] = {0u, 0u, 0u};
     for (int z = 0; z < Z; ++z) {
       U S[4];
       c.diffs(z, S);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) smax = S[j] > smax ? S[j] : smax;
+      for (int j = 0; j < 4; ++j) {
+        if (S[j] > smax) {
+          smax = S[j];
+          cnt = 0;
+        }
+        if (S[j] == smax && smax > 0) {
+#pragma unroll
+          for (int q = 0; q < COL_KEEP; ++q)
+            if (cnt == (unsigned)q) pos[q] = 4u * (unsigned)z + (unsigned)j;
+          ++cnt;
+        }
+      }
       c.step(z);
     }
+    ColMax r;
+    r.s = (unsigned long long)smax;
+    r.cnt = cnt;
+#pragma unroll
+    for (int q = 0; q < COL_KEEP; ++q) r.pos[q] = pos[q];
+    cols[col] = r;
   }
   for (int o = 16; o > 0; o >>= 1) {
     const U t = __shfl_xor_sync(0xffffffffu, smax, o);
@@ -822,16 +1078,28 @@ __global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X,
   if ((threadIdx.x & 31) == 0 && smax) atomicMax(&sc->smax, (unsigned long long)smax);
 }
 
-// Pass 1b: the f64 |g| over the voxels attaining Smax.
+// Pass 1b: the f64 |g| over the voxels attaining Smax, one thread per
+// column record: the recorded voxels, or the whole column again when it
+// attains Smax at more voxels than were recorded.
 template <typename T>
 __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X, int Y, int Z, double c,
-                                                  Hist2DScratch* sc) {
+                                                  Hist2DScratch* sc, const ColMax* __restrict__ cols) {
   const unsigned long long smax = sc->smax;
   if (smax == 0) return;
   const int cpr = X >> 2;
   const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= (long long)cpr * Y) return;
+  const ColMax r = cols[col];
+  if (r.s != smax) return;
   const int y = (int)(col / cpr), x0 = 4 * (int)(col - (long long)y * cpr);
+  if (r.cnt <= (unsigned)COL_KEEP) {
+    for (unsigned q = 0; q < r.cnt; ++q) {
+      const int z = (int)(r.pos[q] >> 2), j = (int)(r.pos[q] & 3u);
+      const double g = grad_f64(v, X, Y, Z, x0 + j, y, z, ((long long)z * Y + y) * X + x0 + j, c);
+      atomicMax(&sc->gmax_bits, (unsigned long long)__double_as_longlong(g));
+    }
+    return;
+  }
   Column<T> cl(v, X, Y, Z, x0, y);
   for (int z = 0; z < Z; ++z) {
     typename SumT<T>::U S[4];
@@ -970,6 +1238,10 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
       if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
       cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(Hist2DScratch), s);
       if (e != cudaSuccess) return e;
+      // one record per column (stream-ordered, freed after the passes)
+      ColMax* cols = nullptr;
+      e = cudaMallocAsync(reinterpret_cast<void**>(&cols), (size_t)ncols * sizeof(ColMax), s);
+      if (e != cudaSuccess) return e;
       // shared counters for the gradient rows k < kshared: 2 bytes per bin, ~48 KB
       const int kshared = (int)std::min<long long>(256, (49152 / (2 * nx)) & ~1LL);
       const bool smem = kshared >= 2;
@@ -981,28 +1253,36 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
       const int nxi = (int)nx, mi = (int)merge, Xi = (int)X, Yi = (int)Y, Zi = (int)Z;
       if (dtype == DT_U8) {
         const uint8_t* v = (const uint8_t*)vol;
-        k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch);
-        k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch);
+        k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch, cols);
+        k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch, cols);
         if (smem) {
           e = cudaFuncSetAttribute(k_h2v_bin<uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
-          if (e != cudaSuccess) return e;
+          if (e != cudaSuccess) {
+            cudaFreeAsync(cols, s);
+            return e;
+          }
           k_h2v_bin<uint8_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps, kshared);
         } else {
           k_h2v_bin<uint8_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0, 0);
         }
       } else {
         const uint16_t* v = (const uint16_t*)vol;
-        k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch);
-        k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch);
+        k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch, cols);
+        k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch, cols);
         if (smem) {
           e = cudaFuncSetAttribute(k_h2v_bin<uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
-          if (e != cudaSuccess) return e;
+          if (e != cudaSuccess) {
+            cudaFreeAsync(cols, s);
+            return e;
+          }
           k_h2v_bin<uint16_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps, kshared);
         } else {
           k_h2v_bin<uint16_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0, 0);
         }
       }
-      return cudaGetLastError();
+      e = cudaGetLastError();
+      const cudaError_t ef = cudaFreeAsync(cols, s);
+      return e != cudaSuccess ? e : ef;
     }
   }
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call

@@ -27,6 +27,7 @@
 // k_line_stops, k_render_lines: FP64 coverage, covered rays re-rendered),
 // the ClearView lens pass (k_render_cv), 2D slice views (k_render_slice) and
 // TF classification of bricks and macro-cells.
+#include <type_traits>
 #include <algorithm>
 
 #include "gbvr_internal.h"
@@ -58,6 +59,20 @@ __device__ __forceinline__ float ldv(const uint16_t* p) {
   return __int_as_float(0x4B000000 | (unsigned)__ldg(p)) - 8388608.0f;
 }
 __device__ __forceinline__ float ldv(const float* p) { return __ldg(p); }
+
+// The same voxel with the bias left in (2^23 + value for 8- and 16-bit data,
+// the value itself for float data), and the x lerp of two such voxels: the
+// difference of two biased values is exact, so only the lerp's base needs
+// the bias taken off -- the same result as lerping ldv values, one FADD
+// fewer.
+__device__ __forceinline__ float ldb(const uint8_t* p) { return __int_as_float(0x4B000000 | (unsigned)__ldg(p)); }
+__device__ __forceinline__ float ldb(const uint16_t* p) { return __int_as_float(0x4B000000 | (unsigned)__ldg(p)); }
+__device__ __forceinline__ float ldb(const float* p) { return __ldg(p); }
+template <typename T>
+__device__ __forceinline__ float lerp_b(float fx, float b0, float b1) {
+  if constexpr (std::is_same<T, float>::value) return fmaf(fx, b1 - b0, b0);
+  else return fmaf(fx, b1 - b0, b0 - 8388608.0f);
+}
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
 
@@ -157,12 +172,12 @@ __device__ __forceinline__ float sample_cell(const FrameDesc& f, const BrickView
     }
     const T* p0 = pool + (b.base + (long long)(lz >> 2) * b.s2 + (ly >> 2) * b.s1 + ((lx >> 2) << 7) +
                           ((lz & 3) * 25 + (ly & 3) * 5 + (lx & 3)));
-    float v000 = ldv(p0), v100 = ldv(p0 + 1), v010 = ldv(p0 + 5), v110 = ldv(p0 + 6);
-    float v001 = ldv(p0 + 25), v101 = ldv(p0 + 26), v011 = ldv(p0 + 30), v111 = ldv(p0 + 31);
-    float c00 = fmaf(fx, v100 - v000, v000);
-    float c10 = fmaf(fx, v110 - v010, v010);
-    float c01 = fmaf(fx, v101 - v001, v001);
-    float c11 = fmaf(fx, v111 - v011, v011);
+    const float v000 = ldb(p0), v100 = ldb(p0 + 1), v010 = ldb(p0 + 5), v110 = ldb(p0 + 6);
+    const float v001 = ldb(p0 + 25), v101 = ldb(p0 + 26), v011 = ldb(p0 + 30), v111 = ldb(p0 + 31);
+    const float c00 = lerp_b<T>(fx, v000, v100);
+    const float c10 = lerp_b<T>(fx, v010, v110);
+    const float c01 = lerp_b<T>(fx, v001, v101);
+    const float c11 = lerp_b<T>(fx, v011, v111);
     float c0 = fmaf(fy, c10 - c00, c00);
     float c1 = fmaf(fy, c11 - c01, c01);
     return fmaf(fz, c1 - c0, c0);
@@ -182,12 +197,12 @@ __device__ __forceinline__ float sample_cell(const FrameDesc& f, const BrickView
     const int dy = (ly & 3) == 3 ? b.s1 - 12 : 4;
     const int dz = (lz & 3) == 3 ? b.s2 - 48 : 16;
     const T* p1 = p0 + dz;
-    float v000 = ldv(p0), v100 = ldv(p0 + dx), v010 = ldv(p0 + dy), v110 = ldv(p0 + dy + dx);
-    float v001 = ldv(p1), v101 = ldv(p1 + dx), v011 = ldv(p1 + dy), v111 = ldv(p1 + dy + dx);
-    float c00 = fmaf(fx, v100 - v000, v000);
-    float c10 = fmaf(fx, v110 - v010, v010);
-    float c01 = fmaf(fx, v101 - v001, v001);
-    float c11 = fmaf(fx, v111 - v011, v011);
+    const float v000 = ldb(p0), v100 = ldb(p0 + dx), v010 = ldb(p0 + dy), v110 = ldb(p0 + dy + dx);
+    const float v001 = ldb(p1), v101 = ldb(p1 + dx), v011 = ldb(p1 + dy), v111 = ldb(p1 + dy + dx);
+    const float c00 = lerp_b<T>(fx, v000, v100);
+    const float c10 = lerp_b<T>(fx, v010, v110);
+    const float c01 = lerp_b<T>(fx, v001, v101);
+    const float c11 = lerp_b<T>(fx, v011, v111);
     float c0 = fmaf(fy, c10 - c00, c00);
     float c1 = fmaf(fy, c11 - c01, c01);
     return fmaf(fz, c1 - c0, c0);
@@ -198,12 +213,12 @@ __device__ __forceinline__ float sample_cell(const FrameDesc& f, const BrickView
   const T* p0 = pool + (b.base + (long long)gz * b.s2 + (long long)gy * b.s1 + (long long)gx * b.s0);
   const T* p1 = p0 + b.s2;
   const int s0 = b.s0, s1 = b.s1;
-  float v000 = ldv(p0), v100 = ldv(p0 + s0), v010 = ldv(p0 + s1), v110 = ldv(p0 + s1 + s0);
-  float v001 = ldv(p1), v101 = ldv(p1 + s0), v011 = ldv(p1 + s1), v111 = ldv(p1 + s1 + s0);
-  float c00 = fmaf(fx, v100 - v000, v000);
-  float c10 = fmaf(fx, v110 - v010, v010);
-  float c01 = fmaf(fx, v101 - v001, v001);
-  float c11 = fmaf(fx, v111 - v011, v011);
+  const float v000 = ldb(p0), v100 = ldb(p0 + s0), v010 = ldb(p0 + s1), v110 = ldb(p0 + s1 + s0);
+  const float v001 = ldb(p1), v101 = ldb(p1 + s0), v011 = ldb(p1 + s1), v111 = ldb(p1 + s1 + s0);
+  const float c00 = lerp_b<T>(fx, v000, v100);
+  const float c10 = lerp_b<T>(fx, v010, v110);
+  const float c01 = lerp_b<T>(fx, v001, v101);
+  const float c11 = lerp_b<T>(fx, v011, v111);
   float c0 = fmaf(fy, c10 - c00, c00);
   float c1 = fmaf(fy, c11 - c01, c01);
   return fmaf(fz, c1 - c0, c0);
@@ -249,13 +264,15 @@ __device__ __forceinline__ void gradient(const FrameDesc& f, const BrickView& b,
           sample_cell<T, SAMPLER>(f, b, c.x, c.y, c.z - 1, c.fx, c.fy, c.fz)) * 0.5f;
 }
 
-// Trilinear interpolation of 8 voxels in sample_cell's order of operations.
+// Trilinear interpolation of 8 biased voxels (ldb) in sample_cell's order of
+// operations.
+template <typename T>
 __device__ __forceinline__ float trilin(float v000, float v100, float v010, float v110, float v001, float v101,
                                         float v011, float v111, float fx, float fy, float fz) {
-  const float c00 = fmaf(fx, v100 - v000, v000);
-  const float c10 = fmaf(fx, v110 - v010, v010);
-  const float c01 = fmaf(fx, v101 - v001, v001);
-  const float c11 = fmaf(fx, v111 - v011, v011);
+  const float c00 = lerp_b<T>(fx, v000, v100);
+  const float c10 = lerp_b<T>(fx, v010, v110);
+  const float c01 = lerp_b<T>(fx, v001, v101);
+  const float c11 = lerp_b<T>(fx, v011, v111);
   const float c0 = fmaf(fy, c10 - c00, c00);
   const float c1 = fmaf(fy, c11 - c01, c01);
   return fmaf(fz, c1 - c0, c0);
@@ -305,34 +322,35 @@ __device__ __forceinline__ void make_taps(const FrameDesc& f, const BrickView& b
 
 template <typename T>
 __device__ __forceinline__ float tap(const FrameDesc& f, const Taps& t, int i, int j, int k) {
-  return ldv(reinterpret_cast<const T*>(f.pool) + (t.base + (long long)(t.Z[k] + t.Y[j] + t.X[i])));
+  return ldb(reinterpret_cast<const T*>(f.pool) + (t.base + (long long)(t.Z[k] + t.Y[j] + t.X[i])));
 }
 
-// m: the cell's 8 voxels in sample_cell's order (v000, v100, v010, v110, v001, v101, v011, v111)
+// m: the cell's 8 voxels, biased (ldb), in sample_cell's order (v000, v100,
+// v010, v110, v001, v101, v011, v111)
 template <typename T>
 __device__ __forceinline__ float sample_taps(const FrameDesc& f, const Taps& t, const Cell& c, float m[8]) {
   m[0] = tap<T>(f, t, 1, 1, 1); m[1] = tap<T>(f, t, 2, 1, 1); m[2] = tap<T>(f, t, 1, 2, 1); m[3] = tap<T>(f, t, 2, 2, 1);
   m[4] = tap<T>(f, t, 1, 1, 2); m[5] = tap<T>(f, t, 2, 1, 2); m[6] = tap<T>(f, t, 1, 2, 2); m[7] = tap<T>(f, t, 2, 2, 2);
-  return trilin(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], c.fx, c.fy, c.fz);
+  return trilin<T>(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], c.fx, c.fy, c.fz);
 }
 
 template <typename T>
 __device__ __forceinline__ void gradient_taps(const FrameDesc& f, const Taps& t, const Cell& c, const float m[8],
                                               float g[3]) {
   const float fx = c.fx, fy = c.fy, fz = c.fz;
-  const float xp = trilin(m[1], tap<T>(f, t, 3, 1, 1), m[3], tap<T>(f, t, 3, 2, 1), m[5], tap<T>(f, t, 3, 1, 2), m[7],
+  const float xp = trilin<T>(m[1], tap<T>(f, t, 3, 1, 1), m[3], tap<T>(f, t, 3, 2, 1), m[5], tap<T>(f, t, 3, 1, 2), m[7],
                           tap<T>(f, t, 3, 2, 2), fx, fy, fz);
-  const float xm = trilin(tap<T>(f, t, 0, 1, 1), m[0], tap<T>(f, t, 0, 2, 1), m[2], tap<T>(f, t, 0, 1, 2), m[4],
+  const float xm = trilin<T>(tap<T>(f, t, 0, 1, 1), m[0], tap<T>(f, t, 0, 2, 1), m[2], tap<T>(f, t, 0, 1, 2), m[4],
                           tap<T>(f, t, 0, 2, 2), m[6], fx, fy, fz);
   g[0] = (xp - xm) * 0.5f;
-  const float yp = trilin(m[2], m[3], tap<T>(f, t, 1, 3, 1), tap<T>(f, t, 2, 3, 1), m[6], m[7], tap<T>(f, t, 1, 3, 2),
+  const float yp = trilin<T>(m[2], m[3], tap<T>(f, t, 1, 3, 1), tap<T>(f, t, 2, 3, 1), m[6], m[7], tap<T>(f, t, 1, 3, 2),
                           tap<T>(f, t, 2, 3, 2), fx, fy, fz);
-  const float ym = trilin(tap<T>(f, t, 1, 0, 1), tap<T>(f, t, 2, 0, 1), m[0], m[1], tap<T>(f, t, 1, 0, 2),
+  const float ym = trilin<T>(tap<T>(f, t, 1, 0, 1), tap<T>(f, t, 2, 0, 1), m[0], m[1], tap<T>(f, t, 1, 0, 2),
                           tap<T>(f, t, 2, 0, 2), m[4], m[5], fx, fy, fz);
   g[1] = (yp - ym) * 0.5f;
-  const float zp = trilin(m[4], m[5], m[6], m[7], tap<T>(f, t, 1, 1, 3), tap<T>(f, t, 2, 1, 3), tap<T>(f, t, 1, 2, 3),
+  const float zp = trilin<T>(m[4], m[5], m[6], m[7], tap<T>(f, t, 1, 1, 3), tap<T>(f, t, 2, 1, 3), tap<T>(f, t, 1, 2, 3),
                           tap<T>(f, t, 2, 2, 3), fx, fy, fz);
-  const float zm = trilin(tap<T>(f, t, 1, 1, 0), tap<T>(f, t, 2, 1, 0), tap<T>(f, t, 1, 2, 0), tap<T>(f, t, 2, 2, 0),
+  const float zm = trilin<T>(tap<T>(f, t, 1, 1, 0), tap<T>(f, t, 2, 1, 0), tap<T>(f, t, 1, 2, 0), tap<T>(f, t, 2, 2, 0),
                           m[0], m[1], m[2], m[3], fx, fy, fz);
   g[2] = (zp - zm) * 0.5f;
 }

@@ -8,10 +8,13 @@
 //   back into the output) and the match length bytes.  The last sequence has
 //   literals only; the last 5 bytes of a block are literals and the last
 //   match starts at least 12 bytes before the block's end.
-// The compressor is a greedy single-probe hash matcher (4-byte hash of the
-// next bytes, one candidate position per hash bucket).  The host decoder
-// checks every bound and fails on malformed input; the GPU decoder is in
-// kernels_build.cu.
+// The compressor is a greedy hash-chain matcher: every position is linked
+// into the chain of its 4-byte hash, and at each position up to `chain`
+// earlier positions of that chain within 65535 bytes are compared, the
+// longest match winning (the nearest on ties).  Fewer, longer sequences make
+// both a smaller block and a faster decode, whose cost on the GPU is per
+// sequence.  The host decoder checks every bound and fails on malformed
+// input; the GPU decoder is in kernels_build.cu.
 #include "lz4.h"
 
 #include <cstdint>
@@ -72,27 +75,50 @@ size_t lz4_bound(size_t n) { return n + n / 255 + 16; }
 
 // Compress src[0, n) into dst (capacity cap); returns the compressed size or
 // 0 when it does not fit.
-size_t lz4_compress(const uint8_t* src, size_t n, uint8_t* dst, size_t cap) {
+size_t lz4_compress(const uint8_t* src, size_t n, uint8_t* dst, size_t cap, int chain) {
   uint8_t* op = dst;
   const uint8_t* oend = dst + cap;
   size_t anchor = 0;
+  if (chain < 1) chain = 1;
   if (n >= kMatchLimit + 1) {
-    std::vector<int32_t> table((size_t)1 << kHashBits, -1);
+    // head: latest position of each hash; prev: the previous position of the
+    // same hash, per position modulo the 64 KiB window
+    std::vector<int32_t> head((size_t)1 << kHashBits, -1);
+    std::vector<int32_t> prev((size_t)1 << 16, -1);
     const size_t last_start = n - kMatchLimit;   // a match starts before this
     const size_t match_end = n - kLastLiterals;  // and ends at or before this
+    size_t ins = 0;                              // positions below this are linked
+    auto link_to = [&](size_t end) {
+      for (; ins < end; ++ins) {
+        const uint32_t h = hash4(rd32(src + ins));
+        prev[ins & 0xffff] = head[h];
+        head[h] = (int32_t)ins;
+      }
+    };
     size_t ip = 0;
     while (ip < last_start) {
+      link_to(ip);
       const uint32_t seq = rd32(src + ip);
-      const uint32_t h = hash4(seq);
-      const int32_t ref = table[h];
-      table[h] = (int32_t)ip;
-      if (ref >= 0 && ip - (size_t)ref <= kMaxOffset && rd32(src + ref) == seq) {
-        size_t len = kMinMatch;
-        while (ip + len < match_end && src[ref + len] == src[ip + len]) ++len;
-        if (!emit(op, oend, src + anchor, ip - anchor, ip - (size_t)ref, len)) return 0;
-        ip += len;
+      size_t best_len = 0, best_off = 0;
+      int32_t ref = head[hash4(seq)];
+      for (int k = 0; k < chain && ref >= 0 && ip - (size_t)ref <= kMaxOffset; ++k) {
+        if (rd32(src + ref) == seq) {
+          size_t len = kMinMatch;
+          while (ip + len < match_end && src[ref + len] == src[ip + len]) ++len;
+          if (len > best_len) {
+            best_len = len;
+            best_off = ip - (size_t)ref;
+            if (ip + len >= match_end) break;
+          }
+        }
+        const int32_t nx = prev[(size_t)ref & 0xffff];
+        if (nx >= ref) break;  // the window wrapped past this chain
+        ref = nx;
+      }
+      if (best_len) {
+        if (!emit(op, oend, src + anchor, ip - anchor, best_off, best_len)) return 0;
+        ip += best_len;
         anchor = ip;
-        if (ip >= 2 && ip - 2 < last_start) table[hash4(rd32(src + ip - 2))] = (int32_t)(ip - 2);
       } else {
         ++ip;
       }
@@ -151,7 +177,7 @@ size_t gbvr_lz4_bound(size_t n) { return gbvr::lz4_bound(n); }
 size_t gbvr_lz4_compress(const void* src, size_t n, void* dst, size_t cap) {
   GBVR_ABI_TRY
   if (!src || !dst) return 0;
-  return gbvr::lz4_compress((const uint8_t*)src, n, (uint8_t*)dst, cap);
+  return gbvr::lz4_compress((const uint8_t*)src, n, (uint8_t*)dst, cap, 16);
   GBVR_ABI_CATCH_SIZE
 }
 

@@ -214,6 +214,17 @@ class Renderer:
         L.call("gbvr_get_brick_minmax", self._h, lod, out.ctypes.data_as(C.POINTER(C.c_double)), nb)
         return out
 
+    def cellMinMax(self, lod):
+        """The level's macro-cell (min, max) grid as a (nz, ny, nx, 2) float32
+        array, and the cell edge in voxels."""
+        nc = (C.c_int32 * 3)()
+        edge = C.c_int32()
+        L.call("gbvr_get_cell_minmax", self._h, lod, None, 0, nc, C.byref(edge))
+        out = np.zeros((nc[2], nc[1], nc[0], 2), np.float32)
+        L.call("gbvr_get_cell_minmax", self._h, lod, out.ctypes.data_as(C.POINTER(C.c_float)), out.size // 2, nc,
+               C.byref(edge))
+        return out, edge.value
+
     def getBrick(self, lod, brick):
         b = (C.c_int32 * 3)(*brick)
         o = (C.c_int64 * 3)()

@@ -95,7 +95,9 @@ typedef struct gbvr_brick_params {
                            sampled by every view; 5: the blocks of that copy
                            also hold their +1 neighbours (5x5x5 voxels in 128
                            elements, 3x memory), so a trilinear footprint is
-                           read at fixed offsets from one address */
+                           read at fixed offsets from one address; 6: both
+                           blocked copies (4x memory), isosurfaces sampled from
+                           the overlapped one, the other modes from the other */
   int32_t compression;  /* out-of-core host store: 0 raw, 1 zlib, 3 LZ4 (the UVF codec ids
                            CT_ZLIB and CT_LZ4, UVFReader/BlockInfo.h:60-93; zlib is the
                            converter's default, CmdLineConverter/main.cpp:146): 16 KiB chunks
@@ -180,6 +182,13 @@ int gbvr_get_hist1d(gbvr_renderer* r, uint64_t* out, size_t n);
 int gbvr_get_hist2d(gbvr_renderer* r, uint64_t* out, size_t nx, size_t ny, float* max_grad);
 /* per-brick min/max of one level in brick order (MaxMinDataBlock) */
 int gbvr_get_brick_minmax(gbvr_renderer* r, int lod, double* out_minmax, size_t nbricks);
+/* the macro-cell min/max grid of a level (the empty-space skipping structure
+ * inside bricks): cell (cx, cy, cz) of edge M voxels (4 in core, 8 out of
+ * core) holds the min and max of the voxels [c M - 1, c M + M + 1] per axis
+ * (clamped to the level), at out_minmax[2 ((cz ny + cy) nx + cx)]; nc
+ * receives (nx, ny, nz) and cell_edge M.  ncells: capacity in cells. */
+int gbvr_get_cell_minmax(gbvr_renderer* r, int lod, float* out_minmax, size_t ncells, int32_t nc[3],
+                         int32_t* cell_edge);
 /* copy one stored brick (interior + ghosts) back to the host */
 int gbvr_get_brick(gbvr_renderer* r, int lod, const int32_t brick[3], void* out, size_t bytes,
                    int64_t origin[3], int64_t stored_dims[3]);

@@ -168,3 +168,53 @@ def test_dev_hist2d_paths_bit_exact(orc, case):
     got, gmg = _dev_hist2d(vol, ms, nx, f, offset)
     assert np.array_equal(got, want), case
     assert np.float32(gmg) == np.float32(wmg)
+
+
+def _cell_ranges(vol, m):
+    """Macro-cell (min, max) of a (z, y, x) level: cell c covers voxels
+    [c m - 1, c m + m + 1] per axis, clamped to the level (edge padding
+    repeats the edge voxel, which the clamped range already holds)."""
+    lo, hi = vol.astype(np.float32), vol.astype(np.float32)
+    for ax in range(3):
+        n = vol.shape[ax]
+        nc = -(-n // m)
+        pad = [(0, 0)] * 3
+        pad[ax] = (1, nc * m + 2 - n)
+        win = [np.lib.stride_tricks.sliding_window_view(np.pad(a, pad, mode="edge"), m + 3, axis=ax)
+               for a in (lo, hi)]
+        sl = [slice(None)] * 3
+        sl[ax] = slice(0, nc * m, m)
+        lo, hi = win[0][tuple(sl)].min(axis=-1), win[1][tuple(sl)].max(axis=-1)
+    return np.stack([lo, hi], axis=-1)
+
+
+@pytest.mark.parametrize("dtype,shape,brick,layouts", [(np.uint16, (37, 50, 23), 32, 4),
+                                                       (np.uint8, (70, 64, 97), 32, 6),
+                                                       (np.float32, (29, 41, 66), 64, 1)])
+def test_macro_cell_ranges_and_brick_minmax_bit_exact(orc, dtype, shape, brick, layouts):
+    """The macro-cell min/max grid of every level (the skipping structure) and
+    each brick's min/max over its stored voxels equal their rules bit for bit,
+    for sizes that are not multiples of the cell edge, every layout copy
+    choice, and float data with negative values."""
+    rng = np.random.default_rng(11)
+    if dtype == np.float32:
+        vol = (rng.normal(0.0, 40.0, shape) - 15.0).astype(np.float32)
+    else:
+        top = 4095 if dtype == np.uint16 else 255
+        vol = rng.integers(0, top + 1, shape).astype(dtype)
+    lv = _levels(orc, vol, brick, 2)
+    with Renderer() as r:
+        r.loadVolume(vol, brick_size=brick, overlap=2, layouts=layouts)
+        for l, level in enumerate(lv):
+            got, edge = r.cellMinMax(l)
+            assert edge == 4
+            assert np.array_equal(got, _cell_ranges(level, 4)), l
+            nb, _ = orc.brick_grid((level.shape[2], level.shape[1], level.shape[0]), brick, 2)
+            mm = r.brickMinMax(l)
+            i = 0
+            for bz in range(nb[2]):
+                for by in range(nb[1]):
+                    for bx in range(nb[0]):
+                        want, _ = orc.extract_brick(level, brick, 2, (bx, by, bz))
+                        assert mm[i, 0] == want.min() and mm[i, 1] == want.max(), (l, bx, by, bz)
+                        i += 1

@@ -1,5 +1,5 @@
 """The sparse fractal workload at its full size: 2048^3 uint8 fBm, 256^3
-bricks with 2 ghosts (and the 4x4x4-blocked copy the benchmark samples),
+bricks with 2 ghosts (and the two blocked copies the benchmark samples),
 2560x1440 views, the 2D TF + Phong path and the isosurface path at the three
 seeded isovalues, against the FP64 oracle on seeded pixel subsets.  The
 oracle evaluates the fractal's voxels where its samples need them
@@ -18,7 +18,7 @@ def c3():
     wl = workloads.config3()
     assert [wl.synth.dims[i] for i in range(3)] == [2048] * 3 and (wl.width, wl.height) == (2560, 1440)
     r = Renderer(float_fb=True)
-    r.loadSynthetic(wl.synth, **wl.brick, layouts=4)
+    r.loadSynthetic(wl.synth, **wl.brick, layouts=6)
     r.resize((wl.width, wl.height))
     r.setValueRange(*wl.value_range)
     r.setSampleRateModifier(wl.spv)

@@ -276,7 +276,7 @@ def test_layout_copies_and_launch_shapes_do_not_change_pixels(multibrick):
     views = workloads.orbit_views(4, 96, 80, elevation=35.0, start=10.0)
     views.append(orbit_camera(0.0, 89.0, 2.5 * workloads.DIAG, 45.0, 96, 80))  # looking down y
     imgs = {}
-    for layouts in (1, 3, 4, 5):
+    for layouts in (1, 3, 4, 5, 6):
         with Renderer(float_fb=True) as r:
             r.loadVolume(vol, brick_size=64, overlap=2, layouts=layouts)
             r.resize((96, 80))
@@ -302,13 +302,14 @@ def test_layout_copies_and_launch_shapes_do_not_change_pixels(multibrick):
 @pytest.mark.parametrize("mode", [GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE, GBVR_RM_MIP])
 @pytest.mark.parametrize("interp", [True, False])
 def test_overlapped_blocks_give_the_same_pixels(multibrick, mode, interp):
-    """The copy in 4^3 blocks that hold their +1 neighbours (layouts 5) reads
-    the same voxels as the x-fastest copy in every mode, with trilinear and
-    nearest sampling: the same pixels bit for bit."""
+    """The copy in 4^3 blocks that hold their +1 neighbours (layouts 5, and 6
+    where isosurfaces use it) reads the same voxels as the x-fastest copy in
+    every mode, with trilinear and nearest sampling: the same pixels bit for
+    bit."""
     vol, _, tf = multibrick
     views = workloads.orbit_views(3, 112, 96, elevation=25.0, start=40.0)
     out = {}
-    for layouts in (1, 5):
+    for layouts in (1, 5, 6):
         with Renderer(float_fb=True) as r:
             r.loadVolume(vol, brick_size=64, overlap=2, layouts=layouts)
             r.resize((112, 96))
@@ -324,8 +325,9 @@ def test_overlapped_blocks_give_the_same_pixels(multibrick, mode, interp):
             r.paintBatch(views)
             out[layouts] = [r.readFramebuffer(i, as_float=True) for i in range(len(views))]
     assert max(float(a[..., 3].max()) for a in out[1]) > 0.2
-    for a, b in zip(out[1], out[5]):
-        assert np.array_equal(a, b)
+    for lay in (5, 6):
+        for a, b in zip(out[1], out[lay]):
+            assert np.array_equal(a, b), lay
 
 
 @pytest.mark.parametrize("mode", [GBVR_RM_1DTRANS, GBVR_RM_2DTRANS, GBVR_RM_ISOSURFACE])

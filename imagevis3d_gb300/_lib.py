@@ -177,6 +177,7 @@ SIGNATURES = {
     "gbvr_zlib_compress": [P, SZ, P, SZ],
     "gbvr_zlib_decompress": [P, SZ, P, SZ],
     "gbvr_dev_zlib_decode": [P, P, P, I, P, P],
+    "gbvr_dev_lz4_decode": [P, P, P, I, P, P],
     "gbvr_set_clearview": [P, I, F, FP, F, F, F, F, F],
     "gbvr_paint_slice": [P, I, C.c_int64, I, I, I],
     "gbvr_paint_path": [P, C.POINTER(View), I, C.POINTER(C.c_int32), U64P, U64P],

@@ -2034,12 +2034,7 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
 
 int ooc_streams(gbvr_renderer* r) {
   if (!r->copy_stream) {
-    // the copies and decodes of frame i + 1 run at the highest priority, so
-    // their CTAs are dispatched as frame i's render CTAs retire instead of
-    // after the whole render
-    int least = 0, greatest = 0;
-    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    CUDA_TRY(cudaStreamCreateWithPriority(&r->copy_stream, cudaStreamNonBlocking, greatest));
+    CUDA_TRY(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
     for (int k = 0; k < 2; ++k) {
       CUDA_TRY(cudaEventCreate(&r->ev_c0[k]));
       CUDA_TRY(cudaEventCreate(&r->ev_c1[k]));
@@ -3550,6 +3545,16 @@ int gbvr_dev_zlib_decode(const void* dev_src, void* dev_dst, const gbvr_zchunk* 
   if (n < 0 || (n > 0 && (!dev_src || !dev_dst || !dev_chunks || !dev_err))) return fail(GBVR_EINVAL, "bad arguments");
   CUDA_TRY(launch_inflate(dev_src, dev_dst, reinterpret_cast<const Lz4Chunk*>(dev_chunks), n, dev_err,
                           (cudaStream_t)stream));
+  return GBVR_OK;
+  GBVR_ABI_CATCH
+}
+
+int gbvr_dev_lz4_decode(const void* dev_src, void* dev_dst, const gbvr_zchunk* dev_chunks, int n, int* dev_err,
+                        void* stream) {
+  GBVR_ABI_TRY
+  if (n < 0 || (n > 0 && (!dev_src || !dev_dst || !dev_chunks || !dev_err))) return fail(GBVR_EINVAL, "bad arguments");
+  CUDA_TRY(launch_lz4_decode(dev_src, dev_dst, reinterpret_cast<const Lz4Chunk*>(dev_chunks), n, dev_err,
+                             (cudaStream_t)stream));
   return GBVR_OK;
   GBVR_ABI_CATCH
 }

@@ -368,12 +368,15 @@ __device__ __forceinline__ void shade(const FrameDesc& f, const float* L, const 
     out[2] = col[2] * f.amb[2];
     return;
   }
-  float n0 = -g[0] / gl, n1 = -g[1] / gl, n2 = -g[2] / gl;
+  // one correctly rounded reciprocal and three products instead of three
+  // divisions
+  const float rg = -__frcp_rn(gl);
+  float n0 = g[0] * rg, n1 = g[1] * rg, n2 = g[2] * rg;
   if (n0 * V[0] + n1 * V[1] + n2 * V[2] < 0.f) { n0 = -n0; n1 = -n1; n2 = -n2; }
   float nl = fmaxf(0.f, n0 * L[0] + n1 * L[1] + n2 * L[2]);
   float H0 = L[0] + V[0], H1 = L[1] + V[1], H2 = L[2] + V[2];
   float hl = sqrtf(H0 * H0 + H1 * H1 + H2 * H2);
-  float nh = hl > 0.f ? fmaxf(0.f, (n0 * H0 + n1 * H1 + n2 * H2) / hl) : 0.f;
+  float nh = hl > 0.f ? fmaxf(0.f, (n0 * H0 + n1 * H1 + n2 * H2) * __frcp_rn(hl)) : 0.f;
   float sp = nh > 0.f ? __powf(nh, f.shininess) : 0.f;
 #pragma unroll
   for (int k = 0; k < 3; ++k) out[k] = col[k] * (f.amb[k] + f.diff[k] * nl) + f.spec[k] * sp;

@@ -711,6 +711,12 @@ typedef struct gbvr_zchunk {
  * returns once the work is queued on `stream` (a cudaStream_t, or null). */
 int gbvr_dev_zlib_decode(const void* dev_src, void* dev_dst, const gbvr_zchunk* dev_chunks, int n, int* dev_err,
                          void* stream);
+/* The same for LZ4 blocks (codec id 3; gbvr_lz4_compress writes them), the
+ * decoder of paged bricks when gbvr_brick_params.compression = 3: one warp
+ * per chunk, each block decoded to exactly `raw` bytes; a malformed block
+ * sets *dev_err nonzero and is left partly written. */
+int gbvr_dev_lz4_decode(const void* dev_src, void* dev_dst, const gbvr_zchunk* dev_chunks, int n, int* dev_err,
+                        void* stream);
 
 #ifdef __cplusplus
 }

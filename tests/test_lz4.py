@@ -77,3 +77,16 @@ def test_hand_built_block():
 def test_malformed_blocks_are_rejected(block, n):
     assert decompress(block, n) is None
     assert orc.lz4_decompress(block, n) is None or len(orc.lz4_decompress(block, n)) != n
+
+
+def test_crafted_blocks_decode_on_the_host_as_the_reference():
+    """The hand-built blocks of the GPU decoder's tests are valid LZ4: the
+    library's host decoder and the plain Python reference agree on them."""
+    from tests.lz4_blocks import cases, reference
+    lib = L.lib()
+    for i, blk in enumerate(cases()):
+        ref = reference(blk)
+        src = np.frombuffer(blk, np.uint8)
+        out = np.zeros(len(ref), np.uint8)
+        assert lib.gbvr_lz4_decompress(src.ctypes.data, len(blk), out.ctypes.data, len(ref)) == 0, i
+        assert out.tobytes() == ref, i

@@ -651,6 +651,8 @@ constexpr int OOC_CELL_SHIFT = 3;
 // raw bytes per compressed chunk of a brick (one LZ4 block): small enough that
 // a paged frame gives the decoder thousands of warps
 constexpr size_t LZ_CHUNK = 16384;
+// the host store's LZ4 encoder: hash-chain depth and the shortest match taken
+constexpr int kStoreLz4Chain = 16, kStoreLz4MinMatch = 8;
 
 int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_params* bp, uint64_t pool_bytes,
                     cudaStream_t s) {
@@ -826,7 +828,8 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
             for (size_t o = 0; o < nbytes; o += LZ_CHUNK) {
               const size_t rn = std::min(LZ_CHUNK, nbytes - o);
               const size_t cn = ds.compression == 1 ? zlib_compress(src + o, rn, buf.data(), buf.size(), 16)
-                                                    : lz4_compress(src + o, rn, buf.data(), buf.size());
+                                                    : lz4_compress(src + o, rn, buf.data(), buf.size(),
+                                                                   kStoreLz4Chain, kStoreLz4MinMatch);
               if (cn > 0 && cn < rn) {
                 out[j].insert(out[j].end(), buf.data(), buf.data() + cn);
                 sizes[j].push_back((unsigned)cn);

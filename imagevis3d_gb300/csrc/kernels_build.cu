@@ -904,6 +904,7 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
   const unsigned long long smax = sc->smax;
   const double gmax = __longlong_as_double((long long)sc->gmax_bits);
   const float smax_f = (float)smax;
+  const float inv_smax = 1.f / smax_f;  // the estimate below needs to be within one bin only
   const bool merge1 = merge == 1;
   // values are below 2^16, so any merge above 2^16 bins like 2^16
   const unsigned merge32 = (unsigned)(merge < 1 ? 1 : merge > 65536 ? 65536 : merge);
@@ -922,7 +923,10 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
         // FP32 estimate (within one of the exact bin: S, Smax < 2^36), then
         // settled by the exact integer tests; FP64 arithmetic is slow on this
         // part and stays confined to ties
-        k = (int)(255.f * sqrtf(__fdiv_rn((float)S, smax_f)));
+        {
+          const float q = (float)S * inv_smax;
+          k = (int)(255.f * (q * rsqrtf(q)));
+        }
         if (k > 255) k = 255;
         while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
         while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;
@@ -1130,6 +1134,7 @@ __global__ void __launch_bounds__(256, 3) k_h2v_bin(const T* __restrict__ v, int
   const unsigned long long smax = sc->smax;
   const double gmax = __longlong_as_double((long long)sc->gmax_bits);
   const float smax_f = (float)smax;
+  const float inv_smax = 1.f / smax_f;  // the estimate below needs to be within one bin only
   const unsigned merge32 = (unsigned)merge;
   const int words = nx * kshared / 2;  // kshared is even
   if (SMEM) {
@@ -1181,7 +1186,8 @@ __global__ void __launch_bounds__(256, 3) k_h2v_bin(const T* __restrict__ v, int
           if (smax > 0 && S[j] > 0) {
             const unsigned long long lhs = 65025ULL * (unsigned long long)S[j];
             // FP32 estimate (within one of the exact bin), settled exactly
-            k = (int)(255.f * sqrtf(__fdiv_rn((float)S[j], smax_f)));
+            const float q = (float)S[j] * inv_smax;
+            k = (int)(255.f * (q * rsqrtf(q)));
             if (k > 255) k = 255;
             while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
             while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;

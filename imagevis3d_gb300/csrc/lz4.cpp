@@ -11,9 +11,10 @@
 // The compressor is a greedy hash-chain matcher: every position is linked
 // into the chain of its 4-byte hash, and at each position up to `chain`
 // earlier positions of that chain within 65535 bytes are compared, the
-// longest match winning (the nearest on ties).  Fewer, longer sequences make
-// both a smaller block and a faster decode, whose cost on the GPU is per
-// sequence.  The host decoder checks every bound and fails on malformed
+// longest match winning (the nearest on ties), and taken when it is at least
+// `min_match` bytes long (4, the format's minimum, by default; a larger one
+// trades ratio for fewer sequences).  Fewer, longer sequences make a faster
+// decode, whose cost on the GPU is per sequence.  The host decoder checks every bound and fails on malformed
 // input; the GPU decoder is in kernels_build.cu.
 #include "lz4.h"
 
@@ -75,7 +76,7 @@ size_t lz4_bound(size_t n) { return n + n / 255 + 16; }
 
 // Compress src[0, n) into dst (capacity cap); returns the compressed size or
 // 0 when it does not fit.
-size_t lz4_compress(const uint8_t* src, size_t n, uint8_t* dst, size_t cap, int chain) {
+size_t lz4_compress(const uint8_t* src, size_t n, uint8_t* dst, size_t cap, int chain, int min_match) {
   uint8_t* op = dst;
   const uint8_t* oend = dst + cap;
   size_t anchor = 0;
@@ -115,7 +116,7 @@ size_t lz4_compress(const uint8_t* src, size_t n, uint8_t* dst, size_t cap, int 
         if (nx >= ref) break;  // the window wrapped past this chain
         ref = nx;
       }
-      if (best_len) {
+      if (best_len && best_len >= (size_t)min_match) {
         if (!emit(op, oend, src + anchor, ip - anchor, best_off, best_len)) return 0;
         ip += best_len;
         anchor = ip;

@@ -113,9 +113,24 @@ cudaError_t launch_synth_blobs(const BlobTablesDev& t, const long long dims[3], 
 // the children that exist, floor for integers, float(sum/count) with a double
 // sum for float32.  One thread per output voxel; x fastest for coalescing.
 // ---------------------------------------------------------------------------
+// two x-adjacent 8- or 16-bit voxels (the first at an even index of a row of
+// even length, so the pair is aligned) summed from one load
+__device__ __forceinline__ unsigned pair_sum(const uint8_t* p) {
+  const unsigned w = __ldg(reinterpret_cast<const unsigned short*>(p));
+  return (w & 0xffu) + (w >> 8);
+}
+__device__ __forceinline__ unsigned pair_sum(const uint16_t* p) {
+  const unsigned w = __ldg(reinterpret_cast<const unsigned*>(p));
+  return (w & 0xffffu) + (w >> 16);
+}
+__device__ __forceinline__ unsigned pair_sum(const float*) { return 0u; }
+
 template <typename T>
 __global__ void k_downsample(const T* __restrict__ in, long long X, long long Y, long long Z, T* __restrict__ out,
                              long long OX, long long OY, long long OZ) {
+  // pairs: rows of even length from an aligned base, so every even x starts
+  // an aligned pair
+  const bool pairs = sizeof(T) < 4 && (X & 1) == 0 && (reinterpret_cast<uintptr_t>(in) % (2 * sizeof(T))) == 0;
   for (long long row = blockIdx.x; row < OY * OZ; row += gridDim.x) {
     const long long z = row / OY, y = row - z * OY;
     const long long y0 = 2 * y, z0 = 2 * z;
@@ -130,6 +145,11 @@ __global__ void k_downsample(const T* __restrict__ in, long long X, long long Y,
           for (int dy = 0; dy < ny; ++dy)
             for (int dx = 0; dx < nx; ++dx) sum += (double)__ldg(in + ((z0 + dz) * Y + (y0 + dy)) * X + x0 + dx);
         out[o] = (T)(float)(sum / (double)(nx * ny * nz));
+      } else if (pairs && nx == 2 && ny == 2 && nz == 2) {
+        // all 8 children: the x pairs in one load each, the mean by a shift
+        const T* p = in + (z0 * Y + y0) * X + x0;
+        const unsigned sum = pair_sum(p) + pair_sum(p + X) + pair_sum(p + X * Y) + pair_sum(p + X * Y + X);
+        out[o] = (T)(sum >> 3);
       } else {
         unsigned sum = 0;
         for (int dz = 0; dz < nz; ++dz)
@@ -763,6 +783,54 @@ __global__ void k_hist1d_smem(const T* __restrict__ v, long long n, unsigned lon
     if (sh[i]) atomicAdd(hist + i, (unsigned long long)sh[i]);
 }
 
+// The same from 16-byte loads: a thread takes 16 consecutive bytes (8 16-bit
+// or 16 8-bit values) at a time, so runs of one value along x (smooth data,
+// not only empty space) cost one shared-memory atomic.  v must be 16-byte
+// aligned; the last n mod (16 / sizeof(T)) values are counted one by one.
+template <typename T>
+__global__ void k_hist1d_vec(const T* __restrict__ v, long long n, unsigned long long* __restrict__ hist, int nbins) {
+  constexpr int PER = 16 / (int)sizeof(T);
+  extern __shared__ unsigned sh[];
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  unsigned run_bin = 0xffffffffu, run = 0;
+  auto count = [&](unsigned b) {
+    if (b >= (unsigned)nbins) return;
+    if (b == run_bin) {
+      ++run;
+    } else {
+      if (run) atomicAdd(sh + run_bin, run);
+      run_bin = b;
+      run = 1;
+    }
+  };
+  const long long nv = n / PER;
+  const uint4* v4 = reinterpret_cast<const uint4*>(v);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nv; i += stride) {
+    const uint4 w = __ldg(v4 + i);
+    const unsigned q[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (sizeof(T) == 2) {
+        count(q[k] & 0xffffu);
+        count(q[k] >> 16);
+      } else {
+        count(q[k] & 0xffu);
+        count((q[k] >> 8) & 0xffu);
+        count((q[k] >> 16) & 0xffu);
+        count(q[k] >> 24);
+      }
+    }
+  }
+  for (long long i = nv * PER + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
+    count((unsigned)__ldg(v + i));
+  if (run) atomicAdd(sh + run_bin, run);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+    if (sh[i]) atomicAdd(hist + i, (unsigned long long)sh[i]);
+}
+
 template <typename T>
 __global__ void k_hist1d_global(const T* __restrict__ v, long long n, unsigned long long* __restrict__ hist, int nbins) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -779,13 +847,21 @@ cudaError_t launch_hist1d(const void* vol, int dtype, long long n, unsigned long
   if (blocks > 152 * 4) blocks = 152 * 4;
   if (nbins <= 16384) {
     size_t smem = sizeof(unsigned) * nbins;
+    const bool vec = ((uintptr_t)vol & 15) == 0;
+    const void* fn = vec ? (dtype == DT_U8 ? (const void*)k_hist1d_vec<uint8_t> : (const void*)k_hist1d_vec<uint16_t>)
+                         : (dtype == DT_U8 ? (const void*)k_hist1d_smem<uint8_t> : (const void*)k_hist1d_smem<uint16_t>);
     if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(dtype == DT_U8 ? (const void*)k_hist1d_smem<uint8_t> : (const void*)k_hist1d_smem<uint16_t>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
-    if (dtype == DT_U8) k_hist1d_smem<uint8_t><<<blocks, threads, smem, s>>>((const uint8_t*)vol, n, hist, nbins);
-    else k_hist1d_smem<uint16_t><<<blocks, threads, smem, s>>>((const uint16_t*)vol, n, hist, nbins);
+    if (vec) {
+      if (dtype == DT_U8) k_hist1d_vec<uint8_t><<<blocks, threads, smem, s>>>((const uint8_t*)vol, n, hist, nbins);
+      else k_hist1d_vec<uint16_t><<<blocks, threads, smem, s>>>((const uint16_t*)vol, n, hist, nbins);
+    } else if (dtype == DT_U8) {
+      k_hist1d_smem<uint8_t><<<blocks, threads, smem, s>>>((const uint8_t*)vol, n, hist, nbins);
+    } else {
+      k_hist1d_smem<uint16_t><<<blocks, threads, smem, s>>>((const uint16_t*)vol, n, hist, nbins);
+    }
   } else {
     k_hist1d_global<uint16_t><<<blocks, threads, 0, s>>>((const uint16_t*)vol, n, hist, nbins);
   }

@@ -605,7 +605,9 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
     CUDA_TRY(launch_hist2d(lv[0]->p, dtype, dims, ds.gmax, outsize, ds.merge, d2.as<unsigned long long>(),
                            dsc.as<Hist2DScratch>(), s));
     CUDA_TRY(t_h2.stop(s));
-    bs.hist2d_bytes = 3 * level_bytes(0);
+    // two passes over the level (the largest squared gradient, then the bins);
+    // the f64 pass between them revisits only the voxels attaining it
+    bs.hist2d_bytes = 2 * level_bytes(0);
     ds.hist2d.resize(n2);
     Hist2DScratch hs;
     CUDA_TRY(cudaMemcpyAsync(ds.hist2d.data(), d2.p, sizeof(uint64_t) * n2, cudaMemcpyDeviceToHost, s));

@@ -426,9 +426,14 @@ int gbvr_load_synthetic_fbm(gbvr_renderer* r, const gbvr_fbm_params* p, const gb
  * each phase's launches.  Synthesis, host uploads and texture building are
  * not part of it.  bytes = what each phase must read and write at least:
  * pyramid: every level read once and the next written; cells: every level
- * read; bricks: every level read and its stored bricks written, per layout
- * copy; minmax: the stored bricks of copy 0 read; hist1d: level 0 read;
- * hist2d: level 0 read three times (maximum, maximum gradient, binning). */
+ * read; bricks: every level read once for the x-fastest and 4x4x4-blocked
+ * copies (written together, with each brick's min/max reduced on the way,
+ * so minmax is 0 ms and 0 bytes) and once more per other copy, plus every
+ * stored brick written per copy (twice its size for the overlapped blocks);
+ * hist1d: level 0 read;
+ * hist2d: level 0 read twice (the largest squared gradient, then the bins;
+ * the f64 maximum-gradient pass between them revisits only the voxels that
+ * attain it). */
 typedef struct gbvr_build_stats {
   double total_ms;
   double pyramid_ms, cells_ms, bricks_ms, minmax_ms, hist1d_ms, hist2d_ms;

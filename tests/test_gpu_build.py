@@ -190,7 +190,11 @@ def _cell_ranges(vol, m):
 
 @pytest.mark.parametrize("dtype,shape,brick,layouts", [(np.uint16, (37, 50, 23), 32, 4),
                                                        (np.uint8, (70, 64, 97), 32, 6),
-                                                       (np.float32, (29, 41, 66), 64, 1)])
+                                                       (np.float32, (29, 41, 66), 64, 1),
+                                                       # 16-bit rows of whole 4-byte words: the tiles
+                                                       # away from the x faces read their rows as words
+                                                       (np.uint16, (21, 30, 128), 64, 4),
+                                                       (np.uint8, (19, 27, 136), 64, 1)])
 def test_macro_cell_ranges_and_brick_minmax_bit_exact(orc, dtype, shape, brick, layouts):
     """The macro-cell min/max grid of every level (the skipping structure) and
     each brick's min/max over its stored voxels equal their rules bit for bit,

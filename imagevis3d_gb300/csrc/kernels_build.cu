@@ -1491,14 +1491,21 @@ __global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restr
   }
   // The warp parses in lockstep from a 32-byte window of the input, one byte
   // per lane (refilled with one coalesced load when the parse leaves it):
-  // header bytes come by shuffle, not by dependent loads.
-  unsigned wbase = 0xffffffffu, wbyte = 0;
+  // header bytes come by shuffle, not by dependent loads.  wpair: the lane's
+  // byte and the next one, so a 2-byte offset is one shuffle.
+  unsigned wbase = 0xffffffffu, wbyte = 0, wpair = 0;
+  auto refill = [&](unsigned pos) {
+    wbase = pos;
+    wbyte = pos + lane < n ? (unsigned)__ldg(in + pos + lane) : 0u;
+    wpair = wbyte | (__shfl_down_sync(0xffffffffu, wbyte, 1) << 8);
+  };
   auto byte_at = [&](unsigned pos) -> unsigned {
-    if (pos < wbase || pos >= wbase + 32) {
-      wbase = pos;
-      wbyte = pos + lane < n ? (unsigned)__ldg(in + pos + lane) : 0u;
-    }
+    if (pos < wbase || pos >= wbase + 32) refill(pos);
     return __shfl_sync(0xffffffffu, wbyte, (int)(pos - wbase));
+  };
+  auto pair_at = [&](unsigned pos) -> unsigned {
+    if (pos < wbase || pos + 1 >= wbase + 32) refill(pos);
+    return __shfl_sync(0xffffffffu, wpair, (int)(pos - wbase)) & 0xffffu;
   };
   unsigned ip = 0, op = 0;
   for (;;) {
@@ -1523,7 +1530,7 @@ __global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restr
       break;
     }
     if (n - ip < 2) break;
-    const unsigned off = byte_at(ip) | (byte_at(ip + 1) << 8);
+    const unsigned off = pair_at(ip);
     ip += 2;
     unsigned mlen = token & 15;
     if (mlen == 15) {
@@ -1542,7 +1549,10 @@ __global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restr
       // match: a literal of this step (taken from its lane) or earlier
       // output (in memory, ordered by the last __syncwarp).
       const unsigned j = lane;
-      const unsigned lit = j < nlit ? (unsigned)__ldg(in + lit_at + j) : 0u;
+      // literals inside the current window come from it by shuffle
+      const bool lit_in_win = lit_at >= wbase && lit_at + nlit <= wbase + 32;
+      const unsigned wl = __shfl_sync(0xffffffffu, wbyte, (int)((lit_at - wbase + j) & 31u));
+      const unsigned lit = j < nlit ? (lit_in_win ? wl : (unsigned)__ldg(in + lit_at + j)) : 0u;
       int src = 0;
       if (j >= nlit) {
         int d = (int)(j - nlit);

@@ -393,7 +393,7 @@ def run_c4(args):
     r = Renderer()
     t0 = time.perf_counter()
     codec = 0 if args.no_compress else {"lz4": 3, "zlib": 1}[args.codec]
-    r.loadSyntheticOutOfCore(wl.synth, pool, compression=codec, **wl.brick)
+    r.loadSyntheticOutOfCore(wl.synth, pool, compression=codec, brick_order=args.brick_order, **wl.brick)
     build_s = time.perf_counter() - t0
     info = r.datasetInfo()
     r.resize((wl.width, wl.height))
@@ -467,6 +467,7 @@ def run_c4(args):
     paged = sum(int(p[3].sum()) for p in passes)
     page_ms = sum(p[4]["page_ms"] for p in passes)
     paged_comp = sum(int(p[4]["bytes_paged_compressed"]) for p in passes)
+    host_copies = sum(int(p[4]["host_copies"]) for p in passes)
     h2d = paged_comp if info["compression"] else paged
     lod_hist = {}
     for p in passes:
@@ -481,6 +482,7 @@ def run_c4(args):
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded blob volume, streamed from seed)",
         "config": {"workload": wl.name, "volume_bytes": vol_bytes, "host_store_bytes": info["host_bytes"],
                    "host_store_raw_bytes": info["host_raw_bytes"],
+                   "store_brick_order": ["scanline", "Morton", "Hilbert", "random"][args.brick_order],
                    "store_compression": ({3: "lz4", 1: "zlib"}[info["compression"]] + " (16 KiB chunks, decoded on "
                                          "the GPU)") if info["compression"] else "none",
                    "device_pool_bytes": pool, "device_slots": info["device_slots"], "bricks": info["total_bricks"],
@@ -491,6 +493,7 @@ def run_c4(args):
         "h2d_gbps": h2d / (page_ms / 1000.0) / 1e9 if page_ms > 0 else None,
         "paged_raw_gbps": paged / (page_ms / 1000.0) / 1e9 if page_ms > 0 else None,
         "paged_compressed_bytes_per_frame": paged_comp / (frames * len(passes)),
+        "host_copies_per_frame": host_copies / (frames * len(passes)),
         "store_ratio": info["host_raw_bytes"] / max(info["host_bytes"], 1),
         "lod_frames": lod_hist,
         "first_pass_fps": frames / walls[0], "last_pass_fps": frames / walls[-1],
@@ -728,6 +731,8 @@ def main():
     ap.add_argument("--pool-gib", type=float, default=0.0)
     ap.add_argument("--no-compress", action="store_true", help="c4: raw host brick store")
     ap.add_argument("--codec", default="lz4", choices=["lz4", "zlib"], help="c4: codec of the host brick store")
+    ap.add_argument("--brick-order", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="c4: host store brick order: 0 scanline, 1 Morton, 2 Hilbert, 3 random")
     ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--plain-requests", type=int, default=600)
     ap.add_argument("--max-batch", type=int, default=64)

@@ -26,7 +26,7 @@ ERRORS = {
 class BrickParams(C.Structure):
     _fields_ = [("brick_size", C.c_int32), ("overlap", C.c_int32), ("max_lods", C.c_int32),
                 ("build_texture", C.c_int32), ("layouts", C.c_int32), ("compression", C.c_int32),
-                ("aspect", C.c_double * 3)]
+                ("brick_order", C.c_int32), ("reserved", C.c_int32), ("aspect", C.c_double * 3)]
 
 
 class DatasetInfo(C.Structure):
@@ -49,7 +49,7 @@ class Stats(C.Structure):
                 ("brick_misses", C.c_uint64), ("bytes_paged", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("lod", C.c_int32), ("subframes", C.c_int32), ("gpu_ms", C.c_double),
                 ("kernel_ms", C.c_double), ("cells_touched", C.c_uint64), ("cell_bytes", C.c_uint64),
-                ("page_ms", C.c_double), ("bytes_paged_compressed", C.c_uint64)]
+                ("page_ms", C.c_double), ("bytes_paged_compressed", C.c_uint64), ("host_copies", C.c_uint64)]
 
 
 class TuneResult(C.Structure):
@@ -178,6 +178,8 @@ SIGNATURES = {
     "gbvr_zlib_decompress": [P, SZ, P, SZ],
     "gbvr_dev_zlib_decode": [P, P, P, I, P, P],
     "gbvr_dev_lz4_decode": [P, P, P, I, P, P],
+    "gbvr_brick_order": [C.POINTER(C.c_int32), C.c_int32, C.c_uint64, C.POINTER(C.c_int32), SZ],
+    "gbvr_hilbert3": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32],
     "gbvr_set_clearview": [P, I, F, FP, F, F, F, F, F],
     "gbvr_paint_slice": [P, I, C.c_int64, I, I, I],
     "gbvr_paint_path": [P, C.POINTER(View), I, C.POINTER(C.c_int32), U64P, U64P],
@@ -257,7 +259,8 @@ _lib = None
 
 
 # functions that return something other than a status
-RESTYPES = {"gbvr_lz4_bound": SZ, "gbvr_lz4_compress": SZ, "gbvr_zlib_bound": SZ, "gbvr_zlib_compress": SZ}
+RESTYPES = {"gbvr_lz4_bound": SZ, "gbvr_lz4_compress": SZ, "gbvr_zlib_bound": SZ, "gbvr_zlib_compress": SZ,
+            "gbvr_hilbert3": C.c_uint64}
 
 
 def lib():

@@ -19,7 +19,7 @@ DRIVER = os.path.join(HERE, "gbvr_batch")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 CUDA_UNITS = ["kernels_render.cu", "kernels_build.cu", "gbvr_api.cu", "noalloc.cu", "tf2d.cu"]
-HOST_UNITS = ["uvf.cpp", "uvf_api.cpp", "image_io.cpp", "lz4.cpp", "deflate.cpp"]
+HOST_UNITS = ["uvf.cpp", "uvf_api.cpp", "image_io.cpp", "lz4.cpp", "deflate.cpp", "brick_order.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -27,6 +27,7 @@
 #include "abi_guard.h"
 #include "gbvr_internal.h"
 #include "deflate.h"
+#include "brick_order.h"
 #include "lz4.h"
 #include "synth_tables.h"
 #include "uvf.h"
@@ -276,6 +277,8 @@ struct Dataset {
   // The compressed store is a list of page-locked segments (a brick's run
   // lies in one): segment host_cseg[b], byte host_coff[b].
   int compression = 0;
+  int brick_order = 0;            // host store: order of each level's bricks (0 scanline, 1 Morton, 2 Hilbert, 3 random)
+  std::vector<int> store_order;   // the bricks in host-store order, level by level
   std::vector<void*> seg_p;
   std::vector<size_t> seg_used;
   std::vector<int> host_cseg;
@@ -702,6 +705,25 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
   ds.slot_of.assign(nb, -1);
   ds.slot_brick.assign(ds.nslots, -1);
   ds.slot_used.assign(ds.nslots, 0);
+  // the bricks' order in the host store (the converter's brick layouts)
+  ds.brick_order = bp ? bp->brick_order : 0;
+  ds.store_order.clear();
+  for (const Level& L : ds.levels) {
+    std::vector<int> perm;
+    if (!brick_order(L.nb, ds.brick_order, 0x5eedull + (uint64_t)L.brick_base, perm))
+      return fail(GBVR_EINVAL, "brick order must be 0 (scanline), 1 (Morton), 2 (Hilbert) or 3 (random)");
+    for (int k : perm) ds.store_order.push_back(L.brick_base + k);
+  }
+  if (ds.brick_order) {
+    // the same extents (each brick's share of the cursor), laid out in store order
+    std::vector<unsigned long long> ext(nb);
+    for (size_t i = 0; i < nb; ++i) ext[i] = (i + 1 < nb ? ds.host_off[i + 1] : cursor) - ds.host_off[i];
+    unsigned long long at = 0;
+    for (int bi : ds.store_order) {
+      ds.host_off[(size_t)bi] = at;
+      at += ext[(size_t)bi];
+    }
+  }
   for (auto& b : ds.bricks) b.offset = 0;
   ds.compression = bp ? bp->compression : 0;
   if (ds.compression != 0 && ds.compression != 1 && ds.compression != 3)
@@ -915,6 +937,31 @@ int build_ooc_synth(Dataset& ds, const gbvr_synth_params* p, const gbvr_brick_pa
   for (int l = 0; l < nlev; ++l)
     if (st[l].next_bz != ds.levels[l].nb[2] || st[l].next_cz != ds.levels[l].nc[2])
       return fail(GBVR_ECUDA, "out-of-core build did not complete level " + std::to_string(l));
+  if (ds.compression && ds.brick_order) {
+    // the compressed runs were appended layer by layer: lay them out again
+    // in store order, so that bricks adjacent in that order are adjacent in
+    // the segments
+    std::vector<void*> old_p;
+    std::vector<size_t> old_used;
+    old_p.swap(ds.seg_p);
+    old_used.swap(ds.seg_used);
+    const std::vector<int> old_seg = ds.host_cseg;
+    const std::vector<unsigned long long> old_off = ds.host_coff;
+    ds.comp_store_bytes = 0;
+    int rc = GBVR_OK;
+    for (int bi : ds.store_order) {
+      const BrickInfo& b = ds.bricks[(size_t)bi];
+      const size_t nbytes = (size_t)b.sx * b.sy * b.sz * es;
+      const unsigned nck = (unsigned)((nbytes + LZ_CHUNK - 1) / LZ_CHUNK);
+      size_t run = 0;
+      for (unsigned k = 0; k < nck; ++k) run += ds.chunk_size[ds.chunk_first[(size_t)bi] + k] & 0x7fffffffu;
+      rc = seg_append((const uint8_t*)old_p[(size_t)old_seg[(size_t)bi]] + old_off[(size_t)bi], run,
+                      ds.host_cseg[(size_t)bi], ds.host_coff[(size_t)bi]);
+      if (rc != GBVR_OK) break;
+    }
+    for (void* q : old_p) cudaFreeHost(q);
+    if (rc != GBVR_OK) return rc;
+  }
   if (ds.compression) {
     if (h_layer.p) cudaFreeHost(h_layer.p);
     h_layer.p = nullptr;
@@ -1304,6 +1351,7 @@ struct gbvr_renderer {
   std::vector<char> occ_valid;
   uint64_t last_misses = 0, last_paged = 0;
   uint64_t last_paged_comp = 0;  // compressed store: bytes copied host to device by the last paint
+  uint64_t last_host_copies = 0; // out of core: host-to-device brick copies of the last paint
   float last_page_ms = 0.f;
   long long cell_words = 0;
   PinnedBuf h_frames, h_prefix;
@@ -1763,9 +1811,14 @@ struct PtrSnapshot {
 // Out of core, compressed store: the compressed runs of the paged bricks
 // (brick, slot) to the device staging, then one decode of all their chunks
 // into the slots, both on the copy stream.  comp_bytes: bytes copied.
-int page_compressed(gbvr_renderer* r, const std::vector<std::pair<int, int>>& paged, uint64_t& comp_bytes) {
+int page_compressed(gbvr_renderer* r, std::vector<std::pair<int, int>>& paged, uint64_t& comp_bytes) {
   Dataset& ds = r->ds;
   const size_t es = dtype_size(ds.dtype);
+  // in store order, so that bricks adjacent in the store go in one copy
+  std::sort(paged.begin(), paged.end(), [&](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+    const int sx = ds.host_cseg[(size_t)x.first], sy = ds.host_cseg[(size_t)y.first];
+    return sx != sy ? sx < sy : ds.host_coff[(size_t)x.first] < ds.host_coff[(size_t)y.first];
+  });
   // compressed runs to the device staging, then one decode of all their
   // chunks into the slots (both on the copy stream)
   std::vector<Lz4Chunk> jobs;
@@ -1792,8 +1845,7 @@ int page_compressed(gbvr_renderer* r, const std::vector<std::pair<int, int>>& pa
   }
   CUDA_TRY(ds.d_stage.alloc(std::max<size_t>(total, 16)));
   CUDA_TRY(ds.d_chunks.alloc(sizeof(Lz4Chunk) * jobs.size()));
-  // bricks page in index order and the store holds them in build order, so
-  // runs of consecutive bricks are adjacent: one copy per adjacent stretch
+  // bricks page in store order: one copy per stretch of adjacent runs
   size_t at = 0, cp_at = 0, cp_n = 0;
   const uint8_t* cp_src = nullptr;
   for (size_t q = 0; q < paged.size(); ++q) {
@@ -1801,16 +1853,20 @@ int page_compressed(gbvr_renderer* r, const std::vector<std::pair<int, int>>& pa
     if (cp_n && h == cp_src + cp_n) {
       cp_n += run[q];
     } else {
-      if (cp_n)
+      if (cp_n) {
         CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + cp_at, cp_src, cp_n, cudaMemcpyHostToDevice, r->copy_stream));
+        ++r->last_host_copies;
+      }
       cp_src = h;
       cp_at = at;
       cp_n = run[q];
     }
     at += run[q];
   }
-  if (cp_n)
+  if (cp_n) {
     CUDA_TRY(cudaMemcpyAsync((char*)ds.d_stage.p + cp_at, cp_src, cp_n, cudaMemcpyHostToDevice, r->copy_stream));
+    ++r->last_host_copies;
+  }
   // pageable source: the copy returns once it is staged
   CUDA_TRY(cudaMemcpyAsync(ds.d_chunks.p, jobs.data(), sizeof(Lz4Chunk) * jobs.size(), cudaMemcpyHostToDevice,
                            r->copy_stream));
@@ -1991,6 +2047,7 @@ int ooc_page(gbvr_renderer* r, const gbvr_view* views, int n, int& level, uint64
       CUDA_TRY(cudaMemcpyAsync((char*)ds.pool.p + (size_t)sl * ds.slot_elems * es,
                                (const char*)ds.host_store.p + ds.host_off[bidx] * es, nbytes, cudaMemcpyHostToDevice,
                                r->copy_stream));
+      ++r->last_host_copies;
     }
     bytes += nbytes;
   }
@@ -2080,6 +2137,7 @@ int prepare(gbvr_renderer* r, int nviews, int& level, const gbvr_view* views) {
     }
     // every earlier paint has finished (paints are synchronous): no slot is in use
     r->last_paged_comp = 0;
+    r->last_host_copies = 0;
     TRY(ooc_page(r, views, views == vs.data() ? 1 : nviews, level, 0, nullptr, 0, &r->last_misses, &r->last_paged,
                  r->slice_sel));
     CUDA_TRY(cudaEventSynchronize(r->ev_c1[0]));
@@ -2256,6 +2314,7 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
   }
   TRY(ooc_streams(r));
   r->last_paged_comp = 0;
+  r->last_host_copies = 0;
   const size_t npix = (size_t)r->width * r->height;
   if (r->fb_views < n || r->fb_w != r->width || r->fb_h != r->height) {
     CUDA_TRY(r->d_fb8.alloc(npix * 4 * n));
@@ -3428,6 +3487,7 @@ int gbvr_get_stats(gbvr_renderer* r, gbvr_stats* out) {
   out->brick_misses = r->last_misses;
   out->bytes_paged = r->last_paged;
   out->bytes_paged_compressed = r->last_paged_comp;
+  out->host_copies = r->last_host_copies;
   out->page_ms = r->last_page_ms;
   if (r->last_views < 1 || !r->ds.loaded) return GBVR_OK;
   const int n = r->last_views;

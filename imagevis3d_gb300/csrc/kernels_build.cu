@@ -1249,17 +1249,20 @@ __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X
 // practice, go to global memory directly.  Blocks loop over groups of
 // blockDim columns.  Runs of equal bins along a thread's voxels are counted
 // in registers first either way.
-template <typename T, bool SMEM>
-__global__ void __launch_bounds__(256, 3) k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx,
-                                                 int merge, unsigned long long* __restrict__ hist,
-                                                 const Hist2DScratch* sc, int flush_steps, int kshared) {
+// WIDE: 32-bit shared counters, one per bin (one 768-thread block per SM with
+// about 200 KB of them), flushed only when a counter could overflow, i.e. in
+// practice once at the end, instead of 16-bit pairs flushed every 63 z-steps.
+template <typename T, bool SMEM, bool WIDE = false>
+__global__ void __launch_bounds__(WIDE ? 768 : 256, WIDE ? 1 : 3)
+    k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx, int merge,
+              unsigned long long* __restrict__ hist, const Hist2DScratch* sc, int flush_steps, int kshared) {
   extern __shared__ unsigned sh[];
   const unsigned long long smax = sc->smax;
   const double gmax = __longlong_as_double((long long)sc->gmax_bits);
   const float smax_f = (float)smax;
   const float inv_smax = 1.f / smax_f;  // the estimate below needs to be within one bin only
   const unsigned merge32 = (unsigned)merge;
-  const int words = nx * kshared / 2;  // kshared is even
+  const int words = WIDE ? nx * kshared : nx * kshared / 2;  // kshared is even
   if (SMEM) {
     for (int i = threadIdx.x; i < words; i += blockDim.x) sh[i] = 0;
     __syncthreads();
@@ -1269,7 +1272,8 @@ __global__ void __launch_bounds__(256, 3) k_h2v_bin(const T* __restrict__ v, int
     const unsigned k = bin & 255u;
     if (SMEM && k < (unsigned)kshared) {
       const unsigned sb = (bin >> 8) * (unsigned)kshared + k;
-      atomicAdd(sh + (sb >> 1), cnt << ((sb & 1u) << 4));
+      if (WIDE) atomicAdd(sh + sb, cnt);
+      else atomicAdd(sh + (sb >> 1), cnt << ((sb & 1u) << 4));
     } else {
       atomicAdd(hist + bin, (unsigned long long)cnt);
     }
@@ -1282,9 +1286,14 @@ __global__ void __launch_bounds__(256, 3) k_h2v_bin(const T* __restrict__ v, int
     for (int i = threadIdx.x; i < words; i += blockDim.x) {
       const unsigned wv = sh[i];
       if (wv) {
-        const unsigned sb = 2u * i, bx = sb / (unsigned)kshared, k = sb - bx * (unsigned)kshared;  // k even
-        if (wv & 0xffffu) atomicAdd(hist + bx * 256u + k, (unsigned long long)(wv & 0xffffu));
-        if (wv >> 16) atomicAdd(hist + bx * 256u + k + 1, (unsigned long long)(wv >> 16));
+        if (WIDE) {
+          const unsigned bx = (unsigned)i / (unsigned)kshared, k = (unsigned)i - bx * (unsigned)kshared;
+          atomicAdd(hist + bx * 256u + k, (unsigned long long)wv);
+        } else {
+          const unsigned sb = 2u * i, bx = sb / (unsigned)kshared, k = sb - bx * (unsigned)kshared;  // k even
+          if (wv & 0xffffu) atomicAdd(hist + bx * 256u + k, (unsigned long long)(wv & 0xffffu));
+          if (wv >> 16) atomicAdd(hist + bx * 256u + k + 1, (unsigned long long)(wv >> 16));
+        }
         sh[i] = 0;
       }
     }
@@ -1369,26 +1378,30 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
       ColMax* cols = nullptr;
       e = cudaMallocAsync(reinterpret_cast<void**>(&cols), (size_t)ncols * sizeof(ColMax), s);
       if (e != cudaSuccess) return e;
-      // shared counters for the gradient rows k < kshared: 2 bytes per bin, ~48 KB
-      const int kshared = (int)std::min<long long>(256, (49152 / (2 * nx)) & ~1LL);
+      // shared counters for the gradient rows k < kshared: 32 bits per bin in
+      // about 200 KB for one 768-thread block per SM (the same 24 warps per SM
+      // as three 256-thread blocks at the kernel's 80 registers); a block adds
+      // at most 4 * 768 voxels per z-step, so counters flush before 2^32
+      constexpr int wide_threads = 768;
+      const int kshared = (int)std::min<long long>(256, ((200 * 1024) / (4 * nx)) & ~1LL);
       const bool smem = kshared >= 2;
-      const size_t shbytes = smem ? (size_t)nx * kshared * 2 : 0;
-      // a block adds 4 * threads voxels per z-step to its shared counters
-      const int flush_steps = 65535 / (4 * threads);
-      const int per_sm = smem ? (int)std::max<size_t>(1, std::min<size_t>(2048 / threads, (227 * 1024) / shbytes)) : 0;
-      const int grid2 = smem ? (int)std::min<long long>(blocks, (long long)sms * per_sm) : (int)blocks;
+      const size_t shbytes = smem ? (size_t)nx * kshared * 4 : 0;
+      const int flush_steps = (int)std::min<long long>(0x7fffffffLL, 0xffffffffLL / (4 * wide_threads));
+      const long long wblocks = (ncols + wide_threads - 1) / wide_threads;
+      const int grid2 = smem ? (int)std::min<long long>(wblocks, (long long)sms) : (int)blocks;
       const int nxi = (int)nx, mi = (int)merge, Xi = (int)X, Yi = (int)Y, Zi = (int)Z;
       if (dtype == DT_U8) {
         const uint8_t* v = (const uint8_t*)vol;
         k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch, cols);
         k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch, cols);
         if (smem) {
-          e = cudaFuncSetAttribute(k_h2v_bin<uint8_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
+          e = cudaFuncSetAttribute(k_h2v_bin<uint8_t, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
           if (e != cudaSuccess) {
             cudaFreeAsync(cols, s);
             return e;
           }
-          k_h2v_bin<uint8_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps, kshared);
+          k_h2v_bin<uint8_t, true, true><<<grid2, wide_threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps,
+                                                                         kshared);
         } else {
           k_h2v_bin<uint8_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0, 0);
         }
@@ -1397,12 +1410,13 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
         k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch, cols);
         k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch, cols);
         if (smem) {
-          e = cudaFuncSetAttribute(k_h2v_bin<uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
+          e = cudaFuncSetAttribute(k_h2v_bin<uint16_t, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
           if (e != cudaSuccess) {
             cudaFreeAsync(cols, s);
             return e;
           }
-          k_h2v_bin<uint16_t, true><<<grid2, threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps, kshared);
+          k_h2v_bin<uint16_t, true, true><<<grid2, wide_threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps,
+                                                                         kshared);
         } else {
           k_h2v_bin<uint16_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0, 0);
         }

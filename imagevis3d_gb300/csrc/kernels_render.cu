@@ -1148,9 +1148,10 @@ constexpr int RENDER_THREADS = 128;
 // Resident CTAs per SM each mode's kernels are compiled for (registers =
 // 65536 / (128 x this)): the 1D TF and MIP walks 10 (48 registers; measured
 // ahead of 6, 8 and 12); the 2D TF path 6 (80 registers: it keeps a sample's
-// 8 voxels and 12 tap offsets for its gradient); the isosurface path 8 (64).
+// 8 voxels and 12 tap offsets for its gradient; 7 spills and is 5 % slower);
+// the isosurface path 7 (72 registers, no spills; 1.5 % ahead of 8 at 64).
 template <int MODE>
-constexpr int uniform_ctas_per_sm() { return (MODE == MODE_1D || MODE == MODE_MIP) ? 10 : (MODE == MODE_2D ? 6 : 8); }
+constexpr int uniform_ctas_per_sm() { return (MODE == MODE_1D || MODE == MODE_MIP) ? 10 : (MODE == MODE_2D ? 6 : 7); }
 // Two samples per step keep two samples' voxels live, and warp-shared
 // sampling (4, 8) keeps a task's owner data live: 8 CTAs/SM (64 registers).
 template <int MODE, int SPS>

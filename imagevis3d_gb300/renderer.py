@@ -23,8 +23,10 @@ def _fp(a):
 
 
 def brick_params(brick_size=256, overlap=2, max_lods=0, build_texture=False, layouts=1,
-                 aspect=(1, 1, 1), compression=0):
-    """compression: out-of-core host store codec, 0 raw or 3 (LZ4)."""
+                 aspect=(1, 1, 1), compression=0, brick_order=0):
+    """compression: out-of-core host store codec, 0 raw, 1 zlib or 3 (LZ4);
+    brick_order: the host store's order of each level's bricks, 0 scanline,
+    1 Morton, 2 Hilbert, 3 random."""
     bp = L.BrickParams()
     bp.brick_size = brick_size
     bp.overlap = overlap
@@ -32,6 +34,7 @@ def brick_params(brick_size=256, overlap=2, max_lods=0, build_texture=False, lay
     bp.build_texture = 1 if build_texture else 0
     bp.layouts = layouts
     bp.compression = compression
+    bp.brick_order = brick_order
     for i in range(3):
         bp.aspect[i] = aspect[i]
     return bp

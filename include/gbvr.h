@@ -102,6 +102,11 @@ typedef struct gbvr_brick_params {
                            CT_ZLIB and CT_LZ4, UVFReader/BlockInfo.h:60-93; zlib is the
                            converter's default, CmdLineConverter/main.cpp:146): 16 KiB chunks
                            compressed by host threads at build, decoded on the GPU when paged */
+  int32_t brick_order;  /* out-of-core host store: order of the bricks of each level (the
+                           converter's -bricklayout, CmdLineConverter/main.cpp:175-178): 0
+                           scanline (brick index), 1 Morton, 2 Hilbert, 3 random (seeded);
+                           a paint copies each stretch of adjacent missing bricks at once */
+  int32_t reserved;     /* 0 */
   double aspect[3];     /* voxel spacing; 0 = (1,1,1) */
 } gbvr_brick_params;
 
@@ -147,7 +152,17 @@ typedef struct gbvr_stats {
   uint64_t cell_bytes;         /* ... times the cell's voxel bytes (4^3 voxels) */
   double page_ms;              /* out of core: device time of the last paint's brick uploads */
   uint64_t bytes_paged_compressed; /* out of core, compressed store: host->device bytes of those bricks */
+  uint64_t host_copies;        /* out of core: host->device copies that brought those bricks */
 } gbvr_stats;
+
+/* ---- brick orders (the converter's -bricklayout, CmdLineConverter/main.cpp:175-178) ----
+ * gbvr_brick_order: the bricks of an nb[0] x nb[1] x nb[2] grid (index
+ * (z ny + y) nx + x) in storage order for order 0 scanline, 1 Morton, 2 Hilbert
+ * (positions along the curve of the enclosing power-of-two cube), 3 random
+ * (seeded): perm[k] = the brick stored k-th.  gbvr_hilbert3: the position of
+ * (x, y, z) along the 3D Hilbert curve of a 2^bits cube. */
+int gbvr_brick_order(const int32_t nb[3], int32_t order, uint64_t seed, int32_t* perm, size_t n);
+uint64_t gbvr_hilbert3(uint32_t x, uint32_t y, uint32_t z, int32_t bits);
 
 /* ---- errors / device ---- */
 int gbvr_last_error(char* buf, size_t size);

@@ -13,7 +13,7 @@ from tests.conftest import ROOT
 def declared_functions():
     text = open(os.path.join(ROOT, "include", "gbvr.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|size_t)\s+(gbvr_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|uint64_t)\s+(gbvr_\w+)\s*\(", text, flags=re.M)))
 
 
 def test_every_declared_symbol_is_exported_and_bound():

@@ -349,3 +349,44 @@ def test_ooc_compression_shrinks_smooth_volumes(codec):
         r.loadSyntheticOutOfCore(sp, 1 << 28, brick_size=64, overlap=2, compression=codec)
         info = r.datasetInfo()
     assert info["host_bytes"] * 2 < info["host_raw_bytes"]
+
+
+@pytest.mark.parametrize("order", [1, 2, 3], ids=["morton", "hilbert", "random"])
+@pytest.mark.parametrize("codec", [0, 3], ids=["raw", "lz4"])
+def test_ooc_store_orders_page_the_same_bricks(order, codec):
+    """Every host-store brick order (the converter's brick layouts: Morton,
+    Hilbert, random) holds and pages the same bricks as the scanline order:
+    a fly-through gives the same images bit for bit, raw or compressed, and
+    each paint's host-to-device copies are counted (one per stretch of bricks
+    adjacent in the store)."""
+    sp, bp = CASES["u16_200x180x170_b64"]
+    slot = (bp["brick_size"] ** 3) * 2
+    views = _inside_path(6, 128, 96)
+    with Renderer(float_fb=True) as a, Renderer(float_fb=True) as b:
+        a.loadSyntheticOutOfCore(sp, 30 * slot, compression=codec, **bp)
+        b.loadSyntheticOutOfCore(sp, 30 * slot, compression=codec, brick_order=order, **bp)
+        ia, ib = a.datasetInfo(), b.datasetInfo()
+        assert ia["host_bytes"] == ib["host_bytes"] > 0
+        for lod in range(ia["lod_count"]):
+            nb = ia["lod_bricks"][lod]
+            for k in range(0, nb[0] * nb[1] * nb[2], 3):
+                bx, by, bz = k % nb[0], (k // nb[0]) % nb[1], k // (nb[0] * nb[1])
+                va, oa = a.getBrick(lod, (bx, by, bz))
+                vb, ob = b.getBrick(lod, (bx, by, bz))
+                assert oa == ob and np.array_equal(va, vb), (lod, bx, by, bz)
+        for r in (a, b):
+            _setup(r, sp, 128, 96)
+        la, _, pa = a.paintPath(views)
+        lb, _, pb = b.paintPath(views)
+        assert np.array_equal(la, lb) and np.array_equal(pa, pb)
+        for i in range(len(views)):
+            assert np.array_equal(a.readFramebuffer(i, as_float=True), b.readFramebuffer(i, as_float=True)), i
+        a.setView(*views[2])
+        b.setView(*views[2])
+        a.paint()
+        b.paint()
+        assert np.array_equal(a.readFramebuffer(0, as_float=True), b.readFramebuffer(0, as_float=True))
+        sa, sb = a.stats(), b.stats()
+        assert sa["brick_misses"] == sb["brick_misses"] and sa["bytes_paged"] == sb["bytes_paged"]
+        for st in (sa, sb):
+            assert (st["host_copies"] > 0) == (st["bytes_paged"] > 0)

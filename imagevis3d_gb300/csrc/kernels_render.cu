@@ -660,6 +660,46 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
     BrickView b;
     int bi = -1, bke = 0;  // current brick and the end of the ray's run in it
     const int sh = f.cell_shift;
+    if constexpr (MODE == MODE_MIP) {
+      if (f.empty_skip >= 2) {
+        // Largest cell first: walk the ray's macro-cells reading only their
+        // maxima and sample the cell with the largest one (in a brick the walk
+        // samples at all).  The walk below then starts from that cell's
+        // largest sample and leaves every cell and brick that cannot exceed
+        // it.  The maximum is over the same samples, so it is the same value.
+        float best = -INFINITY;
+        int b0 = 0, b1 = 0;
+        for (int kk = k; kk < K;) {
+          float qx, qy, qz;
+          pos_of(kk, qx, qy, qz);
+          const int cx = max(clamp_cell(qx, f.dims[0]), 0) >> sh, cy = max(clamp_cell(qy, f.dims[1]), 0) >> sh,
+                    cz = max(clamp_cell(qz, f.dims[2]), 0) >> sh;
+          const float cm = __ldg(&f.cells[((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx].y);
+          const float kef = ceilf(exit_k(r.dv[0] > 0.f ? min((cx + 1) << sh, f.dims[0]) : cx << sh,
+                                         r.dv[1] > 0.f ? min((cy + 1) << sh, f.dims[1]) : cy << sh,
+                                         r.dv[2] > 0.f ? min((cz + 1) << sh, f.dims[2]) : cz << sh));
+          const int ke = kef >= (float)K ? K : max(kk + 1, (int)kef);
+          if (cm > best) {
+            best = cm;
+            b0 = kk;
+            b1 = ke;
+          }
+          kk = ke;
+        }
+        for (int kk = b0; kk < b1; ++kk) {
+          float qx, qy, qz;
+          pos_of(kk, qx, qy, qz);
+          const Cell c = make_cell(f, qx, qy, qz);
+          const int bj = brick_index(f, c.x, c.y, c.z);
+          if (f.empty_skip >= 1 && __ldg(f.skip + bj)) continue;
+          BrickView bv;
+          load_brick(f, bj, bv);
+          ++nsamp;
+          runmax = fmaxf(runmax, sample_cell<T, SAMPLER>(f, bv, c.x, c.y, c.z, c.fx, c.fy, c.fz));
+        }
+        if (runmax >= f.level_max) done = true;
+      }
+    }
     while (k < K && !done) {
       float px, py, pz;
       pos_of(k, px, py, pz);

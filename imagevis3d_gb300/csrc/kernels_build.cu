@@ -604,9 +604,15 @@ __global__ void k_cell_minmax(const T* __restrict__ v, long long X, long long Y,
 // voxel values.  Each voxel is read from memory about 1.6 times instead of
 // 5.4, with one 64-bit row address per row.
 template <typename T> struct CellTile {
-  static constexpr int CX = 15;
+  static constexpr int CX = 15;  // 16-bit voxels: rows of 63 voxels, two warp-wide loads or one of words
   __device__ static T mn(T a, T b) { return a < b ? a : b; }
   __device__ static T mx(T a, T b) { return a > b ? a : b; }
+};
+// 8-bit voxels: rows of 127 voxels, so the halo is a smaller share
+template <> struct CellTile<uint8_t> {
+  static constexpr int CX = 31;
+  __device__ static uint8_t mn(uint8_t a, uint8_t b) { return a < b ? a : b; }
+  __device__ static uint8_t mx(uint8_t a, uint8_t b) { return a > b ? a : b; }
 };
 // float: fminf / fmaxf from +inf / -inf, as k_cell_minmax (NaN voxels are
 // passed over)
@@ -634,11 +640,12 @@ __global__ void __launch_bounds__(256) k_cell_minmax_tiled(const T* __restrict__
   // not write
   const long long zlo = max(4LL * cz0 - 1, 0LL), zhi = min(4LL * cz1 + 1, Z - 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // a row is at most two warp-wide loads (VX <= 64); four rows per step so
-  // that eight loads of a lane are in flight together
-  static_assert(VX <= 64, "a tile row is at most two warps wide");
-  const int xa = (int)min(max(vx0 + lane, 0LL), X - 1), xb = (int)min(max(vx0 + lane + 32, 0LL), X - 1);
-  const bool hb = lane + 32 < VX;
+  // four rows per step, so that several loads of a lane are in flight together
+  constexpr int NXL = (VX + 31) / 32;  // loads per lane and row
+  static_assert(NXL <= 4, "a tile row is at most four warps wide");
+  int xcol[NXL];
+#pragma unroll
+  for (int q = 0; q < NXL; ++q) xcol[q] = (int)min(max(vx0 + lane + 32 * q, 0LL), X - 1);
   constexpr int ROWS = CV_Y * CV_Z;
   // 16-bit voxels of a tile inside the level, rows of 4-byte-aligned words:
   // VPL voxels per load, from the word holding voxel vx0 on (lane l loads
@@ -671,10 +678,12 @@ __global__ void __launch_bounds__(256) k_cell_minmax_tiled(const T* __restrict__
       const int ly = row % CV_Y, lz = row / CV_Y;
       const long long y = min(max(vy0 + ly, 0LL), Y - 1), z = min(max(vzz0 + lz, zlo), zhi);
       const T* src = v + ((z - vz0) * Y + y) * X;
-      const T a = __ldg(src + xa);
-      const T b = hb ? __ldg(src + xb) : T(0);
-      if (lane < VX) tile[lz][ly][lane] = a;
-      if (hb) tile[lz][ly][lane + 32] = b;
+      T val[NXL];
+#pragma unroll
+      for (int q = 0; q < NXL; ++q) val[q] = lane + 32 * q < VX ? __ldg(src + xcol[q]) : T(0);
+#pragma unroll
+      for (int q = 0; q < NXL; ++q)
+        if (lane + 32 * q < VX) tile[lz][ly][lane + 32 * q] = val[q];
     }
   }
   __syncthreads();
@@ -728,7 +737,8 @@ cudaError_t launch_cell_minmax_layers(const void* level, int dtype, const long l
   const long long n = (long long)nc[0] * nc[1] * (cz1 - cz0);
   if (n <= 0) return cudaSuccess;
   if (sh == 2) {
-    const int cx = dtype == DT_F32 ? CellTile<float>::CX : CellTile<uint8_t>::CX;
+    const int cx = dtype == DT_F32 ? CellTile<float>::CX : dtype == DT_U8 ? CellTile<uint8_t>::CX
+                                                                            : CellTile<uint16_t>::CX;
     const int tiles_x = (nc[0] + cx - 1) / cx, tiles_y = (nc[1] + CT_Y - 1) / CT_Y,
               tiles_z = (cz1 - cz0 + CT_Z - 1) / CT_Z;
     const long long nt = (long long)tiles_x * tiles_y * tiles_z;

@@ -661,32 +661,66 @@ __device__ float4 march(const FrameDesc& f, const RaySetup& r, unsigned& nsamp, 
     int bi = -1, bke = 0;  // current brick and the end of the ray's run in it
     const int sh = f.cell_shift;
     if constexpr (MODE == MODE_MIP) {
-      if (f.empty_skip >= 2) {
-        // Largest cell first: walk the ray's macro-cells reading only their
-        // maxima and sample the cell with the largest one (in a brick the walk
-        // samples at all).  The walk below then starts from that cell's
-        // largest sample and leaves every cell and brick that cannot exceed
-        // it.  The maximum is over the same samples, so it is the same value.
+      if (f.empty_skip >= 2 && f.smax) {
+        // Largest cell first: walk the ray's super-cells (4^3 macro-cells),
+        // jumping over bricks the walk skips or that cannot hold a larger
+        // maximum, reading only their maxima; then
+        // the macro-cells of the ray's stretch through the best one; then
+        // sample the best macro-cell.  The walk below starts from its largest
+        // sample and leaves every cell and brick that cannot exceed it.  The
+        // maximum is over the same samples, so it is the same value.
+        constexpr int SS = SUPERCELL_SHIFT;
+        const int s2 = sh + SS;
+        auto exit_of = [&](int kk, int lx, int ly, int lz, int hx, int hy, int hz) {
+          const float kef = ceilf(exit_k(r.dv[0] > 0.f ? hx : lx, r.dv[1] > 0.f ? hy : ly, r.dv[2] > 0.f ? hz : lz));
+          return kef >= (float)K ? K : max(kk + 1, (int)kef);
+        };
         float best = -INFINITY;
         int b0 = 0, b1 = 0;
         for (int kk = k; kk < K;) {
           float qx, qy, qz;
           pos_of(kk, qx, qy, qz);
-          const int cx = max(clamp_cell(qx, f.dims[0]), 0) >> sh, cy = max(clamp_cell(qy, f.dims[1]), 0) >> sh,
-                    cz = max(clamp_cell(qz, f.dims[2]), 0) >> sh;
-          const float cm = __ldg(&f.cells[((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx].y);
-          const float kef = ceilf(exit_k(r.dv[0] > 0.f ? min((cx + 1) << sh, f.dims[0]) : cx << sh,
-                                         r.dv[1] > 0.f ? min((cy + 1) << sh, f.dims[1]) : cy << sh,
-                                         r.dv[2] > 0.f ? min((cz + 1) << sh, f.dims[2]) : cz << sh));
-          const int ke = kef >= (float)K ? K : max(kk + 1, (int)kef);
-          if (cm > best) {
-            best = cm;
+          const int gx = clamp_cell(qx, f.dims[0]), gy = clamp_cell(qy, f.dims[1]), gz = clamp_cell(qz, f.dims[2]);
+          const int bx = brick_col(f, gx, f.nb[0]), by = brick_col(f, gy, f.nb[1]), bz = brick_col(f, gz, f.nb[2]);
+          const int bj = (bz * f.nb[1] + by) * f.nb[0] + bx;
+          // a brick the walk skips, or whose largest voxel cannot beat the
+          // best super-cell so far, is crossed in one step
+          if ((f.empty_skip >= 1 && __ldg(f.skip + bj)) || __ldg(&f.bricks[bj].vmax) <= best) {
+            const int I = f.interior;
+            kk = exit_of(kk, bx * I, by * I, bz * I, min(bx * I + I, f.dims[0]), min(by * I + I, f.dims[1]),
+                         min(bz * I + I, f.dims[2]));
+            continue;
+          }
+          const int sx = max(gx, 0) >> s2, sy = max(gy, 0) >> s2, sz = max(gz, 0) >> s2;
+          const float sm = __ldg(f.smax + ((size_t)sz * f.nsc[1] + sy) * f.nsc[0] + sx);
+          const int ke = exit_of(kk, sx << s2, sy << s2, sz << s2, min((sx + 1) << s2, f.dims[0]),
+                                 min((sy + 1) << s2, f.dims[1]), min((sz + 1) << s2, f.dims[2]));
+          if (sm > best) {
+            best = sm;
             b0 = kk;
             b1 = ke;
           }
           kk = ke;
         }
-        for (int kk = b0; kk < b1; ++kk) {
+        best = -INFINITY;
+        int c0 = 0, c1 = 0;
+        for (int kk = b0; kk < b1;) {
+          float qx, qy, qz;
+          pos_of(kk, qx, qy, qz);
+          const int cx = max(clamp_cell(qx, f.dims[0]), 0) >> sh, cy = max(clamp_cell(qy, f.dims[1]), 0) >> sh,
+                    cz = max(clamp_cell(qz, f.dims[2]), 0) >> sh;
+          const float cm = __ldg(&f.cells[((size_t)cz * f.nc[1] + cy) * f.nc[0] + cx].y);
+          const int ke = min(exit_of(kk, cx << sh, cy << sh, cz << sh, min((cx + 1) << sh, f.dims[0]),
+                                     min((cy + 1) << sh, f.dims[1]), min((cz + 1) << sh, f.dims[2])),
+                             b1);
+          if (cm > best) {
+            best = cm;
+            c0 = kk;
+            c1 = ke;
+          }
+          kk = ke;
+        }
+        for (int kk = c0; kk < c1; ++kk) {
           float qx, qy, qz;
           pos_of(kk, qx, qy, qz);
           const Cell c = make_cell(f, qx, qy, qz);

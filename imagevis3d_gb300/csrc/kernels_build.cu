@@ -1486,13 +1486,30 @@ cudaError_t launch_hist2d_slab(const void* slab, int dtype, const long long dims
 
 // ---------------------------------------------------------------------------
 // LZ4 block decoding of paged bricks (out-of-core store compressed with the
-// codec of lz4.cpp, one block per 16 KiB chunk of a brick).  One warp per
-// chunk parses each sequence header in lockstep (every read and write bound
-// checked), copies the literals, then the match.  A match reads only
-// output before its start: with offset >= 32 a 32-byte step reads bytes
-// written by earlier steps; a shorter offset repeats its pattern, so byte i
-// of the match is output[start - offset + i mod offset].  __syncwarp orders
-// the lanes' writes between steps.  A malformed block sets *err and stops.
+// codec of lz4.cpp, one block per 16 KiB chunk of a brick), one warp per
+// chunk, every read and write bound checked.
+//
+// Window path (most sequences of brick data: no or few literals, a 2-byte
+// offset, at most one length byte, i.e. 3-4 input bytes for ~30 output
+// bytes): the warp loads the 32 input bytes at the parse position, and every
+// lane decodes the sequence that would start at its byte.  Walking the true
+// starts from lane 0 is one shuffle per sequence; the sequences that lie
+// wholly in the window (up to 10) are then written together, 32 output bytes
+// per step.  A lane finds the sequence of its byte from the sequences'
+// output starts (a prefix sum), and takes a literal from the window, a match
+// byte written by an earlier step from memory, or a match byte of the same
+// step from the lane that writes it (pointer jumping, at most 5 rounds:
+// sources lie before their bytes).
+//
+// Single-sequence path (the block's last sequence, long literal runs,
+// lengths of more than one extension byte, a sequence at the window's end):
+// the warp parses the header in lockstep, copies the literals, then the
+// match.  With offset >= 32 a 32-byte step reads bytes written by earlier
+// steps; a shorter offset repeats its pattern, so byte i of the match is
+// output[start - offset + i mod offset].
+//
+// __syncwarp orders the lanes' writes between steps.  A malformed block sets
+// *err and stops.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restrict__ stage,
                                                     unsigned char* __restrict__ pool,
@@ -1531,9 +1548,113 @@ __global__ void __launch_bounds__(128) k_lz4_decode(const unsigned char* __restr
     if (pos < wbase || pos + 1 >= wbase + 32) refill(pos);
     return __shfl_sync(0xffffffffu, wpair, (int)(pos - wbase)) & 0xffffu;
   };
+  constexpr unsigned FULL = 0xffffffffu;
+  __shared__ unsigned char seq_lane_all[4][32];  // per warp: window byte of its k-th sequence
+  unsigned char* seq_lane = seq_lane_all[threadIdx.x >> 5];
   unsigned ip = 0, op = 0;
   for (;;) {
     if (ip >= n) break;  // malformed: the block ended after a match
+    {
+      // window path: the sequence that would start at this lane's byte
+      const unsigned avail = min(n - ip, 32u);
+      const unsigned wb = lane < avail ? (unsigned)__ldg(in + ip + lane) : 0u;
+      unsigned nl = wb >> 4, ml = wb & 15u, pos = lane + 1;
+      const unsigned e1 = __shfl_sync(FULL, wb, (lane + 1) & 31);
+      bool ok = true;
+      if (nl == 15) {
+        ok = e1 < 255;
+        nl += e1;
+        ++pos;
+      }
+      const unsigned lit_pos = pos;
+      pos += nl;
+      const unsigned o0 = __shfl_sync(FULL, wb, pos & 31), o1 = __shfl_sync(FULL, wb, (pos + 1) & 31);
+      pos += 2;
+      const unsigned e2 = __shfl_sync(FULL, wb, pos & 31);
+      if (ml == 15) {
+        ok = ok && e2 < 255;
+        ml += e2;
+        ++pos;
+      }
+      ml += 4;
+      // wholly inside the input bytes of the window (so never the block's
+      // last sequence, which has no offset)
+      ok = ok && pos <= avail;
+      const unsigned nxt = ok ? pos : 64u;
+      unsigned starts = 0, s = 0;
+      while (s < 32) {  // s is the same in every lane
+        const unsigned t = __shfl_sync(FULL, nxt, s);
+        if (t == 64u) break;
+        starts |= 1u << s;
+        s = t;  // > s
+      }
+      if (starts) {
+        const unsigned nseq = __popc(starts);
+        // ok lanes: nl <= 29, lit_pos <= 30
+        const unsigned info = (o0 | (o1 << 8)) | ((nl & 31u) << 16) | ((lit_pos & 31u) << 21);
+        if ((starts >> lane) & 1u) seq_lane[__popc(starts & ((1u << lane) - 1u))] = (unsigned char)lane;
+        __syncwarp();
+        const unsigned from = lane < nseq ? seq_lane[lane] : 0u;
+        __syncwarp();
+        unsigned sinfo = __shfl_sync(FULL, info, from);
+        unsigned sml = __shfl_sync(FULL, ml, from);
+        if (lane >= nseq) sinfo = sml = 0;
+        const unsigned snl = (sinfo >> 16) & 31u, soff = sinfo & 0xffffu;
+        const unsigned len = snl + sml;
+        unsigned incl = len;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const unsigned y = __shfl_up_sync(FULL, incl, d);
+          if (lane >= (unsigned)d) incl += y;
+        }
+        const unsigned excl = incl - len;  // output start of sequence `lane`, from op
+        const unsigned total = __shfl_sync(FULL, incl, 31);
+        // a match starts inside the output written so far; the output fits the chunk
+        const bool bad = lane < nseq && (soff == 0 || soff > op + excl + snl);
+        if (__any_sync(FULL, bad) || total > raw - op) break;
+        for (unsigned base = 0; base < total; base += 32) {
+          const unsigned q = base + lane;
+          // the sequence holding byte base, then the starts inside (base, base + 32)
+          const unsigned first = __popc(__ballot_sync(FULL, lane < nseq && excl <= base)) - 1u;
+          const bool st = lane < nseq && excl > base && excl < base + 32;
+          const unsigned M = __reduce_or_sync(FULL, st ? 1u << (excl - base) : 0u);
+          const unsigned k = (first + __popc(M & ((2u << lane) - 1u))) & 31u;
+          const unsigned ki = __shfl_sync(FULL, sinfo, k), ke = __shfl_sync(FULL, excl, k);
+          const unsigned r = q - ke, knl = (ki >> 16) & 31u, koff = ki & 0xffffu;
+          const unsigned lit = __shfl_sync(FULL, wb, ((ki >> 21) + r) & 31u);
+          const bool valid = q < total;
+          unsigned val = 0;
+          int ptr = -1;
+          if (valid) {
+            if (r < knl) {
+              val = lit;
+            } else {
+              const int src = (int)q - (int)koff;  // from op; op + src >= 0 by the check above
+              if (src < (int)base) val = out[(int)op + src];
+              else ptr = src - (int)base;  // a lane below this one
+            }
+          }
+          while (__any_sync(FULL, ptr >= 0)) {
+            const unsigned pv = __shfl_sync(FULL, val, ptr & 31);
+            const int pp = __shfl_sync(FULL, ptr, ptr & 31);
+            if (ptr >= 0) {
+              if (pp < 0) {
+                val = pv;
+                ptr = -1;
+              } else {
+                ptr = pp;
+              }
+            }
+          }
+          if (valid) out[op + q] = (unsigned char)val;
+          __syncwarp();
+        }
+        op += total;
+        ip += s;
+        continue;
+      }
+    }
+    // single-sequence path
     const unsigned token = byte_at(ip++);
     unsigned nlit = token >> 4;
     bool bad = false;

@@ -63,7 +63,7 @@ def reference(block):
             out.append(out[-off])
 
 
-def crafted(seed, offsets, lengths, n_seq, head=700):
+def crafted(seed, offsets, lengths, n_seq, head=700, lits=(0, 1, 3, 14, 15, 16, 40, 300)):
     rng = np.random.default_rng(seed)
     block = b""
     out_len = 0
@@ -71,7 +71,7 @@ def crafted(seed, offsets, lengths, n_seq, head=700):
     first = True
     for _ in range(n_seq):
         if not first:
-            lit = rng.integers(0, 256, int(rng.choice([0, 1, 3, 14, 15, 16, 40, 300])), dtype=np.uint8).tobytes()
+            lit = rng.integers(0, 256, int(rng.choice(lits)), dtype=np.uint8).tobytes()
         first = False
         off = int(rng.choice(offsets))
         mlen = int(rng.choice(lengths))
@@ -81,6 +81,27 @@ def crafted(seed, offsets, lengths, n_seq, head=700):
         out_len += len(lit) + mlen
     block += sequence(b"tail!", 0, 0)
     return block
+
+
+def dense(seed, n_seq=700, zero_offset_at=None):
+    """Many short sequences: literal runs of 0-2 bytes (now and then 14-16),
+    offsets 1-33 and a few far ones, match lengths 4-40 and 272-275.  With
+    zero_offset_at=i, sequence i gets offset 0 (malformed)."""
+    rng = np.random.default_rng(seed)
+    block = b""
+    lit = rng.integers(0, 256, 64, dtype=np.uint8).tobytes()
+    out_len = 0
+    for i in range(n_seq):
+        if i:
+            lit = rng.integers(0, 256, int(rng.choice([0] * 12 + [1, 2, 14, 15, 16])), dtype=np.uint8).tobytes()
+        off = int(rng.choice(list(range(1, 34)) + [100, 1000, 5000]))
+        off = min(off, out_len + len(lit))
+        if i == zero_offset_at:
+            off = 0
+        mlen = int(rng.choice(list(range(4, 41)) + [272, 273, 274, 275]))
+        block += sequence(lit, off, mlen)
+        out_len += len(lit) + mlen
+    return block + sequence(b"end", 0, 0)
 
 
 def library(data):
@@ -99,6 +120,9 @@ def cases():
         crafted(2, [32, 33, 100, 260, 479, 480], [4, 9, 28, 29, 60, 200, 700], 80),
         crafted(3, [481, 500, 511, 512, 513, 1000, 4000], [4, 12, 30, 90, 400, 2000], 60),
         crafted(4, [1, 5, 32, 480, 481, 700, 3000], [4, 5, 31, 32, 64, 520, 3000], 120, head=3100),
+        # dense: mostly 3- and 4-byte sequences, several per 32 input bytes,
+        # match lengths around the one-extension-byte limits (18/19, 273/274)
+        dense(12),
     ]
     rng = np.random.default_rng(9)
     x = np.arange(16384)

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from imagevis3d_gb300 import _lib as L
-from tests.lz4_blocks import cases, reference
+from tests.lz4_blocks import cases, dense, reference
 
 pytestmark = pytest.mark.gpu
 
@@ -65,3 +65,18 @@ def test_stored_chunks_and_a_malformed_block():
     got, err = _decode(torch, blocks, [len(refs[0]), len(refs[1]) + 7, len(refs[2])])
     assert err != 0
     assert got[0] == refs[0] and got[2] == refs[2]
+
+
+def test_malformed_sequence_inside_a_window_of_short_sequences():
+    """An offset of 0 among short sequences (decoded several per 32 input
+    bytes), and a chunk whose length ends inside such a window: both set the
+    error flag; the good blocks of the batch still decode."""
+    torch = pytest.importorskip("torch")
+    good = dense(21)
+    ref = reference(good)
+    bad = dense(21, zero_offset_at=350)
+    got, err = _decode(torch, [good, bad, good], [len(ref), len(ref), len(ref)])
+    assert err != 0
+    assert got[0] == ref and got[2] == ref
+    got, err = _decode(torch, [good, good], [len(ref), len(ref) // 2])
+    assert err != 0 and got[0] == ref

@@ -152,16 +152,23 @@ def _hist2d_cases(orc):
         "u16_global": (blobs((128, 40, 36), np.uint16, 4095.0, 2600.0), 0),
         "u8_deep": (blobs((64, 8, 300), np.uint8, 255.0, 255.0), 0),
         "u16_wide_nosmem": (blobs((64, 20, 10), np.uint16, 16000.0, 16000.0), 0),
+        # z split into segments (4 of 33 planes, the last 31; 3 of 34, the
+        # last 32; 2 of 35): columns restart mid-volume
+        "u16_zsegments": (blobs((96, 40, 130), np.uint16, 4095.0, 2600.0), 0),
+        "u8_ramp_ties_zsegments": ((np.add.outer(np.arange(100), np.add.outer(np.arange(30), np.arange(40))) % 200)
+                                   .astype(np.uint8), 0),
+        "u16_wide_nosmem_zsegments": (blobs((64, 12, 70), np.uint16, 16000.0, 16000.0), 0),
     }
 
 
 @pytest.mark.parametrize("case", ["u8_smem", "u8_periodic_flush", "u8_x4", "u8_misaligned", "u8_ramp_ties",
-                                  "u16_smem", "u16_global", "u8_deep", "u16_wide_nosmem"])
+                                  "u16_smem", "u16_global", "u8_deep", "u16_wide_nosmem", "u16_zsegments",
+                                  "u8_ramp_ties_zsegments", "u16_wide_nosmem_zsegments"])
 def test_dev_hist2d_paths_bit_exact(orc, case):
     vol, offset = _hist2d_cases(orc)[case]
     h1, f = orc.hist1d(vol)
     nx = h1.size
-    if case == "u16_wide_nosmem":
+    if case.startswith("u16_wide_nosmem"):
         nx, f = int(vol.max()) + 1, 1  # 16001 value bins: no gradient row fits in shared memory
     ms = float(vol.max())
     want, wmg = orc.hist2d(vol, ms, nx, f)

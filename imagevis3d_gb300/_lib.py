@@ -183,6 +183,7 @@ SIGNATURES = {
     "gbvr_set_clearview": [P, I, F, FP, F, F, F, F, F],
     "gbvr_paint_slice": [P, I, C.c_int64, I, I, I],
     "gbvr_paint_path": [P, C.POINTER(View), I, C.POINTER(C.c_int32), U64P, U64P],
+    "gbvr_paint_path_capture": [P, C.POINTER(View), I, C.POINTER(C.c_int32), U64P, U64P, P, SZ],
     "gbvr_paint_batch_async": [P, C.POINTER(View), I, I],
     "gbvr_read_framebuffers_async": [P, I, I, I, P, SZ],
     "gbvr_wait_read": [P, I],

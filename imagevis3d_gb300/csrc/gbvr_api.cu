@@ -605,8 +605,9 @@ int build_dataset(Dataset& ds, DevBuf& d_level0, int dtype, const long long dims
     CUDA_TRY(dsc.alloc(sizeof(Hist2DScratch)));
     CUDA_TRY(cudaMemsetAsync(d2.p, 0, sizeof(uint64_t) * n2, s));
     CUDA_TRY(t_h2.start(s));
+    // ds.gmax is the level's largest voxel (the bricks' maxima)
     CUDA_TRY(launch_hist2d(lv[0]->p, dtype, dims, ds.gmax, outsize, ds.merge, d2.as<unsigned long long>(),
-                           dsc.as<Hist2DScratch>(), s));
+                           dsc.as<Hist2DScratch>(), s, dtype == DT_U16 && ds.gmax < 16384.0));
     CUDA_TRY(t_h2.stop(s));
     // two passes over the level (the largest squared gradient, then the bins);
     // the f64 pass between them revisits only the voxels attaining it
@@ -2298,10 +2299,15 @@ int paint_slice(gbvr_renderer* r, int axis, int64_t index, int flip_x, int flip_
 // flight (frame i is paged only after frame i - 2 has finished, which frees
 // its staging and its slots).  Each frame renders with the per-view kernel
 // at its own level.  In core the frames simply render one after the other.
+// capture (optional): frame i's RGBA8 pixels are copied to capture + i *
+// width * height * 4 on the read stream once frame i is done.
 int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out, uint64_t* miss_out,
-               uint64_t* paged_out) {
+               uint64_t* paged_out, uint8_t* capture = nullptr, size_t capture_bytes = 0) {
   TRY(check_loaded(r));
   if (n <= 0 || !views) return fail(GBVR_EINVAL, "bad view list");
+  const size_t frame_bytes = (size_t)r->width * r->height * 4;
+  if (capture && capture_bytes < frame_bytes * n) return fail(GBVR_EINVAL, "capture buffer too small");
+  if (capture && !r->read_stream) CUDA_TRY(cudaStreamCreateWithFlags(&r->read_stream, cudaStreamNonBlocking));
   Dataset& ds = r->ds;
   if (!ds.ooc) {
     TRY(paint_plain(r, views, n));
@@ -2309,6 +2315,10 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
       if (lod_out) lod_out[i] = r->last_level;
       if (miss_out) miss_out[i] = 0;
       if (paged_out) paged_out[i] = 0;
+    }
+    if (capture) {
+      CUDA_TRY(cudaMemcpyAsync(capture, r->d_fb8.p, frame_bytes * n, cudaMemcpyDeviceToHost, r->stream));
+      CUDA_TRY(cudaStreamSynchronize(r->stream));
     }
     return GBVR_OK;
   }
@@ -2366,6 +2376,12 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
     TRY(render_lines(r));  // while the frame's bricks are resident
     TRY(render_cv(r, f));
     CUDA_TRY(cudaEventRecord(r->ev_done[st], r->stream));
+    if (capture) {
+      // the frame's framebuffer is written once per path: no later frame reuses it
+      CUDA_TRY(cudaStreamWaitEvent(r->read_stream, r->ev_done[st], 0));
+      CUDA_TRY(cudaMemcpyAsync(capture + frame_bytes * i, (const char*)r->d_fb8.p + frame_bytes * i, frame_bytes,
+                               cudaMemcpyDeviceToHost, r->read_stream));
+    }
     if (lod_out) lod_out[i] = level;
     if (miss_out) miss_out[i] = miss;
     if (paged_out) paged_out[i] = bytes;
@@ -2375,6 +2391,7 @@ int paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod_out
   CUDA_TRY(cudaEventRecord(r->evk1, r->stream));
   CUDA_TRY(cudaEventRecord(r->ev1, r->stream));
   CUDA_TRY(cudaEventSynchronize(r->ev1));
+  if (capture) CUDA_TRY(cudaStreamSynchronize(r->read_stream));
   for (int i = std::max(0, n - 2); i < n; ++i) TRY(page_time(i & 1));
   r->last_misses = tot_miss;
   r->last_paged = tot_paged;
@@ -2953,6 +2970,16 @@ int gbvr_paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lo
   TRY(check_r(r));
   TRY(settle_async(r));
   return paint_path(r, views, n, lod, misses, bytes_paged);
+  GBVR_ABI_CATCH
+}
+
+int gbvr_paint_path_capture(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod, uint64_t* misses,
+                            uint64_t* bytes_paged, uint8_t* rgba8, size_t bytes) {
+  GBVR_ABI_TRY
+  TRY(check_r(r));
+  if (!rgba8) return fail(GBVR_EINVAL, "null capture buffer");
+  TRY(settle_async(r));
+  return paint_path(r, views, n, lod, misses, bytes_paged, rgba8, bytes);
   GBVR_ABI_CATCH
 }
 

@@ -304,9 +304,10 @@ struct Hist2DScratch {
   unsigned long long smax;      // max integer squared central-difference sum
   unsigned long long gmax_bits; // max f64 |grad| among voxels attaining smax
 };
+// narrow: 16-bit data known to lie below 16384 (gradient sums in 32 bits)
 cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], double max_scalar,
                           long long nx, long long merge, unsigned long long* hist,
-                          Hist2DScratch* scratch, cudaStream_t s);
+                          Hist2DScratch* scratch, cudaStream_t s, bool narrow = false);
 // LZ4-compressed brick chunks to decode on the device: the compressed bytes
 // at stage + src (comp bytes; bit 31 set: stored uncompressed) become raw
 // bytes at pool + dst.

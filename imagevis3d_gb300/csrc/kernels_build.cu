@@ -967,7 +967,8 @@ __device__ __noinline__ double grad_f64(const T* __restrict__ v, long long X, lo
 // top row) the exact integer tests decide: the largest k with
 // k^2 Smax <= 65025 S.  tie: k^2 Smax == 65025 S, the real value is the
 // integer k and the f64 formula decides between k and k - 1.
-__device__ __forceinline__ int h2_row(unsigned long long S, unsigned long long smax, float inv_smax, bool& tie) {
+template <typename U>
+__device__ __forceinline__ int h2_row(U S, unsigned long long smax, float inv_smax, bool& tie) {
   const float q = (float)S * inv_smax;
   const float est = 255.f * (q * rsqrtf(q));
   const float fl = floorf(est);
@@ -975,7 +976,7 @@ __device__ __forceinline__ int h2_row(unsigned long long S, unsigned long long s
   int k = (int)fl;
   tie = false;
   if (fr > 1.f / 256.f && fr < 255.f / 256.f && k < 255) return k;
-  const unsigned long long lhs = 65025ULL * S;
+  const unsigned long long lhs = 65025ULL * (unsigned long long)S;
   if (k > 255) k = 255;
   while (k < 255 && (unsigned long long)(k + 1) * (k + 1) * smax <= lhs) ++k;
   while (k > 0 && (unsigned long long)k * k * smax > lhs) --k;
@@ -1107,9 +1108,12 @@ __device__ __forceinline__ void ld4(const T* p, int q[4]) {
 }
 
 // Squared-difference sums: below 2^20 for 8-bit voxels (32-bit arithmetic),
-// up to 3 (2 x 65535)^2 for 16-bit ones (64-bit).
-template <typename T> struct SumT { using U = unsigned long long; };
-template <> struct SumT<uint8_t> { using U = unsigned; };
+// up to 3 (2 x 65535)^2 for 16-bit ones (64-bit), or, NARROW, below
+// 3 (2 x 16383)^2 < 2^32 for 16-bit volumes whose values stay below 16384
+// (12-bit data; the caller knows the volume's maximum): 32-bit again.
+template <typename T, bool NARROW = false> struct SumT { using U = unsigned long long; };
+template <bool NARROW> struct SumT<uint8_t, NARROW> { using U = unsigned; };
+template <> struct SumT<uint16_t, true> { using U = unsigned; };
 
 template <typename T>
 struct Column {
@@ -1130,9 +1134,10 @@ struct Column {
     else { nxt[0] = cur[0]; nxt[1] = cur[1]; nxt[2] = cur[2]; nxt[3] = cur[3]; }
     prv[0] = cur[0]; prv[1] = cur[1]; prv[2] = cur[2]; prv[3] = cur[3];
   }
-  // S = Dx^2 + Dy^2 + Dz^2 of the 4 voxels at plane z (their values in cur)
-  __device__ __forceinline__ void diffs(int z, typename SumT<T>::U S[4]) const {
-    using U = typename SumT<T>::U;
+  // S = Dx^2 + Dy^2 + Dz^2 of the 4 voxels at plane z (their values in cur),
+  // in U: unsigned arithmetic modulo 2^bits, exact while the sum fits
+  template <typename U>
+  __device__ __forceinline__ void diffs(int z, U S[4]) const {
     const T* row = base + z * plane;
     int a[4], b[4];
     ld4(row + ym, a);
@@ -1149,8 +1154,8 @@ struct Column {
     const int* zp = z == Z - 1 ? cur : nxt;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int dy = my * (b[j] - a[j]), dz = mz * (zp[j] - zm[j]);
-      S[j] = (U)((U)((long long)dx[j] * dx[j]) + (U)((long long)dy * dy) + (U)((long long)dz * dz));
+      const U ux = (U)dx[j], uy = (U)(my * (b[j] - a[j])), uz = (U)(mz * (zp[j] - zm[j]));
+      S[j] = ux * ux + uy * uy + uz * uz;
     }
   }
   // move to plane z + 1
@@ -1172,12 +1177,12 @@ struct ColMax {
   unsigned pos[COL_KEEP];
 };
 
-template <typename T>
+template <typename T, bool NARROW>
 __global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X, int Y, int Z, Hist2DScratch* sc,
                                                  ColMax* __restrict__ cols) {
   const int cpr = X >> 2;
   const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  using U = typename SumT<T>::U;
+  using U = typename SumT<T, NARROW>::U;
   U smax = 0;
   if (col < (long long)cpr * Y) {
     const int y = (int)(col / cpr), x0 = 4 * (int)(col - (long long)y * cpr);
@@ -1218,7 +1223,7 @@ __global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X,
 // Pass 1b: the f64 |g| over the voxels attaining Smax, one thread per
 // column record: the recorded voxels, or the whole column again when it
 // attains Smax at more voxels than were recorded.
-template <typename T>
+template <typename T, bool NARROW>
 __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X, int Y, int Z, double c,
                                                   Hist2DScratch* sc, const ColMax* __restrict__ cols) {
   const unsigned long long smax = sc->smax;
@@ -1239,7 +1244,7 @@ __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X
   }
   Column<T> cl(v, X, Y, Z, x0, y);
   for (int z = 0; z < Z; ++z) {
-    typename SumT<T>::U S[4];
+    typename SumT<T, NARROW>::U S[4];
     cl.diffs(z, S);
 #pragma unroll
     for (int j = 0; j < 4; ++j)
@@ -1262,7 +1267,7 @@ __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X
 // WIDE: 32-bit shared counters, one per bin (one 768-thread block per SM with
 // about 200 KB of them), flushed only when a counter could overflow, i.e. in
 // practice once at the end, instead of 16-bit pairs flushed every 63 z-steps.
-template <typename T, bool SMEM, bool WIDE = false>
+template <typename T, bool SMEM, bool WIDE = false, bool NARROW = false>
 __global__ void __launch_bounds__(WIDE ? 768 : 256, WIDE ? 1 : 3)
     k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx, int merge,
               unsigned long long* __restrict__ hist, const Hist2DScratch* sc, int flush_steps, int kshared) {
@@ -1320,7 +1325,7 @@ __global__ void __launch_bounds__(WIDE ? 768 : 256, WIDE ? 1 : 3)
     Column<T> cl(v, X, Y, Z, x0, y);  // inactive threads walk column 0 and count nothing
     for (int z = 0; z < Z; ++z) {
       if (active) {
-        typename SumT<T>::U S[4];
+        typename SumT<T, NARROW>::U S[4];
         cl.diffs(z, S);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -1330,7 +1335,7 @@ __global__ void __launch_bounds__(WIDE ? 768 : 256, WIDE ? 1 : 3)
             // FP32 estimate (within one of the exact bin), settled exactly
             (void)lhs;
             bool tie;
-            k = h2_row((unsigned long long)S[j], smax, inv_smax, tie);
+            k = h2_row(S[j], smax, inv_smax, tie);
             if (tie) {
               // exact tie: the f64 formula decides
               const double gg = grad_f64(v, X, Y, Z, x0 + j, y, z, ((long long)z * Y + y) * X + x0 + j, c);
@@ -1364,8 +1369,29 @@ __global__ void __launch_bounds__(WIDE ? 768 : 256, WIDE ? 1 : 3)
   }
 }
 
+// The three passes of the 4-voxel-column path.
+template <typename T, bool NARROW>
+static cudaError_t hist2d_vec_passes(const T* v, int X, int Y, int Z, double c, int nx, int merge,
+                                     unsigned long long* hist, Hist2DScratch* scratch, ColMax* cols, long long blocks,
+                                     int threads, bool smem, size_t shbytes, int grid2, int wide_threads,
+                                     int flush_steps, int kshared, cudaStream_t s) {
+  k_h2v_max<T, NARROW><<<(unsigned)blocks, threads, 0, s>>>(v, X, Y, Z, scratch, cols);
+  k_h2v_gmax<T, NARROW><<<(unsigned)blocks, threads, 0, s>>>(v, X, Y, Z, c, scratch, cols);
+  if (smem) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_h2v_bin<T, true, true, NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
+    if (e != cudaSuccess) return e;
+    k_h2v_bin<T, true, true, NARROW><<<grid2, wide_threads, shbytes, s>>>(v, X, Y, Z, c, nx, merge, hist, scratch,
+                                                                         flush_steps, kshared);
+  } else {
+    k_h2v_bin<T, false, false, NARROW><<<grid2, threads, 0, s>>>(v, X, Y, Z, c, nx, merge, hist, scratch, 0, 0);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], double max_scalar, long long nx,
-                          long long merge, unsigned long long* hist, Hist2DScratch* scratch, cudaStream_t s) {
+                          long long merge, unsigned long long* hist, Hist2DScratch* scratch, cudaStream_t s,
+                          bool narrow) {
   (void)cudaGetLastError();  // drop a stale error of an earlier runtime call
   if (dtype == DT_F32) return cudaErrorInvalidValue;
   {
@@ -1400,36 +1426,21 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
       const long long wblocks = (ncols + wide_threads - 1) / wide_threads;
       const int grid2 = smem ? (int)std::min<long long>(wblocks, (long long)sms) : (int)blocks;
       const int nxi = (int)nx, mi = (int)merge, Xi = (int)X, Yi = (int)Y, Zi = (int)Z;
-      if (dtype == DT_U8) {
-        const uint8_t* v = (const uint8_t*)vol;
-        k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch, cols);
-        k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch, cols);
-        if (smem) {
-          e = cudaFuncSetAttribute(k_h2v_bin<uint8_t, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
-          if (e != cudaSuccess) {
-            cudaFreeAsync(cols, s);
-            return e;
-          }
-          k_h2v_bin<uint8_t, true, true><<<grid2, wide_threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps,
-                                                                         kshared);
-        } else {
-          k_h2v_bin<uint8_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0, 0);
-        }
-      } else {
-        const uint16_t* v = (const uint16_t*)vol;
-        k_h2v_max<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, scratch, cols);
-        k_h2v_gmax<<<(unsigned)blocks, threads, 0, s>>>(v, Xi, Yi, Zi, c, scratch, cols);
-        if (smem) {
-          e = cudaFuncSetAttribute(k_h2v_bin<uint16_t, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes);
-          if (e != cudaSuccess) {
-            cudaFreeAsync(cols, s);
-            return e;
-          }
-          k_h2v_bin<uint16_t, true, true><<<grid2, wide_threads, shbytes, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, flush_steps,
-                                                                         kshared);
-        } else {
-          k_h2v_bin<uint16_t, false><<<grid2, threads, 0, s>>>(v, Xi, Yi, Zi, c, nxi, mi, hist, scratch, 0, 0);
-        }
+      if (dtype == DT_U8)
+        e = hist2d_vec_passes<uint8_t, false>((const uint8_t*)vol, Xi, Yi, Zi, c, nxi, mi, hist, scratch, cols,
+                                              blocks, threads, smem, shbytes, grid2, wide_threads, flush_steps,
+                                              kshared, s);
+      else if (narrow)
+        e = hist2d_vec_passes<uint16_t, true>((const uint16_t*)vol, Xi, Yi, Zi, c, nxi, mi, hist, scratch, cols,
+                                              blocks, threads, smem, shbytes, grid2, wide_threads, flush_steps,
+                                              kshared, s);
+      else
+        e = hist2d_vec_passes<uint16_t, false>((const uint16_t*)vol, Xi, Yi, Zi, c, nxi, mi, hist, scratch, cols,
+                                               blocks, threads, smem, shbytes, grid2, wide_threads, flush_steps,
+                                               kshared, s);
+      if (e != cudaSuccess) {
+        cudaFreeAsync(cols, s);
+        return e;
       }
       e = cudaGetLastError();
       const cudaError_t ef = cudaFreeAsync(cols, s);

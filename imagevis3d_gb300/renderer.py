@@ -260,17 +260,25 @@ class Renderer:
         """changed2DTrans from a .2dt file (rasterised on the GPU)."""
         L.call("gbvr_set_tf2d_file", self._h, path.encode(), max_grad)
 
-    def paintPath(self, views):
+    def paintPath(self, views, capture=None):
         """Frames of a camera path into framebuffers 0..n-1 (out of core: paging
         of frame i + 1 overlaps the render of frame i).  Returns per-frame
-        (lod, misses, bytes_paged) arrays."""
+        (lod, misses, bytes_paged) arrays.  capture: a writable buffer of
+        n*h*w*4 bytes (page-locked for overlap, e.g. a pinned torch tensor)
+        that receives each frame's RGBA8 pixels as soon as the frame is done."""
         arr = self._views(views)
         n = len(views)
         lod = np.zeros(n, np.int32)
         miss = np.zeros(n, np.uint64)
         paged = np.zeros(n, np.uint64)
-        L.call("gbvr_paint_path", self._h, arr, n, lod.ctypes.data_as(C.POINTER(C.c_int32)),
-               miss.ctypes.data_as(L.U64P), paged.ctypes.data_as(L.U64P))
+        args = (self._h, arr, n, lod.ctypes.data_as(C.POINTER(C.c_int32)), miss.ctypes.data_as(L.U64P),
+                paged.ctypes.data_as(L.U64P))
+        if capture is None:
+            L.call("gbvr_paint_path", *args)
+        else:
+            ptr = capture.data_ptr() if hasattr(capture, "data_ptr") else capture.ctypes.data
+            nbytes = capture.numel() * capture.element_size() if hasattr(capture, "numel") else capture.nbytes
+            L.call("gbvr_paint_path_capture", *args, C.c_void_p(ptr), nbytes)
         self._nviews = n
         return lod, miss, paged
 

@@ -224,6 +224,14 @@ int gbvr_set_tf2d(gbvr_renderer* r, const float* rgba, int w, int h, float max_g
  * datasets render the frames one after the other.  gbvr_get_stats then reports the whole path. */
 int gbvr_paint_path(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod, uint64_t* misses,
                     uint64_t* bytes_paged);
+/* The same path with every frame captured (the capture sequence of ImageVis3D_Capturing.cpp:63-96 and
+ * RenderWindow.cpp:1718-1725, one image per frame): frame i's RGBA8 pixels (rows top first, as
+ * gbvr_read_framebuffers gives them) go to rgba8 + i * width * height * 4 as soon as frame i is done, on a
+ * copy stream of their own, while the following frames page and render; returns when every frame is in
+ * host memory.  rgba8 must hold n frames (bytes >= n * width * height * 4); page-locked memory lets the
+ * copies overlap the path. */
+int gbvr_paint_path_capture(gbvr_renderer* r, const gbvr_view* views, int n, int32_t* lod, uint64_t* misses,
+                            uint64_t* bytes_paged, uint8_t* rgba8, size_t bytes);
 
 /* 2D render region (tuvok.renderRegion2D.new(mode, sliceIndex, renderer), setSliceDepth, set2DFlipMode,
  * setUseMIP: RenderWindow.cpp:1548-1571, 235-239, 270-289) into framebuffer 0.  axis = the window mode:

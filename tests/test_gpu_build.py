@@ -110,6 +110,25 @@ def test_hist_merge_for_wide_16bit_range(orc):
         assert np.array_equal(g2, h2) and np.float32(mg) == np.float32(gmg)
 
 
+@pytest.mark.parametrize("top", [16383, 16384])
+def test_hist2d_of_16bit_volumes_at_the_32bit_sum_limit(orc, top):
+    """A build's 2D histogram sums squared differences in 32 bits when the
+    16-bit volume's largest value is below 16384, and in 64 bits otherwise:
+    both equal the rule bit for bit at the extreme gradients next to that
+    limit (voxels alternating between 0 and the top value)."""
+    rng = np.random.default_rng(top)
+    vol = np.where(rng.random((40, 36, 64)) < 0.5, 0, top).astype(np.uint16)
+    vol[5:9, 4:30, 10:50] = rng.integers(0, top + 1, (4, 26, 40), dtype=np.uint16)
+    vol[0, 0, 0] = top
+    with Renderer() as r:
+        r.loadVolume(vol, brick_size=32, overlap=2)
+        h1, f = orc.hist1d(vol)
+        assert np.array_equal(r.getHistogram(), h1)
+        h2, mg = orc.hist2d(vol, float(top), h1.size, f)
+        g2, gmg = r.get2DHistogram()
+        assert np.array_equal(g2, h2) and np.float32(gmg) == np.float32(mg)
+
+
 def test_constant_and_tiny_volumes(orc):
     for vol in (np.full((9, 10, 11), 7, np.uint8), np.zeros((1, 1, 1), np.uint16),
                 np.arange(8, dtype=np.uint8).reshape(2, 2, 2)):

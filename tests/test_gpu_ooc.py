@@ -229,6 +229,32 @@ def test_ooc_paint_path_pipeline_matches_incore_per_frame():
         assert np.array_equal(lod2, lod)
 
 
+def test_path_capture_equals_read_back_frames():
+    """gbvr_paint_path_capture: each frame's RGBA8 pixels, copied out while
+    later frames page and render, equal the frames read back after a plain
+    path paint (out of core, a small pool that pages every frame; and in
+    core); a buffer one frame short is rejected."""
+    import torch
+    sp, bp = CASES["u16_200x180x170_b64"]
+    slot = 64 ** 3 * 2
+    views = _inside_path(10, 128, 96)
+    with Renderer() as b, Renderer() as a:
+        b.loadSyntheticOutOfCore(sp, 30 * slot, **bp)
+        a.loadSynthetic(sp, **bp)
+        for r in (a, b):
+            _setup(r, sp, 128, 96)
+            lod, miss, paged = r.paintPath(views)
+            want = r.readFramebuffers(0, len(views))
+            cap = torch.zeros((len(views), 96, 128, 4), dtype=torch.uint8).pin_memory()
+            lod2, miss2, paged2 = r.paintPath(views, capture=cap)
+            assert np.array_equal(cap.numpy(), want) and np.array_equal(lod2, lod)
+            assert np.array_equal(r.readFramebuffers(0, len(views)), want)
+        short = np.zeros((len(views) - 1, 96, 128, 4), np.uint8)
+        with pytest.raises(GbvrError) as e:
+            b.paintPath(views, capture=short)
+        assert e.value.code == -1
+
+
 def test_paint_path_in_core_equals_views():
     sp, bp = CASES["u8_131x97x203_b32"]
     views = _inside_path(4, 96, 64)

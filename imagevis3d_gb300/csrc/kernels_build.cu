@@ -445,6 +445,55 @@ __device__ __forceinline__ void atomic_max_float(float* a, float v) {
 
 constexpr int GATHER_WARPS = 8;
 
+// Tiles of 4 rows x 4 voxels: two loads of voxel pairs per row, one store
+// of 4 voxels per row into each copy; in the blocked copy the tile is one
+// z-slice of a 4^3 block, contiguous, so its sectors are written whole by
+// one thread.  Pair / Quad: 2 and 4 voxels as one word.
+template <typename T> struct GatherVec;
+template <> struct GatherVec<uint8_t> {
+  using Pair = unsigned short;
+  using Quad = unsigned;
+  __device__ static Quad quad(Pair a, Pair b) { return (unsigned)a | ((unsigned)b << 16); }
+  __device__ static Quad make4(uint8_t a, uint8_t b, uint8_t c, uint8_t d) {
+    return (unsigned)a | ((unsigned)b << 8) | ((unsigned)c << 16) | ((unsigned)d << 24);
+  }
+  // packed per-byte min / max
+  __device__ static void acc(Quad q, unsigned& mn, unsigned& mx) { mn = __vminu4(mn, q); mx = __vmaxu4(mx, q); }
+  __device__ static void fold(unsigned mn, unsigned mx, float& fmn, float& fmx) {
+    for (int i = 0; i < 4; ++i) {
+      fmn = fminf(fmn, (float)((mn >> (8 * i)) & 0xffu));
+      fmx = fmaxf(fmx, (float)((mx >> (8 * i)) & 0xffu));
+    }
+  }
+};
+template <> struct GatherVec<uint16_t> {
+  using Pair = unsigned;
+  using Quad = uint2;
+  __device__ static Quad quad(Pair a, Pair b) { return make_uint2(a, b); }
+  __device__ static Quad make4(uint16_t a, uint16_t b, uint16_t c, uint16_t d) {
+    return make_uint2((unsigned)a | ((unsigned)b << 16), (unsigned)c | ((unsigned)d << 16));
+  }
+  __device__ static void acc(Quad q, unsigned& mn, unsigned& mx) {
+    mn = __vminu2(mn, __vminu2(q.x, q.y));
+    mx = __vmaxu2(mx, __vmaxu2(q.x, q.y));
+  }
+  __device__ static void fold(unsigned mn, unsigned mx, float& fmn, float& fmx) {
+    fmn = fminf(fmn, (float)min(mn & 0xffffu, mn >> 16));
+    fmx = fmaxf(fmx, (float)max(mx & 0xffffu, mx >> 16));
+  }
+};
+template <> struct GatherVec<float> {
+  using Pair = float2;
+  using Quad = float4;
+  __device__ static Quad quad(Pair a, Pair b) { return make_float4(a.x, a.y, b.x, b.y); }
+  __device__ static Quad make4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+  // min / max kept in the float accumulators directly (NaN voxels passed over)
+  __device__ static void acc(Quad q, float& mn, float& mx) {
+    mn = fminf(fminf(mn, q.x), fminf(q.y, fminf(q.z, q.w)));
+    mx = fmaxf(fmaxf(mx, q.x), fmaxf(q.y, fmaxf(q.z, q.w)));
+  }
+};
+
 template <typename T, bool BLOCKED>
 __global__ void __launch_bounds__(32 * GATHER_WARPS) k_gather_fused(const T* __restrict__ level, long long X,
                                                                     long long Y, long long Z,
@@ -456,9 +505,65 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS) k_gather_fused(const T* __r
   const int nbx = (sx + 3) >> 2, nby = (sy + 3) >> 2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float mn = INFINITY, mx = -INFINITY;
+  using V = GatherVec<T>;
+  // the tiled path needs voxel pairs at even level x (X, ox even, aligned
+  // rows) and 4-voxel stores at multiples of 4 elements in both copies
+  const bool tiled = (X % 2 == 0) && (ox % 2 == 0) && (sx % 4 == 0) &&
+                     reinterpret_cast<uintptr_t>(level) % (2 * sizeof(T)) == 0 &&
+                     reinterpret_cast<uintptr_t>(pool0 + off) % (4 * sizeof(T)) == 0 &&
+                     (!BLOCKED || reinterpret_cast<uintptr_t>(pool1 + off) % (4 * sizeof(T)) == 0);
+  const int row_start = tiled ? (sy & ~3) : 0;  // rows below it go by tiles
+  if (tiled) {
+    using Acc = typename std::conditional<std::is_same<T, float>::value, float, unsigned>::type;
+    Acc pmn, pmx;
+    if constexpr (std::is_same<T, float>::value) { pmn = INFINITY; pmx = -INFINITY; }
+    else { pmn = 0xffffffffu; pmx = 0u; }
+    const int nq = sx >> 2;
+    for (int zs = blockIdx.x; zs < sz; zs += gridDim.x) {
+      const long long z = min(max((long long)oz + zs, 0LL), Z - 1);
+      for (int band = warp; 4 * band < row_start; band += GATHER_WARPS) {
+        const int r0 = 4 * band;
+        const T* src[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) src[k] = level + (z * Y + min(max((long long)oy + r0 + k, 0LL), Y - 1)) * X;
+        T* d0 = pool0 + off + ((long long)zs * sy + r0) * sx;
+        T* d1 = BLOCKED ? pool1 + off + ((((long long)(zs >> 2) * nby + band) * nbx) << 6) + ((zs & 3) << 4) : nullptr;
+        for (int q = lane; q < nq; q += 32) {
+          const long long x = (long long)ox + 4 * q;
+          typename V::Quad t[4];
+          if (x >= 0 && x + 3 < X) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const typename V::Pair* pp = reinterpret_cast<const typename V::Pair*>(src[k] + x);
+              t[k] = V::quad(__ldg(pp), __ldg(pp + 1));
+            }
+          } else {
+            // ghosts outside the level replicate its edge voxels
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              auto at = [&](int i) { return __ldg(src[k] + min(max(x + i, 0LL), X - 1)); };
+              t[k] = V::make4(at(0), at(1), at(2), at(3));
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            *reinterpret_cast<typename V::Quad*>(d0 + (long long)k * sx + 4 * q) = t[k];
+            if (BLOCKED) *reinterpret_cast<typename V::Quad*>(d1 + ((long long)q << 6) + (k << 2)) = t[k];
+            V::acc(t[k], pmn, pmx);
+          }
+        }
+      }
+    }
+    if constexpr (std::is_same<T, float>::value) {
+      mn = pmn;
+      mx = pmx;
+    } else {
+      V::fold(pmn, pmx, mn, mx);
+    }
+  }
   for (int zs = blockIdx.x; zs < sz; zs += gridDim.x) {
     const long long z = min(max((long long)oz + zs, 0LL), Z - 1);
-    for (int r = warp; r < sy; r += GATHER_WARPS) {
+    for (int r = row_start + warp; r < sy; r += GATHER_WARPS) {
       // ghosts outside the level replicate its edge voxels
       const long long y = min(max((long long)oy + r, 0LL), Y - 1);
       const T* src = level + (z * Y + y) * X;

@@ -513,6 +513,9 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS) k_gather_fused(const T* __r
                      reinterpret_cast<uintptr_t>(pool0 + off) % (4 * sizeof(T)) == 0 &&
                      (!BLOCKED || reinterpret_cast<uintptr_t>(pool1 + off) % (4 * sizeof(T)) == 0);
   const int row_start = tiled ? (sy & ~3) : 0;  // rows below it go by tiles
+  // blocked copy at 16-byte boundaries: a slice (16 voxels at a multiple of
+  // 16 elements from the brick's start) goes out in 16-byte stores
+  const bool wide1 = BLOCKED && reinterpret_cast<uintptr_t>(pool1 + off) % 16 == 0;
   if (tiled) {
     using Acc = typename std::conditional<std::is_same<T, float>::value, float, unsigned>::type;
     Acc pmn, pmx;
@@ -548,8 +551,29 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS) k_gather_fused(const T* __r
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             *reinterpret_cast<typename V::Quad*>(d0 + (long long)k * sx + 4 * q) = t[k];
-            if (BLOCKED) *reinterpret_cast<typename V::Quad*>(d1 + ((long long)q << 6) + (k << 2)) = t[k];
             V::acc(t[k], pmn, pmx);
+          }
+          if (BLOCKED) {
+            // the block's z-slice: 16 contiguous voxels, in 16-byte stores
+            // where the copy is aligned for them
+            T* ds = d1 + ((long long)q << 6);
+            if constexpr (sizeof(T) == 1) {
+              if (wide1) *reinterpret_cast<uint4*>(ds) = make_uint4(t[0], t[1], t[2], t[3]);
+              else
+#pragma unroll
+                for (int k = 0; k < 4; ++k) *reinterpret_cast<typename V::Quad*>(ds + (k << 2)) = t[k];
+            } else if constexpr (sizeof(T) == 2) {
+              if (wide1) {
+                reinterpret_cast<uint4*>(ds)[0] = make_uint4(t[0].x, t[0].y, t[1].x, t[1].y);
+                reinterpret_cast<uint4*>(ds)[1] = make_uint4(t[2].x, t[2].y, t[3].x, t[3].y);
+              } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) *reinterpret_cast<typename V::Quad*>(ds + (k << 2)) = t[k];
+              }
+            } else {
+#pragma unroll
+              for (int k = 0; k < 4; ++k) *reinterpret_cast<typename V::Quad*>(ds + (k << 2)) = t[k];
+            }
           }
         }
       }

@@ -1236,6 +1236,16 @@ __device__ __forceinline__ void ld4(const T* p, int q[4]) {
   q[0] = w.x; q[1] = w.y; q[2] = w.z; q[3] = w.w;
 }
 
+// 4 consecutive 8-bit voxels of a row as one 32-bit word (the 8-bit column
+// walker keeps its planes packed so that the neighbour rows of the next
+// plane fit in registers too).
+template <typename T> struct Packed4;
+template <> struct Packed4<uint8_t> {
+  using W = unsigned;
+  __device__ static W load(const uint8_t* p) { return __ldg(reinterpret_cast<const unsigned*>(p)); }
+  __device__ static int at(W w, int j) { return (int)((w >> (8 * j)) & 0xffu); }
+};
+
 // Squared-difference sums: below 2^20 for 8-bit voxels (32-bit arithmetic),
 // up to 3 (2 x 65535)^2 for 16-bit ones (64-bit), or, NARROW, below
 // 3 (2 x 16383)^2 < 2^32 for 16-bit volumes whose values stay below 16384
@@ -1244,6 +1254,9 @@ template <typename T, bool NARROW = false> struct SumT { using U = unsigned long
 template <bool NARROW> struct SumT<uint8_t, NARROW> { using U = unsigned; };
 template <> struct SumT<uint16_t, true> { using U = unsigned; };
 
+// 16-bit voxels: the planes as int arrays, the neighbour rows loaded in
+// diffs (keeping them a plane ahead spills at the binning pass's 80 registers
+// and was slower: c2's 2D histogram 9.12 -> 9.38 ms).
 template <typename T>
 struct Column {
   const T* base;  // voxel (x0, y, 0)
@@ -1287,6 +1300,7 @@ struct Column {
       S[j] = ux * ux + uy * uy + uz * uz;
     }
   }
+  __device__ __forceinline__ int val(int j) const { return cur[j]; }
   // move to plane z + 1
   __device__ __forceinline__ void step(int z) {
 #pragma unroll
@@ -1294,6 +1308,76 @@ struct Column {
     if (z + 2 < Z) ld4(base + (z + 2) * plane, nxt);
   }
 };
+
+// 8-bit voxels: packed planes, the neighbour rows of plane z + 1 loaded in
+// step(z), a full step before they are used (c3's 2D histogram 39.4 ->
+// 33.4 ms).
+template <typename T>
+struct ColumnAhead {
+  using P = Packed4<T>;
+  using W = typename P::W;
+  const T* base;  // voxel (x0, y, 0)
+  long long plane;
+  int X, Z, x0, ym, yp, my;
+  W prv, cur, nxt;  // planes z - 1, z, z + 1 of the 4 voxels
+  W na, nb;         // rows y - 1 and y + 1 of plane z, loaded a plane ahead
+  int nxl, nxr;     // voxels x0 - 1 and x0 + 4 of plane z, likewise
+  __device__ __forceinline__ void load_neighbours(int z) {
+    const T* row = base + z * plane;
+    na = P::load(row + ym);
+    nb = P::load(row + yp);
+    nxl = x0 > 0 ? (int)__ldg(row - 1) : 0;
+    nxr = x0 + 4 < X ? (int)__ldg(row + 4) : 0;
+  }
+  __device__ __forceinline__ ColumnAhead(const T* v, int X_, int Y, int Z_, int x0_, int y) {
+    X = X_; Z = Z_; x0 = x0_;
+    plane = (long long)X * Y;
+    base = v + (long long)y * X + x0;
+    if (Y == 1) { ym = yp = 0; my = 0; }
+    else if (y == 0) { ym = 0; yp = X; my = 2; }
+    else if (y == Y - 1) { ym = -X; yp = 0; my = 2; }
+    else { ym = -X; yp = X; my = 1; }
+    cur = P::load(base);
+    nxt = Z > 1 ? P::load(base + plane) : cur;
+    prv = cur;
+    load_neighbours(0);
+  }
+  // voxel j of plane z (after step(z - 1))
+  __device__ __forceinline__ int val(int j) const { return P::at(cur, j); }
+  // S = Dx^2 + Dy^2 + Dz^2 of the 4 voxels at plane z (their values in cur),
+  // in U: unsigned arithmetic modulo 2^bits, exact while the sum fits
+  template <typename U>
+  __device__ __forceinline__ void diffs(int z, U S[4]) const {
+    int c[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) c[j] = P::at(cur, j);
+    int dx[4];
+    dx[0] = x0 == 0 ? 2 * (c[1] - c[0]) : c[1] - nxl;
+    dx[1] = c[2] - c[0];
+    dx[2] = c[3] - c[1];
+    dx[3] = x0 + 4 == X ? 2 * (c[3] - c[2]) : nxr - c[2];
+    const int mz = Z == 1 ? 0 : ((z == 0 || z == Z - 1) ? 2 : 1);
+    const W zm = z == 0 ? cur : prv;
+    const W zp = z == Z - 1 ? cur : nxt;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const U ux = (U)dx[j], uy = (U)(my * (P::at(nb, j) - P::at(na, j))),
+              uz = (U)(mz * (P::at(zp, j) - P::at(zm, j)));
+      S[j] = ux * ux + uy * uy + uz * uz;
+    }
+  }
+  // move to plane z + 1: its neighbour rows and the plane after it are
+  // loaded now, a full step before they are used
+  __device__ __forceinline__ void step(int z) {
+    prv = cur;
+    cur = nxt;
+    if (z + 2 < Z) nxt = P::load(base + (z + 2) * plane);
+    if (z + 1 < Z) load_neighbours(z + 1);
+  }
+};
+
+template <typename T>
+using ColumnOf = typename std::conditional<sizeof(T) == 1, ColumnAhead<T>, Column<T>>::type;
 
 // Pass 1: the largest S.  One thread per 4-voxel column (all of z), which
 // also records where its column attains its own largest S (the first
@@ -1315,7 +1399,7 @@ __global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X,
   U smax = 0;
   if (col < (long long)cpr * Y) {
     const int y = (int)(col / cpr), x0 = 4 * (int)(col - (long long)y * cpr);
-    Column<T> c(v, X, Y, Z, x0, y);
+    ColumnOf<T> c(v, X, Y, Z, x0, y);
     unsigned cnt = 0, pos[COL_KEEP] = {0u, 0u, 0u};
     for (int z = 0; z < Z; ++z) {
       U S[4];
@@ -1371,7 +1455,7 @@ __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X
     }
     return;
   }
-  Column<T> cl(v, X, Y, Z, x0, y);
+  ColumnOf<T> cl(v, X, Y, Z, x0, y);
   for (int z = 0; z < Z; ++z) {
     typename SumT<T, NARROW>::U S[4];
     cl.diffs(z, S);
@@ -1451,7 +1535,7 @@ __global__ void __launch_bounds__(WIDE ? 768 : 256, WIDE ? 1 : 3)
     const long long col = g * blockDim.x + threadIdx.x;
     const bool active = col < ncols;
     const int y = active ? (int)(col / cpr) : 0, x0 = active ? 4 * (int)(col - (long long)y * cpr) : 0;
-    Column<T> cl(v, X, Y, Z, x0, y);  // inactive threads walk column 0 and count nothing
+    ColumnOf<T> cl(v, X, Y, Z, x0, y);  // inactive threads walk column 0 and count nothing
     for (int z = 0; z < Z; ++z) {
       if (active) {
         typename SumT<T, NARROW>::U S[4];
@@ -1472,7 +1556,7 @@ __global__ void __launch_bounds__(WIDE ? 768 : 256, WIDE ? 1 : 3)
               if (k > 255) k = 255;
             }
           }
-          int bx = merge32 == 1 ? cl.cur[j] : (int)((unsigned)cl.cur[j] / merge32);
+          int bx = merge32 == 1 ? cl.val(j) : (int)((unsigned)cl.val(j) / merge32);
           if (bx >= nx) bx = nx - 1;
           const unsigned bin = (unsigned)bx * 256u + (unsigned)k;
           if (bin == run_bin) {

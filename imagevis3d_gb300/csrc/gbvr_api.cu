@@ -1367,6 +1367,11 @@ struct gbvr_renderer {
   } other;
   int cur_slot = 0;
   cudaStream_t read_stream = nullptr;
+  // a second copy stream for the other half of an asynchronous read-back
+  // (two device-to-host copies in flight use two copy engines), joined back
+  // into read_stream through read2_done
+  cudaStream_t read_stream2 = nullptr;
+  cudaEvent_t read2_done = nullptr;
   cudaEvent_t slot_rendered[2] = {nullptr, nullptr}, slot_read[2] = {nullptr, nullptr};
   bool slot_render_pending[2] = {false, false}, slot_read_pending[2] = {false, false};
   void select_slot(int slot) {
@@ -1427,6 +1432,8 @@ struct gbvr_renderer {
       if (slot_read[k]) cudaEventDestroy(slot_read[k]);
     }
     if (read_stream) cudaStreamDestroy(read_stream);
+    if (read_stream2) cudaStreamDestroy(read_stream2);
+    if (read2_done) cudaEventDestroy(read2_done);
     for (int k = 0; k < 2; ++k) {
       if (ev_c0[k]) cudaEventDestroy(ev_c0[k]);
       if (ev_c1[k]) cudaEventDestroy(ev_c1[k]);
@@ -3328,12 +3335,13 @@ int gbvr_paint_batch_async(gbvr_renderer* r, const gbvr_view* views, int n, int 
   if (!views || n <= 0) return fail(GBVR_EINVAL, "bad view list");
   if (slot < 0 || slot > 1) return fail(GBVR_EINVAL, "slot must be 0 or 1");
   if (r->ds.ooc) return fail(GBVR_ESTATE, "asynchronous batches need an in-core dataset");
-  if (!r->read_stream) {
-    CUDA_TRY(cudaStreamCreateWithFlags(&r->read_stream, cudaStreamNonBlocking));
-    for (int k = 0; k < 2; ++k) {
-      CUDA_TRY(cudaEventCreateWithFlags(&r->slot_rendered[k], cudaEventDisableTiming));
-      CUDA_TRY(cudaEventCreateWithFlags(&r->slot_read[k], cudaEventDisableTiming));
-    }
+  // each resource on its own: a captured path may have made the read stream
+  if (!r->read_stream) CUDA_TRY(cudaStreamCreateWithFlags(&r->read_stream, cudaStreamNonBlocking));
+  if (!r->read_stream2) CUDA_TRY(cudaStreamCreateWithFlags(&r->read_stream2, cudaStreamNonBlocking));
+  if (!r->read2_done) CUDA_TRY(cudaEventCreateWithFlags(&r->read2_done, cudaEventDisableTiming));
+  for (int k = 0; k < 2; ++k) {
+    if (!r->slot_rendered[k]) CUDA_TRY(cudaEventCreateWithFlags(&r->slot_rendered[k], cudaEventDisableTiming));
+    if (!r->slot_read[k]) CUDA_TRY(cudaEventCreateWithFlags(&r->slot_read[k], cudaEventDisableTiming));
   }
   r->select_slot(slot);
   return paint_batch(r, views, n, true);
@@ -3343,7 +3351,7 @@ int gbvr_paint_batch_async(gbvr_renderer* r, const gbvr_view* views, int n, int 
 int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, void* host, size_t bytes) {
   GBVR_ABI_TRY
   TRY(check_r(r));
-  if (slot < 0 || slot > 1 || !r->read_stream || !r->slot_render_pending[slot])
+  if (slot < 0 || slot > 1 || !r->read_stream || !r->read2_done || !r->slot_render_pending[slot])
     return fail(GBVR_ESTATE, "no asynchronous batch rendered into that slot");
   const bool cur = slot == r->cur_slot;
   const int w = cur ? r->fb_w : r->other.fb_w, h = cur ? r->fb_h : r->other.fb_h;
@@ -3353,7 +3361,16 @@ int gbvr_read_framebuffers_async(gbvr_renderer* r, int slot, int first, int n, v
   if (first < 0 || n <= 0 || first + n > views) return fail(GBVR_EINVAL, "view range out of range");
   if (!host || bytes < per * n) return fail(GBVR_EINVAL, "host buffer too small");
   CUDA_TRY(cudaStreamWaitEvent(r->read_stream, r->slot_rendered[slot], 0));
-  CUDA_TRY(cudaMemcpyAsync(host, (const char*)fb + per * first, per * n, cudaMemcpyDeviceToHost, r->read_stream));
+  const int n2 = (r->read_stream2 && n >= 2) ? n / 2 : 0;  // frames on the second stream
+  if (n2 > 0) {
+    CUDA_TRY(cudaStreamWaitEvent(r->read_stream2, r->slot_rendered[slot], 0));
+    CUDA_TRY(cudaMemcpyAsync((char*)host + per * (n - n2), (const char*)fb + per * (first + n - n2), per * n2,
+                             cudaMemcpyDeviceToHost, r->read_stream2));
+    CUDA_TRY(cudaEventRecord(r->read2_done, r->read_stream2));
+  }
+  CUDA_TRY(cudaMemcpyAsync(host, (const char*)fb + per * first, per * (n - n2), cudaMemcpyDeviceToHost,
+                           r->read_stream));
+  if (n2 > 0) CUDA_TRY(cudaStreamWaitEvent(r->read_stream, r->read2_done, 0));
   CUDA_TRY(cudaEventRecord(r->slot_read[slot], r->read_stream));
   r->slot_read_pending[slot] = true;
   return GBVR_OK;

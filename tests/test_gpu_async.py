@@ -109,3 +109,24 @@ def test_async_errors(sp):
         with pytest.raises(GbvrError):
             r.readFramebuffersAsync(1, np.zeros((1, H, W, 4), np.uint8), 0, 2)  # too small
         r.waitAsync()
+
+
+def test_async_batches_after_a_captured_path(sp):
+    """A captured path first (it creates the read stream), then asynchronous
+    batches of 5 views (the read-back split unevenly over two copy streams) on
+    the same renderer: every step equals its synchronous batch."""
+    steps = [workloads.orbit_views(5, W, H, elevation=e, start=s) for e, s in ((12, 5), (-18, 50), (33, 95))]
+    with _renderer(sp) as r:
+        want = []
+        for views in steps:
+            r.paintBatch(views)
+            want.append(r.readFramebuffers(0, len(views)).copy())
+        cap = torch.empty((5, H, W, 4), dtype=torch.uint8).pin_memory()
+        r.paintPath(steps[0], capture=cap)
+        outs = [torch.empty((5, H, W, 4), dtype=torch.uint8).pin_memory() for _ in steps]
+        for i, views in enumerate(steps):
+            r.paintBatchAsync(views, i % 2)
+            r.readFramebuffersAsync(i % 2, outs[i])
+        r.waitAsync()
+        for o, w in zip(outs, want):
+            assert np.array_equal(o.numpy(), w)

@@ -1226,24 +1226,19 @@ __global__ void k_hist2d_pass2(const T* __restrict__ v, long long X, long long Y
 // rows y - 1 and y + 1, and two scalar loads for the x neighbours.  The
 // border rules (one-sided difference x 2 on the faces) are the multipliers
 // my / mz.  Same integer differences as int_diffs.
-template <typename T> struct Quad;
-template <> struct Quad<uint8_t> { using V = uchar4; };
-template <> struct Quad<uint16_t> { using V = ushort4; };
-
-template <typename T>
-__device__ __forceinline__ void ld4(const T* p, int q[4]) {
-  const typename Quad<T>::V w = __ldg(reinterpret_cast<const typename Quad<T>::V*>(p));
-  q[0] = w.x; q[1] = w.y; q[2] = w.z; q[3] = w.w;
-}
-
-// 4 consecutive 8-bit voxels of a row as one 32-bit word (the 8-bit column
-// walker keeps its planes packed so that the neighbour rows of the next
-// plane fit in registers too).
+// 4 consecutive voxels of a row as raw words: one 32-bit word for 8-bit
+// voxels, two for 16-bit ones (the column walker keeps its planes packed so
+// that the neighbour rows of the next plane fit in registers too).
 template <typename T> struct Packed4;
 template <> struct Packed4<uint8_t> {
   using W = unsigned;
   __device__ static W load(const uint8_t* p) { return __ldg(reinterpret_cast<const unsigned*>(p)); }
   __device__ static int at(W w, int j) { return (int)((w >> (8 * j)) & 0xffu); }
+};
+template <> struct Packed4<uint16_t> {
+  using W = uint2;
+  __device__ static W load(const uint16_t* p) { return __ldg(reinterpret_cast<const uint2*>(p)); }
+  __device__ static int at(W w, int j) { return (int)(((j < 2 ? w.x : w.y) >> (16 * (j & 1))) & 0xffffu); }
 };
 
 // Squared-difference sums: below 2^20 for 8-bit voxels (32-bit arithmetic),
@@ -1254,64 +1249,10 @@ template <typename T, bool NARROW = false> struct SumT { using U = unsigned long
 template <bool NARROW> struct SumT<uint8_t, NARROW> { using U = unsigned; };
 template <> struct SumT<uint16_t, true> { using U = unsigned; };
 
-// 16-bit voxels: the planes as int arrays, the neighbour rows loaded in
-// diffs (keeping them a plane ahead spills at the binning pass's 80 registers
-// and was slower: c2's 2D histogram 9.12 -> 9.38 ms).
-template <typename T>
-struct Column {
-  const T* base;  // voxel (x0, y, 0)
-  long long plane;
-  int X, Z, x0, ym, yp, my;
-  int prv[4], cur[4], nxt[4];
-  __device__ __forceinline__ Column(const T* v, int X_, int Y, int Z_, int x0_, int y) {
-    X = X_; Z = Z_; x0 = x0_;
-    plane = (long long)X * Y;
-    base = v + (long long)y * X + x0;
-    if (Y == 1) { ym = yp = 0; my = 0; }
-    else if (y == 0) { ym = 0; yp = X; my = 2; }
-    else if (y == Y - 1) { ym = -X; yp = 0; my = 2; }
-    else { ym = -X; yp = X; my = 1; }
-    ld4(base, cur);
-    if (Z > 1) ld4(base + plane, nxt);
-    else { nxt[0] = cur[0]; nxt[1] = cur[1]; nxt[2] = cur[2]; nxt[3] = cur[3]; }
-    prv[0] = cur[0]; prv[1] = cur[1]; prv[2] = cur[2]; prv[3] = cur[3];
-  }
-  // S = Dx^2 + Dy^2 + Dz^2 of the 4 voxels at plane z (their values in cur),
-  // in U: unsigned arithmetic modulo 2^bits, exact while the sum fits
-  template <typename U>
-  __device__ __forceinline__ void diffs(int z, U S[4]) const {
-    const T* row = base + z * plane;
-    int a[4], b[4];
-    ld4(row + ym, a);
-    ld4(row + yp, b);
-    const int xl = x0 > 0 ? (int)__ldg(row - 1) : 0;
-    const int xr = x0 + 4 < X ? (int)__ldg(row + 4) : 0;
-    int dx[4];
-    dx[0] = x0 == 0 ? 2 * (cur[1] - cur[0]) : cur[1] - xl;
-    dx[1] = cur[2] - cur[0];
-    dx[2] = cur[3] - cur[1];
-    dx[3] = x0 + 4 == X ? 2 * (cur[3] - cur[2]) : xr - cur[2];
-    const int mz = Z == 1 ? 0 : ((z == 0 || z == Z - 1) ? 2 : 1);
-    const int* zm = z == 0 ? cur : prv;
-    const int* zp = z == Z - 1 ? cur : nxt;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const U ux = (U)dx[j], uy = (U)(my * (b[j] - a[j])), uz = (U)(mz * (zp[j] - zm[j]));
-      S[j] = ux * ux + uy * uy + uz * uz;
-    }
-  }
-  __device__ __forceinline__ int val(int j) const { return cur[j]; }
-  // move to plane z + 1
-  __device__ __forceinline__ void step(int z) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) { prv[j] = cur[j]; cur[j] = nxt[j]; }
-    if (z + 2 < Z) ld4(base + (z + 2) * plane, nxt);
-  }
-};
-
-// 8-bit voxels: packed planes, the neighbour rows of plane z + 1 loaded in
-// step(z), a full step before they are used (c3's 2D histogram 39.4 ->
-// 33.4 ms).
+// A 4-voxel column walked along z: packed planes, the neighbour rows of
+// plane z + 1 loaded in step(z), a full step before they are used (c3's 2D
+// histogram 39.4 -> 33.4 ms; for 16-bit voxels, with the binning pass at
+// 640 threads and 96 registers, c2's 9.40 -> 8.86 ms).
 template <typename T>
 struct ColumnAhead {
   using P = Packed4<T>;
@@ -1376,9 +1317,6 @@ struct ColumnAhead {
   }
 };
 
-template <typename T>
-using ColumnOf = typename std::conditional<sizeof(T) == 1, ColumnAhead<T>, Column<T>>::type;
-
 // Pass 1: the largest S.  One thread per 4-voxel column (all of z), which
 // also records where its column attains its own largest S (the first
 // COL_KEEP voxels as 4 z + j, and how many there are), so that the f64 pass
@@ -1399,7 +1337,7 @@ __global__ void __launch_bounds__(256) k_h2v_max(const T* __restrict__ v, int X,
   U smax = 0;
   if (col < (long long)cpr * Y) {
     const int y = (int)(col / cpr), x0 = 4 * (int)(col - (long long)y * cpr);
-    ColumnOf<T> c(v, X, Y, Z, x0, y);
+    ColumnAhead<T> c(v, X, Y, Z, x0, y);
     unsigned cnt = 0, pos[COL_KEEP] = {0u, 0u, 0u};
     for (int z = 0; z < Z; ++z) {
       U S[4];
@@ -1455,7 +1393,7 @@ __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X
     }
     return;
   }
-  ColumnOf<T> cl(v, X, Y, Z, x0, y);
+  ColumnAhead<T> cl(v, X, Y, Z, x0, y);
   for (int z = 0; z < Z; ++z) {
     typename SumT<T, NARROW>::U S[4];
     cl.diffs(z, S);
@@ -1477,11 +1415,12 @@ __global__ void __launch_bounds__(256) k_h2v_gmax(const T* __restrict__ v, int X
 // practice, go to global memory directly.  Blocks loop over groups of
 // blockDim columns.  Runs of equal bins along a thread's voxels are counted
 // in registers first either way.
-// WIDE: 32-bit shared counters, one per bin (one 768-thread block per SM with
-// about 200 KB of them), flushed only when a counter could overflow, i.e. in
-// practice once at the end, instead of 16-bit pairs flushed every 63 z-steps.
+// WIDE: 32-bit shared counters, one per bin (one block per SM with about
+// 200 KB of them: 768 threads for 8-bit data, 640 at 96 registers for 16-bit
+// data), flushed only when a counter could overflow, i.e. in practice once at
+// the end, instead of 16-bit pairs flushed every 63 z-steps.
 template <typename T, bool SMEM, bool WIDE = false, bool NARROW = false>
-__global__ void __launch_bounds__(WIDE ? 768 : 256, WIDE ? 1 : 3)
+__global__ void __launch_bounds__(WIDE ? (sizeof(T) == 2 ? 640 : 768) : 256, WIDE ? 1 : 3)
     k_h2v_bin(const T* __restrict__ v, int X, int Y, int Z, double c, int nx, int merge,
               unsigned long long* __restrict__ hist, const Hist2DScratch* sc, int flush_steps, int kshared) {
   extern __shared__ unsigned sh[];
@@ -1535,7 +1474,7 @@ __global__ void __launch_bounds__(WIDE ? 768 : 256, WIDE ? 1 : 3)
     const long long col = g * blockDim.x + threadIdx.x;
     const bool active = col < ncols;
     const int y = active ? (int)(col / cpr) : 0, x0 = active ? 4 * (int)(col - (long long)y * cpr) : 0;
-    ColumnOf<T> cl(v, X, Y, Z, x0, y);  // inactive threads walk column 0 and count nothing
+    ColumnAhead<T> cl(v, X, Y, Z, x0, y);  // inactive threads walk column 0 and count nothing
     for (int z = 0; z < Z; ++z) {
       if (active) {
         typename SumT<T, NARROW>::U S[4];
@@ -1628,10 +1567,11 @@ cudaError_t launch_hist2d(const void* vol, int dtype, const long long dims[3], d
       e = cudaMallocAsync(reinterpret_cast<void**>(&cols), (size_t)ncols * sizeof(ColMax), s);
       if (e != cudaSuccess) return e;
       // shared counters for the gradient rows k < kshared: 32 bits per bin in
-      // about 200 KB for one 768-thread block per SM (the same 24 warps per SM
-      // as three 256-thread blocks at the kernel's 80 registers); a block adds
-      // at most 4 * 768 voxels per z-step, so counters flush before 2^32
-      constexpr int wide_threads = 768;
+      // about 200 KB for one block per SM (768 threads at 80 registers for
+      // 8-bit data, 640 at 96 for 16-bit data, whose packed column walker
+      // needs the registers); a block adds at most 4 * wide_threads voxels
+      // per z-step, so counters flush before 2^32
+      const int wide_threads = dtype == DT_U16 ? 640 : 768;
       const int kshared = (int)std::min<long long>(256, ((200 * 1024) / (4 * nx)) & ~1LL);
       const bool smem = kshared >= 2;
       const size_t shbytes = smem ? (size_t)nx * kshared * 4 : 0;
